@@ -1,0 +1,267 @@
+/*
+ * topo_gb300.h -- C ABI of the GB300-native topology-optimisation hot path.
+ *
+ * One handle owns one design problem on one GPU: the voxel grid and its
+ * multigrid hierarchy, boundary conditions, the B-spline design field, the
+ * solver state and every device buffer.  All calls return a TOPO_* status and
+ * never exit the process; topo_last_error() gives the message.  Arrays cross
+ * the boundary as plain host pointers with explicit element counts.
+ *
+ * Layout shared by every array (dense grid, lexicographic, x fastest):
+ *   element e = ex + nx*(ey + ny*ez);  vertex v = x + (nx+1)*(y + (ny+1)*z)
+ *   vertex vectors are SoA [3][nv]; element matrices [ne][24*24] with local node
+ *   a = ax + 2ay + 4az and DOF 3a+c; coarse stencils [27][9][nv] with neighbour
+ *   d = (dx+1) + 3(dy+1) + 9(dz+1) and a row-major 3x3 block.
+ * topo_gs_maps() converts to the reference's GS-coloured ordering.
+ *
+ * Each entry point names the reference interface it replaces
+ * (NanXYZH/TopOptSpline3D, file:line).
+ */
+#ifndef TOPO_GB300_H
+#define TOPO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum topo_status {
+  TOPO_OK = 0,
+  TOPO_E_CUDA = 1,          /* a CUDA runtime call failed */
+  TOPO_E_BAD_INPUT = 2,     /* invalid argument (sizes, pointers, ranges) */
+  TOPO_E_STATE = 3,         /* call order violated (e.g. solve before set_bc) */
+  TOPO_E_NOT_CONVERGED = 4, /* solver hit its iteration cap above tolerance */
+  TOPO_E_SINGULAR = 5,      /* coarsest-level factorisation met a non-positive pivot */
+  TOPO_E_NOMEM = 6,         /* device allocation failed */
+  TOPO_E_NONFINITE = 7      /* NaN/Inf detected in a result */
+};
+
+/* Array ids for topo_put_array / topo_get_array / topo_device_ptr. */
+enum topo_array {
+  TOPO_RHO = 0,      /* double[ne]   element density */
+  TOPO_RHOP = 1,     /* double[ne]   rho^p */
+  TOPO_COEFF = 2,    /* double[nc]   spline coefficients, x fastest */
+  TOPO_SENS = 3,     /* double[ne]   d compliance / d rho (filtered in place) */
+  TOPO_CSENS = 4,    /* double[nc]   d compliance / d coefficient */
+  TOPO_U = 5,        /* double[3*nv] displacement (per level) */
+  TOPO_F = 6,        /* double[3*nv] force / right-hand side (per level) */
+  TOPO_R = 7,        /* double[3*nv] residual (per level) */
+  TOPO_STENCIL = 8,  /* double[243*nv] coarse-level stencil (level >= 1) */
+  TOPO_KELEM = 9,    /* double[576*ne] coarse element matrices (level >= 1) */
+  TOPO_VMASK = 10,   /* uint8[nv]    bits 0-2 DOF free, bit 3 vertex active */
+  TOPO_EACTIVE = 11, /* uint8[ne]    element active mask (per level) */
+  TOPO_KE = 12,      /* double[576]  element template */
+  TOPO_WORK = 13     /* double[3*nv] scratch vector (level 0): input of topo_apply_fine */
+};
+
+typedef struct topo_config {
+  int nx, ny, nz;               /* element grid (domain bounding box) */
+  double h;                     /* element edge length */
+  double youngs_modulus;        /* E   (reference flag youngs_modulus, default 1e6) */
+  double poisson_ratio;         /* nu  (reference flag poisson_ratio, default 0.4) */
+  double power_penalty;         /* SIMP p (default 3) */
+  double min_density;           /* rho_min (default 1e-3) */
+  int max_coarse_elements;      /* coarsen while active elements exceed this (reference: 400) */
+  int device;                   /* CUDA device ordinal */
+} topo_config;
+
+typedef struct topo_handle topo_handle;
+
+/* Solver modes for topo_solve. */
+enum topo_solve_mode {
+  TOPO_SOLVE_VCYCLE = 0,  /* reference: repeated V-cycles (utils/test_utils.cpp:937-941) */
+  TOPO_SOLVE_PCG64 = 1,   /* FP64 MG-PCG, symmetric V-cycle preconditioner */
+  TOPO_SOLVE_MIXED = 2    /* FP64 flexible CG preconditioned by FP32 multigrid */
+};
+
+enum topo_smoother {
+  TOPO_SMOOTH_GS = 0,        /* 8-colour point-block Gauss-Seidel (reference) */
+  TOPO_SMOOTH_CHEBYSHEV = 1  /* point-block-Jacobi Chebyshev */
+};
+
+typedef struct topo_solve_opts {
+  int mode;           /* topo_solve_mode */
+  int smoother;       /* topo_smoother */
+  int pre, post;      /* smoothing steps per level */
+  double rtol;        /* relative residual target ||f - K u|| / ||f|| (FP64) */
+  int max_iter;       /* V-cycles (mode 0) or outer CG iterations (modes 1, 2) */
+  double inner_rtol;  /* mode 2: relative reduction of each inner FP32 solve */
+  int cheb_degree;    /* Chebyshev polynomial degree per smoothing step */
+  double cheb_lo, cheb_hi; /* Chebyshev interval [lo*lmax, hi*lmax] */
+  int inner_max;      /* mode 2: FP32 iterations per preconditioner application (1 = one V-cycle) */
+} topo_solve_opts;
+
+typedef struct topo_solve_stats {
+  int iterations;     /* V-cycles (mode 0) or outer CG iterations = FP64 fine matvecs (modes 1, 2) */
+  int vcycles;        /* V-cycles applied (FP32 ones in mode 2) */
+  double relres;      /* final FP64 relative residual */
+  double ms;          /* device time of the solve */
+} topo_solve_stats;
+
+typedef struct topo_oc_opts {
+  double vgoal;       /* target volume ratio */
+  double damp;        /* OC exponent (reference damp_ratio 0.5) */
+  double step;        /* move limit (reference design_step 0.03) */
+  double cmin, cmax;  /* coefficient bounds (reference min_coeff 0, max_coeff 1) */
+  int apply_twice;    /* reproduce the reference's double application of the final step */
+  int reference_volume; /* volume denominator with the reference's GS padding */
+} topo_oc_opts;
+
+typedef struct topo_oc_stats {
+  int trials;
+  double lambda;
+  double volume;
+} topo_oc_stats;
+
+/* --- lifetime ------------------------------------------------------------ */
+/* Replaces HierarchyGrid::genFromMesh(const std::vector<unsigned>&, int[3]) (grid/Grid.cpp:977)
+ * plus setParameters (optimization/optimization.cpp:35-65) and buildGrids (15-22).
+ * eactive: uint8[nx*ny*nz] or NULL (all active). */
+int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** out);
+/* Replaces HierarchyGrid::~HierarchyGrid (grid/Grid.h:1027-1033) and gpu_manager_t teardown. */
+void topo_destroy(topo_handle* h);
+/* Replaces the printf-only cuda_error_check (culib/cudaCommon.cuh:6-11). */
+const char* topo_last_error(const topo_handle* h);
+/* Replaces HierarchyGrid::n_grid (grid/Grid.h:1017) and Grid::_layer / elementLength. */
+int topo_num_levels(const topo_handle* h, int* nlevels);
+int topo_level_dims(const topo_handle* h, int level, int* dims3, int* factor);
+/* Waits for all work queued on the handle's stream. */
+int topo_sync(topo_handle* h);
+
+/* --- set-up -------------------------------------------------------------- */
+/* Replaces setBoundaryCondition + setForceSupport(getPreloadForce(), F)
+ * (optimization/optimization.cpp:1023-1028, optimization/projection.cu:344-368).
+ * fixed: uint8[nv], bit c set = DOF c fixed; loads: double[3*nv]. */
+int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads);
+/* Replaces HierarchyGrid::set_spline_partition (grid/Grid.cu:3134-3203) and
+ * Grid::set_spline_knot_series / set_spline_knot_infoSymbol (grid/Grid.cpp:3253-3377,
+ * grid/Grid.cu:3205-3216).  bmin/bmax: spline box before the 2*delta/(p+1) enlargement. */
+int topo_set_spline(topo_handle* h, int order, const int* partition3, const double* bmin3,
+                    const double* bmax3);
+int topo_num_coeffs(const topo_handle* h, int* ncoeff);
+int topo_get_knots(const topo_handle* h, int axis, double* out, size_t count);
+
+/* --- arrays -------------------------------------------------------------- */
+/* Replace Grid::getRho/getCoeff/getSens/getCSens/getForce/getDisplacement
+ * (grid/Grid.h:420-450), init_coefflist/init_rholist, and the *2matlab dumps. */
+int topo_array_size(const topo_handle* h, int which, int level, size_t* count);
+int topo_put_array(topo_handle* h, int which, int level, const void* src, size_t count);
+int topo_get_array(topo_handle* h, int which, int level, void* dst, size_t count);
+/* Borrowed device pointer, valid until topo_destroy. */
+int topo_device_ptr(topo_handle* h, int which, int level, void** dptr);
+
+/* --- hot path ------------------------------------------------------------ */
+/* Replaces Grid::coeff2density (grid/Grid.cu:3361-3456): rho = clamp(spline(coeff)). */
+int topo_coeff_to_density(topo_handle* h);
+/* Which coarse operators topo_update_operators builds: bit 0 FP64 (V-cycle and FP64
+ * PCG modes), bit 1 FP32 (mixed mode).  Default 3.  The reference builds FP64 only
+ * (grid/Grid.cu:839-1265). */
+int topo_set_operator_precision(topo_handle* h, int mask);
+/* Replaces HierarchyGrid::update_stencil (grid/Grid.cpp:4167-4178): rho^p, Galerkin
+ * coarse operators (grid/Grid.cu:839-1265) and the coarsest factorisation
+ * (grid/Grid.cpp:3614-3669). */
+int topo_update_operators(topo_handle* h);
+/* Replaces Grid::applyK (grid/Grid.cu:4278-4356): TOPO_R(level 0) <- K(rho) TOPO_WORK,
+ * fixed rows zero.  precision: 0 = FP64, 1 = FP32 kernel. */
+int topo_apply_fine(topo_handle* h, int precision);
+/* Replaces Grid::update_residual (grid/Grid.cu:2420-2454). */
+int topo_residual(topo_handle* h, int level);
+/* Replaces Grid::gs_relax (grid/Grid.cu:1844-1887); reverse = adjoint sweep order. */
+int topo_smooth(topo_handle* h, int level, int sweeps, int reverse);
+/* Replace Grid::restrict_residual / prolongate_correction (grid/Grid.cu:2572-2691). */
+int topo_restrict(topo_handle* h, int coarse_level);
+int topo_prolong(topo_handle* h, int fine_level);
+/* Replaces Grid::solve_fem_host (grid/Grid.cpp:4040-4102), on the GPU. */
+int topo_coarsest_solve(topo_handle* h);
+/* Replaces HierarchyGrid::v_cycle (grid/Grid.cpp:2399-2444); returns ||R||/||F||. */
+int topo_vcycle(topo_handle* h, int pre, int post, double* relres);
+/* Replaces the driver's solve loop (utils/test_utils.cpp:937-941); warm-starts from U. */
+int topo_solve(topo_handle* h, const topo_solve_opts* opts, topo_solve_stats* stats);
+/* Replaces Grid::compliance (grid/Grid.cpp:4035-4038): F . U. */
+int topo_compliance(topo_handle* h, double* c);
+/* Replaces Grid::volumeRatio (grid/Grid.cu:5462-5470). */
+int topo_volume(topo_handle* h, int reference_denominator, double* v);
+/* Replaces computeSensitivity_kernel (optimization/optimization.cu:96-159). */
+int topo_sensitivity(topo_handle* h);
+/* Replaces Grid::filterSensitivity (grid/Grid.cu:4218-4246). */
+int topo_filter(topo_handle* h, double radius);
+/* Replaces Grid::ddensity2dcoeff_update (grid/Grid.cu:3643-3748). */
+int topo_spline_adjoint(topo_handle* h);
+/* Replaces updateCoeff (optimization/optimization.cu:589-695). */
+int topo_oc_update(topo_handle* h, const topo_oc_opts* opts, topo_oc_stats* stats);
+
+/* --- reference ordering -------------------------------------------------- */
+/* Reproduces Grid::enumerate_gs_subset (grid/Grid.cpp:4104-4165) with the colour of
+ * grid/Grid.cu:1286-1328: vidmap[active vertex rank] = GS id, eidmap likewise,
+ * gs_num[8] padded colour sizes.  Arrays sized by the active counts. */
+int topo_gs_maps(topo_handle* h, int level, int* vidmap, size_t nvid, int* eidmap, size_t neid,
+                 int* gs_num8, int* n_gsvertices, int* n_gselements);
+
+/* --- measurement --------------------------------------------------------- */
+/* When enabled, CUDA events bracket every launch of a kernel family on the
+ * handle's stream; topo_profile_read returns launches and summed milliseconds. */
+int topo_profile_enable(topo_handle* h, int enable);
+int topo_profile_read(topo_handle* h, int family, int* launches, double* ms);
+
+enum topo_kernel_family {
+  TOPO_K_FINE_APPLY64 = 0,
+  TOPO_K_FINE_APPLY32 = 1,
+  TOPO_K_FINE_SMOOTH64 = 2,
+  TOPO_K_FINE_SMOOTH32 = 3,
+  TOPO_K_COUNT = 8
+};
+
+/* Number of kernel launches the library has issued in this process. */
+int topo_launch_count(const topo_handle* h, long long* launches);
+
+/* Pinned host staging memory for topo_put_array / topo_get_array. */
+int topo_host_alloc(size_t bytes, void** ptr);
+int topo_host_free(void* ptr);
+/* CUDA events on the handle's stream: topo_timer_stop returns the device time
+ * since the matching topo_timer_start, after waiting for it. */
+int topo_timer_start(topo_handle* h);
+int topo_timer_stop(topo_handle* h, double* ms);
+
+/* --- one design iteration ------------------------------------------------- */
+typedef struct topo_iter_opts {
+  topo_solve_opts solve;
+  topo_oc_opts oc;
+  double filter_radius;       /* reference filter_radius (default 2) */
+} topo_iter_opts;
+
+typedef struct topo_iter_stats {
+  double compliance;          /* F . U after the solve */
+  double volume;              /* volume ratio after the OC update */
+  topo_solve_stats solve;
+  int oc_trials;
+  double ms;                  /* device time of the whole iteration */
+} topo_iter_stats;
+
+/* Replaces one pass of the loop body of TestSuit::testOrdinarySplineTopopt
+ * (utils/test_utils.cpp:928-958): update_stencil, solve (warm start), compliance,
+ * computeSensitivity (sensitivity, filter, spline adjoint) and updateCoeff. */
+int topo_design_iteration(topo_handle* h, const topo_iter_opts* opts, topo_iter_stats* stats);
+
+/* --- host-only set-up helpers (no GPU needed) ----------------------------- */
+/* Element template (element/templateMatrix.cpp:31-99), row-major 24x24. */
+int topo_element_template(double E, double nu, double h, double* Ke576);
+/* Level plan (grid/Grid.cpp:747-769, 909-911): writes up to max_levels element dims
+ * (3 ints each) and coarsening factors. */
+int topo_plan_levels(int nx, int ny, int nz, const uint8_t* eactive, int max_coarse_elements,
+                     int max_levels, int* nlevels, int* dims, int* factors);
+/* Knot vector (2*order+partition) and basis tables at element centres along one axis
+ * (grid/Grid.cpp:3253-3337, grid/Grid.cu:384-466): i0[nelem] first basis index or -1,
+ * N[nelem*order] basis values. */
+int topo_spline_axis(int order, int partition, double bmin, double bmax, int nelem, double h,
+                     double* knots, int* i0, double* N);
+/* Reference GS ordering of one level of the plan (see topo_gs_maps). */
+int topo_plan_gs_maps(int nx, int ny, int nz, const uint8_t* eactive, int max_coarse_elements,
+                      int level, int* vidmap, size_t nvid, int* eidmap, size_t neid, int* gs_num8,
+                      int* n_gsvertices, int* n_gselements);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TOPO_GB300_H */

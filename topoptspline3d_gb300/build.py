@@ -1,0 +1,82 @@
+"""Build libtopo_gb300.so in-tree: nvcc for sm_103a, one process per source.
+
+Usage: python -m topoptspline3d_gb300.build [--force]
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_lib")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(OUT_DIR, "libtopo_gb300.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+CU_SOURCES = ["capi.cu", "k_fine.cu", "k_coarse.cu", "k_vec.cu", "k_design.cu"]
+CPP_SOURCES = ["host_setup.cpp"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libtopo_gb300")
+
+
+def _sources():
+    return [os.path.join(CSRC, s) for s in CU_SOURCES + CPP_SOURCES]
+
+
+def _headers():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    hs.append(os.path.join(HERE, "..", "include", "topo_gb300.h"))
+    return hs
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    return any(os.path.getmtime(p) > t for p in _sources() + _headers() + [__file__])
+
+
+def _compile(src: str) -> str:
+    nvcc = _nvcc()
+    obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include")]
+    if src.endswith(".cu"):
+        cmd = [nvcc, ARCH, "-lineinfo", "--expt-relaxed-constexpr", "-c", src, "-o", obj] + common
+    else:
+        cmd = [nvcc, "-x", "c++", "-c", src, "-o", obj] + common
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    if not force and not _stale():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    os.makedirs(OUT_DIR, exist_ok=True)
+    srcs = _sources()
+    with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(_compile, srcs))
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    cmd = [_nvcc(), ARCH, "-shared", "-o", tmp] + objs + ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    if verbose:
+        print("built", LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)

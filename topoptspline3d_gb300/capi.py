@@ -1,0 +1,485 @@
+"""ctypes binding of the C ABI declared in include/topo_gb300.h.
+
+``Problem`` wraps one ``topo_handle``.  The library is loaded from the in-tree
+build (``_lib/libtopo_gb300.so``); there is no fallback: if the CUDA library
+cannot be built or loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+TOPO_OK, TOPO_E_CUDA, TOPO_E_BAD_INPUT, TOPO_E_STATE, TOPO_E_NOT_CONVERGED, TOPO_E_SINGULAR, \
+    TOPO_E_NOMEM, TOPO_E_NONFINITE = range(8)
+STATUS_NAMES = {0: "TOPO_OK", 1: "TOPO_E_CUDA", 2: "TOPO_E_BAD_INPUT", 3: "TOPO_E_STATE",
+                4: "TOPO_E_NOT_CONVERGED", 5: "TOPO_E_SINGULAR", 6: "TOPO_E_NOMEM", 7: "TOPO_E_NONFINITE"}
+
+ARRAYS = {"rho": 0, "rhop": 1, "coeff": 2, "sens": 3, "csens": 4, "u": 5, "f": 6, "r": 7,
+          "stencil": 8, "kelem": 9, "vmask": 10, "eactive": 11, "ke": 12, "work": 13}
+BYTE_ARRAYS = {"vmask", "eactive"}
+
+SOLVE_VCYCLE, SOLVE_PCG64, SOLVE_MIXED = 0, 1, 2
+SMOOTH_GS, SMOOTH_CHEBYSHEV = 0, 1
+K_FINE_APPLY64, K_FINE_APPLY32, K_FINE_SMOOTH64, K_FINE_SMOOTH32 = 0, 1, 2, 3
+
+# Every symbol the header declares (checked by the CPU test suite).
+EXPORTED = [
+    "topo_create", "topo_destroy", "topo_last_error", "topo_num_levels", "topo_level_dims", "topo_sync",
+    "topo_set_bc", "topo_set_spline", "topo_num_coeffs", "topo_get_knots", "topo_array_size",
+    "topo_put_array", "topo_get_array", "topo_device_ptr", "topo_coeff_to_density",
+    "topo_update_operators", "topo_apply_fine", "topo_residual", "topo_smooth", "topo_restrict",
+    "topo_prolong", "topo_coarsest_solve", "topo_vcycle", "topo_solve", "topo_compliance",
+    "topo_volume", "topo_sensitivity", "topo_filter", "topo_spline_adjoint", "topo_oc_update",
+    "topo_gs_maps", "topo_profile_enable", "topo_profile_read", "topo_launch_count",
+    "topo_set_operator_precision", "topo_host_alloc", "topo_host_free", "topo_design_iteration",
+    "topo_element_template", "topo_plan_levels", "topo_spline_axis", "topo_plan_gs_maps",
+    "topo_timer_start", "topo_timer_stop",
+]
+
+
+class TopoConfig(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("h", C.c_double),
+                ("youngs_modulus", C.c_double), ("poisson_ratio", C.c_double),
+                ("power_penalty", C.c_double), ("min_density", C.c_double),
+                ("max_coarse_elements", C.c_int), ("device", C.c_int)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("mode", C.c_int), ("smoother", C.c_int), ("pre", C.c_int), ("post", C.c_int),
+                ("rtol", C.c_double), ("max_iter", C.c_int), ("inner_rtol", C.c_double),
+                ("cheb_degree", C.c_int), ("cheb_lo", C.c_double), ("cheb_hi", C.c_double),
+                ("inner_max", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("vcycles", C.c_int), ("relres", C.c_double), ("ms", C.c_double)]
+
+
+class OcOpts(C.Structure):
+    _fields_ = [("vgoal", C.c_double), ("damp", C.c_double), ("step", C.c_double), ("cmin", C.c_double),
+                ("cmax", C.c_double), ("apply_twice", C.c_int), ("reference_volume", C.c_int)]
+
+
+class OcStats(C.Structure):
+    _fields_ = [("trials", C.c_int), ("lambda_", C.c_double), ("volume", C.c_double)]
+
+
+class IterOpts(C.Structure):
+    _fields_ = [("solve", SolveOpts), ("oc", OcOpts), ("filter_radius", C.c_double)]
+
+
+class IterStats(C.Structure):
+    _fields_ = [("compliance", C.c_double), ("volume", C.c_double), ("solve", SolveStats),
+                ("oc_trials", C.c_int), ("ms", C.c_double)]
+
+
+class TopoError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build: bool = True):
+    """Load (building first if needed) the CUDA library; raises if unavailable."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB_PATH
+    if not os.path.exists(path):
+        raise OSError(f"libtopo_gb300 not built at {path}")
+    lib = C.CDLL(path)
+    vp, i, d, ip, dp, sz = C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_size_t
+    sigs = {
+        "topo_create": (i, [C.POINTER(TopoConfig), vp, C.POINTER(vp)]),
+        "topo_destroy": (None, [vp]),
+        "topo_last_error": (C.c_char_p, [vp]),
+        "topo_num_levels": (i, [vp, ip]),
+        "topo_level_dims": (i, [vp, i, ip, ip]),
+        "topo_sync": (i, [vp]),
+        "topo_set_bc": (i, [vp, vp, vp]),
+        "topo_set_spline": (i, [vp, i, ip, dp, dp]),
+        "topo_num_coeffs": (i, [vp, ip]),
+        "topo_get_knots": (i, [vp, i, dp, sz]),
+        "topo_array_size": (i, [vp, i, i, C.POINTER(sz)]),
+        "topo_put_array": (i, [vp, i, i, vp, sz]),
+        "topo_get_array": (i, [vp, i, i, vp, sz]),
+        "topo_device_ptr": (i, [vp, i, i, C.POINTER(vp)]),
+        "topo_coeff_to_density": (i, [vp]),
+        "topo_set_operator_precision": (i, [vp, i]),
+        "topo_update_operators": (i, [vp]),
+        "topo_apply_fine": (i, [vp, i]),
+        "topo_residual": (i, [vp, i]),
+        "topo_smooth": (i, [vp, i, i, i]),
+        "topo_restrict": (i, [vp, i]),
+        "topo_prolong": (i, [vp, i]),
+        "topo_coarsest_solve": (i, [vp]),
+        "topo_vcycle": (i, [vp, i, i, dp]),
+        "topo_solve": (i, [vp, C.POINTER(SolveOpts), C.POINTER(SolveStats)]),
+        "topo_compliance": (i, [vp, dp]),
+        "topo_volume": (i, [vp, i, dp]),
+        "topo_sensitivity": (i, [vp]),
+        "topo_filter": (i, [vp, d]),
+        "topo_spline_adjoint": (i, [vp]),
+        "topo_oc_update": (i, [vp, C.POINTER(OcOpts), C.POINTER(OcStats)]),
+        "topo_gs_maps": (i, [vp, i, vp, sz, vp, sz, vp, ip, ip]),
+        "topo_profile_enable": (i, [vp, i]),
+        "topo_profile_read": (i, [vp, i, ip, dp]),
+        "topo_launch_count": (i, [vp, C.POINTER(C.c_longlong)]),
+        "topo_host_alloc": (i, [sz, C.POINTER(vp)]),
+        "topo_host_free": (i, [vp]),
+        "topo_design_iteration": (i, [vp, C.POINTER(IterOpts), C.POINTER(IterStats)]),
+        "topo_element_template": (i, [d, d, d, dp]),
+        "topo_plan_levels": (i, [i, i, i, vp, i, i, ip, ip, ip]),
+        "topo_spline_axis": (i, [i, i, d, d, i, d, dp, ip, dp]),
+        "topo_plan_gs_maps": (i, [i, i, i, vp, i, i, vp, sz, vp, sz, vp, ip, ip]),
+        "topo_timer_start": (i, [vp]),
+        "topo_timer_stop": (i, [vp, dp]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ck_free(rc, what):
+    if rc != TOPO_OK:
+        raise TopoError(rc, what)
+
+
+def element_template(E, nu, h) -> np.ndarray:
+    """Host-only: the library's 24x24 element template."""
+    lib = load()
+    out = np.zeros(576)
+    _ck_free(lib.topo_element_template(E, nu, h, out.ctypes.data_as(C.POINTER(C.c_double))), "element_template")
+    return out.reshape(24, 24)
+
+
+def plan_levels(nx, ny, nz, eactive=None, max_coarse=400):
+    """Host-only: element dims and coarsening factors of the multigrid levels."""
+    lib = load()
+    dims = np.zeros(3 * 16, dtype=np.int32)
+    fac = np.zeros(16, dtype=np.int32)
+    n = C.c_int()
+    m = None
+    if eactive is not None:
+        ea = np.ascontiguousarray(eactive, dtype=np.uint8).ravel()
+        m = ea.ctypes.data
+    _ck_free(lib.topo_plan_levels(nx, ny, nz, m, max_coarse, 16, C.byref(n), dims.ctypes.data_as(C.POINTER(C.c_int)),
+                                  fac.ctypes.data_as(C.POINTER(C.c_int))), "plan_levels")
+    return [tuple(dims[3 * l:3 * l + 3]) for l in range(n.value)], list(fac[:n.value])
+
+
+def spline_axis(order, partition, bmin, bmax, nelem, h=1.0):
+    """Host-only: knots, first basis index per element slice and basis values."""
+    lib = load()
+    knots = np.zeros(2 * order + partition)
+    i0 = np.zeros(nelem, dtype=np.int32)
+    N = np.zeros(nelem * order)
+    _ck_free(lib.topo_spline_axis(order, partition, bmin, bmax, nelem, h, knots.ctypes.data_as(C.POINTER(C.c_double)),
+                                  i0.ctypes.data_as(C.POINTER(C.c_int)), N.ctypes.data_as(C.POINTER(C.c_double))),
+             "spline_axis")
+    return knots, i0, N.reshape(nelem, order)
+
+
+def plan_gs_maps(nx, ny, nz, level=0, eactive=None, max_coarse=400):
+    """Host-only: the reference's GS-coloured ordering of one level."""
+    lib = load()
+    m, ea = None, None
+    if eactive is not None:
+        ea = np.ascontiguousarray(eactive, dtype=np.uint8).ravel()
+        m = ea.ctypes.data
+    gsn = np.zeros(8, dtype=np.int32)
+    ngv, nge = C.c_int(), C.c_int()
+    _ck_free(lib.topo_plan_gs_maps(nx, ny, nz, m, max_coarse, level, None, 0, None, 0, gsn.ctypes.data,
+                                   C.byref(ngv), C.byref(nge)), "plan_gs_maps")
+    # active counts: padded colour sizes bound them; ask with exact sizes by counting actives
+    dims, facs = plan_levels(nx, ny, nz, eactive, max_coarse)
+    ex, ey, ez = (int(v) for v in dims[level])
+    eact = _plan_eactive(nx, ny, nz, ea, dims, facs, level)
+    vact = np.zeros((ez + 1, ey + 1, ex + 1), bool)
+    e3 = eact.reshape(ez, ey, ex)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                vact[dz:dz + ez, dy:dy + ey, dx:dx + ex] |= e3
+    nva, nea = int(vact.sum()), int(eact.sum())
+    vid = np.zeros(max(nva, 1), dtype=np.int32)
+    eid = np.zeros(max(nea, 1), dtype=np.int32)
+    _ck_free(lib.topo_plan_gs_maps(nx, ny, nz, m, max_coarse, level, vid.ctypes.data, nva, eid.ctypes.data, nea,
+                                   gsn.ctypes.data, C.byref(ngv), C.byref(nge)), "plan_gs_maps")
+    return vid[:nva], eid[:nea], gsn, ngv.value, nge.value
+
+
+def _plan_eactive(nx, ny, nz, ea, dims, facs, level):
+    """Active-element mask of a planned level (child-OR of the fine mask)."""
+    cur = np.ones((nz, ny, nx), bool) if ea is None else ea.reshape(nz, ny, nx).astype(bool)
+    for l in range(1, level + 1):
+        cx, cy, cz = (int(v) for v in dims[l])
+        f = int(facs[l])
+        pad = np.zeros((cz * f, cy * f, cx * f), bool)
+        pad[:cur.shape[0], :cur.shape[1], :cur.shape[2]] = cur
+        cur = pad.reshape(cz, f, cy, f, cx, f).any(axis=(1, 3, 5))
+    return cur.ravel()
+
+
+class PinnedBuffer:
+    """Page-locked host buffer from topo_host_alloc, viewed as a numpy array."""
+
+    def __init__(self, n, dtype=np.float64):
+        self.lib = load()
+        self.nbytes = int(n) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        _ck_free(self.lib.topo_host_alloc(self.nbytes, C.byref(p)), "topo_host_alloc")
+        self.ptr = p.value
+        self.array = np.frombuffer((C.c_char * self.nbytes).from_address(self.ptr), dtype=dtype)
+
+    def close(self):
+        if self.ptr:
+            self.array = None
+            self.lib.topo_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Problem:
+    """One topology-optimisation problem on one GPU (wraps ``topo_handle``)."""
+
+    def __init__(self, nx, ny, nz, h=1.0, E=1e6, nu=0.4, penal=3.0, rho_min=1e-3, eactive=None,
+                 max_coarse_elements=400, device=0):
+        self.lib = load()
+        self.dims = (nx, ny, nz)
+        self.nv = (nx + 1) * (ny + 1) * (nz + 1)
+        self.ne = nx * ny * nz
+        cfg = TopoConfig(nx, ny, nz, h, E, nu, penal, rho_min, max_coarse_elements, device)
+        mask = None
+        if eactive is not None:
+            self._mask = np.ascontiguousarray(eactive, dtype=np.uint8).ravel()
+            assert self._mask.size == self.ne
+            mask = self._mask.ctypes.data
+        hp = C.c_void_p()
+        rc = self.lib.topo_create(C.byref(cfg), mask, C.byref(hp))
+        if rc != TOPO_OK:
+            raise TopoError(rc, "topo_create failed")
+        self.h = hp
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.topo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != TOPO_OK:
+            raise TopoError(rc, self.lib.topo_last_error(self.h).decode())
+        return rc
+
+    # --- hierarchy
+    def num_levels(self) -> int:
+        n = C.c_int()
+        self._ck(self.lib.topo_num_levels(self.h, C.byref(n)))
+        return n.value
+
+    def level_dims(self, level):
+        d = (C.c_int * 3)()
+        f = C.c_int()
+        self._ck(self.lib.topo_level_dims(self.h, level, d, C.byref(f)))
+        return tuple(d), f.value
+
+    # --- set-up
+    def set_bc(self, fixed, loads):
+        fixed = np.ascontiguousarray(fixed, dtype=np.uint8).ravel()
+        loads = np.ascontiguousarray(loads, dtype=np.float64).ravel()
+        assert fixed.size == self.nv and loads.size == 3 * self.nv
+        self._ck(self.lib.topo_set_bc(self.h, fixed.ctypes.data, loads.ctypes.data))
+
+    def set_spline(self, order, partition, bmin, bmax):
+        p = (C.c_int * 3)(*partition)
+        a = (C.c_double * 3)(*bmin)
+        b = (C.c_double * 3)(*bmax)
+        self._ck(self.lib.topo_set_spline(self.h, order, p, a, b))
+
+    def num_coeffs(self) -> int:
+        n = C.c_int()
+        self._ck(self.lib.topo_num_coeffs(self.h, C.byref(n)))
+        return n.value
+
+    def knots(self, axis, count):
+        out = np.zeros(count)
+        self._ck(self.lib.topo_get_knots(self.h, axis, out.ctypes.data_as(C.POINTER(C.c_double)), count))
+        return out
+
+    # --- arrays
+    def size(self, name, level=0) -> int:
+        n = C.c_size_t()
+        self._ck(self.lib.topo_array_size(self.h, ARRAYS[name], level, C.byref(n)))
+        return n.value
+
+    def get(self, name, level=0) -> np.ndarray:
+        n = self.size(name, level)
+        out = np.zeros(n, dtype=np.uint8 if name in BYTE_ARRAYS else np.float64)
+        self._ck(self.lib.topo_get_array(self.h, ARRAYS[name], level, out.ctypes.data, n))
+        return out
+
+    def put(self, name, arr, level=0):
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        self._ck(self.lib.topo_put_array(self.h, ARRAYS[name], level, a.ctypes.data, a.size))
+
+    def device_ptr(self, name, level=0) -> int:
+        p = C.c_void_p()
+        self._ck(self.lib.topo_device_ptr(self.h, ARRAYS[name], level, C.byref(p)))
+        return p.value
+
+    # --- hot path
+    def coeff_to_density(self):
+        self._ck(self.lib.topo_coeff_to_density(self.h))
+
+    def set_operator_precision(self, mask):
+        self._ck(self.lib.topo_set_operator_precision(self.h, mask))
+
+    def update_operators(self):
+        self._ck(self.lib.topo_update_operators(self.h))
+
+    def apply_fine(self, u, precision=0) -> np.ndarray:
+        self.put("work", u)
+        self._ck(self.lib.topo_apply_fine(self.h, precision))
+        return self.get("r")
+
+    def residual(self, level=0):
+        self._ck(self.lib.topo_residual(self.h, level))
+
+    def smooth(self, level, sweeps, reverse=False):
+        self._ck(self.lib.topo_smooth(self.h, level, sweeps, int(reverse)))
+
+    def restrict(self, coarse_level):
+        self._ck(self.lib.topo_restrict(self.h, coarse_level))
+
+    def prolong(self, fine_level):
+        self._ck(self.lib.topo_prolong(self.h, fine_level))
+
+    def coarsest_solve(self):
+        self._ck(self.lib.topo_coarsest_solve(self.h))
+
+    def vcycle(self, pre=5, post=5) -> float:
+        rr = C.c_double()
+        self._ck(self.lib.topo_vcycle(self.h, pre, post, C.byref(rr)))
+        return rr.value
+
+    def solve(self, mode=SOLVE_PCG64, smoother=SMOOTH_GS, pre=2, post=2, rtol=1e-6, max_iter=200,
+              inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1, check=True):
+        o = SolveOpts(mode, smoother, pre, post, rtol, max_iter, inner_rtol, cheb_degree, cheb_lo, cheb_hi,
+                      inner_max)
+        s = SolveStats()
+        rc = self.lib.topo_solve(self.h, C.byref(o), C.byref(s))
+        if check:
+            self._ck(rc)
+        return {"iterations": s.iterations, "vcycles": s.vcycles, "relres": s.relres, "ms": s.ms, "rc": rc}
+
+    def compliance(self) -> float:
+        c = C.c_double()
+        self._ck(self.lib.topo_compliance(self.h, C.byref(c)))
+        return c.value
+
+    def volume(self, reference_denominator=True) -> float:
+        v = C.c_double()
+        self._ck(self.lib.topo_volume(self.h, int(reference_denominator), C.byref(v)))
+        return v.value
+
+    def sensitivity(self):
+        self._ck(self.lib.topo_sensitivity(self.h))
+
+    def filter(self, radius):
+        self._ck(self.lib.topo_filter(self.h, radius))
+
+    def spline_adjoint(self):
+        self._ck(self.lib.topo_spline_adjoint(self.h))
+
+    def oc_update(self, vgoal, damp=0.5, step=0.03, cmin=0.0, cmax=1.0, apply_twice=False,
+                  reference_denominator=True):
+        o = OcOpts(vgoal, damp, step, cmin, cmax, int(apply_twice), int(reference_denominator))
+        s = OcStats()
+        self._ck(self.lib.topo_oc_update(self.h, C.byref(o), C.byref(s)))
+        return s.trials, s.lambda_
+
+    def gs_maps(self, level=0):
+        vm = self.get("vmask", level)
+        nva = int(((vm & 8) != 0).sum())
+        nea = int((self.get("eactive", level) != 0).sum())
+        vid = np.zeros(max(nva, 1), dtype=np.int32)
+        eid = np.zeros(max(nea, 1), dtype=np.int32)
+        gsn = np.zeros(8, dtype=np.int32)
+        ngv, nge = C.c_int(), C.c_int()
+        self._ck(self.lib.topo_gs_maps(self.h, level, vid.ctypes.data, nva, eid.ctypes.data, nea,
+                                       gsn.ctypes.data, C.byref(ngv), C.byref(nge)))
+        return vid[:nva], eid[:nea], gsn, ngv.value, nge.value
+
+    def profile_enable(self, on=True):
+        self._ck(self.lib.topo_profile_enable(self.h, int(on)))
+
+    def profile_read(self, family):
+        n, ms = C.c_int(), C.c_double()
+        self._ck(self.lib.topo_profile_read(self.h, family, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def launch_count(self) -> int:
+        n = C.c_longlong()
+        self._ck(self.lib.topo_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def sync(self):
+        self._ck(self.lib.topo_sync(self.h))
+
+    def timer_start(self):
+        self._ck(self.lib.topo_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._ck(self.lib.topo_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def put_from(self, name, host_ptr, count, level=0):
+        """Copy ``count`` elements from a raw host pointer (e.g. pinned memory)."""
+        self._ck(self.lib.topo_put_array(self.h, ARRAYS[name], level, host_ptr, count))
+
+    def get_into(self, name, host_ptr, count, level=0):
+        self._ck(self.lib.topo_get_array(self.h, ARRAYS[name], level, host_ptr, count))
+
+    def design_iteration(self, solve=None, oc=None, filter_radius=2.0):
+        s = dict(mode=SOLVE_MIXED, smoother=SMOOTH_GS, pre=2, post=2, rtol=1e-6, max_iter=200,
+                 inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1)
+        s.update(solve or {})
+        c = dict(vgoal=0.4, damp=0.5, step=0.03, cmin=0.0, cmax=1.0, apply_twice=0, reference_volume=1)
+        c.update(oc or {})
+        o = IterOpts(SolveOpts(s["mode"], s["smoother"], s["pre"], s["post"], s["rtol"], s["max_iter"],
+                               s["inner_rtol"], s["cheb_degree"], s["cheb_lo"], s["cheb_hi"], s["inner_max"]),
+                     OcOpts(c["vgoal"], c["damp"], c["step"], c["cmin"], c["cmax"], int(c["apply_twice"]),
+                            int(c["reference_volume"])), filter_radius)
+        st = IterStats()
+        rc = self.lib.topo_design_iteration(self.h, C.byref(o), C.byref(st))
+        if rc not in (TOPO_OK, TOPO_E_NOT_CONVERGED):
+            self._ck(rc)
+        return {"compliance": st.compliance, "volume": st.volume, "iterations": st.solve.iterations,
+                "vcycles": st.solve.vcycles, "relres": st.solve.relres, "solve_ms": st.solve.ms,
+                "oc_trials": st.oc_trials, "ms": st.ms, "rc": rc}

@@ -1,0 +1,1399 @@
+// C ABI of libtopo_gb300: handle life cycle, array transfer and the host
+// orchestration of the hot path (operator update, V-cycle, PCG, mixed-precision
+// defect correction, sensitivity chain and OC bisection).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "topo_internal.h"
+
+namespace topo {
+std::atomic<long long> g_launches{0};
+}
+
+using namespace topo;
+
+namespace {
+
+// Scalar slots in device memory used by the PCG drivers.
+enum Slot { S_RZ = 0, S_ZROLD = 1, S_RZOLD = 2, S_DQ = 3, S_RR = 4, S_FF = 5, S_TMP = 6, S_COUNT = 16 };
+
+struct EventPair {
+  cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct topo_handle {
+  topo_config cfg{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  Hierarchy H;
+  std::vector<DevLevel> lv;
+  double Ke[576];
+  double lam = 0, mu = 0;
+  std::vector<void*> allocs;
+  // element template and Galerkin tables
+  double* dKe = nullptr;
+  double* dT64 = nullptr;
+  float* dT32 = nullptr;
+  // level-0 design arrays
+  double *rho = nullptr, *rhop = nullptr, *sens = nullptr, *sens_tmp = nullptr;
+  float* rhop32 = nullptr;
+  bool rhop_stale = false;
+  // spline
+  bool spline_set = false;
+  SplineTables st;
+  SplineDev sd{};
+  double *coeff = nullptr, *csens = nullptr, *coeff_old = nullptr, *coeff_tmp = nullptr;
+  double *adj1 = nullptr, *adj2 = nullptr;
+  // level-0 work vectors
+  double *work = nullptr, *x = nullptr, *r = nullptr, *d = nullptr, *q = nullptr, *rold = nullptr,
+         *f = nullptr;
+  float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *q32 = nullptr, *rold32 = nullptr;
+  // coarsest level
+  int ndense = 0;
+  double* A = nullptr;
+  float* A32 = nullptr;
+  double* coarse64tmp = nullptr;  // FP64 copy of an FP32 coarsest stencil
+  int* status = nullptr;
+  // first coarse level: elements whose fine elements touch fixed DOFs
+  int* gal_fixed = nullptr;
+  int n_gal_fixed = 0;
+  int coarse_dropped = 0;  // null directions dropped by the coarsest inverse
+  cudaEvent_t timer_ev[2] = {nullptr, nullptr};
+  // sensitivity filter ball (offsets and weights) for the last radius used
+  double filt_radius = -1.0;
+  int4* filt_offs = nullptr;
+  double* filt_w = nullptr;
+  int filt_n = 0;
+  // reductions
+  double* partial = nullptr;
+  double* sc = nullptr;    // device scalar slots
+  double* hsc = nullptr;   // pinned host mirror
+  int64_t active_elements = 0, gs_padded_elements = 0;
+  bool bc_set = false, ops_ready = false;
+  int op_precision = 3;    // bit0 FP64 operators, bit1 FP32 operators
+  bool ops64 = false, ops32 = false;
+  // profiling
+  bool prof = false;
+  std::vector<EventPair> evs[TOPO_K_COUNT];
+  std::vector<EventPair> evpool;
+};
+
+namespace {
+
+int fail(topo_handle* h, int code, const char* fmt, ...) {
+  if (h) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    h->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(h, TOPO_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                    \
+  } while (0)
+
+#define CKL()                                                                              \
+  do {                                                                                     \
+    cudaError_t e_ = cudaGetLastError();                                                   \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(h, TOPO_E_CUDA, "kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                     \
+  } while (0)
+
+#define RET(x)                   \
+  do {                           \
+    int rc_ = (x);               \
+    if (rc_ != TOPO_OK) return rc_; \
+  } while (0)
+
+template <typename T>
+int dalloc(topo_handle* h, T** p, int64_t n) {
+  *p = nullptr;
+  if (n <= 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (size_t)n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, TOPO_E_NOMEM, "cudaMalloc of %lld bytes failed: %s", (long long)(sizeof(T) * n),
+                cudaGetErrorString(e));
+  }
+  h->allocs.push_back((void*)*p);
+  cudaMemsetAsync(*p, 0, sizeof(T) * (size_t)n, h->stream);
+  return TOPO_OK;
+}
+
+// ---- profiling brackets --------------------------------------------------
+EventPair* prof_begin(topo_handle* h, int fam) {
+  if (!h->prof) return nullptr;
+  EventPair p;
+  if (!h->evpool.empty()) {
+    p = h->evpool.back();
+    h->evpool.pop_back();
+  } else {
+    cudaEventCreate(&p.a);
+    cudaEventCreate(&p.b);
+  }
+  cudaEventRecord(p.a, h->stream);
+  h->evs[fam].push_back(p);
+  return &h->evs[fam].back();
+}
+void prof_end(topo_handle* h, EventPair* p) {
+  if (p) cudaEventRecord(p->b, h->stream);
+}
+
+// ---- level operations (templated on precision) ---------------------------
+template <typename T> struct P;
+template <> struct P<double> {
+  static double* U(DevLevel& L) { return L.U; }
+  static double* U2(DevLevel& L) { return L.U2; }
+  static double* F(DevLevel& L) { return L.F; }
+  static double* R(DevLevel& L) { return L.R; }
+  static double* st(DevLevel& L) { return L.stencil; }
+  static double* dinv(DevLevel& L) { return L.dinv; }
+  static double* cd(DevLevel& L) { return L.cd; }
+  static double* rhop(topo_handle* h) { return h->rhop; }
+  static double* Ainv(topo_handle* h) { return h->A; }
+  static double& lmax(DevLevel& L) { return L.lmax; }
+  static const int fam_apply = TOPO_K_FINE_APPLY64, fam_smooth = TOPO_K_FINE_SMOOTH64;
+};
+template <> struct P<float> {
+  static float* U(DevLevel& L) { return L.U32; }
+  static float* U2(DevLevel& L) { return L.U2_32; }
+  static float* F(DevLevel& L) { return L.F32; }
+  static float* R(DevLevel& L) { return L.R32; }
+  static float* st(DevLevel& L) { return L.stencil32; }
+  static float* dinv(DevLevel& L) { return L.dinv32; }
+  static float* cd(DevLevel& L) { return L.cd32; }
+  static float* rhop(topo_handle* h) { return h->rhop32; }
+  static float* Ainv(topo_handle* h) { return h->A32; }
+  static double& lmax(DevLevel& L) { return L.lmax32; }
+  static const int fam_apply = TOPO_K_FINE_APPLY32, fam_smooth = TOPO_K_FINE_SMOOTH32;
+};
+
+// out = A_l u (residual: out = f - A_l u)
+template <typename T>
+void level_apply(topo_handle* h, int l, const T* u, const T* f, T* out, bool residual) {
+  DevLevel& L = h->lv[l];
+  if (l == 0) {
+    EventPair* ev = prof_begin(h, P<T>::fam_apply);
+    launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual);
+    prof_end(h, ev);
+  } else {
+    launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual);
+  }
+  count_launch();
+}
+
+template <typename T>
+void level_residual(topo_handle* h, int l) {
+  DevLevel& L = h->lv[l];
+  level_apply<T>(h, l, P<T>::U(L), P<T>::F(L), P<T>::R(L), true);
+}
+
+template <typename T>
+void gs_level(topo_handle* h, int l, int sweeps, bool reverse) {
+  DevLevel& L = h->lv[l];
+  for (int s = 0; s < sweeps; ++s)
+    for (int cc = 0; cc < 8; ++cc) {
+      const int col = reverse ? 7 - cc : cc;
+      if (l == 0) {
+        EventPair* ev = prof_begin(h, P<T>::fam_smooth);
+        launch_fine_gs<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, P<T>::U(L), P<T>::F(L), col, reverse);
+        prof_end(h, ev);
+      } else {
+        launch_stencil_gs<T>(h->stream, L.d, P<T>::st(L), L.vmask, P<T>::U(L), P<T>::F(L), col, reverse);
+      }
+      count_launch();
+    }
+}
+
+template <typename T>
+void diag_inv_level(topo_handle* h, int l) {
+  DevLevel& L = h->lv[l];
+  if (l == 0) launch_fine_diag_inv<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, P<T>::dinv(L));
+  else launch_stencil_diag_inv<T>(h->stream, L.d, P<T>::st(L), L.vmask, P<T>::dinv(L));
+  count_launch();
+}
+
+struct ChebParams {
+  int degree = 2;
+  double lo = 0.3, hi = 1.1;
+};
+
+// Chebyshev polynomial smoother in point-block-Jacobi form (three-term
+// recurrence, Saad, Iterative Methods for Sparse Linear Systems, Alg. 12.1).
+// Each step is one fused kernel that reads the iterate from one buffer and
+// writes the next into the other; the result ends in level U.
+template <typename T>
+void cheb_level(topo_handle* h, int l, const ChebParams& cp) {
+  DevLevel& L = h->lv[l];
+  const double lmax = P<T>::lmax(L) * cp.hi, lmin = P<T>::lmax(L) * cp.lo;
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+  const double sigma = theta / delta;
+  double rho_old = 1.0 / sigma;
+  T* ua = P<T>::U(L);
+  T* ub = P<T>::U2(L);
+  for (int k = 0; k < cp.degree; ++k) {
+    double c_old = 0.0, c_new = 1.0 / theta;
+    if (k > 0) {
+      const double rho_new = 1.0 / (2.0 * sigma - rho_old);
+      c_old = rho_new * rho_old;
+      c_new = 2.0 * rho_new / delta;
+      rho_old = rho_new;
+    }
+    if (l == 0) {
+      EventPair* ev = prof_begin(h, P<T>::fam_smooth);
+      launch_fine_cheb<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L),
+                          P<T>::cd(L), c_old, c_new, k == 0);
+      prof_end(h, ev);
+    } else {
+      launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
+                             c_old, c_new, k == 0);
+    }
+    count_launch();
+    std::swap(ua, ub);
+  }
+  if (ua != P<T>::U(L)) {
+    cudaMemcpyAsync(P<T>::U(L), ua, sizeof(T) * 3 * L.d.nv, cudaMemcpyDeviceToDevice, h->stream);
+  }
+}
+
+template <typename T>
+void smooth_level(topo_handle* h, int l, int sweeps, bool reverse, int smoother, const ChebParams& cp) {
+  if (smoother == TOPO_SMOOTH_CHEBYSHEV) {
+    for (int s = 0; s < sweeps; ++s) cheb_level<T>(h, l, cp);
+  } else {
+    gs_level<T>(h, l, sweeps, reverse);
+  }
+}
+
+template <typename T>
+void coarsest_solve_T(topo_handle* h) {
+  DevLevel& L = h->lv.back();
+  launch_dense_gemv<T>(h->stream, h->ndense, P<T>::Ainv(h), P<T>::F(L), P<T>::U(L), L.d.nv);
+  count_launch();
+}
+
+template <typename T>
+void restrict_T(topo_handle* h, int lc) {
+  launch_restrict<T>(h->stream, h->lv[lc - 1].d, h->lv[lc].d, P<T>::R(h->lv[lc - 1]), P<T>::F(h->lv[lc]));
+  count_launch();
+}
+
+template <typename T>
+void prolong_T(topo_handle* h, int lf) {
+  launch_prolong<T>(h->stream, h->lv[lf].d, h->lv[lf + 1].d, P<T>::U(h->lv[lf + 1]), P<T>::U(h->lv[lf]),
+                    h->lv[lf].vmask);
+  count_launch();
+}
+
+// V-cycle in the reference order (grid/Grid.cpp:2399-2444).  `sym` runs the
+// adjoint sweep after the coarse correction so the cycle is a symmetric
+// preconditioner.  Level-0 U must hold the initial guess, F the right-hand side.
+template <typename T>
+void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, const ChebParams& cp) {
+  const int nl = (int)h->lv.size();
+  if (nl == 1) {
+    smooth_level<T>(h, 0, pre, false, smoother, cp);
+    smooth_level<T>(h, 0, post, sym, smoother, cp);
+    return;
+  }
+  for (int l = 0; l < nl; ++l) {
+    if (l > 0) {
+      level_residual<T>(h, l - 1);
+      restrict_T<T>(h, l);
+      cudaMemsetAsync(P<T>::U(h->lv[l]), 0, sizeof(T) * 3 * h->lv[l].d.nv, h->stream);
+    }
+    if (l < nl - 1) smooth_level<T>(h, l, pre, false, smoother, cp);
+    else coarsest_solve_T<T>(h);
+  }
+  for (int l = nl - 2; l >= 0; --l) {
+    prolong_T<T>(h, l);
+    smooth_level<T>(h, l, post, sym, smoother, cp);
+  }
+}
+
+// Power iteration for the largest eigenvalue of D^{-1} A on a level, from the
+// same deterministic start vector as the oracle.
+__global__ void k_power_start(int64_t nv, const uint8_t* vmask, double* x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nv) return;
+  uint64_t hsh = (uint64_t)i * 0x9E3779B97F4A7C15ull;
+  hsh ^= hsh >> 29;
+  double v = 0.5 + (double)(hsh % 1000) / 1000.0;
+  const int64_t vv = i % nv;
+  const int c = (int)(i / nv);
+  if (!((vmask[vv] >> c) & 1) || !(vmask[vv] & 8)) v = 0.0;
+  x[i] = v;
+}
+
+template <typename T>
+__global__ void k_scale_cast(int64_t n, const double* x, double s_num_sqrt_inv_slot_dummy, const double* sc,
+                             int slot, T* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double nrm = sqrt(sc[slot]);
+  out[i] = (T)(x[i] / nrm);
+}
+
+template <typename T>
+__global__ void k_dinv_apply(int64_t nv, const T* dinv, const T* r, T* z) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const T r0 = r[v], r1 = r[nv + v], r2 = r[2 * nv + v];
+  for (int i = 0; i < 3; ++i)
+    z[i * nv + v] = dinv[(3 * i) * nv + v] * r0 + dinv[(3 * i + 1) * nv + v] * r1 + dinv[(3 * i + 2) * nv + v] * r2;
+}
+
+template <typename T>
+__global__ void k_to_double(int64_t n, const T* a, double* b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+
+inline unsigned nb256(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+template <typename T>
+int estimate_lmax(topo_handle* h, int l, double* out) {
+  DevLevel& L = h->lv[l];
+  const int64_t n3 = 3 * L.d.nv;
+  // x (double) lives in h->work-sized scratch: use level buffers: R (as T) and cd (as T)
+  double* xd = nullptr;
+  T *xt = nullptr, *yt = nullptr, *zt = nullptr;
+  CK(cudaMallocAsync((void**)&xd, sizeof(double) * n3, h->stream));
+  CK(cudaMallocAsync((void**)&xt, sizeof(T) * n3, h->stream));
+  CK(cudaMallocAsync((void**)&yt, sizeof(T) * n3, h->stream));
+  CK(cudaMallocAsync((void**)&zt, sizeof(T) * n3, h->stream));
+  k_power_start<<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, xd);
+  double lam = 0.0;
+  for (int it = 0; it < 12; ++it) {
+    launch_dot<double>(h->stream, xd, xd, n3, h->partial, h->sc + S_TMP);
+    k_scale_cast<T><<<nb256(n3), 256, 0, h->stream>>>(n3, xd, 0.0, h->sc, S_TMP, xt);
+    if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, xt, nullptr, yt, false);
+    else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), xt, nullptr, yt, false);
+    k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), yt, zt);
+    launch_dot<T>(h->stream, xt, zt, n3, h->partial, h->sc + S_TMP + 1);
+    k_to_double<T><<<nb256(n3), 256, 0, h->stream>>>(n3, zt, xd);
+    count_launch(7);
+  }
+  CK(cudaMemcpyAsync(h->hsc, h->sc + S_TMP + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  lam = h->hsc[0];
+  cudaFreeAsync(xd, h->stream);
+  cudaFreeAsync(xt, h->stream);
+  cudaFreeAsync(yt, h->stream);
+  cudaFreeAsync(zt, h->stream);
+  *out = lam;
+  return TOPO_OK;
+}
+
+template <typename T>
+int prepare_smoother(topo_handle* h, int smoother) {
+  if (smoother != TOPO_SMOOTH_CHEBYSHEV) return TOPO_OK;
+  for (size_t l = 0; l < h->lv.size(); ++l) {
+    DevLevel& L = h->lv[l];
+    if (P<T>::lmax(L) != 0.0) continue;
+    diag_inv_level<T>(h, (int)l);
+    double lm = 0;
+    RET(estimate_lmax<T>(h, (int)l, &lm));
+    P<T>::lmax(L) = lm;
+  }
+  return TOPO_OK;
+}
+
+int read_scalars(topo_handle* h, int first, int count) {
+  CK(cudaMemcpyAsync(h->hsc + first, h->sc + first, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return TOPO_OK;
+}
+
+// Flexible conjugate gradients (Polak-Ribiere beta, i.e. FCG with one stored
+// direction) on level 0 in precision T.  Solves A x = b (warm start in x);
+// prec(r, z) writes z = M r.  Scalars live in device slots sc[base .. base+6],
+// so an FCG may run nested inside another one's preconditioner.
+template <typename T, typename Prec>
+int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, double rtol, int maxit,
+          int base, Prec&& prec, int* iters, double* rel_out, double bnorm_ref) {
+  DevLevel& L0 = h->lv[0];
+  const int64_t n3 = 3 * L0.d.nv;
+  double* sc = h->sc + base;
+  level_apply<T>(h, 0, x, b, r, true);  // r = b - A x
+  launch_dot<T>(h->stream, r, r, n3, h->partial, sc + S_RR);
+  count_launch(2);
+  RET(read_scalars(h, base + S_RR, 1));
+  double rn = std::sqrt(h->hsc[base + S_RR]);
+  const double bn = bnorm_ref;
+  int it = 0;
+  while (rn / bn > rtol && it < maxit) {
+    RET(prec(r, z));
+    launch_dot<T>(h->stream, r, z, n3, h->partial, sc + S_RZ);
+    count_launch(2);
+    if (it > 0) {
+      launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD);
+      count_launch(2);
+    }
+    launch_pcg_dir<T>(h->stream, z, d, sc, S_RZ, S_RZOLD, it == 0, n3);
+    level_apply<T>(h, 0, d, nullptr, q, false);
+    launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ);
+    launch_pcg_update<T>(h->stream, x, r, rold, d, q, sc, S_RZ, S_DQ, n3);
+    CK(cudaMemcpyAsync(sc + S_RZOLD, sc + S_RZ, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    launch_dot<T>(h->stream, r, r, n3, h->partial, sc + S_RR);
+    count_launch(7);
+    CKL();
+    RET(read_scalars(h, base + S_RR, 1));
+    rn = std::sqrt(h->hsc[base + S_RR]);
+    if (!std::isfinite(rn)) return fail(h, TOPO_E_NONFINITE, "CG residual became non-finite at iteration %d", it);
+    ++it;
+  }
+  *iters = it;
+  *rel_out = rn / bn;
+  return TOPO_OK;
+}
+
+// V-cycle preconditioner in precision T: z = V(r) with a zero initial guess.
+// z must be level-0 U of precision T (the V-cycle works in place there).
+template <typename T>
+int vcycle_prec(topo_handle* h, const T* r, int pre, int post, int smoother, const ChebParams& cp) {
+  DevLevel& L0 = h->lv[0];
+  const int64_t n3 = 3 * L0.d.nv;
+  CK(cudaMemcpyAsync(P<T>::F(L0), r, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemsetAsync(P<T>::U(L0), 0, sizeof(T) * n3, h->stream));
+  vcycle_core<T>(h, pre, post, true, smoother, cp);
+  return TOPO_OK;
+}
+
+int check_ready(topo_handle* h, bool need_ops) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (!h->bc_set) return fail(h, TOPO_E_STATE, "boundary conditions not set (call topo_set_bc)");
+  if (need_ops && !h->ops_ready) return fail(h, TOPO_E_STATE, "operators not built (call topo_update_operators)");
+  return TOPO_OK;
+}
+
+int update_penalised_if_stale(topo_handle* h) {
+  if (!h->rhop_stale) return TOPO_OK;
+  launch_penalise(h->stream, h->lv[0].d.ne, h->lv[0].eactive, h->rho, h->cfg.power_penalty, h->rhop,
+                  h->rhop32);
+  count_launch();
+  CKL();
+  h->rhop_stale = false;
+  return TOPO_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** out) {
+  if (!cfg || !out) return TOPO_E_BAD_INPUT;
+  *out = nullptr;
+  if (cfg->nx < 1 || cfg->ny < 1 || cfg->nz < 1 || !(cfg->h > 0) || !(cfg->youngs_modulus > 0) ||
+      !(cfg->poisson_ratio > -1.0 && cfg->poisson_ratio < 0.5) || !(cfg->power_penalty >= 1.0) ||
+      !(cfg->min_density > 0 && cfg->min_density <= 1.0))
+    return TOPO_E_BAD_INPUT;
+  if ((int64_t)(cfg->nx + 1) * (cfg->ny + 1) * (cfg->nz + 1) >= ((int64_t)1 << 31))
+    return TOPO_E_BAD_INPUT;
+  auto h = std::make_unique<topo_handle>();
+  h->cfg = *cfg;
+  if (h->cfg.max_coarse_elements <= 0) h->cfg.max_coarse_elements = 400;
+  topo_handle* hp = h.get();
+  {
+    topo_handle* h = hp;  // for CK
+    CK(cudaSetDevice(cfg->device));
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  }
+  h->H = build_hierarchy(cfg->nx, cfg->ny, cfg->nz, eactive, h->cfg.max_coarse_elements);
+  element_template(cfg->youngs_modulus, cfg->poisson_ratio, cfg->h, h->Ke);
+  h->lam = cfg->youngs_modulus * cfg->poisson_ratio / ((1 + cfg->poisson_ratio) * (1 - 2 * cfg->poisson_ratio));
+  h->mu = cfg->youngs_modulus / (2 * (1 + cfg->poisson_ratio));
+  upload_template(h->Ke, h->lam, h->mu, cfg->h);
+  const int nl = (int)h->H.dims.size();
+  h->lv.resize(nl);
+  int rc = TOPO_OK;
+  auto A = [&](int r) { if (rc == TOPO_OK) rc = r; };
+  for (int l = 0; l < nl; ++l) {
+    DevLevel& L = h->lv[l];
+    L.d = h->H.dims[l];
+    const int64_t nv = L.d.nv, ne = L.d.ne;
+    A(dalloc(hp, &L.eactive, ne));
+    A(dalloc(hp, &L.vmask, nv));
+    A(dalloc(hp, &L.U, 3 * nv)); A(dalloc(hp, &L.F, 3 * nv)); A(dalloc(hp, &L.R, 3 * nv));
+    A(dalloc(hp, &L.U32, 3 * nv)); A(dalloc(hp, &L.F32, 3 * nv)); A(dalloc(hp, &L.R32, 3 * nv));
+    A(dalloc(hp, &L.dinv, 9 * nv)); A(dalloc(hp, &L.dinv32, 9 * nv));
+    A(dalloc(hp, &L.cd, 3 * nv)); A(dalloc(hp, &L.cd32, 3 * nv));
+    A(dalloc(hp, &L.U2, 3 * nv)); A(dalloc(hp, &L.U2_32, 3 * nv));
+    if (l > 0) {
+      A(dalloc(hp, &L.kel, 576 * ne)); A(dalloc(hp, &L.kel32, 576 * ne));
+      A(dalloc(hp, &L.stencil, 243 * nv)); A(dalloc(hp, &L.stencil32, 243 * nv));
+    }
+    if (rc != TOPO_OK) break;
+    std::vector<uint8_t> vm(h->H.vactive[l]);
+    for (auto& m : vm) m = (m & 8) ? 0xF : 0;
+    cudaMemcpyAsync(L.eactive, h->H.eactive[l].data(), ne, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(L.vmask, vm.data(), nv, cudaMemcpyHostToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
+  }
+  const LevelDims& d0 = h->lv.empty() ? LevelDims{} : h->lv[0].d;
+  if (rc == TOPO_OK) {
+    A(dalloc(hp, &h->rho, d0.ne)); A(dalloc(hp, &h->rhop, d0.ne)); A(dalloc(hp, &h->rhop32, d0.ne));
+    A(dalloc(hp, &h->sens, d0.ne)); A(dalloc(hp, &h->sens_tmp, d0.ne));
+    A(dalloc(hp, &h->work, 3 * d0.nv)); A(dalloc(hp, &h->x, 3 * d0.nv)); A(dalloc(hp, &h->r, 3 * d0.nv));
+    A(dalloc(hp, &h->d, 3 * d0.nv)); A(dalloc(hp, &h->q, 3 * d0.nv)); A(dalloc(hp, &h->rold, 3 * d0.nv));
+    A(dalloc(hp, &h->f, 3 * d0.nv));
+    A(dalloc(hp, &h->x32, 3 * d0.nv)); A(dalloc(hp, &h->r32, 3 * d0.nv)); A(dalloc(hp, &h->d32, 3 * d0.nv));
+    A(dalloc(hp, &h->q32, 3 * d0.nv)); A(dalloc(hp, &h->rold32, 3 * d0.nv));
+    A(dalloc(hp, &h->dKe, 576));
+    A(dalloc(hp, &h->partial, 2048)); A(dalloc(hp, &h->sc, S_COUNT)); A(dalloc(hp, &h->status, 4));
+  }
+  if (rc == TOPO_OK && nl > 1) {
+    const LevelDims& dl = h->lv.back().d;
+    h->ndense = (int)(3 * dl.nv);
+    if (h->ndense > 20000) rc = fail(hp, TOPO_E_BAD_INPUT, "coarsest level too large (%d DOFs)", h->ndense);
+    else {
+      A(dalloc(hp, &h->A, (int64_t)h->ndense * h->ndense));
+      A(dalloc(hp, &h->A32, (int64_t)h->ndense * h->ndense));
+      A(dalloc(hp, &h->coarse64tmp, 243 * dl.nv));
+    }
+    std::vector<double> T;
+    galerkin_tables(h->Ke, h->lv[1].d.factor, T);
+    std::vector<float> T32(T.begin(), T.end());
+    A(dalloc(hp, &h->dT64, (int64_t)T.size()));
+    A(dalloc(hp, &h->dT32, (int64_t)T.size()));
+    if (rc == TOPO_OK) {
+      cudaMemcpyAsync(h->dT64, T.data(), sizeof(double) * T.size(), cudaMemcpyHostToDevice, h->stream);
+      cudaMemcpyAsync(h->dT32, T32.data(), sizeof(float) * T32.size(), cudaMemcpyHostToDevice, h->stream);
+      cudaStreamSynchronize(h->stream);
+    }
+  }
+  if (rc == TOPO_OK) {
+    cudaMemcpyAsync(h->dKe, h->Ke, sizeof(double) * 576, cudaMemcpyHostToDevice, h->stream);
+    cudaHostAlloc((void**)&h->hsc, sizeof(double) * S_COUNT, cudaHostAllocDefault);
+    // density starts at 1 on active elements
+    std::vector<double> one(d0.ne);
+    for (int64_t e = 0; e < d0.ne; ++e) one[e] = h->H.eactive[0][e] ? 1.0 : 0.0;
+    cudaMemcpyAsync(h->rho, one.data(), sizeof(double) * d0.ne, cudaMemcpyHostToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
+    h->rhop_stale = true;
+    for (auto a : h->H.eactive[0]) h->active_elements += a ? 1 : 0;
+    h->gs_padded_elements = gs_padded_count(d0, h->H.eactive[0].data(), false);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fail(hp, TOPO_E_CUDA, "set-up failed: %s", cudaGetErrorString(e));
+  }
+  if (rc != TOPO_OK) {
+    std::string msg = hp->err;
+    topo_destroy(h.release());
+    (void)msg;
+    return rc;
+  }
+  *out = h.release();
+  return TOPO_OK;
+}
+
+void topo_destroy(topo_handle* h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (void* p : h->allocs) cudaFree(p);
+  for (int f = 0; f < TOPO_K_COUNT; ++f)
+    for (auto& e : h->evs[f]) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+  for (auto& e : h->evpool) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+  if (h->hsc) cudaFreeHost(h->hsc);
+  if (h->gal_fixed) cudaFree(h->gal_fixed);
+  if (h->filt_offs) cudaFree(h->filt_offs);
+  if (h->timer_ev[0]) { cudaEventDestroy(h->timer_ev[0]); cudaEventDestroy(h->timer_ev[1]); }
+  if (h->filt_w) cudaFree(h->filt_w);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+const char* topo_last_error(const topo_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int topo_num_levels(const topo_handle* h, int* n) {
+  if (!h || !n) return TOPO_E_BAD_INPUT;
+  *n = (int)h->lv.size();
+  return TOPO_OK;
+}
+
+int topo_level_dims(const topo_handle* h, int level, int* dims3, int* factor) {
+  if (!h || !dims3 || level < 0 || level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
+  const LevelDims& d = h->lv[level].d;
+  dims3[0] = d.ex; dims3[1] = d.ey; dims3[2] = d.ez;
+  if (factor) *factor = d.factor;
+  return TOPO_OK;
+}
+
+int topo_sync(topo_handle* h) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  CK(cudaStreamSynchronize(h->stream));
+  return TOPO_OK;
+}
+
+int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads) {
+  if (!h || !fixed || !loads) return TOPO_E_BAD_INPUT;
+  DevLevel& L = h->lv[0];
+  const int64_t nv = L.d.nv;
+  std::vector<uint8_t> vm(nv);
+  std::vector<double> F(3 * nv);
+  for (int64_t v = 0; v < nv; ++v) {
+    uint8_t m = h->H.vactive[0][v] & 0x8;
+    if (m) m |= (uint8_t)(~fixed[v] & 0x7);
+    vm[v] = m;
+    for (int c = 0; c < 3; ++c) {
+      const double ld = loads[c * nv + v];
+      if (!std::isfinite(ld)) return fail(h, TOPO_E_BAD_INPUT, "non-finite load at vertex %lld", (long long)v);
+      F[c * nv + v] = ((m >> c) & 1) ? ld : 0.0;
+    }
+  }
+  CK(cudaMemcpyAsync(L.vmask, vm.data(), nv, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(L.F, F.data(), sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, h->stream));
+  if (h->lv.size() > 1) {
+    // coarse elements of level 1 containing a fine element with a fixed DOF
+    const LevelDims& c = h->lv[1].d;
+    const LevelDims& fd = L.d;
+    const int fct = c.factor;
+    std::vector<int> list;
+    for (int cz = 0; cz < c.ez; ++cz)
+      for (int cy = 0; cy < c.ey; ++cy)
+        for (int cx = 0; cx < c.ex; ++cx) {
+          bool hit = false;
+          for (int pz = 0; pz < fct && !hit; ++pz)
+            for (int py = 0; py < fct && !hit; ++py)
+              for (int px = 0; px < fct && !hit; ++px) {
+                const int fx = cx * fct + px, fy = cy * fct + py, fz = cz * fct + pz;
+                if (fx >= fd.ex || fy >= fd.ey || fz >= fd.ez) continue;
+                if (!h->H.eactive[0][fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz)]) continue;
+                for (int a = 0; a < 8 && !hit; ++a) {
+                  const int64_t vv = (fx + (a & 1)) + (int64_t)fd.vx * ((fy + ((a >> 1) & 1)) + (int64_t)fd.vy * (fz + (a >> 2)));
+                  if ((vm[vv] & 7) != 7) hit = true;
+                }
+              }
+          if (hit) list.push_back((int)(cx + (int64_t)c.ex * (cy + (int64_t)c.ey * cz)));
+        }
+    if (h->gal_fixed) { cudaFree(h->gal_fixed); h->gal_fixed = nullptr; }
+    h->n_gal_fixed = (int)list.size();
+    if (!list.empty()) {
+      CK(cudaMalloc((void**)&h->gal_fixed, sizeof(int) * list.size()));
+      CK(cudaMemcpyAsync(h->gal_fixed, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, h->stream));
+    }
+  }
+  CK(cudaMemsetAsync(L.U, 0, sizeof(double) * 3 * nv, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->bc_set = true;
+  h->ops_ready = false;
+  for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
+  return TOPO_OK;
+}
+
+int topo_set_spline(topo_handle* h, int order, const int* partition3, const double* bmin3,
+                    const double* bmax3) {
+  if (!h || !partition3 || !bmin3 || !bmax3 || order < 2 || order > 4) return TOPO_E_BAD_INPUT;
+  for (int a = 0; a < 3; ++a)
+    if (partition3[a] < 0 || !(bmax3[a] > bmin3[a])) return TOPO_E_BAD_INPUT;
+  const LevelDims& d0 = h->lv[0].d;
+  int nelem[3] = {d0.ex, d0.ey, d0.ez};
+  spline_tables(order, partition3, bmin3, bmax3, nelem, h->cfg.h, h->st);
+  SplineDev& sd = h->sd;
+  sd.order = order;
+  for (int a = 0; a < 3; ++a) {
+    sd.nb[a] = h->st.nb[a];
+    int *i0 = nullptr, *lo = nullptr, *hi = nullptr;
+    double* N = nullptr;
+    RET(dalloc(h, &i0, nelem[a]));
+    RET(dalloc(h, &N, (int64_t)nelem[a] * order));
+    RET(dalloc(h, &lo, sd.nb[a]));
+    RET(dalloc(h, &hi, sd.nb[a]));
+    CK(cudaMemcpyAsync(i0, h->st.i0[a].data(), sizeof(int) * nelem[a], cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(N, h->st.N[a].data(), sizeof(double) * nelem[a] * order, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(lo, h->st.lo[a].data(), sizeof(int) * sd.nb[a], cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(hi, h->st.hi[a].data(), sizeof(int) * sd.nb[a], cudaMemcpyHostToDevice, h->stream));
+    sd.i0[a] = i0; sd.N[a] = N; sd.lo[a] = lo; sd.hi[a] = hi;
+  }
+  const int64_t nc = (int64_t)sd.nb[0] * sd.nb[1] * sd.nb[2];
+  RET(dalloc(h, &h->coeff, nc));
+  RET(dalloc(h, &h->csens, nc));
+  RET(dalloc(h, &h->coeff_old, nc));
+  RET(dalloc(h, &h->coeff_tmp, nc));
+  RET(dalloc(h, &h->adj1, (int64_t)sd.nb[0] * d0.ey * d0.ez));
+  RET(dalloc(h, &h->adj2, (int64_t)sd.nb[0] * sd.nb[1] * d0.ez));
+  CK(cudaStreamSynchronize(h->stream));
+  h->spline_set = true;
+  return TOPO_OK;
+}
+
+int topo_num_coeffs(const topo_handle* h, int* n) {
+  if (!h || !n) return TOPO_E_BAD_INPUT;
+  if (!h->spline_set) return TOPO_E_STATE;
+  *n = h->sd.nb[0] * h->sd.nb[1] * h->sd.nb[2];
+  return TOPO_OK;
+}
+
+int topo_get_knots(const topo_handle* h, int axis, double* out, size_t count) {
+  if (!h || !out || axis < 0 || axis > 2) return TOPO_E_BAD_INPUT;
+  if (!h->spline_set) return TOPO_E_STATE;
+  if (count != h->st.knots[axis].size()) return TOPO_E_BAD_INPUT;
+  std::copy(h->st.knots[axis].begin(), h->st.knots[axis].end(), out);
+  return TOPO_OK;
+}
+
+static int array_info(topo_handle* h, int which, int level, void** dptr, size_t* count, size_t* esize) {
+  if (level < 0 || level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
+  DevLevel& L = h->lv[level];
+  const LevelDims& d0 = h->lv[0].d;
+  const int64_t nc = h->spline_set ? (int64_t)h->sd.nb[0] * h->sd.nb[1] * h->sd.nb[2] : 0;
+  *esize = sizeof(double);
+  switch (which) {
+    case TOPO_RHO: *dptr = h->rho; *count = d0.ne; break;
+    case TOPO_RHOP: *dptr = h->rhop; *count = d0.ne; break;
+    case TOPO_SENS: *dptr = h->sens; *count = d0.ne; break;
+    case TOPO_COEFF: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->coeff; *count = nc; break;
+    case TOPO_CSENS: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->csens; *count = nc; break;
+    case TOPO_U: *dptr = L.U; *count = 3 * L.d.nv; break;
+    case TOPO_F: *dptr = L.F; *count = 3 * L.d.nv; break;
+    case TOPO_R: *dptr = L.R; *count = 3 * L.d.nv; break;
+    case TOPO_STENCIL: if (level == 0) return TOPO_E_BAD_INPUT; *dptr = L.stencil; *count = 243 * L.d.nv; break;
+    case TOPO_KELEM: if (level == 0) return TOPO_E_BAD_INPUT; *dptr = L.kel; *count = 576 * L.d.ne; break;
+    case TOPO_VMASK: *dptr = L.vmask; *count = L.d.nv; *esize = 1; break;
+    case TOPO_EACTIVE: *dptr = L.eactive; *count = L.d.ne; *esize = 1; break;
+    case TOPO_KE: *dptr = h->dKe; *count = 576; break;
+    case TOPO_WORK: if (level != 0) return TOPO_E_BAD_INPUT; *dptr = h->work; *count = 3 * d0.nv; break;
+    default: return TOPO_E_BAD_INPUT;
+  }
+  return TOPO_OK;
+}
+
+int topo_array_size(const topo_handle* h, int which, int level, size_t* count) {
+  if (!h || !count) return TOPO_E_BAD_INPUT;
+  void* p; size_t es;
+  return array_info(const_cast<topo_handle*>(h), which, level, &p, count, &es);
+}
+
+int topo_put_array(topo_handle* h, int which, int level, const void* src, size_t count) {
+  if (!h || !src) return TOPO_E_BAD_INPUT;
+  void* p; size_t n, es;
+  int rc = array_info(h, which, level, &p, &n, &es);
+  if (rc != TOPO_OK) return fail(h, rc, "bad array id/level %d/%d", which, level);
+  if (count != n) return fail(h, TOPO_E_BAD_INPUT, "array %d expects %zu elements, got %zu", which, n, count);
+  if (which == TOPO_VMASK || which == TOPO_EACTIVE || which == TOPO_KE || which == TOPO_STENCIL ||
+      which == TOPO_KELEM || which == TOPO_RHOP)
+    return fail(h, TOPO_E_BAD_INPUT, "array %d is read-only", which);
+  CK(cudaMemcpyAsync(p, src, n * es, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (which == TOPO_RHO) { h->rhop_stale = true; h->ops_ready = false; }
+  return TOPO_OK;
+}
+
+int topo_get_array(topo_handle* h, int which, int level, void* dst, size_t count) {
+  if (!h || !dst) return TOPO_E_BAD_INPUT;
+  void* p; size_t n, es;
+  int rc = array_info(h, which, level, &p, &n, &es);
+  if (rc != TOPO_OK) return fail(h, rc, "bad array id/level %d/%d", which, level);
+  if (count != n) return fail(h, TOPO_E_BAD_INPUT, "array %d has %zu elements, asked %zu", which, n, count);
+  if (which == TOPO_RHOP) RET(update_penalised_if_stale(h));
+  CK(cudaMemcpyAsync(dst, p, n * es, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return TOPO_OK;
+}
+
+int topo_device_ptr(topo_handle* h, int which, int level, void** dptr) {
+  if (!h || !dptr) return TOPO_E_BAD_INPUT;
+  size_t n, es;
+  return array_info(h, which, level, dptr, &n, &es);
+}
+
+int topo_coeff_to_density(topo_handle* h) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set (call topo_set_spline)");
+  const DevLevel& L = h->lv[0];
+  launch_coeff_to_density(h->stream, L.d, L.eactive, h->sd, h->coeff, h->cfg.min_density,
+                          h->cfg.power_penalty, h->rho, h->rhop, h->rhop32);
+  count_launch();
+  CKL();
+  h->rhop_stale = false;
+  h->ops_ready = false;
+  return TOPO_OK;
+}
+
+int topo_set_operator_precision(topo_handle* h, int mask) {
+  if (!h || mask < 1 || mask > 3) return TOPO_E_BAD_INPUT;
+  h->op_precision = mask;
+  h->ops_ready = false;
+  return TOPO_OK;
+}
+
+int topo_update_operators(topo_handle* h) {
+  RET(check_ready(h, false));
+  RET(update_penalised_if_stale(h));
+  const int nl = (int)h->lv.size();
+  const bool b64 = (h->op_precision & 1) != 0, b32 = (h->op_precision & 2) != 0;
+  for (int l = 1; l < nl; ++l) {
+    DevLevel& C = h->lv[l];
+    DevLevel& Fl = h->lv[l - 1];
+    if (l == 1) {
+      launch_galerkin_first_impl(h->stream, Fl.d, C.d, h->rhop, Fl.eactive, Fl.vmask, h->dT64, h->dT32,
+                                 h->dKe, h->gal_fixed, h->n_gal_fixed, b64 ? C.kel : nullptr,
+                                 b32 ? C.kel32 : nullptr);
+      count_launch((b64 ? 2 : 0) + (b32 ? 2 : 0));
+    } else {
+      if (b64) launch_galerkin_dyadic_t<double>(h->stream, Fl.d, C.d, Fl.eactive, Fl.kel, C.kel);
+      if (b32) launch_galerkin_dyadic_t<float>(h->stream, Fl.d, C.d, Fl.eactive, Fl.kel32, C.kel32);
+      count_launch((b64 ? 1 : 0) + (b32 ? 1 : 0));
+    }
+    if (b64) launch_assemble_stencil_t<double>(h->stream, C.d, C.eactive, C.vmask, C.kel, C.stencil);
+    if (b32) launch_assemble_stencil_t<float>(h->stream, C.d, C.eactive, C.vmask, C.kel32, C.stencil32);
+    count_launch((b64 ? 1 : 0) + (b32 ? 1 : 0));
+    CKL();
+  }
+  if (nl > 1) {
+    DevLevel& Lc = h->lv.back();
+    const double* st = Lc.stencil;
+    if (!b64) {  // FP64 copy of the FP32 coarsest stencil
+      CK(cudaMemsetAsync(h->coarse64tmp, 0, sizeof(double) * 243 * Lc.d.nv, h->stream));
+      launch_f2d_add(h->stream, Lc.stencil32, h->coarse64tmp, 243 * Lc.d.nv);
+      count_launch();
+      st = h->coarse64tmp;
+    }
+    launch_dense_from_stencil(h->stream, Lc.d, st, h->A);
+    count_launch(2);
+    CKL();
+    int e = coarsest_invert(h->stream, h->ndense, h->A, nullptr, h->status);
+    count_launch();
+    if (e != (int)cudaSuccess)
+      return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    int hstat[2] = {0, 0};
+    CK(cudaMemcpyAsync(hstat, h->status, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (hstat[1] != 0) return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", hstat[1] - 1);
+    h->coarse_dropped = hstat[0];
+    launch_to_float(h->stream, h->A, h->A32, (int64_t)h->ndense * h->ndense);
+    count_launch();
+    CKL();
+  }
+  for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
+  h->ops64 = b64;
+  h->ops32 = b32;
+  h->ops_ready = true;
+  return TOPO_OK;
+}
+
+int topo_apply_fine(topo_handle* h, int precision) {
+  RET(check_ready(h, false));
+  RET(update_penalised_if_stale(h));
+  DevLevel& L = h->lv[0];
+  const int64_t n3 = 3 * L.d.nv;
+  if (precision == 0) {
+    level_apply<double>(h, 0, h->work, nullptr, L.R, false);
+  } else if (precision == 2) {  // dense-row FP64 kernel (cross-check of the modal kernel)
+    launch_fine_apply_dense<double>(h->stream, L.d, h->rhop, L.vmask, h->work, nullptr, L.R, false);
+    count_launch();
+  } else {
+    launch_d2f(h->stream, h->work, h->x32, n3);
+    level_apply<float>(h, 0, h->x32, nullptr, h->r32, false);
+    CK(cudaMemsetAsync(L.R, 0, sizeof(double) * n3, h->stream));
+    launch_f2d_add(h->stream, h->r32, L.R, n3);
+    count_launch(2);
+  }
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_residual(topo_handle* h, int level) {
+  RET(check_ready(h, level > 0));
+  if (level < 0 || level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
+  RET(update_penalised_if_stale(h));
+  level_residual<double>(h, level);
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_smooth(topo_handle* h, int level, int sweeps, int reverse) {
+  RET(check_ready(h, level > 0));
+  if (level < 0 || level >= (int)h->lv.size() || sweeps < 0) return TOPO_E_BAD_INPUT;
+  RET(update_penalised_if_stale(h));
+  gs_level<double>(h, level, sweeps, reverse != 0);
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_restrict(topo_handle* h, int coarse_level) {
+  if (!h || coarse_level < 1 || coarse_level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
+  restrict_T<double>(h, coarse_level);
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_prolong(topo_handle* h, int fine_level) {
+  if (!h || fine_level < 0 || fine_level >= (int)h->lv.size() - 1) return TOPO_E_BAD_INPUT;
+  prolong_T<double>(h, fine_level);
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_coarsest_solve(topo_handle* h) {
+  RET(check_ready(h, true));
+  if (h->lv.size() < 2) return TOPO_E_STATE;
+  coarsest_solve_T<double>(h);
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_vcycle(topo_handle* h, int pre, int post, double* relres) {
+  RET(check_ready(h, true));
+  if (!h->ops64) return fail(h, TOPO_E_STATE, "FP64 operators not built");
+  ChebParams cp;
+  vcycle_core<double>(h, pre, post, false, TOPO_SMOOTH_GS, cp);
+  level_residual<double>(h, 0);
+  DevLevel& L = h->lv[0];
+  const int64_t n3 = 3 * L.d.nv;
+  launch_dot<double>(h->stream, L.R, L.R, n3, h->partial, h->sc + S_RR);
+  launch_dot<double>(h->stream, L.F, L.F, n3, h->partial, h->sc + S_FF);
+  count_launch(4);
+  CKL();
+  RET(read_scalars(h, S_RR, 2));
+  if (relres) *relres = std::sqrt(h->hsc[S_RR]) / std::sqrt(h->hsc[S_FF]);
+  return TOPO_OK;
+}
+
+int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats) {
+  RET(check_ready(h, true));
+  if (!o || o->rtol <= 0 || o->max_iter < 0 || o->pre < 0 || o->post < 0) return TOPO_E_BAD_INPUT;
+  DevLevel& L0 = h->lv[0];
+  const int64_t n3 = 3 * L0.d.nv;
+  ChebParams cp;
+  if (o->cheb_degree > 0) cp.degree = o->cheb_degree;
+  if (o->cheb_lo > 0) cp.lo = o->cheb_lo;
+  if (o->cheb_hi > 0) cp.hi = o->cheb_hi;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, h->stream));
+  topo_solve_stats st{};
+  // ||F||
+  launch_dot<double>(h->stream, L0.F, L0.F, n3, h->partial, h->sc + S_FF);
+  count_launch(2);
+  RET(read_scalars(h, S_FF, 1));
+  const double fn = std::sqrt(h->hsc[S_FF]);
+  int rc = TOPO_OK;
+  if (fn == 0.0) {
+    CK(cudaMemsetAsync(L0.U, 0, sizeof(double) * n3, h->stream));
+    st.relres = 0.0;
+  } else if (o->mode == TOPO_SOLVE_VCYCLE) {
+    if (!h->ops64) return fail(h, TOPO_E_STATE, "FP64 operators not built");
+    RET(prepare_smoother<double>(h, o->smoother));
+    double rr = 1.0;
+    int it = 0;
+    while (rr > o->rtol && it < o->max_iter) {
+      vcycle_core<double>(h, o->pre, o->post, false, o->smoother, cp);
+      level_residual<double>(h, 0);
+      launch_dot<double>(h->stream, L0.R, L0.R, n3, h->partial, h->sc + S_RR);
+      count_launch(2);
+      CKL();
+      RET(read_scalars(h, S_RR, 1));
+      rr = std::sqrt(h->hsc[S_RR]) / fn;
+      if (!std::isfinite(rr)) return fail(h, TOPO_E_NONFINITE, "V-cycle residual non-finite");
+      ++it;
+    }
+    st.iterations = it;
+    st.vcycles = it;
+    st.relres = rr;
+  } else if (o->mode == TOPO_SOLVE_PCG64) {
+    if (!h->ops64) return fail(h, TOPO_E_STATE, "FP64 operators not built");
+    RET(prepare_smoother<double>(h, o->smoother));
+    CK(cudaMemcpyAsync(h->x, L0.U, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->f, L0.F, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    int it = 0;
+    double rel = 0;
+    int nvc = 0;
+    auto prec = [&](const double* r, double* z) -> int {
+      (void)z;  // z is level-0 U, where the V-cycle works
+      ++nvc;
+      return vcycle_prec<double>(h, r, o->pre, o->post, o->smoother, cp);
+    };
+    rc = fcg_T<double>(h, h->x, h->f, h->r, h->d, h->q, h->rold, L0.U, o->rtol, o->max_iter, 0, prec,
+                       &it, &rel, fn);
+    // restore level-0 state: F = f, U = x
+    CK(cudaMemcpyAsync(L0.F, h->f, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(L0.U, h->x, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    if (rc != TOPO_OK) return rc;
+    st.iterations = it;
+    st.vcycles = nvc;
+  } else if (o->mode == TOPO_SOLVE_MIXED) {
+    // FP64 flexible CG (FP64 fine matvec, dot products and step lengths) whose
+    // preconditioner is an FP32 multigrid solve: one FP32 V-cycle, or up to
+    // inner_max FP32 FCG iterations to a relative reduction of inner_rtol.
+    if (!h->ops32) return fail(h, TOPO_E_STATE, "FP32 operators not built");
+    RET(prepare_smoother<float>(h, o->smoother));
+    CK(cudaMemcpyAsync(h->x, L0.U, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->f, L0.F, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-1;
+    const int inner_max = o->inner_max > 0 ? o->inner_max : 1;
+    float* b32 = reinterpret_cast<float*>(h->work);
+    int it = 0, nvc = 0;
+    double rel = 0;
+    auto prec32 = [&](const float* r, float* z) -> int {
+      (void)z;
+      ++nvc;
+      return vcycle_prec<float>(h, r, o->pre, o->post, o->smoother, cp);
+    };
+    auto prec = [&](const double* r, double* z) -> int {
+      if (inner_max <= 1) {
+        launch_d2f(h->stream, r, L0.F32, n3);
+        CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3, h->stream));
+        ++nvc;
+        vcycle_core<float>(h, o->pre, o->post, true, o->smoother, cp);
+        k_to_double<float><<<nb256(n3), 256, 0, h->stream>>>(n3, L0.U32, z);
+        count_launch(2);
+        return TOPO_OK;
+      }
+      launch_d2f(h->stream, r, b32, n3);
+      CK(cudaMemsetAsync(h->x32, 0, sizeof(float) * n3, h->stream));
+      count_launch();
+      int iit = 0;
+      double irel = 0;
+      // relative to ||r|| (FP64 norm of the outer residual)
+      RET(read_scalars(h, S_RR, 1));
+      const double rnorm = std::sqrt(h->hsc[S_RR]);
+      RET(fcg_T<float>(h, h->x32, b32, h->r32, h->d32, h->q32, h->rold32, L0.U32, inner_rtol, inner_max,
+                       8, prec32, &iit, &irel, rnorm > 0 ? rnorm : 1.0));
+      k_to_double<float><<<nb256(n3), 256, 0, h->stream>>>(n3, h->x32, z);
+      count_launch();
+      return TOPO_OK;
+    };
+    rc = fcg_T<double>(h, h->x, h->f, h->r, h->d, h->q, h->rold, L0.U, o->rtol, o->max_iter, 0, prec,
+                       &it, &rel, fn);
+    CK(cudaMemcpyAsync(L0.F, h->f, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(L0.U, h->x, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    if (rc != TOPO_OK) return rc;
+    st.iterations = it;
+    st.vcycles = nvc;
+  } else {
+    return fail(h, TOPO_E_BAD_INPUT, "unknown solve mode %d", o->mode);
+  }
+  if (o->mode != TOPO_SOLVE_VCYCLE && fn != 0.0) {
+    // true FP64 residual of the final iterate
+    level_residual<double>(h, 0);
+    launch_dot<double>(h->stream, L0.R, L0.R, n3, h->partial, h->sc + S_RR);
+    count_launch(2);
+    RET(read_scalars(h, S_RR, 1));
+    st.relres = std::sqrt(h->hsc[S_RR]) / fn;
+  }
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  st.ms = ms;
+  if (stats) *stats = st;
+  CKL();
+  if (st.relres > o->rtol) return fail(h, TOPO_E_NOT_CONVERGED, "relative residual %.3e above %.3e after %d iterations", st.relres, o->rtol, st.iterations);
+  return TOPO_OK;
+}
+
+int topo_compliance(topo_handle* h, double* c) {
+  if (!h || !c) return TOPO_E_BAD_INPUT;
+  DevLevel& L = h->lv[0];
+  launch_dot<double>(h->stream, L.F, L.U, 3 * L.d.nv, h->partial, h->sc + S_TMP);
+  count_launch(2);
+  CKL();
+  RET(read_scalars(h, S_TMP, 1));
+  *c = h->hsc[S_TMP];
+  return TOPO_OK;
+}
+
+int topo_volume(topo_handle* h, int refden, double* v) {
+  if (!h || !v) return TOPO_E_BAD_INPUT;
+  launch_sum(h->stream, h->rho, h->lv[0].d.ne, h->partial, h->sc + S_TMP);
+  count_launch(2);
+  CKL();
+  RET(read_scalars(h, S_TMP, 1));
+  *v = h->hsc[S_TMP] / (double)(refden ? h->gs_padded_elements : h->active_elements);
+  return TOPO_OK;
+}
+
+int topo_sensitivity(topo_handle* h) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  const DevLevel& L = h->lv[0];
+  launch_sensitivity(h->stream, L.d, L.eactive, h->rho, L.U, h->cfg.power_penalty, h->lam, h->mu,
+                     h->cfg.h, h->sens);
+  count_launch();
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_filter(topo_handle* h, double radius) {
+  if (!h || !(radius > 0)) return TOPO_E_BAD_INPUT;
+  if (radius > 16.0) return fail(h, TOPO_E_BAD_INPUT, "filter radius %.3g above 16 elements", radius);
+  const DevLevel& L = h->lv[0];
+  if (radius != h->filt_radius) {
+    std::vector<int4> offs;
+    std::vector<double> w;
+    filter_table(radius, offs, w);
+    if (h->filt_offs) { cudaFree(h->filt_offs); h->filt_offs = nullptr; }
+    if (h->filt_w) { cudaFree(h->filt_w); h->filt_w = nullptr; }
+    CK(cudaMalloc((void**)&h->filt_offs, sizeof(int4) * offs.size()));
+    CK(cudaMalloc((void**)&h->filt_w, sizeof(double) * w.size()));
+    CK(cudaMemcpyAsync(h->filt_offs, offs.data(), sizeof(int4) * offs.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->filt_w, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->filt_n = (int)offs.size();
+    h->filt_radius = radius;
+  }
+  CK(cudaMemcpyAsync(h->sens_tmp, h->sens, sizeof(double) * L.d.ne, cudaMemcpyDeviceToDevice, h->stream));
+  launch_filter(h->stream, L.d, L.eactive, h->sens_tmp, h->sens, h->filt_offs, h->filt_w, h->filt_n);
+  count_launch();
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_spline_adjoint(topo_handle* h) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");
+  const DevLevel& L = h->lv[0];
+  launch_spline_adjoint(h->stream, L.d, L.eactive, h->sd, h->sens, h->csens, h->adj1, h->adj2);
+  count_launch(3);
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) {
+  if (!h || !o) return TOPO_E_BAD_INPUT;
+  if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");
+  const DevLevel& L = h->lv[0];
+  const int64_t nc = (int64_t)h->sd.nb[0] * h->sd.nb[1] * h->sd.nb[2];
+  const double den = (double)(o->reference_volume ? h->gs_padded_elements : h->active_elements);
+  launch_maxabs(h->stream, h->csens, nc, h->partial, h->sc + S_TMP);
+  count_launch(2);
+  RET(read_scalars(h, S_TMP, 1));
+  const double gmax = h->hsc[S_TMP];
+  CK(cudaMemcpyAsync(h->coeff_old, h->coeff, sizeof(double) * nc, cudaMemcpyDeviceToDevice, h->stream));
+  double lo = 0.0, hi = gmax, thres = 0.5 * (lo + hi), V = 0.0;
+  int itn = 0, trials = 0;
+  do {
+    thres = 0.5 * (lo + hi);
+    launch_oc_trial(h->stream, nc, h->coeff_old, h->csens, thres, o->damp, o->step, o->cmin, o->cmax, h->coeff);
+    launch_trial_volume(h->stream, L.d, L.eactive, h->sd, h->coeff, h->cfg.min_density, h->partial,
+                        h->sc + S_TMP);
+    count_launch(3);
+    CKL();
+    RET(read_scalars(h, S_TMP, 1));
+    V = h->hsc[S_TMP] / den;
+    ++trials;
+    if (V > o->vgoal) lo = thres;
+    else if (V < o->vgoal) hi = thres;
+  } while (std::fabs(V - o->vgoal) > 1e-4 && itn++ < 30);
+  if (o->apply_twice) {
+    launch_oc_trial(h->stream, nc, h->coeff, h->csens, thres, o->damp, o->step, o->cmin, o->cmax, h->coeff_tmp);
+    CK(cudaMemcpyAsync(h->coeff, h->coeff_tmp, sizeof(double) * nc, cudaMemcpyDeviceToDevice, h->stream));
+    count_launch();
+  }
+  RET(topo_coeff_to_density(h));
+  if (stats) {
+    stats->trials = trials;
+    stats->lambda = thres;
+    double v = 0;
+    RET(topo_volume(h, o->reference_volume, &v));
+    stats->volume = v;
+  }
+  return TOPO_OK;
+}
+
+static int gs_maps_impl(topo_handle* h, const LevelDims& d, const std::vector<uint8_t>& va,
+                        const std::vector<uint8_t>& ea, int* vidmap, size_t nvid, int* eidmap,
+                        size_t neid, int* gs_num8, int* n_gsvertices, int* n_gselements) {
+  int64_t nvs[8] = {0}, nes[8] = {0}, nva = 0, nea = 0;
+  for (int z = 0; z < d.vz; ++z)
+    for (int y = 0; y < d.vy; ++y)
+      for (int x = 0; x < d.vx; ++x)
+        if (va[x + (int64_t)d.vx * (y + (int64_t)d.vy * z)] & 8) { nvs[(x & 1) + 2 * (y & 1) + 4 * (z & 1)]++; ++nva; }
+  for (int z = 0; z < d.ez; ++z)
+    for (int y = 0; y < d.ey; ++y)
+      for (int x = 0; x < d.ex; ++x)
+        if (ea[x + (int64_t)d.ex * (y + (int64_t)d.ey * z)]) { nes[(x & 1) + 2 * (y & 1) + 4 * (z & 1)]++; ++nea; }
+  if ((vidmap && nvid != (size_t)nva) || (eidmap && neid != (size_t)nea))
+    return fail(h, TOPO_E_BAD_INPUT, "gs map sizes: need %lld vertices, %lld elements", (long long)nva, (long long)nea);
+  int64_t voff[8], eoff[8], vt = 0, et = 0;
+  for (int c = 0; c < 8; ++c) {
+    voff[c] = vt; eoff[c] = et;
+    const int64_t pv = (nvs[c] + 31) / 32 * 32, pe = (nes[c] + 31) / 32 * 32;
+    if (gs_num8) gs_num8[c] = (int)pv;
+    vt += pv; et += pe;
+  }
+  int64_t cv[8] = {0}, ce[8] = {0}, k = 0;
+  if (vidmap)
+    for (int z = 0; z < d.vz; ++z)
+      for (int y = 0; y < d.vy; ++y)
+        for (int x = 0; x < d.vx; ++x)
+          if (va[x + (int64_t)d.vx * (y + (int64_t)d.vy * z)] & 8) {
+            const int c = (x & 1) + 2 * (y & 1) + 4 * (z & 1);
+            vidmap[k++] = (int)(voff[c] + cv[c]++);
+          }
+  k = 0;
+  if (eidmap)
+    for (int z = 0; z < d.ez; ++z)
+      for (int y = 0; y < d.ey; ++y)
+        for (int x = 0; x < d.ex; ++x)
+          if (ea[x + (int64_t)d.ex * (y + (int64_t)d.ey * z)]) {
+            const int c = (x & 1) + 2 * (y & 1) + 4 * (z & 1);
+            eidmap[k++] = (int)(eoff[c] + ce[c]++);
+          }
+  if (n_gsvertices) *n_gsvertices = (int)vt;
+  if (n_gselements) *n_gselements = (int)et;
+  return TOPO_OK;
+}
+
+int topo_gs_maps(topo_handle* h, int level, int* vidmap, size_t nvid, int* eidmap, size_t neid,
+                 int* gs_num8, int* n_gsvertices, int* n_gselements) {
+  if (!h || level < 0 || level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
+  return gs_maps_impl(h, h->lv[level].d, h->H.vactive[level], h->H.eactive[level], vidmap, nvid,
+                      eidmap, neid, gs_num8, n_gsvertices, n_gselements);
+}
+
+int topo_plan_gs_maps(int nx, int ny, int nz, const uint8_t* eactive, int max_coarse, int level,
+                      int* vidmap, size_t nvid, int* eidmap, size_t neid, int* gs_num8,
+                      int* n_gsvertices, int* n_gselements) {
+  if (nx < 1 || ny < 1 || nz < 1) return TOPO_E_BAD_INPUT;
+  Hierarchy H = build_hierarchy(nx, ny, nz, eactive, max_coarse > 0 ? max_coarse : 400);
+  if (level < 0 || level >= (int)H.dims.size()) return TOPO_E_BAD_INPUT;
+  return gs_maps_impl(nullptr, H.dims[level], H.vactive[level], H.eactive[level], vidmap, nvid, eidmap,
+                      neid, gs_num8, n_gsvertices, n_gselements);
+}
+
+int topo_element_template(double E, double nu, double h, double* Ke576) {
+  if (!Ke576 || !(h > 0) || !(nu > -1.0 && nu < 0.5)) return TOPO_E_BAD_INPUT;
+  element_template(E, nu, h, Ke576);
+  return TOPO_OK;
+}
+
+int topo_plan_levels(int nx, int ny, int nz, const uint8_t* eactive, int max_coarse, int max_levels,
+                     int* nlevels, int* dims, int* factors) {
+  if (nx < 1 || ny < 1 || nz < 1 || !nlevels) return TOPO_E_BAD_INPUT;
+  Hierarchy H = build_hierarchy(nx, ny, nz, eactive, max_coarse > 0 ? max_coarse : 400);
+  *nlevels = (int)H.dims.size();
+  for (int l = 0; l < (int)H.dims.size() && l < max_levels; ++l) {
+    if (dims) { dims[3 * l] = H.dims[l].ex; dims[3 * l + 1] = H.dims[l].ey; dims[3 * l + 2] = H.dims[l].ez; }
+    if (factors) factors[l] = H.dims[l].factor;
+  }
+  return TOPO_OK;
+}
+
+int topo_spline_axis(int order, int partition, double bmin, double bmax, int nelem, double h,
+                     double* knots, int* i0, double* N) {
+  if (order < 2 || order > 4 || partition < 0 || nelem < 1 || !(bmax > bmin) || !(h > 0)) return TOPO_E_BAD_INPUT;
+  SplineTables t;
+  int part3[3] = {partition, partition, partition};
+  double a3[3] = {bmin, bmin, bmin}, b3[3] = {bmax, bmax, bmax};
+  int ne3[3] = {nelem, 1, 1};
+  spline_tables(order, part3, a3, b3, ne3, h, t);
+  if (knots) std::copy(t.knots[0].begin(), t.knots[0].end(), knots);
+  if (i0) std::copy(t.i0[0].begin(), t.i0[0].end(), i0);
+  if (N) std::copy(t.N[0].begin(), t.N[0].end(), N);
+  return TOPO_OK;
+}
+
+int topo_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return TOPO_E_BAD_INPUT;
+  cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocDefault);
+  return e == cudaSuccess ? TOPO_OK : TOPO_E_NOMEM;
+}
+
+int topo_host_free(void* ptr) {
+  return cudaFreeHost(ptr) == cudaSuccess ? TOPO_OK : TOPO_E_CUDA;
+}
+
+int topo_timer_start(topo_handle* h) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (!h->timer_ev[0]) {
+    CK(cudaEventCreate(&h->timer_ev[0]));
+    CK(cudaEventCreate(&h->timer_ev[1]));
+  }
+  CK(cudaEventRecord(h->timer_ev[0], h->stream));
+  return TOPO_OK;
+}
+
+int topo_timer_stop(topo_handle* h, double* ms) {
+  if (!h || !ms || !h->timer_ev[0]) return TOPO_E_BAD_INPUT;
+  CK(cudaEventRecord(h->timer_ev[1], h->stream));
+  CK(cudaEventSynchronize(h->timer_ev[1]));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, h->timer_ev[0], h->timer_ev[1]));
+  *ms = t;
+  return TOPO_OK;
+}
+
+int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* stats) {
+  if (!h || !o) return TOPO_E_BAD_INPUT;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, h->stream));
+  topo_iter_stats st{};
+  RET(topo_update_operators(h));
+  int rc = topo_solve(h, &o->solve, &st.solve);
+  if (rc != TOPO_OK && rc != TOPO_E_NOT_CONVERGED) return rc;
+  RET(topo_compliance(h, &st.compliance));
+  if (!std::isfinite(st.compliance)) return fail(h, TOPO_E_NONFINITE, "compliance is not finite");
+  RET(topo_sensitivity(h));
+  RET(topo_filter(h, o->filter_radius > 0 ? o->filter_radius : 2.0));
+  RET(topo_spline_adjoint(h));
+  topo_oc_stats oc{};
+  RET(topo_oc_update(h, &o->oc, &oc));
+  st.oc_trials = oc.trials;
+  st.volume = oc.volume;
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  st.ms = ms;
+  if (stats) *stats = st;
+  return rc;
+}
+
+int topo_profile_enable(topo_handle* h, int enable) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  h->prof = enable != 0;
+  return TOPO_OK;
+}
+
+int topo_profile_read(topo_handle* h, int family, int* launches, double* ms) {
+  if (!h || family < 0 || family >= TOPO_K_COUNT) return TOPO_E_BAD_INPUT;
+  CK(cudaStreamSynchronize(h->stream));
+  double tot = 0;
+  for (auto& p : h->evs[family]) {
+    float t = 0;
+    cudaEventElapsedTime(&t, p.a, p.b);
+    tot += t;
+    h->evpool.push_back(p);
+  }
+  if (launches) *launches = (int)h->evs[family].size();
+  if (ms) *ms = tot;
+  h->evs[family].clear();
+  return TOPO_OK;
+}
+
+int topo_launch_count(const topo_handle* h, long long* n) {
+  (void)h;
+  if (!n) return TOPO_E_BAD_INPUT;
+  *n = g_launches.load();
+  return TOPO_OK;
+}
+
+}  // extern "C"

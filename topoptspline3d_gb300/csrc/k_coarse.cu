@@ -1,0 +1,688 @@
+// Coarse-level kernels: 27-point 3x3-block stencil apply / Gauss-Seidel,
+// trilinear transfers, Galerkin coarse operators and the coarsest dense solve.
+#include <cooperative_groups.h>
+
+#include "topo_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace topo {
+
+static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// ---------------------------------------------------------------------------
+// Stencil apply: y_v = sum_d S(v,d) u_{v+d}  (grid/Grid.cu:2126-2224 residual form).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void stencil_row(const LevelDims& d, const T* __restrict__ st,
+                                            const T* __restrict__ u, int x, int y, int z, int64_t v,
+                                            T o[3]) {
+  o[0] = o[1] = o[2] = T(0);
+  const int64_t nv = d.nv;
+#pragma unroll
+  for (int k = 0; k < 27; ++k) {
+    const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
+    if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) continue;
+    const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
+    const T u0 = u[n], u1 = u[nv + n], u2 = u[2 * nv + n];
+    const T* s = st + (int64_t)(k * 9) * nv + v;
+    o[0] += s[0] * u0 + s[nv] * u1 + s[2 * nv] * u2;
+    o[1] += s[3 * nv] * u0 + s[4 * nv] * u1 + s[5 * nv] * u2;
+    o[2] += s[6 * nv] * u0 + s[7 * nv] * u1 + s[8 * nv] * u2;
+  }
+}
+
+template <typename T>
+__global__ void k_stencil_apply(LevelDims d, const T* __restrict__ st, const T* __restrict__ u,
+                                const T* __restrict__ f, T* __restrict__ out, bool residual) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.nv) return;
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  T o[3];
+  stencil_row<T>(d, st, u, x, y, z, v, o);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int64_t i = c * d.nv + v;
+    out[i] = residual ? f[i] - o[c] : o[c];
+  }
+}
+
+template <typename T>
+__global__ void k_stencil_gs(LevelDims d, const T* __restrict__ st, const uint8_t* __restrict__ vmask,
+                             T* u, const T* __restrict__ f, int cx, int cy, int cz, int hx, int hy,
+                             int64_t cnt, bool reverse) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  const int x = cx + 2 * (int)(t % hx);
+  const int64_t t2 = t / hx;
+  const int y = cy + 2 * (int)(t2 % hy), z = cz + 2 * (int)(t2 / hy);
+  const int64_t v = x + (int64_t)d.vx * (y + (int64_t)d.vy * z);
+  if (!(vmask[v] & 8)) return;
+  T o[3], S[9], r[3];
+  stencil_row<T>(d, st, u, x, y, z, v, o);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) S[k] = st[(int64_t)(13 * 9 + k) * d.nv + v];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) r[c] = f[c * d.nv + v] - o[c];
+  T du[3] = {T(0), T(0), T(0)};
+  if (!reverse) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      T s = r[i];
+#pragma unroll
+      for (int j = 0; j < i; ++j) s -= S[3 * i + j] * du[j];
+      du[i] = s / S[4 * i];
+    }
+  } else {
+#pragma unroll
+    for (int i = 2; i >= 0; --i) {
+      T s = r[i];
+#pragma unroll
+      for (int j = i + 1; j < 3; ++j) s -= S[3 * i + j] * du[j];
+      du[i] = s / S[4 * i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) u[i * d.nv + v] += du[i];
+}
+
+template <typename T>
+__global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st,
+                                   const uint8_t* __restrict__ vmask, T* __restrict__ dinv) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.nv) return;
+  T S[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) S[k] = st[(int64_t)(13 * 9 + k) * d.nv + v];
+  const T a = S[0], b = S[1], c = S[2], dd = S[4], e = S[5], f = S[8];
+  const T A0 = dd * f - e * e, A1 = c * e - b * f, A2 = b * e - c * dd;
+  const T det = a * A0 + b * A1 + c * A2;
+  const T inv[9] = {A0, A1, A2, A1, a * f - c * c, b * c - a * e, A2, b * c - a * e, a * dd - b * b};
+  const T rd = T(1) / det;
+  const bool act = (vmask[v] & 8) != 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) dinv[k * d.nv + v] = act ? inv[k] * rd : T(0);
+}
+
+// One Chebyshev step on a stencil level: uout = u + d, d = c_old d + c_new Dinv (f - A u).
+template <typename T>
+__global__ void k_stencil_cheb(LevelDims d, const T* __restrict__ st, const T* __restrict__ u,
+                               const T* __restrict__ f, T* __restrict__ uout, const T* __restrict__ dinv,
+                               T* __restrict__ dv, T c_old, T c_new, bool first) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.nv) return;
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  T o[3];
+  stencil_row<T>(d, st, u, x, y, z, v, o);
+  const int64_t nv = d.nv;
+  const T r0 = f[v] - o[0], r1 = f[nv + v] - o[1], r2 = f[2 * nv + v] - o[2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const T zz = dinv[(3 * c) * nv + v] * r0 + dinv[(3 * c + 1) * nv + v] * r1 + dinv[(3 * c + 2) * nv + v] * r2;
+    const T dn = first ? c_new * zz : c_old * dv[c * nv + v] + c_new * zz;
+    dv[c * nv + v] = dn;
+    uout[c * nv + v] = u[c * nv + v] + dn;
+  }
+}
+
+template <typename T>
+void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
+                          T* out, bool residual) {
+  k_stencil_apply<T><<<nblk(d.nv, 128), 128, 0, s>>>(d, st, u, f, out, residual);
+}
+
+template <typename T>
+void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
+                         const T* dinv, T* dvec, double c_old, double c_new, bool first) {
+  k_stencil_cheb<T><<<nblk(d.nv, 128), 128, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old, (T)c_new, first);
+}
+
+template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,
+                                          const double*, double*, const double*, double*, double, double, bool);
+template void launch_stencil_cheb<float>(cudaStream_t, const LevelDims&, const float*, const float*,
+                                         const float*, float*, const float*, float*, double, double, bool);
+
+template <typename T>
+void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask, T* u,
+                       const T* f, int colour, bool reverse) {
+  const int cx = colour & 1, cy = (colour >> 1) & 1, cz = colour >> 2;
+  const int hx = (d.vx - cx + 1) / 2, hy = (d.vy - cy + 1) / 2, hz = (d.vz - cz + 1) / 2;
+  const int64_t cnt = (int64_t)hx * hy * hz;
+  if (cnt <= 0) return;
+  k_stencil_gs<T><<<nblk(cnt, 128), 128, 0, s>>>(d, st, vmask, u, f, cx, cy, cz, hx, hy, cnt, reverse);
+}
+
+template <typename T>
+void launch_stencil_diag_inv(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask,
+                             T* dinv) {
+  k_stencil_diag_inv<T><<<nblk(d.nv, 256), 256, 0, s>>>(d, st, vmask, dinv);
+}
+
+// ---------------------------------------------------------------------------
+// Transfers.  Prolongation is trilinear interpolation from the coarse element
+// corners, masked on fixed fine DOFs; restriction is its exact transpose
+// (factor 4: grid/Grid.cu:2509-2570 and 2635-2671; factor 2: 2456-2507, 2594-2632).
+// ---------------------------------------------------------------------------
+template <typename T, int FCT>
+__global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf, T* __restrict__ fc) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= cd.nv) return;
+  const int x = (int)(v % cd.vx);
+  const int64_t t = v / cd.vx;
+  const int y = (int)(t % cd.vy), z = (int)(t / cd.vy);
+  T s0 = T(0), s1 = T(0), s2 = T(0);
+  const T inv = T(1) / T(FCT * FCT * FCT);
+  for (int dz = -(FCT - 1); dz <= FCT - 1; ++dz) {
+    const int fz = z * FCT + dz;
+    if (fz < 0 || fz >= fd.vz) continue;
+    const int wz = FCT - (dz < 0 ? -dz : dz);
+    for (int dy = -(FCT - 1); dy <= FCT - 1; ++dy) {
+      const int fy = y * FCT + dy;
+      if (fy < 0 || fy >= fd.vy) continue;
+      const int wyz = wz * (FCT - (dy < 0 ? -dy : dy));
+#pragma unroll
+      for (int dx = -(FCT - 1); dx <= FCT - 1; ++dx) {
+        const int fx = x * FCT + dx;
+        if (fx < 0 || fx >= fd.vx) continue;
+        const T w = T(wyz * (FCT - (dx < 0 ? -dx : dx))) * inv;
+        const int64_t fv = fx + (int64_t)fd.vx * (fy + (int64_t)fd.vy * fz);
+        s0 += w * rf[fv];
+        s1 += w * rf[fd.nv + fv];
+        s2 += w * rf[2 * fd.nv + fv];
+      }
+    }
+  }
+  fc[v] = s0; fc[cd.nv + v] = s1; fc[2 * cd.nv + v] = s2;
+}
+
+template <typename T, int FCT>
+__global__ void k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc, T* __restrict__ uf,
+                          const uint8_t* __restrict__ vmask) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= fd.nv) return;
+  const int x = (int)(v % fd.vx);
+  const int64_t t = v / fd.vx;
+  const int y = (int)(t % fd.vy), z = (int)(t / fd.vy);
+  const uint8_t m = vmask[v];
+  if (!(m & 7) || !(m & 8)) return;
+  const int cx = x / FCT, cy = y / FCT, cz = z / FCT;
+  const int rx = x % FCT, ry = y % FCT, rz = z % FCT;
+  T s0 = T(0), s1 = T(0), s2 = T(0);
+  const T inv = T(1) / T(FCT * FCT * FCT);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+    const int wx = ox ? rx : FCT - rx, wy = oy ? ry : FCT - ry, wz = oz ? rz : FCT - rz;
+    const int wi = wx * wy * wz;
+    if (wi == 0) continue;
+    const T w = T(wi) * inv;
+    const int64_t cv = (cx + ox) + (int64_t)cd.vx * ((cy + oy) + (int64_t)cd.vy * (cz + oz));
+    s0 += w * uc[cv];
+    s1 += w * uc[cd.nv + cv];
+    s2 += w * uc[2 * cd.nv + cv];
+  }
+  if (m & 1) uf[v] += s0;
+  if (m & 2) uf[fd.nv + v] += s1;
+  if (m & 4) uf[2 * fd.nv + v] += s2;
+}
+
+template <typename T>
+void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
+                     T* fc) {
+  if (coarse.factor == 4)
+    k_restrict<T, 4><<<nblk(coarse.nv, 128), 128, 0, s>>>(fine, coarse, rf, fc);
+  else
+    k_restrict<T, 2><<<nblk(coarse.nv, 128), 128, 0, s>>>(fine, coarse, rf, fc);
+}
+
+template <typename T>
+void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* uc,
+                    T* uf, const uint8_t* vmask_fine) {
+  if (coarse.factor == 4)
+    k_prolong<T, 4><<<nblk(fine.nv, 256), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
+  else
+    k_prolong<T, 2><<<nblk(fine.nv, 256), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin, first coarse level (grid/Grid.cu:1111-1225 restated per element):
+// K_E = sum_pos rho^p_pos T_pos over fine elements without fixed DOFs (a
+// [N_E x 64] x [64 x 300] product over the symmetric entries), plus the exact
+// Q^T Ktilde Q of fine elements that touch fixed DOFs, where Ktilde has the
+// fixed rows/columns zeroed and 1e6 on their diagonal (grid/Grid.cu:1196-1207).
+// ---------------------------------------------------------------------------
+constexpr int GAL_CE = 16;    // coarse elements per CTA
+constexpr int GAL_THREADS = 320;
+
+template <typename T, int FCT>
+__global__ void __launch_bounds__(GAL_THREADS) k_galerkin_gemm(LevelDims fd, LevelDims cd,
+                                                               const double* __restrict__ rhop,
+                                                               const uint8_t* __restrict__ vmask,
+                                                               const T* __restrict__ Ttab,
+                                                               T* __restrict__ kel) {
+  constexpr int NPOS = FCT * FCT * FCT;
+  __shared__ T rp[GAL_CE][NPOS];
+  const int64_t ce0 = (int64_t)blockIdx.x * GAL_CE;
+  for (int i = threadIdx.x; i < GAL_CE * NPOS; i += blockDim.x) {
+    const int k = i / NPOS, pos = i % NPOS;
+    const int64_t ce = ce0 + k;
+    T val = T(0);
+    if (ce < cd.ne) {
+      const int cx = (int)(ce % cd.ex);
+      const int64_t t = ce / cd.ex;
+      const int cy = (int)(t % cd.ey), cz = (int)(t / cd.ey);
+      const int fx = cx * FCT + pos % FCT, fy = cy * FCT + pos / FCT % FCT, fz = cz * FCT + pos / (FCT * FCT);
+      if (fx < fd.ex && fy < fd.ey && fz < fd.ez) {
+        const int64_t fe = fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz);
+        bool fixed = false;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          const int64_t vv = (fx + (a & 1)) + (int64_t)fd.vx * ((fy + ((a >> 1) & 1)) + (int64_t)fd.vy * (fz + (a >> 2)));
+          const uint8_t m = vmask[vv];
+          fixed |= (m & 7) != 7;
+        }
+        val = fixed ? T(0) : T(rhop[fe]);
+      }
+    }
+    rp[k][pos] = val;
+  }
+  __syncthreads();
+  const int ent = threadIdx.x;
+  if (ent >= 300) return;
+  // upper-triangle index -> (i, j), i <= j
+  int i = 0, rem = ent;
+  while (rem >= 24 - i) { rem -= 24 - i; ++i; }
+  const int j = i + rem;
+  T acc[GAL_CE];
+#pragma unroll
+  for (int k = 0; k < GAL_CE; ++k) acc[k] = T(0);
+  for (int pos = 0; pos < NPOS; ++pos) {
+    const T tv = Ttab[pos * 576 + i * 24 + j];
+#pragma unroll
+    for (int k = 0; k < GAL_CE; ++k) acc[k] += rp[k][pos] * tv;
+  }
+#pragma unroll
+  for (int k = 0; k < GAL_CE; ++k) {
+    const int64_t ce = ce0 + k;
+    if (ce >= cd.ne) break;
+    kel[ce * 576 + i * 24 + j] = acc[k];
+    kel[ce * 576 + j * 24 + i] = acc[k];
+  }
+}
+
+// Fixed-DOF fine elements: K_E += Q^T Ktilde_e Q, one CTA per coarse element,
+// one thread per entry; fine elements are visited in a fixed order.
+template <typename T, int FCT>
+__global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims cd,
+                                                        const double* __restrict__ rhop,
+                                                        const uint8_t* __restrict__ eactive,
+                                                        const uint8_t* __restrict__ vmask,
+                                                        const double* __restrict__ Ke,
+                                                        const int* __restrict__ list,
+                                                        T* __restrict__ kel) {
+  __shared__ double sK[576];
+  __shared__ double sQ[8][8];
+  __shared__ uint8_t sfree[24];
+  __shared__ int sflag;
+  const int64_t ce = list[blockIdx.x];
+  const int cx = (int)(ce % cd.ex);
+  const int64_t t = ce / cd.ex;
+  const int cy = (int)(t % cd.ey), cz = (int)(t / cd.ey);
+  const int ent = threadIdx.x;
+  const int R = ent / 24, S = ent % 24;
+  const int A = R / 3, i = R % 3, B = S / 3, j = S % 3;
+  double acc = 0.0;
+  for (int pos = 0; pos < FCT * FCT * FCT; ++pos) {
+    const int px = pos % FCT, py = pos / FCT % FCT, pz = pos / (FCT * FCT);
+    const int fx = cx * FCT + px, fy = cy * FCT + py, fz = cz * FCT + pz;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int flag = 0;
+      if (fx < fd.ex && fy < fd.ey && fz < fd.ez &&
+          eactive[fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz)]) {
+        for (int a = 0; a < 8; ++a) {
+          const int64_t vv = (fx + (a & 1)) + (int64_t)fd.vx * ((fy + ((a >> 1) & 1)) + (int64_t)fd.vy * (fz + (a >> 2)));
+          const uint8_t m = vmask[vv];
+          for (int c = 0; c < 3; ++c) sfree[3 * a + c] = (m >> c) & 1;
+          if ((m & 7) != 7) flag = 1;
+        }
+      }
+      sflag = flag;
+    }
+    __syncthreads();
+    if (!sflag) continue;
+    const double pe = rhop[fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz)];
+    {
+      const int r = ent / 24, s2 = ent % 24;
+      double k = pe * Ke[ent];
+      if (!sfree[r] || !sfree[s2]) k = (r == s2) ? 1e6 : 0.0;
+      sK[ent] = k;
+    }
+    if (ent < 64) {
+      const int a = ent / 8, C = ent % 8;
+      const int q[3] = {px + (a & 1), py + ((a >> 1) & 1), pz + (a >> 2)};
+      const int cc[3] = {C & 1, (C >> 1) & 1, C >> 2};
+      double w = 1.0;
+      for (int k = 0; k < 3; ++k) w *= cc[k] ? (double)q[k] / FCT : (double)(FCT - q[k]) / FCT;
+      sQ[a][C] = w;
+    }
+    __syncthreads();
+    double s = 0.0;
+    for (int a = 0; a < 8; ++a) {
+      const double qa = sQ[a][A];
+      if (qa == 0.0) continue;
+      double inner = 0.0;
+      for (int b = 0; b < 8; ++b) inner += sK[(3 * a + i) * 24 + 3 * b + j] * sQ[b][B];
+      s += qa * inner;
+    }
+    acc += s;
+  }
+  if (acc != 0.0) kel[ce * 576 + ent] += T(acc);
+}
+
+// Dyadic Galerkin: K_E = sum_children Q_c^T K_child Q_c (grid/Grid.cu:839-896 in
+// element form).  One CTA per coarse element, two-stage product per child.
+template <typename T>
+__global__ void __launch_bounds__(576) k_galerkin_dyadic(LevelDims fd, LevelDims cd,
+                                                         const uint8_t* __restrict__ eactive_f,
+                                                         const T* __restrict__ kel_f,
+                                                         T* __restrict__ kel_c) {
+  __shared__ T sK[576];
+  __shared__ T sT[576];
+  __shared__ T sQ[8][8];
+  const int64_t ce = blockIdx.x;
+  const int cx = (int)(ce % cd.ex);
+  const int64_t t = ce / cd.ex;
+  const int cy = (int)(t % cd.ey), cz = (int)(t / cd.ey);
+  const int ent = threadIdx.x;
+  const int R = ent / 24, S = ent % 24;
+  T acc = T(0);
+  for (int c = 0; c < 8; ++c) {
+    const int ox = c & 1, oy = (c >> 1) & 1, oz = c >> 2;
+    const int fx = 2 * cx + ox, fy = 2 * cy + oy, fz = 2 * cz + oz;
+    const bool on = fx < fd.ex && fy < fd.ey && fz < fd.ez &&
+                    eactive_f[fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz)];
+    if (!on) continue;  // uniform across the CTA
+    const int64_t fe = fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz);
+    __syncthreads();
+    sK[ent] = kel_f[fe * 576 + ent];
+    if (ent < 64) {
+      const int a = ent / 8, C = ent % 8;
+      const int q[3] = {ox + (a & 1), oy + ((a >> 1) & 1), oz + (a >> 2)};
+      const int cc[3] = {C & 1, (C >> 1) & 1, C >> 2};
+      T w = T(1);
+      for (int k = 0; k < 3; ++k) w *= cc[k] ? T(q[k]) / T(2) : T(2 - q[k]) / T(2);
+      sQ[a][C] = w;
+    }
+    __syncthreads();
+    {  // stage 1: sT[r][3C+jj] = sum_b K[r][3b+jj] Q[b][C]
+      const int r = ent / 24, col = ent % 24, C = col / 3, jj = col % 3;
+      T s = T(0);
+#pragma unroll
+      for (int b = 0; b < 8; ++b) s += sK[r * 24 + 3 * b + jj] * sQ[b][C];
+      sT[ent] = s;
+    }
+    __syncthreads();
+    {  // stage 2: acc[(A,i),S] += sum_a Q[a][A] T[3a+i][S]
+      const int A = R / 3, i = R % 3;
+      T s = T(0);
+#pragma unroll
+      for (int a = 0; a < 8; ++a) s += sQ[a][A] * sT[(3 * a + i) * 24 + S];
+      acc += s;
+    }
+  }
+  kel_c[ce * 576 + ent] = acc;
+}
+
+// Stencil assembly from element matrices: thread per (neighbour d, vertex v).
+template <typename T>
+__global__ void k_assemble_stencil(LevelDims d, const uint8_t* __restrict__ eactive,
+                                   const uint8_t* __restrict__ vmask, const T* __restrict__ kel,
+                                   T* __restrict__ st) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= 27 * d.nv) return;
+  const int k = (int)(gid / d.nv);
+  const int64_t v = gid % d.nv;
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  const int dx = k % 3 - 1, dy = k / 3 % 3 - 1, dz = k / 9 - 1;
+  T blk[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) blk[q] = T(0);
+  // elements containing both v and v+(dx,dy,dz)
+  for (int ez = z - 1; ez <= z; ++ez) {
+    if (ez < 0 || ez >= d.ez) continue;
+    const int az = z - ez, bz = az + dz;
+    if (bz < 0 || bz > 1) continue;
+    for (int ey = y - 1; ey <= y; ++ey) {
+      if (ey < 0 || ey >= d.ey) continue;
+      const int ay = y - ey, by = ay + dy;
+      if (by < 0 || by > 1) continue;
+      for (int ex = x - 1; ex <= x; ++ex) {
+        if (ex < 0 || ex >= d.ex) continue;
+        const int ax = x - ex, bx = ax + dx;
+        if (bx < 0 || bx > 1) continue;
+        const int64_t e = ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez);
+        if (!eactive[e]) continue;
+        const int a = ax + 2 * ay + 4 * az, b = bx + 2 * by + 4 * bz;
+        const T* K = kel + e * 576;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) blk[3 * i + j] += K[(3 * a + i) * 24 + 3 * b + j];
+      }
+    }
+  }
+  if (k == 13 && !(vmask[v] & 8)) {
+    blk[0] = T(1); blk[4] = T(1); blk[8] = T(1);
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) st[(int64_t)(k * 9 + q) * d.nv + v] = blk[q];
+}
+
+__global__ void k_dense_from_stencil(LevelDims d, const double* __restrict__ st,
+                                     double* __restrict__ A) {
+  const int64_t n = 3 * d.nv;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= 243 * d.nv) return;
+  const int q = (int)(gid / d.nv);  // k*9 + 3i + j
+  const int64_t v = gid % d.nv;
+  const int k = q / 9, i = (q % 9) / 3, j = q % 3;
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
+  if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) return;
+  const int64_t nb = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
+  A[(3 * v + i) * n + 3 * nb + j] = st[(int64_t)q * d.nv + v];
+}
+
+__global__ void k_symmetrize(int n, double* A) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (int64_t)n * n) return;
+  const int i = (int)(gid / n), j = (int)(gid % n);
+  if (j >= i) return;
+  const double s = 0.5 * (A[(int64_t)i * n + j] + A[(int64_t)j * n + i]);
+  A[(int64_t)i * n + j] = s;
+  A[(int64_t)j * n + i] = s;
+}
+
+// In-place Gauss-Jordan inverse of a symmetric positive (semi-)definite matrix
+// (no pivoting needed), one cooperative launch; two grid barriers per pivot.
+// A pivot below 1e-10 of the largest diagonal entry belongs to a null
+// direction (a floating part of the domain): its row and column are dropped,
+// which gives the inverse of the remaining DOFs, as the reference's
+// pseudo-inverse does for its coarsest system (grid/Grid.cpp:3657, 4072).
+// status[0] counts dropped pivots; a clearly negative pivot sets status[1] = k+1
+// and every block stops at the same step (all threads read the same pivot).
+__global__ void k_gauss_jordan(int n, double* A, int* status) {
+  cg::grid_group grid = cg::this_grid();
+  const int64_t nn = (int64_t)n * n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t tid0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double dmax = 0.0;
+  for (int k = 0; k < n; ++k) dmax = fmax(dmax, fabs(A[(int64_t)k * n + k]));
+  const double tol = 1e-10 * dmax;
+  for (int k = 0; k < n; ++k) {
+    const double p = A[(int64_t)k * n + k];
+    if (p < -tol) {
+      if (tid0 == 0) status[1] = k + 1;
+      return;
+    }
+    if (p <= tol) {  // drop DOF k
+      for (int64_t g = tid0; g < 2 * (int64_t)n; g += stride) {
+        if (g < n) A[(int64_t)k * n + g] = 0.0;
+        else A[(g - n) * n + k] = 0.0;
+      }
+      if (tid0 == 0) status[0] += 1;
+      grid.sync();
+      continue;
+    }
+    const double rp = 1.0 / p;
+    for (int64_t g = tid0; g < nn; g += stride) {
+      const int i = (int)(g / n), j = (int)(g % n);
+      if (i == k || j == k) continue;
+      A[g] -= A[(int64_t)i * n + k] * A[(int64_t)k * n + j] * rp;
+    }
+    grid.sync();
+    for (int64_t g = tid0; g < 2 * (int64_t)n; g += stride) {
+      if (g < n) {
+        const int j = (int)g;
+        if (j != k) A[(int64_t)k * n + j] *= rp;
+        else A[(int64_t)k * n + k] = rp;
+      } else {
+        const int i = (int)(g - n);
+        if (i != k) A[(int64_t)i * n + k] *= -rp;
+      }
+    }
+    grid.sync();
+  }
+}
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+// u_soa = Ainv * f_soa over the dense DOF ordering 3v+c; one warp per row.
+template <typename T>
+__global__ void k_dense_gemv(int n, const T* __restrict__ Ainv, const T* __restrict__ f, T* __restrict__ u,
+                             int64_t nv) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  T s = T(0);
+  for (int j = lane; j < n; j += 32) s += Ainv[(int64_t)warp * n + j] * f[(j % 3) * nv + j / 3];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) u[(warp % 3) * nv + warp / 3] = s;
+}
+
+void launch_galerkin_first_impl(cudaStream_t s, const LevelDims& fd, const LevelDims& cd,
+                                const double* rhop, const uint8_t* eactive_f, const uint8_t* vmask_f,
+                                const double* Ttab64, const float* Ttab32, const double* Ke,
+                                const int* fixed_list, int nfixed, double* kel, float* kel32) {
+  const unsigned g = nblk(cd.ne, GAL_CE);
+  const unsigned nf = (unsigned)nfixed;
+  if (cd.factor == 4) {
+    if (kel) {
+      k_galerkin_gemm<double, 4><<<g, GAL_THREADS, 0, s>>>(fd, cd, rhop, vmask_f, Ttab64, kel);
+      if (nf) k_galerkin_fixed<double, 4><<<nf, 576, 0, s>>>(fd, cd, rhop, eactive_f, vmask_f, Ke, fixed_list, kel);
+    }
+    if (kel32) {
+      k_galerkin_gemm<float, 4><<<g, GAL_THREADS, 0, s>>>(fd, cd, rhop, vmask_f, Ttab32, kel32);
+      if (nf) k_galerkin_fixed<float, 4><<<nf, 576, 0, s>>>(fd, cd, rhop, eactive_f, vmask_f, Ke, fixed_list, kel32);
+    }
+  } else {
+    if (kel) {
+      k_galerkin_gemm<double, 2><<<g, GAL_THREADS, 0, s>>>(fd, cd, rhop, vmask_f, Ttab64, kel);
+      if (nf) k_galerkin_fixed<double, 2><<<nf, 576, 0, s>>>(fd, cd, rhop, eactive_f, vmask_f, Ke, fixed_list, kel);
+    }
+    if (kel32) {
+      k_galerkin_gemm<float, 2><<<g, GAL_THREADS, 0, s>>>(fd, cd, rhop, vmask_f, Ttab32, kel32);
+      if (nf) k_galerkin_fixed<float, 2><<<nf, 576, 0, s>>>(fd, cd, rhop, eactive_f, vmask_f, Ke, fixed_list, kel32);
+    }
+  }
+}
+
+template <typename T>
+void launch_galerkin_dyadic_t(cudaStream_t s, const LevelDims& fd, const LevelDims& cd,
+                              const uint8_t* eactive_f, const T* kel_f, T* kel_c) {
+  k_galerkin_dyadic<T><<<(unsigned)cd.ne, 576, 0, s>>>(fd, cd, eactive_f, kel_f, kel_c);
+}
+
+template <typename T>
+void launch_assemble_stencil_t(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                               const uint8_t* vmask, const T* kel, T* st) {
+  k_assemble_stencil<T><<<nblk(27 * d.nv, 256), 256, 0, s>>>(d, eactive, vmask, kel, st);
+}
+
+void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double* st, double* A) {
+  const int64_t n = 3 * d.nv;
+  cudaMemsetAsync(A, 0, sizeof(double) * n * n, s);
+  k_dense_from_stencil<<<nblk(243 * d.nv, 256), 256, 0, s>>>(d, st, A);
+  k_symmetrize<<<nblk(n * n, 256), 256, 0, s>>>((int)n, A);
+}
+
+int coarsest_invert(cudaStream_t s, int n, double* A, double* /*work*/, int* status_dev) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 256;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gauss_jordan, threads, 0);
+  if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
+  int64_t want = ((int64_t)n * n + threads - 1) / threads;
+  int blocks = (int)std::min<int64_t>(want, (int64_t)nsm * std::min(per_sm, 2));
+  if (blocks < 1) blocks = 1;
+  cudaMemsetAsync(status_dev, 0, 2 * sizeof(int), s);
+  void* args[] = {&n, &A, &status_dev};
+  return (int)cudaLaunchCooperativeKernel((void*)k_gauss_jordan, dim3(blocks), dim3(threads), args,
+                                          0, s);
+}
+
+void launch_to_float(cudaStream_t s, const double* a, float* b, int64_t n) {
+  k_to_float<<<nblk(n, 256), 256, 0, s>>>(a, b, n);
+}
+
+template <typename T>
+void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv) {
+  k_dense_gemv<T><<<nblk((int64_t)n * 32, 256), 256, 0, s>>>(n, Ainv, f_soa, u_soa, nv);
+}
+
+template void launch_stencil_apply<double>(cudaStream_t, const LevelDims&, const double*, const double*,
+                                           const double*, double*, bool);
+template void launch_stencil_apply<float>(cudaStream_t, const LevelDims&, const float*, const float*,
+                                          const float*, float*, bool);
+template void launch_stencil_gs<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
+                                        double*, const double*, int, bool);
+template void launch_stencil_gs<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
+                                       float*, const float*, int, bool);
+template void launch_stencil_diag_inv<double>(cudaStream_t, const LevelDims&, const double*,
+                                              const uint8_t*, double*);
+template void launch_stencil_diag_inv<float>(cudaStream_t, const LevelDims&, const float*,
+                                             const uint8_t*, float*);
+template void launch_restrict<double>(cudaStream_t, const LevelDims&, const LevelDims&, const double*,
+                                      double*);
+template void launch_restrict<float>(cudaStream_t, const LevelDims&, const LevelDims&, const float*,
+                                     float*);
+template void launch_prolong<double>(cudaStream_t, const LevelDims&, const LevelDims&, const double*,
+                                     double*, const uint8_t*);
+template void launch_prolong<float>(cudaStream_t, const LevelDims&, const LevelDims&, const float*,
+                                    float*, const uint8_t*);
+template void launch_galerkin_dyadic_t<double>(cudaStream_t, const LevelDims&, const LevelDims&,
+                                               const uint8_t*, const double*, double*);
+template void launch_galerkin_dyadic_t<float>(cudaStream_t, const LevelDims&, const LevelDims&,
+                                              const uint8_t*, const float*, float*);
+template void launch_assemble_stencil_t<double>(cudaStream_t, const LevelDims&, const uint8_t*,
+                                                const uint8_t*, const double*, double*);
+template void launch_assemble_stencil_t<float>(cudaStream_t, const LevelDims&, const uint8_t*,
+                                               const uint8_t*, const float*, float*);
+template void launch_dense_gemv<double>(cudaStream_t, int, const double*, const double*, double*,
+                                        int64_t);
+template void launch_dense_gemv<float>(cudaStream_t, int, const float*, const float*, float*, int64_t);
+
+}  // namespace topo

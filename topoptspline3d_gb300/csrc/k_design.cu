@@ -1,0 +1,341 @@
+// Design-chain kernels: B-spline density, element sensitivity, sensitivity
+// filter, spline adjoint and the OC coefficient trial.
+#include <cmath>
+#include <cstring>
+
+#include "topo_internal.h"
+
+namespace topo {
+
+static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+constexpr int MAX_ORDER = 4;
+
+// Spline value at element (x,y,z): sum over order^3 taps of c * Nx Ny Nz, or the
+// reference's out-of-range value -0.2 (grid/Grid.cu:3396-3430).
+__device__ __forceinline__ double spline_at(const SplineDev& sp, const double* __restrict__ coeff,
+                                            int x, int y, int z) {
+  const int ix = sp.i0[0][x], iy = sp.i0[1][y], iz = sp.i0[2][z];
+  if (ix < 0 || iy < 0 || iz < 0) return -0.2;
+  const int k = sp.order;
+  double val = 0.0;
+  for (int r = 0; r < k; ++r) {
+    const double nr = sp.N[0][x * k + r];
+    for (int s = 0; s < k; ++s) {
+      const double ns = sp.N[1][y * k + s];
+      for (int t = 0; t < k; ++t) {
+        const int64_t idx = (ix + r) + (int64_t)sp.nb[0] * ((iy + s) + (int64_t)sp.nb[1] * (iz + t));
+        val += coeff[idx] * nr * ns * sp.N[2][z * k + t];
+      }
+    }
+  }
+  return val;
+}
+
+__global__ void k_coeff_to_density(LevelDims d, const uint8_t* __restrict__ eactive, SplineDev sp,
+                                   const double* __restrict__ coeff, double rho_min, double penal,
+                                   double* __restrict__ rho, double* __restrict__ rhop,
+                                   float* __restrict__ rhop32) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  const int x = (int)(e % d.ex);
+  const int64_t t = e / d.ex;
+  const int y = (int)(t % d.ey), z = (int)(t / d.ey);
+  if (!eactive[e]) {
+    rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
+    return;
+  }
+  const double v = fmin(fmax(spline_at(sp, coeff, x, y, z), rho_min), 1.0);
+  const double vp = pow(v, penal);
+  rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
+}
+
+constexpr int VOL_THREADS = 256;
+
+__global__ void __launch_bounds__(VOL_THREADS) k_trial_volume(LevelDims d, const uint8_t* __restrict__ eactive,
+                                                              SplineDev sp, const double* __restrict__ coeff,
+                                                              double rho_min, double* __restrict__ partial) {
+  double s = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < d.ne; e += (int64_t)gridDim.x * blockDim.x) {
+    if (!eactive[e]) continue;
+    const int x = (int)(e % d.ex);
+    const int64_t t = e / d.ex;
+    const int y = (int)(t % d.ey), z = (int)(t / d.ey);
+    s += fmin(fmax(spline_at(sp, coeff, x, y, z), rho_min), 1.0);
+  }
+  __shared__ double ws[VOL_THREADS / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < VOL_THREADS / 32; ++w) r += ws[w];
+    partial[blockIdx.x] = r;
+  }
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partial[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                             const SplineDev& sp, const double* coeff, double rho_min, double penal,
+                             double* rho, double* rhop, float* rhop32) {
+  k_coeff_to_density<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, coeff, rho_min, penal, rho, rhop,
+                                                     rhop32);
+}
+
+void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                         const SplineDev& sp, const double* coeff, double rho_min, double* partial,
+                         double* out) {
+  int nb = (int)std::min<int64_t>(1024, (d.ne + VOL_THREADS * 4 - 1) / (VOL_THREADS * 4));
+  if (nb < 1) nb = 1;
+  k_trial_volume<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, coeff, rho_min, partial);
+  k_sum_partials<<<1, 256, 0, s>>>(partial, nb, out);
+}
+
+// Element sensitivity g_e = -p rho^(p-1) u_e^T Ke u_e (optimization/optimization.cu:96-159),
+// with u_e^T Ke u_e evaluated in the sum-factorised modal form: Walsh-Hadamard
+// coefficients of the nodal values, the displacement gradient split over the
+// orthogonal functions {1, X, Y, Z, YZ, XZ, XY} of the reference cube, and the
+// isotropic energy of each part weighted by the function's L2 norm.
+__device__ __forceinline__ void hadamard8(double v[8]) {
+#pragma unroll
+  for (int h = 1; h < 8; h <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (!(i & h)) {
+        const double a = v[i], b = v[i | h];
+        v[i] = a + b;
+        v[i | h] = b - a;
+      }
+}
+
+__device__ __forceinline__ double energy_part(const double G[3][3], double lam, double mu) {
+  const double tr = G[0][0] + G[1][1] + G[2][2];
+  double ee = G[0][0] * G[0][0] + G[1][1] * G[1][1] + G[2][2] * G[2][2];
+  const double e01 = 0.5 * (G[0][1] + G[1][0]), e02 = 0.5 * (G[0][2] + G[2][0]),
+               e12 = 0.5 * (G[1][2] + G[2][1]);
+  ee += 2.0 * (e01 * e01 + e02 * e02 + e12 * e12);
+  return 0.5 * lam * tr * tr + mu * ee;
+}
+
+__global__ void k_sensitivity(LevelDims d, const uint8_t* __restrict__ eactive,
+                              const double* __restrict__ rho, const double* __restrict__ u,
+                              double penal, double lam, double mu, double h, double* __restrict__ sens) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  if (!eactive[e]) { sens[e] = 0.0; return; }
+  const int x = (int)(e % d.ex);
+  const int64_t t = e / d.ex;
+  const int y = (int)(t % d.ey), z = (int)(t / d.ey);
+  // c[i][S]: modal coefficient of component i for mode S (bit0 x, bit1 y, bit2 z),
+  // with sign convention H[a][S] = prod_{k in S} (2 a_k - 1); scaled by 2/h * 1/8.
+  double c[3][8];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int64_t v = (x + (a & 1)) + (int64_t)d.vx * ((y + ((a >> 1) & 1)) + (int64_t)d.vy * (z + (a >> 2)));
+      c[i][a] = u[i * d.nv + v];
+    }
+    hadamard8(c[i]);
+  }
+  const double sc = 2.0 / h / 8.0;
+  double tot = 0.0;
+#pragma unroll
+  for (int f = 0; f < 7; ++f) {
+    double G[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        G[i][j] = ((f >> j) & 1) ? 0.0 : sc * c[i][f | (1 << j)];
+    const int nbits = (f & 1) + ((f >> 1) & 1) + ((f >> 2) & 1);
+    const double nf = nbits == 0 ? 8.0 : (nbits == 1 ? 8.0 / 3.0 : 8.0 / 9.0);
+    tot += nf * energy_part(G, lam, mu);
+  }
+  const double hh = 0.5 * h;
+  const double q = 2.0 * hh * hh * hh * tot;  // u_e^T Ke u_e
+  sens[e] = -penal * pow(rho[e], penal - 1.0) * q;
+}
+
+void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                        const double* rho, const double* u, double penal, double lam, double mu,
+                        double h, double* sens) {
+  k_sensitivity<<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, rho, u, penal, lam, mu, h, sens);
+}
+
+// Sensitivity filter (grid/Grid.cu:4130-4229): normalised average over the ball
+// r^2 <= R^2, R_int = floor(R + 0.5), weight 1 - 6s^2 + 8s^3 - 3s^4 with s = r/R.
+// The ball's offsets and weights depend only on R; they come precomputed (in the
+// reference's loop order dx, dy, dz) so no square root is taken per neighbour.
+__global__ void k_filter(LevelDims d, const uint8_t* __restrict__ eactive, const double* __restrict__ src,
+                         double* __restrict__ dst, const int4* __restrict__ offs,
+                         const double* __restrict__ wts, int noffs) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  if (!eactive[e]) { dst[e] = 0.0; return; }
+  const int x = (int)(e % d.ex);
+  const int64_t t = e / d.ex;
+  const int y = (int)(t % d.ey), z = (int)(t / d.ey);
+  double ws = 0.0, gs = 0.0;
+  for (int k = 0; k < noffs; ++k) {
+    const int4 o = offs[k];
+    const int nx = x + o.x, ny = y + o.y, nz = z + o.z;
+    if (nx < 0 || ny < 0 || nz < 0 || nx >= d.ex || ny >= d.ey || nz >= d.ez) continue;
+    const int64_t n = nx + (int64_t)d.ex * (ny + (int64_t)d.ey * nz);
+    if (!eactive[n]) continue;
+    const double w = wts[k];
+    gs += w * src[n];
+    ws += w;
+  }
+  dst[e] = gs / ws;
+}
+
+void launch_filter(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* src,
+                   double* dst, const int4* offs, const double* wts, int noffs) {
+  k_filter<<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, src, dst, offs, wts, noffs);
+}
+
+// Ball offsets within r^2 <= R^2, R_int = floor(R + 0.5), weight
+// 1 - 6s^2 + 8s^3 - 3s^4 with s = r/R (grid/Grid.cu:4156-4209, 4226-4229).
+void filter_table(double R, std::vector<int4>& offs, std::vector<double>& w) {
+  const int Ri = (int)(R + 0.5);
+  const double R2 = R * R;
+  offs.clear();
+  w.clear();
+  for (int dx = -Ri; dx <= Ri; ++dx)
+    for (int dy = -Ri; dy <= Ri; ++dy)
+      for (int dz = -Ri; dz <= Ri; ++dz) {
+        const double r2 = (double)(dx * dx + dy * dy + dz * dz);
+        if (r2 > R2) continue;
+        const double sv = std::sqrt(r2 / R2), s2 = sv * sv;
+        w.push_back(1.0 - 6.0 * s2 + 8.0 * s2 * sv - 3.0 * s2 * s2);
+        offs.push_back(make_int4(dx, dy, dz, 0));
+      }
+}
+
+// Spline adjoint (grid/Grid.cu:3671-3724) as a deterministic separable gather:
+// T1[i][y][z] = sum_x g Nx, T2[i][j][z] = sum_y T1 Ny, dc[i][j][k] = sum_z T2 Nz.
+// Elements outside the spline range (any axis) and inactive elements contribute 0.
+__global__ void k_adj_x(LevelDims d, const uint8_t* __restrict__ eactive, SplineDev sp,
+                        const double* __restrict__ g, double* __restrict__ T1) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nbx = sp.nb[0];
+  if (gid >= (int64_t)nbx * d.ey * d.ez) return;
+  const int i = (int)(gid % nbx);
+  const int64_t yz = gid / nbx;
+  const int y = (int)(yz % d.ey), z = (int)(yz / d.ey);
+  double s = 0.0;
+  if (sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0) {
+    const int k = sp.order;
+    for (int x = sp.lo[0][i]; x < sp.hi[0][i]; ++x) {
+      const int ix = sp.i0[0][x];
+      if (ix < 0) continue;
+      const int r = i - ix;
+      if (r < 0 || r >= k) continue;
+      const int64_t e = x + (int64_t)d.ex * (y + (int64_t)d.ey * z);
+      if (!eactive[e]) continue;
+      s += g[e] * sp.N[0][x * k + r];
+    }
+  }
+  T1[gid] = s;  // layout [z][y][i]
+}
+
+__global__ void k_adj_y(LevelDims d, SplineDev sp, const double* __restrict__ T1, double* __restrict__ T2) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nbx = sp.nb[0], nby = sp.nb[1];
+  if (gid >= (int64_t)nbx * nby * d.ez) return;
+  const int i = (int)(gid % nbx);
+  const int64_t t = gid / nbx;
+  const int j = (int)(t % nby), z = (int)(t / nby);
+  const int k = sp.order;
+  double s = 0.0;
+  for (int y = sp.lo[1][j]; y < sp.hi[1][j]; ++y) {
+    const int iy = sp.i0[1][y];
+    if (iy < 0) continue;
+    const int r = j - iy;
+    if (r < 0 || r >= k) continue;
+    s += T1[i + (int64_t)nbx * (y + (int64_t)d.ey * z)] * sp.N[1][y * k + r];
+  }
+  T2[gid] = s;  // layout [z][j][i]
+}
+
+__global__ void k_adj_z(LevelDims d, SplineDev sp, const double* __restrict__ T2, double* __restrict__ dc) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nbx = sp.nb[0], nby = sp.nb[1], nbz = sp.nb[2];
+  if (gid >= (int64_t)nbx * nby * nbz) return;
+  const int i = (int)(gid % nbx);
+  const int64_t t = gid / nbx;
+  const int j = (int)(t % nby), kk = (int)(t / nby);
+  const int k = sp.order;
+  double s = 0.0;
+  for (int z = sp.lo[2][kk]; z < sp.hi[2][kk]; ++z) {
+    const int iz = sp.i0[2][z];
+    if (iz < 0) continue;
+    const int r = kk - iz;
+    if (r < 0 || r >= k) continue;
+    s += T2[i + (int64_t)nbx * (j + (int64_t)nby * z)] * sp.N[2][z * k + r];
+  }
+  dc[gid] = s;
+}
+
+void launch_spline_adjoint(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                           const SplineDev& sp, const double* sens, double* csens, double* tmp1,
+                           double* tmp2) {
+  const int64_t n1 = (int64_t)sp.nb[0] * d.ey * d.ez;
+  const int64_t n2 = (int64_t)sp.nb[0] * sp.nb[1] * d.ez;
+  const int64_t n3 = (int64_t)sp.nb[0] * sp.nb[1] * sp.nb[2];
+  k_adj_x<<<nblk(n1, 256), 256, 0, s>>>(d, eactive, sp, sens, tmp1);
+  k_adj_y<<<nblk(n2, 256), 256, 0, s>>>(d, sp, tmp1, tmp2);
+  k_adj_z<<<nblk(n3, 256), 256, 0, s>>>(d, sp, tmp2, csens);
+}
+
+__global__ void k_penalise(int64_t ne, const uint8_t* __restrict__ eactive, const double* __restrict__ rho,
+                           double penal, double* __restrict__ rhop, float* __restrict__ rhop32) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const double v = eactive[e] ? pow(rho[e], penal) : 0.0;
+  rhop[e] = v;
+  rhop32[e] = (float)v;
+}
+
+void launch_penalise(cudaStream_t s, int64_t ne, const uint8_t* eactive, const double* rho,
+                     double penal, double* rhop, float* rhop32) {
+  k_penalise<<<nblk(ne, 256), 256, 0, s>>>(ne, eactive, rho, penal, rhop, rhop32);
+}
+
+// OC trial on the coefficients (optimization/optimization.cu:559-587):
+// c' = clamp(clamp(c (max(-dc,0)/thres)^damp, c-step, c+step), cmin, cmax).
+__global__ void k_oc_trial(int64_t nc, const double* __restrict__ cold, const double* __restrict__ csens,
+                           double thres, double damp, double step, double cmin, double cmax,
+                           double* __restrict__ cnew) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  double g = csens[i];
+  if (g > 0) g = 0;
+  g = fabs(g);
+  const double co = cold[i];
+  double cn = co * pow(g / thres, damp);
+  cn = fmin(fmax(cn, co - step), co + step);
+  cn = fmin(fmax(cn, cmin), cmax);
+  cnew[i] = cn;
+}
+
+void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,
+                     double damp, double step, double cmin, double cmax, double* cnew) {
+  k_oc_trial<<<nblk(nc, 256), 256, 0, s>>>(nc, cold, csens, thres, damp, step, cmin, cmax, cnew);
+}
+
+}  // namespace topo

@@ -1,0 +1,510 @@
+// Fine-level (level 0) matrix-free elasticity kernels on the dense voxel grid.
+//
+// The operator is y = K(rho) u with K = sum_e rho_e^p Ke, Ke the 24x24 template
+// (element/templateMatrix.cpp:31-99).  Rows of fixed DOFs and inactive vertices
+// are zero; vectors are kept zero on fixed DOFs, which removes the fixed columns
+// exactly as the reference's WS kernels do (grid/Grid.cu:2277-2333, 1699-1842).
+#include "topo_internal.h"
+
+namespace topo {
+
+__constant__ double cKe64[576];
+__constant__ float cKe32[576];
+
+template <typename T>
+__device__ __forceinline__ T ke(int i);
+template <>
+__device__ __forceinline__ double ke<double>(int i) { return cKe64[i]; }
+template <>
+__device__ __forceinline__ float ke<float>(int i) { return cKe32[i]; }
+
+// Modal constants: lambda, mu, k0 = h/16, k1 = h/48, k2 = h/144 (see k_fine_modal).
+__constant__ double cModal64[5];
+__constant__ float cModal32[5];
+
+template <typename T>
+__device__ __forceinline__ T modal_c(int i);
+template <>
+__device__ __forceinline__ double modal_c<double>(int i) { return cModal64[i]; }
+template <>
+__device__ __forceinline__ float modal_c<float>(int i) { return cModal32[i]; }
+
+void upload_template(const double* Ke576, double lam, double mu, double h) {
+  float k32[576];
+  for (int i = 0; i < 576; ++i) k32[i] = (float)Ke576[i];
+  cudaMemcpyToSymbol(cKe64, Ke576, sizeof(double) * 576);
+  cudaMemcpyToSymbol(cKe32, k32, sizeof(float) * 576);
+  const double m64[5] = {lam, mu, h / 16.0, h / 48.0, h / 144.0};
+  const float m32[5] = {(float)m64[0], (float)m64[1], (float)m64[2], (float)m64[3], (float)m64[4]};
+  cudaMemcpyToSymbol(cModal64, m64, sizeof(m64));
+  cudaMemcpyToSymbol(cModal32, m32, sizeof(m32));
+}
+
+// ---------------------------------------------------------------------------
+// Sum-factorised ("modal") element operator.  The nodal values of one
+// displacement component are Walsh-Hadamard transformed (c_S = sum_a H[a][S] u_a,
+// H[a][S] = prod_{k in S} (2a_k - 1)), which splits the trilinear field into the
+// orthogonal functions {1, X, Y, Z, XY, XZ, YZ, XYZ} of the reference cube.  The
+// displacement gradient restricted to each orthogonal function gives one
+// isotropic stress, and the element forces are the transposed transform of the
+// modal forces.  The result equals rho^p Ke u_e (Ke integrated exactly, as the
+// 2x2x2 Gauss rule of element/templateMatrix.cpp:31-99 does) with about 240
+// flops per element instead of the 1152 of the dense 24x24 product.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void wht_fwd(T v[8]) {
+#pragma unroll
+  for (int hb = 1; hb < 8; hb <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (!(i & hb)) {
+        const T a = v[i], b = v[i | hb];
+        v[i] = a + b;
+        v[i | hb] = b - a;
+      }
+}
+
+template <typename T>
+__device__ __forceinline__ void wht_bwd(T v[8]) {
+#pragma unroll
+  for (int hb = 1; hb < 8; hb <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (!(i & hb)) {
+        const T a = v[i], b = v[i | hb];
+        v[i] = a - b;
+        v[i | hb] = a + b;
+      }
+}
+
+// In: c[3][8] nodal values per component.  Out: c[3][8] nodal forces of pe*Ke*u.
+template <typename T>
+__device__ __forceinline__ void modal_element(T c[3][8], T pe) {
+  wht_fwd<T>(c[0]); wht_fwd<T>(c[1]); wht_fwd<T>(c[2]);
+  const T L = modal_c<T>(0) * pe, M = modal_c<T>(1) * pe;
+  const T k0 = modal_c<T>(2), k1 = modal_c<T>(3), k2 = modal_c<T>(4);
+  T g[3][8];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) g[i][0] = T(0);
+  {  // constant part of the gradient
+    const T tr = c[0][1] + c[1][2] + c[2][4];
+    const T sxy = M * (c[0][2] + c[1][1]), sxz = M * (c[0][4] + c[2][1]), syz = M * (c[1][4] + c[2][2]);
+    g[0][1] = k0 * (L * tr + T(2) * M * c[0][1]);
+    g[1][2] = k0 * (L * tr + T(2) * M * c[1][2]);
+    g[2][4] = k0 * (L * tr + T(2) * M * c[2][4]);
+    g[0][2] = k0 * sxy; g[1][1] = k0 * sxy;
+    g[0][4] = k0 * sxz; g[2][1] = k0 * sxz;
+    g[1][4] = k0 * syz; g[2][2] = k0 * syz;
+  }
+  {  // X part (modes XY -> 3, XZ -> 5)
+    const T tr = c[1][3] + c[2][5];
+    const T syz = M * (c[1][5] + c[2][3]);
+    g[0][3] = k1 * M * c[0][3];
+    g[1][3] = k1 * (L * tr + T(2) * M * c[1][3]);
+    g[2][3] = k1 * syz;
+    g[0][5] = k1 * M * c[0][5];
+    g[1][5] = k1 * syz;
+    g[2][5] = k1 * (L * tr + T(2) * M * c[2][5]);
+  }
+  {  // Y part (XY -> 3, YZ -> 6)
+    const T tr = c[0][3] + c[2][6];
+    const T sxz = M * (c[0][6] + c[2][3]);
+    g[0][3] += k1 * (L * tr + T(2) * M * c[0][3]);
+    g[1][3] += k1 * M * c[1][3];
+    g[2][3] += k1 * sxz;
+    g[0][6] = k1 * sxz;
+    g[1][6] = k1 * M * c[1][6];
+    g[2][6] = k1 * (L * tr + T(2) * M * c[2][6]);
+  }
+  {  // Z part (XZ -> 5, YZ -> 6)
+    const T tr = c[0][5] + c[1][6];
+    const T sxy = M * (c[0][6] + c[1][5]);
+    g[0][5] += k1 * (L * tr + T(2) * M * c[0][5]);
+    g[1][5] += k1 * sxy;
+    g[2][5] += k1 * M * c[2][5];
+    g[0][6] += k1 * sxy;
+    g[1][6] += k1 * (L * tr + T(2) * M * c[1][6]);
+    g[2][6] += k1 * M * c[2][6];
+  }
+  {  // YZ, XZ, XY parts all act on the XYZ mode
+    const T kk = k2 * (L + T(4) * M);
+    g[0][7] = kk * c[0][7]; g[1][7] = kk * c[1][7]; g[2][7] = kk * c[2][7];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    wht_bwd<T>(g[i]);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) c[i][a] = g[i][a];
+  }
+}
+
+// y = K(rho) u (or f - K u) on level 0.  A CTA owns a (TXE-1) x (TYE-1) column of
+// vertices over TZ vertex planes and marches in z: per element layer it stages
+// the vertex plane above in shared memory (double buffered), computes the
+// TXE x TYE elements of the layer (one per thread) into shared memory, and each
+// owned vertex adds its four in-layer elements' bottom-node forces to the
+// top-node forces carried in registers from the layer below.
+// MODE 0: out = K u; 1: out = f - K u; 2: one Chebyshev step, r = f - K u,
+// z = Dinv r, d = c_old d + c_new z (first: c_new z), out = u + d (out != u).
+struct ChebArgs {
+  const void* dinv;  // [9][nv]
+  void* dvec;        // [3][nv]
+  double c_old, c_new;
+  int first;
+};
+
+template <typename T, int TXE, int TYE, int MODE>
+__global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* __restrict__ rhop,
+                                                         const uint8_t* __restrict__ vmask,
+                                                         const T* __restrict__ u, const T* __restrict__ f,
+                                                         T* __restrict__ out, int TZ, ChebArgs ch) {
+  constexpr int NT = TXE * TYE, PX = TXE + 1, PY = TYE + 1, NP = PX * PY;
+  extern __shared__ __align__(16) unsigned char modal_smem[];
+  T(*us)[3][NP] = reinterpret_cast<T(*)[3][NP]>(modal_smem);
+  T(*fe)[NT] = reinterpret_cast<T(*)[NT]>(modal_smem + sizeof(T) * 2 * 3 * NP);
+  const int t = threadIdx.x, i = t % TXE, j = t / TXE;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = blockIdx.z * TZ;
+  const int64_t nv = d.nv;
+  const int gx = x0 + i, gy = y0 + j;  // owned vertex (x, y) and element (x-1, y-1)
+  const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
+  const int zend = min(z0 + TZ, d.vz);
+  T acc0 = T(0), acc1 = T(0), acc2 = T(0);
+  auto load_plane = [&](int z) {
+    const int slot = z & 1;
+    for (int k = t; k < NP; k += NT) {
+      const int px = k % PX, py = k / PX;
+      const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+      T a = T(0), b = T(0), c = T(0);
+      if (vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz) {
+        const int64_t v = vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z);
+        a = u[v]; b = u[nv + v]; c = u[2 * nv + v];
+      }
+      us[slot][0][k] = a; us[slot][1][k] = b; us[slot][2][k] = c;
+    }
+  };
+  load_plane(z0 - 1);
+  for (int ez = z0 - 1; ez < zend; ++ez) {
+    load_plane(ez + 1);
+    __syncthreads();
+    {
+      const int ex = gx - 1, ey = gy - 1;
+      T pe = T(0);
+      if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
+        pe = rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)];
+      if (pe != T(0)) {
+        T c[3][8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
+          const int slot = (ez + (a >> 2)) & 1;
+          c[0][a] = us[slot][0][k]; c[1][a] = us[slot][1][k]; c[2][a] = us[slot][2][k];
+        }
+        modal_element<T>(c, pe);
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          fe[3 * a][t] = c[0][a]; fe[3 * a + 1][t] = c[1][a]; fe[3 * a + 2][t] = c[2][a];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 24; ++q) fe[q][t] = T(0);
+      }
+    }
+    __syncthreads();
+    if (own) {
+      T b0 = acc0, b1 = acc1, b2 = acc2, t0 = T(0), t1 = T(0), t2 = T(0);
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const int wx = w & 1, wy = w >> 1;
+        const int te = (i + wx) + TXE * (j + wy);
+        const int a = (1 - wx) + 2 * (1 - wy);  // bottom node of that element
+        b0 += fe[3 * a][te]; b1 += fe[3 * a + 1][te]; b2 += fe[3 * a + 2][te];
+        t0 += fe[3 * (a + 4)][te]; t1 += fe[3 * (a + 4) + 1][te]; t2 += fe[3 * (a + 4) + 2][te];
+      }
+      if (ez >= z0) {
+        const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
+        const uint8_t m = vmask[v];
+        const T y[3] = {b0, b1, b2};
+        if (MODE < 2) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const bool fr = (m >> c) & 1;
+            const int64_t idx = c * nv + v;
+            out[idx] = MODE == 1 ? (fr ? f[idx] - y[c] : T(0)) : (fr ? y[c] : T(0));
+          }
+        } else {
+          const T* __restrict__ dinv = static_cast<const T*>(ch.dinv);
+          T* __restrict__ dv = static_cast<T*>(ch.dvec);
+          T r[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] - y[c] : T(0);
+          const int k = (i + 1) + PX * (j + 1);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const T z = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] +
+                        dinv[(3 * c + 2) * nv + v] * r[2];
+            const T dn = ch.first ? T(ch.c_new) * z : T(ch.c_old) * dv[c * nv + v] + T(ch.c_new) * z;
+            dv[c * nv + v] = dn;
+            out[c * nv + v] = us[ez & 1][c][k] + dn;
+          }
+        }
+      }
+      acc0 = t0; acc1 = t1; acc2 = t2;
+    }
+    __syncthreads();
+  }
+}
+
+// Row block of vertex (x,y,z): out = sum over incident elements of rho^p Ke[a,:] u_e,
+// S = diagonal 3x3 block.  Template arguments fix whether S is needed.
+template <typename T, bool NEED_S>
+__device__ __forceinline__ void fine_row(const LevelDims& d, const T* __restrict__ rhop,
+                                         const T* __restrict__ u, int x, int y, int z, T out[3],
+                                         T S[9]) {
+  out[0] = out[1] = out[2] = T(0);
+  if (NEED_S)
+#pragma unroll
+    for (int i = 0; i < 9; ++i) S[i] = T(0);
+  const int64_t nv = d.nv;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    const int ex = x - 1 + (w & 1), ey = y - 1 + ((w >> 1) & 1), ez = z - 1 + (w >> 2);
+    if (ex < 0 || ey < 0 || ez < 0 || ex >= d.ex || ey >= d.ey || ez >= d.ez) continue;
+    const T pe = rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)];
+    if (pe == T(0)) continue;
+    const int a = 7 - w;
+    T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int64_t vb = (ex + (b & 1)) + (int64_t)d.vx * ((ey + ((b >> 1) & 1)) + (int64_t)d.vy * (ez + (b >> 2)));
+      const T u0 = u[vb], u1 = u[nv + vb], u2 = u[2 * nv + vb];
+      const int r0 = (3 * a) * 24 + 3 * b;
+      s0 += ke<T>(r0) * u0 + ke<T>(r0 + 1) * u1 + ke<T>(r0 + 2) * u2;
+      s1 += ke<T>(r0 + 24) * u0 + ke<T>(r0 + 25) * u1 + ke<T>(r0 + 26) * u2;
+      s2 += ke<T>(r0 + 48) * u0 + ke<T>(r0 + 49) * u1 + ke<T>(r0 + 50) * u2;
+    }
+    out[0] += pe * s0; out[1] += pe * s1; out[2] += pe * s2;
+    if (NEED_S) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) S[3 * i + j] += pe * ke<T>((3 * a + i) * 24 + 3 * a + j);
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fine_apply(LevelDims d, const T* __restrict__ rhop,
+                                                    const uint8_t* __restrict__ vmask,
+                                                    const T* __restrict__ u, const T* __restrict__ f,
+                                                    T* __restrict__ out, bool residual) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.nv) return;
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  const uint8_t m = vmask[v];
+  T o[3] = {T(0), T(0), T(0)};
+  if (m & 7) fine_row<T, false>(d, rhop, u, x, y, z, o, nullptr);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const bool fr = (m >> c) & 1;
+    const int64_t i = c * d.nv + v;
+    out[i] = residual ? (fr ? f[i] - o[c] : T(0)) : (fr ? o[c] : T(0));
+  }
+}
+
+// One colour of the 8-colour point-block Gauss-Seidel sweep.  Forward: DOFs
+// 0,1,2 (grid/Grid.cu:1830-1838); reverse: DOFs 2,1,0 (adjoint sweep).
+template <typename T>
+__device__ __forceinline__ void block_update(T* u, int64_t nv, int64_t v, const T r[3], const T S[9],
+                                             uint8_t fb, bool reverse) {
+  T du[3] = {T(0), T(0), T(0)};
+  if (!reverse) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (!((fb >> i) & 1)) continue;
+      T s = r[i];
+#pragma unroll
+      for (int j = 0; j < i; ++j) s -= S[3 * i + j] * du[j];
+      du[i] = s / S[4 * i];
+    }
+  } else {
+#pragma unroll
+    for (int i = 2; i >= 0; --i) {
+      if (!((fb >> i) & 1)) continue;
+      T s = r[i];
+#pragma unroll
+      for (int j = i + 1; j < 3; ++j) s -= S[3 * i + j] * du[j];
+      du[i] = s / S[4 * i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if ((fb >> i) & 1) u[i * nv + v] += du[i];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fine_gs(LevelDims d, const T* __restrict__ rhop,
+                                                 const uint8_t* __restrict__ vmask, T* u,
+                                                 const T* __restrict__ f, int cx, int cy, int cz,
+                                                 int hx, int hy, int64_t cnt, bool reverse) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  const int x = cx + 2 * (int)(t % hx);
+  const int64_t t2 = t / hx;
+  const int y = cy + 2 * (int)(t2 % hy), z = cz + 2 * (int)(t2 / hy);
+  const int64_t v = x + (int64_t)d.vx * (y + (int64_t)d.vy * z);
+  const uint8_t m = vmask[v];
+  const uint8_t fb = (m & 8) ? (m & 7) : 0;
+  if (!fb) return;
+  T o[3], S[9], r[3];
+  fine_row<T, true>(d, rhop, u, x, y, z, o, S);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) r[c] = f[c * d.nv + v] - o[c];
+  block_update<T>(u, d.nv, v, r, S, fb, reverse);
+}
+
+// Inverse of the free-DOF part of each diagonal 3x3 block, [9][nv] (Chebyshev).
+template <typename T>
+__device__ __forceinline__ void invert_block(const T S_in[9], uint8_t fb, T* dinv, int64_t nv,
+                                             int64_t v) {
+  T S[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      S[3 * i + j] = (((fb >> i) & 1) && ((fb >> j) & 1)) ? S_in[3 * i + j] : (i == j ? T(1) : T(0));
+  const T a = S[0], b = S[1], c = S[2], dd = S[4], e = S[5], f = S[8];
+  const T A0 = dd * f - e * e, A1 = c * e - b * f, A2 = b * e - c * dd;
+  const T det = a * A0 + b * A1 + c * A2;
+  const T inv[9] = {A0, A1, A2, A1, a * f - c * c, b * c - a * e, A2, b * c - a * e, a * dd - b * b};
+  const T rd = T(1) / det;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int i = k / 3, j = k % 3;
+    const bool keep = ((fb >> i) & 1) && ((fb >> j) & 1);
+    dinv[k * nv + v] = keep ? inv[k] * rd : T(0);
+  }
+}
+
+template <typename T>
+__global__ void k_fine_diag_inv(LevelDims d, const T* __restrict__ rhop,
+                                const uint8_t* __restrict__ vmask, T* __restrict__ dinv) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.nv) return;
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  const uint8_t m = vmask[v];
+  const uint8_t fb = (m & 8) ? (m & 7) : 0;
+  T S[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) S[i] = T(0);
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    const int ex = x - 1 + (w & 1), ey = y - 1 + ((w >> 1) & 1), ez = z - 1 + (w >> 2);
+    if (ex < 0 || ey < 0 || ez < 0 || ex >= d.ex || ey >= d.ey || ez >= d.ez) continue;
+    const T pe = rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)];
+    const int a = 7 - w;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[3 * i + j] += pe * ke<T>((3 * a + i) * 24 + 3 * a + j);
+  }
+  invert_block<T>(S, fb, dinv, d.nv, v);
+}
+
+static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+constexpr int MODAL_TXE = 32, MODAL_TYE = 8, MODAL_TZ = 16;
+
+// Opt the modal kernels into more than 48 KB of dynamic shared memory (once).
+template <typename T>
+void modal_smem_attr(size_t smem) {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  done = true;
+}
+
+template <typename T>
+void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
+                       const T* u, const T* f, T* out, bool residual) {
+  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
+                  (d.vz + MODAL_TZ - 1) / MODAL_TZ);
+  constexpr int NT = MODAL_TXE * MODAL_TYE, NP = (MODAL_TXE + 1) * (MODAL_TYE + 1);
+  const size_t smem = sizeof(T) * (2 * 3 * NP + 24 * NT);
+  modal_smem_attr<T>(smem);
+  ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0};
+  if (residual)
+    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ, ch);
+  else
+    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ, ch);
+}
+
+// One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u).
+template <typename T>
+void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
+                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first) {
+  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
+                  (d.vz + MODAL_TZ - 1) / MODAL_TZ);
+  constexpr int NT = MODAL_TXE * MODAL_TYE, NP = (MODAL_TXE + 1) * (MODAL_TYE + 1);
+  const size_t smem = sizeof(T) * (2 * 3 * NP + 24 * NT);
+  modal_smem_attr<T>(smem);
+  ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0};
+  k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, MODAL_TZ, ch);
+}
+
+template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
+                                       const double*, const double*, double*, const double*, double*, double,
+                                       double, bool);
+template void launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
+                                      const float*, const float*, float*, const float*, float*, double, double,
+                                      bool);
+
+// Dense-row form of the same operator (thread per vertex, 8 x 3 x 24 products);
+// kept as the cross-check of the modal kernel.
+template <typename T>
+void launch_fine_apply_dense(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
+                             const T* u, const T* f, T* out, bool residual) {
+  k_fine_apply<T><<<blocks_for(d.nv, 256), 256, 0, s>>>(d, rhop, vmask, u, f, out, residual);
+}
+
+template void launch_fine_apply_dense<double>(cudaStream_t, const LevelDims&, const double*,
+                                              const uint8_t*, const double*, const double*, double*, bool);
+template void launch_fine_apply_dense<float>(cudaStream_t, const LevelDims&, const float*,
+                                             const uint8_t*, const float*, const float*, float*, bool);
+
+template <typename T>
+void launch_fine_gs(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, T* u,
+                    const T* f, int colour, bool reverse) {
+  const int cx = colour & 1, cy = (colour >> 1) & 1, cz = colour >> 2;
+  const int hx = (d.vx - cx + 1) / 2, hy = (d.vy - cy + 1) / 2, hz = (d.vz - cz + 1) / 2;
+  const int64_t cnt = (int64_t)hx * hy * hz;
+  if (cnt <= 0) return;
+  k_fine_gs<T><<<blocks_for(cnt, 256), 256, 0, s>>>(d, rhop, vmask, u, f, cx, cy, cz, hx, hy, cnt,
+                                                    reverse);
+}
+
+template <typename T>
+void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
+                          T* dinv) {
+  k_fine_diag_inv<T><<<blocks_for(d.nv, 256), 256, 0, s>>>(d, rhop, vmask, dinv);
+}
+
+template void launch_fine_apply<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
+                                        const double*, const double*, double*, bool);
+template void launch_fine_apply<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
+                                       const float*, const float*, float*, bool);
+template void launch_fine_gs<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
+                                     double*, const double*, int, bool);
+template void launch_fine_gs<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
+                                    float*, const float*, int, bool);
+template void launch_fine_diag_inv<double>(cudaStream_t, const LevelDims&, const double*,
+                                           const uint8_t*, double*);
+template void launch_fine_diag_inv<float>(cudaStream_t, const LevelDims&, const float*,
+                                          const uint8_t*, float*);
+
+}  // namespace topo

@@ -1,0 +1,189 @@
+// Internal declarations shared by the translation units of libtopo_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "../../include/topo_gb300.h"
+
+namespace topo {
+
+// Process-wide count of kernel launches issued by this library.
+extern std::atomic<long long> g_launches;
+inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Dense grid level.  Element/vertex numbering is lexicographic (x fastest).
+struct LevelDims {
+  int ex, ey, ez;
+  int vx, vy, vz;
+  int64_t ne, nv;
+  int factor;  // coarsening factor from the previous used level (1 for level 0)
+};
+
+// Device buffers of one level.  Vertex vectors are SoA [3][nv].
+struct DevLevel {
+  LevelDims d{};
+  uint8_t* eactive = nullptr;  // [ne]
+  uint8_t* vmask = nullptr;    // [nv] bits0-2 DOF free, bit3 active
+  double *U = nullptr, *F = nullptr, *R = nullptr;    // FP64 [3nv]
+  float *U32 = nullptr, *F32 = nullptr, *R32 = nullptr;  // FP32 [3nv]
+  double* kel = nullptr;        // coarse: FP64 element matrices [ne][576]
+  float* kel32 = nullptr;       // coarse: FP32 element matrices [ne][576]
+  double* stencil = nullptr;    // coarse: FP64 [243][nv]
+  float* stencil32 = nullptr;   // coarse: FP32 [243][nv]
+  double* dinv = nullptr;       // FP64 inverse diagonal blocks [9][nv] (Chebyshev)
+  float* dinv32 = nullptr;      // FP32 inverse diagonal blocks [9][nv]
+  double* cd = nullptr;         // FP64 Chebyshev direction [3nv]
+  float* cd32 = nullptr;        // FP32 Chebyshev direction [3nv]
+  double* U2 = nullptr;         // FP64 second iterate buffer (Chebyshev ping-pong) [3nv]
+  float* U2_32 = nullptr;       // FP32 second iterate buffer [3nv]
+  double lmax = 0, lmax32 = 0;  // Chebyshev spectral bound estimates
+};
+
+// Host-side hierarchy description (computed once from the active mask).
+struct Hierarchy {
+  std::vector<LevelDims> dims;
+  std::vector<std::vector<uint8_t>> eactive;  // per used level
+  std::vector<std::vector<uint8_t>> vactive;  // per used level (bit3 only)
+};
+
+// Host-side set-up helpers (host_setup.cpp).
+void element_template(double E, double nu, double h, double* Ke576);
+Hierarchy build_hierarchy(int nx, int ny, int nz, const uint8_t* eactive, int max_coarse);
+void spline_knots(int order, int partition, double bmin, double bmax, std::vector<double>& knots,
+                  double& kmin, double& kstep);
+// Galerkin transfer tables: T_pos = Q_pos^T Ke Q_pos for the 64 (factor 4) or 8
+// (factor 2) fine-element positions, and the interpolation weights Q[pos][a][C].
+void interp_weights(int factor, int px, int py, int pz, double Q[8][8]);
+void galerkin_tables(const double* Ke, int factor, std::vector<double>& T);
+int64_t gs_padded_count(const LevelDims& d, const uint8_t* active, bool vertices);
+
+// Kernel launch wrappers (the .cu files).
+struct Stream {
+  cudaStream_t s;
+};
+
+// fine level (k_fine.cu)
+template <typename T>
+void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
+                       const T* u, const T* f, T* out, bool residual);
+template <typename T>
+void launch_fine_gs(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, T* u,
+                    const T* f, int colour, bool reverse);
+template <typename T>
+void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
+                          T* dinv);
+template <typename T>
+void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
+                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first);
+template <typename T>
+void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
+                         const T* dinv, T* dvec, double c_old, double c_new, bool first);
+template <typename T>
+void launch_fine_apply_dense(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
+                             const T* u, const T* f, T* out, bool residual);
+void upload_template(const double* Ke576, double lam, double mu, double h);
+
+// coarse levels (k_coarse.cu)
+template <typename T>
+void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
+                          T* out, bool residual);
+template <typename T>
+void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask, T* u,
+                       const T* f, int colour, bool reverse);
+template <typename T>
+void launch_stencil_diag_inv(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask,
+                             T* dinv);
+template <typename T>
+void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
+                     T* fc);
+template <typename T>
+void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* uc,
+                    T* uf, const uint8_t* vmask_fine);
+void launch_galerkin_first_impl(cudaStream_t s, const LevelDims& fd, const LevelDims& cd,
+                                const double* rhop, const uint8_t* eactive_f, const uint8_t* vmask_f,
+                                const double* Ttab64, const float* Ttab32, const double* Ke,
+                                const int* fixed_list, int nfixed, double* kel, float* kel32);
+template <typename T>
+void launch_galerkin_dyadic_t(cudaStream_t s, const LevelDims& fd, const LevelDims& cd,
+                              const uint8_t* eactive_f, const T* kel_f, T* kel_c);
+template <typename T>
+void launch_assemble_stencil_t(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                               const uint8_t* vmask, const T* kel, T* st);
+void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double* st, double* A);
+int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev);
+void launch_to_float(cudaStream_t s, const double* a, float* b, int64_t n);
+template <typename T>
+void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv);
+
+// vectors and reductions (k_vec.cu)
+int reduce_blocks(int64_t n);
+template <typename T>
+void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out);
+// b == nullptr sums a.
+void launch_sum(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);
+void launch_axpby(cudaStream_t s, double a, const double* x, double b, double* y, int64_t n);
+template <typename T>
+void launch_fill(cudaStream_t s, T* a, T v, int64_t n);
+template <typename T>
+void launch_copy(cudaStream_t s, const T* a, T* b, int64_t n);
+void launch_d2f(cudaStream_t s, const double* a, float* b, int64_t n);
+void launch_f2d_add(cudaStream_t s, const float* a, double* b, int64_t n);
+// PCG helpers with device-resident scalars (sc: double scalar slots)
+template <typename T>
+void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int num, int den, bool first,
+                    int64_t n);
+template <typename T>
+void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q,
+                       const double* sc, int num, int den, int64_t n);
+template <typename T>
+void launch_cheb_step(cudaStream_t s, const LevelDims& dm, const T* dinv, const T* r, T* dvec, T* u,
+                      double c_old, double c_new, bool first);
+
+// design chain (k_design.cu)
+struct SplineDev {
+  int order;
+  int nb[3];
+  const int* i0[3];      // device [n_axis]: first basis index of each element slice, -1 out of range
+  const double* N[3];    // device [n_axis][order]: basis values at the element centres
+  const int* lo[3];      // device [nb]: first element slice in the support of basis i
+  const int* hi[3];      // device [nb]: one past the last element slice
+};
+// Host-side basis tables (Cox-de Boor, grid/Grid.cu:384-466 at element centres).
+struct SplineTables {
+  int order = 0;
+  int nb[3] = {0, 0, 0};
+  std::vector<double> knots[3];
+  double kmin[3] = {0, 0, 0}, kstep[3] = {0, 0, 0};
+  std::vector<int> i0[3];
+  std::vector<double> N[3];
+  std::vector<int> lo[3], hi[3];
+};
+void spline_tables(int order, const int* partition, const double* bmin, const double* bmax,
+                   const int* nelem, double h, SplineTables& t);
+void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                             const SplineDev& sp, const double* coeff, double rho_min, double penal,
+                             double* rho, double* rhop, float* rhop32);
+void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                         const SplineDev& sp, const double* coeff, double rho_min, double* partial,
+                         double* out);
+void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                        const double* rho, const double* u, double penal, double lam, double mu,
+                        double h, double* sens);
+void launch_filter(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* src,
+                   double* dst, const int4* offs, const double* wts, int noffs);
+void filter_table(double R, std::vector<int4>& offs, std::vector<double>& w);
+void launch_spline_adjoint(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                           const SplineDev& sp, const double* sens, double* csens, double* tmp1,
+                           double* tmp2);
+void launch_penalise(cudaStream_t s, int64_t ne, const uint8_t* eactive, const double* rho,
+                     double penal, double* rhop, float* rhop32);
+void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,
+                     double damp, double step, double cmin, double cmax, double* cnew);
+void launch_maxabs(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);
+
+}  // namespace topo

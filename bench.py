@@ -42,6 +42,10 @@ def parse():
     ap.add_argument("--smoother", default="chebyshev", choices=["chebyshev", "gs"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="FP64 MG-PCG comparison steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-iteration", action="store_true",
+                    help="run exactly one mixed design iteration and exit (for ncu captures)")
+    ap.add_argument("--profile-solve-steps", type=int, default=0,
+                    help="with --profile-iteration: stop the solve after this many outer CG steps")
     return ap.parse_args()
 
 
@@ -140,7 +144,7 @@ def make_problem(nx, ny, nz, device, op_precision):
 def solve_opts(mode, smoother):
     from topoptspline3d_gb300 import capi
     return dict(mode=mode, smoother=capi.SMOOTH_CHEBYSHEV if smoother == "chebyshev" else capi.SMOOTH_GS,
-                pre=2, post=2, rtol=1e-6, max_iter=300, inner_max=1, inner_rtol=0.1)
+                pre=2, post=2, rtol=1e-6, max_iter=300, inner_max=4, inner_rtol=0.1)
 
 
 def load_traffic():
@@ -227,6 +231,13 @@ def main():
     wl, p = make_problem(nx, ny, nz, device, op_precision=2)
     opts = solve_opts(capi.SOLVE_MIXED, args.smoother)
     oc = dict(vgoal=wl.vgoal, damp=0.5, step=0.03, cmin=0.0, cmax=1.0)
+    if args.profile_iteration:
+        if args.profile_solve_steps > 0:
+            opts["max_iter"] = args.profile_solve_steps
+        s = p.design_iteration(solve=opts, oc=oc)
+        print(json.dumps({"profile_iteration": s}), flush=True)
+        p.close()
+        return
     for _ in range(args.warmup):
         p.design_iteration(solve=opts, oc=oc)
     # ---- timed region: K design iterations, device-resident inputs
@@ -278,8 +289,10 @@ def main():
     nv, ne = (d0[0] + 1) * (d0[1] + 1) * (d0[2] + 1), d0[0] * d0[1] * d0[2]
     fams = {capi.K_FINE_APPLY64: ("k_fine_modal<double> (FP64 K.u, outer CG)", nv * (24 + 24 + 1) + ne * 8,
                                   ne * 240.0),
+            # u in, f in, d in/out, u out (FP32 x3 each), vertex mask, rho^p; the
+            # block-Jacobi diagonal is rebuilt from rho^p in the kernel
             capi.K_FINE_SMOOTH32: ("k_fine_modal<float, Chebyshev> (FP32 smoother step)",
-                                   nv * (12 + 12 + 36 + 24 + 12 + 1) + ne * 4, ne * 240.0 + nv * 30.0),
+                                   nv * (12 + 12 + 24 + 12 + 1) + ne * 4, ne * 240.0 + nv * 120.0),
             capi.K_FINE_APPLY32: ("k_fine_modal<float> (FP32 K.u)", nv * (12 + 12 + 1) + ne * 4, ne * 240.0),
             capi.K_FINE_SMOOTH64: ("k_fine_gs<double>", nv * (24 + 24 + 24 + 1) + ne * 8, nv * 1170.0)}
     dom = max(prof, key=lambda k: prof[k][1])

@@ -1,0 +1,49 @@
+"""The C++ driver (cpp/topopt_driver.cpp over the grid::HierarchyGrid facade)."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from topoptspline3d_gb300 import build, capi, workloads
+from tests.helpers import setup_oracle
+
+
+def _driver():
+    capi.load()
+    assert os.path.exists(build.DRIVER_PATH)
+    return build.DRIVER_PATH
+
+
+def test_driver_rejects_bad_arguments():
+    r = subprocess.run([_driver(), "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 2 and "unknown argument" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_matches_oracle_history(oracle_mod):
+    r = subprocess.run([_driver(), "--case", "cantilever", "--nx", "16", "--ny", "8", "--nz", "8", "--lattice",
+                        "7", "5", "5", "--iters", "4", "--mode", "pcg64"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    summary = json.loads(r.stdout.strip().splitlines()[-1])
+    wl = workloads.cantilever(16, 8, 8, lattice=(7, 5, 5))
+    o = setup_oracle(wl)
+    co = []
+    for _ in range(4):
+        o.update_operators()
+        o.pcg(2, 2, 1e-6, 300, 1)
+        co.append(o.compliance())
+        o.sensitivity(); o.filter(2.0); o.spline_adjoint(); o.oc_update(0.4)
+    assert np.allclose(summary["compliance"], co, rtol=1e-6, atol=0), (summary["compliance"], co)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["mixed", "vcycle"])
+def test_driver_modes_run(mode):
+    r = subprocess.run([_driver(), "--case", "mbb", "--nx", "32", "--ny", "16", "--nz", "16", "--lattice",
+                        "11", "7", "7", "--iters", "3", "--mode", mode], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    c = json.loads(r.stdout.strip().splitlines()[-1])["compliance"]
+    assert all(np.isfinite(c)) and c[-1] < c[0]

@@ -35,6 +35,8 @@ def _sources():
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     hs.append(os.path.join(HERE, "..", "include", "topo_gb300.h"))
+    cpp = os.path.join(HERE, "cpp")
+    hs += [os.path.join(cpp, f) for f in os.listdir(cpp) if f.endswith((".hpp", ".cpp"))]
     return hs
 
 
@@ -73,9 +75,27 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB_PATH)
+    build_driver()
     if verbose:
         print("built", LIB_PATH)
     return LIB_PATH
+
+
+DRIVER_PATH = os.path.join(OUT_DIR, "topopt_driver")
+
+
+def build_driver() -> str:
+    """C++ driver (cpp/topopt_driver.cpp) linked against the in-tree library."""
+    src = os.path.join(HERE, "cpp", "topopt_driver.cpp")
+    tmp = DRIVER_PATH + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include"),
+           "-I" + os.path.join(HERE, "cpp"), src, "-o", tmp, "-L" + OUT_DIR, "-ltopo_gb300",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DRIVER_PATH)
+    return DRIVER_PATH
 
 
 if __name__ == "__main__":

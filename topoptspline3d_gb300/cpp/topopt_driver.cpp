@@ -1,0 +1,130 @@
+// topopt_driver -- C++ driver of the spline OC topology optimisation, the loop of
+// TestSuit::testOrdinarySplineTopopt (utils/test_utils.cpp:878-970) written
+// against the grid::HierarchyGrid facade of topo_grid.hpp.
+//
+//   topopt_driver [--case cantilever|mbb] [--nx N --ny N --nz N] [--iters K]
+//                 [--mode vcycle|pcg64|mixed] [--vf 0.4] [--filter 2] [--order 3]
+//                 [--lattice LX LY LZ]
+//
+// Prints one line per design iteration and a JSON summary line.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "topo_grid.hpp"
+
+namespace {
+
+struct Args {
+  std::string kase = "cantilever";
+  int nx = 48, ny = 24, nz = 24, iters = 10, order = 3;
+  int lattice[3] = {13, 7, 7};
+  std::string mode = "mixed";
+  double vf = 0.4, filter = 2.0;
+};
+
+Args parse(int argc, char** argv) {
+  Args a;
+  for (int i = 1; i < argc; ++i) {
+    std::string s = argv[i];
+    auto next = [&]() -> const char* {
+      if (i + 1 >= argc) { std::fprintf(stderr, "missing value for %s\n", s.c_str()); std::exit(2); }
+      return argv[++i];
+    };
+    if (s == "--case") a.kase = next();
+    else if (s == "--nx") a.nx = std::atoi(next());
+    else if (s == "--ny") a.ny = std::atoi(next());
+    else if (s == "--nz") a.nz = std::atoi(next());
+    else if (s == "--iters") a.iters = std::atoi(next());
+    else if (s == "--mode") a.mode = next();
+    else if (s == "--vf") a.vf = std::atof(next());
+    else if (s == "--filter") a.filter = std::atof(next());
+    else if (s == "--order") a.order = std::atoi(next());
+    else if (s == "--lattice") { for (int k = 0; k < 3; ++k) a.lattice[k] = std::atoi(next()); }
+    else { std::fprintf(stderr, "unknown argument %s\n", s.c_str()); std::exit(2); }
+  }
+  return a;
+}
+
+// Boundary conditions of the two benchmark cases (same as workloads.py).
+void make_bc(const Args& a, std::vector<uint8_t>& fixed, std::vector<double>& loads) {
+  const int vx = a.nx + 1, vy = a.ny + 1, vz = a.nz + 1;
+  const int64_t nv = (int64_t)vx * vy * vz;
+  fixed.assign(nv, 0);
+  loads.assign(3 * nv, 0.0);
+  auto vid = [&](int x, int y, int z) { return x + (int64_t)vx * (y + (int64_t)vy * z); };
+  if (a.kase == "cantilever") {
+    // x = 0 face fixed; unit downward force over the bottom edge of the x = nx face
+    for (int z = 0; z < vz; ++z)
+      for (int y = 0; y < vy; ++y) fixed[vid(0, y, z)] = 7;
+    for (int y = 0; y < vy; ++y) loads[2 * nv + vid(a.nx, y, 0)] = -1.0 / vy;
+  } else {
+    // half-MBB: u_x = 0 on x = 0; u_y = u_z = 0 on the bottom edge at x = nx; line load at the top of x = 0
+    for (int z = 0; z < vz; ++z)
+      for (int y = 0; y < vy; ++y) fixed[vid(0, y, z)] |= 1;
+    for (int y = 0; y < vy; ++y) fixed[vid(a.nx, y, 0)] |= 6;
+    for (int y = 0; y < vy; ++y) loads[2 * nv + vid(0, y, a.nz)] = -1.0 / vy;
+  }
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  const Args a = parse(argc, argv);
+  try {
+    topo_config cfg{a.nx, a.ny, a.nz, 1.0, 1e6, 0.4, 3.0, 1e-3, 400, 0};
+    grid::HierarchyGrid grids(cfg);
+    std::vector<uint8_t> fixed;
+    std::vector<double> loads;
+    make_bc(a, fixed, loads);
+    grids.setBoundaryCondition(fixed, loads);
+    const int part[3] = {a.lattice[0] - a.order, a.lattice[1] - a.order, a.lattice[2] - a.order};
+    const double bmin[3] = {0, 0, 0}, bmax[3] = {(double)a.nx, (double)a.ny, (double)a.nz};
+    grids.set_spline(a.order, part, bmin, bmax);
+    grids[0]->init_coeff(a.vf);  // initCoeffs(volume_ratio), optimization/optimization.cpp:1045-1058
+    grids[0]->coeff2density();
+
+    topo_solve_opts so{};
+    so.mode = a.mode == "vcycle" ? TOPO_SOLVE_VCYCLE : a.mode == "pcg64" ? TOPO_SOLVE_PCG64 : TOPO_SOLVE_MIXED;
+    so.smoother = so.mode == TOPO_SOLVE_VCYCLE ? TOPO_SMOOTH_GS : TOPO_SMOOTH_CHEBYSHEV;
+    so.pre = so.mode == TOPO_SOLVE_VCYCLE ? 5 : 2;
+    so.post = so.pre;
+    so.rtol = so.mode == TOPO_SOLVE_VCYCLE ? 1e-3 : 1e-6;
+    so.max_iter = so.mode == TOPO_SOLVE_VCYCLE ? 50 : 300;
+    so.inner_rtol = 0.1;
+    so.inner_max = 4;
+    so.cheb_degree = 2;
+    so.cheb_lo = 0.3;
+    so.cheb_hi = 1.1;
+    if (so.mode == TOPO_SOLVE_MIXED) grid::check(grids.handle(), topo_set_operator_precision(grids.handle(), 2), "precision");
+
+    std::vector<double> crec;
+    double total_ms = 0;
+    for (int itn = 1; itn <= a.iters; ++itn) {
+      const auto t0 = std::chrono::steady_clock::now();
+      grids.update_stencil();
+      topo_solve_stats st = grids.solve(so);
+      const double c = grids[0]->compliance();
+      computeSensitivity(grids, a.filter);
+      updateCoeff(grids, a.vf);
+      const double vol = grids[0]->volumeRatio();
+      const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      total_ms += ms;
+      crec.push_back(c);
+      std::printf("-- iter %3d  c = %.10e  v = %.6f  its = %d  r = %.2e  %.2f ms\n", itn, c, vol, st.iterations,
+                  st.relres, ms);
+    }
+    std::printf("{\"driver\": \"topopt_driver\", \"case\": \"%s\", \"grid\": [%d, %d, %d], \"iters\": %d, "
+                "\"mode\": \"%s\", \"ms_per_iter\": %.4f, \"compliance\": [",
+                a.kase.c_str(), a.nx, a.ny, a.nz, a.iters, a.mode.c_str(), total_ms / a.iters);
+    for (size_t k = 0; k < crec.size(); ++k) std::printf("%s%.15e", k ? ", " : "", crec[k]);
+    std::printf("]}\n");
+  } catch (const grid::TopoError& e) {
+    std::fprintf(stderr, "topopt_driver: %s\n", e.what());
+    return 1;
+  }
+  return 0;
+}

@@ -21,7 +21,11 @@ using namespace topo;
 namespace {
 
 // Scalar slots in device memory used by the PCG drivers.
-enum Slot { S_RZ = 0, S_ZROLD = 1, S_RZOLD = 2, S_DQ = 3, S_RR = 4, S_FF = 5, S_TMP = 6, S_COUNT = 16 };
+// Slots 0-7 belong to one CG level; a nested CG uses base 8 (slots 8-15).
+enum Slot {
+  S_RZ = 0, S_ZROLD = 1, S_RZOLD = 2, S_DQ = 3, S_RR = 4, S_FF = 5, S_ALPHA = 6, S_BETA = 7,
+  S_TMP = 16, S_COUNT = 24
+};
 
 struct EventPair {
   cudaEvent_t a, b;
@@ -330,7 +334,8 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
 
 // Power iteration for the largest eigenvalue of D^{-1} A on a level, from the
 // same deterministic start vector as the oracle.
-__global__ void k_power_start(int64_t nv, const uint8_t* vmask, double* x) {
+template <typename T>
+__global__ void k_power_start(int64_t nv, const uint8_t* vmask, T* x) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * nv) return;
   uint64_t hsh = (uint64_t)i * 0x9E3779B97F4A7C15ull;
@@ -339,16 +344,7 @@ __global__ void k_power_start(int64_t nv, const uint8_t* vmask, double* x) {
   const int64_t vv = i % nv;
   const int c = (int)(i / nv);
   if (!((vmask[vv] >> c) & 1) || !(vmask[vv] & 8)) v = 0.0;
-  x[i] = v;
-}
-
-template <typename T>
-__global__ void k_scale_cast(int64_t n, const double* x, double s_num_sqrt_inv_slot_dummy, const double* sc,
-                             int slot, T* out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double nrm = sqrt(sc[slot]);
-  out[i] = (T)(x[i] / nrm);
+  x[i] = (T)v;
 }
 
 template <typename T>
@@ -372,33 +368,26 @@ template <typename T>
 int estimate_lmax(topo_handle* h, int l, double* out) {
   DevLevel& L = h->lv[l];
   const int64_t n3 = 3 * L.d.nv;
-  // x (double) lives in h->work-sized scratch: use level buffers: R (as T) and cd (as T)
-  double* xd = nullptr;
-  T *xt = nullptr, *yt = nullptr, *zt = nullptr;
-  CK(cudaMallocAsync((void**)&xd, sizeof(double) * n3, h->stream));
-  CK(cudaMallocAsync((void**)&xt, sizeof(T) * n3, h->stream));
-  CK(cudaMallocAsync((void**)&yt, sizeof(T) * n3, h->stream));
-  CK(cudaMallocAsync((void**)&zt, sizeof(T) * n3, h->stream));
-  k_power_start<<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, xd);
-  double lam = 0.0;
+  // work vectors in precision T: the level's R, U2 and Chebyshev direction
+  // buffers (all free outside a V-cycle)
+  T* x = P<T>::R(L);
+  T* xn = P<T>::cd(L);
+  T* z = P<T>::U2(L);
+  k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, x);
+  count_launch();
   for (int it = 0; it < 12; ++it) {
-    launch_dot<double>(h->stream, xd, xd, n3, h->partial, h->sc + S_TMP);
-    k_scale_cast<T><<<nb256(n3), 256, 0, h->stream>>>(n3, xd, 0.0, h->sc, S_TMP, xt);
-    if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, xt, nullptr, yt, false);
-    else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), xt, nullptr, yt, false);
-    k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), yt, zt);
-    launch_dot<T>(h->stream, xt, zt, n3, h->partial, h->sc + S_TMP + 1);
-    k_to_double<T><<<nb256(n3), 256, 0, h->stream>>>(n3, zt, xd);
+    launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP);
+    launch_scale_by_rnorm<T>(h->stream, x, xn, h->sc, S_TMP, n3);
+    if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, xn, nullptr, x, false);
+    else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), xn, nullptr, x, false);
+    k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), x, z);
+    launch_dot<T>(h->stream, xn, z, n3, h->partial, h->sc + S_TMP + 1);
+    std::swap(x, z);
     count_launch(7);
   }
   CK(cudaMemcpyAsync(h->hsc, h->sc + S_TMP + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  lam = h->hsc[0];
-  cudaFreeAsync(xd, h->stream);
-  cudaFreeAsync(xt, h->stream);
-  cudaFreeAsync(yt, h->stream);
-  cudaFreeAsync(zt, h->stream);
-  *out = lam;
+  *out = h->hsc[0];
   return TOPO_OK;
 }
 
@@ -448,13 +437,15 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
       launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD);
       count_launch(2);
     }
-    launch_pcg_dir<T>(h->stream, z, d, sc, S_RZ, S_RZOLD, it == 0, n3);
+    if (it > 0) launch_scalar_ratio(h->stream, sc, S_RZ, S_ZROLD, S_RZOLD, S_BETA);
+    launch_pcg_dir<T>(h->stream, z, d, sc, S_BETA, it == 0, n3);
     level_apply<T>(h, 0, d, nullptr, q, false);
     launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ);
-    launch_pcg_update<T>(h->stream, x, r, rold, d, q, sc, S_RZ, S_DQ, n3);
+    launch_scalar_ratio(h->stream, sc, S_RZ, -1, S_DQ, S_ALPHA);
+    launch_pcg_update<T>(h->stream, x, r, rold, d, q, sc, S_ALPHA, n3);
     CK(cudaMemcpyAsync(sc + S_RZOLD, sc + S_RZ, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     launch_dot<T>(h->stream, r, r, n3, h->partial, sc + S_RR);
-    count_launch(7);
+    count_launch(it > 0 ? 9 : 8);
     CKL();
     RET(read_scalars(h, base + S_RR, 1));
     rn = std::sqrt(h->hsc[base + S_RR]);
@@ -822,8 +813,8 @@ int topo_coeff_to_density(topo_handle* h) {
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set (call topo_set_spline)");
   const DevLevel& L = h->lv[0];
   launch_coeff_to_density(h->stream, L.d, L.eactive, h->sd, h->coeff, h->cfg.min_density,
-                          h->cfg.power_penalty, h->rho, h->rhop, h->rhop32);
-  count_launch();
+                          h->cfg.power_penalty, h->rho, h->rhop, h->rhop32, h->adj1);
+  count_launch(2);
   CKL();
   h->rhop_stale = false;
   h->ops_ready = false;
@@ -1189,8 +1180,8 @@ int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) 
     thres = 0.5 * (lo + hi);
     launch_oc_trial(h->stream, nc, h->coeff_old, h->csens, thres, o->damp, o->step, o->cmin, o->cmax, h->coeff);
     launch_trial_volume(h->stream, L.d, L.eactive, h->sd, h->coeff, h->cfg.min_density, h->partial,
-                        h->sc + S_TMP);
-    count_launch(3);
+                        h->sc + S_TMP, h->adj1);
+    count_launch(4);
     CKL();
     RET(read_scalars(h, S_TMP, 1));
     V = h->hsc[S_TMP] / den;

@@ -32,22 +32,6 @@ __device__ __forceinline__ void stencil_row(const LevelDims& d, const T* __restr
   }
 }
 
-template <typename T>
-__global__ void k_stencil_apply(LevelDims d, const T* __restrict__ st, const T* __restrict__ u,
-                                const T* __restrict__ f, T* __restrict__ out, bool residual) {
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= d.nv) return;
-  const int x = (int)(v % d.vx);
-  const int64_t t = v / d.vx;
-  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
-  T o[3];
-  stencil_row<T>(d, st, u, x, y, z, v, o);
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const int64_t i = c * d.nv + v;
-    out[i] = residual ? f[i] - o[c] : o[c];
-  }
-}
 
 template <typename T>
 __global__ void k_stencil_gs(LevelDims d, const T* __restrict__ st, const uint8_t* __restrict__ vmask,
@@ -106,39 +90,80 @@ __global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st,
   for (int k = 0; k < 9; ++k) dinv[k * d.nv + v] = act ? inv[k] * rd : T(0);
 }
 
-// One Chebyshev step on a stencil level: uout = u + d, d = c_old d + c_new Dinv (f - A u).
+// Row-split stencil kernels: a CTA of 3 x SV threads covers SV vertices, one
+// thread per (vertex, row); the three rows of a vertex share its neighbours'
+// values through L1.  Three times the threads of a vertex-per-thread kernel keep
+// enough loads in flight on the small coarse levels.
+constexpr int SV = 64;
+
 template <typename T>
-__global__ void k_stencil_cheb(LevelDims d, const T* __restrict__ st, const T* __restrict__ u,
-                               const T* __restrict__ f, T* __restrict__ uout, const T* __restrict__ dinv,
-                               T* __restrict__ dv, T c_old, T c_new, bool first) {
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ T stencil_row_i(const LevelDims& d, const T* __restrict__ st, const T* __restrict__ u,
+                                           int x, int y, int z, int64_t v, int row) {
+  T o = T(0);
+  const int64_t nv = d.nv;
+#pragma unroll
+  for (int k = 0; k < 27; ++k) {
+    const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
+    if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) continue;
+    const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
+    const T* s = st + (int64_t)(k * 9 + 3 * row) * nv + v;
+    o += s[0] * u[n] + s[nv] * u[nv + n] + s[2 * nv] * u[2 * nv + n];
+  }
+  return o;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st,
+                                                           const T* __restrict__ u, const T* __restrict__ f,
+                                                           T* __restrict__ out, bool residual) {
+  const int row = threadIdx.x / SV;
+  const int64_t v = (int64_t)blockIdx.x * SV + threadIdx.x % SV;
   if (v >= d.nv) return;
   const int x = (int)(v % d.vx);
   const int64_t t = v / d.vx;
   const int y = (int)(t % d.vy), z = (int)(t / d.vy);
-  T o[3];
-  stencil_row<T>(d, st, u, x, y, z, v, o);
+  const T o = stencil_row_i<T>(d, st, u, x, y, z, v, row);
+  const int64_t i = row * d.nv + v;
+  out[i] = residual ? f[i] - o : o;
+}
+
+// One Chebyshev step on a stencil level: uout = u + d, d = c_old d + c_new Dinv (f - A u).
+template <typename T>
+__global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* __restrict__ st,
+                                                         const T* __restrict__ u, const T* __restrict__ f,
+                                                         T* __restrict__ uout, const T* __restrict__ dinv,
+                                                         T* __restrict__ dv, T c_old, T c_new, bool first) {
+  __shared__ T sr[3][SV];
+  const int row = threadIdx.x / SV, lv = threadIdx.x % SV;
+  const int64_t v = (int64_t)blockIdx.x * SV + lv;
   const int64_t nv = d.nv;
-  const T r0 = f[v] - o[0], r1 = f[nv + v] - o[1], r2 = f[2 * nv + v] - o[2];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const T zz = dinv[(3 * c) * nv + v] * r0 + dinv[(3 * c + 1) * nv + v] * r1 + dinv[(3 * c + 2) * nv + v] * r2;
-    const T dn = first ? c_new * zz : c_old * dv[c * nv + v] + c_new * zz;
-    dv[c * nv + v] = dn;
-    uout[c * nv + v] = u[c * nv + v] + dn;
+  const bool ok = v < nv;
+  if (ok) {
+    const int x = (int)(v % d.vx);
+    const int64_t t = v / d.vx;
+    const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+    sr[row][lv] = f[row * nv + v] - stencil_row_i<T>(d, st, u, x, y, z, v, row);
   }
+  __syncthreads();
+  if (!ok) return;
+  const T zz = dinv[(3 * row) * nv + v] * sr[0][lv] + dinv[(3 * row + 1) * nv + v] * sr[1][lv] +
+               dinv[(3 * row + 2) * nv + v] * sr[2][lv];
+  const int64_t i = row * nv + v;
+  const T dn = first ? c_new * zz : c_old * dv[i] + c_new * zz;
+  dv[i] = dn;
+  uout[i] = u[i] + dn;
 }
 
 template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
                           T* out, bool residual) {
-  k_stencil_apply<T><<<nblk(d.nv, 128), 128, 0, s>>>(d, st, u, f, out, residual);
+  k_stencil_apply3<T><<<nblk(d.nv, SV), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
 }
 
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, double c_old, double c_new, bool first) {
-  k_stencil_cheb<T><<<nblk(d.nv, 128), 128, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old, (T)c_new, first);
+  k_stencil_cheb<T><<<nblk(d.nv, SV), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old, (T)c_new, first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,

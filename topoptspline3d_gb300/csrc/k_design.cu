@@ -11,6 +11,18 @@ static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) 
 
 constexpr int MAX_ORDER = 4;
 
+// v^p for the SIMP exponent: repeated products for small integer p (the
+// reference default p = 3), the general pow otherwise.
+__device__ __forceinline__ double simp_pow(double v, double p) {
+  const int ip = (int)p;
+  if ((double)ip == p && ip >= 0 && ip <= 8) {
+    double r = 1.0;
+    for (int k = 0; k < ip; ++k) r *= v;
+    return r;
+  }
+  return pow(v, p);
+}
+
 // Spline value at element (x,y,z): sum over order^3 taps of c * Nx Ny Nz, or the
 // reference's out-of-range value -0.2 (grid/Grid.cu:3396-3430).
 __device__ __forceinline__ double spline_at(const SplineDev& sp, const double* __restrict__ coeff,
@@ -46,34 +58,11 @@ __global__ void k_coeff_to_density(LevelDims d, const uint8_t* __restrict__ eact
     return;
   }
   const double v = fmin(fmax(spline_at(sp, coeff, x, y, z), rho_min), 1.0);
-  const double vp = pow(v, penal);
+  const double vp = simp_pow(v, penal);
   rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
 }
 
 constexpr int VOL_THREADS = 256;
-
-__global__ void __launch_bounds__(VOL_THREADS) k_trial_volume(LevelDims d, const uint8_t* __restrict__ eactive,
-                                                              SplineDev sp, const double* __restrict__ coeff,
-                                                              double rho_min, double* __restrict__ partial) {
-  double s = 0.0;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < d.ne; e += (int64_t)gridDim.x * blockDim.x) {
-    if (!eactive[e]) continue;
-    const int x = (int)(e % d.ex);
-    const int64_t t = e / d.ex;
-    const int y = (int)(t % d.ey), z = (int)(t / d.ey);
-    s += fmin(fmax(spline_at(sp, coeff, x, y, z), rho_min), 1.0);
-  }
-  __shared__ double ws[VOL_THREADS / 32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r = 0.0;
-    for (int w = 0; w < VOL_THREADS / 32; ++w) r += ws[w];
-    partial[blockIdx.x] = r;
-  }
-}
 
 __global__ void k_sum_partials(const double* __restrict__ partial, int nb, double* __restrict__ out) {
   __shared__ double sh[256];
@@ -88,20 +77,109 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int nb, doubl
   if (threadIdx.x == 0) *out = sh[0];
 }
 
+// Separable evaluation, pass 1: B[z][y][i] = sum_{s,t} c[i, iy+s, iz+t] Ny[y][s] Nz[z][t]
+// for every x-basis index i (0 where y or z is outside the spline range).
+__global__ void k_spline_yz(LevelDims d, SplineDev sp, const double* __restrict__ coeff,
+                            double* __restrict__ B) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nbx = sp.nb[0];
+  if (gid >= (int64_t)nbx * d.ey * d.ez) return;
+  const int i = (int)(gid % nbx);
+  const int64_t yz = gid / nbx;
+  const int y = (int)(yz % d.ey), z = (int)(yz / d.ey);
+  const int iy = sp.i0[1][y], iz = sp.i0[2][z];
+  double v = 0.0;
+  if (iy >= 0 && iz >= 0) {
+    const int k = sp.order;
+    for (int s = 0; s < k; ++s) {
+      const double ns = sp.N[1][y * k + s];
+      double a = 0.0;
+      for (int t = 0; t < k; ++t)
+        a += coeff[i + (int64_t)nbx * ((iy + s) + (int64_t)sp.nb[1] * (iz + t))] * sp.N[2][z * k + t];
+      v += ns * a;
+    }
+  }
+  B[gid] = v;
+}
+
+// Pass 2: value at element (x,y,z) = sum_r Nx[x][r] B[z][y][ix + r], or -0.2 out of range.
+__device__ __forceinline__ double spline_from_B(const SplineDev& sp, const double* __restrict__ B,
+                                                int x, int y, int z, int ey) {
+  const int ix = sp.i0[0][x];
+  if (ix < 0 || sp.i0[1][y] < 0 || sp.i0[2][z] < 0) return -0.2;
+  const int k = sp.order;
+  const double* b = B + (int64_t)sp.nb[0] * (y + (int64_t)ey * z) + ix;
+  double v = 0.0;
+  for (int r = 0; r < k; ++r) v += sp.N[0][x * k + r] * b[r];
+  return v;
+}
+
+__global__ void k_density_from_B(LevelDims d, const uint8_t* __restrict__ eactive, SplineDev sp,
+                                 const double* __restrict__ B, double rho_min, double penal,
+                                 double* __restrict__ rho, double* __restrict__ rhop, float* __restrict__ rhop32) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  if (!eactive[e]) {
+    rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
+    return;
+  }
+  const int x = (int)(e % d.ex);
+  const int64_t t = e / d.ex;
+  const int y = (int)(t % d.ey), z = (int)(t / d.ey);
+  const double v = fmin(fmax(spline_from_B(sp, B, x, y, z, d.ey), rho_min), 1.0);
+  const double vp = simp_pow(v, penal);
+  rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
+}
+
+__global__ void __launch_bounds__(VOL_THREADS) k_volume_from_B(LevelDims d, const uint8_t* __restrict__ eactive,
+                                                               SplineDev sp, const double* __restrict__ B,
+                                                               double rho_min, double* __restrict__ partial) {
+  double s = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < d.ne; e += (int64_t)gridDim.x * blockDim.x) {
+    if (!eactive[e]) continue;
+    const int x = (int)(e % d.ex);
+    const int64_t t = e / d.ex;
+    const int y = (int)(t % d.ey), z = (int)(t / d.ey);
+    s += fmin(fmax(spline_from_B(sp, B, x, y, z, d.ey), rho_min), 1.0);
+  }
+  __shared__ double ws[VOL_THREADS / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < VOL_THREADS / 32; ++w) r += ws[w];
+    partial[blockIdx.x] = r;
+  }
+}
+
 void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,
-                             double* rho, double* rhop, float* rhop32) {
-  k_coeff_to_density<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, coeff, rho_min, penal, rho, rhop,
-                                                     rhop32);
+                             double* rho, double* rhop, float* rhop32, double* Btmp) {
+  const int64_t nB = (int64_t)sp.nb[0] * d.ey * d.ez;
+  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, Btmp);
+  k_density_from_B<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, Btmp, rho_min, penal, rho, rhop, rhop32);
 }
 
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                          const SplineDev& sp, const double* coeff, double rho_min, double* partial,
-                         double* out) {
+                         double* out, double* Btmp) {
+  const int64_t nB = (int64_t)sp.nb[0] * d.ey * d.ez;
+  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, Btmp);
   int nb = (int)std::min<int64_t>(1024, (d.ne + VOL_THREADS * 4 - 1) / (VOL_THREADS * 4));
   if (nb < 1) nb = 1;
-  k_trial_volume<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, coeff, rho_min, partial);
+  k_volume_from_B<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, Btmp, rho_min, partial);
   k_sum_partials<<<1, 256, 0, s>>>(partial, nb, out);
+}
+
+// Direct (non-separable) density evaluation, kept as the cross-check of the
+// two-pass path: 27 taps per element.
+void launch_coeff_to_density_direct(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                                    const SplineDev& sp, const double* coeff, double rho_min, double penal,
+                                    double* rho, double* rhop, float* rhop32) {
+  k_coeff_to_density<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, coeff, rho_min, penal, rho, rhop,
+                                                     rhop32);
 }
 
 // Element sensitivity g_e = -p rho^(p-1) u_e^T Ke u_e (optimization/optimization.cu:96-159),
@@ -167,7 +245,7 @@ __global__ void k_sensitivity(LevelDims d, const uint8_t* __restrict__ eactive,
   }
   const double hh = 0.5 * h;
   const double q = 2.0 * hh * hh * hh * tot;  // u_e^T Ke u_e
-  sens[e] = -penal * pow(rho[e], penal - 1.0) * q;
+  sens[e] = -penal * simp_pow(rho[e], penal - 1.0) * q;
 }
 
 void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
@@ -306,7 +384,7 @@ __global__ void k_penalise(int64_t ne, const uint8_t* __restrict__ eactive, cons
                            double penal, double* __restrict__ rhop, float* __restrict__ rhop32) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
-  const double v = eactive[e] ? pow(rho[e], penal) : 0.0;
+  const double v = eactive[e] ? simp_pow(rho[e], penal) : 0.0;
   rhop[e] = v;
   rhop32[e] = (float)v;
 }

@@ -29,11 +29,19 @@ __device__ __forceinline__ double modal_c<double>(int i) { return cModal64[i]; }
 template <>
 __device__ __forceinline__ float modal_c<float>(int i) { return cModal32[i]; }
 
+// Diagonal 3x3 blocks Ke[a,a] of the eight local nodes (FP32 smoother epilogue).
+__constant__ float cKdiag32[8][9];
+
 void upload_template(const double* Ke576, double lam, double mu, double h) {
   float k32[576];
   for (int i = 0; i < 576; ++i) k32[i] = (float)Ke576[i];
   cudaMemcpyToSymbol(cKe64, Ke576, sizeof(double) * 576);
   cudaMemcpyToSymbol(cKe32, k32, sizeof(float) * 576);
+  float kd[8][9];
+  for (int a = 0; a < 8; ++a)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) kd[a][3 * i + j] = (float)Ke576[(3 * a + i) * 24 + 3 * a + j];
+  cudaMemcpyToSymbol(cKdiag32, kd, sizeof(kd));
   const double m64[5] = {lam, mu, h / 16.0, h / 48.0, h / 144.0};
   const float m32[5] = {(float)m64[0], (float)m64[1], (float)m64[2], (float)m64[3], (float)m64[4]};
   cudaMemcpyToSymbol(cModal64, m64, sizeof(m64));
@@ -139,11 +147,13 @@ __device__ __forceinline__ void modal_element(T c[3][8], T pe) {
 }
 
 // y = K(rho) u (or f - K u) on level 0.  A CTA owns a (TXE-1) x (TYE-1) column of
-// vertices over TZ vertex planes and marches in z: per element layer it stages
-// the vertex plane above in shared memory (double buffered), computes the
-// TXE x TYE elements of the layer (one per thread) into shared memory, and each
+// vertices over TZ vertex planes and marches in z.  Vertex planes are staged in
+// shared memory by asynchronous copies (cp.async, zero-filled outside the
+// domain) two planes ahead of use in a 3-slot ring; per element layer the CTA
+// computes its TXE x TYE elements (one per thread) into shared memory, and each
 // owned vertex adds its four in-layer elements' bottom-node forces to the
-// top-node forces carried in registers from the layer below.
+// top-node forces carried in registers from the layer below.  Shared arrays
+// hold one 4-vector per vertex / element node so each gather is one access.
 // MODE 0: out = K u; 1: out = f - K u; 2: one Chebyshev step, r = f - K u,
 // z = Dinv r, d = c_old d + c_new z (first: c_new z), out = u + d (out != u).
 struct ChebArgs {
@@ -153,15 +163,70 @@ struct ChebArgs {
   int first;
 };
 
+template <typename T>
+struct alignas(4 * sizeof(T)) Vec4 {
+  T x, y, z, w;
+};
+
+__device__ __forceinline__ void cp_async_4(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0));
+}
+__device__ __forceinline__ void cp_async_8(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 8 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem, bool valid) {
+  if (sizeof(T) == 4) cp_async_4(smem, gmem, valid);
+  else cp_async_8(smem, gmem, valid);
+}
+
+template <typename T, int TXE, int TYE>
+struct ModalSmem {
+  static constexpr int NT = TXE * TYE, PX = TXE + 1, PY = TYE + 1, NP = PX * PY;
+  Vec4<T> plane[3][NP];  // vertex planes (u0, u1, u2, -) in a 3-slot ring
+  Vec4<T> fe[8][NT];     // nodal forces of the layer's elements, per local node
+  T pe[NT];              // rho^p of the layer's elements (FP32 smoother diagonal)
+};
+
+// z = S^-1 r for the free-DOF part of a symmetric 3x3 block S (fixed rows and
+// columns act as identity and give z = 0), by the adjugate.
+template <typename T>
+__device__ __forceinline__ void block_solve_free(const T S_in[9], uint8_t fb, const T r[3], T z[3]) {
+  T S[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      S[3 * i + j] = (((fb >> i) & 1) && ((fb >> j) & 1)) ? S_in[3 * i + j] : (i == j ? T(1) : T(0));
+  const T a = S[0], b = S[1], c = S[2], dd = S[4], e = S[5], f = S[8];
+  const T A0 = dd * f - e * e, A1 = c * e - b * f, A2 = b * e - c * dd;
+  const T A4 = a * f - c * c, A5 = b * c - a * e, A8 = a * dd - b * b;
+  const T rd = T(1) / (a * A0 + b * A1 + c * A2);
+  T rr[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) rr[i] = ((fb >> i) & 1) ? r[i] : T(0);
+  z[0] = (A0 * rr[0] + A1 * rr[1] + A2 * rr[2]) * rd;
+  z[1] = (A1 * rr[0] + A4 * rr[1] + A5 * rr[2]) * rd;
+  z[2] = (A2 * rr[0] + A5 * rr[1] + A8 * rr[2]) * rd;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if (!((fb >> i) & 1)) z[i] = T(0);
+}
+
 template <typename T, int TXE, int TYE, int MODE>
 __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* __restrict__ rhop,
                                                          const uint8_t* __restrict__ vmask,
                                                          const T* __restrict__ u, const T* __restrict__ f,
                                                          T* __restrict__ out, int TZ, ChebArgs ch) {
-  constexpr int NT = TXE * TYE, PX = TXE + 1, PY = TYE + 1, NP = PX * PY;
-  extern __shared__ __align__(16) unsigned char modal_smem[];
-  T(*us)[3][NP] = reinterpret_cast<T(*)[3][NP]>(modal_smem);
-  T(*fe)[NT] = reinterpret_cast<T(*)[NT]>(modal_smem + sizeof(T) * 2 * 3 * NP);
+  using S = ModalSmem<T, TXE, TYE>;
+  constexpr int NT = S::NT, PX = S::PX, NP = S::NP;
+  extern __shared__ __align__(32) unsigned char modal_smem[];
+  S& sm = *reinterpret_cast<S*>(modal_smem);
   const int t = threadIdx.x, i = t % TXE, j = t / TXE;
   const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = blockIdx.z * TZ;
   const int64_t nv = d.nv;
@@ -169,23 +234,37 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
   const int zend = min(z0 + TZ, d.vz);
   T acc0 = T(0), acc1 = T(0), acc2 = T(0);
-  auto load_plane = [&](int z) {
-    const int slot = z & 1;
-    for (int k = t; k < NP; k += NT) {
-      const int px = k % PX, py = k / PX;
-      const int vx = x0 - 1 + px, vy = y0 - 1 + py;
-      T a = T(0), b = T(0), c = T(0);
-      if (vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz) {
-        const int64_t v = vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z);
-        a = u[v]; b = u[nv + v]; c = u[2 * nv + v];
+  // FP32 Chebyshev steps rebuild the diagonal block from rho^p instead of
+  // streaming a stored inverse (36 bytes per vertex); FP64 steps read the
+  // stored inverse, which is cheaper than the FP64 arithmetic.
+  constexpr bool FLY_DIAG = (MODE == 2) && (sizeof(T) == 4);
+  T pprev[4] = {T(0), T(0), T(0), T(0)};
+  // asynchronous copy of vertex plane z into its ring slot (z + 3) % 3
+  auto prefetch = [&](int z) {
+    if (z <= zend) {
+      Vec4<T>* dst = sm.plane[(z + 3) % 3];
+      for (int k = t; k < NP; k += NT) {
+        const int px = k % PX, py = k / PX;
+        const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+        const bool ok = vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz;
+        const int64_t v = ok ? vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z) : 0;
+        cp_async_elem<T>(&dst[k].x, u + v, ok);
+        cp_async_elem<T>(&dst[k].y, u + nv + v, ok);
+        cp_async_elem<T>(&dst[k].z, u + 2 * nv + v, ok);
       }
-      us[slot][0][k] = a; us[slot][1][k] = b; us[slot][2][k] = c;
     }
+    cp_async_commit();
   };
-  load_plane(z0 - 1);
+  prefetch(z0 - 1);
+  prefetch(z0);
   for (int ez = z0 - 1; ez < zend; ++ez) {
-    load_plane(ez + 1);
+    prefetch(ez + 2);
+    cp_async_wait1();
     __syncthreads();
+    // the owned vertex's own value at plane ez (Chebyshev update); read here,
+    // before the slot can be refilled by the next layer's prefetch
+    Vec4<T> uo{T(0), T(0), T(0), T(0)};
+    if (MODE == 2) uo = sm.plane[(ez + 3) % 3][(i + 1) + PX * (j + 1)];
     {
       const int ex = gx - 1, ey = gy - 1;
       T pe = T(0);
@@ -196,29 +275,31 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
           const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
-          const int slot = (ez + (a >> 2)) & 1;
-          c[0][a] = us[slot][0][k]; c[1][a] = us[slot][1][k]; c[2][a] = us[slot][2][k];
+          const Vec4<T> p = sm.plane[(ez + (a >> 2) + 3) % 3][k];
+          c[0][a] = p.x; c[1][a] = p.y; c[2][a] = p.z;
         }
         modal_element<T>(c, pe);
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          fe[3 * a][t] = c[0][a]; fe[3 * a + 1][t] = c[1][a]; fe[3 * a + 2][t] = c[2][a];
-        }
+        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<T>{c[0][a], c[1][a], c[2][a], T(0)};
       } else {
 #pragma unroll
-        for (int q = 0; q < 24; ++q) fe[q][t] = T(0);
+        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<T>{T(0), T(0), T(0), T(0)};
       }
+      if (FLY_DIAG) sm.pe[t] = pe;
     }
     __syncthreads();
     if (own) {
       T b0 = acc0, b1 = acc1, b2 = acc2, t0 = T(0), t1 = T(0), t2 = T(0);
+      T pl[4];
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int wx = w & 1, wy = w >> 1;
         const int te = (i + wx) + TXE * (j + wy);
         const int a = (1 - wx) + 2 * (1 - wy);  // bottom node of that element
-        b0 += fe[3 * a][te]; b1 += fe[3 * a + 1][te]; b2 += fe[3 * a + 2][te];
-        t0 += fe[3 * (a + 4)][te]; t1 += fe[3 * (a + 4) + 1][te]; t2 += fe[3 * (a + 4) + 2][te];
+        const Vec4<T> bo = sm.fe[a][te], to = sm.fe[a + 4][te];
+        b0 += bo.x; b1 += bo.y; b2 += bo.z;
+        t0 += to.x; t1 += to.y; t2 += to.z;
+        if (FLY_DIAG) pl[w] = sm.pe[te];
       }
       if (ez >= z0) {
         const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
@@ -237,21 +318,43 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
           T r[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] - y[c] : T(0);
-          const int k = (i + 1) + PX * (j + 1);
+          const T uv[3] = {uo.x, uo.y, uo.z};
+          T zc[3];
+          if (FLY_DIAG) {
+            // diagonal block sum_e rho^p_e Ke[a_e, a_e] from the four in-layer elements
+            // (bottom nodes) and the four of the layer below (top nodes)
+            T S[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) S[k] = T(0);
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+              const int a = (1 - (w & 1)) + 2 * (1 - (w >> 1));
+#pragma unroll
+              for (int k = 0; k < 9; ++k) S[k] += pl[w] * T(cKdiag32[a][k]) + pprev[w] * T(cKdiag32[a + 4][k]);
+            }
+            block_solve_free<T>(S, (m & 8) ? (m & 7) : 0, r, zc);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
+          }
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const T z = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] +
-                        dinv[(3 * c + 2) * nv + v] * r[2];
-            const T dn = ch.first ? T(ch.c_new) * z : T(ch.c_old) * dv[c * nv + v] + T(ch.c_new) * z;
+            const T dn = ch.first ? T(ch.c_new) * zc[c] : T(ch.c_old) * dv[c * nv + v] + T(ch.c_new) * zc[c];
             dv[c * nv + v] = dn;
-            out[c * nv + v] = us[ez & 1][c][k] + dn;
+            out[c * nv + v] = uv[c] + dn;
           }
         }
       }
       acc0 = t0; acc1 = t1; acc2 = t2;
+      if (FLY_DIAG) {
+#pragma unroll
+        for (int w = 0; w < 4; ++w) pprev[w] = pl[w];
+      }
     }
-    __syncthreads();
   }
+  // drain the (empty) trailing copy groups before the CTA exits
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 // Row block of vertex (x,y,z): out = sum over incident elements of rho^p Ke[a,:] u_e,
@@ -434,8 +537,8 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
                        const T* u, const T* f, T* out, bool residual) {
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
                   (d.vz + MODAL_TZ - 1) / MODAL_TZ);
-  constexpr int NT = MODAL_TXE * MODAL_TYE, NP = (MODAL_TXE + 1) * (MODAL_TYE + 1);
-  const size_t smem = sizeof(T) * (2 * 3 * NP + 24 * NT);
+  constexpr int NT = MODAL_TXE * MODAL_TYE;
+  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
   modal_smem_attr<T>(smem);
   ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0};
   if (residual)
@@ -450,8 +553,8 @@ void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const u
                       const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first) {
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
                   (d.vz + MODAL_TZ - 1) / MODAL_TZ);
-  constexpr int NT = MODAL_TXE * MODAL_TYE, NP = (MODAL_TXE + 1) * (MODAL_TYE + 1);
-  const size_t smem = sizeof(T) * (2 * 3 * NP + 24 * NT);
+  constexpr int NT = MODAL_TXE * MODAL_TYE;
+  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
   modal_smem_attr<T>(smem);
   ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0};
   k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, MODAL_TZ, ch);

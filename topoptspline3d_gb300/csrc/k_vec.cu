@@ -32,14 +32,17 @@ __device__ __forceinline__ double block_sum(double v) {
   return s;  // valid in thread 0
 }
 
+// Per-thread partial sums are accumulated in the vector's precision (FP32
+// vectors: a few dozen terms per thread, inside the FP32 inner solver only) and
+// combined in FP64 across threads and blocks.
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_dot_partial(const T* __restrict__ a, const T* __restrict__ b,
                                                              int64_t n, double* __restrict__ partial) {
-  double s = 0.0;
+  T s = T(0);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    s += (double)a[i] * (b ? (double)b[i] : 1.0);
-  s = block_sum(s);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    s += a[i] * (b ? b[i] : T(1));
+  const double bs = block_sum((double)s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = bs;
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_finalize_sum(const double* __restrict__ partial, int nb,
@@ -134,64 +137,71 @@ void launch_f2d_add(cudaStream_t s, const float* a, double* b, int64_t n) {
   k_f2d_add<<<nblk(n, 256), 256, 0, s>>>(a, b, n);
 }
 
-// d = z + beta d, beta = (sc[num0] - sc[num1]) / sc[den] (Polak-Ribiere), or d = z.
+// The CG step scalars are formed once by a one-thread kernel (an FP64 division
+// per vector element is expensive on this part) and read by the vector kernels.
+// sc[out] = (sc[num] - (sub >= 0 ? sc[sub] : 0)) / sc[den]
+__global__ void k_scalar_ratio(double* sc, int num, int sub, int den, int out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) sc[out] = (sc[num] - (sub >= 0 ? sc[sub] : 0.0)) / sc[den];
+}
+
+void launch_scalar_ratio(cudaStream_t s, double* sc, int num, int sub, int den, int out) {
+  k_scalar_ratio<<<1, 32, 0, s>>>(sc, num, sub, den, out);
+}
+
+// d = z + beta d (beta = sc[beta_slot]), or d = z.
 template <typename T>
 __global__ void k_pcg_dir(const T* __restrict__ z, T* __restrict__ d, const double* __restrict__ sc,
-                          int num, int den, bool first, int64_t n) {
+                          int beta_slot, bool first, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (first) { d[i] = z[i]; return; }
-  const double beta = (sc[num] - sc[num + 1]) / sc[den];
-  d[i] = (T)((double)z[i] + beta * (double)d[i]);
+  const T beta = (T)sc[beta_slot];
+  d[i] = z[i] + beta * d[i];
 }
 
 template <typename T>
-void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int num, int den, bool first,
+void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta_slot, bool first,
                     int64_t n) {
-  k_pcg_dir<T><<<nblk(n, 256), 256, 0, s>>>(z, d, sc, num, den, first, n);
+  k_pcg_dir<T><<<nblk(n, 256), 256, 0, s>>>(z, d, sc, beta_slot, first, n);
 }
 
-// alpha = sc[num]/sc[den]; rold = r; x += alpha d; r -= alpha q.
+// alpha = sc[alpha_slot]; rold = r; x += alpha d; r -= alpha q.
 template <typename T>
 __global__ void k_pcg_update(T* __restrict__ x, T* __restrict__ r, T* __restrict__ rold,
                              const T* __restrict__ d, const T* __restrict__ q,
-                             const double* __restrict__ sc, int num, int den, int64_t n) {
+                             const double* __restrict__ sc, int alpha_slot, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double alpha = sc[num] / sc[den];
+  const T alpha = (T)sc[alpha_slot];
   const T ri = r[i];
   rold[i] = ri;
-  x[i] = (T)((double)x[i] + alpha * (double)d[i]);
-  r[i] = (T)((double)ri - alpha * (double)q[i]);
+  x[i] = x[i] + alpha * d[i];
+  r[i] = ri - alpha * q[i];
 }
 
 template <typename T>
 void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
-                       int num, int den, int64_t n) {
-  k_pcg_update<T><<<nblk(n, 256), 256, 0, s>>>(x, r, rold, d, q, sc, num, den, n);
+                       int alpha_slot, int64_t n) {
+  k_pcg_update<T><<<nblk(n, 256), 256, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n);
 }
 
-// Chebyshev step: z = Dinv r (3x3 blocks), d = c_old d + c_new z (first: d = c_new z), u += d.
+// x = a * sc_scale(y) where the scale is 1/sqrt(sc[slot]) (power-iteration normalisation).
 template <typename T>
-__global__ void k_cheb_step(int64_t nv, const T* __restrict__ dinv, const T* __restrict__ r,
-                            T* __restrict__ dvec, T* __restrict__ u, T c_old, T c_new, bool first) {
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
-  const T r0 = r[v], r1 = r[nv + v], r2 = r[2 * nv + v];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const T z = dinv[(3 * i) * nv + v] * r0 + dinv[(3 * i + 1) * nv + v] * r1 + dinv[(3 * i + 2) * nv + v] * r2;
-    const T dn = first ? c_new * z : c_old * dvec[i * nv + v] + c_new * z;
-    dvec[i * nv + v] = dn;
-    u[i * nv + v] += dn;
-  }
+__global__ void k_scale_by_rnorm(const T* __restrict__ y, T* __restrict__ x, const double* __restrict__ sc,
+                                 int slot, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T s = (T)rsqrt(sc[slot]);
+  x[i] = y[i] * s;
 }
 
 template <typename T>
-void launch_cheb_step(cudaStream_t s, const LevelDims& dm, const T* dinv, const T* r, T* dvec, T* u,
-                      double c_old, double c_new, bool first) {
-  k_cheb_step<T><<<nblk(dm.nv, 256), 256, 0, s>>>(dm.nv, dinv, r, dvec, u, (T)c_old, (T)c_new, first);
+void launch_scale_by_rnorm(cudaStream_t s, const T* y, T* x, const double* sc, int slot, int64_t n) {
+  k_scale_by_rnorm<T><<<nblk(n, 256), 256, 0, s>>>(y, x, sc, slot, n);
 }
+
+template void launch_scale_by_rnorm<double>(cudaStream_t, const double*, double*, const double*, int, int64_t);
+template void launch_scale_by_rnorm<float>(cudaStream_t, const float*, float*, const double*, int, int64_t);
 
 template void launch_dot<double>(cudaStream_t, const double*, const double*, int64_t, double*, double*);
 template void launch_dot<float>(cudaStream_t, const float*, const float*, int64_t, double*, double*);
@@ -199,17 +209,11 @@ template void launch_fill<double>(cudaStream_t, double*, double, int64_t);
 template void launch_fill<float>(cudaStream_t, float*, float, int64_t);
 template void launch_copy<double>(cudaStream_t, const double*, double*, int64_t);
 template void launch_copy<float>(cudaStream_t, const float*, float*, int64_t);
-template void launch_pcg_dir<double>(cudaStream_t, const double*, double*, const double*, int, int, bool,
-                                     int64_t);
-template void launch_pcg_dir<float>(cudaStream_t, const float*, float*, const double*, int, int, bool,
-                                    int64_t);
+template void launch_pcg_dir<double>(cudaStream_t, const double*, double*, const double*, int, bool, int64_t);
+template void launch_pcg_dir<float>(cudaStream_t, const float*, float*, const double*, int, bool, int64_t);
 template void launch_pcg_update<double>(cudaStream_t, double*, double*, double*, const double*,
-                                        const double*, const double*, int, int, int64_t);
+                                        const double*, const double*, int, int64_t);
 template void launch_pcg_update<float>(cudaStream_t, float*, float*, float*, const float*, const float*,
-                                       const double*, int, int, int64_t);
-template void launch_cheb_step<double>(cudaStream_t, const LevelDims&, const double*, const double*,
-                                       double*, double*, double, double, bool);
-template void launch_cheb_step<float>(cudaStream_t, const LevelDims&, const float*, const float*, float*,
-                                      float*, double, double, bool);
+                                       const double*, int, int64_t);
 
 }  // namespace topo

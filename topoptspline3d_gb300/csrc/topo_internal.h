@@ -134,15 +134,14 @@ void launch_copy(cudaStream_t s, const T* a, T* b, int64_t n);
 void launch_d2f(cudaStream_t s, const double* a, float* b, int64_t n);
 void launch_f2d_add(cudaStream_t s, const float* a, double* b, int64_t n);
 // PCG helpers with device-resident scalars (sc: double scalar slots)
+void launch_scalar_ratio(cudaStream_t s, double* sc, int num, int sub, int den, int out);
 template <typename T>
-void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int num, int den, bool first,
-                    int64_t n);
+void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta_slot, bool first, int64_t n);
 template <typename T>
 void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q,
-                       const double* sc, int num, int den, int64_t n);
+                       const double* sc, int alpha_slot, int64_t n);
 template <typename T>
-void launch_cheb_step(cudaStream_t s, const LevelDims& dm, const T* dinv, const T* r, T* dvec, T* u,
-                      double c_old, double c_new, bool first);
+void launch_scale_by_rnorm(cudaStream_t s, const T* y, T* x, const double* sc, int slot, int64_t n);
 
 // design chain (k_design.cu)
 struct SplineDev {
@@ -165,12 +164,16 @@ struct SplineTables {
 };
 void spline_tables(int order, const int* partition, const double* bmin, const double* bmax,
                    const int* nelem, double h, SplineTables& t);
+// Two-pass separable evaluation; Btmp holds nb[0]*ey*ez doubles.
 void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,
-                             double* rho, double* rhop, float* rhop32);
+                             double* rho, double* rhop, float* rhop32, double* Btmp);
+void launch_coeff_to_density_direct(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
+                                    const SplineDev& sp, const double* coeff, double rho_min, double penal,
+                                    double* rho, double* rhop, float* rhop32);
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                          const SplineDev& sp, const double* coeff, double rho_min, double* partial,
-                         double* out);
+                         double* out, double* Btmp);
 void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                         const double* rho, const double* u, double penal, double lam, double mu,
                         double h, double* sens);

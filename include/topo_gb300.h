@@ -189,6 +189,19 @@ int topo_sensitivity(topo_handle* h);
 int topo_filter(topo_handle* h, double radius);
 /* Replaces Grid::ddensity2dcoeff_update (grid/Grid.cu:3643-3748). */
 int topo_spline_adjoint(topo_handle* h);
+/* Allocation-free spline adjoint; it has no counterpart in the reference.
+ * It does the same work as topo_spline_adjoint for callers that must not
+ * allocate device memory when they call it: a fixed memory budget, a loop that
+ * must stay out of the CUDA allocator, or memory owned by another component.
+ * sens_dev (double[ne]) and csens_dev (double[nc]) are device pointers the caller
+ * owns; work is queued on the handle's stream.  The intermediate planes
+ * (nb_x*ny*nz + nb_x*nb_y*nz doubles) live in one fixed 2097152-double (16 MiB)
+ * device array per GPU, kept until the process exits; larger problems get
+ * TOPO_E_BAD_INPUT.  No cudaMalloc/cudaFree is called.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress), so make
+ * it before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (several streams or handles at once) race. */
+int topo_spline_adjoint_noalloc(topo_handle* h, const double* sens_dev, double* csens_dev);
 /* Replaces updateCoeff (optimization/optimization.cu:589-695). */
 int topo_oc_update(topo_handle* h, const topo_oc_opts* opts, topo_oc_stats* stats);
 

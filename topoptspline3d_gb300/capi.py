@@ -37,7 +37,7 @@ EXPORTED = [
     "topo_gs_maps", "topo_profile_enable", "topo_profile_read", "topo_launch_count",
     "topo_set_operator_precision", "topo_host_alloc", "topo_host_free", "topo_design_iteration",
     "topo_element_template", "topo_plan_levels", "topo_spline_axis", "topo_plan_gs_maps",
-    "topo_timer_start", "topo_timer_stop",
+    "topo_timer_start", "topo_timer_stop", "topo_spline_adjoint_noalloc",
 ]
 
 
@@ -145,6 +145,7 @@ def load(build: bool = True):
         "topo_plan_gs_maps": (i, [i, i, i, vp, i, i, vp, sz, vp, sz, vp, ip, ip]),
         "topo_timer_start": (i, [vp]),
         "topo_timer_stop": (i, [vp, dp]),
+        "topo_spline_adjoint_noalloc": (i, [vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

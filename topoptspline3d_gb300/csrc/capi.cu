@@ -1163,6 +1163,25 @@ int topo_spline_adjoint(topo_handle* h) {
   return TOPO_OK;
 }
 
+}  // extern "C"
+
+namespace topo {
+// Read-only view of the handle state the allocation-free spline adjoint needs.
+int handle_spline_view(topo_handle* h, SplineView* out) {
+  if (!h || !out) return TOPO_E_BAD_INPUT;
+  if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");
+  out->d = h->lv[0].d;
+  out->eactive = h->lv[0].eactive;
+  out->sp = h->sd;
+  out->stream = h->stream;
+  out->device = h->cfg.device;
+  return TOPO_OK;
+}
+int handle_fail(topo_handle* h, int code, const char* msg) { return fail(h, code, "%s", msg); }
+}  // namespace topo
+
+extern "C" {
+
 int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) {
   if (!h || !o) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");

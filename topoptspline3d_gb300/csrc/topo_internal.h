@@ -185,6 +185,16 @@ void launch_spline_adjoint(cudaStream_t s, const LevelDims& d, const uint8_t* ea
                            double* tmp2);
 void launch_penalise(cudaStream_t s, int64_t ne, const uint8_t* eactive, const double* rho,
                      double penal, double* rhop, float* rhop32);
+// Handle state used by the allocation-free entry point (k_noalloc.cu).
+struct SplineView {
+  LevelDims d;
+  const uint8_t* eactive;
+  SplineDev sp;
+  cudaStream_t stream;
+  int device;
+};
+int handle_spline_view(topo_handle* h, SplineView* out);
+int handle_fail(topo_handle* h, int code, const char* msg);
 void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,
                      double damp, double step, double cmin, double cmax, double* cnew);
 void launch_maxabs(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);

@@ -53,7 +53,8 @@ enum topo_array {
   TOPO_VMASK = 10,   /* uint8[nv]    bits 0-2 DOF free, bit 3 vertex active */
   TOPO_EACTIVE = 11, /* uint8[ne]    element active mask (per level) */
   TOPO_KE = 12,      /* double[576]  element template */
-  TOPO_WORK = 13     /* double[3*nv] scratch vector (level 0): input of topo_apply_fine */
+  TOPO_WORK = 13,    /* double[3*nv] scratch vector (level 0): input of topo_apply_fine */
+  TOPO_VOLCSENS = 14 /* double[nc]   scaled d volume / d coefficient (topo_volume_csens) */
 };
 
 typedef struct topo_config {
@@ -204,6 +205,52 @@ int topo_spline_adjoint(topo_handle* h);
 int topo_spline_adjoint_noalloc(topo_handle* h, const double* sens_dev, double* csens_dev);
 /* Replaces updateCoeff (optimization/optimization.cu:589-695). */
 int topo_oc_update(topo_handle* h, const topo_oc_opts* opts, topo_oc_stats* stats);
+/* Replaces Grid::dvol2dcoeff (grid/Grid.cu:3750-3859): out_dev[nc] (device; NULL =
+ * the handle's TOPO_VOLCSENS array, reference getVolCSens) = scale * d volume /
+ * d coefficient, volume = sum(rho) / den with den the padded GS element count
+ * (refden = 1, reference volumeRatio) or the active count.  The reference reads an
+ * uninitialised d volume / d rho on this path; here it is 1/den on every active
+ * element.  Uses the SENS scratch, not SENS itself. */
+int topo_volume_csens(topo_handle* h, int refden, double scale, double* out_dev);
+
+/* --- MMA: Method of Moving Asymptotes -------------------------------------- */
+/* Replaces MMA::mma_t (optimization/mma_t.h:159-266, mma_t.cpp, mma_t.cu): Svanberg's
+ * MMA with the primal-dual interior-point subproblem, parameters a0 = 1, a = 0,
+ * c = 10, d = 1, m <= 4 constraints g_i(x) <= 0.  One cooperative kernel runs the
+ * whole subproblem per update, in FP64. */
+typedef struct topo_mma topo_mma;
+
+typedef struct topo_mma_stats {
+  int subiterations;          /* Newton steps of the subproblem (reference caps at 81) */
+  double kkt_err;             /* inf-norm of the KKT residual at the last step */
+  double step;                /* last line-search step */
+  double dx_norm;             /* |x_new - x_old|_2 */
+  int overflow;               /* 1 if the Newton-step cap was hit */
+  int converged;              /* mma_t::update's return: change < 1e-3 for more than 10 calls */
+} topo_mma_stats;
+
+/* mma_t(n, m): own CUDA stream on `device`. */
+int topo_mma_create(int n, int m, int device, topo_mma** out);
+/* MMA over the spline coefficients of h (n = coefficient count), on h's stream. */
+int topo_mma_create_for(topo_handle* h, int m, topo_mma** out);
+void topo_mma_destroy(topo_mma* mma);
+const char* topo_mma_last_error(const topo_mma* mma);
+int topo_mma_size(const topo_mma* mma, int* n, int* m);
+/* mma_t::set_constrain_amplifier (optimization/mma_t.cpp:468-472). */
+int topo_mma_set_constraint_amplifier(topo_mma* mma, double c, double d);
+/* mma_t::init(lower, upper) with per-variable host arrays or uniform bounds
+ * (optimization/mma_t.h:221-230); x starts at the midpoint of the move limits. */
+int topo_mma_init(topo_mma* mma, const double* lb, const double* ub);
+int topo_mma_init_uniform(topo_mma* mma, double lb, double ub);
+/* mma_t::update(df, dg, g) (optimization/mma_t.cpp:18-51): df_dev[n] and dg_dev[i][n]
+ * are device pointers, g[m] host values.  Blocks until the step is done. */
+int topo_mma_update(topo_mma* mma, const double* df_dev, const double* const* dg_dev, const double* g,
+                    topo_mma_stats* stats);
+/* mma_t::get_x(dst) (optimization/mma_t.cu:150-153): device-to-device copy, queued. */
+int topo_mma_get_x(topo_mma* mma, double* dst_dev);
+/* Host copies of x (blocking). */
+int topo_mma_read_x(topo_mma* mma, double* dst_host);
+int topo_mma_write_x(topo_mma* mma, const double* src_host);
 
 /* --- reference ordering -------------------------------------------------- */
 /* Reproduces Grid::enumerate_gs_subset (grid/Grid.cpp:4104-4165) with the colour of

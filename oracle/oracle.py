@@ -21,14 +21,18 @@ _NAMES = {
 }
 
 
+ORACLE_SOURCES = ("topo_oracle.cpp", "mma_oracle.cpp")
+
+
 def build_oracle(force: bool = False) -> str:
-    src = os.path.join(HERE, "topo_oracle.cpp")
-    if not force and os.path.exists(ORACLE_LIB) and os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, s) for s in ORACLE_SOURCES] + [os.path.join(HERE, "topo_oracle.h")]
+    if not force and os.path.exists(ORACLE_LIB) and all(
+            os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(s) for s in srcs):
         return ORACLE_LIB
     os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
     tmp = ORACLE_LIB + f".tmp{os.getpid()}"
     subprocess.check_call(["g++", "-O3", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
-                           "-std=c++17", "-o", tmp, src])
+                           "-std=c++17", "-o", tmp] + srcs[:-1])
     os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
 
@@ -78,6 +82,14 @@ def _load():
                                     C.c_int, C.c_int, dp]),
         "orc_gs_maps": (C.c_int, [vp, C.c_int, vp, vp, vp, vp]),
         "orc_set_chebyshev": (None, [vp, C.c_int, C.c_double, C.c_double]),
+        "orc_mma_create": (vp, [C.c_int, C.c_int]),
+        "orc_mma_destroy": (None, [vp]),
+        "orc_mma_set_constraint_amplifier": (None, [vp, C.c_double, C.c_double]),
+        "orc_mma_init": (None, [vp, dp, dp]),
+        "orc_mma_update": (C.c_int, [vp, dp, dp, dp]),
+        "orc_mma_get_x": (None, [vp, dp]),
+        "orc_mma_set_x": (None, [vp, dp]),
+        "orc_mma_get_stats": (None, [vp, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -236,3 +248,59 @@ class Oracle:
 
     def set_chebyshev(self, degree=2, lo=0.3, hi=1.1):
         self.lib.orc_set_chebyshev(self.h, degree, lo, hi)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class OracleMMA:
+    """CPU restatement of the reference MMA (optimization/mma_t.*): n variables,
+    m constraints g_i(x) <= 0, update(df, dg, g) -> converged."""
+
+    def __init__(self, n, m, lb=0.0, ub=1.0):
+        self.lib = _load()
+        self.n, self.m = n, m
+        self.h = self.lib.orc_mma_create(n, m)
+        if not self.h:
+            raise ValueError("bad MMA size")
+        self.init(lb, ub)
+
+    def init(self, lb, ub):
+        lb = np.ascontiguousarray(np.broadcast_to(np.asarray(lb, dtype=np.float64), (self.n,)))
+        ub = np.ascontiguousarray(np.broadcast_to(np.asarray(ub, dtype=np.float64), (self.n,)))
+        self.lib.orc_mma_init(self.h, _dp(lb), _dp(ub))
+
+    def set_constraint_amplifier(self, c, d):
+        self.lib.orc_mma_set_constraint_amplifier(self.h, c, d)
+
+    def update(self, df, dg, g) -> bool:
+        df = np.ascontiguousarray(df, dtype=np.float64)
+        dg = np.ascontiguousarray(np.asarray(dg, dtype=np.float64).reshape(self.m, self.n))
+        g = np.ascontiguousarray(np.asarray(g, dtype=np.float64).reshape(self.m))
+        return bool(self.lib.orc_mma_update(self.h, _dp(df), _dp(dg), _dp(g)))
+
+    @property
+    def x(self) -> np.ndarray:
+        out = np.zeros(self.n)
+        self.lib.orc_mma_get_x(self.h, _dp(out))
+        return out
+
+    @x.setter
+    def x(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        self.lib.orc_mma_set_x(self.h, _dp(v))
+
+    def stats(self) -> dict:
+        s = np.zeros(5)
+        self.lib.orc_mma_get_stats(self.h, _dp(s))
+        return {"subiterations": int(s[0]), "kkt_err": s[1], "step": s[2], "dx_norm": s[3],
+                "overflow": bool(s[4])}
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.orc_mma_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

@@ -90,6 +90,20 @@ int orc_gs_maps(const orc_problem* p, int level, int* vidmap, int* eidmap, int* 
 /* Chebyshev smoother bounds for the point-block-Jacobi-preconditioned operator. */
 void orc_set_chebyshev(orc_problem* p, int degree, double lo_frac, double hi_scale);
 
+/* MMA optimiser (mma_oracle.cpp; reference optimization/mma_t.*): n design
+ * variables, m <= ORC_MMA_MAX_M constraints g_i(x) <= 0. */
+#define ORC_MMA_MAX_M 8
+typedef struct orc_mma orc_mma;
+orc_mma* orc_mma_create(int n, int m);
+void orc_mma_destroy(orc_mma* o);
+void orc_mma_set_constraint_amplifier(orc_mma* o, double c, double d);
+void orc_mma_init(orc_mma* o, const double* lb, const double* ub);
+int orc_mma_update(orc_mma* o, const double* df, const double* dg, const double* g);
+void orc_mma_get_x(const orc_mma* o, double* x);
+void orc_mma_set_x(orc_mma* o, const double* x);
+/* sub-iterations, final KKT inf-norm, last step, |x - x_prev|_2, overflowed */
+void orc_mma_get_stats(const orc_mma* o, double* s5);
+
 enum {
   ORC_RHO = 0,     /* double[ne] */
   ORC_RHOP = 1,    /* double[ne] */

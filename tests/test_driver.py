@@ -47,3 +47,40 @@ def test_driver_modes_run(mode):
     assert r.returncode == 0, r.stderr
     c = json.loads(r.stdout.strip().splitlines()[-1])["compliance"]
     assert all(np.isfinite(c)) and c[-1] < c[0]
+
+
+def test_driver_rejects_bad_optimizer():
+    r = subprocess.run([_driver(), "--optimizer", "sqp"], capture_output=True, text=True)
+    assert r.returncode == 2 and "--optimizer" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_mma_matches_oracle_history(oracle_mod):
+    """--optimizer mma (the reference's testOrdinarySplineTopoptMMA loop) against the
+    oracle chain with the oracle MMA, 4 design iterations."""
+    from oracle.oracle import OracleMMA
+    r = subprocess.run([_driver(), "--case", "cantilever", "--nx", "16", "--ny", "8", "--nz", "8", "--lattice",
+                        "7", "5", "5", "--iters", "4", "--mode", "pcg64", "--optimizer", "mma"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    summary = json.loads(r.stdout.strip().splitlines()[-1])
+    assert summary["optimizer"] == "mma"
+    wl = workloads.cantilever(16, 8, 8, lattice=(7, 5, 5))
+    o = setup_oracle(wl)
+    nc = o.num_coeffs()
+    _, _, _, _, nge = o.gs_maps(0)
+    o.put("sens", np.where(o.get("eactive") != 0, 1e3 / nge, 0.0))
+    o.spline_adjoint()
+    dv = o.get("csens")[None, :]
+    om = OracleMMA(nc, 1, 1e-3, 1.0)
+    co = []
+    for _ in range(4):
+        o.put("coeff", om.x)
+        o.coeff_to_density()
+        vol = o.volume(True)
+        o.update_operators()
+        o.pcg(2, 2, 1e-6, 300, 1)
+        co.append(o.compliance())
+        o.sensitivity(); o.filter(2.0); o.spline_adjoint()
+        om.update(o.get("csens"), dv, [1e3 * (vol - 0.4)])
+    assert np.allclose(summary["compliance"], co, rtol=1e-6, atol=0), (summary["compliance"], co)

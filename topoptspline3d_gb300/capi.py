@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "TOPO_OK", 1: "TOPO_E_CUDA", 2: "TOPO_E_BAD_INPUT", 3: "TOPO_
                 4: "TOPO_E_NOT_CONVERGED", 5: "TOPO_E_SINGULAR", 6: "TOPO_E_NOMEM", 7: "TOPO_E_NONFINITE"}
 
 ARRAYS = {"rho": 0, "rhop": 1, "coeff": 2, "sens": 3, "csens": 4, "u": 5, "f": 6, "r": 7,
-          "stencil": 8, "kelem": 9, "vmask": 10, "eactive": 11, "ke": 12, "work": 13}
+          "stencil": 8, "kelem": 9, "vmask": 10, "eactive": 11, "ke": 12, "work": 13, "volcsens": 14}
 BYTE_ARRAYS = {"vmask", "eactive"}
 
 SOLVE_VCYCLE, SOLVE_PCG64, SOLVE_MIXED = 0, 1, 2
@@ -37,7 +37,10 @@ EXPORTED = [
     "topo_gs_maps", "topo_profile_enable", "topo_profile_read", "topo_launch_count",
     "topo_set_operator_precision", "topo_host_alloc", "topo_host_free", "topo_design_iteration",
     "topo_element_template", "topo_plan_levels", "topo_spline_axis", "topo_plan_gs_maps",
-    "topo_timer_start", "topo_timer_stop", "topo_spline_adjoint_noalloc",
+    "topo_timer_start", "topo_timer_stop", "topo_spline_adjoint_noalloc", "topo_volume_csens",
+    "topo_mma_create", "topo_mma_create_for", "topo_mma_destroy", "topo_mma_last_error", "topo_mma_size",
+    "topo_mma_set_constraint_amplifier", "topo_mma_init", "topo_mma_init_uniform", "topo_mma_update",
+    "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x",
 ]
 
 
@@ -75,6 +78,11 @@ class IterOpts(C.Structure):
 class IterStats(C.Structure):
     _fields_ = [("compliance", C.c_double), ("volume", C.c_double), ("solve", SolveStats),
                 ("oc_trials", C.c_int), ("ms", C.c_double)]
+
+
+class MmaStats(C.Structure):
+    _fields_ = [("subiterations", C.c_int), ("kkt_err", C.c_double), ("step", C.c_double),
+                ("dx_norm", C.c_double), ("overflow", C.c_int), ("converged", C.c_int)]
 
 
 class TopoError(RuntimeError):
@@ -146,6 +154,19 @@ def load(build: bool = True):
         "topo_timer_start": (i, [vp]),
         "topo_timer_stop": (i, [vp, dp]),
         "topo_spline_adjoint_noalloc": (i, [vp, vp, vp]),
+        "topo_volume_csens": (i, [vp, i, d, vp]),
+        "topo_mma_create": (i, [i, i, i, C.POINTER(vp)]),
+        "topo_mma_create_for": (i, [vp, i, C.POINTER(vp)]),
+        "topo_mma_destroy": (None, [vp]),
+        "topo_mma_last_error": (C.c_char_p, [vp]),
+        "topo_mma_size": (i, [vp, ip, ip]),
+        "topo_mma_set_constraint_amplifier": (i, [vp, d, d]),
+        "topo_mma_init": (i, [vp, dp, dp]),
+        "topo_mma_init_uniform": (i, [vp, d, d]),
+        "topo_mma_update": (i, [vp, vp, C.POINTER(vp), dp, C.POINTER(MmaStats)]),
+        "topo_mma_get_x": (i, [vp, vp]),
+        "topo_mma_read_x": (i, [vp, dp]),
+        "topo_mma_write_x": (i, [vp, dp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -417,6 +438,12 @@ class Problem:
     def spline_adjoint(self):
         self._ck(self.lib.topo_spline_adjoint(self.h))
 
+    def volume_csens(self, dst_ptr=None, scale=1.0, reference_denominator=True):
+        """scale * d volume / d coefficient into the device buffer at dst_ptr
+        (None: the handle's "volcsens" array)."""
+        self._ck(self.lib.topo_volume_csens(self.h, int(reference_denominator), scale,
+                                            C.c_void_p(dst_ptr) if dst_ptr else None))
+
     def oc_update(self, vgoal, damp=0.5, step=0.03, cmin=0.0, cmax=1.0, apply_twice=False,
                   reference_denominator=True):
         o = OcOpts(vgoal, damp, step, cmin, cmax, int(apply_twice), int(reference_denominator))
@@ -484,3 +511,115 @@ class Problem:
         return {"compliance": st.compliance, "volume": st.volume, "iterations": st.solve.iterations,
                 "vcycles": st.solve.vcycles, "relres": st.solve.relres, "solve_ms": st.solve.ms,
                 "oc_trials": st.oc_trials, "ms": st.ms, "rc": rc}
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class MMA:
+    """Method of Moving Asymptotes on the GPU (wraps ``topo_mma``; reference
+    ``MMA::mma_t``, optimization/mma_t.h).  ``MMA(n, m)`` is standalone with its own
+    stream; ``MMA.for_problem(p, m)`` optimises ``p``'s spline coefficients on its
+    stream.  ``update(df_ptr, [dg_ptr...], g)`` takes device pointers for the
+    gradients and host values for the constraints."""
+
+    def __init__(self, n=None, m=1, device=0, lb=None, ub=None, _handle=None):
+        self.lib = load()
+        self.problem = None
+        hp = C.c_void_p()
+        if _handle is not None:
+            rc = self.lib.topo_mma_create_for(_handle.h, m, C.byref(hp))
+            if rc != TOPO_OK:
+                raise TopoError(rc, self.lib.topo_last_error(_handle.h).decode())
+            self.problem = _handle
+        else:
+            rc = self.lib.topo_mma_create(int(n), int(m), int(device), C.byref(hp))
+            if rc != TOPO_OK:
+                raise TopoError(rc, "topo_mma_create failed")
+        self.h = hp
+        nn, mm = C.c_int(), C.c_int()
+        self._ck(self.lib.topo_mma_size(self.h, C.byref(nn), C.byref(mm)))
+        self.n, self.m = nn.value, mm.value
+        if lb is not None and ub is not None:
+            self.init(lb, ub)
+
+    @classmethod
+    def for_problem(cls, problem, m=1, lb=None, ub=None):
+        return cls(m=m, lb=lb, ub=ub, _handle=problem)
+
+    def _ck(self, rc):
+        if rc != TOPO_OK:
+            raise TopoError(rc, self.lib.topo_mma_last_error(self.h).decode())
+
+    def init(self, lb, ub):
+        if np.ndim(lb) == 0 and np.ndim(ub) == 0:
+            self._ck(self.lib.topo_mma_init_uniform(self.h, float(lb), float(ub)))
+        else:
+            lbv = np.ascontiguousarray(np.broadcast_to(np.asarray(lb, dtype=np.float64), (self.n,)))
+            ubv = np.ascontiguousarray(np.broadcast_to(np.asarray(ub, dtype=np.float64), (self.n,)))
+            self._ck(self.lib.topo_mma_init(self.h, _dp(lbv), _dp(ubv)))
+
+    def set_constraint_amplifier(self, c, d):
+        self._ck(self.lib.topo_mma_set_constraint_amplifier(self.h, c, d))
+
+    def update(self, df_ptr, dg_ptrs, g) -> dict:
+        dg = (C.c_void_p * self.m)(*[C.c_void_p(int(q)) for q in dg_ptrs])
+        gv = np.ascontiguousarray(np.asarray(g, dtype=np.float64).reshape(self.m))
+        st = MmaStats()
+        self._ck(self.lib.topo_mma_update(self.h, C.c_void_p(int(df_ptr)), dg, _dp(gv), C.byref(st)))
+        return {"subiterations": st.subiterations, "kkt_err": st.kkt_err, "step": st.step,
+                "dx_norm": st.dx_norm, "overflow": bool(st.overflow), "converged": bool(st.converged)}
+
+    def get_x(self, dst_ptr):
+        self._ck(self.lib.topo_mma_get_x(self.h, C.c_void_p(int(dst_ptr))))
+
+    @property
+    def x(self) -> np.ndarray:
+        out = np.zeros(self.n)
+        self._ck(self.lib.topo_mma_read_x(self.h, _dp(out)))
+        return out
+
+    @x.setter
+    def x(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        assert v.size == self.n
+        self._ck(self.lib.topo_mma_write_x(self.h, _dp(v)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.topo_mma_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mma_design_iteration(p, mma, vfrac, dvol_ptr=None, solve=None, filter_radius=2.0, vol_scale=1e3,
+                         reference_volume=True):
+    """One MMA design iteration of the spline coefficients (the loop body of the
+    reference's testOrdinarySplineTopoptMMA, utils/test_utils.cpp:1047-1186):
+    coefficients from MMA, density, operators, solve, compliance, sensitivity,
+    filter, spline adjoint, then ``mma.update`` with the volume constraint
+    ``vol_scale * (vol - vfrac) <= 0``.  ``dvol_ptr`` holds ``vol_scale * dvol/dc``
+    (default: the handle's "volcsens" array, filled by ``Problem.volume_csens``).
+    Returns compliance, volume and MMA stats."""
+    if dvol_ptr is None:
+        dvol_ptr = p.device_ptr("volcsens")
+    mma.get_x(p.device_ptr("coeff"))
+    p.coeff_to_density()
+    vol = p.volume(reference_volume)
+    p.update_operators()
+    s = dict(mode=SOLVE_PCG64, smoother=SMOOTH_GS, pre=2, post=2, rtol=1e-6, max_iter=300)
+    s.update(solve or {})
+    r = p.solve(**s)
+    c = p.compliance()
+    p.sensitivity()
+    p.filter(filter_radius)
+    p.spline_adjoint()
+    st = mma.update(p.device_ptr("csens"), [dvol_ptr], [vol_scale * (vol - vfrac)])
+    st.update({"compliance": c, "volume": vol, "iterations": r["iterations"], "relres": r["relres"]})
+    return st

@@ -200,3 +200,52 @@ inline double updateCoeff(grid::HierarchyGrid& grids, double vgoal, double damp 
   grid::check(grids.handle(), topo_oc_update(grids.handle(), &o, &s), "updateCoeff");
   return s.lambda;
 }
+
+namespace MMA {
+
+// reference MMA::mma_t (optimization/mma_t.h:159-266): the optimiser lives on the
+// GPU; gradients are device pointers, constraint values host scalars.
+class mma_t {
+ public:
+  // mma_t(ndim, nConstrain): standalone, own stream on `device`
+  mma_t(int ndim, int nconstrain, int device = 0) {
+    const int rc = topo_mma_create(ndim, nconstrain, device, &m_);
+    if (rc != TOPO_OK) throw grid::TopoError(rc, "topo_mma_create");
+  }
+  // over the spline coefficients of `grids`, on its stream
+  mma_t(grid::HierarchyGrid& grids, int nconstrain) {
+    grid::check(grids.handle(), topo_mma_create_for(grids.handle(), nconstrain, &m_), "topo_mma_create_for");
+  }
+  mma_t(const mma_t&) = delete;
+  mma_t& operator=(const mma_t&) = delete;
+  ~mma_t() { topo_mma_destroy(m_); }
+
+  void init(double lower_bound, double upper_bound) { ck(topo_mma_init_uniform(m_, lower_bound, upper_bound)); }
+  void init(const double* lower_bound, const double* upper_bound) { ck(topo_mma_init(m_, lower_bound, upper_bound)); }
+  void set_constrain_amplifier(double prefer_c, double prefer_d) {
+    ck(topo_mma_set_constraint_amplifier(m_, prefer_c, prefer_d));
+  }
+  // returns "converged" as the reference's update does (optimization/mma_t.cpp:18-51)
+  bool update(const double* dev_df, const double* const* dev_dg, const double* g) {
+    ck(topo_mma_update(m_, dev_df, dev_dg, g, &last_));
+    return last_.converged != 0;
+  }
+  void get_x(double* dst_dev) { ck(topo_mma_get_x(m_, dst_dev)); }
+  std::vector<double> get_x() {
+    int n = 0, m = 0;
+    ck(topo_mma_size(m_, &n, &m));
+    std::vector<double> x(n);
+    ck(topo_mma_read_x(m_, x.data()));
+    return x;
+  }
+  const topo_mma_stats& last_stats() const { return last_; }
+
+ private:
+  void ck(int rc) {
+    if (rc != TOPO_OK) throw grid::TopoError(rc, std::string("mma: ") + topo_mma_last_error(m_));
+  }
+  topo_mma* m_ = nullptr;
+  topo_mma_stats last_{};
+};
+
+}  // namespace MMA

@@ -4,13 +4,18 @@
 //
 //   topopt_driver [--case cantilever|mbb] [--nx N --ny N --nz N] [--iters K]
 //                 [--mode vcycle|pcg64|mixed] [--vf 0.4] [--filter 2] [--order 3]
-//                 [--lattice LX LY LZ]
+//                 [--lattice LX LY LZ] [--optimizer oc|mma]
+//
+// --optimizer mma runs the loop of TestSuit::testOrdinarySplineTopoptMMA
+// (utils/test_utils.cpp:972-1217): MMA on the coefficients with the volume
+// constraint 1e3 * (vol - vf) <= 0 and coefficient bounds [1e-3, 1].
 //
 // Prints one line per design iteration and a JSON summary line.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -23,6 +28,7 @@ struct Args {
   int nx = 48, ny = 24, nz = 24, iters = 10, order = 3;
   int lattice[3] = {13, 7, 7};
   std::string mode = "mixed";
+  std::string optimizer = "oc";
   double vf = 0.4, filter = 2.0;
 };
 
@@ -44,8 +50,10 @@ Args parse(int argc, char** argv) {
     else if (s == "--filter") a.filter = std::atof(next());
     else if (s == "--order") a.order = std::atoi(next());
     else if (s == "--lattice") { for (int k = 0; k < 3; ++k) a.lattice[k] = std::atoi(next()); }
+    else if (s == "--optimizer") a.optimizer = next();
     else { std::fprintf(stderr, "unknown argument %s\n", s.c_str()); std::exit(2); }
   }
+  if (a.optimizer != "oc" && a.optimizer != "mma") { std::fprintf(stderr, "--optimizer oc|mma\n"); std::exit(2); }
   return a;
 }
 
@@ -103,14 +111,38 @@ int main(int argc, char** argv) {
 
     std::vector<double> crec;
     double total_ms = 0;
+    const bool use_mma = a.optimizer == "mma";
+    const double vol_scale = 1e3;  // volScale, utils/test_utils.cpp:1059
+    std::unique_ptr<MMA::mma_t> mma;
+    double* dcoeff = nullptr;
+    double* dvol = nullptr;
+    if (use_mma) {
+      mma.reset(new MMA::mma_t(grids, 1));
+      mma->init(1e-3, 1.0);
+      dcoeff = static_cast<double*>(grids[0]->devicePtr(TOPO_COEFF));
+      dvol = static_cast<double*>(grids[0]->devicePtr(TOPO_VOLCSENS));
+      grid::check(grids.handle(), topo_volume_csens(grids.handle(), 1, vol_scale, nullptr), "dvol2dcoeff");
+    }
     for (int itn = 1; itn <= a.iters; ++itn) {
       const auto t0 = std::chrono::steady_clock::now();
+      double vol = 0;
+      if (use_mma) {
+        mma->get_x(dcoeff);  // setCoeff(mma.get_x())
+        grids[0]->coeff2density();
+        vol = grids[0]->volumeRatio();
+      }
       grids.update_stencil();
       topo_solve_stats st = grids.solve(so);
       const double c = grids[0]->compliance();
       computeSensitivity(grids, a.filter);
-      updateCoeff(grids, a.vf);
-      const double vol = grids[0]->volumeRatio();
+      if (use_mma) {
+        const double g = vol_scale * (vol - a.vf);
+        const double* dg[1] = {dvol};
+        mma->update(static_cast<const double*>(grids[0]->devicePtr(TOPO_CSENS)), dg, &g);
+      } else {
+        updateCoeff(grids, a.vf);
+        vol = grids[0]->volumeRatio();
+      }
       const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       total_ms += ms;
       crec.push_back(c);
@@ -118,8 +150,9 @@ int main(int argc, char** argv) {
                   st.relres, ms);
     }
     std::printf("{\"driver\": \"topopt_driver\", \"case\": \"%s\", \"grid\": [%d, %d, %d], \"iters\": %d, "
-                "\"mode\": \"%s\", \"ms_per_iter\": %.4f, \"compliance\": [",
-                a.kase.c_str(), a.nx, a.ny, a.nz, a.iters, a.mode.c_str(), total_ms / a.iters);
+                "\"mode\": \"%s\", \"optimizer\": \"%s\", \"ms_per_iter\": %.4f, \"compliance\": [",
+                a.kase.c_str(), a.nx, a.ny, a.nz, a.iters, a.mode.c_str(), a.optimizer.c_str(),
+                total_ms / a.iters);
     for (size_t k = 0; k < crec.size(); ++k) std::printf("%s%.15e", k ? ", " : "", crec[k]);
     std::printf("]}\n");
   } catch (const grid::TopoError& e) {

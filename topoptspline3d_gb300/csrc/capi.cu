@@ -55,6 +55,7 @@ struct topo_handle {
   SplineTables st;
   SplineDev sd{};
   double *coeff = nullptr, *csens = nullptr, *coeff_old = nullptr, *coeff_tmp = nullptr;
+  double* volcsens = nullptr;  // scale * d volume / d coefficient (topo_volume_csens)
   double *adj1 = nullptr, *adj2 = nullptr;
   // level-0 work vectors
   double *work = nullptr, *x = nullptr, *r = nullptr, *d = nullptr, *q = nullptr, *rold = nullptr,
@@ -719,6 +720,7 @@ int topo_set_spline(topo_handle* h, int order, const int* partition3, const doub
   const int64_t nc = (int64_t)sd.nb[0] * sd.nb[1] * sd.nb[2];
   RET(dalloc(h, &h->coeff, nc));
   RET(dalloc(h, &h->csens, nc));
+  RET(dalloc(h, &h->volcsens, nc));
   RET(dalloc(h, &h->coeff_old, nc));
   RET(dalloc(h, &h->coeff_tmp, nc));
   RET(dalloc(h, &h->adj1, (int64_t)sd.nb[0] * d0.ey * d0.ez));
@@ -755,6 +757,7 @@ static int array_info(topo_handle* h, int which, int level, void** dptr, size_t*
     case TOPO_SENS: *dptr = h->sens; *count = d0.ne; break;
     case TOPO_COEFF: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->coeff; *count = nc; break;
     case TOPO_CSENS: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->csens; *count = nc; break;
+    case TOPO_VOLCSENS: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->volcsens; *count = nc; break;
     case TOPO_U: *dptr = L.U; *count = 3 * L.d.nv; break;
     case TOPO_F: *dptr = L.F; *count = 3 * L.d.nv; break;
     case TOPO_R: *dptr = L.R; *count = 3 * L.d.nv; break;
@@ -1159,6 +1162,20 @@ int topo_spline_adjoint(topo_handle* h) {
   const DevLevel& L = h->lv[0];
   launch_spline_adjoint(h->stream, L.d, L.eactive, h->sd, h->sens, h->csens, h->adj1, h->adj2);
   count_launch(3);
+  CKL();
+  return TOPO_OK;
+}
+
+int topo_volume_csens(topo_handle* h, int refden, double scale, double* out_dev) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");
+  if (!out_dev) out_dev = h->volcsens;
+  const DevLevel& L = h->lv[0];
+  const double den = (double)(refden ? h->gs_padded_elements : h->active_elements);
+  // d volume / d rho_e = 1/den on every active element; the adjoint skips the rest
+  launch_fill<double>(h->stream, h->sens_tmp, scale / den, L.d.ne);
+  launch_spline_adjoint(h->stream, L.d, L.eactive, h->sd, h->sens_tmp, out_dev, h->adj1, h->adj2);
+  count_launch(4);
   CKL();
   return TOPO_OK;
 }

@@ -142,6 +142,49 @@ int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads);
 int topo_set_spline(topo_handle* h, int order, const int* partition3, const double* bmin3,
                     const double* bmax3);
 int topo_num_coeffs(const topo_handle* h, int* ncoeff);
+
+/* Boundary conditions from region predicates: the reference's JSON "fixedarea",
+ * "loadarea" and "force" sections (config_parser.cpp:389-455,
+ * boundary/BoundaryCondition.h) evaluated on the surface vertices of the active
+ * domain as Grid::computeProjectionMatrix does (grid/Grid.cpp:2660-2726): a
+ * surface vertex in the fixed union has all three DOFs fixed; otherwise, in the
+ * load union, its nodal force is the sum of the force fields whose region holds it. */
+enum topo_region_type {
+  TOPO_REGION_BOX = 0,        /* corners a, b */
+  TOPO_REGION_SPHERE = 1,     /* center a, radius r */
+  TOPO_REGION_HALFSPACE = 2,  /* plane through a, b, c; positive side of (b-a) x (c-a) */
+  TOPO_REGION_CYLINDER = 3    /* bottom center a, height vector b, radius r */
+};
+typedef struct topo_region {
+  int type;                   /* topo_region_type */
+  int closed;                 /* include the boundary */
+  int complement;             /* negate */
+  double a[3], b[3], c[3];
+  double r;
+} topo_region;
+enum topo_field_type {
+  TOPO_FIELD_CONST = 0,                  /* norm * direction */
+  TOPO_FIELD_RADIAL_NORM_CONST_DIR = 1,  /* amplifier*exp(-|center-p|^(2 damp)) * direction */
+  TOPO_FIELD_CONST_NORM_RADIAL_DIR = 2,  /* norm * unit(center - p) */
+  TOPO_FIELD_RADIAL_NORM_RADIAL_DIR = 3, /* amplifier*exp(-|center-p|^(2 damp)) * unit(center2 - p) */
+  TOPO_FIELD_TWIST = 4                   /* axis center -> center2, amplifier */
+};
+typedef struct topo_force_field {
+  int type;                   /* topo_field_type */
+  topo_region region;         /* where the field acts */
+  double norm, amplifier, damp_ratio;
+  double direction[3], center[3], center2[3];
+} topo_force_field;
+typedef struct topo_bc_regions {
+  double origin[3];           /* position of vertex (0,0,0) */
+  double spacing;             /* vertex spacing */
+  const topo_region* fixed; int nfixed;        /* "fixedarea" union */
+  const topo_region* load; int nload;          /* "loadarea" union */
+  const topo_force_field* force; int nforce;   /* "force" fields (summed) */
+} topo_bc_regions;
+/* Computes the per-DOF fixed mask and loads and applies them as topo_set_bc does;
+ * nfixed / nloaded (may be NULL) receive the support and load vertex counts. */
+int topo_set_bc_regions(topo_handle* h, const topo_bc_regions* spec, int* nfixed, int* nloaded);
 int topo_get_knots(const topo_handle* h, int axis, double* out, size_t count);
 
 /* --- arrays -------------------------------------------------------------- */
@@ -316,6 +359,10 @@ int topo_plan_levels(int nx, int ny, int nz, const uint8_t* eactive, int max_coa
  * N[nelem*order] basis values. */
 int topo_spline_axis(int order, int partition, double bmin, double bmax, int nelem, double h,
                      double* knots, int* i0, double* N);
+/* topo_set_bc_regions on the host: fixed[nv] and loads[3*nv] for an element box with
+ * mask eactive (NULL = all active). */
+int topo_plan_bc_regions(int nx, int ny, int nz, const uint8_t* eactive, const topo_bc_regions* spec,
+                         uint8_t* fixed, double* loads, int* nfixed, int* nloaded);
 /* Reference GS ordering of one level of the plan (see topo_gs_maps). */
 int topo_plan_gs_maps(int nx, int ny, int nz, const uint8_t* eactive, int max_coarse_elements,
                       int level, int* vidmap, size_t nvid, int* eidmap, size_t neid, int* gs_num8,

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(OUT_DIR, "libtopo_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["capi.cu", "k_fine.cu", "k_coarse.cu", "k_vec.cu", "k_design.cu", "k_noalloc.cu", "k_mma.cu"]
-CPP_SOURCES = ["host_setup.cpp"]
+CPP_SOURCES = ["host_setup.cpp", "bc_regions.cpp"]
 
 
 def _nvcc() -> str:

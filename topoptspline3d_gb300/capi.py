@@ -40,7 +40,7 @@ EXPORTED = [
     "topo_timer_start", "topo_timer_stop", "topo_spline_adjoint_noalloc", "topo_volume_csens",
     "topo_mma_create", "topo_mma_create_for", "topo_mma_destroy", "topo_mma_last_error", "topo_mma_size",
     "topo_mma_set_constraint_amplifier", "topo_mma_init", "topo_mma_init_uniform", "topo_mma_update",
-    "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x",
+    "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x", "topo_set_bc_regions", "topo_plan_bc_regions",
 ]
 
 
@@ -155,6 +155,8 @@ def load(build: bool = True):
         "topo_timer_stop": (i, [vp, dp]),
         "topo_spline_adjoint_noalloc": (i, [vp, vp, vp]),
         "topo_volume_csens": (i, [vp, i, d, vp]),
+        "topo_set_bc_regions": (i, [vp, vp, ip, ip]),
+        "topo_plan_bc_regions": (i, [i, i, i, vp, vp, vp, vp, ip, ip]),
         "topo_mma_create": (i, [i, i, i, C.POINTER(vp)]),
         "topo_mma_create_for": (i, [vp, i, C.POINTER(vp)]),
         "topo_mma_destroy": (None, [vp]),
@@ -336,6 +338,13 @@ class Problem:
         loads = np.ascontiguousarray(loads, dtype=np.float64).ravel()
         assert fixed.size == self.nv and loads.size == 3 * self.nv
         self._ck(self.lib.topo_set_bc(self.h, fixed.ctypes.data, loads.ctypes.data))
+
+    def set_bc_regions(self, spec):
+        """Boundary conditions from a parsed region spec (bc_regions.parse):
+        returns (support vertices, load vertices)."""
+        nf, nl = C.c_int(), C.c_int()
+        self._ck(self.lib.topo_set_bc_regions(self.h, C.byref(spec.c), C.byref(nf), C.byref(nl)))
+        return nf.value, nl.value
 
     def set_spline(self, order, partition, bmin, bmax):
         p = (C.c_int * 3)(*partition)

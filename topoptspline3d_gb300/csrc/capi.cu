@@ -637,6 +637,26 @@ int topo_sync(topo_handle* h) {
   return TOPO_OK;
 }
 
+int topo_set_bc_regions(topo_handle* h, const topo_bc_regions* spec, int* nfixed, int* nloaded) {
+  if (!h || !spec) return TOPO_E_BAD_INPUT;
+  if ((spec->nfixed > 0 && !spec->fixed) || (spec->nload > 0 && !spec->load) || (spec->nforce > 0 && !spec->force) ||
+      spec->nfixed < 0 || spec->nload < 0 || spec->nforce < 0 || !(spec->spacing > 0))
+    return fail(h, TOPO_E_BAD_INPUT, "bad region spec");
+  const LevelDims& d = h->lv[0].d;
+  std::vector<uint8_t> fixed(d.nv);
+  std::vector<double> loads(3 * d.nv);
+  bc_from_regions(d.ex, d.ey, d.ez, h->H.eactive[0].data(), spec, fixed.data(), loads.data(), nfixed, nloaded);
+  return topo_set_bc(h, fixed.data(), loads.data());
+}
+
+int topo_plan_bc_regions(int nx, int ny, int nz, const uint8_t* eactive, const topo_bc_regions* spec,
+                         uint8_t* fixed, double* loads, int* nfixed, int* nloaded) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || !spec || !fixed || !loads || !(spec->spacing > 0) ||
+      (spec->nfixed > 0 && !spec->fixed) || (spec->nload > 0 && !spec->load) || (spec->nforce > 0 && !spec->force))
+    return TOPO_E_BAD_INPUT;
+  return bc_from_regions(nx, ny, nz, eactive, spec, fixed, loads, nfixed, nloaded);
+}
+
 int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads) {
   if (!h || !fixed || !loads) return TOPO_E_BAD_INPUT;
   DevLevel& L = h->lv[0];

@@ -199,4 +199,8 @@ void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const doubl
                      double damp, double step, double cmin, double cmax, double* cnew);
 void launch_maxabs(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);
 
+// bc_regions.cpp: region-predicate boundary conditions (host).
+int bc_from_regions(int nx, int ny, int nz, const uint8_t* eactive, const topo_bc_regions* s, uint8_t* fixed,
+                    double* loads, int* nfixed, int* nloaded);
+
 }  // namespace topo

@@ -92,6 +92,12 @@ typedef struct topo_solve_opts {
   int cheb_degree;    /* Chebyshev polynomial degree per smoothing step */
   double cheb_lo, cheb_hi; /* Chebyshev interval [lo*lmax, hi*lmax] */
   int inner_max;      /* mode 2: FP32 iterations per preconditioner application (1 = one V-cycle) */
+  int learned;        /* mode 2: 0 off, 1 add the U-Net correction to every FP32 V-cycle
+                         (topo_unet_enable first), 2 harvest training crops (needs inner_max <= 1) */
+  double learned_stall; /* mode 2, learned = 1: drop the network for the rest of the solve after 10
+                           outer steps in a row that do not bring the best residual below
+                           learned_stall times itself (0 = 0.99), or as soon as a corrected
+                           preconditioner output fails r.z > 0 (that step keeps the plain V-cycle) */
 } topo_solve_opts;
 
 typedef struct topo_solve_stats {
@@ -99,6 +105,8 @@ typedef struct topo_solve_stats {
   int vcycles;        /* V-cycles applied (FP32 ones in mode 2) */
   double relres;      /* final FP64 relative residual */
   double ms;          /* device time of the solve */
+  int learned_applied;  /* U-Net corrections applied */
+  int learned_fallback; /* 1 if the stall rule switched back to the plain V-cycle */
 } topo_solve_stats;
 
 typedef struct topo_oc_opts {
@@ -346,6 +354,40 @@ typedef struct topo_iter_stats {
  * (utils/test_utils.cpp:928-958): update_stencil, solve (warm start), compliance,
  * computeSensitivity (sensitivity, filter, spline adjoint) and updateCoeff. */
 int topo_design_iteration(topo_handle* h, const topo_iter_opts* opts, topo_iter_stats* stats);
+
+/* --- learned preconditioner (U-Net) --------------------------------------- */
+/* A 3-level 3D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, 245,203
+ * effective parameters, bf16 weights, fp32 accumulation) corrects the FP32
+ * multigrid preconditioner of TOPO_SOLVE_MIXED: z = V(r) + rms(V(r)) N(r/rms(r),
+ * log rho).  It is trained with the library's own forward, backward and Adam
+ * kernels on crops harvested from the solver's iterates (target (e_k - z_k)/rms(z_k),
+ * e_k = u* - u_k).  The last layer starts at zero (N = 0: the plain V-cycle).
+ * No reference counterpart. */
+/* Creates the network of h with He-normal weights from `seed`. */
+int topo_unet_enable(topo_handle* h, unsigned long long seed);
+/* Parameter count of the flat fp32 layout: per layer W[cout][27][cin] then b[cout],
+ * layers L0a L0b L1a L1b L2a L2b D1a D1b D0a D0b (cin of L0a padded to 16 with
+ * channels 0-3 used, cout of D0b 16 with channels 0-2 used). */
+int topo_unet_num_params(size_t* n);
+int topo_unet_get_params(topo_handle* h, float* dst, size_t n);
+int topo_unet_set_params(topo_handle* h, const float* src, size_t n);
+/* Host-tensor passes: x [nb][Z][Y][X][4] (residual xyz, log-density), X, Y, Z
+ * multiples of 8; y [..][3] network output; loss = sum m (y - t)^2 / sum m t^2
+ * over DOFs with mask bit c set; grad [n] its parameter gradient. */
+int topo_unet_forward(topo_handle* h, int X, int Y, int Z, int nb, const float* x, float* y);
+int topo_unet_loss_grad(topo_handle* h, int X, int Y, int Z, int nb, const float* x, const float* t,
+                        const uint8_t* mask, double* loss, float* grad);
+/* Crop dataset: `capacity` crops of crop^3 vertices (crop a multiple of 8);
+ * each harvesting solve adds crops_per_iterate crops per recorded iterate. */
+int topo_unet_dataset_reserve(topo_handle* h, int capacity, int crop, int crops_per_iterate);
+int topo_unet_dataset_size(topo_handle* h, int* n);
+/* Host copy of crop `slot`: x [crop^3][4], t [crop^3][3], mask [crop^3] (crop
+ * side returned in *crop; size the arrays for the reserved side). */
+int topo_unet_dataset_get(topo_handle* h, int slot, float* x, float* t, uint8_t* mask, int* crop);
+/* `steps` Adam steps (update = 1) or evaluations (update = 0) on random batches
+ * drawn from crops [lo, hi) (hi <= 0: all); loss = mean relative loss. */
+int topo_unet_train(topo_handle* h, int steps, int batch, double lr, unsigned long long seed, int lo, int hi,
+                    int update, double* loss);
 
 /* --- host-only set-up helpers (no GPU needed) ----------------------------- */
 /* Element template (element/templateMatrix.cpp:31-99), row-major 24x24. */

@@ -41,6 +41,9 @@ EXPORTED = [
     "topo_mma_create", "topo_mma_create_for", "topo_mma_destroy", "topo_mma_last_error", "topo_mma_size",
     "topo_mma_set_constraint_amplifier", "topo_mma_init", "topo_mma_init_uniform", "topo_mma_update",
     "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x", "topo_set_bc_regions", "topo_plan_bc_regions",
+    "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
+    "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
+    "topo_unet_dataset_get",
 ]
 
 
@@ -55,11 +58,12 @@ class SolveOpts(C.Structure):
     _fields_ = [("mode", C.c_int), ("smoother", C.c_int), ("pre", C.c_int), ("post", C.c_int),
                 ("rtol", C.c_double), ("max_iter", C.c_int), ("inner_rtol", C.c_double),
                 ("cheb_degree", C.c_int), ("cheb_lo", C.c_double), ("cheb_hi", C.c_double),
-                ("inner_max", C.c_int)]
+                ("inner_max", C.c_int), ("learned", C.c_int), ("learned_stall", C.c_double)]
 
 
 class SolveStats(C.Structure):
-    _fields_ = [("iterations", C.c_int), ("vcycles", C.c_int), ("relres", C.c_double), ("ms", C.c_double)]
+    _fields_ = [("iterations", C.c_int), ("vcycles", C.c_int), ("relres", C.c_double), ("ms", C.c_double),
+                ("learned_applied", C.c_int), ("learned_fallback", C.c_int)]
 
 
 class OcOpts(C.Structure):
@@ -155,6 +159,16 @@ def load(build: bool = True):
         "topo_timer_stop": (i, [vp, dp]),
         "topo_spline_adjoint_noalloc": (i, [vp, vp, vp]),
         "topo_volume_csens": (i, [vp, i, d, vp]),
+        "topo_unet_enable": (i, [vp, C.c_ulonglong]),
+        "topo_unet_num_params": (i, [C.POINTER(sz)]),
+        "topo_unet_get_params": (i, [vp, vp, sz]),
+        "topo_unet_set_params": (i, [vp, vp, sz]),
+        "topo_unet_forward": (i, [vp, i, i, i, i, vp, vp]),
+        "topo_unet_loss_grad": (i, [vp, i, i, i, i, vp, vp, vp, dp, vp]),
+        "topo_unet_dataset_reserve": (i, [vp, i, i, i]),
+        "topo_unet_dataset_size": (i, [vp, ip]),
+        "topo_unet_dataset_get": (i, [vp, i, vp, vp, vp, ip]),
+        "topo_unet_train": (i, [vp, i, i, d, C.c_ulonglong, i, i, i, dp]),
         "topo_set_bc_regions": (i, [vp, vp, ip, ip]),
         "topo_plan_bc_regions": (i, [i, i, i, vp, vp, vp, vp, ip, ip]),
         "topo_mma_create": (i, [i, i, i, C.POINTER(vp)]),
@@ -419,14 +433,81 @@ class Problem:
         return rr.value
 
     def solve(self, mode=SOLVE_PCG64, smoother=SMOOTH_GS, pre=2, post=2, rtol=1e-6, max_iter=200,
-              inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1, check=True):
+              inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1, learned=0,
+              learned_stall=0.0, check=True):
         o = SolveOpts(mode, smoother, pre, post, rtol, max_iter, inner_rtol, cheb_degree, cheb_lo, cheb_hi,
-                      inner_max)
+                      inner_max, learned, learned_stall)
         s = SolveStats()
         rc = self.lib.topo_solve(self.h, C.byref(o), C.byref(s))
         if check:
             self._ck(rc)
-        return {"iterations": s.iterations, "vcycles": s.vcycles, "relres": s.relres, "ms": s.ms, "rc": rc}
+        return {"iterations": s.iterations, "vcycles": s.vcycles, "relres": s.relres, "ms": s.ms, "rc": rc,
+                "learned_applied": s.learned_applied, "learned_fallback": bool(s.learned_fallback)}
+
+    # --- learned preconditioner
+
+    def unet_enable(self, seed=1):
+        self._ck(self.lib.topo_unet_enable(self.h, seed))
+
+    @staticmethod
+    def unet_num_params() -> int:
+        n = C.c_size_t()
+        _ck_free(load().topo_unet_num_params(C.byref(n)), "topo_unet_num_params")
+        return n.value
+
+    def unet_params(self) -> np.ndarray:
+        n = self.unet_num_params()
+        out = np.zeros(n, dtype=np.float32)
+        self._ck(self.lib.topo_unet_get_params(self.h, out.ctypes.data, n))
+        return out
+
+    def unet_set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._ck(self.lib.topo_unet_set_params(self.h, p.ctypes.data, p.size))
+
+    def unet_forward(self, x):
+        """x [nb, Z, Y, X, 4] float32 -> [nb, Z, Y, X, 3]."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        nb, Z, Y, X, _ = x.shape
+        y = np.zeros((nb, Z, Y, X, 3), dtype=np.float32)
+        self._ck(self.lib.topo_unet_forward(self.h, X, Y, Z, nb, x.ctypes.data, y.ctypes.data))
+        return y
+
+    def unet_loss_grad(self, x, t, m):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        m = np.ascontiguousarray(m, dtype=np.uint8)
+        nb, Z, Y, X, _ = x.shape
+        g = np.zeros(self.unet_num_params(), dtype=np.float32)
+        loss = C.c_double()
+        self._ck(self.lib.topo_unet_loss_grad(self.h, X, Y, Z, nb, x.ctypes.data, t.ctypes.data, m.ctypes.data,
+                                              C.byref(loss), g.ctypes.data))
+        return loss.value, g
+
+    def unet_dataset_reserve(self, capacity, crop=32, crops_per_iterate=64):
+        self._ck(self.lib.topo_unet_dataset_reserve(self.h, capacity, crop, crops_per_iterate))
+
+    def unet_dataset_size(self) -> int:
+        n = C.c_int()
+        self._ck(self.lib.topo_unet_dataset_size(self.h, C.byref(n)))
+        return n.value
+
+    def unet_dataset_get(self, slot, crop=32):
+        per = crop ** 3
+        x = np.zeros((per, 4), dtype=np.float32)
+        t = np.zeros((per, 3), dtype=np.float32)
+        m = np.zeros(per, dtype=np.uint8)
+        side = C.c_int()
+        self._ck(self.lib.topo_unet_dataset_get(self.h, slot, x.ctypes.data, t.ctypes.data, m.ctypes.data,
+                                                C.byref(side)))
+        assert side.value == crop
+        s3 = (crop, crop, crop)
+        return x.reshape(s3 + (4,)), t.reshape(s3 + (3,)), m.reshape(s3)
+
+    def unet_train(self, steps, batch=8, lr=1e-3, seed=1, lo=0, hi=0, update=True) -> float:
+        loss = C.c_double()
+        self._ck(self.lib.topo_unet_train(self.h, steps, batch, lr, seed, lo, hi, int(update), C.byref(loss)))
+        return loss.value
 
     def compliance(self) -> float:
         c = C.c_double()
@@ -505,12 +586,14 @@ class Problem:
 
     def design_iteration(self, solve=None, oc=None, filter_radius=2.0):
         s = dict(mode=SOLVE_MIXED, smoother=SMOOTH_GS, pre=2, post=2, rtol=1e-6, max_iter=200,
-                 inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1)
+                 inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1, learned=0,
+                 learned_stall=0.0)
         s.update(solve or {})
         c = dict(vgoal=0.4, damp=0.5, step=0.03, cmin=0.0, cmax=1.0, apply_twice=0, reference_volume=1)
         c.update(oc or {})
         o = IterOpts(SolveOpts(s["mode"], s["smoother"], s["pre"], s["post"], s["rtol"], s["max_iter"],
-                               s["inner_rtol"], s["cheb_degree"], s["cheb_lo"], s["cheb_hi"], s["inner_max"]),
+                               s["inner_rtol"], s["cheb_degree"], s["cheb_lo"], s["cheb_hi"], s["inner_max"],
+                               s["learned"], s["learned_stall"]),
                      OcOpts(c["vgoal"], c["damp"], c["step"], c["cmin"], c["cmax"], int(c["apply_twice"]),
                             int(c["reference_volume"])), filter_radius)
         st = IterStats()
@@ -519,7 +602,8 @@ class Problem:
             self._ck(rc)
         return {"compliance": st.compliance, "volume": st.volume, "iterations": st.solve.iterations,
                 "vcycles": st.solve.vcycles, "relres": st.solve.relres, "solve_ms": st.solve.ms,
-                "oc_trials": st.oc_trials, "ms": st.ms, "rc": rc}
+                "oc_trials": st.oc_trials, "ms": st.ms, "rc": rc,
+                "learned_applied": st.solve.learned_applied, "learned_fallback": bool(st.solve.learned_fallback)}
 
 
 def _dp(a):

@@ -35,6 +35,8 @@ struct EventPair {
 
 struct topo_handle {
   topo_config cfg{};
+  topo::UNetState* unet = nullptr;  // learned preconditioner (topo_unet_enable)
+  int unet_crops = 64;              // crops per harvested iterate
   cudaStream_t stream = nullptr;
   std::string err;
   Hierarchy H;
@@ -602,6 +604,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
 void topo_destroy(topo_handle* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->unet) unet_free(h->unet);
   for (void* p : h->allocs) cudaFree(p);
   for (int f = 0; f < TOPO_K_COUNT; ++f)
     for (auto& e : h->evs[f]) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
@@ -1060,17 +1063,65 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     float* b32 = reinterpret_cast<float*>(h->work);
     int it = 0, nvc = 0;
     double rel = 0;
+    // learned correction (1) or harvesting (2)
+    if (o->learned < 0 || o->learned > 2) return fail(h, TOPO_E_BAD_INPUT, "learned must be 0, 1 or 2");
+    if (o->learned && !h->unet) return fail(h, TOPO_E_STATE, "learned preconditioner not enabled (topo_unet_enable)");
+    if (o->learned == 2 && inner_max > 1) return fail(h, TOPO_E_BAD_INPUT, "harvesting needs inner_max <= 1");
+    bool net_on = o->learned == 1;
+    const bool harvest = o->learned == 2;
+    const double stall = o->learned_stall > 0 ? o->learned_stall : 0.99;
+    double rbest = -1;  // best outer residual norm so far
+    int since_best = 0;  // outer steps without progress on rbest
+    if (o->learned) {
+      const cudaError_t e = unet_prepare(h->unet, h->stream, L0.d, L0.eactive, h->rho, h->cfg.min_density);
+      if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "U-Net set-up: %s", cudaGetErrorString(e));
+    }
+    auto net = [&](const float* r32, float* z32) -> int {
+      if (!net_on) return TOPO_OK;
+      const cudaError_t e = unet_apply(h->unet, h->stream, L0.d, L0.vmask, r32, z32, h->partial);
+      if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "U-Net apply: %s", cudaGetErrorString(e));
+      ++st.learned_applied;
+      return TOPO_OK;
+    };
     auto prec32 = [&](const float* r, float* z) -> int {
       (void)z;
       ++nvc;
-      return vcycle_prec<float>(h, r, o->pre, o->post, o->smoother, cp);
+      RET(vcycle_prec<float>(h, r, o->pre, o->post, o->smoother, cp));
+      return net(r, L0.U32);
     };
     auto prec = [&](const double* r, double* z) -> int {
+      const double rn = std::sqrt(h->hsc[S_RR]);
+      // Fall back to the plain V-cycle for the rest of the solve when the
+      // positivity guard fired (r.z <= 0 with the correction), or after 10
+      // outer steps in a row that do not bring the best residual down by the
+      // factor `stall` (CG residual norms are not monotone).
+      if (rbest < 0 || rn < stall * rbest) {
+        rbest = rbest < 0 ? rn : std::min(rbest, rn);
+        since_best = 0;
+      } else {
+        ++since_best;
+      }
+      if (net_on) {
+        int rej = 0;
+        if (st.learned_applied > 0) {
+          const cudaError_t e = unet_rejected(h->unet, h->stream, &rej);
+          if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "U-Net guard: %s", cudaGetErrorString(e));
+        }
+        if (rej || since_best >= 10) {
+          net_on = false;
+          st.learned_fallback = 1;
+        }
+      }
       if (inner_max <= 1) {
         launch_d2f(h->stream, r, L0.F32, n3);
         CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3, h->stream));
         ++nvc;
         vcycle_core<float>(h, o->pre, o->post, true, o->smoother, cp);
+        RET(net(L0.F32, L0.U32));
+        if (harvest && rn > 1e-4 * fn) {
+          const cudaError_t e = unet_harvest_record(h->unet, h->stream, n3, r, L0.U32, h->x, 8);
+          if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "harvest: %s", cudaGetErrorString(e));
+        }
         k_to_double<float><<<nb256(n3), 256, 0, h->stream>>>(n3, L0.U32, z);
         count_launch(2);
         return TOPO_OK;
@@ -1094,6 +1145,10 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     CK(cudaMemcpyAsync(L0.F, h->f, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(L0.U, h->x, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     if (rc != TOPO_OK) return rc;
+    if (harvest) {
+      const cudaError_t e = unet_harvest_finish(h->unet, h->stream, L0.d, L0.vmask, h->x, h->unet_crops, h->partial);
+      if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "harvest: %s", cudaGetErrorString(e));
+    }
     st.iterations = it;
     st.vcycles = nvc;
   } else {
@@ -1183,6 +1238,104 @@ int topo_spline_adjoint(topo_handle* h) {
   launch_spline_adjoint(h->stream, L.d, L.eactive, h->sd, h->sens, h->csens, h->adj1, h->adj2);
   count_launch(3);
   CKL();
+  return TOPO_OK;
+}
+
+int topo_unet_enable(topo_handle* h, unsigned long long seed) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (h->unet) { unet_free(h->unet); h->unet = nullptr; }
+  const cudaError_t e = unet_create(&h->unet, h->stream, seed);
+  if (e != cudaSuccess) { h->unet = nullptr; return fail(h, e == cudaErrorMemoryAllocation ? TOPO_E_NOMEM : TOPO_E_CUDA, "U-Net: %s", cudaGetErrorString(e)); }
+  return TOPO_OK;
+}
+
+int topo_unet_num_params(size_t* n) {
+  if (!n) return TOPO_E_BAD_INPUT;
+  *n = unet_param_count();
+  return TOPO_OK;
+}
+
+static int unet_ready(topo_handle* h) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (!h->unet) return fail(h, TOPO_E_STATE, "learned preconditioner not enabled (topo_unet_enable)");
+  return TOPO_OK;
+}
+
+int topo_unet_get_params(topo_handle* h, float* dst, size_t n) {
+  RET(unet_ready(h));
+  if (!dst || n != unet_param_count()) return fail(h, TOPO_E_BAD_INPUT, "expected %zu parameters", unet_param_count());
+  CK(unet_get_params(h->unet, h->stream, dst));
+  return TOPO_OK;
+}
+
+int topo_unet_set_params(topo_handle* h, const float* src, size_t n) {
+  RET(unet_ready(h));
+  if (!src || n != unet_param_count()) return fail(h, TOPO_E_BAD_INPUT, "expected %zu parameters", unet_param_count());
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(src[i])) return fail(h, TOPO_E_BAD_INPUT, "non-finite parameter %zu", i);
+  CK(unet_set_params(h->unet, h->stream, src));
+  return TOPO_OK;
+}
+
+static int unet_dims_ok(topo_handle* h, int X, int Y, int Z, int nb) {
+  if (X <= 0 || Y <= 0 || Z <= 0 || nb <= 0 || X % 8 || Y % 8 || Z % 8 || (int64_t)nb * X * Y * Z > (1LL << 27))
+    return fail(h, TOPO_E_BAD_INPUT, "U-Net tensor dims must be positive multiples of 8");
+  return TOPO_OK;
+}
+
+int topo_unet_forward(topo_handle* h, int X, int Y, int Z, int nb, const float* x, float* y) {
+  RET(unet_ready(h));
+  RET(unet_dims_ok(h, X, Y, Z, nb));
+  if (!x || !y) return TOPO_E_BAD_INPUT;
+  CK(unet_host_pass(h->unet, h->stream, X, Y, Z, nb, x, nullptr, nullptr, y, nullptr, nullptr));
+  return TOPO_OK;
+}
+
+int topo_unet_loss_grad(topo_handle* h, int X, int Y, int Z, int nb, const float* x, const float* t,
+                        const uint8_t* mask, double* loss, float* grad) {
+  RET(unet_ready(h));
+  RET(unet_dims_ok(h, X, Y, Z, nb));
+  if (!x || !t || !mask || !loss || !grad) return TOPO_E_BAD_INPUT;
+  CK(unet_host_pass(h->unet, h->stream, X, Y, Z, nb, x, t, mask, nullptr, loss, grad));
+  return TOPO_OK;
+}
+
+int topo_unet_dataset_reserve(topo_handle* h, int capacity, int crop, int crops_per_iterate) {
+  RET(unet_ready(h));
+  if (capacity <= 0 || crop <= 0 || crop % 8 || crop > 64 || crops_per_iterate <= 0 || crops_per_iterate > 4096)
+    return fail(h, TOPO_E_BAD_INPUT, "dataset: capacity > 0, crop a multiple of 8 up to 64, 1..4096 crops per iterate");
+  const cudaError_t e = unet_dataset_reserve(h->unet, capacity, crop);
+  if (e == cudaErrorInvalidValue) return fail(h, TOPO_E_STATE, "dataset already reserved");
+  if (e != cudaSuccess) return fail(h, TOPO_E_NOMEM, "dataset: %s", cudaGetErrorString(e));
+  h->unet_crops = crops_per_iterate;
+  return TOPO_OK;
+}
+
+int topo_unet_dataset_size(topo_handle* h, int* n) {
+  RET(unet_ready(h));
+  if (!n) return TOPO_E_BAD_INPUT;
+  *n = unet_dataset_count(h->unet);
+  return TOPO_OK;
+}
+
+int topo_unet_dataset_get(topo_handle* h, int slot, float* x, float* t, uint8_t* mask, int* crop) {
+  RET(unet_ready(h));
+  if (!x || !t || !mask || !crop) return TOPO_E_BAD_INPUT;
+  *crop = unet_crop_side(h->unet);
+  const cudaError_t e = unet_dataset_get(h->unet, h->stream, slot, x, t, mask);
+  if (e == cudaErrorInvalidValue) return fail(h, TOPO_E_BAD_INPUT, "no crop %d", slot);
+  if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "dataset: %s", cudaGetErrorString(e));
+  return TOPO_OK;
+}
+
+int topo_unet_train(topo_handle* h, int steps, int batch, double lr, unsigned long long seed, int lo, int hi,
+                    int update, double* loss) {
+  RET(unet_ready(h));
+  if (!loss || steps <= 0 || steps > 65536 || batch <= 0 || batch > 64 || !(lr > 0))
+    return fail(h, TOPO_E_BAD_INPUT, "train: 1..65536 steps, batch 1..64, lr > 0");
+  if (unet_dataset_count(h->unet) == 0) return fail(h, TOPO_E_STATE, "no harvested crops");
+  const cudaError_t e = unet_train(h->unet, h->stream, steps, batch, lr, seed, lo, hi, update != 0, loss);
+  if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "train: %s", cudaGetErrorString(e));
   return TOPO_OK;
 }
 

@@ -203,4 +203,29 @@ void launch_maxabs(cudaStream_t s, const double* a, int64_t n, double* partial, 
 int bc_from_regions(int nx, int ny, int nz, const uint8_t* eactive, const topo_bc_regions* s, uint8_t* fixed,
                     double* loads, int* nfixed, int* nloaded);
 
+// unet.cu: learned preconditioner (U-Net) state, training and application.
+struct UNetState;
+size_t unet_param_count();
+cudaError_t unet_create(UNetState** out, cudaStream_t s, uint64_t seed);
+void unet_free(UNetState* u);
+cudaError_t unet_set_params(UNetState* u, cudaStream_t s, const float* host);
+cudaError_t unet_get_params(UNetState* u, cudaStream_t s, float* host);
+cudaError_t unet_prepare(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* rho,
+                         double rho_min);
+cudaError_t unet_apply(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* vmask, const float* r, float* z,
+                       double* partial);
+cudaError_t unet_rejected(UNetState* u, cudaStream_t s, int* out);
+cudaError_t unet_harvest_record(UNetState* u, cudaStream_t s, int64_t n3, const double* r, const float* z,
+                                const double* x, int cap);
+cudaError_t unet_harvest_finish(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* vmask,
+                                const double* ustar, int crops_per_iterate, double* partial);
+cudaError_t unet_dataset_reserve(UNetState* u, int cap, int S);
+int unet_dataset_count(const UNetState* u);
+int unet_crop_side(const UNetState* u);
+cudaError_t unet_dataset_get(UNetState* u, cudaStream_t s, int slot, float* x, float* t, uint8_t* m);
+cudaError_t unet_train(UNetState* u, cudaStream_t s, int steps, int batch, double lr, uint64_t seed, int lo, int hi,
+                       bool update, double* loss_out);
+cudaError_t unet_host_pass(UNetState* u, cudaStream_t s, int X, int Y, int Z, int nb, const float* x, const float* t,
+                           const uint8_t* m, float* y, double* loss, float* grad);
+
 }  // namespace topo

@@ -110,3 +110,16 @@ def ellipsoid_union(nx, ny, nz, n=12, seed=4000, fill=(0.43, 0.47), axes=(20, 12
             break
         scale *= (0.45 / max(f, 1e-3)) ** (1 / 3)
     return m.astype(np.uint8)
+
+
+def random_density(nx, ny, nz, seed, sigma=None, lo=1e-3) -> np.ndarray:
+    """Seeded Gaussian-smoothed white noise, affinely mapped to mean 0.5 and
+    spread 0.35 and clipped to [lo, 1] (the learned preconditioner's training
+    densities).  sigma defaults to a seeded draw in [3, 6] voxels."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    if sigma is None:
+        sigma = rng.uniform(3.0, 6.0)
+    g = gaussian_filter(rng.standard_normal((nz, ny, nx)), sigma, mode="wrap")
+    g = (g - g.mean()) / max(g.std(), 1e-12)
+    return np.clip(0.5 + 0.35 * g, lo, 1.0).ravel()

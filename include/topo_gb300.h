@@ -54,7 +54,9 @@ enum topo_array {
   TOPO_EACTIVE = 11, /* uint8[ne]    element active mask (per level) */
   TOPO_KE = 12,      /* double[576]  element template */
   TOPO_WORK = 13,    /* double[3*nv] scratch vector (level 0): input of topo_apply_fine */
-  TOPO_VOLCSENS = 14 /* double[nc]   scaled d volume / d coefficient (topo_volume_csens) */
+  TOPO_VOLCSENS = 14, /* double[nc]  scaled d volume / d coefficient (topo_volume_csens) */
+  TOPO_MULTI_F = 15,  /* double[cap*3*nv] right-hand sides of topo_solve_multi (after topo_multi_reserve) */
+  TOPO_MULTI_U = 16   /* double[cap*3*nv] solutions / initial guesses of topo_solve_multi */
 };
 
 typedef struct topo_config {
@@ -354,6 +356,28 @@ typedef struct topo_iter_stats {
  * (utils/test_utils.cpp:928-958): update_stencil, solve (warm start), compliance,
  * computeSensitivity (sensitivity, filter, spline adjoint) and updateCoeff. */
 int topo_design_iteration(topo_handle* h, const topo_iter_opts* opts, topo_iter_stats* stats);
+
+/* --- many load cases in one solve ------------------------------------------ */
+/* Multi-right-hand-side solve (config "batched": many load cases as right-hand
+ * sides of one V-cycle; no reference counterpart).  Every FP32 V-cycle launch
+ * and every FP64 operator application processes all right-hand sides at once:
+ * the operator data (rho^p, masks, stencils, coarsest inverse) is read once per
+ * launch for the whole batch, and each right-hand side has its own flexible-CG
+ * scalars (a converged one is frozen).  Right-hand sides live in TOPO_MULTI_F,
+ * solutions (and initial guesses) in TOPO_MULTI_U, each [cap][3][nv]. */
+typedef struct topo_multi_stats {
+  int iterations;     /* outer FP64 flexible-CG iterations (the slowest right-hand side) */
+  int vcycles;        /* batched FP32 V-cycles */
+  double max_relres;  /* largest final FP64 relative residual */
+  double ms;          /* device time */
+} topo_multi_stats;
+/* Allocates the batched buffers for up to `capacity` right-hand sides. */
+int topo_multi_reserve(topo_handle* h, int capacity);
+/* Solves the first nrhs right-hand sides with TOPO_SOLVE_MIXED and the Chebyshev
+ * smoother (opts->mode / smoother / inner_max must be MIXED / CHEBYSHEV / <= 1);
+ * relres (may be NULL) receives nrhs final FP64 relative residuals. */
+int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* opts, topo_multi_stats* stats,
+                     double* relres);
 
 /* --- learned preconditioner (U-Net) --------------------------------------- */
 /* A 3-level 3D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, 245,203

@@ -19,7 +19,8 @@ STATUS_NAMES = {0: "TOPO_OK", 1: "TOPO_E_CUDA", 2: "TOPO_E_BAD_INPUT", 3: "TOPO_
                 4: "TOPO_E_NOT_CONVERGED", 5: "TOPO_E_SINGULAR", 6: "TOPO_E_NOMEM", 7: "TOPO_E_NONFINITE"}
 
 ARRAYS = {"rho": 0, "rhop": 1, "coeff": 2, "sens": 3, "csens": 4, "u": 5, "f": 6, "r": 7,
-          "stencil": 8, "kelem": 9, "vmask": 10, "eactive": 11, "ke": 12, "work": 13, "volcsens": 14}
+          "stencil": 8, "kelem": 9, "vmask": 10, "eactive": 11, "ke": 12, "work": 13, "volcsens": 14, "multi_f": 15,
+          "multi_u": 16}
 BYTE_ARRAYS = {"vmask", "eactive"}
 
 SOLVE_VCYCLE, SOLVE_PCG64, SOLVE_MIXED = 0, 1, 2
@@ -43,7 +44,7 @@ EXPORTED = [
     "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x", "topo_set_bc_regions", "topo_plan_bc_regions",
     "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
-    "topo_unet_dataset_get",
+    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi",
 ]
 
 
@@ -82,6 +83,10 @@ class IterOpts(C.Structure):
 class IterStats(C.Structure):
     _fields_ = [("compliance", C.c_double), ("volume", C.c_double), ("solve", SolveStats),
                 ("oc_trials", C.c_int), ("ms", C.c_double)]
+
+
+class MultiStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("vcycles", C.c_int), ("max_relres", C.c_double), ("ms", C.c_double)]
 
 
 class MmaStats(C.Structure):
@@ -160,6 +165,8 @@ def load(build: bool = True):
         "topo_spline_adjoint_noalloc": (i, [vp, vp, vp]),
         "topo_volume_csens": (i, [vp, i, d, vp]),
         "topo_unet_enable": (i, [vp, C.c_ulonglong]),
+        "topo_multi_reserve": (i, [vp, i]),
+        "topo_solve_multi": (i, [vp, i, C.POINTER(SolveOpts), C.POINTER(MultiStats), dp]),
         "topo_unet_num_params": (i, [C.POINTER(sz)]),
         "topo_unet_get_params": (i, [vp, vp, sz]),
         "topo_unet_set_params": (i, [vp, vp, sz]),
@@ -443,6 +450,36 @@ class Problem:
             self._ck(rc)
         return {"iterations": s.iterations, "vcycles": s.vcycles, "relres": s.relres, "ms": s.ms, "rc": rc,
                 "learned_applied": s.learned_applied, "learned_fallback": bool(s.learned_fallback)}
+
+    # --- many load cases
+
+    def multi_reserve(self, capacity):
+        self._ck(self.lib.topo_multi_reserve(self.h, capacity))
+        self._multi_cap = capacity
+
+    def solve_multi(self, F, U0=None, pre=2, post=2, rtol=1e-6, max_iter=200, cheb_degree=2, cheb_lo=0.3,
+                    cheb_hi=1.1, check=True):
+        """F [nrhs][3*nv] host right-hand sides -> (U [nrhs][3*nv], stats, relres[nrhs])."""
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        nrhs = F.shape[0]
+        cap = self._multi_cap
+        full = np.zeros((cap, 3 * self.nv))
+        full[:nrhs] = F
+        self.put("multi_f", full.ravel())
+        u = np.zeros((cap, 3 * self.nv))
+        if U0 is not None:
+            u[:nrhs] = U0
+        self.put("multi_u", u.ravel())
+        o = SolveOpts(SOLVE_MIXED, SMOOTH_CHEBYSHEV, pre, post, rtol, max_iter, 0.1, cheb_degree, cheb_lo, cheb_hi,
+                      1, 0, 0.0)
+        st = MultiStats()
+        rel = np.zeros(nrhs)
+        rc = self.lib.topo_solve_multi(self.h, nrhs, C.byref(o), C.byref(st), rel.ctypes.data_as(C.POINTER(C.c_double)))
+        if check:
+            self._ck(rc)
+        U = self.get("multi_u").reshape(cap, 3 * self.nv)[:nrhs].copy()
+        return U, {"iterations": st.iterations, "vcycles": st.vcycles, "max_relres": st.max_relres, "ms": st.ms,
+                   "rc": rc}, rel
 
     # --- learned preconditioner
 

@@ -2,6 +2,7 @@
 // orchestration of the hot path (operator update, V-cycle, PCG, mixed-precision
 // defect correction, sensitivity chain and OC bisection).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -36,6 +37,8 @@ struct EventPair {
 struct topo_handle {
   topo_config cfg{};
   topo::UNetState* unet = nullptr;  // learned preconditioner (topo_unet_enable)
+  int nb = 1;                       // right-hand sides the level vectors hold (multi-RHS solve)
+  topo::MultiRhs* multi = nullptr;  // batched buffers (topo_multi_reserve)
   int unet_crops = 64;              // crops per harvested iterate
   cudaStream_t stream = nullptr;
   std::string err;
@@ -198,10 +201,10 @@ void level_apply(topo_handle* h, int l, const T* u, const T* f, T* out, bool res
   DevLevel& L = h->lv[l];
   if (l == 0) {
     EventPair* ev = prof_begin(h, P<T>::fam_apply);
-    launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual);
+    launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual, h->nb);
     prof_end(h, ev);
   } else {
-    launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual);
+    launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual, h->nb);
   }
   count_launch();
 }
@@ -266,17 +269,17 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp) {
     if (l == 0) {
       EventPair* ev = prof_begin(h, P<T>::fam_smooth);
       launch_fine_cheb<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L),
-                          P<T>::cd(L), c_old, c_new, k == 0);
+                          P<T>::cd(L), c_old, c_new, k == 0, h->nb);
       prof_end(h, ev);
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
-                             c_old, c_new, k == 0);
+                             c_old, c_new, k == 0, h->nb);
     }
     count_launch();
     std::swap(ua, ub);
   }
   if (ua != P<T>::U(L)) {
-    cudaMemcpyAsync(P<T>::U(L), ua, sizeof(T) * 3 * L.d.nv, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(P<T>::U(L), ua, sizeof(T) * 3 * L.d.nv * h->nb, cudaMemcpyDeviceToDevice, h->stream);
   }
 }
 
@@ -292,20 +295,20 @@ void smooth_level(topo_handle* h, int l, int sweeps, bool reverse, int smoother,
 template <typename T>
 void coarsest_solve_T(topo_handle* h) {
   DevLevel& L = h->lv.back();
-  launch_dense_gemv<T>(h->stream, h->ndense, P<T>::Ainv(h), P<T>::F(L), P<T>::U(L), L.d.nv);
+  launch_dense_gemv<T>(h->stream, h->ndense, P<T>::Ainv(h), P<T>::F(L), P<T>::U(L), L.d.nv, h->nb);
   count_launch();
 }
 
 template <typename T>
 void restrict_T(topo_handle* h, int lc) {
-  launch_restrict<T>(h->stream, h->lv[lc - 1].d, h->lv[lc].d, P<T>::R(h->lv[lc - 1]), P<T>::F(h->lv[lc]));
+  launch_restrict<T>(h->stream, h->lv[lc - 1].d, h->lv[lc].d, P<T>::R(h->lv[lc - 1]), P<T>::F(h->lv[lc]), h->nb);
   count_launch();
 }
 
 template <typename T>
 void prolong_T(topo_handle* h, int lf) {
   launch_prolong<T>(h->stream, h->lv[lf].d, h->lv[lf + 1].d, P<T>::U(h->lv[lf + 1]), P<T>::U(h->lv[lf]),
-                    h->lv[lf].vmask);
+                    h->lv[lf].vmask, h->nb);
   count_launch();
 }
 
@@ -324,7 +327,7 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
     if (l > 0) {
       level_residual<T>(h, l - 1);
       restrict_T<T>(h, l);
-      cudaMemsetAsync(P<T>::U(h->lv[l]), 0, sizeof(T) * 3 * h->lv[l].d.nv, h->stream);
+      cudaMemsetAsync(P<T>::U(h->lv[l]), 0, sizeof(T) * 3 * h->lv[l].d.nv * h->nb, h->stream);
     }
     if (l < nl - 1) smooth_level<T>(h, l, pre, false, smoother, cp);
     else coarsest_solve_T<T>(h);
@@ -605,6 +608,10 @@ void topo_destroy(topo_handle* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->unet) unet_free(h->unet);
+  if (h->multi) {
+    for (void* p : h->multi->allocs) cudaFree(p);
+    delete h->multi;
+  }
   for (void* p : h->allocs) cudaFree(p);
   for (int f = 0; f < TOPO_K_COUNT; ++f)
     for (auto& e : h->evs[f]) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
@@ -781,6 +788,8 @@ static int array_info(topo_handle* h, int which, int level, void** dptr, size_t*
     case TOPO_COEFF: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->coeff; *count = nc; break;
     case TOPO_CSENS: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->csens; *count = nc; break;
     case TOPO_VOLCSENS: if (!h->spline_set) return TOPO_E_STATE; *dptr = h->volcsens; *count = nc; break;
+    case TOPO_MULTI_F: if (!h->multi || level != 0) return TOPO_E_STATE; *dptr = h->multi->f; *count = (size_t)h->multi->cap * 3 * d0.nv; break;
+    case TOPO_MULTI_U: if (!h->multi || level != 0) return TOPO_E_STATE; *dptr = h->multi->x; *count = (size_t)h->multi->cap * 3 * d0.nv; break;
     case TOPO_U: *dptr = L.U; *count = 3 * L.d.nv; break;
     case TOPO_F: *dptr = L.F; *count = 3 * L.d.nv; break;
     case TOPO_R: *dptr = L.R; *count = 3 * L.d.nv; break;
@@ -1238,6 +1247,154 @@ int topo_spline_adjoint(topo_handle* h) {
   launch_spline_adjoint(h->stream, L.d, L.eactive, h->sd, h->sens, h->csens, h->adj1, h->adj2);
   count_launch(3);
   CKL();
+  return TOPO_OK;
+}
+
+int topo_multi_reserve(topo_handle* h, int capacity) {
+  if (!h || capacity <= 0 || capacity > 1024) return TOPO_E_BAD_INPUT;
+  if (h->multi) {
+    for (void* p : h->multi->allocs) cudaFree(p);
+    delete h->multi;
+    h->multi = nullptr;
+  }
+  std::unique_ptr<MultiRhs> m(new MultiRhs);
+  m->cap = capacity;
+  auto alloc = [&](void** p, size_t bytes) -> int {
+    if (cudaMalloc(p, std::max<size_t>(bytes, 256)) != cudaSuccess) return TOPO_E_NOMEM;
+    m->allocs.push_back(*p);
+    return cudaMemsetAsync(*p, 0, bytes, h->stream) == cudaSuccess ? TOPO_OK : TOPO_E_CUDA;
+  };
+  int rc = TOPO_OK;
+  for (size_t l = 0; l < h->lv.size() && rc == TOPO_OK; ++l) {
+    const size_t n = (size_t)capacity * 3 * h->lv[l].d.nv * sizeof(float);
+    float *a, *b, *c, *d, *e;
+    rc |= alloc((void**)&a, n); rc |= alloc((void**)&b, n); rc |= alloc((void**)&c, n);
+    rc |= alloc((void**)&d, n); rc |= alloc((void**)&e, n);
+    m->U.push_back(a); m->F.push_back(b); m->R.push_back(c); m->U2.push_back(d); m->cd.push_back(e);
+  }
+  const size_t n64 = (size_t)capacity * 3 * h->lv[0].d.nv * sizeof(double);
+  for (double** v : {&m->x, &m->f, &m->r, &m->d, &m->q, &m->rold, &m->z})
+    if (rc == TOPO_OK) rc = alloc((void**)v, n64);
+  if (rc == TOPO_OK) rc = alloc((void**)&m->part, (size_t)capacity * 256 * sizeof(double));
+  if (rc == TOPO_OK) rc = alloc((void**)&m->sc, (size_t)capacity * 16 * sizeof(double));
+  if (rc != TOPO_OK) {
+    for (void* p : m->allocs) cudaFree(p);
+    return fail(h, rc, "multi-RHS buffers for %d right-hand sides", capacity);
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  h->multi = m.release();
+  return TOPO_OK;
+}
+
+int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_multi_stats* stats, double* relres) {
+  RET(check_ready(h, true));
+  if (!o || o->rtol <= 0 || o->max_iter < 0 || o->pre < 0 || o->post < 0) return TOPO_E_BAD_INPUT;
+  if (!h->multi) return fail(h, TOPO_E_STATE, "call topo_multi_reserve first");
+  if (nrhs <= 0 || nrhs > h->multi->cap) return fail(h, TOPO_E_BAD_INPUT, "nrhs %d outside 1..%d", nrhs, h->multi->cap);
+  if (o->mode != TOPO_SOLVE_MIXED || o->smoother != TOPO_SMOOTH_CHEBYSHEV || o->inner_max > 1 || o->learned)
+    return fail(h, TOPO_E_BAD_INPUT, "multi-RHS solve: mode MIXED, Chebyshev smoother, inner_max <= 1, no learned part");
+  if (!h->ops32) return fail(h, TOPO_E_STATE, "FP32 operators not built");
+  ChebParams cp;
+  if (o->cheb_degree > 0) cp.degree = o->cheb_degree;
+  if (o->cheb_lo > 0) cp.lo = o->cheb_lo;
+  if (o->cheb_hi > 0) cp.hi = o->cheb_hi;
+  RET(prepare_smoother<float>(h, TOPO_SMOOTH_CHEBYSHEV));
+  MultiRhs& m = *h->multi;
+  DevLevel& L0 = h->lv[0];
+  const int nb = nrhs;
+  const int64_t n3 = 3 * L0.d.nv;
+  // the batched buffers stand in for the level vectors during the solve
+  struct Swap {
+    topo_handle* h;
+    std::vector<std::array<float*, 5>> saved;
+    Swap(topo_handle* hh, MultiRhs& mm, int nbb) : h(hh) {
+      for (size_t l = 0; l < h->lv.size(); ++l) {
+        DevLevel& L = h->lv[l];
+        saved.push_back({L.U32, L.F32, L.R32, L.U2_32, L.cd32});
+        L.U32 = mm.U[l]; L.F32 = mm.F[l]; L.R32 = mm.R[l]; L.U2_32 = mm.U2[l]; L.cd32 = mm.cd[l];
+      }
+      h->nb = nbb;
+    }
+    ~Swap() {
+      for (size_t l = 0; l < h->lv.size(); ++l) {
+        DevLevel& L = h->lv[l];
+        L.U32 = saved[l][0]; L.F32 = saved[l][1]; L.R32 = saved[l][2]; L.U2_32 = saved[l][3]; L.cd32 = saved[l][4];
+      }
+      h->nb = 1;
+    }
+  } swap(h, m, nb);
+  enum { B_RR, B_FF, B_RZ, B_ZROLD, B_RZOLD, B_DQ, B_ALPHA, B_BETA };
+  double* sb = m.sc;
+  auto slot = [&](int k) { return sb + (size_t)k * m.cap; };
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, h->stream));
+  // r = f - A x, ||r||^2, ||f||^2 per right-hand side
+  launch_fine_apply<double>(h->stream, L0.d, h->rhop, L0.vmask, m.x, m.f, m.r, true, nb);
+  launch_bdot<double>(h->stream, m.r, m.r, n3, nb, m.part, slot(B_RR));
+  launch_bdot<double>(h->stream, m.f, m.f, n3, nb, m.part, slot(B_FF));
+  count_launch(5);
+  std::vector<double> rr(nb), ff(nb);
+  CK(cudaMemcpyAsync(rr.data(), slot(B_RR), sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(ff.data(), slot(B_FF), sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  const double rtol2 = o->rtol * o->rtol;
+  auto converged = [&]() {
+    for (int k = 0; k < nb; ++k)
+      if (rr[k] > rtol2 * ff[k]) return false;
+    return true;
+  };
+  int it = 0, nvc = 0;
+  while (!converged() && it < o->max_iter) {
+    // z = V(r): one FP32 V-cycle for the whole batch
+    launch_d2f(h->stream, m.r, L0.F32, n3 * nb);
+    CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3 * nb, h->stream));
+    vcycle_core<float>(h, o->pre, o->post, true, TOPO_SMOOTH_CHEBYSHEV, cp);
+    ++nvc;
+    k_to_double<float><<<nb256(n3 * nb), 256, 0, h->stream>>>(n3 * nb, L0.U32, m.z);
+    launch_bdot<double>(h->stream, m.r, m.z, n3, nb, m.part, slot(B_RZ));
+    if (it > 0) launch_bdot<double>(h->stream, m.z, m.rold, n3, nb, m.part, slot(B_ZROLD));
+    launch_bbeta(h->stream, nb, slot(B_RZ), slot(B_ZROLD), slot(B_RZOLD), it == 0, slot(B_BETA));
+    launch_bdir(h->stream, n3, nb, m.z, m.d, slot(B_BETA));
+    launch_fine_apply<double>(h->stream, L0.d, h->rhop, L0.vmask, m.d, nullptr, m.q, false, nb);
+    launch_bdot<double>(h->stream, m.d, m.q, n3, nb, m.part, slot(B_DQ));
+    launch_balpha(h->stream, nb, slot(B_RZ), slot(B_DQ), slot(B_RR), slot(B_FF), rtol2, slot(B_ALPHA),
+                  slot(B_RZOLD));
+    launch_bupdate(h->stream, n3, nb, m.x, m.r, m.rold, m.d, m.q, slot(B_ALPHA));
+    launch_bdot<double>(h->stream, m.r, m.r, n3, nb, m.part, slot(B_RR));
+    count_launch(it > 0 ? 16 : 14);
+    CKL();
+    CK(cudaMemcpyAsync(rr.data(), slot(B_RR), sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < nb; ++k)
+      if (!std::isfinite(rr[k])) return fail(h, TOPO_E_NONFINITE, "right-hand side %d became non-finite", k);
+    ++it;
+  }
+  // true FP64 residuals of the final iterates
+  launch_fine_apply<double>(h->stream, L0.d, h->rhop, L0.vmask, m.x, m.f, m.r, true, nb);
+  launch_bdot<double>(h->stream, m.r, m.r, n3, nb, m.part, slot(B_RR));
+  count_launch(3);
+  CK(cudaMemcpyAsync(rr.data(), slot(B_RR), sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  double worst = 0;
+  for (int k = 0; k < nb; ++k) {
+    const double rel = ff[k] > 0 ? std::sqrt(rr[k] / ff[k]) : 0.0;
+    if (relres) relres[k] = rel;
+    worst = std::max(worst, rel);
+  }
+  if (stats) {
+    stats->iterations = it;
+    stats->vcycles = nvc;
+    stats->max_relres = worst;
+    stats->ms = ms;
+  }
+  if (worst > o->rtol) return fail(h, TOPO_E_NOT_CONVERGED, "largest relative residual %.3e above %.3e", worst, o->rtol);
   return TOPO_OK;
 }
 

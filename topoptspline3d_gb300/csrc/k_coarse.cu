@@ -116,6 +116,10 @@ template <typename T>
 __global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st,
                                                            const T* __restrict__ u, const T* __restrict__ f,
                                                            T* __restrict__ out, bool residual) {
+  const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
+  u += bo;
+  if (f) f += bo;
+  out += bo;
   const int row = threadIdx.x / SV;
   const int64_t v = (int64_t)blockIdx.x * SV + threadIdx.x % SV;
   if (v >= d.nv) return;
@@ -134,6 +138,11 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* _
                                                          T* __restrict__ uout, const T* __restrict__ dinv,
                                                          T* __restrict__ dv, T c_old, T c_new, bool first) {
   __shared__ T sr[3][SV];
+  const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
+  u += bo;
+  f += bo;
+  uout += bo;
+  dv += bo;
   const int row = threadIdx.x / SV, lv = threadIdx.x % SV;
   const int64_t v = (int64_t)blockIdx.x * SV + lv;
   const int64_t nv = d.nv;
@@ -156,20 +165,21 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* _
 
 template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
-                          T* out, bool residual) {
-  k_stencil_apply3<T><<<nblk(d.nv, SV), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
+                          T* out, bool residual, int nb) {
+  k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
 }
 
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
-                         const T* dinv, T* dvec, double c_old, double c_new, bool first) {
-  k_stencil_cheb<T><<<nblk(d.nv, SV), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old, (T)c_new, first);
+                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb) {
+  k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
+                                                                (T)c_new, first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,
-                                          const double*, double*, const double*, double*, double, double, bool);
+                                          const double*, double*, const double*, double*, double, double, bool, int);
 template void launch_stencil_cheb<float>(cudaStream_t, const LevelDims&, const float*, const float*,
-                                         const float*, float*, const float*, float*, double, double, bool);
+                                         const float*, float*, const float*, float*, double, double, bool, int);
 
 template <typename T>
 void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask, T* u,
@@ -194,6 +204,8 @@ void launch_stencil_diag_inv(cudaStream_t s, const LevelDims& d, const T* st, co
 // ---------------------------------------------------------------------------
 template <typename T, int FCT>
 __global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf, T* __restrict__ fc) {
+  rf += (int64_t)blockIdx.y * 3 * fd.nv;  // right-hand side of the batch
+  fc += (int64_t)blockIdx.y * 3 * cd.nv;
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= cd.nv) return;
   const int x = (int)(v % cd.vx);
@@ -227,6 +239,8 @@ __global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
 template <typename T, int FCT>
 __global__ void k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc, T* __restrict__ uf,
                           const uint8_t* __restrict__ vmask) {
+  uc += (int64_t)blockIdx.y * 3 * cd.nv;  // right-hand side of the batch
+  uf += (int64_t)blockIdx.y * 3 * fd.nv;
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= fd.nv) return;
   const int x = (int)(v % fd.vx);
@@ -257,20 +271,20 @@ __global__ void k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc, 
 
 template <typename T>
 void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
-                     T* fc) {
+                     T* fc, int nb) {
   if (coarse.factor == 4)
-    k_restrict<T, 4><<<nblk(coarse.nv, 128), 128, 0, s>>>(fine, coarse, rf, fc);
+    k_restrict<T, 4><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
   else
-    k_restrict<T, 2><<<nblk(coarse.nv, 128), 128, 0, s>>>(fine, coarse, rf, fc);
+    k_restrict<T, 2><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
 }
 
 template <typename T>
 void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* uc,
-                    T* uf, const uint8_t* vmask_fine) {
+                    T* uf, const uint8_t* vmask_fine, int nb) {
   if (coarse.factor == 4)
-    k_prolong<T, 4><<<nblk(fine.nv, 256), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
+    k_prolong<T, 4><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
   else
-    k_prolong<T, 2><<<nblk(fine.nv, 256), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
+    k_prolong<T, 2><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
 }
 
 // ---------------------------------------------------------------------------
@@ -598,6 +612,8 @@ __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, 
 template <typename T>
 __global__ void k_dense_gemv(int n, const T* __restrict__ Ainv, const T* __restrict__ f, T* __restrict__ u,
                              int64_t nv) {
+  f += (int64_t)blockIdx.y * 3 * nv;  // right-hand side of the batch
+  u += (int64_t)blockIdx.y * 3 * nv;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n) return;
   T s = T(0);
@@ -674,14 +690,14 @@ void launch_to_float(cudaStream_t s, const double* a, float* b, int64_t n) {
 }
 
 template <typename T>
-void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv) {
-  k_dense_gemv<T><<<nblk((int64_t)n * 32, 256), 256, 0, s>>>(n, Ainv, f_soa, u_soa, nv);
+void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv, int nb) {
+  k_dense_gemv<T><<<dim3(nblk((int64_t)n * 32, 256), nb), 256, 0, s>>>(n, Ainv, f_soa, u_soa, nv);
 }
 
 template void launch_stencil_apply<double>(cudaStream_t, const LevelDims&, const double*, const double*,
-                                           const double*, double*, bool);
+                                           const double*, double*, bool, int);
 template void launch_stencil_apply<float>(cudaStream_t, const LevelDims&, const float*, const float*,
-                                          const float*, float*, bool);
+                                          const float*, float*, bool, int);
 template void launch_stencil_gs<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                         double*, const double*, int, bool);
 template void launch_stencil_gs<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
@@ -691,13 +707,13 @@ template void launch_stencil_diag_inv<double>(cudaStream_t, const LevelDims&, co
 template void launch_stencil_diag_inv<float>(cudaStream_t, const LevelDims&, const float*,
                                              const uint8_t*, float*);
 template void launch_restrict<double>(cudaStream_t, const LevelDims&, const LevelDims&, const double*,
-                                      double*);
+                                      double*, int);
 template void launch_restrict<float>(cudaStream_t, const LevelDims&, const LevelDims&, const float*,
-                                     float*);
+                                     float*, int);
 template void launch_prolong<double>(cudaStream_t, const LevelDims&, const LevelDims&, const double*,
-                                     double*, const uint8_t*);
+                                     double*, const uint8_t*, int);
 template void launch_prolong<float>(cudaStream_t, const LevelDims&, const LevelDims&, const float*,
-                                    float*, const uint8_t*);
+                                    float*, const uint8_t*, int);
 template void launch_galerkin_dyadic_t<double>(cudaStream_t, const LevelDims&, const LevelDims&,
                                                const uint8_t*, const double*, double*);
 template void launch_galerkin_dyadic_t<float>(cudaStream_t, const LevelDims&, const LevelDims&,
@@ -707,7 +723,7 @@ template void launch_assemble_stencil_t<double>(cudaStream_t, const LevelDims&, 
 template void launch_assemble_stencil_t<float>(cudaStream_t, const LevelDims&, const uint8_t*,
                                                const uint8_t*, const float*, float*);
 template void launch_dense_gemv<double>(cudaStream_t, int, const double*, const double*, double*,
-                                        int64_t);
-template void launch_dense_gemv<float>(cudaStream_t, int, const float*, const float*, float*, int64_t);
+                                        int64_t, int);
+template void launch_dense_gemv<float>(cudaStream_t, int, const float*, const float*, float*, int64_t, int);
 
 }  // namespace topo

@@ -228,8 +228,15 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
   extern __shared__ __align__(32) unsigned char modal_smem[];
   S& sm = *reinterpret_cast<S*>(modal_smem);
   const int t = threadIdx.x, i = t % TXE, j = t / TXE;
-  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = blockIdx.z * TZ;
+  // blockIdx.z enumerates (right-hand side, z block): vectors of a batch of
+  // right-hand sides are stored one after another, the operator is shared
+  const int zblk = (d.vz + TZ - 1) / TZ;
+  const int rhs = blockIdx.z / zblk;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
   const int64_t nv = d.nv;
+  u += (int64_t)rhs * 3 * nv;
+  if (f) f += (int64_t)rhs * 3 * nv;
+  out += (int64_t)rhs * 3 * nv;
   const int gx = x0 + i, gy = y0 + j;  // owned vertex (x, y) and element (x-1, y-1)
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
   const int zend = min(z0 + TZ, d.vz);
@@ -314,7 +321,7 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
           }
         } else {
           const T* __restrict__ dinv = static_cast<const T*>(ch.dinv);
-          T* __restrict__ dv = static_cast<T*>(ch.dvec);
+          T* __restrict__ dv = static_cast<T*>(ch.dvec) + (int64_t)rhs * 3 * nv;
           T r[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] - y[c] : T(0);
@@ -534,9 +541,9 @@ void modal_smem_attr(size_t smem) {
 
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
-                       const T* u, const T* f, T* out, bool residual) {
+                       const T* u, const T* f, T* out, bool residual, int nb) {
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
-                  (d.vz + MODAL_TZ - 1) / MODAL_TZ);
+                  ((d.vz + MODAL_TZ - 1) / MODAL_TZ) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
   modal_smem_attr<T>(smem);
@@ -550,9 +557,9 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
 // One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u).
 template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first) {
+                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb) {
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
-                  (d.vz + MODAL_TZ - 1) / MODAL_TZ);
+                  ((d.vz + MODAL_TZ - 1) / MODAL_TZ) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
   modal_smem_attr<T>(smem);
@@ -562,10 +569,10 @@ void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const u
 
 template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                        const double*, const double*, double*, const double*, double*, double,
-                                       double, bool);
+                                       double, bool, int);
 template void launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
                                       const float*, const float*, float*, const float*, float*, double, double,
-                                      bool);
+                                      bool, int);
 
 // Dense-row form of the same operator (thread per vertex, 8 x 3 x 24 products);
 // kept as the cross-check of the modal kernel.
@@ -598,9 +605,9 @@ void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, con
 }
 
 template void launch_fine_apply<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
-                                        const double*, const double*, double*, bool);
+                                        const double*, const double*, double*, bool, int);
 template void launch_fine_apply<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
-                                       const float*, const float*, float*, bool);
+                                       const float*, const float*, float*, bool, int);
 template void launch_fine_gs<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                      double*, const double*, int, bool);
 template void launch_fine_gs<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,

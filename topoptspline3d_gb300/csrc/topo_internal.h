@@ -70,7 +70,7 @@ struct Stream {
 // fine level (k_fine.cu)
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
-                       const T* u, const T* f, T* out, bool residual);
+                       const T* u, const T* f, T* out, bool residual, int nb = 1);
 template <typename T>
 void launch_fine_gs(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, T* u,
                     const T* f, int colour, bool reverse);
@@ -79,10 +79,11 @@ void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, con
                           T* dinv);
 template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first);
+                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first,
+                      int nb = 1);
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
-                         const T* dinv, T* dvec, double c_old, double c_new, bool first);
+                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);
 template <typename T>
 void launch_fine_apply_dense(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                              const T* u, const T* f, T* out, bool residual);
@@ -91,7 +92,7 @@ void upload_template(const double* Ke576, double lam, double mu, double h);
 // coarse levels (k_coarse.cu)
 template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
-                          T* out, bool residual);
+                          T* out, bool residual, int nb = 1);
 template <typename T>
 void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask, T* u,
                        const T* f, int colour, bool reverse);
@@ -100,10 +101,10 @@ void launch_stencil_diag_inv(cudaStream_t s, const LevelDims& d, const T* st, co
                              T* dinv);
 template <typename T>
 void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
-                     T* fc);
+                     T* fc, int nb = 1);
 template <typename T>
 void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* uc,
-                    T* uf, const uint8_t* vmask_fine);
+                    T* uf, const uint8_t* vmask_fine, int nb = 1);
 void launch_galerkin_first_impl(cudaStream_t s, const LevelDims& fd, const LevelDims& cd,
                                 const double* rhop, const uint8_t* eactive_f, const uint8_t* vmask_f,
                                 const double* Ttab64, const float* Ttab32, const double* Ke,
@@ -118,7 +119,7 @@ void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double*
 int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev);
 void launch_to_float(cudaStream_t s, const double* a, float* b, int64_t n);
 template <typename T>
-void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv);
+void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv, int nb = 1);
 
 // vectors and reductions (k_vec.cu)
 int reduce_blocks(int64_t n);
@@ -227,5 +228,26 @@ cudaError_t unet_train(UNetState* u, cudaStream_t s, int steps, int batch, doubl
                        bool update, double* loss_out);
 cudaError_t unet_host_pass(UNetState* u, cudaStream_t s, int X, int Y, int Z, int nb, const float* x, const float* t,
                            const uint8_t* m, float* y, double* loss, float* grad);
+
+// k_multi.cu: batched vectors of the multi-right-hand-side solver.
+template <typename T>
+void launch_bdot(cudaStream_t s, const T* a, const T* b, int64_t n, int nb, double* partial, double* out);
+void launch_bbeta(cudaStream_t s, int nb, const double* rz, const double* zrold, const double* rzold, bool first,
+                  double* beta);
+void launch_balpha(cudaStream_t s, int nb, const double* rz, const double* dq, const double* rr, const double* ff,
+                   double rtol2, double* alpha, double* rzold);
+void launch_bdir(cudaStream_t s, int64_t n, int nb, const double* z, double* d, const double* beta);
+void launch_bupdate(cudaStream_t s, int64_t n, int nb, double* x, double* r, double* rold, const double* d,
+                    const double* q, const double* alpha);
+
+// Batched buffers of the multi-right-hand-side solver (topo_multi_reserve).
+struct MultiRhs {
+  int cap = 0;
+  std::vector<float*> U, F, R, U2, cd;  // per level, cap * 3 nv
+  double *x = nullptr, *f = nullptr, *r = nullptr, *d = nullptr, *q = nullptr, *rold = nullptr, *z = nullptr;
+  double* part = nullptr;  // reduction partials [cap][256]
+  double* sc = nullptr;    // scalars [kSlots][cap]
+  std::vector<void*> allocs;
+};
 
 }  // namespace topo

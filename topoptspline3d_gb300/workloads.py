@@ -123,3 +123,27 @@ def random_density(nx, ny, nz, seed, sigma=None, lo=1e-3) -> np.ndarray:
     g = gaussian_filter(rng.standard_normal((nz, ny, nx)), sigma, mode="wrap")
     g = (g - g.mean()) / max(g.std(), 1e-12)
     return np.clip(0.5 + 0.35 * g, lo, 1.0).ravel()
+
+
+def patch_loads(nx, ny, nz, nrhs, seed0=1000, patch=8) -> np.ndarray:
+    """Load cases of the batched worst-case study: for k = 0..nrhs-1, with
+    rng = default_rng(seed0 + k), a patch origin uniform over the valid
+    patch x patch voxel positions of the x = nx face ((patch+1)^2 nodes), a
+    direction rng.standard_normal(3) normalised, per-node force dir/(patch+1)^2.
+    Returns [nrhs][3*nv]."""
+    vx, vy, vz = nx + 1, ny + 1, nz + 1
+    nv = vx * vy * vz
+    out = np.zeros((nrhs, 3 * nv))
+    for k in range(nrhs):
+        rng = np.random.default_rng(seed0 + k)
+        y0 = int(rng.integers(0, ny - patch + 1))
+        z0 = int(rng.integers(0, nz - patch + 1))
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        npn = (patch + 1) ** 2
+        for z in range(z0, z0 + patch + 1):
+            for y in range(y0, y0 + patch + 1):
+                v = nx + vx * (y + vy * z)
+                for c in range(3):
+                    out[k, c * nv + v] = d[c] / npn
+    return out

@@ -218,8 +218,14 @@ int topo_set_operator_precision(topo_handle* h, int mask);
  * (grid/Grid.cpp:3614-3669). */
 int topo_update_operators(topo_handle* h);
 /* Replaces Grid::applyK (grid/Grid.cu:4278-4356): TOPO_R(level 0) <- K(rho) TOPO_WORK,
- * fixed rows zero.  precision: 0 = FP64, 1 = FP32 kernel. */
+ * fixed rows zero.  precision: 0 = FP64 modal kernel, 1 = FP32 kernel, 2 = FP64 dense-row
+ * kernel, 3 = FP64 vectors with the double-float modal kernel. */
 int topo_apply_fine(topo_handle* h, int precision);
+/* Arithmetic of the FP64 fine operator used by the solvers (residuals and the
+ * outer CG matvec): 0 = native FP64, 1 = double-float (pairs of floats with
+ * error-free transformations, ~48-bit significands, on the FP32 pipe; default).
+ * Vectors, dot products and step lengths stay FP64 either way. */
+int topo_set_fine_arithmetic(topo_handle* h, int arith);
 /* Replaces Grid::update_residual (grid/Grid.cu:2420-2454). */
 int topo_residual(topo_handle* h, int level);
 /* Replaces Grid::gs_relax (grid/Grid.cu:1844-1887); reverse = adjoint sweep order. */

@@ -48,6 +48,10 @@ def test_fine_operator_fp64_fp32(pair):
     assert rel(g.apply_fine(u, 0), y_o) < 1e-12   # modal FP64 kernel
     assert rel(g.apply_fine(u, 2), y_o) < 1e-12   # dense-row FP64 kernel
     assert rel(g.apply_fine(u, 1), y_o) < 1e-5    # modal FP32 kernel
+    # double-float modal kernel: ~48-bit significands; elementwise against FP64
+    y_df, y_64 = g.apply_fine(u, 3), g.apply_fine(u, 0)
+    assert rel(y_df, y_o) < 1e-12
+    assert np.abs(y_df - y_64).max() <= 1e-12 * np.abs(y_64).max()
 
 
 def test_galerkin_levels(pair):

@@ -44,7 +44,7 @@ EXPORTED = [
     "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x", "topo_set_bc_regions", "topo_plan_bc_regions",
     "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
-    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi",
+    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
 ]
 
 
@@ -166,6 +166,7 @@ def load(build: bool = True):
         "topo_volume_csens": (i, [vp, i, d, vp]),
         "topo_unet_enable": (i, [vp, C.c_ulonglong]),
         "topo_multi_reserve": (i, [vp, i]),
+        "topo_set_fine_arithmetic": (i, [vp, i]),
         "topo_solve_multi": (i, [vp, i, C.POINTER(SolveOpts), C.POINTER(MultiStats), dp]),
         "topo_unet_num_params": (i, [C.POINTER(sz)]),
         "topo_unet_get_params": (i, [vp, vp, sz]),
@@ -407,6 +408,10 @@ class Problem:
     # --- hot path
     def coeff_to_density(self):
         self._ck(self.lib.topo_coeff_to_density(self.h))
+
+    def set_fine_arithmetic(self, arith):
+        """0: native FP64 fine operator, 1: double-float (default)."""
+        self._ck(self.lib.topo_set_fine_arithmetic(self.h, arith))
 
     def set_operator_precision(self, mask):
         self._ck(self.lib.topo_set_operator_precision(self.h, mask))

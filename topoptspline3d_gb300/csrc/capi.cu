@@ -38,6 +38,7 @@ struct topo_handle {
   topo_config cfg{};
   topo::UNetState* unet = nullptr;  // learned preconditioner (topo_unet_enable)
   int nb = 1;                       // right-hand sides the level vectors hold (multi-RHS solve)
+  int fine_df = 1;                  // FP64 fine operator in double-float arithmetic (topo_set_fine_arithmetic)
   topo::MultiRhs* multi = nullptr;  // batched buffers (topo_multi_reserve)
   int unet_crops = 64;              // crops per harvested iterate
   cudaStream_t stream = nullptr;
@@ -201,7 +202,12 @@ void level_apply(topo_handle* h, int l, const T* u, const T* f, T* out, bool res
   DevLevel& L = h->lv[l];
   if (l == 0) {
     EventPair* ev = prof_begin(h, P<T>::fam_apply);
-    launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual, h->nb);
+    if (sizeof(T) == 8 && h->fine_df)
+      launch_fine_apply_df(h->stream, L.d, reinterpret_cast<const double*>(P<T>::rhop(h)), L.vmask,
+                           reinterpret_cast<const double*>(u), reinterpret_cast<const double*>(f),
+                           reinterpret_cast<double*>(out), residual, h->nb);
+    else
+      launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual, h->nb);
     prof_end(h, ev);
   } else {
     launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual, h->nb);
@@ -923,8 +929,12 @@ int topo_apply_fine(topo_handle* h, int precision) {
   RET(update_penalised_if_stale(h));
   DevLevel& L = h->lv[0];
   const int64_t n3 = 3 * L.d.nv;
-  if (precision == 0) {
-    level_apply<double>(h, 0, h->work, nullptr, L.R, false);
+  if (precision == 0) {  // FP64 modal kernel in native FP64
+    launch_fine_apply<double>(h->stream, L.d, h->rhop, L.vmask, h->work, nullptr, L.R, false);
+    count_launch();
+  } else if (precision == 3) {  // FP64 vectors, double-float modal kernel
+    launch_fine_apply_df(h->stream, L.d, h->rhop, L.vmask, h->work, nullptr, L.R, false);
+    count_launch();
   } else if (precision == 2) {  // dense-row FP64 kernel (cross-check of the modal kernel)
     launch_fine_apply_dense<double>(h->stream, L.d, h->rhop, L.vmask, h->work, nullptr, L.R, false);
     count_launch();
@@ -1250,6 +1260,19 @@ int topo_spline_adjoint(topo_handle* h) {
   return TOPO_OK;
 }
 
+// FP64 fine operator on a batch of vectors, in the handle's fine arithmetic.
+static void fine64(topo_handle* h, const LevelDims& d, const double* u, const double* f, double* out, bool residual,
+                   int nb) {
+  if (h->fine_df) launch_fine_apply_df(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb);
+  else launch_fine_apply<double>(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb);
+}
+
+int topo_set_fine_arithmetic(topo_handle* h, int arith) {
+  if (!h || arith < 0 || arith > 1) return TOPO_E_BAD_INPUT;
+  h->fine_df = arith;
+  return TOPO_OK;
+}
+
 int topo_multi_reserve(topo_handle* h, int capacity) {
   if (!h || capacity <= 0 || capacity > 1024) return TOPO_E_BAD_INPUT;
   if (h->multi) {
@@ -1331,7 +1354,7 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
   CK(cudaEventCreate(&e1));
   CK(cudaEventRecord(e0, h->stream));
   // r = f - A x, ||r||^2, ||f||^2 per right-hand side
-  launch_fine_apply<double>(h->stream, L0.d, h->rhop, L0.vmask, m.x, m.f, m.r, true, nb);
+  fine64(h, L0.d, m.x, m.f, m.r, true, nb);
   launch_bdot<double>(h->stream, m.r, m.r, n3, nb, m.part, slot(B_RR));
   launch_bdot<double>(h->stream, m.f, m.f, n3, nb, m.part, slot(B_FF));
   count_launch(5);
@@ -1357,7 +1380,7 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
     if (it > 0) launch_bdot<double>(h->stream, m.z, m.rold, n3, nb, m.part, slot(B_ZROLD));
     launch_bbeta(h->stream, nb, slot(B_RZ), slot(B_ZROLD), slot(B_RZOLD), it == 0, slot(B_BETA));
     launch_bdir(h->stream, n3, nb, m.z, m.d, slot(B_BETA));
-    launch_fine_apply<double>(h->stream, L0.d, h->rhop, L0.vmask, m.d, nullptr, m.q, false, nb);
+    fine64(h, L0.d, m.d, nullptr, m.q, false, nb);
     launch_bdot<double>(h->stream, m.d, m.q, n3, nb, m.part, slot(B_DQ));
     launch_balpha(h->stream, nb, slot(B_RZ), slot(B_DQ), slot(B_RR), slot(B_FF), rtol2, slot(B_ALPHA),
                   slot(B_RZOLD));
@@ -1372,7 +1395,7 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
     ++it;
   }
   // true FP64 residuals of the final iterates
-  launch_fine_apply<double>(h->stream, L0.d, h->rhop, L0.vmask, m.x, m.f, m.r, true, nb);
+  fine64(h, L0.d, m.x, m.f, m.r, true, nb);
   launch_bdot<double>(h->stream, m.r, m.r, n3, nb, m.part, slot(B_RR));
   count_launch(3);
   CK(cudaMemcpyAsync(rr.data(), slot(B_RR), sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));

@@ -32,6 +32,57 @@ __device__ __forceinline__ float modal_c<float>(int i) { return cModal32[i]; }
 // Diagonal 3x3 blocks Ke[a,a] of the eight local nodes (FP32 smoother epilogue).
 __constant__ float cKdiag32[8][9];
 
+// ---------------------------------------------------------------------------
+// Double-float ("float-float") arithmetic: a value is the unevaluated sum
+// hi + lo of two floats with |lo| <= ulp(hi)/2, about 48 significant bits.
+// Addition uses Knuth's error-free TwoSum on the high parts, folds in the low
+// parts and renormalises with Dekker's Fast2Sum; multiplication forms the exact
+// product error of the high parts with an FMA (TwoProd).  This is the sloppy
+// double-double addition of Hida, Li and Bailey (2001) on floats.  All
+// operations use the _rn intrinsics so the compiler cannot fuse or reorder
+// them.  On GB300 the FP32 pipe is 58x the FP64 pipe, so the fine operator of
+// the FP64 outer CG runs in this arithmetic with FP64-level accuracy.
+// ---------------------------------------------------------------------------
+struct df {
+  float hi, lo;
+  __device__ __forceinline__ df() {}
+  __device__ __forceinline__ df(float h, float l) : hi(h), lo(l) {}
+  __device__ __forceinline__ explicit df(int v) : hi((float)v), lo(0.f) {}
+};
+
+__device__ __forceinline__ df df_fast2sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df operator+(df a, df b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return df_fast2sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df operator-(df a, df b) { return a + df(-b.hi, -b.lo); }
+__device__ __forceinline__ df operator*(df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+  return df_fast2sum(p, e);
+}
+__device__ __forceinline__ df& operator+=(df& a, df b) { a = a + b; return a; }
+__device__ __forceinline__ bool operator!=(df a, df b) { return a.hi != b.hi || a.lo != b.lo; }
+__device__ __forceinline__ df df_from(double x) {
+  const float h = __double2float_rn(x);
+  return df(h, __double2float_rn(x - (double)h));
+}
+__device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.lo; }
+
+// Modal constants split into hi + lo floats.
+__constant__ float2 cModalDF[5];
+template <>
+__device__ __forceinline__ df modal_c<df>(int i) {
+  const float2 c = cModalDF[i];
+  return df(c.x, c.y);
+}
+
 void upload_template(const double* Ke576, double lam, double mu, double h) {
   float k32[576];
   for (int i = 0; i < 576; ++i) k32[i] = (float)Ke576[i];
@@ -46,6 +97,12 @@ void upload_template(const double* Ke576, double lam, double mu, double h) {
   const float m32[5] = {(float)m64[0], (float)m64[1], (float)m64[2], (float)m64[3], (float)m64[4]};
   cudaMemcpyToSymbol(cModal64, m64, sizeof(m64));
   cudaMemcpyToSymbol(cModal32, m32, sizeof(m32));
+  float2 mdf[5];
+  for (int i = 0; i < 5; ++i) {
+    mdf[i].x = (float)m64[i];
+    mdf[i].y = (float)(m64[i] - (double)mdf[i].x);
+  }
+  cudaMemcpyToSymbol(cModalDF, mdf, sizeof(mdf));
 }
 
 // ---------------------------------------------------------------------------
@@ -364,6 +421,120 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// The same operator (MODE 0: out = K u, MODE 1: out = f - K u) on FP64 vectors
+// computed in double-float arithmetic.  Vertex planes arrive as doubles by
+// cp.async and are split in place into (hi, lo) float pairs (the same 8 bytes)
+// once per plane, so the only FP64 instructions left are about eight
+// conversions per vertex; the element operator runs on the FP32 pipe.
+template <int TXE, int TYE, int MODE>
+__global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const double* __restrict__ rhop,
+                                                            const uint8_t* __restrict__ vmask,
+                                                            const double* __restrict__ u,
+                                                            const double* __restrict__ f, double* __restrict__ out,
+                                                            int TZ) {
+  using S = ModalSmem<df, TXE, TYE>;
+  constexpr int NT = S::NT, PX = S::PX, NP = S::NP;
+  extern __shared__ __align__(32) unsigned char modal_smem[];
+  S& sm = *reinterpret_cast<S*>(modal_smem);
+  const int t = threadIdx.x, i = t % TXE, j = t / TXE;
+  const int zblk = (d.vz + TZ - 1) / TZ;
+  const int rhs = blockIdx.z / zblk;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int64_t nv = d.nv;
+  u += (int64_t)rhs * 3 * nv;
+  if (f) f += (int64_t)rhs * 3 * nv;
+  out += (int64_t)rhs * 3 * nv;
+  const int gx = x0 + i, gy = y0 + j;
+  const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
+  const int zend = min(z0 + TZ, d.vz);
+  df acc0(0), acc1(0), acc2(0);
+  auto prefetch = [&](int z) {
+    if (z <= zend) {
+      Vec4<df>* dst = sm.plane[(z + 3) % 3];
+      for (int k = t; k < NP; k += NT) {
+        const int px = k % PX, py = k / PX;
+        const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+        const bool ok = vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz;
+        const int64_t v = ok ? vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z) : 0;
+        double* raw = reinterpret_cast<double*>(&dst[k]);
+        cp_async_8(raw, u + v, ok);
+        cp_async_8(raw + 1, u + nv + v, ok);
+        cp_async_8(raw + 2, u + 2 * nv + v, ok);
+      }
+    }
+    cp_async_commit();
+  };
+  // split plane z's doubles into (hi, lo) pairs in place
+  auto convert = [&](int z) {
+    if (z > zend) return;
+    Vec4<df>* p = sm.plane[(z + 3) % 3];
+    for (int k = t; k < NP; k += NT) {
+      const double* raw = reinterpret_cast<const double*>(&p[k]);
+      const double a = raw[0], b = raw[1], c = raw[2];
+      p[k].x = df_from(a);
+      p[k].y = df_from(b);
+      p[k].z = df_from(c);
+    }
+  };
+  prefetch(z0 - 1);
+  prefetch(z0);
+  for (int ez = z0 - 1; ez < zend; ++ez) {
+    prefetch(ez + 2);
+    cp_async_wait1();
+    __syncthreads();
+    if (ez == z0 - 1) convert(ez);
+    convert(ez + 1);
+    __syncthreads();
+    {
+      const int ex = gx - 1, ey = gy - 1;
+      df pe(0);
+      if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
+        pe = df_from(rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)]);
+      if (pe != df(0)) {
+        df c[3][8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
+          const Vec4<df> p = sm.plane[(ez + (a >> 2) + 3) % 3][k];
+          c[0][a] = p.x; c[1][a] = p.y; c[2][a] = p.z;
+        }
+        modal_element<df>(c, pe);
+#pragma unroll
+        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<df>{c[0][a], c[1][a], c[2][a], df(0)};
+      } else {
+#pragma unroll
+        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<df>{df(0), df(0), df(0), df(0)};
+      }
+    }
+    __syncthreads();
+    if (own) {
+      df b0 = acc0, b1 = acc1, b2 = acc2, t0(0), t1(0), t2(0);
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const int wx = w & 1, wy = w >> 1;
+        const int te = (i + wx) + TXE * (j + wy);
+        const int a = (1 - wx) + 2 * (1 - wy);
+        const Vec4<df> bo = sm.fe[a][te], to = sm.fe[a + 4][te];
+        b0 += bo.x; b1 += bo.y; b2 += bo.z;
+        t0 += to.x; t1 += to.y; t2 += to.z;
+      }
+      if (ez >= z0) {
+        const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
+        const uint8_t m = vmask[v];
+        const double y[3] = {df_to(b0), df_to(b1), df_to(b2)};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const bool fr = (m >> c) & 1;
+          const int64_t idx = c * nv + v;
+          out[idx] = MODE == 1 ? (fr ? f[idx] - y[c] : 0.0) : (fr ? y[c] : 0.0);
+        }
+      }
+      acc0 = t0; acc1 = t1; acc2 = t2;
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // Row block of vertex (x,y,z): out = sum over incident elements of rho^p Ke[a,:] u_e,
 // S = diagonal 3x3 block.  Template arguments fix whether S is needed.
 template <typename T, bool NEED_S>
@@ -552,6 +723,24 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
     k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ, ch);
   else
     k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ, ch);
+}
+
+void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
+                          const double* u, const double* f, double* out, bool residual, int nb) {
+  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
+                  ((d.vz + MODAL_TZ - 1) / MODAL_TZ) * nb);
+  constexpr int NT = MODAL_TXE * MODAL_TYE;
+  const size_t smem = sizeof(ModalSmem<df, MODAL_TXE, MODAL_TYE>);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  if (residual)
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ);
+  else
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ);
 }
 
 // One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u).

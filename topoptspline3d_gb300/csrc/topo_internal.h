@@ -71,6 +71,9 @@ struct Stream {
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb = 1);
+// FP64 vectors, double-float arithmetic (k_fine_modal_df)
+void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
+                          const double* u, const double* f, double* out, bool residual, int nb = 1);
 template <typename T>
 void launch_fine_gs(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, T* u,
                     const T* f, int colour, bool reverse);

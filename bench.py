@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--smoother", default="chebyshev", choices=["chebyshev", "gs"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="FP64 MG-PCG comparison steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default solver schedule and tiles")
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run exactly one mixed design iteration and exit (for ncu captures)")
     ap.add_argument("--profile-solve-steps", type=int, default=0,
@@ -144,7 +145,7 @@ def make_problem(nx, ny, nz, device, op_precision):
 def solve_opts(mode, smoother):
     from topoptspline3d_gb300 import capi
     return dict(mode=mode, smoother=capi.SMOOTH_CHEBYSHEV if smoother == "chebyshev" else capi.SMOOTH_GS,
-                pre=2, post=2, rtol=1e-6, max_iter=300, inner_max=4, inner_rtol=0.1)
+                pre=2, post=2, rtol=1e-6, max_iter=300, inner_max=4, inner_rtol=0.1, cheb_degree=2)
 
 
 def load_traffic():
@@ -240,6 +241,11 @@ def main():
         return
     for _ in range(args.warmup):
         p.design_iteration(solve=opts, oc=oc)
+    # kernel tiles and solver schedule for this problem (untimed set-up)
+    tune = None
+    if not args.no_autotune and args.smoother == "chebyshev":
+        p.update_operators()  # operators of the current design (the last OC step changed it)
+        opts, tune = p.autotune(opts)
     # ---- timed region: K design iterations, device-resident inputs
     sampler = ClockSampler(device)
     barrier(pg)
@@ -335,8 +341,10 @@ def main():
            "vs_baseline": None, "dtype": "f32 multigrid / f64 CG", "data": "synthetic",
            "config": {"workload": f"half-MBB {nx}x{ny}x{nz} spline OC design iteration", "grid": [nx, ny, nz],
                       "dofs": 3 * nv, "lattice": [nx // 4 + 1, ny // 4 + 1, nz // 4 + 1],
-                      "solver": f"FP64 flexible CG (fine matvec in double-float, ~1e-14 of FP64) + FP32 "
-                                f"{args.smoother} V(2,2) multigrid, rel-res 1e-6",
+                      "solver": f"FP64 flexible CG (fine matvec in double-float, ~1e-14 of FP64) + "
+                                f"{opts['inner_max']} FP32 CG its with {args.smoother} V({opts['pre']},"
+                                f"{opts['post']}) degree-{opts['cheb_degree']} multigrid, rel-res 1e-6",
+                      "autotune": tune,
                       "l2": "working set (>2 GB) larger than L2; no flush",
                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
            "cg_iterations": [s["iterations"] for s in stats], "relres": max(s["relres"] for s in stats),

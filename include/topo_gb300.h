@@ -363,6 +363,25 @@ typedef struct topo_iter_stats {
  * computeSensitivity (sensitivity, filter, spline adjoint) and updateCoeff. */
 int topo_design_iteration(topo_handle* h, const topo_iter_opts* opts, topo_iter_stats* stats);
 
+/* --- autotuner ------------------------------------------------------------ */
+/* Tile and schedule choice for the current problem state (no reference
+ * counterpart).  Stage 1 times the fine-level kernels at z-march depths
+ * 4, 8, 16 and 32 (the FP32 Chebyshev step and the FP64 operator, CUDA events,
+ * 5 launches each) and keeps the fastest for the handle.  Stage 2 solves from the
+ * current U with each candidate schedule of the mixed solver (FP32 inner
+ * iterations 1, 2, 4, 6 x smoothing steps 1, 2 x Chebyshev degree 2, 3) and
+ * writes the fastest that converges into *best (other fields from *base, which
+ * must be TOPO_SOLVE_MIXED with the Chebyshev smoother).  U is restored. */
+typedef struct topo_tune_report {
+  int tz32, tz64;           /* chosen z-march depths */
+  double cheb_ms[4];        /* FP32 Chebyshev step at depths 4, 8, 16, 32 */
+  double apply_ms[4];       /* FP64 operator at depths 4, 8, 16, 32 */
+  int candidates;           /* schedules tried */
+  double base_ms, best_ms;  /* solve time of *base and of *best */
+  double tune_ms;           /* device time spent tuning */
+} topo_tune_report;
+int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* best, topo_tune_report* report);
+
 /* --- many load cases in one solve ------------------------------------------ */
 /* Multi-right-hand-side solve (config "batched": many load cases as right-hand
  * sides of one V-cycle; no reference counterpart).  Every FP32 V-cycle launch

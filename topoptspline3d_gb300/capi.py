@@ -45,6 +45,7 @@ EXPORTED = [
     "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
+    "topo_autotune",
 ]
 
 
@@ -83,6 +84,11 @@ class IterOpts(C.Structure):
 class IterStats(C.Structure):
     _fields_ = [("compliance", C.c_double), ("volume", C.c_double), ("solve", SolveStats),
                 ("oc_trials", C.c_int), ("ms", C.c_double)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("tz32", C.c_int), ("tz64", C.c_int), ("cheb_ms", C.c_double * 4), ("apply_ms", C.c_double * 4),
+                ("candidates", C.c_int), ("base_ms", C.c_double), ("best_ms", C.c_double), ("tune_ms", C.c_double)]
 
 
 class MultiStats(C.Structure):
@@ -167,6 +173,7 @@ def load(build: bool = True):
         "topo_unet_enable": (i, [vp, C.c_ulonglong]),
         "topo_multi_reserve": (i, [vp, i]),
         "topo_set_fine_arithmetic": (i, [vp, i]),
+        "topo_autotune": (i, [vp, C.POINTER(SolveOpts), C.POINTER(SolveOpts), C.POINTER(TuneReport)]),
         "topo_solve_multi": (i, [vp, i, C.POINTER(SolveOpts), C.POINTER(MultiStats), dp]),
         "topo_unet_num_params": (i, [C.POINTER(sz)]),
         "topo_unet_get_params": (i, [vp, vp, sz]),
@@ -455,6 +462,25 @@ class Problem:
             self._ck(rc)
         return {"iterations": s.iterations, "vcycles": s.vcycles, "relres": s.relres, "ms": s.ms, "rc": rc,
                 "learned_applied": s.learned_applied, "learned_fallback": bool(s.learned_fallback)}
+
+    # --- autotuner
+
+    def autotune(self, base=None):
+        """Tile (z-march depth) and solver-schedule tuning on the current state.
+        Returns (best solve-options dict, report dict)."""
+        b = dict(mode=SOLVE_MIXED, smoother=SMOOTH_CHEBYSHEV, pre=2, post=2, rtol=1e-6, max_iter=300,
+                 inner_rtol=0.1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=4, learned=0,
+                 learned_stall=0.0)
+        b.update(base or {})
+        keys = [f[0] for f in SolveOpts._fields_]
+        o = SolveOpts(*[b[k] for k in keys])
+        best = SolveOpts()
+        r = TuneReport()
+        self._ck(self.lib.topo_autotune(self.h, C.byref(o), C.byref(best), C.byref(r)))
+        bd = {k: getattr(best, k) for k in keys}
+        rep = {"tz32": r.tz32, "tz64": r.tz64, "cheb_ms": list(r.cheb_ms), "apply_ms": list(r.apply_ms),
+               "candidates": r.candidates, "base_ms": r.base_ms, "best_ms": r.best_ms, "tune_ms": r.tune_ms}
+        return bd, rep
 
     # --- many load cases
 

@@ -39,6 +39,7 @@ struct topo_handle {
   topo::UNetState* unet = nullptr;  // learned preconditioner (topo_unet_enable)
   int nb = 1;                       // right-hand sides the level vectors hold (multi-RHS solve)
   int fine_df = 1;                  // FP64 fine operator in double-float arithmetic (topo_set_fine_arithmetic)
+  int tz32 = 16, tz64 = 16;         // z-march depth of the fine kernels, FP32 / FP64 (topo_autotune)
   topo::MultiRhs* multi = nullptr;  // batched buffers (topo_multi_reserve)
   int unet_crops = 64;              // crops per harvested iterate
   cudaStream_t stream = nullptr;
@@ -205,9 +206,10 @@ void level_apply(topo_handle* h, int l, const T* u, const T* f, T* out, bool res
     if (sizeof(T) == 8 && h->fine_df)
       launch_fine_apply_df(h->stream, L.d, reinterpret_cast<const double*>(P<T>::rhop(h)), L.vmask,
                            reinterpret_cast<const double*>(u), reinterpret_cast<const double*>(f),
-                           reinterpret_cast<double*>(out), residual, h->nb);
+                           reinterpret_cast<double*>(out), residual, h->nb, h->tz64);
     else
-      launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual, h->nb);
+      launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual, h->nb,
+                           sizeof(T) == 4 ? h->tz32 : h->tz64);
     prof_end(h, ev);
   } else {
     launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual, h->nb);
@@ -275,7 +277,7 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp) {
     if (l == 0) {
       EventPair* ev = prof_begin(h, P<T>::fam_smooth);
       launch_fine_cheb<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L),
-                          P<T>::cd(L), c_old, c_new, k == 0, h->nb);
+                          P<T>::cd(L), c_old, c_new, k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64);
       prof_end(h, ev);
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
@@ -1263,13 +1265,104 @@ int topo_spline_adjoint(topo_handle* h) {
 // FP64 fine operator on a batch of vectors, in the handle's fine arithmetic.
 static void fine64(topo_handle* h, const LevelDims& d, const double* u, const double* f, double* out, bool residual,
                    int nb) {
-  if (h->fine_df) launch_fine_apply_df(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb);
-  else launch_fine_apply<double>(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb);
+  if (h->fine_df) launch_fine_apply_df(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb, h->tz64);
+  else launch_fine_apply<double>(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb, h->tz64);
 }
 
 int topo_set_fine_arithmetic(topo_handle* h, int arith) {
   if (!h || arith < 0 || arith > 1) return TOPO_E_BAD_INPUT;
   h->fine_df = arith;
+  return TOPO_OK;
+}
+
+int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* best, topo_tune_report* rep) {
+  RET(check_ready(h, true));
+  if (!base || !best || base->mode != TOPO_SOLVE_MIXED || base->smoother != TOPO_SMOOTH_CHEBYSHEV || base->learned)
+    return fail(h, TOPO_E_BAD_INPUT, "autotune: base schedule must be MIXED with the Chebyshev smoother");
+  if (!h->ops32) return fail(h, TOPO_E_STATE, "FP32 operators not built");
+  topo_tune_report r{};
+  DevLevel& L0 = h->lv[0];
+  const int64_t n3 = 3 * L0.d.nv;
+  cudaEvent_t t0, t1, a, b;
+  CK(cudaEventCreate(&t0)); CK(cudaEventCreate(&t1)); CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(t0, h->stream));
+  RET(prepare_smoother<float>(h, TOPO_SMOOTH_CHEBYSHEV));
+  // ---- stage 1: z-march depth of the fine kernels
+  const int tzs[4] = {4, 8, 16, 32};
+  int best32 = h->tz32, best64 = h->tz64;
+  double b32 = 1e30, b64 = 1e30;
+  for (int k = 0; k < 4; ++k) {
+    for (int rep = 0; rep < 2; ++rep) {  // warm-up, then timed
+      CK(cudaEventRecord(a, h->stream));
+      for (int i = 0; i < 5; ++i)
+        launch_fine_cheb<float>(h->stream, L0.d, h->rhop32, L0.vmask, L0.U32, L0.F32, L0.U2_32, L0.dinv32, L0.cd32,
+                                0.0, 1.0, true, 1, tzs[k]);
+      CK(cudaEventRecord(b, h->stream));
+      CK(cudaEventSynchronize(b));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      r.cheb_ms[k] = ms / 5;
+    }
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(cudaEventRecord(a, h->stream));
+      for (int i = 0; i < 5; ++i) {
+        if (h->fine_df) launch_fine_apply_df(h->stream, L0.d, h->rhop, L0.vmask, h->work, nullptr, L0.R, false, 1, tzs[k]);
+        else launch_fine_apply<double>(h->stream, L0.d, h->rhop, L0.vmask, h->work, nullptr, L0.R, false, 1, tzs[k]);
+      }
+      CK(cudaEventRecord(b, h->stream));
+      CK(cudaEventSynchronize(b));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      r.apply_ms[k] = ms / 5;
+    }
+    count_launch(20);
+    if (r.cheb_ms[k] < b32) { b32 = r.cheb_ms[k]; best32 = tzs[k]; }
+    if (r.apply_ms[k] < b64) { b64 = r.apply_ms[k]; best64 = tzs[k]; }
+  }
+  CKL();
+  h->tz32 = best32;
+  h->tz64 = best64;
+  r.tz32 = best32;
+  r.tz64 = best64;
+  // ---- stage 2: solver schedule, each candidate from the same initial U
+  double* u0 = nullptr;
+  CK(cudaMalloc((void**)&u0, sizeof(double) * n3));
+  CK(cudaMemcpyAsync(u0, L0.U, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  auto run = [&](const topo_solve_opts& o, double* ms) -> int {
+    cudaMemcpyAsync(L0.U, u0, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream);
+    topo_solve_stats st{};
+    const int rc = topo_solve(h, &o, &st);
+    *ms = st.ms;
+    return rc;
+  };
+  *best = *base;
+  double bt = 1e30;
+  int rc0 = run(*base, &r.base_ms);
+  if (rc0 == TOPO_OK) bt = r.base_ms;
+  const int inners[4] = {1, 2, 4, 6};
+  for (int ii = 0; ii < 4; ++ii)
+    for (int sm = 1; sm <= 2; ++sm)
+      for (int deg = 2; deg <= 3; ++deg) {
+        topo_solve_opts o = *base;
+        o.inner_max = inners[ii];
+        o.pre = o.post = sm;
+        o.cheb_degree = deg;
+        double ms = 0;
+        ++r.candidates;
+        if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+      }
+  r.best_ms = bt;
+  cudaMemcpyAsync(L0.U, u0, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream);
+  CK(cudaEventRecord(t1, h->stream));
+  CK(cudaEventSynchronize(t1));
+  cudaFree(u0);
+  float tms = 0;
+  cudaEventElapsedTime(&tms, t0, t1);
+  r.tune_ms = tms;
+  cudaEventDestroy(t0); cudaEventDestroy(t1); cudaEventDestroy(a); cudaEventDestroy(b);
+  h->err.clear();
+  if (rep) *rep = r;
+  if (bt >= 1e30) return fail(h, TOPO_E_NOT_CONVERGED, "autotune: no schedule converged");
   return TOPO_OK;
 }
 

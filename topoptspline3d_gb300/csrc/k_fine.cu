@@ -712,23 +712,25 @@ void modal_smem_attr(size_t smem) {
 
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
-                       const T* u, const T* f, T* out, bool residual, int nb) {
+                       const T* u, const T* f, T* out, bool residual, int nb, int tz) {
+  if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
-                  ((d.vz + MODAL_TZ - 1) / MODAL_TZ) * nb);
+                  ((d.vz + tz - 1) / tz) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
   modal_smem_attr<T>(smem);
   ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0};
   if (residual)
-    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ, ch);
+    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
   else
-    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ, ch);
+    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
 }
 
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
-                          const double* u, const double* f, double* out, bool residual, int nb) {
+                          const double* u, const double* f, double* out, bool residual, int nb, int tz) {
+  if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
-                  ((d.vz + MODAL_TZ - 1) / MODAL_TZ) * nb);
+                  ((d.vz + tz - 1) / tz) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(ModalSmem<df, MODAL_TXE, MODAL_TYE>);
   static bool attr = false;
@@ -738,30 +740,32 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
     attr = true;
   }
   if (residual)
-    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ);
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz);
   else
-    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, MODAL_TZ);
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz);
 }
 
 // One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u).
 template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb) {
+                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
+                      int tz) {
+  if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
-                  ((d.vz + MODAL_TZ - 1) / MODAL_TZ) * nb);
+                  ((d.vz + tz - 1) / tz) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
   modal_smem_attr<T>(smem);
   ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0};
-  k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, MODAL_TZ, ch);
+  k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, tz, ch);
 }
 
 template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                        const double*, const double*, double*, const double*, double*, double,
-                                       double, bool, int);
+                                       double, bool, int, int);
 template void launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
                                       const float*, const float*, float*, const float*, float*, double, double,
-                                      bool, int);
+                                      bool, int, int);
 
 // Dense-row form of the same operator (thread per vertex, 8 x 3 x 24 products);
 // kept as the cross-check of the modal kernel.
@@ -794,9 +798,9 @@ void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, con
 }
 
 template void launch_fine_apply<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
-                                        const double*, const double*, double*, bool, int);
+                                        const double*, const double*, double*, bool, int, int);
 template void launch_fine_apply<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
-                                       const float*, const float*, float*, bool, int);
+                                       const float*, const float*, float*, bool, int, int);
 template void launch_fine_gs<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                      double*, const double*, int, bool);
 template void launch_fine_gs<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,

@@ -70,10 +70,10 @@ struct Stream {
 // fine level (k_fine.cu)
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
-                       const T* u, const T* f, T* out, bool residual, int nb = 1);
+                       const T* u, const T* f, T* out, bool residual, int nb = 1, int tz = 0);
 // FP64 vectors, double-float arithmetic (k_fine_modal_df)
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
-                          const double* u, const double* f, double* out, bool residual, int nb = 1);
+                          const double* u, const double* f, double* out, bool residual, int nb = 1, int tz = 0);
 template <typename T>
 void launch_fine_gs(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, T* u,
                     const T* f, int colour, bool reverse);
@@ -83,7 +83,7 @@ void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, con
 template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                       const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first,
-                      int nb = 1);
+                      int nb = 1, int tz = 0);
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);

@@ -32,13 +32,21 @@ import numpy as np  # noqa: E402
 METRIC = "ms/design-iter @256x128x128, rel-res 1e-6: mixed vs FP64 MG-PCG, 1 GB300"
 
 
+def metric_for(args):
+    if args.case == "mbb" and args.size == "256x128x128":
+        return METRIC
+    return f"ms/design-iter @{args.size} ({args.case}), rel-res 1e-6: mixed vs FP64 MG-PCG, 1 GB300"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--size", default="256x128x128")
+    ap.add_argument("--size", default=None, help="grid, e.g. 256x128x128 (default per case)")
+    ap.add_argument("--case", default="mbb", choices=["mbb", "ellipsoids"],
+                    help="mbb: half-MBB beam (headline); ellipsoids: large union-of-ellipsoids design")
     ap.add_argument("--smoother", default="chebyshev", choices=["chebyshev", "gs"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="FP64 MG-PCG comparison steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -129,10 +137,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_problem(nx, ny, nz, device, op_precision):
-    from topoptspline3d_gb300 import capi, workloads
-    wl = workloads.half_mbb(nx, ny, nz, lattice=(nx // 4 + 1, ny // 4 + 1, nz // 4 + 1))
-    p = capi.Problem(nx, ny, nz, device=device)
+def make_workload(case, nx, ny, nz):
+    from topoptspline3d_gb300 import workloads
+    if case == "ellipsoids":
+        return workloads.large_ellipsoids(nx, ny, nz)
+    return workloads.half_mbb(nx, ny, nz, lattice=(nx // 4 + 1, ny // 4 + 1, nz // 4 + 1))
+
+
+def make_problem(nx, ny, nz, device, op_precision, case="mbb"):
+    from topoptspline3d_gb300 import capi
+    wl = make_workload(case, nx, ny, nz)
+    p = capi.Problem(nx, ny, nz, device=device, eactive=wl.eactive)
     p.set_bc(wl.fixed, wl.loads)
     bmin, bmax = wl.spline_box()
     p.set_spline(wl.order, wl.partition, bmin, bmax)
@@ -222,6 +237,8 @@ def run_reference(args, nx, ny, nz, ws, rank):
 
 def main():
     args = parse()
+    if args.size is None:
+        args.size = "511x256x256" if args.case == "ellipsoids" else "256x128x128"
     nx, ny, nz = (int(v) for v in args.size.lower().split("x"))
     ws, rank, local, pg = dist_setup()
     if args.impl == "reference":
@@ -229,7 +246,7 @@ def main():
         return
     from topoptspline3d_gb300 import capi
     device = local
-    wl, p = make_problem(nx, ny, nz, device, op_precision=2)
+    wl, p = make_problem(nx, ny, nz, device, op_precision=2, case=args.case)
     opts = solve_opts(capi.SOLVE_MIXED, args.smoother)
     oc = dict(vgoal=wl.vgoal, damp=0.5, step=0.03, cmin=0.0, cmax=1.0)
     if args.profile_iteration:
@@ -325,7 +342,7 @@ def main():
             "achieved_tflops": flops_per / avg_s / 1e12,
             "family_ms": {fams[k][0]: prof[k][1] for k in prof if prof[k][0]}}
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline and args.case == "mbb":
         try:
             cms, cit, crr, cc = cpu_baseline(nx, ny, nz)
             cpu = {"value": cms, "unit": "ms/design-iter", "cores": os.cpu_count(), "kind": "port",
@@ -336,11 +353,12 @@ def main():
                    "sample": f"failed: {e}"}
     h2d = 8 * nc
     d2h = 8 * nc + 8  # coefficients and the compliance scalar
-    out = {"metric": METRIC, "value": ms_step, "unit": "ms/design-iter", "n_gpus": ws, "steps": args.steps,
+    out = {"metric": metric_for(args), "value": ms_step, "unit": "ms/design-iter", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 multigrid / f64 CG", "data": "synthetic",
-           "config": {"workload": f"half-MBB {nx}x{ny}x{nz} spline OC design iteration", "grid": [nx, ny, nz],
-                      "dofs": 3 * nv, "lattice": [nx // 4 + 1, ny // 4 + 1, nz // 4 + 1],
+           "config": {"workload": f"{wl.name} spline OC design iteration", "grid": [nx, ny, nz],
+                      "dofs": 3 * nv, "active_fraction": float(np.mean(wl.eactive)) if wl.eactive is not None else 1.0,
+                      "lattice": [q + wl.order for q in wl.partition],
                       "solver": f"FP64 flexible CG (fine matvec in double-float, ~1e-14 of FP64) + "
                                 f"{opts['inner_max']} FP32 CG its with {args.smoother} V({opts['pre']},"
                                 f"{opts['post']}) degree-{opts['cheb_degree']} multigrid, rel-res 1e-6",

@@ -88,8 +88,10 @@ def perforated(nx, ny, nz, holes=6, radius=(2.0, 4.0), seed=7) -> np.ndarray:
 
 
 def ellipsoid_union(nx, ny, nz, n=12, seed=4000, fill=(0.43, 0.47), axes=(20, 120)) -> np.ndarray:
-    """Active-element mask: union of seeded random ellipsoids, rescaled until the
-    fill fraction falls in ``fill``."""
+    """Active-element mask: union of seeded random ellipsoids (centres uniform in
+    the box, semi-axes uniform in ``axes``, random rotations), rescaled until the
+    fill fraction falls in ``fill``.  The rescale search runs on a subsampled
+    grid; the mask is then evaluated once at full resolution, slab by slab."""
     rng = np.random.default_rng(seed)
     c = rng.uniform((0, 0, 0), (nx, ny, nz), size=(n, 3))
     ax = rng.uniform(axes[0], axes[1], size=(n, 3))
@@ -97,19 +99,70 @@ def ellipsoid_union(nx, ny, nz, n=12, seed=4000, fill=(0.43, 0.47), axes=(20, 12
     for _ in range(n):
         q, _r = np.linalg.qr(rng.standard_normal((3, 3)))
         rot.append(q)
-    zz, yy, xx = np.meshgrid(np.arange(nz) + 0.5, np.arange(ny) + 0.5, np.arange(nx) + 0.5, indexing="ij")
-    pts = np.stack([xx, yy, zz], -1).reshape(-1, 3)
-    scale = 1.0
-    for _ in range(40):
+
+    def inside(pts, scale):
         m = np.zeros(pts.shape[0], bool)
         for k in range(n):
             d = (pts - c[k]) @ rot[k]
             m |= ((d / (ax[k] * scale)) ** 2).sum(1) <= 1.0
-        f = m.mean()
+        return m
+
+    step = max(1, min(nx, ny, nz) // 32)
+    zz, yy, xx = np.meshgrid(np.arange(0, nz, step) + 0.5, np.arange(0, ny, step) + 0.5,
+                             np.arange(0, nx, step) + 0.5, indexing="ij")
+    sub = np.stack([xx, yy, zz], -1).reshape(-1, 3)
+    scale = 1.0
+    for _ in range(60):
+        f = inside(sub, scale).mean()
         if fill[0] <= f <= fill[1]:
             break
         scale *= (0.45 / max(f, 1e-3)) ** (1 / 3)
-    return m.astype(np.uint8)
+    out = np.zeros((nz, ny, nx), bool)
+    yy2, xx2 = np.meshgrid(np.arange(ny) + 0.5, np.arange(nx) + 0.5, indexing="ij")
+    for z in range(nz):
+        pts = np.stack([xx2.ravel(), yy2.ravel(), np.full(xx2.size, z + 0.5)], -1)
+        out[z] = inside(pts, scale).reshape(ny, nx)
+    return out.astype(np.uint8).ravel()
+
+
+def supported_components(eactive, nx, ny, nz, zmax=2) -> np.ndarray:
+    """Keep the face-connected components of an element mask that reach the
+    layer of elements below z = zmax (the supported ones)."""
+    from scipy.ndimage import label
+    m = np.asarray(eactive).reshape(nz, ny, nx) != 0
+    lab, _ = label(m)
+    keep = np.unique(lab[:zmax][lab[:zmax] > 0])
+    return np.isin(lab, keep).astype(np.uint8).ravel()
+
+
+def large_ellipsoids(nx=511, ny=256, nz=256, seed=4000, nloads=64, spacing=4, vgoal=0.3, order=3) -> Workload:
+    """Large design: the supported part of a 12-ellipsoid union filling about
+    45% of the box; every vertex with z <= 2 fixed; `nloads` unit point loads
+    (direction -z) on top-surface vertices chosen with default_rng(seed + 1);
+    spline control spacing `spacing` voxels; volume fraction `vgoal`."""
+    ea = supported_components(ellipsoid_union(nx, ny, nz, seed=seed), nx, ny, nz)
+    vx, vy, vz = nx + 1, ny + 1, nz + 1
+    e3 = ea.reshape(nz, ny, nx).astype(bool)
+    va = np.zeros((vz, vy, vx), bool)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                va[dz:dz + nz, dy:dy + ny, dx:dx + nx] |= e3
+    fixed = np.zeros((vz, vy, vx), np.uint8)
+    fixed[:3][va[:3]] = 7
+    # top surface: the highest active vertex of each (x, y) column
+    top = np.where(va.any(0), vz - 1 - np.argmax(va[::-1], axis=0), -1)
+    cand = np.argwhere(top > 2)
+    rng = np.random.default_rng(seed + 1)
+    pick = cand[rng.choice(cand.shape[0], size=min(nloads, cand.shape[0]), replace=False)]
+    loads = np.zeros((3, vz, vy, vx))
+    for y, x in pick:
+        loads[2, top[y, x], y, x] = -1.0
+    lattice = (nx // spacing + 1, ny // spacing + 1, nz // spacing + 1)
+    part = tuple(n - order for n in lattice)
+    return Workload(f"ellipsoid union {nx}x{ny}x{nz}", nx, ny, nz, fixed.ravel(), loads.ravel(), part, order,
+                    coeff0=vgoal, vgoal=vgoal, eactive=ea,
+                    notes={"fill": float(ea.mean()), "loads": int(len(pick)), "lattice": lattice})
 
 
 def random_density(nx, ny, nz, seed, sigma=None, lo=1e-3) -> np.ndarray:

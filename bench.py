@@ -45,8 +45,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", default=None, help="grid, e.g. 256x128x128 (default per case)")
-    ap.add_argument("--case", default="mbb", choices=["mbb", "ellipsoids"],
-                    help="mbb: half-MBB beam (headline); ellipsoids: large union-of-ellipsoids design")
+    ap.add_argument("--case", default="mbb", choices=["mbb", "ellipsoids", "loads", "designs"],
+                    help="mbb: half-MBB beam (headline); ellipsoids: large union-of-ellipsoids design; "
+                         "loads: 16 load cases in one multi-right-hand-side solve; designs: 32 independent "
+                         "designs of uneven size at once")
     ap.add_argument("--smoother", default="chebyshev", choices=["chebyshev", "gs"])
     ap.add_argument("--fp64-steps", type=int, default=2, help="FP64 MG-PCG comparison steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -235,14 +237,112 @@ def run_reference(args, nx, ny, nz, ws, rank):
     print(json.dumps(out), flush=True)
 
 
+def run_loads(args, rank):
+    """16 load cases on the 192x96x96 cantilever: one multi-right-hand-side solve
+    (every V-cycle launch serves all loads) against 16 single solves."""
+    from topoptspline3d_gb300 import capi, workloads
+    nx, ny, nz = (int(v) for v in args.size.lower().split("x"))
+    nrhs = 16
+    wl = workloads.cantilever(nx, ny, nz, lattice=(nx // 4 + 1, ny // 4 + 1, nz // 4 + 1))
+    p = capi.Problem(nx, ny, nz)
+    p.set_bc(wl.fixed, wl.loads)
+    bmin, bmax = wl.spline_box()
+    p.set_spline(wl.order, wl.partition, bmin, bmax)
+    p.put("coeff", np.full(p.num_coeffs(), wl.coeff0))
+    p.coeff_to_density()
+    p.set_operator_precision(2)
+    p.update_operators()
+    F = workloads.patch_loads(nx, ny, nz, nrhs, seed0=1000, patch=8)
+    p.multi_reserve(nrhs)
+    kw = dict(pre=1, post=1, rtol=1e-6, max_iter=300)
+    for _ in range(args.warmup):
+        p.solve_multi(F, **kw)
+    ms_multi, its = [], []
+    for _ in range(args.steps):
+        U, st, rr = p.solve_multi(F, **kw)
+        ms_multi.append(st["ms"])
+        its.append(st["iterations"])
+    single = dict(mode=capi.SOLVE_MIXED, smoother=capi.SMOOTH_CHEBYSHEV, pre=1, post=1, rtol=1e-6, max_iter=300,
+                  inner_max=1)
+    ms_single = []
+    for k in range(nrhs):
+        p.put("f", F[k])
+        p.put("u", np.zeros(3 * p.nv))
+        ms_single.append(p.solve(**single)["ms"])
+    comp = [float(F[k] @ U[k]) for k in range(nrhs)]
+    ms = statistics.median(ms_multi)
+    out = {"metric": f"ms per {nrhs}-load solve @{nx}x{ny}x{nz}, rel-res 1e-6 (multi-RHS V-cycle), 1 GB300",
+           "value": ms, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32 multigrid / f64 CG",
+           "data": "synthetic",
+           "config": {"workload": f"cantilever {nx}x{ny}x{nz}, {nrhs} seeded 8x8 patch loads",
+                      "solver": "per-load FP64 flexible CG + batched FP32 Chebyshev V(1,1)"},
+           "sequential_single_solves_ms": sum(ms_single), "speedup_vs_sequential": sum(ms_single) / ms,
+           "iterations": its, "max_relres": float(max(rr)), "worst_case_compliance": max(comp),
+           "worst_case_load": int(np.argmax(comp))}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_designs(args, rank):
+    """32 independent cantilever designs of uneven size: all at once (one host
+    thread per design, CUDA-graph V-cycles) against one after another."""
+    from topoptspline3d_gb300 import capi, workloads
+    wls = workloads.batch_cantilevers(32, seed0=2000)
+    solve = dict(mode=capi.SOLVE_MIXED, smoother=capi.SMOOTH_CHEBYSHEV, pre=1, post=1, rtol=1e-6, max_iter=300,
+                 inner_max=4)
+    ocs = [dict(vgoal=w.vgoal) for w in wls]
+
+    def build():
+        ps = []
+        for w in wls:
+            q = capi.Problem(w.nx, w.ny, w.nz)
+            q.set_bc(w.fixed, w.loads)
+            bmin, bmax = w.spline_box()
+            q.set_spline(w.order, w.partition, bmin, bmax)
+            q.put("coeff", np.full(q.num_coeffs(), w.coeff0))
+            q.coeff_to_density()
+            q.set_operator_precision(2)
+            ps.append(q)
+        return ps
+
+    ps = build()
+    capi.design_batch(ps, args.warmup, threads=len(ps), solve=solve, ocs=ocs)
+    # per-design tiles (z-march depth) from the autotuner, untimed
+    tz = []
+    for q in ps:
+        q.update_operators()
+        _, rep = q.autotune(solve)
+        tz.append(rep["tz32"])
+    _, conc = capi.design_batch(ps, args.steps, threads=len(ps), solve=solve, ocs=ocs)
+    _, seq = capi.design_batch(ps, args.steps, threads=1, solve=solve, ocs=ocs)
+    units = len(ps) * args.steps
+    out = {"metric": "design iterations per second, 32 independent cantilevers 32^3..96x48x48, 1 GB300",
+           "value": units / (conc["wall_ms"] / 1e3), "unit": "design-iter/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": conc["wall_ms"] / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 multigrid / f64 CG", "data": "synthetic",
+           "config": {"workload": "32 cantilevers, sizes and volume fractions from default_rng(2000 + d)",
+                      "designs": [w.name for w in wls], "threads": len(ps), "autotuned_tz32": tz},
+           "sequential_design_iter_per_s": units / (seq["wall_ms"] / 1e3),
+           "speedup_vs_sequential": seq["wall_ms"] / conc["wall_ms"]}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.size is None:
-        args.size = "511x256x256" if args.case == "ellipsoids" else "256x128x128"
+        args.size = {"ellipsoids": "511x256x256", "loads": "192x96x96"}.get(args.case, "256x128x128")
     nx, ny, nz = (int(v) for v in args.size.lower().split("x"))
     ws, rank, local, pg = dist_setup()
     if args.impl == "reference":
         run_reference(args, nx, ny, nz, ws, rank)
+        return
+    if args.case == "loads":
+        run_loads(args, rank)
+        return
+    if args.case == "designs":
+        run_designs(args, rank)
         return
     from topoptspline3d_gb300 import capi
     device = local

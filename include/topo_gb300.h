@@ -129,7 +129,8 @@ typedef struct topo_oc_stats {
 /* --- lifetime ------------------------------------------------------------ */
 /* Replaces HierarchyGrid::genFromMesh(const std::vector<unsigned>&, int[3]) (grid/Grid.cpp:977)
  * plus setParameters (optimization/optimization.cpp:35-65) and buildGrids (15-22).
- * eactive: uint8[nx*ny*nz] or NULL (all active). */
+ * eactive: uint8[nx*ny*nz] or NULL (all active).  The element constants are per device:
+ * TOPO_E_BAD_INPUT if another live handle on the device has a different E, nu or h. */
 int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** out);
 /* Replaces HierarchyGrid::~HierarchyGrid (grid/Grid.h:1027-1033) and gpu_manager_t teardown. */
 void topo_destroy(topo_handle* h);
@@ -226,6 +227,11 @@ int topo_apply_fine(topo_handle* h, int precision);
  * error-free transformations, ~48-bit significands, on the FP32 pipe; default).
  * Vectors, dot products and step lengths stay FP64 either way. */
 int topo_set_fine_arithmetic(topo_handle* h, int arith);
+/* FP32 V-cycles of the mixed solver replayed as one CUDA graph per handle
+ * (captured on first use, re-captured when the schedule, spectral bounds,
+ * tiles or buffers change): 1 = on (default), 0 = direct launches.  Graphs are
+ * not used while topo_profile_enable is on. */
+int topo_set_graphs(topo_handle* h, int enable);
 /* Replaces Grid::update_residual (grid/Grid.cu:2420-2454). */
 int topo_residual(topo_handle* h, int level);
 /* Replaces Grid::gs_relax (grid/Grid.cu:1844-1887); reverse = adjoint sweep order. */
@@ -362,6 +368,22 @@ typedef struct topo_iter_stats {
  * (utils/test_utils.cpp:928-958): update_stencil, solve (warm start), compliance,
  * computeSensitivity (sensitivity, filter, spline adjoint) and updateCoeff. */
 int topo_design_iteration(topo_handle* h, const topo_iter_opts* opts, topo_iter_stats* stats);
+
+/* --- many designs at once ------------------------------------------------- */
+/* Independent designs (no reference counterpart): `iterations` design
+ * iterations on each of n handles, run from `threads` host threads so the
+ * handles' streams execute concurrently on the GPU (each handle's FP32 V-cycles
+ * replay as CUDA graphs).  opts: one set for all (nopts = 1) or one per handle.
+ * last[n] (may be NULL) receives each handle's last iteration statistics.
+ * Handles on one device must share E, nu and h (topo_create enforces it). */
+typedef struct topo_batch_stats {
+  double wall_ms;     /* host wall time of the whole batch */
+  double sum_ms;      /* sum over handles of their own wall time */
+  double max_ms;      /* slowest handle */
+  int failures;       /* handles that stopped on an error */
+} topo_batch_stats;
+int topo_design_batch(topo_handle** handles, int n, const topo_iter_opts* opts, int nopts, int iterations,
+                      int threads, topo_iter_stats* last, topo_batch_stats* stats);
 
 /* --- autotuner ------------------------------------------------------------ */
 /* Tile and schedule choice for the current problem state (no reference

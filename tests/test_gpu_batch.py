@@ -1,0 +1,54 @@
+"""Many independent designs of uneven sizes at once (topo_design_batch): the
+concurrent run reproduces, bit for bit, each design run on its own."""
+import numpy as np
+import pytest
+
+from topoptspline3d_gb300 import capi, workloads
+
+pytestmark = pytest.mark.gpu
+
+SOLVE = dict(mode=capi.SOLVE_MIXED, smoother=capi.SMOOTH_CHEBYSHEV, rtol=1e-6, max_iter=300, inner_max=4)
+
+
+def _make(wl):
+    p = capi.Problem(wl.nx, wl.ny, wl.nz)
+    p.set_bc(wl.fixed, wl.loads)
+    bmin, bmax = wl.spline_box()
+    p.set_spline(wl.order, wl.partition, bmin, bmax)
+    p.put("coeff", np.full(p.num_coeffs(), wl.coeff0))
+    p.coeff_to_density()
+    p.set_operator_precision(2)
+    return p
+
+
+def test_batch_equals_sequential():
+    wls = workloads.batch_cantilevers(6, seed0=2000, nx_range=(24, 48), nyz_range=(16, 24))
+    ocs = [dict(vgoal=w.vgoal) for w in wls]
+    batch = [_make(w) for w in wls]
+    last, bs = capi.design_batch(batch, 3, threads=6, solve=SOLVE, ocs=ocs)
+    assert bs["failures"] == 0 and bs["wall_ms"] > 0
+    for k, w in enumerate(wls):
+        p = _make(w)
+        for _ in range(3):
+            s = p.design_iteration(solve=SOLVE, oc=ocs[k])
+        assert s["compliance"] == last[k]["compliance"], k
+        assert np.array_equal(p.get("coeff"), batch[k].get("coeff")), k
+
+
+def test_graphs_do_not_change_results():
+    wl = workloads.small_cases()["mbb32"]
+    runs = []
+    for g in (0, 1):
+        p = _make(wl)
+        p.set_graphs(g)
+        s = [p.design_iteration(solve=SOLVE, oc=dict(vgoal=0.35)) for _ in range(2)]
+        runs.append(([x["compliance"] for x in s], p.get("u")))
+    assert runs[0][0] == runs[1][0] and np.array_equal(runs[0][1], runs[1][1])
+
+
+def test_material_must_match_live_handles():
+    a = capi.Problem(8, 8, 8)
+    with pytest.raises(capi.TopoError):
+        capi.Problem(8, 8, 8, E=2e6)
+    b = capi.Problem(8, 8, 8)  # same material is fine
+    del a, b

@@ -45,7 +45,7 @@ EXPORTED = [
     "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
-    "topo_autotune",
+    "topo_autotune", "topo_set_graphs", "topo_design_batch",
 ]
 
 
@@ -84,6 +84,10 @@ class IterOpts(C.Structure):
 class IterStats(C.Structure):
     _fields_ = [("compliance", C.c_double), ("volume", C.c_double), ("solve", SolveStats),
                 ("oc_trials", C.c_int), ("ms", C.c_double)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("wall_ms", C.c_double), ("sum_ms", C.c_double), ("max_ms", C.c_double), ("failures", C.c_int)]
 
 
 class TuneReport(C.Structure):
@@ -173,6 +177,9 @@ def load(build: bool = True):
         "topo_unet_enable": (i, [vp, C.c_ulonglong]),
         "topo_multi_reserve": (i, [vp, i]),
         "topo_set_fine_arithmetic": (i, [vp, i]),
+        "topo_set_graphs": (i, [vp, i]),
+        "topo_design_batch": (i, [C.POINTER(vp), i, C.POINTER(IterOpts), i, i, i, C.POINTER(IterStats),
+                                  C.POINTER(BatchStats)]),
         "topo_autotune": (i, [vp, C.POINTER(SolveOpts), C.POINTER(SolveOpts), C.POINTER(TuneReport)]),
         "topo_solve_multi": (i, [vp, i, C.POINTER(SolveOpts), C.POINTER(MultiStats), dp]),
         "topo_unet_num_params": (i, [C.POINTER(sz)]),
@@ -416,6 +423,9 @@ class Problem:
     def coeff_to_density(self):
         self._ck(self.lib.topo_coeff_to_density(self.h))
 
+    def set_graphs(self, enable):
+        self._ck(self.lib.topo_set_graphs(self.h, int(enable)))
+
     def set_fine_arithmetic(self, arith):
         """0: native FP64 fine operator, 1: double-float (default)."""
         self._ck(self.lib.topo_set_fine_arithmetic(self.h, arith))
@@ -652,6 +662,19 @@ class Problem:
     def get_into(self, name, host_ptr, count, level=0):
         self._ck(self.lib.topo_get_array(self.h, ARRAYS[name], level, host_ptr, count))
 
+    @staticmethod
+    def iter_opts(solve=None, oc=None, filter_radius=2.0):
+        s = dict(mode=SOLVE_MIXED, smoother=SMOOTH_GS, pre=2, post=2, rtol=1e-6, max_iter=200,
+                 inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1, learned=0,
+                 learned_stall=0.0)
+        s.update(solve or {})
+        c = dict(vgoal=0.4, damp=0.5, step=0.03, cmin=0.0, cmax=1.0, apply_twice=0, reference_volume=1)
+        c.update(oc or {})
+        keys = [f[0] for f in SolveOpts._fields_]
+        return IterOpts(SolveOpts(*[s[k] for k in keys]),
+                        OcOpts(c["vgoal"], c["damp"], c["step"], c["cmin"], c["cmax"], int(c["apply_twice"]),
+                               int(c["reference_volume"])), filter_radius)
+
     def design_iteration(self, solve=None, oc=None, filter_radius=2.0):
         s = dict(mode=SOLVE_MIXED, smoother=SMOOTH_GS, pre=2, post=2, rtol=1e-6, max_iter=200,
                  inner_rtol=1e-1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1, learned=0,
@@ -784,3 +807,21 @@ def mma_design_iteration(p, mma, vfrac, dvol_ptr=None, solve=None, filter_radius
     st = mma.update(p.device_ptr("csens"), [dvol_ptr], [vol_scale * (vol - vfrac)])
     st.update({"compliance": c, "volume": vol, "iterations": r["iterations"], "relres": r["relres"]})
     return st
+
+
+def design_batch(problems, iterations, threads=None, solve=None, ocs=None, filter_radius=2.0):
+    """topo_design_batch: `iterations` design iterations on every problem, from
+    `threads` host threads (default: one per problem).  ocs: one OC dict per
+    problem (or None).  Returns (per-problem last-iteration stats, batch stats)."""
+    lib = load()
+    n = len(problems)
+    hs = (C.c_void_p * n)(*[p.h for p in problems])
+    opts = (IterOpts * n)(*[Problem.iter_opts(solve, (ocs[k] if ocs else None), filter_radius) for k in range(n)])
+    last = (IterStats * n)()
+    bs = BatchStats()
+    rc = lib.topo_design_batch(hs, n, opts, n, iterations, threads or n, last, C.byref(bs))
+    if rc not in (TOPO_OK, TOPO_E_NOT_CONVERGED):
+        raise TopoError(rc, "topo_design_batch")
+    out = [{"compliance": s.compliance, "volume": s.volume, "iterations": s.solve.iterations, "ms": s.ms}
+           for s in last]
+    return out, {"wall_ms": bs.wall_ms, "sum_ms": bs.sum_ms, "max_ms": bs.max_ms, "failures": bs.failures}

@@ -2,6 +2,10 @@
 // orchestration of the hot path (operator update, V-cycle, PCG, mixed-precision
 // defect correction, sensitivity chain and OC bisection).
 #include <algorithm>
+#include <thread>
+#include <mutex>
+#include <chrono>
+#include <atomic>
 #include <array>
 #include <cmath>
 #include <cstdarg>
@@ -37,9 +41,22 @@ struct EventPair {
 struct topo_handle {
   topo_config cfg{};
   topo::UNetState* unet = nullptr;  // learned preconditioner (topo_unet_enable)
+  bool mat_registered = false;      // holds a reference on the device's element constants
   int nb = 1;                       // right-hand sides the level vectors hold (multi-RHS solve)
   int fine_df = 1;                  // FP64 fine operator in double-float arithmetic (topo_set_fine_arithmetic)
   int tz32 = 16, tz64 = 16;         // z-march depth of the fine kernels, FP32 / FP64 (topo_autotune)
+  // FP32 V-cycle replayed as one CUDA graph (topo_set_graphs); re-captured when its key changes
+  bool graphs = true;
+  cudaGraphExec_t vgraph = nullptr;
+  std::vector<double> vkey;
+  long long vgraph_kernels = 0;
+  // profiling inside the graph: event pairs captured as external event-record
+  // nodes, collected after each replay has completed
+  bool capturing = false;
+  std::vector<std::pair<int, EventPair>> gprof;
+  bool gprof_pending = false;
+  double gprof_ms[TOPO_K_COUNT] = {0};
+  int gprof_n[TOPO_K_COUNT] = {0};
   topo::MultiRhs* multi = nullptr;  // batched buffers (topo_multi_reserve)
   int unet_crops = 64;              // crops per harvested iterate
   cudaStream_t stream = nullptr;
@@ -152,6 +169,14 @@ int dalloc(topo_handle* h, T** p, int64_t n) {
 // ---- profiling brackets --------------------------------------------------
 EventPair* prof_begin(topo_handle* h, int fam) {
   if (!h->prof) return nullptr;
+  if (h->capturing) {
+    EventPair g;
+    cudaEventCreate(&g.a);
+    cudaEventCreate(&g.b);
+    cudaEventRecordWithFlags(g.a, h->stream, cudaEventRecordExternal);
+    h->gprof.push_back({fam, g});
+    return &h->gprof.back().second;
+  }
   EventPair p;
   if (!h->evpool.empty()) {
     p = h->evpool.back();
@@ -165,7 +190,30 @@ EventPair* prof_begin(topo_handle* h, int fam) {
   return &h->evs[fam].back();
 }
 void prof_end(topo_handle* h, EventPair* p) {
-  if (p) cudaEventRecord(p->b, h->stream);
+  if (!p) return;
+  if (h->capturing) cudaEventRecordWithFlags(p->b, h->stream, cudaEventRecordExternal);
+  else cudaEventRecord(p->b, h->stream);
+}
+
+// Adds the timings of the last graph replay to the profile (the replay must be
+// complete before its events are re-recorded by the next one).
+void prof_collect(topo_handle* h) {
+  if (!h->gprof_pending) return;
+  cudaEventSynchronize(h->gprof.back().second.b);
+  for (auto& fp : h->gprof) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, fp.second.a, fp.second.b) == cudaSuccess) {
+      h->gprof_ms[fp.first] += t;
+      h->gprof_n[fp.first] += 1;
+    }
+  }
+  h->gprof_pending = false;
+}
+
+void prof_drop_graph_events(topo_handle* h) {
+  for (auto& fp : h->gprof) { cudaEventDestroy(fp.second.a); cudaEventDestroy(fp.second.b); }
+  h->gprof.clear();
+  h->gprof_pending = false;
 }
 
 // ---- level operations (templated on precision) ---------------------------
@@ -346,6 +394,55 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
   }
 }
 
+// The FP32 preconditioning V-cycle as one CUDA graph launch.  The cycle is a
+// fixed sequence of kernels, memsets and device copies for a given schedule,
+// spectral bounds, tiles and buffers, so it is captured once and replayed;
+// any change of that key re-captures it.  Small grids and the coarse levels
+// are launch-bound, and one graph launch replaces about forty.
+static void vcycle32(topo_handle* h, int pre, int post, int smoother, const ChebParams& cp) {
+  if (!h->graphs) {
+    vcycle_core<float>(h, pre, post, true, smoother, cp);
+    return;
+  }
+  prof_collect(h);
+  std::vector<double> key = {(double)pre, (double)post, (double)smoother, (double)cp.degree, cp.lo, cp.hi,
+                             (double)h->tz32, (double)h->nb, (double)h->prof};
+  for (const DevLevel& L : h->lv) {
+    key.push_back(L.lmax32);
+    key.push_back((double)(uintptr_t)L.U32);
+    key.push_back((double)(uintptr_t)L.F32);
+  }
+  if (!h->vgraph || key != h->vkey) {
+    if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
+    prof_drop_graph_events(h);
+    const long long l0 = g_launches.load();
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      h->capturing = true;
+      vcycle_core<float>(h, pre, post, true, smoother, cp);
+      h->capturing = false;
+      ok = cudaStreamEndCapture(h->stream, &g) == cudaSuccess && g;
+    }
+    h->vgraph_kernels = g_launches.load() - l0;
+    g_launches.fetch_sub(h->vgraph_kernels);
+    if (ok) ok = cudaGraphInstantiate(&h->vgraph, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (!ok) {  // capture not available: launch directly from now on
+      h->vgraph = nullptr;
+      h->graphs = false;
+      prof_drop_graph_events(h);
+      vcycle_core<float>(h, pre, post, true, smoother, cp);
+      return;
+    }
+    h->vkey = key;
+  }
+  cudaGraphLaunch(h->vgraph, h->stream);
+  count_launch((int)h->vgraph_kernels);
+  h->gprof_pending = h->prof && !h->gprof.empty();
+}
+
 // Power iteration for the largest eigenvalue of D^{-1} A on a level, from the
 // same deterministic start vector as the oracle.
 template <typename T>
@@ -479,7 +576,8 @@ int vcycle_prec(topo_handle* h, const T* r, int pre, int post, int smoother, con
   const int64_t n3 = 3 * L0.d.nv;
   CK(cudaMemcpyAsync(P<T>::F(L0), r, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemsetAsync(P<T>::U(L0), 0, sizeof(T) * n3, h->stream));
-  vcycle_core<T>(h, pre, post, true, smoother, cp);
+  if (sizeof(T) == 4) vcycle32(h, pre, post, smoother, cp);
+  else vcycle_core<T>(h, pre, post, true, smoother, cp);
   return TOPO_OK;
 }
 
@@ -504,6 +602,29 @@ int update_penalised_if_stale(topo_handle* h) {
 
 // ===========================================================================
 // C ABI
+// The element constants live in __constant__ memory, one copy per device: live
+// handles on a device must share E, nu and h.
+namespace {
+std::mutex g_mat_mutex;
+struct MatReg { int refs = 0; double E = 0, nu = 0, h = 0; };
+MatReg g_mat[64];
+}  // namespace
+
+static bool material_acquire(const topo_config* c) {
+  if (c->device < 0 || c->device >= 64) return false;
+  std::lock_guard<std::mutex> lock(g_mat_mutex);
+  MatReg& m = g_mat[c->device];
+  if (m.refs > 0 && (m.E != c->youngs_modulus || m.nu != c->poisson_ratio || m.h != c->h)) return false;
+  m.E = c->youngs_modulus; m.nu = c->poisson_ratio; m.h = c->h;
+  ++m.refs;
+  return true;
+}
+static void material_release(int device) {
+  if (device < 0 || device >= 64) return;
+  std::lock_guard<std::mutex> lock(g_mat_mutex);
+  if (g_mat[device].refs > 0) --g_mat[device].refs;
+}
+
 // ===========================================================================
 extern "C" {
 
@@ -516,6 +637,11 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     return TOPO_E_BAD_INPUT;
   if ((int64_t)(cfg->nx + 1) * (cfg->ny + 1) * (cfg->nz + 1) >= ((int64_t)1 << 31))
     return TOPO_E_BAD_INPUT;
+  if (!material_acquire(cfg)) return TOPO_E_BAD_INPUT;  // other live handles on the device use other E, nu, h
+  struct Release {
+    int dev; bool keep = false;
+    ~Release() { if (!keep) material_release(dev); }
+  } release{cfg->device};
   auto h = std::make_unique<topo_handle>();
   h->cfg = *cfg;
   if (h->cfg.max_coarse_elements <= 0) h->cfg.max_coarse_elements = 400;
@@ -608,6 +734,8 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     (void)msg;
     return rc;
   }
+  h->mat_registered = true;
+  release.keep = true;
   *out = h.release();
   return TOPO_OK;
 }
@@ -616,6 +744,9 @@ void topo_destroy(topo_handle* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->unet) unet_free(h->unet);
+  if (h->mat_registered) material_release(h->cfg.device);
+  if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
+  prof_drop_graph_events(h);
   if (h->multi) {
     for (void* p : h->multi->allocs) cudaFree(p);
     delete h->multi;
@@ -1137,7 +1268,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
         launch_d2f(h->stream, r, L0.F32, n3);
         CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3, h->stream));
         ++nvc;
-        vcycle_core<float>(h, o->pre, o->post, true, o->smoother, cp);
+        vcycle32(h, o->pre, o->post, o->smoother, cp);
         RET(net(L0.F32, L0.U32));
         if (harvest && rn > 1e-4 * fn) {
           const cudaError_t e = unet_harvest_record(h->unet, h->stream, n3, r, L0.U32, h->x, 8);
@@ -1269,10 +1400,58 @@ static void fine64(topo_handle* h, const LevelDims& d, const double* u, const do
   else launch_fine_apply<double>(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb, h->tz64);
 }
 
+int topo_set_graphs(topo_handle* h, int enable) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  h->graphs = enable != 0;
+  if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
+  return TOPO_OK;
+}
+
 int topo_set_fine_arithmetic(topo_handle* h, int arith) {
   if (!h || arith < 0 || arith > 1) return TOPO_E_BAD_INPUT;
   h->fine_df = arith;
   return TOPO_OK;
+}
+
+int topo_design_batch(topo_handle** hs, int n, const topo_iter_opts* opts, int nopts, int iterations, int threads,
+                      topo_iter_stats* last, topo_batch_stats* st) {
+  if (!hs || n <= 0 || !opts || (nopts != 1 && nopts != n) || iterations < 0 || threads <= 0) return TOPO_E_BAD_INPUT;
+  for (int i = 0; i < n; ++i)
+    if (!hs[i]) return TOPO_E_BAD_INPUT;
+  std::atomic<int> next{0}, failures{0}, first_rc{TOPO_OK};
+  std::vector<double> busy(n, 0.0);
+  const auto t0 = std::chrono::steady_clock::now();
+  auto worker = [&]() {
+    for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+      const topo_iter_opts& o = opts[nopts == 1 ? 0 : k];
+      const auto a = std::chrono::steady_clock::now();
+      for (int it = 0; it < iterations; ++it) {
+        topo_iter_stats s{};
+        const int rc = topo_design_iteration(hs[k], &o, &s);
+        if (rc != TOPO_OK && rc != TOPO_E_NOT_CONVERGED) {
+          ++failures;
+          int expect = TOPO_OK;
+          first_rc.compare_exchange_strong(expect, rc);
+          break;
+        }
+        if (last) last[k] = s;
+      }
+      busy[k] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+    }
+  };
+  const int nt = std::min(threads, n);
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+  if (st) {
+    st->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    st->sum_ms = 0;
+    st->max_ms = 0;
+    for (double b : busy) { st->sum_ms += b; st->max_ms = std::max(st->max_ms, b); }
+    st->failures = failures.load();
+  }
+  return first_rc.load();
 }
 
 int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* best, topo_tune_report* rep) {
@@ -1466,7 +1645,7 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
     // z = V(r): one FP32 V-cycle for the whole batch
     launch_d2f(h->stream, m.r, L0.F32, n3 * nb);
     CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3 * nb, h->stream));
-    vcycle_core<float>(h, o->pre, o->post, true, TOPO_SMOOTH_CHEBYSHEV, cp);
+    vcycle32(h, o->pre, o->post, TOPO_SMOOTH_CHEBYSHEV, cp);
     ++nvc;
     k_to_double<float><<<nb256(n3 * nb), 256, 0, h->stream>>>(n3 * nb, L0.U32, m.z);
     launch_bdot<double>(h->stream, m.r, m.z, n3, nb, m.part, slot(B_RZ));
@@ -1843,20 +2022,25 @@ int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_sta
 int topo_profile_enable(topo_handle* h, int enable) {
   if (!h) return TOPO_E_BAD_INPUT;
   h->prof = enable != 0;
+  for (int f = 0; f < TOPO_K_COUNT; ++f) { h->gprof_ms[f] = 0; h->gprof_n[f] = 0; }
   return TOPO_OK;
 }
 
 int topo_profile_read(topo_handle* h, int family, int* launches, double* ms) {
   if (!h || family < 0 || family >= TOPO_K_COUNT) return TOPO_E_BAD_INPUT;
   CK(cudaStreamSynchronize(h->stream));
-  double tot = 0;
+  prof_collect(h);
+  double tot = h->gprof_ms[family];
+  const int ng = h->gprof_n[family];
+  h->gprof_ms[family] = 0;
+  h->gprof_n[family] = 0;
   for (auto& p : h->evs[family]) {
     float t = 0;
     cudaEventElapsedTime(&t, p.a, p.b);
     tot += t;
     h->evpool.push_back(p);
   }
-  if (launches) *launches = (int)h->evs[family].size();
+  if (launches) *launches = (int)h->evs[family].size() + ng;
   if (ms) *ms = tot;
   h->evs[family].clear();
   return TOPO_OK;

@@ -4,6 +4,8 @@
 // (element/templateMatrix.cpp:31-99).  Rows of fixed DOFs and inactive vertices
 // are zero; vectors are kept zero on fixed DOFs, which removes the fixed columns
 // exactly as the reference's WS kernels do (grid/Grid.cu:2277-2333, 1699-1842).
+#include <mutex>
+
 #include "topo_internal.h"
 
 namespace topo {
@@ -702,12 +704,12 @@ constexpr int MODAL_TXE = 32, MODAL_TYE = 8, MODAL_TZ = 16;
 // Opt the modal kernels into more than 48 KB of dynamic shared memory (once).
 template <typename T>
 void modal_smem_attr(size_t smem) {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  done = true;
+  static std::once_flag once;
+  std::call_once(once, [smem] {
+    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
 }
 
 template <typename T>
@@ -733,12 +735,11 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
                   ((d.vz + tz - 1) / tz) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(ModalSmem<df, MODAL_TXE, MODAL_TYE>);
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag once;
+  std::call_once(once, [smem] {
     cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  });
   if (residual)
     k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz);
   else

@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "topo_internal.h"
 
@@ -430,13 +431,13 @@ static size_t conv_smem() {
 template <int CIN, int COUT>
 static cudaError_t conv_launch(cudaStream_t s, const ConvIn& in, const __nv_bfloat16* W, const float* bias, int X,
                                int Y, int Z, int nb, int relu, int out_mode, void* out) {
-  static bool attr = false;
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
   const size_t smem = conv_smem<CIN, COUT>();
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  std::call_once(once, [smem] {
+    attr_err = cudaFuncSetAttribute(k_conv3<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
+  if (attr_err != cudaSuccess) return attr_err;
   dim3 grid((X + kTX - 1) / kTX, (Y + kTY - 1) / kTY, nb * Z / kTZ);
   k_conv3<CIN, COUT><<<grid, kConvThreads, smem, s>>>(in, W, bias, X, Y, Z, relu, out_mode, out);
   return cudaGetLastError();

@@ -200,3 +200,23 @@ def patch_loads(nx, ny, nz, nrhs, seed0=1000, patch=8) -> np.ndarray:
                 for c in range(3):
                     out[k, c * nv + v] = d[c] / npn
     return out
+
+
+def batch_cantilevers(n=32, seed0=2000, nx_range=(32, 96), nyz_range=(32, 48), vf_range=(0.2, 0.5), spacing=4):
+    """Independent cantilever designs of uneven sizes: for d = 0..n-1, with
+    rng = default_rng(seed0 + d), nx uniform in nx_range, ny and nz uniform in
+    nyz_range (integers, inclusive), volume fraction uniform in vf_range;
+    cantilever boundary conditions; spline control spacing `spacing` voxels."""
+    out = []
+    for d in range(n):
+        rng = np.random.default_rng(seed0 + d)
+        nx = int(rng.integers(nx_range[0], nx_range[1] + 1))
+        ny = int(rng.integers(nyz_range[0], nyz_range[1] + 1))
+        nz = int(rng.integers(nyz_range[0], nyz_range[1] + 1))
+        vf = float(rng.uniform(*vf_range))
+        wl = cantilever(nx, ny, nz, lattice=(nx // spacing + 1, ny // spacing + 1, nz // spacing + 1))
+        wl.vgoal = vf
+        wl.coeff0 = vf
+        wl.name = f"cantilever {nx}x{ny}x{nz} vf {vf:.3f}"
+        out.append(wl)
+    return out

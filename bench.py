@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default solver schedule and tiles")
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run exactly one mixed design iteration and exit (for ncu captures)")
+    ap.add_argument("--schedule", default=None,
+                    help="inner,pre,degree,tz32,tz64: use this mixed-solver schedule and these tiles instead of "
+                         "autotuning (e.g. the values an earlier run's autotune chose)")
     ap.add_argument("--profile-solve-steps", type=int, default=0,
                     help="with --profile-iteration: stop the solve after this many outer CG steps")
     return ap.parse_args()
@@ -349,6 +352,11 @@ def main():
     wl, p = make_problem(nx, ny, nz, device, op_precision=2, case=args.case)
     opts = solve_opts(capi.SOLVE_MIXED, args.smoother)
     oc = dict(vgoal=wl.vgoal, damp=0.5, step=0.03, cmin=0.0, cmax=1.0)
+    if args.schedule:
+        inner, pre, deg, tz32, tz64 = (int(v) for v in args.schedule.split(","))
+        opts.update(inner_max=inner, pre=pre, post=pre, cheb_degree=deg)
+        p.set_tiles(tz32, tz64)
+        args.no_autotune = True
     if args.profile_iteration:
         if args.profile_solve_steps > 0:
             opts["max_iter"] = args.profile_solve_steps

@@ -403,6 +403,9 @@ typedef struct topo_tune_report {
   double tune_ms;           /* device time spent tuning */
 } topo_tune_report;
 int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* best, topo_tune_report* report);
+/* Sets the fine kernels' z-march depths (FP32 kernels, FP64 operator) directly,
+ * e.g. to replay an earlier autotune result. */
+int topo_set_tiles(topo_handle* h, int tz32, int tz64);
 
 /* --- many load cases in one solve ------------------------------------------ */
 /* Multi-right-hand-side solve (config "batched": many load cases as right-hand

@@ -20,9 +20,10 @@ def _problem():
     return p
 
 
-def _solve(p, rho, **kw):
-    p.put("rho", rho)
-    p.update_operators()
+def _solve(p, rho, update=True, **kw):
+    if update:
+        p.put("rho", rho)
+        p.update_operators()
     p.put("u", np.zeros(3 * p.nv))
     opts = dict(mode=capi.SOLVE_MIXED, smoother=capi.SMOOTH_CHEBYSHEV, pre=2, post=2, rtol=1e-6, max_iter=200,
                 inner_max=1)
@@ -40,10 +41,11 @@ def test_learned_requires_enable_and_valid_options():
     with pytest.raises(capi.TopoError) as e:
         _solve(p, rho, learned=2, inner_max=4)
     assert e.value.code == capi.TOPO_E_BAD_INPUT
-    # untrained network: zero last layer, same iterates as without it
+    # untrained network: zero last layer, same iterates as without it (same
+    # operators and spectral bounds for both solves)
     a = _solve(p, rho, learned=0)
     ua = p.get("u")
-    b = _solve(p, rho, learned=1)
+    b = _solve(p, rho, update=False, learned=1)
     assert b["learned_applied"] == b["vcycles"] and a["iterations"] == b["iterations"]
     assert np.array_equal(ua, p.get("u"))
 
@@ -72,7 +74,7 @@ def test_harvest_train_ablation():
     # the positivity guard and stagnation fallback keep the learned solve sound
     rho = workloads.random_density(NX, NY, NZ, 3999)
     plain = _solve(p, rho, learned=0)
-    learned = _solve(p, rho, learned=1)
+    learned = _solve(p, rho, update=False, learned=1)
     print(f"ablation: V-cycle {plain['iterations']} its {plain['ms']:.2f} ms; "
           f"V-cycle + U-Net {learned['iterations']} its {learned['ms']:.2f} ms "
           f"(applied {learned['learned_applied']}, fallback {learned['learned_fallback']})")

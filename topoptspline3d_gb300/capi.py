@@ -45,7 +45,7 @@ EXPORTED = [
     "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
-    "topo_autotune", "topo_set_graphs", "topo_design_batch",
+    "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles",
 ]
 
 
@@ -178,6 +178,7 @@ def load(build: bool = True):
         "topo_multi_reserve": (i, [vp, i]),
         "topo_set_fine_arithmetic": (i, [vp, i]),
         "topo_set_graphs": (i, [vp, i]),
+        "topo_set_tiles": (i, [vp, i, i]),
         "topo_design_batch": (i, [C.POINTER(vp), i, C.POINTER(IterOpts), i, i, i, C.POINTER(IterStats),
                                   C.POINTER(BatchStats)]),
         "topo_autotune": (i, [vp, C.POINTER(SolveOpts), C.POINTER(SolveOpts), C.POINTER(TuneReport)]),
@@ -422,6 +423,9 @@ class Problem:
     # --- hot path
     def coeff_to_density(self):
         self._ck(self.lib.topo_coeff_to_density(self.h))
+
+    def set_tiles(self, tz32, tz64):
+        self._ck(self.lib.topo_set_tiles(self.h, tz32, tz64))
 
     def set_graphs(self, enable):
         self._ck(self.lib.topo_set_graphs(self.h, int(enable)))

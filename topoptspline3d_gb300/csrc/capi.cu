@@ -89,6 +89,7 @@ struct topo_handle {
   int ndense = 0;
   double* A = nullptr;
   float* A32 = nullptr;
+  double* gjwork = nullptr;  // panels of the blocked Gauss-Jordan inversion
   double* coarse64tmp = nullptr;  // FP64 copy of an FP32 coarsest stencil
   int* status = nullptr;
   // first coarse level: elements whose fine elements touch fixed DOFs
@@ -229,6 +230,8 @@ template <> struct P<double> {
   static double* rhop(topo_handle* h) { return h->rhop; }
   static double* Ainv(topo_handle* h) { return h->A; }
   static double& lmax(DevLevel& L) { return L.lmax; }
+  static double*& eig(DevLevel& L) { return L.eig; }
+  static double& lprev(DevLevel& L) { return L.lprev; }
   static const int fam_apply = TOPO_K_FINE_APPLY64, fam_smooth = TOPO_K_FINE_SMOOTH64;
 };
 template <> struct P<float> {
@@ -242,6 +245,8 @@ template <> struct P<float> {
   static float* rhop(topo_handle* h) { return h->rhop32; }
   static float* Ainv(topo_handle* h) { return h->A32; }
   static double& lmax(DevLevel& L) { return L.lmax32; }
+  static float*& eig(DevLevel& L) { return L.eig32; }
+  static double& lprev(DevLevel& L) { return L.lprev32; }
   static const int fam_apply = TOPO_K_FINE_APPLY32, fam_smooth = TOPO_K_FINE_SMOOTH32;
 };
 
@@ -484,21 +489,45 @@ int estimate_lmax(topo_handle* h, int l, double* out) {
   T* x = P<T>::R(L);
   T* xn = P<T>::cd(L);
   T* z = P<T>::U2(L);
-  k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, x);
-  count_launch();
-  for (int it = 0; it < 12; ++it) {
-    launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP);
-    launch_scale_by_rnorm<T>(h->stream, x, xn, h->sc, S_TMP, n3);
-    if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, xn, nullptr, x, false);
-    else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), xn, nullptr, x, false);
-    k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), x, z);
-    launch_dot<T>(h->stream, xn, z, n3, h->partial, h->sc + S_TMP + 1);
-    std::swap(x, z);
-    count_launch(7);
+  // First estimate: 12 steps from the deterministic start (as the oracle).
+  // After an operator update: 4 steps from the previous design's vector (the
+  // design moves a little per iteration, so the estimate keeps refining); if
+  // that estimate falls more than 5% below the previous one (an abrupt change
+  // of the operator), continue to 12 steps.
+  int steps = 12;
+  const bool warm = P<T>::eig(L) != nullptr;
+  if (warm) {
+    CK(cudaMemcpyAsync(x, P<T>::eig(L), sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    steps = 4;
+  } else {
+    RET(dalloc(h, &P<T>::eig(L), n3));
+    k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, x);
+    count_launch();
   }
+  auto power_steps = [&](int k) {
+    for (int it = 0; it < k; ++it) {
+      launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP);
+      launch_scale_by_rnorm<T>(h->stream, x, xn, h->sc, S_TMP, n3);
+      if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, xn, nullptr, x, false, 1,
+                                       sizeof(T) == 4 ? h->tz32 : h->tz64);
+      else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), xn, nullptr, x, false);
+      k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), x, z);
+      launch_dot<T>(h->stream, xn, z, n3, h->partial, h->sc + S_TMP + 1);
+      std::swap(x, z);
+      count_launch(7);
+    }
+  };
+  power_steps(steps);
+  if (warm) {
+    CK(cudaMemcpyAsync(h->hsc, h->sc + S_TMP + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->hsc[0] < 0.95 * P<T>::lprev(L)) power_steps(8);
+  }
+  CK(cudaMemcpyAsync(P<T>::eig(L), x, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemcpyAsync(h->hsc, h->sc + S_TMP + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   *out = h->hsc[0];
+  P<T>::lprev(L) = h->hsc[0];
   return TOPO_OK;
 }
 
@@ -701,6 +730,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     else {
       A(dalloc(hp, &h->A, (int64_t)h->ndense * h->ndense));
       A(dalloc(hp, &h->A32, (int64_t)h->ndense * h->ndense));
+      A(dalloc(hp, &h->gjwork, 64 * (int64_t)h->ndense + 32 * 32));
       A(dalloc(hp, &h->coarse64tmp, 243 * dl.nv));
     }
     std::vector<double> T;
@@ -1037,7 +1067,7 @@ int topo_update_operators(topo_handle* h) {
     launch_dense_from_stencil(h->stream, Lc.d, st, h->A);
     count_launch(2);
     CKL();
-    int e = coarsest_invert(h->stream, h->ndense, h->A, nullptr, h->status);
+    int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status);
     count_launch();
     if (e != (int)cudaSuccess)
       return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));
@@ -1398,6 +1428,13 @@ static void fine64(topo_handle* h, const LevelDims& d, const double* u, const do
                    int nb) {
   if (h->fine_df) launch_fine_apply_df(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb, h->tz64);
   else launch_fine_apply<double>(h->stream, d, h->rhop, h->lv[0].vmask, u, f, out, residual, nb, h->tz64);
+}
+
+int topo_set_tiles(topo_handle* h, int tz32, int tz64) {
+  if (!h || tz32 < 1 || tz32 > 256 || tz64 < 1 || tz64 > 256) return TOPO_E_BAD_INPUT;
+  h->tz32 = tz32;
+  h->tz64 = tz64;
+  return TOPO_OK;
 }
 
 int topo_set_graphs(topo_handle* h, int enable) {

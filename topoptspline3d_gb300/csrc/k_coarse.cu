@@ -603,6 +603,124 @@ __global__ void k_gauss_jordan(int n, double* A, int* status) {
   }
 }
 
+// Blocked Gauss-Jordan inversion (in place, SPD matrix, same pivot-drop rule as
+// k_gauss_jordan).  For each panel K of GJB pivots: one CTA inverts the
+// diagonal block D = A[K,K] pivot by pivot in shared memory (dropping pivots
+// <= tol); all CTAs form the row panel P = D^-1 A[K,:] and copy the column panel
+// C = A[:,K]; then every element gets its rank-GJB update
+//   A[i,c] = D^-1 | P | -C D^-1 | A[i,c] - C[i,:] P[:,c]
+// for (i in K, c in K) | (i in K) | (c in K) | otherwise.  Three grid barriers
+// per panel instead of two per pivot.
+constexpr int GJB = 32;
+
+__global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ A, double* __restrict__ work,
+                                                    int* __restrict__ status) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ double sd[GJB][GJB + 1];
+  __shared__ double sc[GJB][GJB + 1];
+  __shared__ double sp[GJB][GJB + 1];
+  __shared__ int sflag;
+  double* Dg = work;                 // [GJB][GJB]
+  double* P = work + GJB * GJB;      // [GJB][n]
+  double* Cp = P + (int64_t)GJB * n; // [n][GJB]
+  const int tid = threadIdx.x;
+  double dmax = 0.0;
+  for (int k = 0; k < n; ++k) dmax = fmax(dmax, fabs(A[(int64_t)k * n + k]));
+  const double tol = 1e-10 * dmax;
+  const int nblk_tiles = (n + GJB - 1) / GJB;
+  for (int k0 = 0; k0 < n; k0 += GJB) {
+    const int kb = min(GJB, n - k0);
+    // ---- A: invert the diagonal block (CTA 0)
+    if (blockIdx.x == 0) {
+      for (int e = tid; e < GJB * GJB; e += blockDim.x) {
+        const int r = e / GJB, c = e % GJB;
+        sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+      }
+      if (tid == 0) sflag = 0;
+      __syncthreads();
+      for (int j = 0; j < kb; ++j) {
+        const double p = sd[j][j];
+        if (p < -tol) {
+          if (tid == 0) { status[1] = k0 + j + 1; sflag = 1; }
+          break;
+        }
+        __syncthreads();
+        if (p <= tol) {  // drop DOF k0 + j
+          for (int e = tid; e < 2 * GJB; e += blockDim.x) {
+            if (e < GJB) sd[j][e] = 0.0;
+            else sd[e - GJB][j] = 0.0;
+          }
+          if (tid == 0) status[0] += 1;
+          __syncthreads();
+          continue;
+        }
+        const double rp = 1.0 / p;
+        for (int e = tid; e < kb * kb; e += blockDim.x) {
+          const int r = e / kb, c = e % kb;
+          if (r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
+        }
+        __syncthreads();
+        for (int e = tid; e < 2 * kb; e += blockDim.x) {
+          if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
+          else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
+        }
+        __syncthreads();
+      }
+      __syncthreads();
+      for (int e = tid; e < GJB * GJB; e += blockDim.x) Dg[e] = sd[e / GJB][e % GJB];
+    }
+    grid.sync();
+    if (status[1]) return;  // indefinite pivot: every CTA sees it after the barrier
+    // ---- B: row panel P = D^-1 A[K,:] (columns outside K) and column panel C = A[:,K]
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid, gs = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = gt; e < (int64_t)kb * n; e += gs) {
+      const int r = (int)(e / n), c = (int)(e % n);
+      double v = 0.0;
+      if (c < k0 || c >= k0 + kb)
+        for (int m = 0; m < kb; ++m) v += Dg[r * GJB + m] * A[(int64_t)(k0 + m) * n + c];
+      P[(int64_t)r * n + c] = v;
+    }
+    for (int64_t e = gt; e < (int64_t)n * kb; e += gs) {
+      const int i = (int)(e / kb), m = (int)(e % kb);
+      Cp[(int64_t)i * GJB + m] = (i < k0 || i >= k0 + kb) ? A[(int64_t)i * n + k0 + m] : 0.0;
+    }
+    grid.sync();
+    // ---- C: rank-kb update, GJB x GJB tiles of A per CTA iteration
+    for (int t = blockIdx.x; t < nblk_tiles * nblk_tiles; t += gridDim.x) {
+      const int ti = (t / nblk_tiles) * GJB, tc = (t % nblk_tiles) * GJB;
+      __syncthreads();
+      for (int e = tid; e < GJB * GJB; e += blockDim.x) {
+        const int r = e / GJB, c = e % GJB;
+        sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : 0.0;
+        sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : 0.0;
+        sd[r][c] = Dg[r * GJB + c];
+      }
+      __syncthreads();
+      for (int e = tid; e < GJB * GJB; e += blockDim.x) {
+        const int r = e / GJB, c = e % GJB;
+        const int i = ti + r, col = tc + c;
+        if (i >= n || col >= n) continue;
+        const bool iK = i >= k0 && i < k0 + kb, cK = col >= k0 && col < k0 + kb;
+        double& a = A[(int64_t)i * n + col];
+        if (iK && cK) {
+          a = sd[i - k0][col - k0];
+        } else if (iK) {
+          a = sp[i - k0][c];
+        } else if (cK) {
+          double v = 0.0;
+          for (int m = 0; m < kb; ++m) v += sc[r][m] * sd[m][col - k0];
+          a = -v;
+        } else {
+          double v = a;
+          for (int m = 0; m < kb; ++m) v -= sc[r][m] * sp[m][c];
+          a = v;
+        }
+      }
+    }
+    grid.sync();
+  }
+}
+
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];
@@ -669,11 +787,20 @@ void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double*
   k_symmetrize<<<nblk(n * n, 256), 256, 0, s>>>((int)n, A);
 }
 
-int coarsest_invert(cudaStream_t s, int n, double* A, double* /*work*/, int* status_dev) {
+int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int threads = 256;
+  if (work) {  // blocked form: GJB-pivot panels, rank-GJB updates
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_blocked, threads, 0);
+    if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
+    const int tiles = ((n + GJB - 1) / GJB) * ((n + GJB - 1) / GJB);
+    const int blocks = std::max(1, std::min(tiles, nsm * std::min(per_sm, 2)));
+    cudaMemsetAsync(status_dev, 0, 2 * sizeof(int), s);
+    void* args[] = {&n, &A, &work, &status_dev};
+    return (int)cudaLaunchCooperativeKernel((void*)k_gj_blocked, dim3(blocks), dim3(threads), args, 0, s);
+  }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gauss_jordan, threads, 0);
   if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
   int64_t want = ((int64_t)n * n + threads - 1) / threads;

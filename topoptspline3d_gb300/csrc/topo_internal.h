@@ -42,6 +42,9 @@ struct DevLevel {
   double* U2 = nullptr;         // FP64 second iterate buffer (Chebyshev ping-pong) [3nv]
   float* U2_32 = nullptr;       // FP32 second iterate buffer [3nv]
   double lmax = 0, lmax32 = 0;  // Chebyshev spectral bound estimates
+  double* eig = nullptr;        // last power-iteration vector, FP64 [3nv] (warm start)
+  float* eig32 = nullptr;       // same, FP32
+  double lprev = 0, lprev32 = 0;  // last estimates (warm-start guard)
 };
 
 // Host-side hierarchy description (computed once from the active mask).

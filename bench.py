@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2, help="FP64 MG-PCG comparison steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default solver schedule and tiles")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner ablation")
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run exactly one mixed design iteration and exit (for ncu captures)")
     ap.add_argument("--schedule", default=None,
@@ -198,6 +199,76 @@ def cpu_baseline(nx, ny, nz, threads_note=""):
     o.oc_update(wl.vgoal)
     dt = (time.perf_counter() - t0) * 1e3
     return dt, it, rr, c
+
+
+def compliance_vs_oracle(p, wl, opts):
+    """Compliance of the GPU mixed solve against the FP64 CPU oracle solved to
+    1e-10 on the same final design (operators rebuilt on both sides)."""
+    from oracle.oracle import Oracle, build_oracle
+    from topoptspline3d_gb300 import capi
+    build_oracle()
+    coeff = p.get("coeff")
+    p.coeff_to_density()
+    p.update_operators()
+    p.put("u", np.zeros(3 * p.nv))
+    s = p.solve(**opts)
+    c_gpu = p.compliance()
+    o = Oracle(wl.nx, wl.ny, wl.nz, eactive=wl.eactive)
+    o.set_bc(wl.fixed, wl.loads)
+    bmin, bmax = wl.spline_box()
+    o.set_spline(wl.order, wl.partition, bmin, bmax)
+    o.put("coeff", coeff)
+    o.coeff_to_density()
+    o.update_operators()
+    t0 = time.perf_counter()
+    it, rr = o.pcg(2, 2, 1e-10, 400, 0)
+    c_o = o.compliance()
+    return {"compliance_gpu_mixed": c_gpu, "compliance_oracle_fp64": c_o, "rel_err": abs(c_gpu - c_o) / abs(c_o),
+            "gpu_relres": s["relres"], "oracle_relres": rr, "oracle_pcg_its": it,
+            "oracle_solve_s": time.perf_counter() - t0}
+
+
+def learned_ablation(p, wl, opts):
+    """Learned preconditioner at this grid: harvest residual -> error crops from
+    mixed solves on 8 seeded smoothed random densities, 400 Adam steps, then the
+    same solve (one FP32 V-cycle per outer step) with and without the network on
+    an unseen density.  Restores the design state afterwards."""
+    from topoptspline3d_gb300 import capi, workloads
+    rho0 = p.get("rho")
+    u0 = p.get("u")
+    nx, ny, nz = wl.nx, wl.ny, wl.nz
+    p.unet_enable(11)
+    p.unet_dataset_reserve(2048, crop=32, crops_per_iterate=32)
+    base = dict(opts)
+    base.update(inner_max=1, learned=0)
+    t0 = time.perf_counter()
+    for i in range(8):
+        p.put("rho", workloads.random_density(nx, ny, nz, 3000 + i))
+        p.update_operators()
+        p.put("u", np.zeros(3 * p.nv))
+        p.solve(**dict(base, learned=2, rtol=1e-8, max_iter=400), check=False)
+    harvest_s = time.perf_counter() - t0
+    n = p.unet_dataset_size()
+    split = int(0.85 * n)
+    t0 = time.perf_counter()
+    fit0 = p.unet_train(20, batch=8, lo=0, hi=split, update=False, seed=7)
+    p.unet_train(400, batch=8, lr=1e-4, lo=0, hi=split, seed=6)
+    train_s = time.perf_counter() - t0
+    fit = p.unet_train(20, batch=8, lo=0, hi=split, update=False, seed=7)
+    held = p.unet_train(20, batch=8, lo=split, hi=n, update=False, seed=5)
+    p.put("rho", workloads.random_density(nx, ny, nz, 3999))
+    p.update_operators()
+    res = {}
+    for name, lr in (("plain", 0), ("learned", 1)):
+        p.put("u", np.zeros(3 * p.nv))
+        st = p.solve(**dict(base, learned=lr), check=False)
+        res[name] = {"iterations": st["iterations"], "ms": st["ms"], "relres": st["relres"],
+                     "applied": st["learned_applied"], "fallback": st["learned_fallback"]}
+    p.put("rho", rho0)
+    p.update_operators()
+    p.put("u", u0)
+    return {"crops": n, "harvest_s": harvest_s, "train_steps": 400, "train_s": train_s,
+            "loss_train_crops": [fit0, fit], "loss_heldout_density": held, "solve_unseen_density": res}
 
 
 def run_reference(args, nx, ny, nz, ws, rank):
@@ -459,6 +530,17 @@ def main():
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "ms/design-iter", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
+    extra = {}
+    if rank == 0 and ws == 1 and args.case == "mbb" and not args.no_cpu_baseline:
+        try:
+            extra["compliance_vs_oracle"] = compliance_vs_oracle(p, wl, opts)
+        except Exception as e:
+            extra["compliance_vs_oracle"] = {"failed": str(e)}
+    if args.case == "mbb" and not args.no_learned:
+        try:
+            extra["learned"] = learned_ablation(p, wl, opts)
+        except Exception as e:
+            extra["learned"] = {"failed": str(e)}
     h2d = 8 * nc
     d2h = 8 * nc + 8  # coefficients and the compliance scalar
     out = {"metric": metric_for(args), "value": ms_step, "unit": "ms/design-iter", "n_gpus": ws, "steps": args.steps,
@@ -479,6 +561,7 @@ def main():
            "speedup_vs_fp64_mgpcg": (fp64["ms_per_step"] / ms_step) if fp64 else None,
            "e2e": {"value": e2e_ms, "unit": "ms/design-iter", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks}
+    out.update(extra)
     if rank == 0:
         print(json.dumps(out), flush=True)
     p.close()

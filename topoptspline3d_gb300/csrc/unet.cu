@@ -12,7 +12,7 @@
 // bf16 (what the tensor cores read); activations are bf16, accumulation fp32.
 //
 // The network corrects the FP32 multigrid preconditioner of the mixed solver:
-//   z = V(r) + rms(V(r)) * N(r / rms(r), log rho)
+//   z = V(r) + rms(V(r)) * N(s(r / rms(r)), log rho),  s(x) = x / (1 + |x|/8)
 // and is trained on pairs harvested from the solver's own iterates: for a
 // residual r_k with V-cycle output z_k and error e_k = u* - u_k, the target is
 // (e_k - z_k) / rms(z_k).  Its last layer starts at zero, so an untrained
@@ -68,6 +68,12 @@ uint64_t splitmix(uint64_t& s) {
 double uniform01(uint64_t& s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
 
 // ---- kernels ---------------------------------------------------------------
+
+// Network input of a normalised residual component: linear near zero,
+// saturating at +-8 (the residual of a solve concentrates on loads and
+// supports, so r / rms(r) reaches the thousands there).  Applied identically
+// to training crops and at inference.
+__device__ __forceinline__ float squash(float x) { return x / (1.f + fabsf(x) * 0.125f); }
 
 // log10(rho) averaged over the active elements around each vertex, mapped to
 // log10(rho)/3 + 0.5 (rho in [1e-3, 1] -> [-0.5, 0.5]).
@@ -134,7 +140,7 @@ __global__ void k_pack_input_dev(LevelDims d, int X, int Y, int Z, const T* __re
   for (int k = 0; k < 16; ++k) c[k] = __float2bfloat16_rn(0.f);
   if (x < d.vx && y < d.vy && z < d.vz) {
     const int64_t v = x + (int64_t)d.vx * (y + (int64_t)d.vy * z);
-    for (int k = 0; k < 3; ++k) c[k] = __float2bfloat16_rn((float)r[k * d.nv + v] * is);
+    for (int k = 0; k < 3; ++k) c[k] = __float2bfloat16_rn(squash((float)r[k * d.nv + v] * is));
     c[3] = __float2bfloat16_rn(lr[v]);
   }
   uint4* dst = reinterpret_cast<uint4*>(x0 + i * 16);
@@ -164,7 +170,7 @@ __global__ void k_crop(LevelDims d, int S, const int* __restrict__ org, int ncro
     m = vmask[v];
     l = lr[v];
     for (int k = 0; k < 3; ++k) {
-      rv[k] = r[k * d.nv + v] * *inv_r;
+      rv[k] = squash(r[k * d.nv + v] * *inv_r);
       tv[k] = t[k * d.nv + v] * *inv_t;
     }
   }

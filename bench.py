@@ -61,6 +61,9 @@ def parse():
                          "autotuning (e.g. the values an earlier run's autotune chose)")
     ap.add_argument("--profile-solve-steps", type=int, default=0,
                     help="with --profile-iteration: stop the solve after this many outer CG steps")
+    ap.add_argument("--profile-warmup", type=int, default=0,
+                    help="with --profile-iteration: run this many design iterations first and open the profiler's "
+                         "capture range (cudaProfilerStart) only around the last one, for ncu --profile-from-start off")
     return ap.parse_args()
 
 
@@ -431,7 +434,15 @@ def main():
     if args.profile_iteration:
         if args.profile_solve_steps > 0:
             opts["max_iter"] = args.profile_solve_steps
+        for _ in range(args.profile_warmup):
+            p.design_iteration(solve=opts, oc=oc)
+        if args.profile_warmup > 0:
+            p.sync()
+            capi.profiler_range(True)
         s = p.design_iteration(solve=opts, oc=oc)
+        if args.profile_warmup > 0:
+            p.sync()
+            capi.profiler_range(False)
         print(json.dumps({"profile_iteration": s}), flush=True)
         p.close()
         return

@@ -406,6 +406,10 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
 /* Sets the fine kernels' z-march depths (FP32 kernels, FP64 operator) directly,
  * e.g. to replay an earlier autotune result. */
 int topo_set_tiles(topo_handle* h, int tz32, int tz64);
+/* Opens (start = 1) or closes (start = 0) the profiler's capture range
+ * (cudaProfilerStart / cudaProfilerStop), so a profiler started with capture
+ * off records only warm work, e.g. one design iteration after the warm-up. */
+int topo_profiler_range(int start);
 
 /* --- many load cases in one solve ------------------------------------------ */
 /* Multi-right-hand-side solve (config "batched": many load cases as right-hand

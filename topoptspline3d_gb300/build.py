@@ -1,6 +1,10 @@
 """Build libtopo_gb300.so in-tree: nvcc for sm_103a, one process per source.
 
 Usage: python -m topoptspline3d_gb300.build [--force]
+
+Extra nvcc flags for the CUDA sources (e.g. -DTOPO_FINE32_MIN_CTAS=3) can be
+given in the TOPO_NVCC_FLAGS environment variable; rebuild with --force after
+changing them.
 """
 from __future__ import annotations
 
@@ -53,6 +57,7 @@ def _compile(src: str) -> str:
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include")]
     if src.endswith(".cu"):
         cmd = [nvcc, ARCH, "-lineinfo", "--expt-relaxed-constexpr", "-c", src, "-o", obj] + common
+        cmd += os.environ.get("TOPO_NVCC_FLAGS", "").split()
     else:
         cmd = [nvcc, "-x", "c++", "-c", src, "-o", obj] + common
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -45,7 +45,7 @@ EXPORTED = [
     "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
-    "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles",
+    "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
 ]
 
 
@@ -179,6 +179,7 @@ def load(build: bool = True):
         "topo_set_fine_arithmetic": (i, [vp, i]),
         "topo_set_graphs": (i, [vp, i]),
         "topo_set_tiles": (i, [vp, i, i]),
+        "topo_profiler_range": (i, [i]),
         "topo_design_batch": (i, [C.POINTER(vp), i, C.POINTER(IterOpts), i, i, i, C.POINTER(IterStats),
                                   C.POINTER(BatchStats)]),
         "topo_autotune": (i, [vp, C.POINTER(SolveOpts), C.POINTER(SolveOpts), C.POINTER(TuneReport)]),
@@ -218,6 +219,11 @@ def load(build: bool = True):
 def _ck_free(rc, what):
     if rc != TOPO_OK:
         raise TopoError(rc, what)
+
+
+def profiler_range(start: bool) -> None:
+    """Open or close the profiler's capture range (cudaProfilerStart/Stop)."""
+    _ck_free(load(build=False).topo_profiler_range(int(bool(start))), "topo_profiler_range")
 
 
 def element_template(E, nu, h) -> np.ndarray:

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_profiler_api.h>
+
 #include "topo_internal.h"
 
 namespace topo {
@@ -309,9 +311,11 @@ struct ChebParams {
 // Chebyshev polynomial smoother in point-block-Jacobi form (three-term
 // recurrence, Saad, Iterative Methods for Sparse Linear Systems, Alg. 12.1).
 // Each step is one fused kernel that reads the iterate from one buffer and
-// writes the next into the other; the result ends in level U.
+// writes the next into the other; the result ends in level U.  With
+// zero_start the iterate is known to be zero on entry (level U is not read),
+// and the first step is the operator-free d = c_new D^-1 f.
 template <typename T>
-void cheb_level(topo_handle* h, int l, const ChebParams& cp) {
+void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start) {
   DevLevel& L = h->lv[l];
   const double lmax = P<T>::lmax(L) * cp.hi, lmin = P<T>::lmax(L) * cp.lo;
   const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
@@ -327,7 +331,15 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp) {
       c_new = 2.0 * rho_new / delta;
       rho_old = rho_new;
     }
-    if (l == 0) {
+    if (k == 0 && zero_start) {
+      // not in the smoother's profiling family: no operator is applied
+      if (l == 0)
+        launch_fine_cheb_zero<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
+                                 c_new, h->nb);
+      else
+        launch_cheb_zero_stored<T>(h->stream, L.d.nv, nullptr, P<T>::dinv(L), P<T>::F(L), P<T>::cd(L), ub, c_new,
+                                   h->nb);
+    } else if (l == 0) {
       EventPair* ev = prof_begin(h, P<T>::fam_smooth);
       launch_fine_cheb<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L),
                           P<T>::cd(L), c_old, c_new, k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64);
@@ -345,9 +357,10 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp) {
 }
 
 template <typename T>
-void smooth_level(topo_handle* h, int l, int sweeps, bool reverse, int smoother, const ChebParams& cp) {
+void smooth_level(topo_handle* h, int l, int sweeps, bool reverse, int smoother, const ChebParams& cp,
+                  bool zero_start = false) {
   if (smoother == TOPO_SMOOTH_CHEBYSHEV) {
-    for (int s = 0; s < sweeps; ++s) cheb_level<T>(h, l, cp);
+    for (int s = 0; s < sweeps; ++s) cheb_level<T>(h, l, cp, zero_start && s == 0);
   } else {
     gs_level<T>(h, l, sweeps, reverse);
   }
@@ -375,12 +388,18 @@ void prolong_T(topo_handle* h, int lf) {
 
 // V-cycle in the reference order (grid/Grid.cpp:2399-2444).  `sym` runs the
 // adjoint sweep after the coarse correction so the cycle is a symmetric
-// preconditioner.  Level-0 U must hold the initial guess, F the right-hand side.
+// preconditioner.  Level-0 U must hold the initial guess, F the right-hand side;
+// zero0 declares that guess to be zero (a preconditioner application), which
+// lets the first Chebyshev step on level 0 skip the operator.  Coarse levels
+// always start from zero: with Chebyshev pre-smoothing their first step skips
+// the operator and writes U in full, so U is not cleared first.
 template <typename T>
-void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, const ChebParams& cp) {
+void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, const ChebParams& cp,
+                 bool zero0 = false) {
   const int nl = (int)h->lv.size();
+  const bool cheb_pre = smoother == TOPO_SMOOTH_CHEBYSHEV && pre >= 1 && cp.degree >= 1;
   if (nl == 1) {
-    smooth_level<T>(h, 0, pre, false, smoother, cp);
+    smooth_level<T>(h, 0, pre, false, smoother, cp, zero0);
     smooth_level<T>(h, 0, post, sym, smoother, cp);
     return;
   }
@@ -388,9 +407,10 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
     if (l > 0) {
       level_residual<T>(h, l - 1);
       restrict_T<T>(h, l);
-      cudaMemsetAsync(P<T>::U(h->lv[l]), 0, sizeof(T) * 3 * h->lv[l].d.nv * h->nb, h->stream);
+      if (!(cheb_pre && l < nl - 1))
+        cudaMemsetAsync(P<T>::U(h->lv[l]), 0, sizeof(T) * 3 * h->lv[l].d.nv * h->nb, h->stream);
     }
-    if (l < nl - 1) smooth_level<T>(h, l, pre, false, smoother, cp);
+    if (l < nl - 1) smooth_level<T>(h, l, pre, false, smoother, cp, l > 0 || zero0);
     else coarsest_solve_T<T>(h);
   }
   for (int l = nl - 2; l >= 0; --l) {
@@ -404,14 +424,14 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
 // spectral bounds, tiles and buffers, so it is captured once and replayed;
 // any change of that key re-captures it.  Small grids and the coarse levels
 // are launch-bound, and one graph launch replaces about forty.
-static void vcycle32(topo_handle* h, int pre, int post, int smoother, const ChebParams& cp) {
+static void vcycle32(topo_handle* h, int pre, int post, int smoother, const ChebParams& cp, bool zero0) {
   if (!h->graphs) {
-    vcycle_core<float>(h, pre, post, true, smoother, cp);
+    vcycle_core<float>(h, pre, post, true, smoother, cp, zero0);
     return;
   }
   prof_collect(h);
   std::vector<double> key = {(double)pre, (double)post, (double)smoother, (double)cp.degree, cp.lo, cp.hi,
-                             (double)h->tz32, (double)h->nb, (double)h->prof};
+                             (double)h->tz32, (double)h->nb, (double)h->prof, (double)zero0};
   for (const DevLevel& L : h->lv) {
     key.push_back(L.lmax32);
     key.push_back((double)(uintptr_t)L.U32);
@@ -425,7 +445,7 @@ static void vcycle32(topo_handle* h, int pre, int post, int smoother, const Cheb
     bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
       h->capturing = true;
-      vcycle_core<float>(h, pre, post, true, smoother, cp);
+      vcycle_core<float>(h, pre, post, true, smoother, cp, zero0);
       h->capturing = false;
       ok = cudaStreamEndCapture(h->stream, &g) == cudaSuccess && g;
     }
@@ -438,7 +458,7 @@ static void vcycle32(topo_handle* h, int pre, int post, int smoother, const Cheb
       h->vgraph = nullptr;
       h->graphs = false;
       prof_drop_graph_events(h);
-      vcycle_core<float>(h, pre, post, true, smoother, cp);
+      vcycle_core<float>(h, pre, post, true, smoother, cp, zero0);
       return;
     }
     h->vkey = key;
@@ -605,8 +625,8 @@ int vcycle_prec(topo_handle* h, const T* r, int pre, int post, int smoother, con
   const int64_t n3 = 3 * L0.d.nv;
   CK(cudaMemcpyAsync(P<T>::F(L0), r, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemsetAsync(P<T>::U(L0), 0, sizeof(T) * n3, h->stream));
-  if (sizeof(T) == 4) vcycle32(h, pre, post, smoother, cp);
-  else vcycle_core<T>(h, pre, post, true, smoother, cp);
+  if (sizeof(T) == 4) vcycle32(h, pre, post, smoother, cp, true);
+  else vcycle_core<T>(h, pre, post, true, smoother, cp, true);
   return TOPO_OK;
 }
 
@@ -1298,7 +1318,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
         launch_d2f(h->stream, r, L0.F32, n3);
         CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3, h->stream));
         ++nvc;
-        vcycle32(h, o->pre, o->post, o->smoother, cp);
+        vcycle32(h, o->pre, o->post, o->smoother, cp, true);
         RET(net(L0.F32, L0.U32));
         if (harvest && rn > 1e-4 * fn) {
           const cudaError_t e = unet_harvest_record(h->unet, h->stream, n3, r, L0.U32, h->x, 8);
@@ -1448,6 +1468,11 @@ int topo_set_fine_arithmetic(topo_handle* h, int arith) {
   if (!h || arith < 0 || arith > 1) return TOPO_E_BAD_INPUT;
   h->fine_df = arith;
   return TOPO_OK;
+}
+
+int topo_profiler_range(int start) {
+  const cudaError_t e = start ? cudaProfilerStart() : cudaProfilerStop();
+  return e == cudaSuccess ? TOPO_OK : TOPO_E_CUDA;
 }
 
 int topo_design_batch(topo_handle** hs, int n, const topo_iter_opts* opts, int nopts, int iterations, int threads,
@@ -1682,7 +1707,7 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
     // z = V(r): one FP32 V-cycle for the whole batch
     launch_d2f(h->stream, m.r, L0.F32, n3 * nb);
     CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3 * nb, h->stream));
-    vcycle32(h, o->pre, o->post, TOPO_SMOOTH_CHEBYSHEV, cp);
+    vcycle32(h, o->pre, o->post, TOPO_SMOOTH_CHEBYSHEV, cp, true);
     ++nvc;
     k_to_double<float><<<nb256(n3 * nb), 256, 0, h->stream>>>(n3 * nb, L0.U32, m.z);
     launch_bdot<double>(h->stream, m.r, m.z, n3, nb, m.part, slot(B_RZ));

@@ -181,6 +181,42 @@ template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const 
 template void launch_stencil_cheb<float>(cudaStream_t, const LevelDims&, const float*, const float*,
                                          const float*, float*, const float*, float*, double, double, bool, int);
 
+// First Chebyshev step from a zero iterate with a stored block-Jacobi inverse
+// (coarse levels; FP64 level 0 with its free-DOF mask): r = f, d = c_new D^-1 r,
+// u_out = d.  Equals the full step on u = 0, since A 0 = 0 exactly.
+template <typename T>
+__global__ void k_cheb_zero_stored(int64_t nv, const uint8_t* __restrict__ vmask, const T* __restrict__ dinv,
+                                   const T* __restrict__ f, T* __restrict__ dv, T* __restrict__ uout, T c_new) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int64_t bo = (int64_t)blockIdx.y * 3 * nv;
+  f += bo;
+  dv += bo;
+  uout += bo;
+  const uint8_t m = vmask ? vmask[v] : 7;
+  T r[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] : T(0);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const T zz = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
+    const T dn = c_new * zz;
+    dv[c * nv + v] = dn;
+    uout[c * nv + v] = dn;
+  }
+}
+
+template <typename T>
+void launch_cheb_zero_stored(cudaStream_t s, int64_t nv, const uint8_t* vmask, const T* dinv, const T* f, T* dvec,
+                             T* uout, double c_new, int nb) {
+  k_cheb_zero_stored<T><<<dim3(nblk(nv, 256), nb), 256, 0, s>>>(nv, vmask, dinv, f, dvec, uout, (T)c_new);
+}
+
+template void launch_cheb_zero_stored<double>(cudaStream_t, int64_t, const uint8_t*, const double*, const double*,
+                                              double*, double*, double, int);
+template void launch_cheb_zero_stored<float>(cudaStream_t, int64_t, const uint8_t*, const float*, const float*,
+                                             float*, float*, double, int);
+
 template <typename T>
 void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask, T* u,
                        const T* f, int colour, bool reverse) {

@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "df.cuh"
 #include "topo_internal.h"
 
 namespace topo {
@@ -186,28 +187,43 @@ void launch_coeff_to_density_direct(cudaStream_t s, const LevelDims& d, const ui
 // with u_e^T Ke u_e evaluated in the sum-factorised modal form: Walsh-Hadamard
 // coefficients of the nodal values, the displacement gradient split over the
 // orthogonal functions {1, X, Y, Z, YZ, XZ, XY} of the reference cube, and the
-// isotropic energy of each part weighted by the function's L2 norm.
-__device__ __forceinline__ void hadamard8(double v[8]) {
+// isotropic energy of each part weighted by the function's L2 norm.  The
+// energy is formed in double-float arithmetic (about 1e-14 relative, on the
+// FP32 pipe); only the final scaling by -p rho^(p-1) (h/2)^3 runs in FP64.
+template <typename T>
+__device__ __forceinline__ T cst(double v);
+template <>
+__device__ __forceinline__ double cst<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ df cst<df>(double v) { return df_from(v); }
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(df v) { return df_to(v); }
+
+template <typename T>
+__device__ __forceinline__ void hadamard8(T v[8]) {
 #pragma unroll
   for (int h = 1; h < 8; h <<= 1)
 #pragma unroll
     for (int i = 0; i < 8; ++i)
       if (!(i & h)) {
-        const double a = v[i], b = v[i | h];
+        const T a = v[i], b = v[i | h];
         v[i] = a + b;
         v[i | h] = b - a;
       }
 }
 
-__device__ __forceinline__ double energy_part(const double G[3][3], double lam, double mu) {
-  const double tr = G[0][0] + G[1][1] + G[2][2];
-  double ee = G[0][0] * G[0][0] + G[1][1] * G[1][1] + G[2][2] * G[2][2];
-  const double e01 = 0.5 * (G[0][1] + G[1][0]), e02 = 0.5 * (G[0][2] + G[2][0]),
-               e12 = 0.5 * (G[1][2] + G[2][1]);
-  ee += 2.0 * (e01 * e01 + e02 * e02 + e12 * e12);
-  return 0.5 * lam * tr * tr + mu * ee;
+// 0.5 lam tr(G)^2 + mu |sym G|^2 with lam2 = lam / 2
+template <typename T>
+__device__ __forceinline__ T energy_part(const T G[3][3], T lam2, T mu) {
+  const T half = cst<T>(0.5), two = cst<T>(2.0);
+  const T tr = G[0][0] + G[1][1] + G[2][2];
+  T ee = G[0][0] * G[0][0] + G[1][1] * G[1][1] + G[2][2] * G[2][2];
+  const T e01 = half * (G[0][1] + G[1][0]), e02 = half * (G[0][2] + G[2][0]), e12 = half * (G[1][2] + G[2][1]);
+  ee += two * (e01 * e01 + e02 * e02 + e12 * e12);
+  return lam2 * tr * tr + mu * ee;
 }
 
+template <typename T>
 __global__ void k_sensitivity(LevelDims d, const uint8_t* __restrict__ eactive,
                               const double* __restrict__ rho, const double* __restrict__ u,
                               double penal, double lam, double mu, double h, double* __restrict__ sens) {
@@ -219,39 +235,39 @@ __global__ void k_sensitivity(LevelDims d, const uint8_t* __restrict__ eactive,
   const int y = (int)(t % d.ey), z = (int)(t / d.ey);
   // c[i][S]: modal coefficient of component i for mode S (bit0 x, bit1 y, bit2 z),
   // with sign convention H[a][S] = prod_{k in S} (2 a_k - 1); scaled by 2/h * 1/8.
-  double c[3][8];
+  T c[3][8];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
       const int64_t v = (x + (a & 1)) + (int64_t)d.vx * ((y + ((a >> 1) & 1)) + (int64_t)d.vy * (z + (a >> 2)));
-      c[i][a] = u[i * d.nv + v];
+      c[i][a] = cst<T>(u[i * d.nv + v]);
     }
-    hadamard8(c[i]);
+    hadamard8<T>(c[i]);
   }
-  const double sc = 2.0 / h / 8.0;
-  double tot = 0.0;
+  const T sc = cst<T>(2.0 / h / 8.0), lam2 = cst<T>(0.5 * lam), muT = cst<T>(mu), zero = cst<T>(0.0);
+  T tot = zero;
 #pragma unroll
   for (int f = 0; f < 7; ++f) {
-    double G[3][3];
+    T G[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        G[i][j] = ((f >> j) & 1) ? 0.0 : sc * c[i][f | (1 << j)];
+        G[i][j] = ((f >> j) & 1) ? zero : sc * c[i][f | (1 << j)];
     const int nbits = (f & 1) + ((f >> 1) & 1) + ((f >> 2) & 1);
-    const double nf = nbits == 0 ? 8.0 : (nbits == 1 ? 8.0 / 3.0 : 8.0 / 9.0);
-    tot += nf * energy_part(G, lam, mu);
+    const T nf = cst<T>(nbits == 0 ? 8.0 : (nbits == 1 ? 8.0 / 3.0 : 8.0 / 9.0));
+    tot += nf * energy_part<T>(G, lam2, muT);
   }
   const double hh = 0.5 * h;
-  const double q = 2.0 * hh * hh * hh * tot;  // u_e^T Ke u_e
+  const double q = 2.0 * hh * hh * hh * to_double(tot);  // u_e^T Ke u_e
   sens[e] = -penal * simp_pow(rho[e], penal - 1.0) * q;
 }
 
 void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                         const double* rho, const double* u, double penal, double lam, double mu,
                         double h, double* sens) {
-  k_sensitivity<<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, rho, u, penal, lam, mu, h, sens);
+  k_sensitivity<df><<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, rho, u, penal, lam, mu, h, sens);
 }
 
 // Sensitivity filter (grid/Grid.cu:4130-4229): normalised average over the ball

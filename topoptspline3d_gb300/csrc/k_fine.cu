@@ -6,6 +6,7 @@
 // exactly as the reference's WS kernels do (grid/Grid.cu:2277-2333, 1699-1842).
 #include <mutex>
 
+#include "df.cuh"
 #include "topo_internal.h"
 
 namespace topo {
@@ -33,49 +34,6 @@ __device__ __forceinline__ float modal_c<float>(int i) { return cModal32[i]; }
 
 // Diagonal 3x3 blocks Ke[a,a] of the eight local nodes (FP32 smoother epilogue).
 __constant__ float cKdiag32[8][9];
-
-// ---------------------------------------------------------------------------
-// Double-float ("float-float") arithmetic: a value is the unevaluated sum
-// hi + lo of two floats with |lo| <= ulp(hi)/2, about 48 significant bits.
-// Addition uses Knuth's error-free TwoSum on the high parts, folds in the low
-// parts and renormalises with Dekker's Fast2Sum; multiplication forms the exact
-// product error of the high parts with an FMA (TwoProd).  This is the sloppy
-// double-double addition of Hida, Li and Bailey (2001) on floats.  All
-// operations use the _rn intrinsics so the compiler cannot fuse or reorder
-// them.  On GB300 the FP32 pipe is 58x the FP64 pipe, so the fine operator of
-// the FP64 outer CG runs in this arithmetic with FP64-level accuracy.
-// ---------------------------------------------------------------------------
-struct df {
-  float hi, lo;
-  __device__ __forceinline__ df() {}
-  __device__ __forceinline__ df(float h, float l) : hi(h), lo(l) {}
-  __device__ __forceinline__ explicit df(int v) : hi((float)v), lo(0.f) {}
-};
-
-__device__ __forceinline__ df df_fast2sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return df(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-__device__ __forceinline__ df operator+(df a, df b) {
-  const float s = __fadd_rn(a.hi, b.hi);
-  const float bb = __fsub_rn(s, a.hi);
-  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-  return df_fast2sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
-}
-__device__ __forceinline__ df operator-(df a, df b) { return a + df(-b.hi, -b.lo); }
-__device__ __forceinline__ df operator*(df a, df b) {
-  const float p = __fmul_rn(a.hi, b.hi);
-  float e = __fmaf_rn(a.hi, b.hi, -p);
-  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
-  return df_fast2sum(p, e);
-}
-__device__ __forceinline__ df& operator+=(df& a, df b) { a = a + b; return a; }
-__device__ __forceinline__ bool operator!=(df a, df b) { return a.hi != b.hi || a.lo != b.lo; }
-__device__ __forceinline__ df df_from(double x) {
-  const float h = __double2float_rn(x);
-  return df(h, __double2float_rn(x - (double)h));
-}
-__device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.lo; }
 
 // Modal constants split into hi + lo floats.
 __constant__ float2 cModalDF[5];
@@ -277,8 +235,21 @@ __device__ __forceinline__ void block_solve_free(const T S_in[9], uint8_t fb, co
     if (!((fb >> i) & 1)) z[i] = T(0);
 }
 
+// Minimum resident CTAs per SM asked of the FP32 variants (256 threads each).
+// Operator and residual: 4 (64 registers per thread, no spills).  Chebyshev
+// step: 3, which leaves it the registers for its block solve without spilling
+// (measured on GB300 at 256x128x128: 159 us per step at 3 against 163 us at 4).
+#ifndef TOPO_FINE32_MIN_CTAS
+#define TOPO_FINE32_MIN_CTAS 4
+#endif
+#ifndef TOPO_FINE32_CHEB_MIN_CTAS
+#define TOPO_FINE32_CHEB_MIN_CTAS 3
+#endif
+
 template <typename T, int TXE, int TYE, int MODE>
-__global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* __restrict__ rhop,
+__global__ void __launch_bounds__(TXE* TYE,
+                                  sizeof(T) == 4 ? (MODE == 2 ? TOPO_FINE32_CHEB_MIN_CTAS : TOPO_FINE32_MIN_CTAS) : 1)
+    k_fine_modal(LevelDims d, const T* __restrict__ rhop,
                                                          const uint8_t* __restrict__ vmask,
                                                          const T* __restrict__ u, const T* __restrict__ f,
                                                          T* __restrict__ out, int TZ, ChebArgs ch) {
@@ -321,10 +292,43 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
     }
     cp_async_commit();
   };
+  // Per-layer global operands (the element's rho^p; the owned vertex's mask,
+  // load and Chebyshev direction) are read one layer ahead into registers, so
+  // their latency overlaps the current layer's work instead of stalling it.
+  const int pex = gx - 1, pey = gy - 1;
+  const bool pe_xy = pex >= 0 && pey >= 0 && pex < d.ex && pey < d.ey;
+  auto load_pe = [&](int ez) -> T {
+    return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (int64_t)d.ex * (pey + (int64_t)d.ey * ez)] : T(0);
+  };
+  const T* __restrict__ dvin =
+      (MODE == 2 && !ch.first) ? static_cast<const T*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
+  uint8_t vm_n = 0;
+  T f_n[3] = {T(0), T(0), T(0)}, dv_n[3] = {T(0), T(0), T(0)};
+  auto load_vertex = [&](int z) {
+    if (!own || z < z0 || z >= zend) return;
+    const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * z);
+    vm_n = vmask[v];
+    if (MODE >= 1) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f_n[c] = f[c * nv + v];
+    }
+    if (MODE == 2 && dvin) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) dv_n[c] = dvin[c * nv + v];
+    }
+  };
+  T pe_n = load_pe(z0 - 1);
   prefetch(z0 - 1);
   prefetch(z0);
   for (int ez = z0 - 1; ez < zend; ++ez) {
     prefetch(ez + 2);
+    const T pe = pe_n;
+    const uint8_t vm_c = vm_n;
+    T f_c[3], dv_c[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
+    if (ez + 1 < zend) pe_n = load_pe(ez + 1);
+    load_vertex(ez + 1);
     cp_async_wait1();
     __syncthreads();
     // the owned vertex's own value at plane ez (Chebyshev update); read here,
@@ -332,10 +336,6 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
     Vec4<T> uo{T(0), T(0), T(0), T(0)};
     if (MODE == 2) uo = sm.plane[(ez + 3) % 3][(i + 1) + PX * (j + 1)];
     {
-      const int ex = gx - 1, ey = gy - 1;
-      T pe = T(0);
-      if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
-        pe = rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)];
       if (pe != T(0)) {
         T c[3][8];
 #pragma unroll
@@ -369,21 +369,21 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
       }
       if (ez >= z0) {
         const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
-        const uint8_t m = vmask[v];
+        const uint8_t m = vm_c;
         const T y[3] = {b0, b1, b2};
         if (MODE < 2) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const bool fr = (m >> c) & 1;
             const int64_t idx = c * nv + v;
-            out[idx] = MODE == 1 ? (fr ? f[idx] - y[c] : T(0)) : (fr ? y[c] : T(0));
+            out[idx] = MODE == 1 ? (fr ? f_c[c] - y[c] : T(0)) : (fr ? y[c] : T(0));
           }
         } else {
           const T* __restrict__ dinv = static_cast<const T*>(ch.dinv);
           T* __restrict__ dv = static_cast<T*>(ch.dvec) + (int64_t)rhs * 3 * nv;
           T r[3];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] - y[c] : T(0);
+          for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : T(0);
           const T uv[3] = {uo.x, uo.y, uo.z};
           T zc[3];
           if (FLY_DIAG) {
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal(LevelDims d, const T* _
           }
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const T dn = ch.first ? T(ch.c_new) * zc[c] : T(ch.c_old) * dv[c * nv + v] + T(ch.c_new) * zc[c];
+            const T dn = ch.first ? T(ch.c_new) * zc[c] : T(ch.c_old) * dv_c[c] + T(ch.c_new) * zc[c];
             dv[c * nv + v] = dn;
             out[c * nv + v] = uv[c] + dn;
           }
@@ -767,6 +767,73 @@ template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const dou
 template void launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
                                       const float*, const float*, float*, const float*, float*, double, double,
                                       bool, int, int);
+
+// First Chebyshev step from a zero iterate (every pre-smoothing sweep of a
+// preconditioning V-cycle starts from u = 0): K u vanishes, so r = f on the
+// free DOFs, d = c_new D^-1 r and u_out = d.  No vertex planes are read and no
+// element operator is applied; the result equals the fused step's on u = 0.
+// The FP32 diagonal block is rebuilt from the eight incident elements' rho^p
+// (four in layer z, four in layer z - 1) in the fused step's order; FP64 uses
+// the stored inverse.  blockIdx.y is the right-hand side of a batch.
+__global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
+                                   const float* __restrict__ f, float* __restrict__ dv, float* __restrict__ out,
+                                   float c_new) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.nv) return;
+  const int64_t nv = d.nv, bo = (int64_t)blockIdx.y * 3 * nv;
+  f += bo;
+  dv += bo;
+  out += bo;
+  const uint8_t m = vmask[v];
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  float pl[4], pp[4];
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    const int ex = x - 1 + (w & 1), ey = y - 1 + (w >> 1);
+    const bool xy = ex >= 0 && ey >= 0 && ex < d.ex && ey < d.ey;
+    const int64_t e = ex + (int64_t)d.ex * (ey + (int64_t)d.ey * z);
+    pl[w] = (xy && z < d.ez) ? rhop[e] : 0.f;
+    pp[w] = (xy && z >= 1 && z - 1 < d.ez) ? rhop[e - (int64_t)d.ex * d.ey] : 0.f;
+  }
+  float S[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) S[k] = 0.f;
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    const int a = (1 - (w & 1)) + 2 * (1 - (w >> 1));
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S[k] += pl[w] * cKdiag32[a][k] + pp[w] * cKdiag32[a + 4][k];
+  }
+  float r[3], zc[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] : 0.f;
+  block_solve_free<float>(S, (m & 8) ? (m & 7) : 0, r, zc);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float dn = c_new * zc[c];
+    dv[c * nv + v] = dn;
+    out[c * nv + v] = dn;
+  }
+}
+
+template <typename T>
+void launch_fine_cheb_zero(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* f,
+                           T* uout, const T* dinv, T* dvec, double c_new, int nb) {
+  if (sizeof(T) == 4) {
+    k_fine_cheb_zero32<<<dim3(blocks_for(d.nv, 256), nb), 256, 0, s>>>(
+        d, reinterpret_cast<const float*>(rhop), vmask, reinterpret_cast<const float*>(f),
+        reinterpret_cast<float*>(dvec), reinterpret_cast<float*>(uout), (float)c_new);
+  } else {
+    launch_cheb_zero_stored<T>(s, d.nv, vmask, dinv, f, dvec, uout, c_new, nb);
+  }
+}
+
+template void launch_fine_cheb_zero<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
+                                            const double*, double*, const double*, double*, double, int);
+template void launch_fine_cheb_zero<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
+                                           const float*, float*, const float*, float*, double, int);
 
 // Dense-row form of the same operator (thread per vertex, 8 x 3 x 24 products);
 // kept as the cross-check of the modal kernel.

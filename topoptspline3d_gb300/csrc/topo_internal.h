@@ -90,6 +90,13 @@ void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const u
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);
+// First Chebyshev step from a zero iterate (u = 0): d = c_new D^-1 f, uout = d.
+template <typename T>
+void launch_fine_cheb_zero(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* f,
+                           T* uout, const T* dinv, T* dvec, double c_new, int nb = 1);
+template <typename T>
+void launch_cheb_zero_stored(cudaStream_t s, int64_t nv, const uint8_t* vmask, const T* dinv, const T* f, T* dvec,
+                             T* uout, double c_new, int nb = 1);
 template <typename T>
 void launch_fine_apply_dense(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                              const T* u, const T* f, T* out, bool residual);

@@ -235,20 +235,39 @@ __device__ __forceinline__ void block_solve_free(const T S_in[9], uint8_t fb, co
     if (!((fb >> i) & 1)) z[i] = T(0);
 }
 
-// Minimum resident CTAs per SM asked of the FP32 variants (256 threads each).
-// Operator and residual: 4 (64 registers per thread, no spills).  Chebyshev
-// step: 3, which leaves it the registers for its block solve without spilling
-// (measured on GB300 at 256x128x128: 159 us per step at 3 against 163 us at 4).
-#ifndef TOPO_FINE32_MIN_CTAS
-#define TOPO_FINE32_MIN_CTAS 4
+// Build-time choices for the FP32 variants, measured on GB300 (half-MBB
+// 256x128x128, Chebyshev step per launch):
+//  - TOPO_FINE32_STORED_DIAG 1: the Chebyshev step reads the stored FP32
+//    block-Jacobi inverse (36 bytes per vertex) instead of rebuilding the
+//    diagonal blocks from rho^p and solving them (about 150 instructions per
+//    vertex); the kernel is issue-bound, so reading wins: 143 us against 154 us.
+//  - resident threads per SM (launch bounds): 1024 for all three modes (64
+//    registers per thread, no spills with the stored inverse).  With the
+//    rebuilt diagonal the step needs 80 registers and runs best at 768.
+//  - TOPO_MODAL32_TYE 8: element rows of a 32-wide CTA tile.  16 rows halve
+//    the halo overhead but run slower (162 us).
+// FP64 variants ask for 512 resident threads (two 256-thread CTAs, at most
+// 128 registers per thread).
+#ifndef TOPO_FINE32_THREADS_PER_SM
+#define TOPO_FINE32_THREADS_PER_SM 1024
 #endif
-#ifndef TOPO_FINE32_CHEB_MIN_CTAS
-#define TOPO_FINE32_CHEB_MIN_CTAS 3
+#ifndef TOPO_FINE32_CHEB_THREADS_PER_SM
+#define TOPO_FINE32_CHEB_THREADS_PER_SM 1024
+#endif
+#ifndef TOPO_FINE32_STORED_DIAG
+#define TOPO_FINE32_STORED_DIAG 1
+#endif
+#ifndef TOPO_MODAL32_TYE
+#define TOPO_MODAL32_TYE 8
 #endif
 
+constexpr int modal_min_ctas(int threads, int per_sm) { return per_sm / threads > 0 ? per_sm / threads : 1; }
+
 template <typename T, int TXE, int TYE, int MODE>
-__global__ void __launch_bounds__(TXE* TYE,
-                                  sizeof(T) == 4 ? (MODE == 2 ? TOPO_FINE32_CHEB_MIN_CTAS : TOPO_FINE32_MIN_CTAS) : 1)
+__global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE * TYE, MODE == 2
+                                                                                          ? TOPO_FINE32_CHEB_THREADS_PER_SM
+                                                                                          : TOPO_FINE32_THREADS_PER_SM)
+                                                           : modal_min_ctas(TXE * TYE, 512))
     k_fine_modal(LevelDims d, const T* __restrict__ rhop,
                                                          const uint8_t* __restrict__ vmask,
                                                          const T* __restrict__ u, const T* __restrict__ f,
@@ -271,23 +290,38 @@ __global__ void __launch_bounds__(TXE* TYE,
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
   const int zend = min(z0 + TZ, d.vz);
   T acc0 = T(0), acc1 = T(0), acc2 = T(0);
-  // FP32 Chebyshev steps rebuild the diagonal block from rho^p instead of
-  // streaming a stored inverse (36 bytes per vertex); FP64 steps read the
-  // stored inverse, which is cheaper than the FP64 arithmetic.
-  constexpr bool FLY_DIAG = (MODE == 2) && (sizeof(T) == 4);
+  // With TOPO_FINE32_STORED_DIAG 0, FP32 Chebyshev steps rebuild the diagonal
+  // block from rho^p instead of streaming the stored inverse; FP64 steps
+  // always read the stored inverse.
+  constexpr bool FLY_DIAG = (MODE == 2) && (sizeof(T) == 4) && !TOPO_FINE32_STORED_DIAG;
   T pprev[4] = {T(0), T(0), T(0), T(0)};
+  // This thread's plane slots k = t + s NT and their in-plane vertex offsets
+  // (-1 outside the domain), fixed for the whole z march.
+  constexpr int KS = (NP + NT - 1) / NT;
+  int pxy[KS];
+#pragma unroll
+  for (int s = 0; s < KS; ++s) {
+    const int k = t + s * NT, px = k % PX, py = k / PX;
+    const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+    pxy[s] = (k < NP && vx >= 0 && vy >= 0 && vx < d.vx && vy < d.vy) ? vx + d.vx * vy : -1;
+  }
+  const int64_t plane_n = (int64_t)d.vx * d.vy;
   // asynchronous copy of vertex plane z into its ring slot (z + 3) % 3
   auto prefetch = [&](int z) {
     if (z <= zend) {
       Vec4<T>* dst = sm.plane[(z + 3) % 3];
-      for (int k = t; k < NP; k += NT) {
-        const int px = k % PX, py = k / PX;
-        const int vx = x0 - 1 + px, vy = y0 - 1 + py;
-        const bool ok = vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz;
-        const int64_t v = ok ? vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z) : 0;
-        cp_async_elem<T>(&dst[k].x, u + v, ok);
-        cp_async_elem<T>(&dst[k].y, u + nv + v, ok);
-        cp_async_elem<T>(&dst[k].z, u + 2 * nv + v, ok);
+      const bool zok = z >= 0 && z < d.vz;
+      const int64_t zoff = (int64_t)z * plane_n;
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        const int k = t + s * NT;
+        if (k < NP) {
+          const bool ok = zok && pxy[s] >= 0;
+          const int64_t v = ok ? zoff + pxy[s] : 0;
+          cp_async_elem<T>(&dst[k].x, u + v, ok);
+          cp_async_elem<T>(&dst[k].y, u + nv + v, ok);
+          cp_async_elem<T>(&dst[k].z, u + 2 * nv + v, ok);
+        }
       }
     }
     cp_async_commit();
@@ -429,7 +463,7 @@ __global__ void __launch_bounds__(TXE* TYE,
 // once per plane, so the only FP64 instructions left are about eight
 // conversions per vertex; the element operator runs on the FP32 pipe.
 template <int TXE, int TYE, int MODE>
-__global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const double* __restrict__ rhop,
+__global__ void __launch_bounds__(TXE* TYE, 2) k_fine_modal_df(LevelDims d, const double* __restrict__ rhop,
                                                             const uint8_t* __restrict__ vmask,
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ f, double* __restrict__ out,
@@ -450,22 +484,54 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
   const int zend = min(z0 + TZ, d.vz);
   df acc0(0), acc1(0), acc2(0);
+  // plane slots of this thread and their in-plane offsets (-1 outside)
+  constexpr int KS = (NP + NT - 1) / NT;
+  int pxy[KS];
+#pragma unroll
+  for (int s = 0; s < KS; ++s) {
+    const int k = t + s * NT, px = k % PX, py = k / PX;
+    const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+    pxy[s] = (k < NP && vx >= 0 && vy >= 0 && vx < d.vx && vy < d.vy) ? vx + d.vx * vy : -1;
+  }
+  const int64_t plane_n = (int64_t)d.vx * d.vy;
   auto prefetch = [&](int z) {
     if (z <= zend) {
       Vec4<df>* dst = sm.plane[(z + 3) % 3];
-      for (int k = t; k < NP; k += NT) {
-        const int px = k % PX, py = k / PX;
-        const int vx = x0 - 1 + px, vy = y0 - 1 + py;
-        const bool ok = vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz;
-        const int64_t v = ok ? vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z) : 0;
-        double* raw = reinterpret_cast<double*>(&dst[k]);
-        cp_async_8(raw, u + v, ok);
-        cp_async_8(raw + 1, u + nv + v, ok);
-        cp_async_8(raw + 2, u + 2 * nv + v, ok);
+      const bool zok = z >= 0 && z < d.vz;
+      const int64_t zoff = (int64_t)z * plane_n;
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        const int k = t + s * NT;
+        if (k < NP) {
+          const bool ok = zok && pxy[s] >= 0;
+          const int64_t v = ok ? zoff + pxy[s] : 0;
+          double* raw = reinterpret_cast<double*>(&dst[k]);
+          cp_async_8(raw, u + v, ok);
+          cp_async_8(raw + 1, u + nv + v, ok);
+          cp_async_8(raw + 2, u + 2 * nv + v, ok);
+        }
       }
     }
     cp_async_commit();
   };
+  // per-layer operands one layer ahead (element rho^p, owned vertex's mask and load)
+  const int pex = gx - 1, pey = gy - 1;
+  const bool pe_xy = pex >= 0 && pey >= 0 && pex < d.ex && pey < d.ey;
+  auto load_pe = [&](int ez) -> double {
+    return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (int64_t)d.ex * (pey + (int64_t)d.ey * ez)] : 0.0;
+  };
+  uint8_t vm_n = 0;
+  double f_n[3] = {0.0, 0.0, 0.0};
+  auto load_vertex = [&](int z) {
+    if (!own || z < z0 || z >= zend) return;
+    const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * z);
+    vm_n = vmask[v];
+    if (MODE == 1) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f_n[c] = f[c * nv + v];
+    }
+  };
+  double pe_n = load_pe(z0 - 1);
   // split plane z's doubles into (hi, lo) pairs in place
   auto convert = [&](int z) {
     if (z > zend) return;
@@ -482,16 +548,20 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
   prefetch(z0);
   for (int ez = z0 - 1; ez < zend; ++ez) {
     prefetch(ez + 2);
+    const double pe_d = pe_n;
+    const uint8_t vm_c = vm_n;
+    double f_c[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) f_c[c] = f_n[c];
+    if (ez + 1 < zend) pe_n = load_pe(ez + 1);
+    load_vertex(ez + 1);
     cp_async_wait1();
     __syncthreads();
     if (ez == z0 - 1) convert(ez);
     convert(ez + 1);
     __syncthreads();
     {
-      const int ex = gx - 1, ey = gy - 1;
-      df pe(0);
-      if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
-        pe = df_from(rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)]);
+      const df pe = df_from(pe_d);
       if (pe != df(0)) {
         df c[3][8];
 #pragma unroll
@@ -522,13 +592,13 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
       }
       if (ez >= z0) {
         const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
-        const uint8_t m = vmask[v];
+        const uint8_t m = vm_c;
         const double y[3] = {df_to(b0), df_to(b1), df_to(b2)};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const bool fr = (m >> c) & 1;
           const int64_t idx = c * nv + v;
-          out[idx] = MODE == 1 ? (fr ? f[idx] - y[c] : 0.0) : (fr ? y[c] : 0.0);
+          out[idx] = MODE == 1 ? (fr ? f_c[c] - y[c] : 0.0) : (fr ? y[c] : 0.0);
         }
       }
       acc0 = t0; acc1 = t1; acc2 = t2;
@@ -700,32 +770,37 @@ __global__ void k_fine_diag_inv(LevelDims d, const T* __restrict__ rhop,
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 constexpr int MODAL_TXE = 32, MODAL_TYE = 8, MODAL_TZ = 16;
+// CTA tile rows of the FP32 / FP64 modal kernels
+template <typename T>
+constexpr int modal_tye() { return sizeof(T) == 4 ? TOPO_MODAL32_TYE : MODAL_TYE; }
 
 // Opt the modal kernels into more than 48 KB of dynamic shared memory (once).
 template <typename T>
 void modal_smem_attr(size_t smem) {
+  constexpr int TYE = modal_tye<T>();
   static std::once_flag once;
   std::call_once(once, [smem] {
-    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
 }
 
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb, int tz) {
+  constexpr int TYE = modal_tye<T>();
   if (tz <= 0) tz = MODAL_TZ;
-  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
+  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1),
                   ((d.vz + tz - 1) / tz) * nb);
-  constexpr int NT = MODAL_TXE * MODAL_TYE;
-  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
+  constexpr int NT = MODAL_TXE * TYE;
+  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
   modal_smem_attr<T>(smem);
   ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0};
   if (residual)
-    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+    k_fine_modal<T, MODAL_TXE, TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
   else
-    k_fine_modal<T, MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+    k_fine_modal<T, MODAL_TXE, TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
 }
 
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
@@ -751,14 +826,15 @@ template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                       const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
                       int tz) {
+  constexpr int TYE = modal_tye<T>();
   if (tz <= 0) tz = MODAL_TZ;
-  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
+  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1),
                   ((d.vz + tz - 1) / tz) * nb);
-  constexpr int NT = MODAL_TXE * MODAL_TYE;
-  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, MODAL_TYE>);
+  constexpr int NT = MODAL_TXE * TYE;
+  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
   modal_smem_attr<T>(smem);
   ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0};
-  k_fine_modal<T, MODAL_TXE, MODAL_TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, tz, ch);
+  k_fine_modal<T, MODAL_TXE, TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, tz, ch);
 }
 
 template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,

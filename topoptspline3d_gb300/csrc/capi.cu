@@ -386,6 +386,13 @@ void prolong_T(topo_handle* h, int lf) {
   count_launch();
 }
 
+// True when a V-cycle from a zero guess never reads level U before writing it
+// in full: Chebyshev pre-smoothing, whose first step from zero writes the
+// iterate without reading it.
+inline bool cheb_zero_start(int smoother, int pre, const ChebParams& cp) {
+  return smoother == TOPO_SMOOTH_CHEBYSHEV && pre >= 1 && cp.degree >= 1;
+}
+
 // V-cycle in the reference order (grid/Grid.cpp:2399-2444).  `sym` runs the
 // adjoint sweep after the coarse correction so the cycle is a symmetric
 // preconditioner.  Level-0 U must hold the initial guess, F the right-hand side;
@@ -397,7 +404,7 @@ template <typename T>
 void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, const ChebParams& cp,
                  bool zero0 = false) {
   const int nl = (int)h->lv.size();
-  const bool cheb_pre = smoother == TOPO_SMOOTH_CHEBYSHEV && pre >= 1 && cp.degree >= 1;
+  const bool cheb_pre = cheb_zero_start(smoother, pre, cp);
   if (nl == 1) {
     smooth_level<T>(h, 0, pre, false, smoother, cp, zero0);
     smooth_level<T>(h, 0, post, sym, smoother, cp);
@@ -483,11 +490,14 @@ __global__ void k_power_start(int64_t nv, const uint8_t* vmask, T* x) {
   x[i] = (T)v;
 }
 
+// z = s D^-1 r with s = 1/sqrt(*nrm2) (the power iteration's normalisation of
+// its vector, applied after the operator, which is linear).
 template <typename T>
-__global__ void k_dinv_apply(int64_t nv, const T* dinv, const T* r, T* z) {
+__global__ void k_dinv_apply(int64_t nv, const T* dinv, const T* r, T* z, const double* nrm2) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
-  const T r0 = r[v], r1 = r[nv + v], r2 = r[2 * nv + v];
+  const T sc = (T)rsqrt(*nrm2);
+  const T r0 = r[v] * sc, r1 = r[nv + v] * sc, r2 = r[2 * nv + v] * sc;
   for (int i = 0; i < 3; ++i)
     z[i * nv + v] = dinv[(3 * i) * nv + v] * r0 + dinv[(3 * i + 1) * nv + v] * r1 + dinv[(3 * i + 2) * nv + v] * r2;
 }
@@ -500,6 +510,8 @@ __global__ void k_to_double(int64_t n, const T* a, double* b) {
 
 inline unsigned nb256(int64_t n) { return (unsigned)((n + 255) / 256); }
 
+int read_scalars(topo_handle* h, int first, int count);
+
 template <typename T>
 int estimate_lmax(topo_handle* h, int l, double* out) {
   DevLevel& L = h->lv[l];
@@ -507,7 +519,7 @@ int estimate_lmax(topo_handle* h, int l, double* out) {
   // work vectors in precision T: the level's R, U2 and Chebyshev direction
   // buffers (all free outside a V-cycle)
   T* x = P<T>::R(L);
-  T* xn = P<T>::cd(L);
+  T* y = P<T>::cd(L);
   T* z = P<T>::U2(L);
   // First estimate: 12 steps from the deterministic start (as the oracle).
   // After an operator update: 4 steps from the previous design's vector (the
@@ -524,30 +536,36 @@ int estimate_lmax(topo_handle* h, int l, double* out) {
     k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, x);
     count_launch();
   }
+  // One step: with s = 1/|x|, z = D^-1 A (s x) = s D^-1 (A x) and the
+  // Rayleigh estimate (s x).z = s (x.z); x <- z.
   auto power_steps = [&](int k) {
     for (int it = 0; it < k; ++it) {
       launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP);
-      launch_scale_by_rnorm<T>(h->stream, x, xn, h->sc, S_TMP, n3);
-      if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, xn, nullptr, x, false, 1,
+      if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, x, nullptr, y, false, 1,
                                        sizeof(T) == 4 ? h->tz32 : h->tz64);
-      else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), xn, nullptr, x, false);
-      k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), x, z);
-      launch_dot<T>(h->stream, xn, z, n3, h->partial, h->sc + S_TMP + 1);
+      else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), x, nullptr, y, false);
+      k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), y, z, h->sc + S_TMP);
+      launch_dot<T>(h->stream, x, z, n3, h->partial, h->sc + S_TMP + 1);
       std::swap(x, z);
-      count_launch(7);
+      count_launch(6);
     }
+  };
+  double lam = 0.0;
+  auto estimate = [&]() -> int {
+    RET(read_scalars(h, S_TMP, 2));
+    const double xx = h->hsc[S_TMP], xz = h->hsc[S_TMP + 1];
+    lam = xx > 0 ? xz / std::sqrt(xx) : 0.0;
+    return TOPO_OK;
   };
   power_steps(steps);
   if (warm) {
-    CK(cudaMemcpyAsync(h->hsc, h->sc + S_TMP + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    if (h->hsc[0] < 0.95 * P<T>::lprev(L)) power_steps(8);
+    RET(estimate());
+    if (lam < 0.95 * P<T>::lprev(L)) power_steps(8);
   }
   CK(cudaMemcpyAsync(P<T>::eig(L), x, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemcpyAsync(h->hsc, h->sc + S_TMP + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
-  *out = h->hsc[0];
-  P<T>::lprev(L) = h->hsc[0];
+  RET(estimate());
+  *out = lam;
+  P<T>::lprev(L) = lam;
   return TOPO_OK;
 }
 
@@ -578,11 +596,15 @@ int read_scalars(topo_handle* h, int first, int count) {
 // so an FCG may run nested inside another one's preconditioner.
 template <typename T, typename Prec>
 int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, double rtol, int maxit,
-          int base, Prec&& prec, int* iters, double* rel_out, double bnorm_ref) {
+          int base, Prec&& prec, int* iters, double* rel_out, double bnorm_ref, bool x_zero = false) {
   DevLevel& L0 = h->lv[0];
   const int64_t n3 = 3 * L0.d.nv;
   double* sc = h->sc + base;
-  level_apply<T>(h, 0, x, b, r, true);  // r = b - A x
+  if (x_zero) {  // x = 0 on entry: r = b (r may be b itself)
+    if (r != b) CK(cudaMemcpyAsync(r, b, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  } else {
+    level_apply<T>(h, 0, x, b, r, true);  // r = b - A x
+  }
   launch_dot<T>(h->stream, r, r, n3, h->partial, sc + S_RR);
   count_launch(2);
   RET(read_scalars(h, base + S_RR, 1));
@@ -623,8 +645,8 @@ template <typename T>
 int vcycle_prec(topo_handle* h, const T* r, int pre, int post, int smoother, const ChebParams& cp) {
   DevLevel& L0 = h->lv[0];
   const int64_t n3 = 3 * L0.d.nv;
-  CK(cudaMemcpyAsync(P<T>::F(L0), r, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaMemsetAsync(P<T>::U(L0), 0, sizeof(T) * n3, h->stream));
+  if (P<T>::F(L0) != r) CK(cudaMemcpyAsync(P<T>::F(L0), r, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
+  if (!cheb_zero_start(smoother, pre, cp)) CK(cudaMemsetAsync(P<T>::U(L0), 0, sizeof(T) * n3, h->stream));
   if (sizeof(T) == 4) vcycle32(h, pre, post, smoother, cp, true);
   else vcycle_core<T>(h, pre, post, true, smoother, cp, true);
   return TOPO_OK;
@@ -1262,7 +1284,6 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     CK(cudaMemcpyAsync(h->f, L0.F, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-1;
     const int inner_max = o->inner_max > 0 ? o->inner_max : 1;
-    float* b32 = reinterpret_cast<float*>(h->work);
     int it = 0, nvc = 0;
     double rel = 0;
     // learned correction (1) or harvesting (2)
@@ -1316,7 +1337,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       }
       if (inner_max <= 1) {
         launch_d2f(h->stream, r, L0.F32, n3);
-        CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3, h->stream));
+        if (!cheb_zero_start(o->smoother, o->pre, cp)) CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3, h->stream));
         ++nvc;
         vcycle32(h, o->pre, o->post, o->smoother, cp, true);
         RET(net(L0.F32, L0.U32));
@@ -1328,7 +1349,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
         count_launch(2);
         return TOPO_OK;
       }
-      launch_d2f(h->stream, r, b32, n3);
+      launch_d2f(h->stream, r, L0.F32, n3);
       CK(cudaMemsetAsync(h->x32, 0, sizeof(float) * n3, h->stream));
       count_launch();
       int iit = 0;
@@ -1336,8 +1357,10 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       // relative to ||r|| (FP64 norm of the outer residual)
       RET(read_scalars(h, S_RR, 1));
       const double rnorm = std::sqrt(h->hsc[S_RR]);
-      RET(fcg_T<float>(h, h->x32, b32, h->r32, h->d32, h->q32, h->rold32, L0.U32, inner_rtol, inner_max,
-                       8, prec32, &iit, &irel, rnorm > 0 ? rnorm : 1.0));
+      // the inner residual lives in level-0 F32, the V-cycle's right-hand side,
+      // so the preconditioner needs no copy; x32 = 0 gives r = b without a matvec
+      RET(fcg_T<float>(h, h->x32, L0.F32, L0.F32, h->d32, h->q32, h->rold32, L0.U32, inner_rtol, inner_max,
+                       8, prec32, &iit, &irel, rnorm > 0 ? rnorm : 1.0, true));
       k_to_double<float><<<nb256(n3), 256, 0, h->stream>>>(n3, h->x32, z);
       count_launch();
       return TOPO_OK;
@@ -1706,7 +1729,8 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
   while (!converged() && it < o->max_iter) {
     // z = V(r): one FP32 V-cycle for the whole batch
     launch_d2f(h->stream, m.r, L0.F32, n3 * nb);
-    CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3 * nb, h->stream));
+    if (!cheb_zero_start(TOPO_SMOOTH_CHEBYSHEV, o->pre, cp))
+      CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3 * nb, h->stream));
     vcycle32(h, o->pre, o->post, TOPO_SMOOTH_CHEBYSHEV, cp, true);
     ++nvc;
     k_to_double<float><<<nb256(n3 * nb), 256, 0, h->stream>>>(n3 * nb, L0.U32, m.z);

@@ -2,6 +2,7 @@
 // trilinear transfers, Galerkin coarse operators and the coarsest dense solve.
 #include <cooperative_groups.h>
 
+#include "df.cuh"
 #include "topo_internal.h"
 
 namespace cg = cooperative_groups;
@@ -647,18 +648,31 @@ __global__ void k_gauss_jordan(int n, double* A, int* status) {
 //   A[i,c] = D^-1 | P | -C D^-1 | A[i,c] - C[i,:] P[:,c]
 // for (i in K, c in K) | (i in K) | (c in K) | otherwise.  Three grid barriers
 // per panel instead of two per pivot.
+//
+// G is the arithmetic of the panels and updates: double, or double-float (df,
+// about 48-bit significands on the FP32 pipe, which has 58x the FP64 rate on
+// GB300).  The matrix stays FP64 in global memory either way; pivots and their
+// reciprocals are taken in FP64.  The double-float form serves the inverse of a
+// coarsest matrix assembled from FP32 stencils, whose entries carry 24 bits.
 constexpr int GJB = 32;
 
-__global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ A, double* __restrict__ work,
+__device__ __forceinline__ double gj_from(double v, double) { return v; }
+__device__ __forceinline__ df gj_from(double v, df) { return df_from(v); }
+__device__ __forceinline__ double gj_to(double v) { return v; }
+__device__ __forceinline__ double gj_to(df v) { return df_to(v); }
+
+template <typename G>
+__global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ A, G* __restrict__ work,
                                                     int* __restrict__ status) {
   cg::grid_group grid = cg::this_grid();
-  __shared__ double sd[GJB][GJB + 1];
-  __shared__ double sc[GJB][GJB + 1];
-  __shared__ double sp[GJB][GJB + 1];
+  __shared__ G sd[GJB][GJB + 1];
+  __shared__ G sc[GJB][GJB + 1];
+  __shared__ G sp[GJB][GJB + 1];
   __shared__ int sflag;
-  double* Dg = work;                 // [GJB][GJB]
-  double* P = work + GJB * GJB;      // [GJB][n]
-  double* Cp = P + (int64_t)GJB * n; // [n][GJB]
+  const G zero = gj_from(0.0, G());
+  G* Dg = work;                 // [GJB][GJB]
+  G* P = work + GJB * GJB;      // [GJB][n]
+  G* Cp = P + (int64_t)GJB * n; // [n][GJB]
   const int tid = threadIdx.x;
   double dmax = 0.0;
   for (int k = 0; k < n; ++k) dmax = fmax(dmax, fabs(A[(int64_t)k * n + k]));
@@ -670,12 +684,12 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
     if (blockIdx.x == 0) {
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+        sd[r][c] = (r < kb && c < kb) ? gj_from(A[(int64_t)(k0 + r) * n + k0 + c], G()) : zero;
       }
       if (tid == 0) sflag = 0;
       __syncthreads();
       for (int j = 0; j < kb; ++j) {
-        const double p = sd[j][j];
+        const double p = gj_to(sd[j][j]);
         if (p < -tol) {
           if (tid == 0) { status[1] = k0 + j + 1; sflag = 1; }
           break;
@@ -683,22 +697,22 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         __syncthreads();
         if (p <= tol) {  // drop DOF k0 + j
           for (int e = tid; e < 2 * GJB; e += blockDim.x) {
-            if (e < GJB) sd[j][e] = 0.0;
-            else sd[e - GJB][j] = 0.0;
+            if (e < GJB) sd[j][e] = zero;
+            else sd[e - GJB][j] = zero;
           }
           if (tid == 0) status[0] += 1;
           __syncthreads();
           continue;
         }
-        const double rp = 1.0 / p;
+        const G rp = gj_from(1.0 / p, G());
         for (int e = tid; e < kb * kb; e += blockDim.x) {
           const int r = e / kb, c = e % kb;
-          if (r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
+          if (r != j && c != j) sd[r][c] = sd[r][c] - sd[r][j] * sd[j][c] * rp;
         }
         __syncthreads();
         for (int e = tid; e < 2 * kb; e += blockDim.x) {
-          if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
-          else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
+          if (e < kb) { if (e != j) sd[j][e] = sd[j][e] * rp; else sd[j][j] = rp; }
+          else { const int r = e - kb; if (r != j) sd[r][j] = zero - sd[r][j] * rp; }
         }
         __syncthreads();
       }
@@ -711,14 +725,14 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid, gs = (int64_t)gridDim.x * blockDim.x;
     for (int64_t e = gt; e < (int64_t)kb * n; e += gs) {
       const int r = (int)(e / n), c = (int)(e % n);
-      double v = 0.0;
+      G v = zero;
       if (c < k0 || c >= k0 + kb)
-        for (int m = 0; m < kb; ++m) v += Dg[r * GJB + m] * A[(int64_t)(k0 + m) * n + c];
+        for (int m = 0; m < kb; ++m) v = v + Dg[r * GJB + m] * gj_from(A[(int64_t)(k0 + m) * n + c], G());
       P[(int64_t)r * n + c] = v;
     }
     for (int64_t e = gt; e < (int64_t)n * kb; e += gs) {
       const int i = (int)(e / kb), m = (int)(e % kb);
-      Cp[(int64_t)i * GJB + m] = (i < k0 || i >= k0 + kb) ? A[(int64_t)i * n + k0 + m] : 0.0;
+      Cp[(int64_t)i * GJB + m] = (i < k0 || i >= k0 + kb) ? gj_from(A[(int64_t)i * n + k0 + m], G()) : zero;
     }
     grid.sync();
     // ---- C: rank-kb update, GJB x GJB tiles of A per CTA iteration
@@ -727,8 +741,8 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
       __syncthreads();
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : 0.0;
-        sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : 0.0;
+        sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : zero;
+        sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : zero;
         sd[r][c] = Dg[r * GJB + c];
       }
       __syncthreads();
@@ -739,17 +753,17 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         const bool iK = i >= k0 && i < k0 + kb, cK = col >= k0 && col < k0 + kb;
         double& a = A[(int64_t)i * n + col];
         if (iK && cK) {
-          a = sd[i - k0][col - k0];
+          a = gj_to(sd[i - k0][col - k0]);
         } else if (iK) {
-          a = sp[i - k0][c];
+          a = gj_to(sp[i - k0][c]);
         } else if (cK) {
-          double v = 0.0;
-          for (int m = 0; m < kb; ++m) v += sc[r][m] * sd[m][col - k0];
-          a = -v;
+          G v = zero;
+          for (int m = 0; m < kb; ++m) v = v + sc[r][m] * sd[m][col - k0];
+          a = -gj_to(v);
         } else {
-          double v = a;
-          for (int m = 0; m < kb; ++m) v -= sc[r][m] * sp[m][c];
-          a = v;
+          G v = gj_from(a, G());
+          for (int m = 0; m < kb; ++m) v = v - sc[r][m] * sp[m][c];
+          a = gj_to(v);
         }
       }
     }
@@ -823,19 +837,21 @@ void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double*
   k_symmetrize<<<nblk(n * n, 256), 256, 0, s>>>((int)n, A);
 }
 
-int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev) {
+int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev, bool df_arith) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int threads = 256;
   if (work) {  // blocked form: GJB-pivot panels, rank-GJB updates
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_blocked, threads, 0);
+    static_assert(sizeof(df) == sizeof(double), "the work array holds either type");
+    void* fn = df_arith ? (void*)k_gj_blocked<df> : (void*)k_gj_blocked<double>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
     if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
     const int tiles = ((n + GJB - 1) / GJB) * ((n + GJB - 1) / GJB);
     const int blocks = std::max(1, std::min(tiles, nsm * std::min(per_sm, 2)));
     cudaMemsetAsync(status_dev, 0, 2 * sizeof(int), s);
     void* args[] = {&n, &A, &work, &status_dev};
-    return (int)cudaLaunchCooperativeKernel((void*)k_gj_blocked, dim3(blocks), dim3(threads), args, 0, s);
+    return (int)cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
   }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gauss_jordan, threads, 0);
   if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;

@@ -106,6 +106,8 @@ struct topo_handle {
   int filt_n = 0;
   // reductions
   double* partial = nullptr;
+  double* fdot = nullptr;  // per-CTA partials of the fine operator's fused dot
+  int fdot_cap = 0;
   double* sc = nullptr;    // device scalar slots
   double* hsc = nullptr;   // pinned host mirror
   int64_t active_elements = 0, gs_padded_elements = 0;
@@ -621,13 +623,27 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
     }
     if (it > 0) launch_scalar_ratio(h->stream, sc, S_RZ, S_ZROLD, S_RZOLD, S_BETA);
     launch_pcg_dir<T>(h->stream, z, d, sc, S_BETA, it == 0, n3);
-    level_apply<T>(h, 0, d, nullptr, q, false);
-    launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ);
+    // q = A d with d.q: fused into the FP32 operator's epilogue
+    int nparts = 0;
+    if (sizeof(T) == 4 && h->fdot && h->nb == 1) {
+      EventPair* ev = prof_begin(h, P<T>::fam_apply);
+      nparts = launch_fine_apply_dot<T>(h->stream, L0.d, P<T>::rhop(h), L0.vmask, d, q, h->tz32, h->fdot,
+                                        h->fdot_cap);
+      prof_end(h, ev);
+    }
+    if (nparts > 0) {
+      launch_finalize_sum(h->stream, h->fdot, nparts, sc + S_DQ);
+      count_launch(2);
+    } else {
+      level_apply<T>(h, 0, d, nullptr, q, false);
+      launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ);
+      count_launch(2);
+    }
     launch_scalar_ratio(h->stream, sc, S_RZ, -1, S_DQ, S_ALPHA);
-    launch_pcg_update<T>(h->stream, x, r, rold, d, q, sc, S_ALPHA, n3);
+    // x += alpha d, rold = r, r -= alpha q with r.r of the new residual
+    launch_pcg_update_rr<T>(h->stream, x, r, rold, d, q, sc, S_ALPHA, n3, h->partial, sc + S_RR);
     CK(cudaMemcpyAsync(sc + S_RZOLD, sc + S_RZ, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-    launch_dot<T>(h->stream, r, r, n3, h->partial, sc + S_RR);
-    count_launch(it > 0 ? 9 : 8);
+    count_launch(it > 0 ? 5 : 4);
     CKL();
     RET(read_scalars(h, base + S_RR, 1));
     rn = std::sqrt(h->hsc[base + S_RR]);
@@ -764,6 +780,10 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     A(dalloc(hp, &h->q32, 3 * d0.nv)); A(dalloc(hp, &h->rold32, 3 * d0.nv));
     A(dalloc(hp, &h->dKe, 576));
     A(dalloc(hp, &h->partial, 2048)); A(dalloc(hp, &h->sc, S_COUNT)); A(dalloc(hp, &h->status, 4));
+    // partials of the fused fine-operator dot: one per CTA of 32 x 8 element
+    // tiles (31 x 7 owned vertices) at z-march depths of 4 and more
+    h->fdot_cap = (int)std::min<int64_t>(1 << 24, (int64_t)((d0.vx + 30) / 31) * ((d0.vy + 6) / 7) * ((d0.vz + 3) / 4));
+    A(dalloc(hp, &h->fdot, h->fdot_cap));
   }
   if (rc == TOPO_OK && nl > 1) {
     const LevelDims& dl = h->lv.back().d;

@@ -178,7 +178,25 @@ struct ChebArgs {
   void* dvec;        // [3][nv]
   double c_old, c_new;
   int first;
+  double* dotp;      // MODE 0: per-CTA partial sums of u.out (null: none)
 };
+
+// Sum of v over the CTA (valid in thread 0); every thread must call it.
+__device__ __forceinline__ double modal_block_sum(double v) {
+  __shared__ double ws[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) ws[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = lane < nw ? ws[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;
+}
 
 template <typename T>
 struct alignas(4 * sizeof(T)) Vec4 {
@@ -295,6 +313,7 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
   // always read the stored inverse.
   constexpr bool FLY_DIAG = (MODE == 2) && (sizeof(T) == 4) && !TOPO_FINE32_STORED_DIAG;
   T pprev[4] = {T(0), T(0), T(0), T(0)};
+  T dsum = T(0);  // MODE 0 with ch.dotp: this thread's share of u.out
   // This thread's plane slots k = t + s NT and their in-plane vertex offsets
   // (-1 outside the domain), fixed for the whole z march.
   constexpr int KS = (NP + NT - 1) / NT;
@@ -368,7 +387,7 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
     // the owned vertex's own value at plane ez (Chebyshev update); read here,
     // before the slot can be refilled by the next layer's prefetch
     Vec4<T> uo{T(0), T(0), T(0), T(0)};
-    if (MODE == 2) uo = sm.plane[(ez + 3) % 3][(i + 1) + PX * (j + 1)];
+    if (MODE == 2 || (MODE == 0 && ch.dotp)) uo = sm.plane[(ez + 3) % 3][(i + 1) + PX * (j + 1)];
     {
       if (pe != T(0)) {
         T c[3][8];
@@ -406,11 +425,14 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
         const uint8_t m = vm_c;
         const T y[3] = {b0, b1, b2};
         if (MODE < 2) {
+          const T uv[3] = {uo.x, uo.y, uo.z};
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const bool fr = (m >> c) & 1;
             const int64_t idx = c * nv + v;
-            out[idx] = MODE == 1 ? (fr ? f_c[c] - y[c] : T(0)) : (fr ? y[c] : T(0));
+            const T o = MODE == 1 ? (fr ? f_c[c] - y[c] : T(0)) : (fr ? y[c] : T(0));
+            out[idx] = o;
+            if (MODE == 0) dsum += uv[c] * o;
           }
         } else {
           const T* __restrict__ dinv = static_cast<const T*>(ch.dinv);
@@ -455,6 +477,10 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
   }
   // drain the (empty) trailing copy groups before the CTA exits
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+  if (MODE == 0 && ch.dotp) {
+    const double bs = modal_block_sum((double)dsum);
+    if (t == 0) ch.dotp[blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z)] = bs;
+  }
 }
 
 // The same operator (MODE 0: out = K u, MODE 1: out = f - K u) on FP64 vectors
@@ -796,12 +822,36 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
   constexpr int NT = MODAL_TXE * TYE;
   const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
   modal_smem_attr<T>(smem);
-  ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0};
+  ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr};
   if (residual)
     k_fine_modal<T, MODAL_TXE, TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
   else
     k_fine_modal<T, MODAL_TXE, TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
 }
+
+// out = K u with the per-CTA partial sums of u.out in partial[0, n) (one
+// right-hand side).  Returns n, or 0, launching nothing, when the grid has more
+// CTAs than the cap partial slots.
+template <typename T>
+int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
+                          T* out, int tz, double* partial, int cap) {
+  constexpr int TYE = modal_tye<T>();
+  if (tz <= 0) tz = MODAL_TZ;
+  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1), (d.vz + tz - 1) / tz);
+  const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
+  if (nparts > cap) return 0;
+  constexpr int NT = MODAL_TXE * TYE;
+  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
+  modal_smem_attr<T>(smem);
+  ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial};
+  k_fine_modal<T, MODAL_TXE, TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, nullptr, out, tz, ch);
+  return (int)nparts;
+}
+
+template int launch_fine_apply_dot<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
+                                          const float*, float*, int, double*, int);
+template int launch_fine_apply_dot<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
+                                           const double*, double*, int, double*, int);
 
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
                           const double* u, const double* f, double* out, bool residual, int nb, int tz) {
@@ -833,7 +883,7 @@ void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const u
   constexpr int NT = MODAL_TXE * TYE;
   const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
   modal_smem_attr<T>(smem);
-  ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0};
+  ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nullptr};
   k_fine_modal<T, MODAL_TXE, TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, tz, ch);
 }
 

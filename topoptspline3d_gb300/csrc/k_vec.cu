@@ -185,6 +185,44 @@ void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T*
   k_pcg_update<T><<<nblk(n, 256), 256, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n);
 }
 
+// The same update fused with the new residual's squared norm: per-thread sums
+// in the vectors' precision, combined in FP64 in a fixed order (deterministic).
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_update_rr(T* __restrict__ x, T* __restrict__ r,
+                                                               T* __restrict__ rold, const T* __restrict__ d,
+                                                               const T* __restrict__ q, const double* __restrict__ sc,
+                                                               int alpha_slot, int64_t n, double* __restrict__ partial) {
+  const T alpha = (T)sc[alpha_slot];
+  T acc = T(0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T ri = r[i];
+    rold[i] = ri;
+    x[i] = x[i] + alpha * d[i];
+    const T rn = ri - alpha * q[i];
+    r[i] = rn;
+    acc += rn * rn;
+  }
+  const double bs = block_sum((double)acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = bs;
+}
+
+template <typename T>
+void launch_pcg_update_rr(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
+                          int alpha_slot, int64_t n, double* partial, double* rr) {
+  const int nb = reduce_blocks(n);
+  k_pcg_update_rr<T><<<nb, RED_THREADS, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n, partial);
+  k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, rr);
+}
+
+template void launch_pcg_update_rr<double>(cudaStream_t, double*, double*, double*, const double*, const double*,
+                                           const double*, int, int64_t, double*, double*);
+template void launch_pcg_update_rr<float>(cudaStream_t, float*, float*, float*, const float*, const float*,
+                                          const double*, int, int64_t, double*, double*);
+
+void launch_finalize_sum(cudaStream_t s, const double* partial, int nb, double* out) {
+  k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, out);
+}
+
 // x = a * sc_scale(y) where the scale is 1/sqrt(sc[slot]) (power-iteration normalisation).
 template <typename T>
 __global__ void k_scale_by_rnorm(const T* __restrict__ y, T* __restrict__ x, const double* __restrict__ sc,

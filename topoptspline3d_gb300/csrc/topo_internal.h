@@ -74,6 +74,12 @@ struct Stream {
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb = 1, int tz = 0);
+// out = K u (level 0, one right-hand side) with per-CTA partial sums of u.out
+// in partial; returns their count (sum them with launch_finalize_sum), or 0 and
+// launches nothing when the kernel would need more than cap partial slots.
+template <typename T>
+int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
+                          T* out, int tz, double* partial, int cap);
 // FP64 vectors, double-float arithmetic (k_fine_modal_df)
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
                           const double* u, const double* f, double* out, bool residual, int nb = 1, int tz = 0);
@@ -156,6 +162,12 @@ void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta
 template <typename T>
 void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q,
                        const double* sc, int alpha_slot, int64_t n);
+// launch_pcg_update fused with rr = r.r of the updated residual (2 launches)
+template <typename T>
+void launch_pcg_update_rr(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
+                          int alpha_slot, int64_t n, double* partial, double* rr);
+// out = sum of nb partials in a fixed order
+void launch_finalize_sum(cudaStream_t s, const double* partial, int nb, double* out);
 template <typename T>
 void launch_scale_by_rnorm(cudaStream_t s, const T* y, T* x, const double* sc, int slot, int64_t n);
 

@@ -1129,9 +1129,7 @@ int topo_update_operators(topo_handle* h) {
     launch_dense_from_stencil(h->stream, Lc.d, st, h->A);
     count_launch(2);
     CKL();
-    // FP32-only operators: the matrix comes from FP32 stencils, and the
-    // double-float elimination keeps twice their precision on the FP32 pipe
-    int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status, !b64);
+    int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status);
     count_launch();
     if (e != (int)cudaSuccess)
       return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));

@@ -2,7 +2,8 @@
 // trilinear transfers, Galerkin coarse operators and the coarsest dense solve.
 #include <cooperative_groups.h>
 
-#include "df.cuh"
+#include <mutex>
+
 #include "topo_internal.h"
 
 namespace cg = cooperative_groups;
@@ -273,55 +274,141 @@ __global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
   fc[v] = s0; fc[cd.nv + v] = s1; fc[2 * cd.nv + v] = s2;
 }
 
+// Restriction by a factor of 4, separably: a CTA owns CX x CY coarse vertices
+// (one thread each) over CZ coarse planes and marches over the fine planes of
+// their support.  Per fine plane it stages the (4 CX + 3) x (4 CY + 3) region
+// in shared memory (zero outside the domain), applies the 7-tap weights
+// 1 2 3 4 3 2 1 along x and then y, and adds the result with the z weight to
+// the coarse planes it touches.  The fine residual is read about 1.3 times
+// instead of through 343 scattered loads per coarse vertex.
+constexpr int R4X = 16, R4Y = 8, R4Z = 4, R4FX = 4 * R4X + 3, R4FY = 4 * R4Y + 3;
+constexpr int R4_THREADS = R4X * R4Y;
+
+template <typename T>
+constexpr size_t restrict4_smem() { return sizeof(T) * 3 * R4FY * (R4FX + R4X); }
+
+template <typename T>
+__global__ void __launch_bounds__(R4_THREADS) k_restrict4(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
+                                                          T* __restrict__ fc, int nbx) {
+  extern __shared__ __align__(16) unsigned char r4_smem[];
+  T* sp = reinterpret_cast<T*>(r4_smem);  // [3][R4FY][R4FX] fine plane region
+  T* tx = sp + 3 * R4FY * R4FX;           // [3][R4FY][R4X] after the x pass
+  rf += (int64_t)blockIdx.z * 3 * fd.nv;  // right-hand side of the batch
+  fc += (int64_t)blockIdx.z * 3 * cd.nv;
+  const int cx0 = (blockIdx.x % nbx) * R4X, cy0 = (blockIdx.x / nbx) * R4Y, cz0 = blockIdx.y * R4Z;
+  const int t = threadIdx.x, lx = t % R4X, ly = t / R4X;
+  const int fx0 = 4 * cx0 - 3, fy0 = 4 * cy0 - 3;
+  T acc[R4Z][3];
+#pragma unroll
+  for (int k = 0; k < R4Z; ++k) acc[k][0] = acc[k][1] = acc[k][2] = T(0);
+  const int fz_lo = max(0, 4 * cz0 - 3), fz_hi = min(fd.vz - 1, 4 * (cz0 + R4Z - 1) + 3);
+  for (int fz = fz_lo; fz <= fz_hi; ++fz) {
+    __syncthreads();  // the previous plane's readers are done
+    const int64_t zoff = (int64_t)fd.vx * fd.vy * fz;
+#pragma unroll 4
+    for (int k = t; k < 3 * R4FY * R4FX; k += R4_THREADS) {
+      const int c = k / (R4FY * R4FX), r = k - c * (R4FY * R4FX), yy = r / R4FX, xx = r - yy * R4FX;
+      const int fx = fx0 + xx, fy = fy0 + yy;
+      T v = T(0);
+      if (fx >= 0 && fy >= 0 && fx < fd.vx && fy < fd.vy) v = rf[c * fd.nv + zoff + fx + (int64_t)fd.vx * fy];
+      sp[k] = v;
+    }
+    __syncthreads();
+    for (int k = t; k < 3 * R4FY * R4X; k += R4_THREADS) {
+      const int c = k / (R4FY * R4X), r = k - c * (R4FY * R4X), yy = r / R4X, cx = r - yy * R4X;
+      const T* row = sp + (c * R4FY + yy) * R4FX + 4 * cx;  // taps dx = -3..3
+      tx[k] = (row[0] + row[6]) + T(2) * (row[1] + row[5]) + T(3) * (row[2] + row[4]) + T(4) * row[3];
+    }
+    __syncthreads();
+    T p[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const T* col = tx + (c * R4FY + 4 * ly) * R4X + lx;  // taps dy = -3..3
+      p[c] = (col[0] + col[6 * R4X]) + T(2) * (col[R4X] + col[5 * R4X]) + T(3) * (col[2 * R4X] + col[4 * R4X]) +
+             T(4) * col[3 * R4X];
+    }
+#pragma unroll
+    for (int k = 0; k < R4Z; ++k) {
+      const int dz = fz - 4 * (cz0 + k), ad = dz < 0 ? -dz : dz;
+      if (ad <= 3) {
+        const T w = T(4 - ad);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) acc[k][c] += w * p[c];
+      }
+    }
+  }
+  const int cx = cx0 + lx, cy = cy0 + ly;
+  if (cx >= cd.vx || cy >= cd.vy) return;
+  const T inv = T(1) / T(64);
+#pragma unroll
+  for (int k = 0; k < R4Z; ++k) {
+    const int cz = cz0 + k;
+    if (cz >= cd.vz) break;
+    const int64_t cv = cx + (int64_t)cd.vx * (cy + (int64_t)cd.vy * cz);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fc[c * cd.nv + cv] = acc[k][c] * inv;
+  }
+}
+
+// Prolongation: one fine vertex per thread on a (64 x 4) x-y tile of one fine
+// plane (no index division); blockIdx.z is the plane, the batch loops inside.
 template <typename T, int FCT>
-__global__ void k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc, T* __restrict__ uf,
-                          const uint8_t* __restrict__ vmask) {
-  uc += (int64_t)blockIdx.y * 3 * cd.nv;  // right-hand side of the batch
-  uf += (int64_t)blockIdx.y * 3 * fd.nv;
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= fd.nv) return;
-  const int x = (int)(v % fd.vx);
-  const int64_t t = v / fd.vx;
-  const int y = (int)(t % fd.vy), z = (int)(t / fd.vy);
+__global__ void __launch_bounds__(256) k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc,
+                                                 T* __restrict__ uf, const uint8_t* __restrict__ vmask, int nb) {
+  const int x = blockIdx.x * 64 + threadIdx.x, y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
+  if (x >= fd.vx || y >= fd.vy) return;
+  const int64_t v = x + (int64_t)fd.vx * (y + (int64_t)fd.vy * z);
   const uint8_t m = vmask[v];
   if (!(m & 7) || !(m & 8)) return;
   const int cx = x / FCT, cy = y / FCT, cz = z / FCT;
   const int rx = x % FCT, ry = y % FCT, rz = z % FCT;
-  T s0 = T(0), s1 = T(0), s2 = T(0);
   const T inv = T(1) / T(FCT * FCT * FCT);
+  for (int b = 0; b < nb; ++b) {
+    const T* ucb = uc + (int64_t)b * 3 * cd.nv;
+    T* ufb = uf + (int64_t)b * 3 * fd.nv;
+    T s0 = T(0), s1 = T(0), s2 = T(0);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
-    const int wx = ox ? rx : FCT - rx, wy = oy ? ry : FCT - ry, wz = oz ? rz : FCT - rz;
-    const int wi = wx * wy * wz;
-    if (wi == 0) continue;
-    const T w = T(wi) * inv;
-    const int64_t cv = (cx + ox) + (int64_t)cd.vx * ((cy + oy) + (int64_t)cd.vy * (cz + oz));
-    s0 += w * uc[cv];
-    s1 += w * uc[cd.nv + cv];
-    s2 += w * uc[2 * cd.nv + cv];
+    for (int k = 0; k < 8; ++k) {
+      const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+      const int wx = ox ? rx : FCT - rx, wy = oy ? ry : FCT - ry, wz = oz ? rz : FCT - rz;
+      const int wi = wx * wy * wz;
+      if (wi == 0) continue;
+      const T w = T(wi) * inv;
+      const int64_t cv = (cx + ox) + (int64_t)cd.vx * ((cy + oy) + (int64_t)cd.vy * (cz + oz));
+      s0 += w * ucb[cv];
+      s1 += w * ucb[cd.nv + cv];
+      s2 += w * ucb[2 * cd.nv + cv];
+    }
+    if (m & 1) ufb[v] += s0;
+    if (m & 2) ufb[fd.nv + v] += s1;
+    if (m & 4) ufb[2 * fd.nv + v] += s2;
   }
-  if (m & 1) uf[v] += s0;
-  if (m & 2) uf[fd.nv + v] += s1;
-  if (m & 4) uf[2 * fd.nv + v] += s2;
 }
 
 template <typename T>
 void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
                      T* fc, int nb) {
-  if (coarse.factor == 4)
-    k_restrict<T, 4><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
-  else
+  if (coarse.factor == 4) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+      cudaFuncSetAttribute(k_restrict4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)restrict4_smem<T>());
+    });
+    const int nbx = (coarse.vx + R4X - 1) / R4X, nby = (coarse.vy + R4Y - 1) / R4Y;
+    k_restrict4<T><<<dim3(nbx * nby, (coarse.vz + R4Z - 1) / R4Z, nb), R4_THREADS, restrict4_smem<T>(), s>>>(
+        fine, coarse, rf, fc, nbx);
+  } else {
     k_restrict<T, 2><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
+  }
 }
 
 template <typename T>
 void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* uc,
                     T* uf, const uint8_t* vmask_fine, int nb) {
+  const dim3 grid((fine.vx + 63) / 64, (fine.vy + 3) / 4, fine.vz), block(64, 4);
   if (coarse.factor == 4)
-    k_prolong<T, 4><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
+    k_prolong<T, 4><<<grid, block, 0, s>>>(fine, coarse, uc, uf, vmask_fine, nb);
   else
-    k_prolong<T, 2><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
+    k_prolong<T, 2><<<grid, block, 0, s>>>(fine, coarse, uc, uf, vmask_fine, nb);
 }
 
 // ---------------------------------------------------------------------------
@@ -648,31 +735,18 @@ __global__ void k_gauss_jordan(int n, double* A, int* status) {
 //   A[i,c] = D^-1 | P | -C D^-1 | A[i,c] - C[i,:] P[:,c]
 // for (i in K, c in K) | (i in K) | (c in K) | otherwise.  Three grid barriers
 // per panel instead of two per pivot.
-//
-// G is the arithmetic of the panels and updates: double, or double-float (df,
-// about 48-bit significands on the FP32 pipe, which has 58x the FP64 rate on
-// GB300).  The matrix stays FP64 in global memory either way; pivots and their
-// reciprocals are taken in FP64.  The double-float form serves the inverse of a
-// coarsest matrix assembled from FP32 stencils, whose entries carry 24 bits.
 constexpr int GJB = 32;
 
-__device__ __forceinline__ double gj_from(double v, double) { return v; }
-__device__ __forceinline__ df gj_from(double v, df) { return df_from(v); }
-__device__ __forceinline__ double gj_to(double v) { return v; }
-__device__ __forceinline__ double gj_to(df v) { return df_to(v); }
-
-template <typename G>
-__global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ A, G* __restrict__ work,
+__global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ A, double* __restrict__ work,
                                                     int* __restrict__ status) {
   cg::grid_group grid = cg::this_grid();
-  __shared__ G sd[GJB][GJB + 1];
-  __shared__ G sc[GJB][GJB + 1];
-  __shared__ G sp[GJB][GJB + 1];
+  __shared__ double sd[GJB][GJB + 1];
+  __shared__ double sc[GJB][GJB + 1];
+  __shared__ double sp[GJB][GJB + 1];
   __shared__ int sflag;
-  const G zero = gj_from(0.0, G());
-  G* Dg = work;                 // [GJB][GJB]
-  G* P = work + GJB * GJB;      // [GJB][n]
-  G* Cp = P + (int64_t)GJB * n; // [n][GJB]
+  double* Dg = work;                 // [GJB][GJB]
+  double* P = work + GJB * GJB;      // [GJB][n]
+  double* Cp = P + (int64_t)GJB * n; // [n][GJB]
   const int tid = threadIdx.x;
   double dmax = 0.0;
   for (int k = 0; k < n; ++k) dmax = fmax(dmax, fabs(A[(int64_t)k * n + k]));
@@ -684,12 +758,12 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
     if (blockIdx.x == 0) {
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        sd[r][c] = (r < kb && c < kb) ? gj_from(A[(int64_t)(k0 + r) * n + k0 + c], G()) : zero;
+        sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
       }
       if (tid == 0) sflag = 0;
       __syncthreads();
       for (int j = 0; j < kb; ++j) {
-        const double p = gj_to(sd[j][j]);
+        const double p = sd[j][j];
         if (p < -tol) {
           if (tid == 0) { status[1] = k0 + j + 1; sflag = 1; }
           break;
@@ -697,22 +771,22 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         __syncthreads();
         if (p <= tol) {  // drop DOF k0 + j
           for (int e = tid; e < 2 * GJB; e += blockDim.x) {
-            if (e < GJB) sd[j][e] = zero;
-            else sd[e - GJB][j] = zero;
+            if (e < GJB) sd[j][e] = 0.0;
+            else sd[e - GJB][j] = 0.0;
           }
           if (tid == 0) status[0] += 1;
           __syncthreads();
           continue;
         }
-        const G rp = gj_from(1.0 / p, G());
+        const double rp = 1.0 / p;
         for (int e = tid; e < kb * kb; e += blockDim.x) {
           const int r = e / kb, c = e % kb;
-          if (r != j && c != j) sd[r][c] = sd[r][c] - sd[r][j] * sd[j][c] * rp;
+          if (r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
         }
         __syncthreads();
         for (int e = tid; e < 2 * kb; e += blockDim.x) {
-          if (e < kb) { if (e != j) sd[j][e] = sd[j][e] * rp; else sd[j][j] = rp; }
-          else { const int r = e - kb; if (r != j) sd[r][j] = zero - sd[r][j] * rp; }
+          if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
+          else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
         }
         __syncthreads();
       }
@@ -725,14 +799,14 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid, gs = (int64_t)gridDim.x * blockDim.x;
     for (int64_t e = gt; e < (int64_t)kb * n; e += gs) {
       const int r = (int)(e / n), c = (int)(e % n);
-      G v = zero;
+      double v = 0.0;
       if (c < k0 || c >= k0 + kb)
-        for (int m = 0; m < kb; ++m) v = v + Dg[r * GJB + m] * gj_from(A[(int64_t)(k0 + m) * n + c], G());
+        for (int m = 0; m < kb; ++m) v += Dg[r * GJB + m] * A[(int64_t)(k0 + m) * n + c];
       P[(int64_t)r * n + c] = v;
     }
     for (int64_t e = gt; e < (int64_t)n * kb; e += gs) {
       const int i = (int)(e / kb), m = (int)(e % kb);
-      Cp[(int64_t)i * GJB + m] = (i < k0 || i >= k0 + kb) ? gj_from(A[(int64_t)i * n + k0 + m], G()) : zero;
+      Cp[(int64_t)i * GJB + m] = (i < k0 || i >= k0 + kb) ? A[(int64_t)i * n + k0 + m] : 0.0;
     }
     grid.sync();
     // ---- C: rank-kb update, GJB x GJB tiles of A per CTA iteration
@@ -741,8 +815,8 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
       __syncthreads();
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : zero;
-        sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : zero;
+        sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : 0.0;
+        sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : 0.0;
         sd[r][c] = Dg[r * GJB + c];
       }
       __syncthreads();
@@ -753,17 +827,17 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         const bool iK = i >= k0 && i < k0 + kb, cK = col >= k0 && col < k0 + kb;
         double& a = A[(int64_t)i * n + col];
         if (iK && cK) {
-          a = gj_to(sd[i - k0][col - k0]);
+          a = sd[i - k0][col - k0];
         } else if (iK) {
-          a = gj_to(sp[i - k0][c]);
+          a = sp[i - k0][c];
         } else if (cK) {
-          G v = zero;
-          for (int m = 0; m < kb; ++m) v = v + sc[r][m] * sd[m][col - k0];
-          a = -gj_to(v);
+          double v = 0.0;
+          for (int m = 0; m < kb; ++m) v += sc[r][m] * sd[m][col - k0];
+          a = -v;
         } else {
-          G v = gj_from(a, G());
-          for (int m = 0; m < kb; ++m) v = v - sc[r][m] * sp[m][c];
-          a = gj_to(v);
+          double v = a;
+          for (int m = 0; m < kb; ++m) v -= sc[r][m] * sp[m][c];
+          a = v;
         }
       }
     }
@@ -837,21 +911,19 @@ void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double*
   k_symmetrize<<<nblk(n * n, 256), 256, 0, s>>>((int)n, A);
 }
 
-int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev, bool df_arith) {
+int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int threads = 256;
   if (work) {  // blocked form: GJB-pivot panels, rank-GJB updates
-    static_assert(sizeof(df) == sizeof(double), "the work array holds either type");
-    void* fn = df_arith ? (void*)k_gj_blocked<df> : (void*)k_gj_blocked<double>;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_blocked, threads, 0);
     if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
     const int tiles = ((n + GJB - 1) / GJB) * ((n + GJB - 1) / GJB);
     const int blocks = std::max(1, std::min(tiles, nsm * std::min(per_sm, 2)));
     cudaMemsetAsync(status_dev, 0, 2 * sizeof(int), s);
     void* args[] = {&n, &A, &work, &status_dev};
-    return (int)cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
+    return (int)cudaLaunchCooperativeKernel((void*)k_gj_blocked, dim3(blocks), dim3(threads), args, 0, s);
   }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gauss_jordan, threads, 0);
   if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;

@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
 // once per plane, so the only FP64 instructions left are about eight
 // conversions per vertex; the element operator runs on the FP32 pipe.
 template <int TXE, int TYE, int MODE>
-__global__ void __launch_bounds__(TXE* TYE, 2) k_fine_modal_df(LevelDims d, const double* __restrict__ rhop,
+__global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const double* __restrict__ rhop,
                                                             const uint8_t* __restrict__ vmask,
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ f, double* __restrict__ out,
@@ -510,54 +510,22 @@ __global__ void __launch_bounds__(TXE* TYE, 2) k_fine_modal_df(LevelDims d, cons
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
   const int zend = min(z0 + TZ, d.vz);
   df acc0(0), acc1(0), acc2(0);
-  // plane slots of this thread and their in-plane offsets (-1 outside)
-  constexpr int KS = (NP + NT - 1) / NT;
-  int pxy[KS];
-#pragma unroll
-  for (int s = 0; s < KS; ++s) {
-    const int k = t + s * NT, px = k % PX, py = k / PX;
-    const int vx = x0 - 1 + px, vy = y0 - 1 + py;
-    pxy[s] = (k < NP && vx >= 0 && vy >= 0 && vx < d.vx && vy < d.vy) ? vx + d.vx * vy : -1;
-  }
-  const int64_t plane_n = (int64_t)d.vx * d.vy;
   auto prefetch = [&](int z) {
     if (z <= zend) {
       Vec4<df>* dst = sm.plane[(z + 3) % 3];
-      const bool zok = z >= 0 && z < d.vz;
-      const int64_t zoff = (int64_t)z * plane_n;
-#pragma unroll
-      for (int s = 0; s < KS; ++s) {
-        const int k = t + s * NT;
-        if (k < NP) {
-          const bool ok = zok && pxy[s] >= 0;
-          const int64_t v = ok ? zoff + pxy[s] : 0;
-          double* raw = reinterpret_cast<double*>(&dst[k]);
-          cp_async_8(raw, u + v, ok);
-          cp_async_8(raw + 1, u + nv + v, ok);
-          cp_async_8(raw + 2, u + 2 * nv + v, ok);
-        }
+      for (int k = t; k < NP; k += NT) {
+        const int px = k % PX, py = k / PX;
+        const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+        const bool ok = vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz;
+        const int64_t v = ok ? vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z) : 0;
+        double* raw = reinterpret_cast<double*>(&dst[k]);
+        cp_async_8(raw, u + v, ok);
+        cp_async_8(raw + 1, u + nv + v, ok);
+        cp_async_8(raw + 2, u + 2 * nv + v, ok);
       }
     }
     cp_async_commit();
   };
-  // per-layer operands one layer ahead (element rho^p, owned vertex's mask and load)
-  const int pex = gx - 1, pey = gy - 1;
-  const bool pe_xy = pex >= 0 && pey >= 0 && pex < d.ex && pey < d.ey;
-  auto load_pe = [&](int ez) -> double {
-    return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (int64_t)d.ex * (pey + (int64_t)d.ey * ez)] : 0.0;
-  };
-  uint8_t vm_n = 0;
-  double f_n[3] = {0.0, 0.0, 0.0};
-  auto load_vertex = [&](int z) {
-    if (!own || z < z0 || z >= zend) return;
-    const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * z);
-    vm_n = vmask[v];
-    if (MODE == 1) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) f_n[c] = f[c * nv + v];
-    }
-  };
-  double pe_n = load_pe(z0 - 1);
   // split plane z's doubles into (hi, lo) pairs in place
   auto convert = [&](int z) {
     if (z > zend) return;
@@ -574,20 +542,16 @@ __global__ void __launch_bounds__(TXE* TYE, 2) k_fine_modal_df(LevelDims d, cons
   prefetch(z0);
   for (int ez = z0 - 1; ez < zend; ++ez) {
     prefetch(ez + 2);
-    const double pe_d = pe_n;
-    const uint8_t vm_c = vm_n;
-    double f_c[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) f_c[c] = f_n[c];
-    if (ez + 1 < zend) pe_n = load_pe(ez + 1);
-    load_vertex(ez + 1);
     cp_async_wait1();
     __syncthreads();
     if (ez == z0 - 1) convert(ez);
     convert(ez + 1);
     __syncthreads();
     {
-      const df pe = df_from(pe_d);
+      const int ex = gx - 1, ey = gy - 1;
+      df pe(0);
+      if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
+        pe = df_from(rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)]);
       if (pe != df(0)) {
         df c[3][8];
 #pragma unroll
@@ -618,13 +582,13 @@ __global__ void __launch_bounds__(TXE* TYE, 2) k_fine_modal_df(LevelDims d, cons
       }
       if (ez >= z0) {
         const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
-        const uint8_t m = vm_c;
+        const uint8_t m = vmask[v];
         const double y[3] = {df_to(b0), df_to(b1), df_to(b2)};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const bool fr = (m >> c) & 1;
           const int64_t idx = c * nv + v;
-          out[idx] = MODE == 1 ? (fr ? f_c[c] - y[c] : 0.0) : (fr ? y[c] : 0.0);
+          out[idx] = MODE == 1 ? (fr ? f[idx] - y[c] : 0.0) : (fr ? y[c] : 0.0);
         }
       }
       acc0 = t0; acc1 = t1; acc2 = t2;

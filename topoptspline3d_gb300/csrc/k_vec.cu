@@ -187,14 +187,40 @@ void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T*
 
 // The same update fused with the new residual's squared norm: per-thread sums
 // in the vectors' precision, combined in FP64 in a fixed order (deterministic).
+// Each thread moves 16-byte packs (4 floats / 2 doubles) so enough bytes are in
+// flight to stream at HBM bandwidth; the tail past the last whole pack is scalar.
+template <typename T, int W>
+struct alignas(16) Pack16 {
+  T v[W];
+};
+
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_rr(T* __restrict__ x, T* __restrict__ r,
                                                                T* __restrict__ rold, const T* __restrict__ d,
                                                                const T* __restrict__ q, const double* __restrict__ sc,
-                                                               int alpha_slot, int64_t n, double* __restrict__ partial) {
+                                                               int alpha_slot, int64_t n, double* __restrict__ partial,
+                                                               int packed) {
+  constexpr int W = 16 / sizeof(T);
+  using P = Pack16<T, W>;
   const T alpha = (T)sc[alpha_slot];
   T acc = T(0);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
+  const int64_t npk = packed ? n / W : 0;
+  for (int64_t i = gid; i < npk; i += gs) {
+    const P rp = reinterpret_cast<const P*>(r)[i], xp = reinterpret_cast<const P*>(x)[i];
+    const P dp = reinterpret_cast<const P*>(d)[i], qp = reinterpret_cast<const P*>(q)[i];
+    P xn, rn;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      xn.v[k] = xp.v[k] + alpha * dp.v[k];
+      rn.v[k] = rp.v[k] - alpha * qp.v[k];
+      acc += rn.v[k] * rn.v[k];
+    }
+    reinterpret_cast<P*>(rold)[i] = rp;
+    reinterpret_cast<P*>(x)[i] = xn;
+    reinterpret_cast<P*>(r)[i] = rn;
+  }
+  for (int64_t i = npk * W + gid; i < n; i += gs) {
     const T ri = r[i];
     rold[i] = ri;
     x[i] = x[i] + alpha * d[i];
@@ -209,8 +235,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_rr(T* __restrict__ x
 template <typename T>
 void launch_pcg_update_rr(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
                           int alpha_slot, int64_t n, double* partial, double* rr) {
+  // 16-byte packs when all five vectors start on 16-byte boundaries
+  const uintptr_t al = (uintptr_t)x | (uintptr_t)r | (uintptr_t)rold | (uintptr_t)d | (uintptr_t)q;
   const int nb = reduce_blocks(n);
-  k_pcg_update_rr<T><<<nb, RED_THREADS, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n, partial);
+  k_pcg_update_rr<T><<<nb, RED_THREADS, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n, partial, (al & 15) == 0);
   k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, rr);
 }
 

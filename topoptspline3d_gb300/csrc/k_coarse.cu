@@ -165,17 +165,106 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* _
   uout[i] = u[i] + dn;
 }
 
+// Warp-per-vertex forms for the small coarse levels, whose row-per-thread
+// kernels are latency-bound (a thread walks 27 neighbours in sequence while
+// only a few warps per SM are resident): lane k < 27 takes neighbour k, forms
+// its three row contributions from 9 stencil and 3 vector loads, and the warp
+// sums them with shuffles.  One round of independent loads per vertex.  Small
+// levels' stencils stay in L2, so the lanes' scattered stencil reads are cheap.
+constexpr int WV = 8;  // vertices (warps) per 256-thread CTA
+
+template <typename T>
+__device__ __forceinline__ void stencil_warp_rows(const LevelDims& d, const T* __restrict__ st,
+                                                  const T* __restrict__ u, int64_t v, int lane, T o[3]) {
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  o[0] = o[1] = o[2] = T(0);
+  if (lane < 27) {
+    const int nx = x + lane % 3 - 1, ny = y + lane / 3 % 3 - 1, nz = z + lane / 9 - 1;
+    if (nx >= 0 && ny >= 0 && nz >= 0 && nx < d.vx && ny < d.vy && nz < d.vz) {
+      const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz), nv = d.nv;
+      const T u0 = u[n], u1 = u[nv + n], u2 = u[2 * nv + n];
+      const T* sk = st + (int64_t)(lane * 9) * nv + v;
+#pragma unroll
+      for (int row = 0; row < 3; ++row)
+        o[row] = sk[(3 * row) * nv] * u0 + sk[(3 * row + 1) * nv] * u1 + sk[(3 * row + 2) * nv] * u2;
+    }
+  }
+#pragma unroll
+  for (int row = 0; row < 3; ++row)
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) o[row] += __shfl_xor_sync(0xffffffffu, o[row], m);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * WV) k_stencil_apply_warp(LevelDims d, const T* __restrict__ st,
+                                                                const T* __restrict__ u, const T* __restrict__ f,
+                                                                T* __restrict__ out, bool residual) {
+  const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
+  u += bo;
+  if (f) f += bo;
+  out += bo;
+  const int lane = threadIdx.x & 31;
+  const int64_t v = (int64_t)blockIdx.x * WV + (threadIdx.x >> 5);
+  if (v >= d.nv) return;  // whole warp
+  T o[3];
+  stencil_warp_rows<T>(d, st, u, v, lane, o);
+  if (lane < 3) {
+    const int64_t i = lane * d.nv + v;
+    const T ol = lane == 0 ? o[0] : (lane == 1 ? o[1] : o[2]);
+    out[i] = residual ? f[i] - ol : ol;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * WV) k_stencil_cheb_warp(LevelDims d, const T* __restrict__ st,
+                                                               const T* __restrict__ u, const T* __restrict__ f,
+                                                               T* __restrict__ uout, const T* __restrict__ dinv,
+                                                               T* __restrict__ dv, T c_old, T c_new, bool first) {
+  const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
+  u += bo;
+  f += bo;
+  uout += bo;
+  dv += bo;
+  const int lane = threadIdx.x & 31;
+  const int64_t v = (int64_t)blockIdx.x * WV + (threadIdx.x >> 5);
+  if (v >= d.nv) return;  // whole warp
+  T o[3];
+  stencil_warp_rows<T>(d, st, u, v, lane, o);
+  if (lane < 3) {
+    const int64_t nv = d.nv;
+    const T r0 = f[v] - o[0], r1 = f[nv + v] - o[1], r2 = f[2 * nv + v] - o[2];
+    const T zz = dinv[(3 * lane) * nv + v] * r0 + dinv[(3 * lane + 1) * nv + v] * r1 +
+                 dinv[(3 * lane + 2) * nv + v] * r2;
+    const int64_t i = lane * nv + v;
+    const T dn = first ? c_new * zz : c_old * dv[i] + c_new * zz;
+    dv[i] = dn;
+    uout[i] = u[i] + dn;
+  }
+}
+
+// Levels with fewer vertices than this use the warp-per-vertex kernels.
+constexpr int64_t STENCIL_WARP_MAX_NV = 32768;
+
 template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
                           T* out, bool residual, int nb) {
-  k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
+  if (d.nv < STENCIL_WARP_MAX_NV)
+    k_stencil_apply_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, out, residual);
+  else
+    k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
 }
 
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb) {
-  k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
-                                                                (T)c_new, first);
+  if (d.nv < STENCIL_WARP_MAX_NV)
+    k_stencil_cheb_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
+                                                                         (T)c_new, first);
+  else
+    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
+                                                                  (T)c_new, first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,

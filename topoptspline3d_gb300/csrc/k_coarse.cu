@@ -365,24 +365,34 @@ __global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
 
 // Restriction by a factor of 4, separably: a CTA owns CX x CY coarse vertices
 // (one thread each) over CZ coarse planes and marches over the fine planes of
-// their support.  Per fine plane it stages the (4 CX + 3) x (4 CY + 3) region
-// in shared memory (zero outside the domain), applies the 7-tap weights
-// 1 2 3 4 3 2 1 along x and then y, and adds the result with the z weight to
-// the coarse planes it touches.  The fine residual is read about 1.3 times
-// instead of through 343 scattered loads per coarse vertex.
+// their support.  Fine planes of the (4 CX + 3) x (4 CY + 3) region arrive by
+// cp.async one plane ahead into a 2-slot ring (zero fill outside the domain);
+// per plane the CTA applies the 7-tap weights 1 2 3 4 3 2 1 along x and then
+// y in shared memory, and each thread adds its result with the z weight to the
+// coarse planes it touches.  The fine residual is read about 1.3 times instead
+// of through 343 scattered loads per coarse vertex.
 constexpr int R4X = 16, R4Y = 8, R4Z = 4, R4FX = 4 * R4X + 3, R4FY = 4 * R4Y + 3;
-constexpr int R4_THREADS = R4X * R4Y;
+constexpr int R4_THREADS = R4X * R4Y, R4_PLANE = 3 * R4FY * R4FX;
 
 template <typename T>
-constexpr size_t restrict4_smem() { return sizeof(T) * 3 * R4FY * (R4FX + R4X); }
+constexpr size_t restrict4_smem() { return sizeof(T) * (2 * R4_PLANE + 3 * R4FY * R4X); }
+
+template <typename T>
+__device__ __forceinline__ void r4_copy(T* smem, const T* gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 4 : 0));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 8 : 0));
+}
 
 template <typename T>
 __global__ void __launch_bounds__(R4_THREADS) k_restrict4(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
                                                           T* __restrict__ fc, int nbx) {
   extern __shared__ __align__(16) unsigned char r4_smem[];
-  T* sp = reinterpret_cast<T*>(r4_smem);  // [3][R4FY][R4FX] fine plane region
-  T* tx = sp + 3 * R4FY * R4FX;           // [3][R4FY][R4X] after the x pass
-  rf += (int64_t)blockIdx.z * 3 * fd.nv;  // right-hand side of the batch
+  T* ring = reinterpret_cast<T*>(r4_smem);  // 2 x [3][R4FY][R4FX] fine plane regions
+  T* tx = ring + 2 * R4_PLANE;              // [3][R4FY][R4X] after the x pass
+  rf += (int64_t)blockIdx.z * 3 * fd.nv;    // right-hand side of the batch
   fc += (int64_t)blockIdx.z * 3 * cd.nv;
   const int cx0 = (blockIdx.x % nbx) * R4X, cy0 = (blockIdx.x / nbx) * R4Y, cz0 = blockIdx.y * R4Z;
   const int t = threadIdx.x, lx = t % R4X, ly = t / R4X;
@@ -391,18 +401,25 @@ __global__ void __launch_bounds__(R4_THREADS) k_restrict4(LevelDims fd, LevelDim
 #pragma unroll
   for (int k = 0; k < R4Z; ++k) acc[k][0] = acc[k][1] = acc[k][2] = T(0);
   const int fz_lo = max(0, 4 * cz0 - 3), fz_hi = min(fd.vz - 1, 4 * (cz0 + R4Z - 1) + 3);
-  for (int fz = fz_lo; fz <= fz_hi; ++fz) {
-    __syncthreads();  // the previous plane's readers are done
-    const int64_t zoff = (int64_t)fd.vx * fd.vy * fz;
-#pragma unroll 4
-    for (int k = t; k < 3 * R4FY * R4FX; k += R4_THREADS) {
-      const int c = k / (R4FY * R4FX), r = k - c * (R4FY * R4FX), yy = r / R4FX, xx = r - yy * R4FX;
-      const int fx = fx0 + xx, fy = fy0 + yy;
-      T v = T(0);
-      if (fx >= 0 && fy >= 0 && fx < fd.vx && fy < fd.vy) v = rf[c * fd.nv + zoff + fx + (int64_t)fd.vx * fy];
-      sp[k] = v;
+  auto prefetch = [&](int fz) {
+    if (fz <= fz_hi) {
+      T* dst = ring + (fz & 1) * R4_PLANE;
+      const int64_t zoff = (int64_t)fd.vx * fd.vy * fz;
+      for (int k = t; k < R4_PLANE; k += R4_THREADS) {
+        const int c = k / (R4FY * R4FX), r = k - c * (R4FY * R4FX), yy = r / R4FX, xx = r - yy * R4FX;
+        const int fx = fx0 + xx, fy = fy0 + yy;
+        const bool ok = fx >= 0 && fy >= 0 && fx < fd.vx && fy < fd.vy;
+        r4_copy<T>(dst + k, ok ? rf + c * fd.nv + zoff + fx + (int64_t)fd.vx * fy : rf, ok);
+      }
     }
-    __syncthreads();
+    asm volatile("cp.async.commit_group;\n" ::);
+  };
+  prefetch(fz_lo);
+  for (int fz = fz_lo; fz <= fz_hi; ++fz) {
+    prefetch(fz + 1);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    __syncthreads();  // plane fz landed; the previous plane's y pass is done with tx
+    const T* sp = ring + (fz & 1) * R4_PLANE;
     for (int k = t; k < 3 * R4FY * R4X; k += R4_THREADS) {
       const int c = k / (R4FY * R4X), r = k - c * (R4FY * R4X), yy = r / R4X, cx = r - yy * R4X;
       const T* row = sp + (c * R4FY + yy) * R4FX + 4 * cx;  // taps dx = -3..3
@@ -426,6 +443,7 @@ __global__ void __launch_bounds__(R4_THREADS) k_restrict4(LevelDims fd, LevelDim
       }
     }
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   const int cx = cx0 + lx, cy = cy0 + ly;
   if (cx >= cd.vx || cy >= cd.vy) return;
   const T inv = T(1) / T(64);
@@ -439,39 +457,46 @@ __global__ void __launch_bounds__(R4_THREADS) k_restrict4(LevelDims fd, LevelDim
   }
 }
 
-// Prolongation: one fine vertex per thread on a (64 x 4) x-y tile of one fine
-// plane (no index division); blockIdx.z is the plane, the batch loops inside.
 template <typename T, int FCT>
-__global__ void __launch_bounds__(256) k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc,
-                                                 T* __restrict__ uf, const uint8_t* __restrict__ vmask, int nb) {
-  const int x = blockIdx.x * 64 + threadIdx.x, y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x >= fd.vx || y >= fd.vy) return;
-  const int64_t v = x + (int64_t)fd.vx * (y + (int64_t)fd.vy * z);
+__global__ void k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc, T* __restrict__ uf,
+                          const uint8_t* __restrict__ vmask) {
+  uc += (int64_t)blockIdx.y * 3 * cd.nv;  // right-hand side of the batch
+  uf += (int64_t)blockIdx.y * 3 * fd.nv;
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= fd.nv) return;
+  int x, y, z;
+  if (fd.nv < (int64_t)1 << 31) {  // 32-bit index arithmetic
+    const unsigned vv = (unsigned)v, vx = (unsigned)fd.vx, vy = (unsigned)fd.vy, tt = vv / vx;
+    x = (int)(vv - tt * vx);
+    y = (int)(tt % vy);
+    z = (int)(tt / vy);
+  } else {
+    x = (int)(v % fd.vx);
+    const int64_t t = v / fd.vx;
+    y = (int)(t % fd.vy);
+    z = (int)(t / fd.vy);
+  }
   const uint8_t m = vmask[v];
   if (!(m & 7) || !(m & 8)) return;
   const int cx = x / FCT, cy = y / FCT, cz = z / FCT;
   const int rx = x % FCT, ry = y % FCT, rz = z % FCT;
+  T s0 = T(0), s1 = T(0), s2 = T(0);
   const T inv = T(1) / T(FCT * FCT * FCT);
-  for (int b = 0; b < nb; ++b) {
-    const T* ucb = uc + (int64_t)b * 3 * cd.nv;
-    T* ufb = uf + (int64_t)b * 3 * fd.nv;
-    T s0 = T(0), s1 = T(0), s2 = T(0);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
-      const int wx = ox ? rx : FCT - rx, wy = oy ? ry : FCT - ry, wz = oz ? rz : FCT - rz;
-      const int wi = wx * wy * wz;
-      if (wi == 0) continue;
-      const T w = T(wi) * inv;
-      const int64_t cv = (cx + ox) + (int64_t)cd.vx * ((cy + oy) + (int64_t)cd.vy * (cz + oz));
-      s0 += w * ucb[cv];
-      s1 += w * ucb[cd.nv + cv];
-      s2 += w * ucb[2 * cd.nv + cv];
-    }
-    if (m & 1) ufb[v] += s0;
-    if (m & 2) ufb[fd.nv + v] += s1;
-    if (m & 4) ufb[2 * fd.nv + v] += s2;
+  for (int k = 0; k < 8; ++k) {
+    const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+    const int wx = ox ? rx : FCT - rx, wy = oy ? ry : FCT - ry, wz = oz ? rz : FCT - rz;
+    const int wi = wx * wy * wz;
+    if (wi == 0) continue;
+    const T w = T(wi) * inv;
+    const int64_t cv = (cx + ox) + (int64_t)cd.vx * ((cy + oy) + (int64_t)cd.vy * (cz + oz));
+    s0 += w * uc[cv];
+    s1 += w * uc[cd.nv + cv];
+    s2 += w * uc[2 * cd.nv + cv];
   }
+  if (m & 1) uf[v] += s0;
+  if (m & 2) uf[fd.nv + v] += s1;
+  if (m & 4) uf[2 * fd.nv + v] += s2;
 }
 
 template <typename T>
@@ -493,11 +518,10 @@ void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coa
 template <typename T>
 void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* uc,
                     T* uf, const uint8_t* vmask_fine, int nb) {
-  const dim3 grid((fine.vx + 63) / 64, (fine.vy + 3) / 4, fine.vz), block(64, 4);
   if (coarse.factor == 4)
-    k_prolong<T, 4><<<grid, block, 0, s>>>(fine, coarse, uc, uf, vmask_fine, nb);
+    k_prolong<T, 4><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
   else
-    k_prolong<T, 2><<<grid, block, 0, s>>>(fine, coarse, uc, uf, vmask_fine, nb);
+    k_prolong<T, 2><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
 }
 
 // ---------------------------------------------------------------------------

@@ -363,97 +363,60 @@ __global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
   fc[v] = s0; fc[cd.nv + v] = s1; fc[2 * cd.nv + v] = s2;
 }
 
-// Restriction by a factor of 4, separably: a CTA owns CX x CY coarse vertices
-// (one thread each) over CZ coarse planes and marches over the fine planes of
-// their support.  Fine planes of the (4 CX + 3) x (4 CY + 3) region arrive by
-// cp.async one plane ahead into a 2-slot ring (zero fill outside the domain);
-// per plane the CTA applies the 7-tap weights 1 2 3 4 3 2 1 along x and then
-// y in shared memory, and each thread adds its result with the z weight to the
-// coarse planes it touches.  The fine residual is read about 1.3 times instead
-// of through 343 scattered loads per coarse vertex.
-constexpr int R4X = 16, R4Y = 8, R4Z = 4, R4FX = 4 * R4X + 3, R4FY = 4 * R4Y + 3;
-constexpr int R4_THREADS = R4X * R4Y, R4_PLANE = 3 * R4FY * R4FX;
+// Restriction by a factor of 4 with the fine z taps split across warps: a CTA
+// of 7 warps covers 32 consecutive coarse vertices; warp w gathers the fine
+// plane z = 4 cz + w - 3 (7 x 7 taps, weights (4 - |d|) per axis) for its lane's
+// vertex, and warp 0 sums the seven partial sums in a fixed order.  Seven
+// times the threads of a vertex-per-thread gather keep the loads in flight.
+constexpr int R4_WARPS = 7;
 
 template <typename T>
-constexpr size_t restrict4_smem() { return sizeof(T) * (2 * R4_PLANE + 3 * R4FY * R4X); }
-
-template <typename T>
-__device__ __forceinline__ void r4_copy(T* smem, const T* gmem, bool valid) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  if (sizeof(T) == 4)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 4 : 0));
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 8 : 0));
-}
-
-template <typename T>
-__global__ void __launch_bounds__(R4_THREADS) k_restrict4(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
-                                                          T* __restrict__ fc, int nbx) {
-  extern __shared__ __align__(16) unsigned char r4_smem[];
-  T* ring = reinterpret_cast<T*>(r4_smem);  // 2 x [3][R4FY][R4FX] fine plane regions
-  T* tx = ring + 2 * R4_PLANE;              // [3][R4FY][R4X] after the x pass
-  rf += (int64_t)blockIdx.z * 3 * fd.nv;    // right-hand side of the batch
-  fc += (int64_t)blockIdx.z * 3 * cd.nv;
-  const int cx0 = (blockIdx.x % nbx) * R4X, cy0 = (blockIdx.x / nbx) * R4Y, cz0 = blockIdx.y * R4Z;
-  const int t = threadIdx.x, lx = t % R4X, ly = t / R4X;
-  const int fx0 = 4 * cx0 - 3, fy0 = 4 * cy0 - 3;
-  T acc[R4Z][3];
+__global__ void __launch_bounds__(32 * R4_WARPS) k_restrict4(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
+                                                             T* __restrict__ fc) {
+  __shared__ T part[R4_WARPS][3][32];
+  rf += (int64_t)blockIdx.y * 3 * fd.nv;  // right-hand side of the batch
+  fc += (int64_t)blockIdx.y * 3 * cd.nv;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t v = (int64_t)blockIdx.x * 32 + lane;
+  T s0 = T(0), s1 = T(0), s2 = T(0);
+  if (v < cd.nv) {
+    const int x = (int)(v % cd.vx);
+    const int64_t t = v / cd.vx;
+    const int y = (int)(t % cd.vy), z = (int)(t / cd.vy);
+    const int dz = w - 3, fz = 4 * z + dz;
+    if (fz >= 0 && fz < fd.vz) {
+      const T wz = T(4 - (dz < 0 ? -dz : dz));
+      for (int dy = -3; dy <= 3; ++dy) {
+        const int fy = 4 * y + dy;
+        if (fy < 0 || fy >= fd.vy) continue;
+        const T wyz = wz * T(4 - (dy < 0 ? -dy : dy));
+        const int64_t rowv = (int64_t)fd.vx * (fy + (int64_t)fd.vy * fz);
 #pragma unroll
-  for (int k = 0; k < R4Z; ++k) acc[k][0] = acc[k][1] = acc[k][2] = T(0);
-  const int fz_lo = max(0, 4 * cz0 - 3), fz_hi = min(fd.vz - 1, 4 * (cz0 + R4Z - 1) + 3);
-  auto prefetch = [&](int fz) {
-    if (fz <= fz_hi) {
-      T* dst = ring + (fz & 1) * R4_PLANE;
-      const int64_t zoff = (int64_t)fd.vx * fd.vy * fz;
-      for (int k = t; k < R4_PLANE; k += R4_THREADS) {
-        const int c = k / (R4FY * R4FX), r = k - c * (R4FY * R4FX), yy = r / R4FX, xx = r - yy * R4FX;
-        const int fx = fx0 + xx, fy = fy0 + yy;
-        const bool ok = fx >= 0 && fy >= 0 && fx < fd.vx && fy < fd.vy;
-        r4_copy<T>(dst + k, ok ? rf + c * fd.nv + zoff + fx + (int64_t)fd.vx * fy : rf, ok);
-      }
-    }
-    asm volatile("cp.async.commit_group;\n" ::);
-  };
-  prefetch(fz_lo);
-  for (int fz = fz_lo; fz <= fz_hi; ++fz) {
-    prefetch(fz + 1);
-    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-    __syncthreads();  // plane fz landed; the previous plane's y pass is done with tx
-    const T* sp = ring + (fz & 1) * R4_PLANE;
-    for (int k = t; k < 3 * R4FY * R4X; k += R4_THREADS) {
-      const int c = k / (R4FY * R4X), r = k - c * (R4FY * R4X), yy = r / R4X, cx = r - yy * R4X;
-      const T* row = sp + (c * R4FY + yy) * R4FX + 4 * cx;  // taps dx = -3..3
-      tx[k] = (row[0] + row[6]) + T(2) * (row[1] + row[5]) + T(3) * (row[2] + row[4]) + T(4) * row[3];
-    }
-    __syncthreads();
-    T p[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const T* col = tx + (c * R4FY + 4 * ly) * R4X + lx;  // taps dy = -3..3
-      p[c] = (col[0] + col[6 * R4X]) + T(2) * (col[R4X] + col[5 * R4X]) + T(3) * (col[2 * R4X] + col[4 * R4X]) +
-             T(4) * col[3 * R4X];
-    }
-#pragma unroll
-    for (int k = 0; k < R4Z; ++k) {
-      const int dz = fz - 4 * (cz0 + k), ad = dz < 0 ? -dz : dz;
-      if (ad <= 3) {
-        const T w = T(4 - ad);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) acc[k][c] += w * p[c];
+        for (int dx = -3; dx <= 3; ++dx) {
+          const int fx = 4 * x + dx;
+          if (fx < 0 || fx >= fd.vx) continue;
+          const T wt = wyz * T(4 - (dx < 0 ? -dx : dx));
+          const int64_t fv = rowv + fx;
+          s0 += wt * rf[fv];
+          s1 += wt * rf[fd.nv + fv];
+          s2 += wt * rf[2 * fd.nv + fv];
+        }
       }
     }
   }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-  const int cx = cx0 + lx, cy = cy0 + ly;
-  if (cx >= cd.vx || cy >= cd.vy) return;
-  const T inv = T(1) / T(64);
+  part[w][0][lane] = s0;
+  part[w][1][lane] = s1;
+  part[w][2][lane] = s2;
+  __syncthreads();
+  if (w == 0 && v < cd.nv) {
+    const T inv = T(1) / T(64);
 #pragma unroll
-  for (int k = 0; k < R4Z; ++k) {
-    const int cz = cz0 + k;
-    if (cz >= cd.vz) break;
-    const int64_t cv = cx + (int64_t)cd.vx * (cy + (int64_t)cd.vy * cz);
+    for (int c = 0; c < 3; ++c) {
+      T a = T(0);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) fc[c * cd.nv + cv] = acc[k][c] * inv;
+      for (int k = 0; k < R4_WARPS; ++k) a += part[k][c][lane];
+      fc[c * cd.nv + v] = a * inv;
+    }
   }
 }
 
@@ -503,13 +466,7 @@ template <typename T>
 void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
                      T* fc, int nb) {
   if (coarse.factor == 4) {
-    static std::once_flag once;
-    std::call_once(once, [] {
-      cudaFuncSetAttribute(k_restrict4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)restrict4_smem<T>());
-    });
-    const int nbx = (coarse.vx + R4X - 1) / R4X, nby = (coarse.vy + R4Y - 1) / R4Y;
-    k_restrict4<T><<<dim3(nbx * nby, (coarse.vz + R4Z - 1) / R4Z, nb), R4_THREADS, restrict4_smem<T>(), s>>>(
-        fine, coarse, rf, fc, nbx);
+    k_restrict4<T><<<dim3(nblk(coarse.nv, 32), nb), 32 * R4_WARPS, 0, s>>>(fine, coarse, rf, fc);
   } else {
     k_restrict<T, 2><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
   }

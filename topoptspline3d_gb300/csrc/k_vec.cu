@@ -1,10 +1,17 @@
 // Vector kernels: deterministic two-pass FP64 reductions, axpy-type updates
 // and the Chebyshev smoothing step.
+#include <algorithm>
+
 #include "topo_internal.h"
 
 namespace topo {
 
 constexpr int RED_THREADS = 256;
+
+template <typename T, int W>
+struct alignas(16) Pack16 {
+  T v[W];
+};
 constexpr int RED_MAX_BLOCKS = 1024;
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -151,18 +158,34 @@ void launch_scalar_ratio(cudaStream_t s, double* sc, int num, int sub, int den, 
 // d = z + beta d (beta = sc[beta_slot]), or d = z.
 template <typename T>
 __global__ void k_pcg_dir(const T* __restrict__ z, T* __restrict__ d, const double* __restrict__ sc,
-                          int beta_slot, bool first, int64_t n) {
+                          int beta_slot, bool first, int64_t n, int packed) {
+  constexpr int W = 16 / sizeof(T);
+  using P = Pack16<T, W>;
+  const T beta = first ? T(0) : (T)sc[beta_slot];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (first) { d[i] = z[i]; return; }
-  const T beta = (T)sc[beta_slot];
-  d[i] = z[i] + beta * d[i];
+  const int64_t npk = packed ? n / W : 0;
+  if (i < npk) {
+    const P zp = reinterpret_cast<const P*>(z)[i];
+    P dp = first ? zp : reinterpret_cast<const P*>(d)[i];
+    if (!first) {
+#pragma unroll
+      for (int k = 0; k < W; ++k) dp.v[k] = zp.v[k] + beta * dp.v[k];
+    }
+    reinterpret_cast<P*>(d)[i] = dp;
+  }
+  // scalar elements: the tail past the last pack, or all of them unpacked
+  const int64_t j = packed ? npk * W + i : i;
+  if ((!packed || i < W) && j < n) d[j] = first ? z[j] : z[j] + beta * d[j];
 }
 
+// d = z (first) or z + beta d, in 16-byte packs when both vectors are aligned
 template <typename T>
 void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta_slot, bool first,
                     int64_t n) {
-  k_pcg_dir<T><<<nblk(n, 256), 256, 0, s>>>(z, d, sc, beta_slot, first, n);
+  constexpr int W = 16 / sizeof(T);
+  const bool packed = (((uintptr_t)z | (uintptr_t)d) & 15) == 0;
+  const int64_t threads = packed ? std::max<int64_t>(n / W, W) : n;
+  k_pcg_dir<T><<<nblk(threads, 256), 256, 0, s>>>(z, d, sc, beta_slot, first, n, packed ? 1 : 0);
 }
 
 // alpha = sc[alpha_slot]; rold = r; x += alpha d; r -= alpha q.
@@ -189,10 +212,6 @@ void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T*
 // in the vectors' precision, combined in FP64 in a fixed order (deterministic).
 // Each thread moves 16-byte packs (4 floats / 2 doubles) so enough bytes are in
 // flight to stream at HBM bandwidth; the tail past the last whole pack is scalar.
-template <typename T, int W>
-struct alignas(16) Pack16 {
-  T v[W];
-};
 
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_rr(T* __restrict__ x, T* __restrict__ r,

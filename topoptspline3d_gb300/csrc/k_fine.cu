@@ -488,13 +488,26 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
 // cp.async and are split in place into (hi, lo) float pairs (the same 8 bytes)
 // once per plane, so the only FP64 instructions left are about eight
 // conversions per vertex; the element operator runs on the FP32 pipe.
+// Shared memory of the double-float kernel.  High and low parts live in
+// separate 16-byte arrays, so each lane's access is one contiguous 16 bytes and
+// a warp's access touches the minimum of banks (a 32-byte (hi, lo) entry per
+// lane made every access take twice the wavefronts).  Vertex planes arrive as
+// doubles in a 3-slot staging ring and are split into two converted slots.
+template <int TXE, int TYE>
+struct DfSmem {
+  static constexpr int NT = TXE * TYE, PX = TXE + 1, PY = TYE + 1, NP = PX * PY;
+  float4 phi[2][NP], plo[2][NP];  // converted planes: (u0, u1, u2) high / low parts
+  float4 fhi[8][NT], flo[8][NT];  // nodal forces of the layer's elements, high / low parts
+  double raw[3][3][NP];           // cp.async staging: [slot][component][vertex]
+};
+
 template <int TXE, int TYE, int MODE>
 __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const double* __restrict__ rhop,
                                                             const uint8_t* __restrict__ vmask,
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ f, double* __restrict__ out,
                                                             int TZ) {
-  using S = ModalSmem<df, TXE, TYE>;
+  using S = DfSmem<TXE, TYE>;
   constexpr int NT = S::NT, PX = S::PX, NP = S::NP;
   extern __shared__ __align__(32) unsigned char modal_smem[];
   S& sm = *reinterpret_cast<S*>(modal_smem);
@@ -512,30 +525,28 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
   df acc0(0), acc1(0), acc2(0);
   auto prefetch = [&](int z) {
     if (z <= zend) {
-      Vec4<df>* dst = sm.plane[(z + 3) % 3];
+      double (*dst)[NP] = sm.raw[(z + 3) % 3];
       for (int k = t; k < NP; k += NT) {
         const int px = k % PX, py = k / PX;
         const int vx = x0 - 1 + px, vy = y0 - 1 + py;
         const bool ok = vx >= 0 && vy >= 0 && z >= 0 && vx < d.vx && vy < d.vy && z < d.vz;
         const int64_t v = ok ? vx + (int64_t)d.vx * (vy + (int64_t)d.vy * z) : 0;
-        double* raw = reinterpret_cast<double*>(&dst[k]);
-        cp_async_8(raw, u + v, ok);
-        cp_async_8(raw + 1, u + nv + v, ok);
-        cp_async_8(raw + 2, u + 2 * nv + v, ok);
+        cp_async_8(&dst[0][k], u + v, ok);
+        cp_async_8(&dst[1][k], u + nv + v, ok);
+        cp_async_8(&dst[2][k], u + 2 * nv + v, ok);
       }
     }
     cp_async_commit();
   };
-  // split plane z's doubles into (hi, lo) pairs in place
+  // split staged plane z's doubles into high and low parts (converted slot (z + 2) & 1)
   auto convert = [&](int z) {
     if (z > zend) return;
-    Vec4<df>* p = sm.plane[(z + 3) % 3];
+    const double (*src)[NP] = sm.raw[(z + 3) % 3];
+    const int cs = (z + 2) & 1;
     for (int k = t; k < NP; k += NT) {
-      const double* raw = reinterpret_cast<const double*>(&p[k]);
-      const double a = raw[0], b = raw[1], c = raw[2];
-      p[k].x = df_from(a);
-      p[k].y = df_from(b);
-      p[k].z = df_from(c);
+      const df a = df_from(src[0][k]), b = df_from(src[1][k]), c = df_from(src[2][k]);
+      sm.phi[cs][k] = make_float4(a.hi, b.hi, c.hi, 0.f);
+      sm.plo[cs][k] = make_float4(a.lo, b.lo, c.lo, 0.f);
     }
   };
   prefetch(z0 - 1);
@@ -557,15 +568,22 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
           const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
-          const Vec4<df> p = sm.plane[(ez + (a >> 2) + 3) % 3][k];
-          c[0][a] = p.x; c[1][a] = p.y; c[2][a] = p.z;
+          const int cs = (ez + (a >> 2) + 2) & 1;
+          const float4 h = sm.phi[cs][k], l = sm.plo[cs][k];
+          c[0][a] = df(h.x, l.x); c[1][a] = df(h.y, l.y); c[2][a] = df(h.z, l.z);
         }
         modal_element<df>(c, pe);
 #pragma unroll
-        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<df>{c[0][a], c[1][a], c[2][a], df(0)};
+        for (int a = 0; a < 8; ++a) {
+          sm.fhi[a][t] = make_float4(c[0][a].hi, c[1][a].hi, c[2][a].hi, 0.f);
+          sm.flo[a][t] = make_float4(c[0][a].lo, c[1][a].lo, c[2][a].lo, 0.f);
+        }
       } else {
 #pragma unroll
-        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<df>{df(0), df(0), df(0), df(0)};
+        for (int a = 0; a < 8; ++a) {
+          sm.fhi[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
+          sm.flo[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
       }
     }
     __syncthreads();
@@ -576,9 +594,9 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
         const int wx = w & 1, wy = w >> 1;
         const int te = (i + wx) + TXE * (j + wy);
         const int a = (1 - wx) + 2 * (1 - wy);
-        const Vec4<df> bo = sm.fe[a][te], to = sm.fe[a + 4][te];
-        b0 += bo.x; b1 += bo.y; b2 += bo.z;
-        t0 += to.x; t1 += to.y; t2 += to.z;
+        const float4 bh = sm.fhi[a][te], bl = sm.flo[a][te], th = sm.fhi[a + 4][te], tl = sm.flo[a + 4][te];
+        b0 += df(bh.x, bl.x); b1 += df(bh.y, bl.y); b2 += df(bh.z, bl.z);
+        t0 += df(th.x, tl.x); t1 += df(th.y, tl.y); t2 += df(th.z, tl.z);
       }
       if (ez >= z0) {
         const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
@@ -823,7 +841,7 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
                   ((d.vz + tz - 1) / tz) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
-  const size_t smem = sizeof(ModalSmem<df, MODAL_TXE, MODAL_TYE>);
+  const size_t smem = sizeof(DfSmem<MODAL_TXE, MODAL_TYE>);
   static std::once_flag once;
   std::call_once(once, [smem] {
     cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -1129,7 +1129,9 @@ int topo_update_operators(topo_handle* h) {
     launch_dense_from_stencil(h->stream, Lc.d, st, h->A);
     count_launch(2);
     CKL();
-    int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status);
+    // FP32-only operators: the matrix comes from FP32 stencils; the updates
+    // in double-float keep twice their precision on the FP32 pipe
+    int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status, !b64);
     count_launch();
     if (e != (int)cudaSuccess)
       return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));

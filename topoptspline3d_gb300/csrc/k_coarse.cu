@@ -4,6 +4,7 @@
 
 #include <mutex>
 
+#include "df.cuh"
 #include "topo_internal.h"
 
 namespace cg = cooperative_groups;
@@ -807,10 +808,19 @@ __global__ void k_gauss_jordan(int n, double* A, int* status) {
 // per panel instead of two per pivot.
 constexpr int GJB = 32;
 
+//
+// DFC: the rank-GJB updates of phase C (n^3 of the n^3 + O(n^2 GJB) work) run
+// in double-float arithmetic on the FP32 pipe (58x the FP64 rate on GB300),
+// with the panels split into (hi, lo) floats as a tile is staged; the panel
+// factorisation stays FP64, where its serial latency matters more than its
+// rate.  Used when the coarsest matrix comes from FP32 stencils.
+template <bool DFC>
 __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ A, double* __restrict__ work,
                                                     int* __restrict__ status) {
   cg::grid_group grid = cg::this_grid();
   __shared__ double sd[GJB][GJB + 1];
+  __shared__ df scd[DFC ? GJB : 1][GJB + 1];
+  __shared__ df spd[DFC ? GJB : 1][GJB + 1];
   __shared__ double sc[GJB][GJB + 1];
   __shared__ double sp[GJB][GJB + 1];
   __shared__ int sflag;
@@ -888,6 +898,10 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : 0.0;
         sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : 0.0;
         sd[r][c] = Dg[r * GJB + c];
+        if constexpr (DFC) {
+          scd[r][c] = df_from(sc[r][c]);
+          spd[r][c] = df_from(sp[r][c]);
+        }
       }
       __syncthreads();
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
@@ -904,6 +918,10 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
           double v = 0.0;
           for (int m = 0; m < kb; ++m) v += sc[r][m] * sd[m][col - k0];
           a = -v;
+        } else if constexpr (DFC) {
+          df v = df_from(a);
+          for (int m = 0; m < kb; ++m) v = v - scd[r][m] * spd[m][c];
+          a = df_to(v);
         } else {
           double v = a;
           for (int m = 0; m < kb; ++m) v -= sc[r][m] * sp[m][c];
@@ -981,19 +999,20 @@ void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double*
   k_symmetrize<<<nblk(n * n, 256), 256, 0, s>>>((int)n, A);
 }
 
-int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev) {
+int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev, bool df_update) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int threads = 256;
   if (work) {  // blocked form: GJB-pivot panels, rank-GJB updates
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_blocked, threads, 0);
+    void* fn = df_update ? (void*)k_gj_blocked<true> : (void*)k_gj_blocked<false>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
     if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
     const int tiles = ((n + GJB - 1) / GJB) * ((n + GJB - 1) / GJB);
     const int blocks = std::max(1, std::min(tiles, nsm * std::min(per_sm, 2)));
     cudaMemsetAsync(status_dev, 0, 2 * sizeof(int), s);
     void* args[] = {&n, &A, &work, &status_dev};
-    return (int)cudaLaunchCooperativeKernel((void*)k_gj_blocked, dim3(blocks), dim3(threads), args, 0, s);
+    return (int)cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
   }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gauss_jordan, threads, 0);
   if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;

@@ -225,7 +225,6 @@ struct ModalSmem {
   static constexpr int NT = TXE * TYE, PX = TXE + 1, PY = TYE + 1, NP = PX * PY;
   Vec4<T> plane[3][NP];  // vertex planes (u0, u1, u2, -) in a 3-slot ring
   Vec4<T> fe[8][NT];     // nodal forces of the layer's elements, per local node
-  T pe[NT];              // rho^p of the layer's elements (FP32 smoother diagonal)
 };
 
 // z = S^-1 r for the free-DOF part of a symmetric 3x3 block S (fixed rows and
@@ -253,17 +252,16 @@ __device__ __forceinline__ void block_solve_free(const T S_in[9], uint8_t fb, co
     if (!((fb >> i) & 1)) z[i] = T(0);
 }
 
-// Build-time choices for the FP32 variants, measured on GB300 (half-MBB
+// Build-time choices for the FP32 kernel, measured on GB300 (half-MBB
 // 256x128x128, Chebyshev step per launch):
-//  - TOPO_FINE32_STORED_DIAG 1: the Chebyshev step reads the stored FP32
-//    block-Jacobi inverse (36 bytes per vertex) instead of rebuilding the
-//    diagonal blocks from rho^p and solving them (about 150 instructions per
-//    vertex); the kernel is issue-bound, so reading wins: 143 us against 154 us.
+//  - the Chebyshev step reads the stored FP32 block-Jacobi inverse (36 bytes per
+//    vertex); rebuilding the diagonal blocks from rho^p and solving them costs
+//    about 150 instructions per vertex, and the kernel is issue-bound, so
+//    reading wins: 143 us against 154 us (two-barrier form).
 //  - resident threads per SM (launch bounds): 1024 for all three modes (64
-//    registers per thread, no spills with the stored inverse).  With the
-//    rebuilt diagonal the step needs 80 registers and runs best at 768.
-//  - TOPO_MODAL32_TYE 8: element rows of a 32-wide CTA tile.  16 rows halve
-//    the halo overhead but run slower (162 us).
+//    registers per thread, no spills).
+//  - TOPO_MODAL32_TYE 8: element rows (warps) of a 32-wide CTA tile.  16 rows
+//    halve the halo overhead but ran slower (162 us, two-barrier form).
 // FP64 variants ask for 512 resident threads (two 256-thread CTAs, at most
 // 128 registers per thread).
 #ifndef TOPO_FINE32_THREADS_PER_SM
@@ -271,9 +269,6 @@ __device__ __forceinline__ void block_solve_free(const T S_in[9], uint8_t fb, co
 #endif
 #ifndef TOPO_FINE32_CHEB_THREADS_PER_SM
 #define TOPO_FINE32_CHEB_THREADS_PER_SM 1024
-#endif
-#ifndef TOPO_FINE32_STORED_DIAG
-#define TOPO_FINE32_STORED_DIAG 1
 #endif
 #ifndef TOPO_MODAL32_TYE
 #define TOPO_MODAL32_TYE 8
@@ -308,11 +303,6 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
   const int zend = min(z0 + TZ, d.vz);
   T acc0 = T(0), acc1 = T(0), acc2 = T(0);
-  // With TOPO_FINE32_STORED_DIAG 0, FP32 Chebyshev steps rebuild the diagonal
-  // block from rho^p instead of streaming the stored inverse; FP64 steps
-  // always read the stored inverse.
-  constexpr bool FLY_DIAG = (MODE == 2) && (sizeof(T) == 4) && !TOPO_FINE32_STORED_DIAG;
-  T pprev[4] = {T(0), T(0), T(0), T(0)};
   T dsum = T(0);  // MODE 0 with ch.dotp: this thread's share of u.out
   // This thread's plane slots k = t + s NT and their in-plane vertex offsets
   // (-1 outside the domain), fixed for the whole z march.
@@ -404,12 +394,10 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
 #pragma unroll
         for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<T>{T(0), T(0), T(0), T(0)};
       }
-      if (FLY_DIAG) sm.pe[t] = pe;
     }
     __syncthreads();
     if (own) {
       T b0 = acc0, b1 = acc1, b2 = acc2, t0 = T(0), t1 = T(0), t2 = T(0);
-      T pl[4];
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const int wx = w & 1, wy = w >> 1;
@@ -418,7 +406,6 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
         const Vec4<T> bo = sm.fe[a][te], to = sm.fe[a + 4][te];
         b0 += bo.x; b1 += bo.y; b2 += bo.z;
         t0 += to.x; t1 += to.y; t2 += to.z;
-        if (FLY_DIAG) pl[w] = sm.pe[te];
       }
       if (ez >= z0) {
         const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
@@ -442,24 +429,9 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
           for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : T(0);
           const T uv[3] = {uo.x, uo.y, uo.z};
           T zc[3];
-          if (FLY_DIAG) {
-            // diagonal block sum_e rho^p_e Ke[a_e, a_e] from the four in-layer elements
-            // (bottom nodes) and the four of the layer below (top nodes)
-            T S[9];
 #pragma unroll
-            for (int k = 0; k < 9; ++k) S[k] = T(0);
-#pragma unroll
-            for (int w = 0; w < 4; ++w) {
-              const int a = (1 - (w & 1)) + 2 * (1 - (w >> 1));
-#pragma unroll
-              for (int k = 0; k < 9; ++k) S[k] += pl[w] * T(cKdiag32[a][k]) + pprev[w] * T(cKdiag32[a + 4][k]);
-            }
-            block_solve_free<T>(S, (m & 8) ? (m & 7) : 0, r, zc);
-          } else {
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-              zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
-          }
+          for (int c = 0; c < 3; ++c)
+            zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const T dn = ch.first ? T(ch.c_new) * zc[c] : T(ch.c_old) * dv_c[c] + T(ch.c_new) * zc[c];
@@ -469,10 +441,6 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
         }
       }
       acc0 = t0; acc1 = t1; acc2 = t2;
-      if (FLY_DIAG) {
-#pragma unroll
-        for (int w = 0; w < 4; ++w) pprev[w] = pl[w];
-      }
     }
   }
   // drain the (empty) trailing copy groups before the CTA exits
@@ -483,11 +451,217 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 form with one barrier per element layer.  A CTA is TYE warps; lane i of
+// warp j computes element (i, j) of the layer and owns vertex (i, j), the
+// element's (+x, +y) corner.  The element's nodal forces are combined along x
+// with a warp shuffle (vertex column i takes the x = 1 nodes of element i and
+// the x = 0 nodes of element i + 1); the y = 1 half stays in the lane's
+// registers and the y = 0 half (6 floats) goes through a double-buffered
+// shared exchange to warp j - 1.  The owned vertex's sum for plane ez is then
+// formed in the next layer's step, after its single barrier: its own y = 1
+// part, row j + 1's exchanged y = 0 part, and the top-node part carried from
+// the layer below.  Vertex planes sit in a 4-slot ring and only the element
+// phase reads them (the owned vertex's own value is taken into registers
+// there), so the copy issued at the top of a step never lands in a plane that
+// a warp still in the previous step may read.
+// Against the 2-barrier form: a quarter of the shared-memory traffic per
+// element, half the barriers.
+// ---------------------------------------------------------------------------
+template <int TYE>
+struct Modal32Smem {
+  static constexpr int TXE = 32, NT = TXE * TYE, PX = TXE + 1, PY = TYE + 1, NP = PX * PY;
+  float4 plane[4][NP];  // vertex planes (u0, u1, u2, -) in a 4-slot ring
+  float4 xa[2][NT];     // exchanged y = 0 forces: (z = 0: c0, c1, c2; z = 1: c0)
+  float2 xb[2][NT];     //                         (z = 1: c1, c2)
+};
+
+template <int TYE, int MODE>
+__global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ? TOPO_FINE32_CHEB_THREADS_PER_SM
+                                                                               : TOPO_FINE32_THREADS_PER_SM))
+    k_fine_modal32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
+                   const float* __restrict__ u, const float* __restrict__ f, float* __restrict__ out, int TZ,
+                   ChebArgs ch) {
+  using S = Modal32Smem<TYE>;
+  constexpr int TXE = 32, NT = S::NT, PX = S::PX, NP = S::NP;
+  extern __shared__ __align__(16) unsigned char m32_smem[];
+  S& sm = *reinterpret_cast<S*>(m32_smem);
+  const int t = threadIdx.x, i = t & 31, j = t >> 5;
+  const int zblk = (d.vz + TZ - 1) / TZ;
+  const int rhs = blockIdx.z / zblk;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int64_t nv = d.nv;
+  u += (int64_t)rhs * 3 * nv;
+  if (f) f += (int64_t)rhs * 3 * nv;
+  out += (int64_t)rhs * 3 * nv;
+  const int gx = x0 + i, gy = y0 + j;
+  const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
+  const int zend = min(z0 + TZ, d.vz);
+  constexpr int KS = (NP + NT - 1) / NT;
+  int pxy[KS];
+#pragma unroll
+  for (int s = 0; s < KS; ++s) {
+    const int k = t + s * NT, px = k % PX, py = k / PX;
+    const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+    pxy[s] = (k < NP && vx >= 0 && vy >= 0 && vx < d.vx && vy < d.vy) ? vx + d.vx * vy : -1;
+  }
+  const int64_t plane_n = (int64_t)d.vx * d.vy;
+  auto prefetch = [&](int z) {
+    if (z <= zend) {
+      float4* dst = sm.plane[(z + 4) & 3];
+      const bool zok = z >= 0 && z < d.vz;
+      const int64_t zoff = (int64_t)z * plane_n;
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        const int k = t + s * NT;
+        if (k < NP) {
+          const bool ok = zok && pxy[s] >= 0;
+          const int64_t v = ok ? zoff + pxy[s] : 0;
+          cp_async_4(&dst[k].x, u + v, ok);
+          cp_async_4(&dst[k].y, u + nv + v, ok);
+          cp_async_4(&dst[k].z, u + 2 * nv + v, ok);
+        }
+      }
+    }
+    cp_async_commit();
+  };
+  const int pex = gx - 1, pey = gy - 1;
+  const bool pe_xy = pex >= 0 && pey >= 0 && pex < d.ex && pey < d.ey;
+  auto load_pe = [&](int ez) -> float {
+    return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (int64_t)d.ex * (pey + (int64_t)d.ey * ez)] : 0.f;
+  };
+  const float* __restrict__ dvin =
+      (MODE == 2 && !ch.first) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
+  // operands of the owned vertex at plane z, read in step z and used in step z + 1
+  uint8_t vm_n = 0;
+  float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f};
+  auto load_vertex = [&](int z) {
+    if (!own || z < z0 || z >= zend) return;
+    const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * z);
+    vm_n = vmask[v];
+    if (MODE >= 1) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f_n[c] = f[c * nv + v];
+    }
+    if (MODE == 2 && dvin) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) dv_n[c] = dvin[c * nv + v];
+    }
+  };
+  float own1[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // own y = 1 forces of the last layer, z = 0 / 1
+  float top[3] = {0.f, 0.f, 0.f};                          // z = 1 forces of the layer below the last
+  float uo[3] = {0.f, 0.f, 0.f};                           // owned vertex's own value at the last layer's plane
+  float dsum = 0.f;
+  float pe_n = load_pe(z0 - 1);
+  prefetch(z0 - 1);
+  prefetch(z0);
+  // step st: finish vertex plane st - 1 (layers st - 2, st - 1), then compute element layer st
+  for (int st = z0 - 1; st <= zend; ++st) {
+    prefetch(st + 2);
+    const float pe = pe_n;
+    const uint8_t vm_c = vm_n;
+    float f_c[3], dv_c[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
+    if (st + 1 < zend) pe_n = load_pe(st + 1);
+    load_vertex(st);
+    cp_async_wait1();
+    __syncthreads();
+    // ---- vertex plane p = st - 1
+    if (st >= z0) {
+      const int p = st - 1, xs = (st - 1) & 1;
+      float y[3];
+      if (own) {
+        const float4 ra = sm.xa[xs][t + TXE];
+        const float2 rb = sm.xb[xs][t + TXE];
+        const float r0[3] = {ra.x, ra.y, ra.z}, r1[3] = {ra.w, rb.x, rb.y};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          y[c] = top[c] + (own1[0][c] + r0[c]);
+          top[c] = own1[1][c] + r1[c];
+        }
+        if (p >= z0) {
+          const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * p);
+          const uint8_t m = vm_c;
+          const float uv[3] = {uo[0], uo[1], uo[2]};
+          if (MODE < 2) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const bool fr = (m >> c) & 1;
+              const float o = MODE == 1 ? (fr ? f_c[c] - y[c] : 0.f) : (fr ? y[c] : 0.f);
+              out[c * nv + v] = o;
+              if (MODE == 0) dsum += uv[c] * o;
+            }
+          } else {
+            const float* __restrict__ dinv = static_cast<const float*>(ch.dinv);
+            float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * nv;
+            float r[3], zc[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float dn = ch.first ? float(ch.c_new) * zc[c] : float(ch.c_old) * dv_c[c] + float(ch.c_new) * zc[c];
+              dv[c * nv + v] = dn;
+              out[c * nv + v] = uv[c] + dn;
+            }
+          }
+        }
+      }
+    }
+    // ---- element layer st
+    if (st < zend) {
+      if (MODE == 2 || (MODE == 0 && ch.dotp)) {
+        const float4 q = sm.plane[(st + 4) & 3][(i + 1) + PX * (j + 1)];
+        uo[0] = q.x; uo[1] = q.y; uo[2] = q.z;
+      }
+      float c[3][8];
+      if (pe != 0.f) {
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
+          const float4 q = sm.plane[(st + (a >> 2) + 4) & 3][k];
+          c[0][a] = q.x; c[1][a] = q.y; c[2][a] = q.z;
+        }
+        modal_element<float>(c, pe);
+      } else {
+#pragma unroll
+        for (int a = 0; a < 8; ++a) c[0][a] = c[1][a] = c[2][a] = 0.f;
+      }
+      // x combine: vertex column i takes the x = 1 nodes of element i and the
+      // x = 0 nodes of element i + 1 (lane 31's column is not owned)
+      float xc[2][2][3];  // [y bit][z bit][component]
+#pragma unroll
+      for (int yb = 0; yb < 2; ++yb)
+#pragma unroll
+        for (int zb = 0; zb < 2; ++zb)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc)
+            xc[yb][zb][cc] = c[cc][1 + 2 * yb + 4 * zb] +
+                             __shfl_down_sync(0xffffffffu, c[cc][2 * yb + 4 * zb], 1);
+#pragma unroll
+      for (int zb = 0; zb < 2; ++zb)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) own1[zb][cc] = xc[1][zb][cc];
+      sm.xa[st & 1][t] = make_float4(xc[0][0][0], xc[0][0][1], xc[0][0][2], xc[0][1][0]);
+      sm.xb[st & 1][t] = make_float2(xc[0][1][1], xc[0][1][2]);
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  if (MODE == 0 && ch.dotp) {
+    const double bs = modal_block_sum((double)dsum);
+    if (t == 0) ch.dotp[blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z)] = bs;
+  }
+}
+
 // The same operator (MODE 0: out = K u, MODE 1: out = f - K u) on FP64 vectors
 // computed in double-float arithmetic.  Vertex planes arrive as doubles by
-// cp.async and are split in place into (hi, lo) float pairs (the same 8 bytes)
-// once per plane, so the only FP64 instructions left are about eight
-// conversions per vertex; the element operator runs on the FP32 pipe.
+// cp.async and are split into (hi, lo) float pairs once per plane, so the only
+// FP64 instructions left are about eight conversions per vertex; the element
+// operator runs on the FP32 pipe.
+//
 // Shared memory of the double-float kernel.  High and low parts live in
 // separate 16-byte arrays, so each lane's access is one contiguous 16 bytes and
 // a warp's access touches the minimum of banks (a 32-byte (hi, lo) entry per
@@ -782,33 +956,45 @@ constexpr int MODAL_TXE = 32, MODAL_TYE = 8, MODAL_TZ = 16;
 template <typename T>
 constexpr int modal_tye() { return sizeof(T) == 4 ? TOPO_MODAL32_TYE : MODAL_TYE; }
 
-// Opt the modal kernels into more than 48 KB of dynamic shared memory (once).
 template <typename T>
-void modal_smem_attr(size_t smem) {
+dim3 modal_grid(const LevelDims& d, int tz, int nb) {
   constexpr int TYE = modal_tye<T>();
-  static std::once_flag once;
-  std::call_once(once, [smem] {
-    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  });
+  return dim3((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1), ((d.vz + tz - 1) / tz) * nb);
+}
+
+// One launch of the modal operator in mode MODE: the single-barrier kernel for
+// FP32, the generic kernel for FP64.  Kernels are opted into their dynamic
+// shared memory once.
+template <typename T, int MODE>
+void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u, const T* f,
+                  T* out, int tz, int nb, const ChebArgs& ch) {
+  if (tz <= 0) tz = MODAL_TZ;
+  const dim3 grid = modal_grid<T>(d, tz, nb);
+  constexpr int TYE = modal_tye<T>();
+  if constexpr (sizeof(T) == 4) {
+    const size_t smem = sizeof(Modal32Smem<TYE>);
+    static std::once_flag once;
+    std::call_once(once, [smem] {
+      cudaFuncSetAttribute(k_fine_modal32<TYE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    k_fine_modal32<TYE, MODE><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+  } else {
+    const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
+    static std::once_flag once;
+    std::call_once(once, [smem] {
+      cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+    });
+    k_fine_modal<T, MODAL_TXE, TYE, MODE><<<grid, MODAL_TXE * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+  }
 }
 
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb, int tz) {
-  constexpr int TYE = modal_tye<T>();
-  if (tz <= 0) tz = MODAL_TZ;
-  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1),
-                  ((d.vz + tz - 1) / tz) * nb);
-  constexpr int NT = MODAL_TXE * TYE;
-  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
-  modal_smem_attr<T>(smem);
-  ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr};
-  if (residual)
-    k_fine_modal<T, MODAL_TXE, TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
-  else
-    k_fine_modal<T, MODAL_TXE, TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr};
+  if (residual) launch_modal<T, 1>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
+  else launch_modal<T, 0>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
 }
 
 // out = K u with the per-CTA partial sums of u.out in partial[0, n) (one
@@ -817,16 +1003,12 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
 template <typename T>
 int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                           T* out, int tz, double* partial, int cap) {
-  constexpr int TYE = modal_tye<T>();
   if (tz <= 0) tz = MODAL_TZ;
-  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1), (d.vz + tz - 1) / tz);
+  const dim3 grid = modal_grid<T>(d, tz, 1);
   const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
   if (nparts > cap) return 0;
-  constexpr int NT = MODAL_TXE * TYE;
-  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
-  modal_smem_attr<T>(smem);
-  ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial};
-  k_fine_modal<T, MODAL_TXE, TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, nullptr, out, tz, ch);
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial};
+  launch_modal<T, 0>(s, d, rhop, vmask, u, nullptr, out, tz, 1, ch);
   return (int)nparts;
 }
 
@@ -858,15 +1040,8 @@ template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                       const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
                       int tz) {
-  constexpr int TYE = modal_tye<T>();
-  if (tz <= 0) tz = MODAL_TZ;
-  const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1),
-                  ((d.vz + tz - 1) / tz) * nb);
-  constexpr int NT = MODAL_TXE * TYE;
-  const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
-  modal_smem_attr<T>(smem);
-  ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nullptr};
-  k_fine_modal<T, MODAL_TXE, TYE, 2><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, uout, tz, ch);
+  const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nullptr};
+  launch_modal<T, 2>(s, d, rhop, vmask, u, f, uout, tz, nb, ch);
 }
 
 template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,

@@ -333,18 +333,22 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start) {
       c_new = 2.0 * rho_new / delta;
       rho_old = rho_new;
     }
+    // FP32 level 0 after a zero start: d = u after the first step, so it is
+    // not stored and the second step reads it from u
+    const bool d_in_u = l == 0 && sizeof(T) == 4 && zero_start;
     if (k == 0 && zero_start) {
       // not in the smoother's profiling family: no operator is applied
       if (l == 0)
-        launch_fine_cheb_zero<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
-                                 c_new, h->nb);
+        launch_fine_cheb_zero<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, P<T>::F(L), ub, P<T>::dinv(L),
+                                 d_in_u ? nullptr : P<T>::cd(L), c_new, h->nb);
       else
         launch_cheb_zero_stored<T>(h->stream, L.d.nv, nullptr, P<T>::dinv(L), P<T>::F(L), P<T>::cd(L), ub, c_new,
                                    h->nb);
     } else if (l == 0) {
       EventPair* ev = prof_begin(h, P<T>::fam_smooth);
       launch_fine_cheb<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L),
-                          P<T>::cd(L), c_old, c_new, k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64);
+                          P<T>::cd(L), c_old, c_new, k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64,
+                          d_in_u && k == 1);
       prof_end(h, ev);
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),

@@ -179,6 +179,7 @@ struct ChebArgs {
   double c_old, c_new;
   int first;
   double* dotp;      // MODE 0: per-CTA partial sums of u.out (null: none)
+  int d_is_u;        // MODE 2, FP32: d equals u on entry (the step after a zero start); dvec is not read
 };
 
 // Sum of v over the CTA (valid in thread 0); every thread must call it.
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
     return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (int64_t)d.ex * (pey + (int64_t)d.ey * ez)] : 0.f;
   };
   const float* __restrict__ dvin =
-      (MODE == 2 && !ch.first) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
+      (MODE == 2 && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
   // operands of the owned vertex at plane z, read in step z and used in step z + 1
   uint8_t vm_n = 0;
   float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f};
@@ -603,7 +604,8 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
               zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              const float dn = ch.first ? float(ch.c_new) * zc[c] : float(ch.c_old) * dv_c[c] + float(ch.c_new) * zc[c];
+              const float dold = ch.d_is_u ? uv[c] : dv_c[c];
+              const float dn = ch.first ? float(ch.c_new) * zc[c] : float(ch.c_old) * dold + float(ch.c_new) * zc[c];
               dv[c * nv + v] = dn;
               out[c * nv + v] = uv[c] + dn;
             }
@@ -992,7 +994,7 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb, int tz) {
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0};
   if (residual) launch_modal<T, 1>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
   else launch_modal<T, 0>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
 }
@@ -1007,7 +1009,7 @@ int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, con
   const dim3 grid = modal_grid<T>(d, tz, 1);
   const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
   if (nparts > cap) return 0;
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0};
   launch_modal<T, 0>(s, d, rhop, vmask, u, nullptr, out, tz, 1, ch);
   return (int)nparts;
 }
@@ -1039,17 +1041,18 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
 template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                       const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
-                      int tz) {
-  const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nullptr};
+                      int tz, bool d_is_u) {
+  // the FP64 kernel always reads d
+  const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nullptr, (d_is_u && sizeof(T) == 4) ? 1 : 0};
   launch_modal<T, 2>(s, d, rhop, vmask, u, f, uout, tz, nb, ch);
 }
 
 template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                        const double*, const double*, double*, const double*, double*, double,
-                                       double, bool, int, int);
+                                       double, bool, int, int, bool);
 template void launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
                                       const float*, const float*, float*, const float*, float*, double, double,
-                                      bool, int, int);
+                                      bool, int, int, bool);
 
 // First Chebyshev step from a zero iterate (every pre-smoothing sweep of a
 // preconditioning V-cycle starts from u = 0): K u vanishes, so r = f on the
@@ -1065,12 +1068,21 @@ __global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, 
   if (v >= d.nv) return;
   const int64_t nv = d.nv, bo = (int64_t)blockIdx.y * 3 * nv;
   f += bo;
-  dv += bo;
+  if (dv) dv += bo;
   out += bo;
   const uint8_t m = vmask[v];
-  const int x = (int)(v % d.vx);
-  const int64_t t = v / d.vx;
-  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  int x, y, z;
+  if (nv < (int64_t)1 << 31) {  // 32-bit index arithmetic
+    const unsigned vv = (unsigned)v, vx = (unsigned)d.vx, tt = vv / vx;
+    x = (int)(vv - tt * vx);
+    y = (int)(tt % (unsigned)d.vy);
+    z = (int)(tt / (unsigned)d.vy);
+  } else {
+    x = (int)(v % d.vx);
+    const int64_t t = v / d.vx;
+    y = (int)(t % d.vy);
+    z = (int)(t / d.vy);
+  }
   float pl[4], pp[4];
 #pragma unroll
   for (int w = 0; w < 4; ++w) {
@@ -1096,7 +1108,7 @@ __global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, 
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const float dn = c_new * zc[c];
-    dv[c * nv + v] = dn;
+    if (dv) dv[c * nv + v] = dn;
     out[c * nv + v] = dn;
   }
 }
@@ -1104,7 +1116,7 @@ __global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, 
 template <typename T>
 void launch_fine_cheb_zero(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* f,
                            T* uout, const T* dinv, T* dvec, double c_new, int nb) {
-  if (sizeof(T) == 4) {
+  if (sizeof(T) == 4) {  // dvec may be null: d is not stored (the next step takes d = u)
     k_fine_cheb_zero32<<<dim3(blocks_for(d.nv, 256), nb), 256, 0, s>>>(
         d, reinterpret_cast<const float*>(rhop), vmask, reinterpret_cast<const float*>(f),
         reinterpret_cast<float*>(dvec), reinterpret_cast<float*>(uout), (float)c_new);

@@ -92,11 +92,12 @@ void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, con
 template <typename T>
 void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                       const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first,
-                      int nb = 1, int tz = 0);
+                      int nb = 1, int tz = 0, bool d_is_u = false);
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);
 // First Chebyshev step from a zero iterate (u = 0): d = c_new D^-1 f, uout = d.
+// FP32: dvec may be null, and the next step then takes d from u (d_is_u).
 template <typename T>
 void launch_fine_cheb_zero(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* f,
                            T* uout, const T* dinv, T* dvec, double c_new, int nb = 1);

@@ -112,6 +112,9 @@ struct topo_handle {
   double* hsc = nullptr;   // pinned host mirror
   int64_t active_elements = 0, gs_padded_elements = 0;
   bool bc_set = false, ops_ready = false;
+  // design iteration: the solve's final residual also writes element energies
+  // into sens (want_energy), and says so (energy_ready)
+  bool want_energy = false, energy_ready = false;
   int op_precision = 3;    // bit0 FP64 operators, bit1 FP32 operators
   bool ops64 = false, ops32 = false;
   // profiling
@@ -1239,6 +1242,7 @@ int topo_vcycle(topo_handle* h, int pre, int post, double* relres) {
 
 int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats) {
   RET(check_ready(h, true));
+  h->energy_ready = false;
   if (!o || o->rtol <= 0 || o->max_iter < 0 || o->pre < 0 || o->post < 0) return TOPO_E_BAD_INPUT;
   DevLevel& L0 = h->lv[0];
   const int64_t n3 = 3 * L0.d.nv;
@@ -1406,8 +1410,17 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     return fail(h, TOPO_E_BAD_INPUT, "unknown solve mode %d", o->mode);
   }
   if (o->mode != TOPO_SOLVE_VCYCLE && fn != 0.0) {
-    // true FP64 residual of the final iterate
-    level_residual<double>(h, 0);
+    // true FP64 residual of the final iterate (with the element energies of
+    // the sensitivity when a design iteration asks for them)
+    if (h->want_energy && h->fine_df && h->nb == 1) {
+      EventPair* ev = prof_begin(h, P<double>::fam_apply);
+      launch_fine_apply_df(h->stream, L0.d, h->rhop, L0.vmask, L0.U, L0.F, L0.R, true, 1, h->tz64, h->sens);
+      prof_end(h, ev);
+      count_launch();
+      h->energy_ready = true;
+    } else {
+      level_residual<double>(h, 0);
+    }
     launch_dot<double>(h->stream, L0.R, L0.R, n3, h->partial, h->sc + S_RR);
     count_launch(2);
     RET(read_scalars(h, S_RR, 1));
@@ -2109,11 +2122,20 @@ int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_sta
   CK(cudaEventRecord(e0, h->stream));
   topo_iter_stats st{};
   RET(topo_update_operators(h));
+  h->want_energy = true;
   int rc = topo_solve(h, &o->solve, &st.solve);
+  h->want_energy = false;
   if (rc != TOPO_OK && rc != TOPO_E_NOT_CONVERGED) return rc;
   RET(topo_compliance(h, &st.compliance));
   if (!std::isfinite(st.compliance)) return fail(h, TOPO_E_NONFINITE, "compliance is not finite");
-  RET(topo_sensitivity(h));
+  if (h->energy_ready) {  // u is the solve's final iterate, rho unchanged since
+    const DevLevel& L = h->lv[0];
+    launch_sensitivity_from_energy(h->stream, L.d.ne, L.eactive, h->rho, h->cfg.power_penalty, h->sens);
+    count_launch();
+    h->energy_ready = false;
+  } else {
+    RET(topo_sensitivity(h));
+  }
   RET(topo_filter(h, o->filter_radius > 0 ? o->filter_radius : 2.0));
   RET(topo_spline_adjoint(h));
   topo_oc_stats oc{};

@@ -270,6 +270,21 @@ void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eacti
   k_sensitivity<df><<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, rho, u, penal, lam, mu, h, sens);
 }
 
+// The same sensitivity from element energies E = u_e . (rho^p Ke u_e) that the
+// solve's final residual kernel wrote: -p rho^(p-1) u_e^T Ke u_e = -p E / rho.
+__global__ void k_sensitivity_from_energy(int64_t ne, const uint8_t* __restrict__ eactive,
+                                          const double* __restrict__ rho, double penal, double* __restrict__ sens) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const double r = rho[e];
+  sens[e] = (eactive[e] && r > 0.0) ? -penal * sens[e] / r : 0.0;
+}
+
+void launch_sensitivity_from_energy(cudaStream_t s, int64_t ne, const uint8_t* eactive, const double* rho,
+                                    double penal, double* sens) {
+  k_sensitivity_from_energy<<<nblk(ne, 256), 256, 0, s>>>(ne, eactive, rho, penal, sens);
+}
+
 // Sensitivity filter (grid/Grid.cu:4130-4229): normalised average over the ball
 // r^2 <= R^2, R_int = floor(R + 0.5), weight 1 - 6s^2 + 8s^3 - 3s^4 with s = r/R.
 // The ball's offsets and weights depend only on R; they come precomputed (in the

@@ -103,8 +103,10 @@ __device__ __forceinline__ void wht_bwd(T v[8]) {
 }
 
 // In: c[3][8] nodal values per component.  Out: c[3][8] nodal forces of pe*Ke*u.
-template <typename T>
-__device__ __forceinline__ void modal_element(T c[3][8], T pe) {
+// EN: also *energy = u . (pe Ke u) = sum over modes of (transformed u) . (modal
+// force), since the backward transform is the forward one's transpose.
+template <typename T, bool EN = false>
+__device__ __forceinline__ void modal_element(T c[3][8], T pe, T* energy = nullptr) {
   wht_fwd<T>(c[0]); wht_fwd<T>(c[1]); wht_fwd<T>(c[2]);
   const T L = modal_c<T>(0) * pe, M = modal_c<T>(1) * pe;
   const T k0 = modal_c<T>(2), k1 = modal_c<T>(3), k2 = modal_c<T>(4);
@@ -154,6 +156,14 @@ __device__ __forceinline__ void modal_element(T c[3][8], T pe) {
   {  // YZ, XZ, XY parts all act on the XYZ mode
     const T kk = k2 * (L + T(4) * M);
     g[0][7] = kk * c[0][7]; g[1][7] = kk * c[1][7]; g[2][7] = kk * c[2][7];
+  }
+  if constexpr (EN) {
+    T e = T(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int a = 1; a < 8; ++a) e += c[i][a] * g[i][a];  // g[i][0] = 0: rigid translation
+    *energy = e;
   }
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -682,7 +692,7 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
                                                             const uint8_t* __restrict__ vmask,
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ f, double* __restrict__ out,
-                                                            int TZ) {
+                                                            int TZ, double* __restrict__ energy) {
   using S = DfSmem<TXE, TYE>;
   constexpr int NT = S::NT, PX = S::PX, NP = S::NP;
   extern __shared__ __align__(32) unsigned char modal_smem[];
@@ -739,6 +749,9 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
       df pe(0);
       if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
         pe = df_from(rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)]);
+      // MODE 3 writes u_e . (rho^p Ke u_e) of the elements this CTA owns (its
+      // first element row / column and layer belong to the neighbouring tiles)
+      const bool own_e = MODE == 3 && i > 0 && j > 0 && ez >= z0 && ex < d.ex && ey < d.ey && ez < d.ez;
       if (pe != df(0)) {
         df c[3][8];
 #pragma unroll
@@ -748,7 +761,13 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
           const float4 h = sm.phi[cs][k], l = sm.plo[cs][k];
           c[0][a] = df(h.x, l.x); c[1][a] = df(h.y, l.y); c[2][a] = df(h.z, l.z);
         }
-        modal_element<df>(c, pe);
+        if (MODE == 3) {
+          df en;
+          modal_element<df, true>(c, pe, &en);
+          if (own_e) energy[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)] = df_to(en);
+        } else {
+          modal_element<df>(c, pe);
+        }
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
           sm.fhi[a][t] = make_float4(c[0][a].hi, c[1][a].hi, c[2][a].hi, 0.f);
@@ -760,6 +779,7 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
           sm.fhi[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
           sm.flo[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        if (own_e) energy[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)] = 0.0;
       }
     }
     __syncthreads();
@@ -782,7 +802,7 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
         for (int c = 0; c < 3; ++c) {
           const bool fr = (m >> c) & 1;
           const int64_t idx = c * nv + v;
-          out[idx] = MODE == 1 ? (fr ? f[idx] - y[c] : 0.0) : (fr ? y[c] : 0.0);
+          out[idx] = MODE >= 1 ? (fr ? f[idx] - y[c] : 0.0) : (fr ? y[c] : 0.0);
         }
       }
       acc0 = t0; acc1 = t1; acc2 = t2;
@@ -1020,7 +1040,8 @@ template int launch_fine_apply_dot<double>(cudaStream_t, const LevelDims&, const
                                            const double*, double*, int, double*, int);
 
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
-                          const double* u, const double* f, double* out, bool residual, int nb, int tz) {
+                          const double* u, const double* f, double* out, bool residual, int nb, int tz,
+                          double* energy) {
   if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
                   ((d.vz + tz - 1) / tz) * nb);
@@ -1030,11 +1051,14 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
   std::call_once(once, [smem] {
     cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
-  if (residual)
-    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz);
+  if (residual && energy)
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, energy);
+  else if (residual)
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, nullptr);
   else
-    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz);
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, nullptr);
 }
 
 // One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u).

@@ -81,8 +81,10 @@ template <typename T>
 int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                           T* out, int tz, double* partial, int cap);
 // FP64 vectors, double-float arithmetic (k_fine_modal_df)
+// energy (residual only, one right-hand side): per-element u_e . (rho^p Ke u_e)
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
-                          const double* u, const double* f, double* out, bool residual, int nb = 1, int tz = 0);
+                          const double* u, const double* f, double* out, bool residual, int nb = 1, int tz = 0,
+                          double* energy = nullptr);
 template <typename T>
 void launch_fine_gs(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, T* u,
                     const T* f, int colour, bool reverse);
@@ -206,6 +208,9 @@ void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eact
 void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                         const double* rho, const double* u, double penal, double lam, double mu,
                         double h, double* sens);
+// sens = -p E / rho in place, from element energies E = u_e . (rho^p Ke u_e)
+void launch_sensitivity_from_energy(cudaStream_t s, int64_t ne, const uint8_t* eactive, const double* rho,
+                                    double penal, double* sens);
 void launch_filter(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* src,
                    double* dst, const int4* offs, const double* wts, int noffs);
 void filter_table(double R, std::vector<int4>& offs, std::vector<double>& w);

@@ -273,3 +273,26 @@ def test_error_codes():
     assert s["rc"] == capi.TOPO_E_NOT_CONVERGED and s["iterations"] == 2
     s = g.solve(mode=capi.SOLVE_PCG64, rtol=1e-6, max_iter=200)
     assert s["relres"] <= 1e-6
+
+
+@pytest.mark.parametrize("mode", [capi.SOLVE_MIXED, capi.SOLVE_PCG64])
+def test_design_iteration_energy_sensitivity(oracle_mod, mode):
+    """topo_design_iteration takes the sensitivity from the element energies of
+    the solve's final double-float residual; the step-by-step calls take it from
+    topo_sensitivity.  Same solve, so the designs agree to rounding."""
+    wl = _case("mbb32")
+    nc = int(np.prod([p + wl.order for p in wl.partition]))
+    coeff = random_coeff(nc, seed=5)
+    a, b = setup_gpu(wl, coeff), setup_gpu(wl, coeff)
+    opts = dict(mode=mode, smoother=capi.SMOOTH_CHEBYSHEV, rtol=1e-8, max_iter=300, inner_max=4)
+    sa = a.design_iteration(solve=opts, oc=dict(vgoal=wl.vgoal))
+    b.update_operators()
+    b.solve(**opts)
+    cb = b.compliance()
+    b.sensitivity()
+    b.filter(2.0)
+    b.spline_adjoint()
+    b.oc_update(wl.vgoal)
+    assert abs(sa["compliance"] - cb) <= 1e-14 * abs(cb)
+    assert rel(a.get("coeff"), b.get("coeff")) < 1e-12
+    assert rel(a.get("rho"), b.get("rho")) < 1e-12

@@ -824,7 +824,6 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
   __shared__ double sc[GJB][GJB + 1];
   __shared__ double sp[GJB][GJB + 1];
   __shared__ int sflag;
-  double* Dg = work;                 // [GJB][GJB]
   double* P = work + GJB * GJB;      // [GJB][n]
   double* Cp = P + (int64_t)GJB * n; // [n][GJB]
   const int tid = threadIdx.x;
@@ -834,54 +833,60 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
   const int nblk_tiles = (n + GJB - 1) / GJB;
   for (int k0 = 0; k0 < n; k0 += GJB) {
     const int kb = min(GJB, n - k0);
-    // ---- A: invert the diagonal block (CTA 0)
-    if (blockIdx.x == 0) {
+    // ---- A: every CTA inverts the diagonal block in its own shared memory (the
+    // same data and the same operations, so the same result and the same pivot
+    // decisions everywhere; no barrier across CTAs is needed before phase B)
+    for (int e = tid; e < GJB * GJB; e += blockDim.x) {
+      const int r = e / GJB, c = e % GJB;
+      sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+    }
+    if (tid == 0) sflag = 0;
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+      const double p = sd[j][j];
+      if (p < -tol) {
+        if (tid == 0) {
+          sflag = 1;
+          if (blockIdx.x == 0) status[1] = k0 + j + 1;
+        }
+        break;
+      }
+      __syncthreads();
+      if (p <= tol) {  // drop DOF k0 + j
+        for (int e = tid; e < 2 * GJB; e += blockDim.x) {
+          if (e < GJB) sd[j][e] = 0.0;
+          else sd[e - GJB][j] = 0.0;
+        }
+        if (tid == 0 && blockIdx.x == 0) status[0] += 1;
+        __syncthreads();
+        continue;
+      }
+      // 1/p: FP32 estimate refined by two Newton steps r <- r + r (1 - p r)
+      double rp = (double)__frcp_rn((float)p);
+      rp = fma(rp, fma(-p, rp, 1.0), rp);
+      rp = fma(rp, fma(-p, rp, 1.0), rp);
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
-      }
-      if (tid == 0) sflag = 0;
-      __syncthreads();
-      for (int j = 0; j < kb; ++j) {
-        const double p = sd[j][j];
-        if (p < -tol) {
-          if (tid == 0) { status[1] = k0 + j + 1; sflag = 1; }
-          break;
-        }
-        __syncthreads();
-        if (p <= tol) {  // drop DOF k0 + j
-          for (int e = tid; e < 2 * GJB; e += blockDim.x) {
-            if (e < GJB) sd[j][e] = 0.0;
-            else sd[e - GJB][j] = 0.0;
-          }
-          if (tid == 0) status[0] += 1;
-          __syncthreads();
-          continue;
-        }
-        const double rp = 1.0 / p;
-        for (int e = tid; e < kb * kb; e += blockDim.x) {
-          const int r = e / kb, c = e % kb;
-          if (r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
-        }
-        __syncthreads();
-        for (int e = tid; e < 2 * kb; e += blockDim.x) {
-          if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
-          else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
-        }
-        __syncthreads();
+        if (r < kb && c < kb && r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
       }
       __syncthreads();
-      for (int e = tid; e < GJB * GJB; e += blockDim.x) Dg[e] = sd[e / GJB][e % GJB];
+      for (int e = tid; e < 2 * kb; e += blockDim.x) {
+        if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
+        else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
+      }
+      __syncthreads();
     }
-    grid.sync();
-    if (status[1]) return;  // indefinite pivot: every CTA sees it after the barrier
+    __syncthreads();
+    if (sflag) return;  // indefinite pivot: every CTA found it in its own copy
     // ---- B: row panel P = D^-1 A[K,:] (columns outside K) and column panel C = A[:,K]
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid, gs = (int64_t)gridDim.x * blockDim.x;
     for (int64_t e = gt; e < (int64_t)kb * n; e += gs) {
       const int r = (int)(e / n), c = (int)(e % n);
       double v = 0.0;
-      if (c < k0 || c >= k0 + kb)
-        for (int m = 0; m < kb; ++m) v += Dg[r * GJB + m] * A[(int64_t)(k0 + m) * n + c];
+      if (c < k0 || c >= k0 + kb) {
+#pragma unroll 8
+        for (int m = 0; m < kb; ++m) v += sd[r][m] * A[(int64_t)(k0 + m) * n + c];
+      }
       P[(int64_t)r * n + c] = v;
     }
     for (int64_t e = gt; e < (int64_t)n * kb; e += gs) {
@@ -897,7 +902,6 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         const int r = e / GJB, c = e % GJB;
         sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : 0.0;
         sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : 0.0;
-        sd[r][c] = Dg[r * GJB + c];
         if constexpr (DFC) {
           scd[r][c] = df_from(sc[r][c]);
           spd[r][c] = df_from(sp[r][c]);

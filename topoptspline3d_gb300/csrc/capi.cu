@@ -108,6 +108,12 @@ struct topo_handle {
   double* partial = nullptr;
   double* fdot = nullptr;  // per-CTA partials of the fine operator's fused dot
   int fdot_cap = 0;
+  // inner CG: the FP32 V-cycle's last Chebyshev step also forms r.z and z.rold
+  // (partials in vdot[0, 2 fdot_cap)) when vdot_on; the sums land in vdot_out[0..1]
+  double* vdot = nullptr;
+  bool vdot_on = false;
+  double* vdot_out[2] = {nullptr, nullptr};
+  const float* vdot_w2 = nullptr;
   double* sc = nullptr;    // device scalar slots
   double* hsc = nullptr;   // pinned host mirror
   int64_t active_elements = 0, gs_padded_elements = 0;
@@ -320,7 +326,7 @@ struct ChebParams {
 // zero_start the iterate is known to be zero on entry (level U is not read),
 // and the first step is the operator-free d = c_new D^-1 f.
 template <typename T>
-void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start) {
+void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bool last_dots = false) {
   DevLevel& L = h->lv[l];
   const double lmax = P<T>::lmax(L) * cp.hi, lmin = P<T>::lmax(L) * cp.lo;
   const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
@@ -348,11 +354,25 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start) {
         launch_cheb_zero_stored<T>(h->stream, L.d.nv, nullptr, P<T>::dinv(L), P<T>::F(L), P<T>::cd(L), ub, c_new,
                                    h->nb);
     } else if (l == 0) {
+      const bool dots = last_dots && k == cp.degree - 1;
       EventPair* ev = prof_begin(h, P<T>::fam_smooth);
-      launch_fine_cheb<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L),
-                          P<T>::cd(L), c_old, c_new, k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64,
-                          d_in_u && k == 1);
+      const int np = launch_fine_cheb<T>(
+          h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), c_old, c_new,
+          k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr,
+          dots ? h->vdot + h->fdot_cap : nullptr, dots ? reinterpret_cast<const T*>(h->vdot_w2) : nullptr,
+          h->fdot_cap);
       prof_end(h, ev);
+      if (dots) {
+        if (np > 0) {  // r.z and z.rold of the cycle's result (F is r, the output is z)
+          launch_finalize_sum(h->stream, h->vdot, np, h->vdot_out[0]);
+          launch_finalize_sum(h->stream, h->vdot + h->fdot_cap, np, h->vdot_out[1]);
+        } else {
+          launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out[0]);
+          launch_dot<T>(h->stream, ub, reinterpret_cast<const T*>(h->vdot_w2), 3 * L.d.nv, h->partial,
+                        h->vdot_out[1]);
+        }
+        count_launch(2);
+      }
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
                              c_old, c_new, k == 0, h->nb);
@@ -367,9 +387,9 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start) {
 
 template <typename T>
 void smooth_level(topo_handle* h, int l, int sweeps, bool reverse, int smoother, const ChebParams& cp,
-                  bool zero_start = false) {
+                  bool zero_start = false, bool last_dots = false) {
   if (smoother == TOPO_SMOOTH_CHEBYSHEV) {
-    for (int s = 0; s < sweeps; ++s) cheb_level<T>(h, l, cp, zero_start && s == 0);
+    for (int s = 0; s < sweeps; ++s) cheb_level<T>(h, l, cp, zero_start && s == 0, last_dots && s == sweeps - 1);
   } else {
     gs_level<T>(h, l, sweeps, reverse);
   }
@@ -416,7 +436,7 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
   const bool cheb_pre = cheb_zero_start(smoother, pre, cp);
   if (nl == 1) {
     smooth_level<T>(h, 0, pre, false, smoother, cp, zero0);
-    smooth_level<T>(h, 0, post, sym, smoother, cp);
+    smooth_level<T>(h, 0, post, sym, smoother, cp, false, h->vdot_on && sizeof(T) == 4);
     return;
   }
   for (int l = 0; l < nl; ++l) {
@@ -431,7 +451,7 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
   }
   for (int l = nl - 2; l >= 0; --l) {
     prolong_T<T>(h, l);
-    smooth_level<T>(h, l, post, sym, smoother, cp);
+    smooth_level<T>(h, l, post, sym, smoother, cp, false, l == 0 && h->vdot_on && sizeof(T) == 4);
   }
 }
 
@@ -447,7 +467,8 @@ static void vcycle32(topo_handle* h, int pre, int post, int smoother, const Cheb
   }
   prof_collect(h);
   std::vector<double> key = {(double)pre, (double)post, (double)smoother, (double)cp.degree, cp.lo, cp.hi,
-                             (double)h->tz32, (double)h->nb, (double)h->prof, (double)zero0};
+                             (double)h->tz32, (double)h->nb, (double)h->prof, (double)zero0,
+                             (double)h->vdot_on, (double)(uintptr_t)h->vdot_w2};
   for (const DevLevel& L : h->lv) {
     key.push_back(L.lmax32);
     key.push_back((double)(uintptr_t)L.U32);
@@ -605,7 +626,8 @@ int read_scalars(topo_handle* h, int first, int count) {
 // so an FCG may run nested inside another one's preconditioner.
 template <typename T, typename Prec>
 int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, double rtol, int maxit,
-          int base, Prec&& prec, int* iters, double* rel_out, double bnorm_ref, bool x_zero = false) {
+          int base, Prec&& prec, int* iters, double* rel_out, double bnorm_ref, bool x_zero = false,
+          bool prec_dots = false) {
   DevLevel& L0 = h->lv[0];
   const int64_t n3 = 3 * L0.d.nv;
   double* sc = h->sc + base;
@@ -622,11 +644,13 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
   int it = 0;
   while (rn / bn > rtol && it < maxit) {
     RET(prec(r, z));
-    launch_dot<T>(h->stream, r, z, n3, h->partial, sc + S_RZ);
-    count_launch(2);
-    if (it > 0) {
-      launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD);
+    if (!prec_dots) {  // else the preconditioner left r.z and z.rold in the scalar slots
+      launch_dot<T>(h->stream, r, z, n3, h->partial, sc + S_RZ);
       count_launch(2);
+      if (it > 0) {
+        launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD);
+        count_launch(2);
+      }
     }
     if (it > 0) launch_scalar_ratio(h->stream, sc, S_RZ, S_ZROLD, S_RZOLD, S_BETA);
     launch_pcg_dir<T>(h->stream, z, d, sc, S_BETA, it == 0, n3);
@@ -791,6 +815,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     // tiles (31 x 7 owned vertices) at z-march depths of 4 and more
     h->fdot_cap = (int)std::min<int64_t>(1 << 24, (int64_t)((d0.vx + 30) / 31) * ((d0.vy + 6) / 7) * ((d0.vz + 3) / 4));
     A(dalloc(hp, &h->fdot, h->fdot_cap));
+    A(dalloc(hp, &h->vdot, 2 * (int64_t)h->fdot_cap));
   }
   if (rc == TOPO_OK && nl > 1) {
     const LevelDims& dl = h->lv.back().d;
@@ -1336,11 +1361,30 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       ++st.learned_applied;
       return TOPO_OK;
     };
+    // The inner CG's r.z and z.rold: from the V-cycle's last Chebyshev step when
+    // it is a fine FP32 Chebyshev step and no network correction follows, else
+    // by separate dots after the cycle.
+    const bool vdots = o->smoother == TOPO_SMOOTH_CHEBYSHEV && o->post >= 1 && cp.degree >= 1 && h->nb == 1;
     auto prec32 = [&](const float* r, float* z) -> int {
       (void)z;
       ++nvc;
-      RET(vcycle_prec<float>(h, r, o->pre, o->post, o->smoother, cp));
-      return net(r, L0.U32);
+      double* s_rz = h->sc + 8 + S_RZ;
+      double* s_zr = h->sc + 8 + S_ZROLD;
+      h->vdot_on = vdots && !net_on;
+      h->vdot_out[0] = s_rz;
+      h->vdot_out[1] = s_zr;
+      h->vdot_w2 = h->rold32;
+      const int rc = vcycle_prec<float>(h, r, o->pre, o->post, o->smoother, cp);
+      const bool fused = h->vdot_on;
+      h->vdot_on = false;
+      RET(rc);
+      RET(net(r, L0.U32));
+      if (!fused) {
+        launch_dot<float>(h->stream, r, L0.U32, n3, h->partial, s_rz);
+        launch_dot<float>(h->stream, L0.U32, h->rold32, n3, h->partial, s_zr);
+        count_launch(4);
+      }
+      return TOPO_OK;
     };
     auto prec = [&](const double* r, double* z) -> int {
       const double rn = std::sqrt(h->hsc[S_RR]);
@@ -1390,7 +1434,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       // the inner residual lives in level-0 F32, the V-cycle's right-hand side,
       // so the preconditioner needs no copy; x32 = 0 gives r = b without a matvec
       RET(fcg_T<float>(h, h->x32, L0.F32, L0.F32, h->d32, h->q32, h->rold32, L0.U32, inner_rtol, inner_max,
-                       8, prec32, &iit, &irel, rnorm > 0 ? rnorm : 1.0, true));
+                       8, prec32, &iit, &irel, rnorm > 0 ? rnorm : 1.0, true, true));
       k_to_double<float><<<nb256(n3), 256, 0, h->stream>>>(n3, h->x32, z);
       count_launch();
       return TOPO_OK;

@@ -188,8 +188,10 @@ struct ChebArgs {
   void* dvec;        // [3][nv]
   double c_old, c_new;
   int first;
-  double* dotp;      // MODE 0: per-CTA partial sums of u.out (null: none)
+  double* dotp;      // per-CTA partial sums: MODE 0 u.out, MODE 2 (FP32) f.out (null: none)
   int d_is_u;        // MODE 2, FP32: d equals u on entry (the step after a zero start); dvec is not read
+  double* dotp2;     // MODE 2, FP32: per-CTA partial sums of out.w2 (null: none)
+  const void* w2;
 };
 
 // Sum of v over the CTA (valid in thread 0); every thread must call it.
@@ -544,8 +546,9 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
   const float* __restrict__ dvin =
       (MODE == 2 && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
   // operands of the owned vertex at plane z, read in step z and used in step z + 1
+  const float* __restrict__ w2 = (MODE == 2 && ch.dotp2) ? static_cast<const float*>(ch.w2) : nullptr;
   uint8_t vm_n = 0;
-  float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f};
+  float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f}, w_n[3] = {0.f, 0.f, 0.f};
   auto load_vertex = [&](int z) {
     if (!own || z < z0 || z >= zend) return;
     const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * z);
@@ -558,7 +561,12 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
 #pragma unroll
       for (int c = 0; c < 3; ++c) dv_n[c] = dvin[c * nv + v];
     }
+    if (MODE == 2 && w2) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) w_n[c] = w2[c * nv + v];
+    }
   };
+  float dsum2 = 0.f;  // MODE 2 with ch.dotp2: this thread's share of out.w2
   float own1[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // own y = 1 forces of the last layer, z = 0 / 1
   float top[3] = {0.f, 0.f, 0.f};                          // z = 1 forces of the layer below the last
   float uo[3] = {0.f, 0.f, 0.f};                           // owned vertex's own value at the last layer's plane
@@ -571,9 +579,9 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
     prefetch(st + 2);
     const float pe = pe_n;
     const uint8_t vm_c = vm_n;
-    float f_c[3], dv_c[3];
+    float f_c[3], dv_c[3], w_c[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
+    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; w_c[c] = w_n[c]; }
     if (st + 1 < zend) pe_n = load_pe(st + 1);
     load_vertex(st);
     cp_async_wait1();
@@ -617,7 +625,10 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
               const float dold = ch.d_is_u ? uv[c] : dv_c[c];
               const float dn = ch.first ? float(ch.c_new) * zc[c] : float(ch.c_old) * dold + float(ch.c_new) * zc[c];
               dv[c * nv + v] = dn;
-              out[c * nv + v] = uv[c] + dn;
+              const float o = uv[c] + dn;
+              out[c * nv + v] = o;
+              dsum += f_c[c] * o;
+              dsum2 += o * w_c[c];
             }
           }
         }
@@ -662,9 +673,15 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
-  if (MODE == 0 && ch.dotp) {
+  const int64_t cta = blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z);
+  if (MODE != 1 && ch.dotp) {
     const double bs = modal_block_sum((double)dsum);
-    if (t == 0) ch.dotp[blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z)] = bs;
+    if (t == 0) ch.dotp[cta] = bs;
+  }
+  if (MODE == 2 && ch.dotp2) {
+    __syncthreads();  // the block sum's scratch is reused
+    const double bs = modal_block_sum((double)dsum2);
+    if (t == 0) ch.dotp2[cta] = bs;
   }
 }
 
@@ -1014,7 +1031,7 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb, int tz) {
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0, nullptr, nullptr};
   if (residual) launch_modal<T, 1>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
   else launch_modal<T, 0>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
 }
@@ -1029,7 +1046,7 @@ int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, con
   const dim3 grid = modal_grid<T>(d, tz, 1);
   const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
   if (nparts > cap) return 0;
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0, nullptr, nullptr};
   launch_modal<T, 0>(s, d, rhop, vmask, u, nullptr, out, tz, 1, ch);
   return (int)nparts;
 }
@@ -1063,20 +1080,27 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
 
 // One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u).
 template <typename T>
-void launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
-                      int tz, bool d_is_u) {
-  // the FP64 kernel always reads d
-  const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nullptr, (d_is_u && sizeof(T) == 4) ? 1 : 0};
+int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
+                     const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
+                     int tz, bool d_is_u, double* dot_fo, double* dot_ow, const T* w2, int cap) {
+  // the FP64 kernel always reads d and has no fused dots
+  int nparts = 0;
+  if (sizeof(T) == 4 && dot_fo && nb == 1) {
+    const dim3 grid = modal_grid<T>(d, tz <= 0 ? MODAL_TZ : tz, 1);
+    nparts = (int64_t)grid.x * grid.y * grid.z <= cap ? (int)(grid.x * grid.y * grid.z) : 0;
+  }
+  const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nparts ? dot_fo : nullptr,
+                    (d_is_u && sizeof(T) == 4) ? 1 : 0, nparts ? dot_ow : nullptr, w2};
   launch_modal<T, 2>(s, d, rhop, vmask, u, f, uout, tz, nb, ch);
+  return nparts;
 }
 
-template void launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
-                                       const double*, const double*, double*, const double*, double*, double,
-                                       double, bool, int, int, bool);
-template void launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
-                                      const float*, const float*, float*, const float*, float*, double, double,
-                                      bool, int, int, bool);
+template int launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
+                                      const double*, const double*, double*, const double*, double*, double,
+                                      double, bool, int, int, bool, double*, double*, const double*, int);
+template int launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
+                                     const float*, const float*, float*, const float*, float*, double, double,
+                                     bool, int, int, bool, double*, double*, const float*, int);
 
 // First Chebyshev step from a zero iterate (every pre-smoothing sweep of a
 // preconditioning V-cycle starts from u = 0): K u vanishes, so r = f on the

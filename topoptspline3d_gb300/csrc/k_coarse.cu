@@ -823,7 +823,6 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
   __shared__ df spd[DFC ? GJB : 1][GJB + 1];
   __shared__ double sc[GJB][GJB + 1];
   __shared__ double sp[GJB][GJB + 1];
-  __shared__ int sflag;
   double* P = work + GJB * GJB;      // [GJB][n]
   double* Cp = P + (int64_t)GJB * n; // [n][GJB]
   const int tid = threadIdx.x;
@@ -833,40 +832,31 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
   const int nblk_tiles = (n + GJB - 1) / GJB;
   for (int k0 = 0; k0 < n; k0 += GJB) {
     const int kb = min(GJB, n - k0);
-    // ---- A: invert the diagonal block D = A[K,K] into sd.
-    // DFC: every CTA inverts it in its own shared memory in double-float (the
-    // same data and operations, so the same result and pivot decisions
-    // everywhere, and no barrier across CTAs before phase B; FP64 arithmetic
-    // here would load every SM's narrow FP64 pipe with the same n GJB^2 work).
-    // FP64: CTA 0 inverts it and publishes it through the work array.
-    if (DFC || blockIdx.x == 0) {
+    // ---- A: CTA 0 inverts the diagonal block D = A[K,K] in FP64 and publishes
+    // it through the work array.  (Measured alternatives on GB300 at n = 675:
+    // every CTA inverting its own copy saves one grid barrier per panel but ran
+    // at 2.4 ms in FP64, every SM's narrow FP64 pipe then carrying the panel
+    // work, and at 2.6 ms in double-float, whose pivot steps lengthen the serial
+    // chain; this form runs at 2.0 ms.)
+    if (blockIdx.x == 0) {
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        const double v = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
-        if constexpr (DFC) scd[r][c] = df_from(v);
-        else sd[r][c] = v;
+        sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
       }
-      if (tid == 0) sflag = 0;
       __syncthreads();
       for (int j = 0; j < kb; ++j) {
-        double p;
-        if constexpr (DFC) p = df_to(scd[j][j]);
-        else p = sd[j][j];
+        const double p = sd[j][j];
         if (p < -tol) {
-          if (tid == 0) {
-            sflag = 1;
-            if (blockIdx.x == 0) status[1] = k0 + j + 1;
-          }
+          if (tid == 0) status[1] = k0 + j + 1;
           break;
         }
         __syncthreads();
         if (p <= tol) {  // drop DOF k0 + j
           for (int e = tid; e < 2 * GJB; e += blockDim.x) {
-            const int r = e < GJB ? j : e - GJB, c = e < GJB ? e : j;
-            if constexpr (DFC) scd[r][c] = df_from(0.0);
-            else sd[r][c] = 0.0;
+            if (e < GJB) sd[j][e] = 0.0;
+            else sd[e - GJB][j] = 0.0;
           }
-          if (tid == 0 && blockIdx.x == 0) status[0] += 1;
+          if (tid == 0) status[0] += 1;
           __syncthreads();
           continue;
         }
@@ -874,46 +864,24 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         double rp = (double)__frcp_rn((float)p);
         rp = fma(rp, fma(-p, rp, 1.0), rp);
         rp = fma(rp, fma(-p, rp, 1.0), rp);
-        if constexpr (DFC) {
-          const df rpd = df_from(rp);
-          for (int e = tid; e < GJB * GJB; e += blockDim.x) {
-            const int r = e / GJB, c = e % GJB;
-            if (r < kb && c < kb && r != j && c != j) scd[r][c] = scd[r][c] - scd[r][j] * scd[j][c] * rpd;
-          }
-          __syncthreads();
-          for (int e = tid; e < 2 * kb; e += blockDim.x) {
-            if (e < kb) { if (e != j) scd[j][e] = scd[j][e] * rpd; else scd[j][j] = rpd; }
-            else { const int r = e - kb; if (r != j) scd[r][j] = df_from(0.0) - scd[r][j] * rpd; }
-          }
-        } else {
-          for (int e = tid; e < GJB * GJB; e += blockDim.x) {
-            const int r = e / GJB, c = e % GJB;
-            if (r < kb && c < kb && r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
-          }
-          __syncthreads();
-          for (int e = tid; e < 2 * kb; e += blockDim.x) {
-            if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
-            else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
-          }
+        for (int e = tid; e < GJB * GJB; e += blockDim.x) {
+          const int r = e / GJB, c = e % GJB;
+          if (r < kb && c < kb && r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
+        }
+        __syncthreads();
+        for (int e = tid; e < 2 * kb; e += blockDim.x) {
+          if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
+          else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
         }
         __syncthreads();
       }
       __syncthreads();
-      if constexpr (DFC) {
-        for (int e = tid; e < GJB * GJB; e += blockDim.x) sd[e / GJB][e % GJB] = df_to(scd[e / GJB][e % GJB]);
-      } else {
-        for (int e = tid; e < GJB * GJB; e += blockDim.x) work[e] = sd[e / GJB][e % GJB];
-      }
+      for (int e = tid; e < GJB * GJB; e += blockDim.x) work[e] = sd[e / GJB][e % GJB];
     }
-    if constexpr (DFC) {
-      __syncthreads();
-      if (sflag) return;  // indefinite pivot: every CTA found it in its own copy
-    } else {
-      grid.sync();
-      if (status[1]) return;  // indefinite pivot: every CTA sees it after the barrier
-      for (int e = tid; e < GJB * GJB; e += blockDim.x) sd[e / GJB][e % GJB] = work[e];
-      __syncthreads();
-    }
+    grid.sync();
+    if (status[1]) return;  // indefinite pivot: every CTA sees it after the barrier
+    for (int e = tid; e < GJB * GJB; e += blockDim.x) sd[e / GJB][e % GJB] = work[e];
+    __syncthreads();
     // ---- B: row panel P = D^-1 A[K,:] (columns outside K) and column panel C = A[:,K]
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + tid, gs = (int64_t)gridDim.x * blockDim.x;
     for (int64_t e = gt; e < (int64_t)kb * n; e += gs) {

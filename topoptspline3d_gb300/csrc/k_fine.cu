@@ -188,9 +188,9 @@ struct ChebArgs {
   void* dvec;        // [3][nv]
   double c_old, c_new;
   int first;
-  double* dotp;      // per-CTA partial sums: MODE 0 u.out, MODE 2 (FP32) f.out (null: none)
+  double* dotp;      // per-CTA partial sums: MODE 0 u.out, FP32 MODE 3 f.out (null: none)
   int d_is_u;        // MODE 2, FP32: d equals u on entry (the step after a zero start); dvec is not read
-  double* dotp2;     // MODE 2, FP32: per-CTA partial sums of out.w2 (null: none)
+  double* dotp2;     // FP32 MODE 3: per-CTA partial sums of out.w2
   const void* w2;
 };
 
@@ -490,11 +490,13 @@ struct Modal32Smem {
 };
 
 template <int TYE, int MODE>
-__global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ? TOPO_FINE32_CHEB_THREADS_PER_SM
+__global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ? TOPO_FINE32_CHEB_THREADS_PER_SM
                                                                                : TOPO_FINE32_THREADS_PER_SM))
     k_fine_modal32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
                    const float* __restrict__ u, const float* __restrict__ f, float* __restrict__ out, int TZ,
                    ChebArgs ch) {
+  // MODE 3: the Chebyshev step of MODE 2 that also sums f.out and out.w2
+  constexpr bool CHEB = MODE >= 2, DOTS = MODE == 3;
   using S = Modal32Smem<TYE>;
   constexpr int TXE = 32, NT = S::NT, PX = S::PX, NP = S::NP;
   extern __shared__ __align__(16) unsigned char m32_smem[];
@@ -544,9 +546,9 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
     return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (int64_t)d.ex * (pey + (int64_t)d.ey * ez)] : 0.f;
   };
   const float* __restrict__ dvin =
-      (MODE == 2 && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
+      (CHEB && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
   // operands of the owned vertex at plane z, read in step z and used in step z + 1
-  const float* __restrict__ w2 = (MODE == 2 && ch.dotp2) ? static_cast<const float*>(ch.w2) : nullptr;
+  const float* __restrict__ w2 = DOTS ? static_cast<const float*>(ch.w2) : nullptr;
   uint8_t vm_n = 0;
   float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f}, w_n[3] = {0.f, 0.f, 0.f};
   auto load_vertex = [&](int z) {
@@ -557,16 +559,16 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
 #pragma unroll
       for (int c = 0; c < 3; ++c) f_n[c] = f[c * nv + v];
     }
-    if (MODE == 2 && dvin) {
+    if (CHEB && dvin) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) dv_n[c] = dvin[c * nv + v];
     }
-    if (MODE == 2 && w2) {
+    if (DOTS && w2) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) w_n[c] = w2[c * nv + v];
     }
   };
-  float dsum2 = 0.f;  // MODE 2 with ch.dotp2: this thread's share of out.w2
+  float dsum2 = 0.f;  // MODE 3: this thread's share of out.w2
   float own1[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // own y = 1 forces of the last layer, z = 0 / 1
   float top[3] = {0.f, 0.f, 0.f};                          // z = 1 forces of the layer below the last
   float uo[3] = {0.f, 0.f, 0.f};                           // owned vertex's own value at the last layer's plane
@@ -603,7 +605,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
           const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * p);
           const uint8_t m = vm_c;
           const float uv[3] = {uo[0], uo[1], uo[2]};
-          if (MODE < 2) {
+          if (!CHEB) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const bool fr = (m >> c) & 1;
@@ -627,8 +629,10 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
               dv[c * nv + v] = dn;
               const float o = uv[c] + dn;
               out[c * nv + v] = o;
-              dsum += f_c[c] * o;
-              dsum2 += o * w_c[c];
+              if (DOTS) {
+                dsum += f_c[c] * o;
+                dsum2 += o * w_c[c];
+              }
             }
           }
         }
@@ -636,7 +640,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
     }
     // ---- element layer st
     if (st < zend) {
-      if (MODE == 2 || (MODE == 0 && ch.dotp)) {
+      if (CHEB || (MODE == 0 && ch.dotp)) {
         const float4 q = sm.plane[(st + 4) & 3][(i + 1) + PX * (j + 1)];
         uo[0] = q.x; uo[1] = q.y; uo[2] = q.z;
       }
@@ -674,11 +678,11 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE == 2 ?
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   const int64_t cta = blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z);
-  if (MODE != 1 && ch.dotp) {
+  if ((MODE == 0 || DOTS) && ch.dotp) {
     const double bs = modal_block_sum((double)dsum);
     if (t == 0) ch.dotp[cta] = bs;
   }
-  if (MODE == 2 && ch.dotp2) {
+  if (DOTS && ch.dotp2) {
     __syncthreads();  // the block sum's scratch is reused
     const double bs = modal_block_sum((double)dsum2);
     if (t == 0) ch.dotp2[cta] = bs;
@@ -1091,6 +1095,12 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
   }
   const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nparts ? dot_fo : nullptr,
                     (d_is_u && sizeof(T) == 4) ? 1 : 0, nparts ? dot_ow : nullptr, w2};
+  if constexpr (sizeof(T) == 4) {
+    if (nparts) {  // the step with the fused sums is its own instantiation
+      launch_modal<T, 3>(s, d, rhop, vmask, u, f, uout, tz, nb, ch);
+      return nparts;
+    }
+  }
   launch_modal<T, 2>(s, d, rhop, vmask, u, f, uout, tz, nb, ch);
   return nparts;
 }

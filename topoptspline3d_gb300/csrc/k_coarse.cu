@@ -830,55 +830,60 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
   for (int k = 0; k < n; ++k) dmax = fmax(dmax, fabs(A[(int64_t)k * n + k]));
   const double tol = 1e-10 * dmax;
   const int nblk_tiles = (n + GJB - 1) / GJB;
-  for (int k0 = 0; k0 < n; k0 += GJB) {
+  // ---- A: CTA 0 inverts a diagonal block D = A[K,K] (K = [k0, k0 + GJB)) in
+  // FP64 and publishes it through the work array.  The block of panel k + 1
+  // is inverted during panel k's update (look-ahead): CTA 0 updates that one
+  // tile first and inverts it while the other CTAs update the rest.
+  // (Measured alternatives on GB300 at n = 675: every CTA inverting its own
+  // copy saves a grid barrier but ran at 2.4 ms in FP64, every SM's narrow
+  // FP64 pipe then carrying the panel work, and at 2.6 ms in double-float,
+  // whose pivot steps lengthen the serial chain; inverting between the update
+  // phases ran at 1.9 ms.)
+  auto panel_invert = [&](int k0) {
     const int kb = min(GJB, n - k0);
-    // ---- A: CTA 0 inverts the diagonal block D = A[K,K] in FP64 and publishes
-    // it through the work array.  (Measured alternatives on GB300 at n = 675:
-    // every CTA inverting its own copy saves one grid barrier per panel but ran
-    // at 2.4 ms in FP64, every SM's narrow FP64 pipe then carrying the panel
-    // work, and at 2.6 ms in double-float, whose pivot steps lengthen the serial
-    // chain; this form runs at 2.0 ms.)
-    if (blockIdx.x == 0) {
+    for (int e = tid; e < GJB * GJB; e += blockDim.x) {
+      const int r = e / GJB, c = e % GJB;
+      sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+      const double p = sd[j][j];
+      if (p < -tol) {
+        if (tid == 0) status[1] = k0 + j + 1;
+        break;
+      }
+      __syncthreads();
+      if (p <= tol) {  // drop DOF k0 + j
+        for (int e = tid; e < 2 * GJB; e += blockDim.x) {
+          if (e < GJB) sd[j][e] = 0.0;
+          else sd[e - GJB][j] = 0.0;
+        }
+        if (tid == 0) status[0] += 1;
+        __syncthreads();
+        continue;
+      }
+      // 1/p: FP32 estimate refined by two Newton steps r <- r + r (1 - p r)
+      double rp = (double)__frcp_rn((float)p);
+      rp = fma(rp, fma(-p, rp, 1.0), rp);
+      rp = fma(rp, fma(-p, rp, 1.0), rp);
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        sd[r][c] = (r < kb && c < kb) ? A[(int64_t)(k0 + r) * n + k0 + c] : 0.0;
+        if (r < kb && c < kb && r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
       }
       __syncthreads();
-      for (int j = 0; j < kb; ++j) {
-        const double p = sd[j][j];
-        if (p < -tol) {
-          if (tid == 0) status[1] = k0 + j + 1;
-          break;
-        }
-        __syncthreads();
-        if (p <= tol) {  // drop DOF k0 + j
-          for (int e = tid; e < 2 * GJB; e += blockDim.x) {
-            if (e < GJB) sd[j][e] = 0.0;
-            else sd[e - GJB][j] = 0.0;
-          }
-          if (tid == 0) status[0] += 1;
-          __syncthreads();
-          continue;
-        }
-        // 1/p: FP32 estimate refined by two Newton steps r <- r + r (1 - p r)
-        double rp = (double)__frcp_rn((float)p);
-        rp = fma(rp, fma(-p, rp, 1.0), rp);
-        rp = fma(rp, fma(-p, rp, 1.0), rp);
-        for (int e = tid; e < GJB * GJB; e += blockDim.x) {
-          const int r = e / GJB, c = e % GJB;
-          if (r < kb && c < kb && r != j && c != j) sd[r][c] -= sd[r][j] * sd[j][c] * rp;
-        }
-        __syncthreads();
-        for (int e = tid; e < 2 * kb; e += blockDim.x) {
-          if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
-          else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
-        }
-        __syncthreads();
+      for (int e = tid; e < 2 * kb; e += blockDim.x) {
+        if (e < kb) { if (e != j) sd[j][e] *= rp; else sd[j][j] = rp; }
+        else { const int r = e - kb; if (r != j) sd[r][j] *= -rp; }
       }
       __syncthreads();
-      for (int e = tid; e < GJB * GJB; e += blockDim.x) work[e] = sd[e / GJB][e % GJB];
     }
-    grid.sync();
+    __syncthreads();
+    for (int e = tid; e < GJB * GJB; e += blockDim.x) work[e] = sd[e / GJB][e % GJB];
+  };
+  if (blockIdx.x == 0) panel_invert(0);
+  grid.sync();
+  for (int k0 = 0; k0 < n; k0 += GJB) {
+    const int kb = min(GJB, n - k0);
     if (status[1]) return;  // indefinite pivot: every CTA sees it after the barrier
     for (int e = tid; e < GJB * GJB; e += blockDim.x) sd[e / GJB][e % GJB] = work[e];
     __syncthreads();
@@ -898,8 +903,17 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
       Cp[(int64_t)i * GJB + m] = (i < k0 || i >= k0 + kb) ? A[(int64_t)i * n + k0 + m] : 0.0;
     }
     grid.sync();
-    // ---- C: rank-kb update, GJB x GJB tiles of A per CTA iteration
-    for (int t = blockIdx.x; t < nblk_tiles * nblk_tiles; t += gridDim.x) {
+    // ---- C: rank-kb update, GJB x GJB tiles of A.  With a next panel, CTA 0
+    // takes only its diagonal tile and then inverts it; the others share the
+    // rest.
+    const int k1 = k0 + GJB, tn = k1 < n ? (k1 / GJB) * (nblk_tiles + 1) : -1;
+    const bool ahead = tn >= 0 && gridDim.x > 1;
+    const int t_first = ahead ? (blockIdx.x == 0 ? tn : (int)blockIdx.x - 1) : (int)blockIdx.x;
+    const int t_step = ahead ? (blockIdx.x == 0 ? nblk_tiles * nblk_tiles : (int)gridDim.x - 1) : (int)gridDim.x;
+    for (int t0 = t_first; t0 < nblk_tiles * nblk_tiles; t0 += t_step) {
+      // the CTAs other than 0 skip the diagonal tile of the next panel
+      const int t = (ahead && blockIdx.x != 0 && t0 >= tn) ? t0 + 1 : t0;
+      if (t >= nblk_tiles * nblk_tiles) break;
       const int ti = (t / nblk_tiles) * GJB, tc = (t % nblk_tiles) * GJB;
       __syncthreads();
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
@@ -936,6 +950,10 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
           a = v;
         }
       }
+    }
+    if (k1 < n && blockIdx.x == 0) {
+      __syncthreads();  // the tile's updates are visible to the whole CTA
+      panel_invert(k1);
     }
     grid.sync();
   }

@@ -113,7 +113,8 @@ struct topo_handle {
   double* vdot = nullptr;
   bool vdot_on = false;
   double* vdot_out[2] = {nullptr, nullptr};
-  const float* vdot_w2 = nullptr;
+  const float* vdot_w2 = nullptr;  // null: only r.z (vdot_out[1] is left alone)
+  bool inner_fr = false;           // inner CG in Fletcher-Reeves form (z.rold taken as 0)
   double* sc = nullptr;    // device scalar slots
   double* hsc = nullptr;   // pinned host mirror
   int64_t active_elements = 0, gs_padded_elements = 0;
@@ -359,19 +360,20 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bo
       const int np = launch_fine_cheb<T>(
           h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), c_old, c_new,
           k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr,
-          dots ? h->vdot + h->fdot_cap : nullptr, dots ? reinterpret_cast<const T*>(h->vdot_w2) : nullptr,
+          (dots && h->vdot_w2) ? h->vdot + h->fdot_cap : nullptr,
+          dots ? reinterpret_cast<const T*>(h->vdot_w2) : nullptr,
           h->fdot_cap);
       prof_end(h, ev);
       if (dots) {
-        if (np > 0) {  // r.z and z.rold of the cycle's result (F is r, the output is z)
+        const T* w2 = reinterpret_cast<const T*>(h->vdot_w2);
+        if (np > 0) {  // r.z (and z.rold) of the cycle's result (F is r, the output is z)
           launch_finalize_sum(h->stream, h->vdot, np, h->vdot_out[0]);
-          launch_finalize_sum(h->stream, h->vdot + h->fdot_cap, np, h->vdot_out[1]);
+          if (w2) launch_finalize_sum(h->stream, h->vdot + h->fdot_cap, np, h->vdot_out[1]);
         } else {
           launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out[0]);
-          launch_dot<T>(h->stream, ub, reinterpret_cast<const T*>(h->vdot_w2), 3 * L.d.nv, h->partial,
-                        h->vdot_out[1]);
+          if (w2) launch_dot<T>(h->stream, ub, w2, 3 * L.d.nv, h->partial, h->vdot_out[1]);
         }
-        count_launch(2);
+        count_launch(w2 ? 2 : 1);
       }
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
@@ -671,8 +673,10 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
       count_launch(2);
     }
     launch_scalar_ratio(h->stream, sc, S_RZ, -1, S_DQ, S_ALPHA);
-    // x += alpha d, rold = r, r -= alpha q with r.r of the new residual
-    launch_pcg_update_rr<T>(h->stream, x, r, rold, d, q, sc, S_ALPHA, n3, h->partial, sc + S_RR);
+    // x += alpha d, rold = r, r -= alpha q with r.r of the new residual; rold
+    // is not kept when the preconditioner runs the plain (Fletcher-Reeves) form
+    launch_pcg_update_rr<T>(h->stream, x, r, (prec_dots && h->inner_fr) ? nullptr : rold, d, q, sc, S_ALPHA, n3,
+                            h->partial, sc + S_RR);
     CK(cudaMemcpyAsync(sc + S_RZOLD, sc + S_RZ, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     count_launch(it > 0 ? 5 : 4);
     CKL();
@@ -1361,9 +1365,12 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       ++st.learned_applied;
       return TOPO_OK;
     };
-    // The inner CG's r.z and z.rold: from the V-cycle's last Chebyshev step when
-    // it is a fine FP32 Chebyshev step and no network correction follows, else
-    // by separate dots after the cycle.
+    // The inner CG's r.z: from the V-cycle's last Chebyshev step when it is a
+    // fine FP32 Chebyshev step and no network correction follows.  The cycle
+    // is then a fixed symmetric linear operator, and the inner CG takes the
+    // plain Fletcher-Reeves form (z.rold = 0, rold not kept).  With the
+    // network (a varying preconditioner) it stays flexible, with separate
+    // r.z and z.rold after the cycle.
     const bool vdots = o->smoother == TOPO_SMOOTH_CHEBYSHEV && o->post >= 1 && cp.degree >= 1 && h->nb == 1;
     auto prec32 = [&](const float* r, float* z) -> int {
       (void)z;
@@ -1371,9 +1378,11 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       double* s_rz = h->sc + 8 + S_RZ;
       double* s_zr = h->sc + 8 + S_ZROLD;
       h->vdot_on = vdots && !net_on;
+      h->inner_fr = h->vdot_on;
       h->vdot_out[0] = s_rz;
       h->vdot_out[1] = s_zr;
-      h->vdot_w2 = h->rold32;
+      h->vdot_w2 = nullptr;
+      if (h->inner_fr) CK(cudaMemsetAsync(s_zr, 0, sizeof(double), h->stream));
       const int rc = vcycle_prec<float>(h, r, o->pre, o->post, o->smoother, cp);
       const bool fused = h->vdot_on;
       h->vdot_on = false;

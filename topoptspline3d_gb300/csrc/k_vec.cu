@@ -235,13 +235,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_rr(T* __restrict__ x
       rn.v[k] = rp.v[k] - alpha * qp.v[k];
       acc += rn.v[k] * rn.v[k];
     }
-    reinterpret_cast<P*>(rold)[i] = rp;
+    if (rold) reinterpret_cast<P*>(rold)[i] = rp;
     reinterpret_cast<P*>(x)[i] = xn;
     reinterpret_cast<P*>(r)[i] = rn;
   }
   for (int64_t i = npk * W + gid; i < n; i += gs) {
     const T ri = r[i];
-    rold[i] = ri;
+    if (rold) rold[i] = ri;
     x[i] = x[i] + alpha * d[i];
     const T rn = ri - alpha * q[i];
     r[i] = rn;

@@ -170,7 +170,8 @@ void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta
 template <typename T>
 void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q,
                        const double* sc, int alpha_slot, int64_t n);
-// launch_pcg_update fused with rr = r.r of the updated residual (2 launches)
+// launch_pcg_update fused with rr = r.r of the updated residual (2 launches);
+// rold may be null (not kept)
 template <typename T>
 void launch_pcg_update_rr(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
                           int alpha_slot, int64_t n, double* partial, double* rr);

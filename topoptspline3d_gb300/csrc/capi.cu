@@ -108,13 +108,12 @@ struct topo_handle {
   double* partial = nullptr;
   double* fdot = nullptr;  // per-CTA partials of the fine operator's fused dot
   int fdot_cap = 0;
-  // inner CG: the FP32 V-cycle's last Chebyshev step also forms r.z and z.rold
-  // (partials in vdot[0, 2 fdot_cap)) when vdot_on; the sums land in vdot_out[0..1]
+  // inner CG: the FP32 V-cycle's last Chebyshev step also forms r.z (partials
+  // in vdot) when vdot_on; the sum lands in *vdot_out
   double* vdot = nullptr;
   bool vdot_on = false;
-  double* vdot_out[2] = {nullptr, nullptr};
-  const float* vdot_w2 = nullptr;  // null: only r.z (vdot_out[1] is left alone)
-  bool inner_fr = false;           // inner CG in Fletcher-Reeves form (z.rold taken as 0)
+  double* vdot_out = nullptr;
+  bool inner_fr = false;  // inner CG in Fletcher-Reeves form (z.rold taken as 0)
   double* sc = nullptr;    // device scalar slots
   double* hsc = nullptr;   // pinned host mirror
   int64_t active_elements = 0, gs_padded_elements = 0;
@@ -360,20 +359,12 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bo
       const int np = launch_fine_cheb<T>(
           h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), c_old, c_new,
           k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr,
-          (dots && h->vdot_w2) ? h->vdot + h->fdot_cap : nullptr,
-          dots ? reinterpret_cast<const T*>(h->vdot_w2) : nullptr,
           h->fdot_cap);
       prof_end(h, ev);
-      if (dots) {
-        const T* w2 = reinterpret_cast<const T*>(h->vdot_w2);
-        if (np > 0) {  // r.z (and z.rold) of the cycle's result (F is r, the output is z)
-          launch_finalize_sum(h->stream, h->vdot, np, h->vdot_out[0]);
-          if (w2) launch_finalize_sum(h->stream, h->vdot + h->fdot_cap, np, h->vdot_out[1]);
-        } else {
-          launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out[0]);
-          if (w2) launch_dot<T>(h->stream, ub, w2, 3 * L.d.nv, h->partial, h->vdot_out[1]);
-        }
-        count_launch(w2 ? 2 : 1);
+      if (dots) {  // r.z of the cycle's result (F is r, the output is z)
+        if (np > 0) launch_finalize_sum(h->stream, h->vdot, np, h->vdot_out);
+        else launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out);
+        count_launch(np > 0 ? 1 : 2);
       }
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
@@ -470,7 +461,7 @@ static void vcycle32(topo_handle* h, int pre, int post, int smoother, const Cheb
   prof_collect(h);
   std::vector<double> key = {(double)pre, (double)post, (double)smoother, (double)cp.degree, cp.lo, cp.hi,
                              (double)h->tz32, (double)h->nb, (double)h->prof, (double)zero0,
-                             (double)h->vdot_on, (double)(uintptr_t)h->vdot_w2};
+                             (double)h->vdot_on, (double)(uintptr_t)h->vdot_out};
   for (const DevLevel& L : h->lv) {
     key.push_back(L.lmax32);
     key.push_back((double)(uintptr_t)L.U32);
@@ -819,7 +810,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     // tiles (31 x 7 owned vertices) at z-march depths of 4 and more
     h->fdot_cap = (int)std::min<int64_t>(1 << 24, (int64_t)((d0.vx + 30) / 31) * ((d0.vy + 6) / 7) * ((d0.vz + 3) / 4));
     A(dalloc(hp, &h->fdot, h->fdot_cap));
-    A(dalloc(hp, &h->vdot, 2 * (int64_t)h->fdot_cap));
+    A(dalloc(hp, &h->vdot, h->fdot_cap));
   }
   if (rc == TOPO_OK && nl > 1) {
     const LevelDims& dl = h->lv.back().d;
@@ -1379,9 +1370,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       double* s_zr = h->sc + 8 + S_ZROLD;
       h->vdot_on = vdots && !net_on;
       h->inner_fr = h->vdot_on;
-      h->vdot_out[0] = s_rz;
-      h->vdot_out[1] = s_zr;
-      h->vdot_w2 = nullptr;
+      h->vdot_out = s_rz;
       if (h->inner_fr) CK(cudaMemsetAsync(s_zr, 0, sizeof(double), h->stream));
       const int rc = vcycle_prec<float>(h, r, o->pre, o->post, o->smoother, cp);
       const bool fused = h->vdot_on;

@@ -190,8 +190,6 @@ struct ChebArgs {
   int first;
   double* dotp;      // per-CTA partial sums: MODE 0 u.out, FP32 MODE 3 f.out (null: none)
   int d_is_u;        // MODE 2, FP32: d equals u on entry (the step after a zero start); dvec is not read
-  double* dotp2;     // FP32 MODE 3: per-CTA partial sums of out.w2
-  const void* w2;
 };
 
 // Sum of v over the CTA (valid in thread 0); every thread must call it.
@@ -495,7 +493,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
     k_fine_modal32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
                    const float* __restrict__ u, const float* __restrict__ f, float* __restrict__ out, int TZ,
                    ChebArgs ch) {
-  // MODE 3: the Chebyshev step of MODE 2 that also sums f.out and out.w2
+  // MODE 3: the Chebyshev step of MODE 2 that also sums f.out
   constexpr bool CHEB = MODE >= 2, DOTS = MODE == 3;
   using S = Modal32Smem<TYE>;
   constexpr int TXE = 32, NT = S::NT, PX = S::PX, NP = S::NP;
@@ -548,9 +546,8 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   const float* __restrict__ dvin =
       (CHEB && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
   // operands of the owned vertex at plane z, read in step z and used in step z + 1
-  const float* __restrict__ w2 = DOTS ? static_cast<const float*>(ch.w2) : nullptr;
   uint8_t vm_n = 0;
-  float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f}, w_n[3] = {0.f, 0.f, 0.f};
+  float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f};
   auto load_vertex = [&](int z) {
     if (!own || z < z0 || z >= zend) return;
     const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * z);
@@ -563,12 +560,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
 #pragma unroll
       for (int c = 0; c < 3; ++c) dv_n[c] = dvin[c * nv + v];
     }
-    if (DOTS && w2) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) w_n[c] = w2[c * nv + v];
-    }
   };
-  float dsum2 = 0.f;  // MODE 3: this thread's share of out.w2
   float own1[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // own y = 1 forces of the last layer, z = 0 / 1
   float top[3] = {0.f, 0.f, 0.f};                          // z = 1 forces of the layer below the last
   float uo[3] = {0.f, 0.f, 0.f};                           // owned vertex's own value at the last layer's plane
@@ -581,9 +573,9 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
     prefetch(st + 2);
     const float pe = pe_n;
     const uint8_t vm_c = vm_n;
-    float f_c[3], dv_c[3], w_c[3];
+    float f_c[3], dv_c[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; w_c[c] = w_n[c]; }
+    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
     if (st + 1 < zend) pe_n = load_pe(st + 1);
     load_vertex(st);
     cp_async_wait1();
@@ -629,10 +621,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
               dv[c * nv + v] = dn;
               const float o = uv[c] + dn;
               out[c * nv + v] = o;
-              if (DOTS) {
-                dsum += f_c[c] * o;
-                dsum2 += o * w_c[c];
-              }
+              if (DOTS) dsum += f_c[c] * o;
             }
           }
         }
@@ -681,11 +670,6 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   if ((MODE == 0 || DOTS) && ch.dotp) {
     const double bs = modal_block_sum((double)dsum);
     if (t == 0) ch.dotp[cta] = bs;
-  }
-  if (DOTS && ch.dotp2) {
-    __syncthreads();  // the block sum's scratch is reused
-    const double bs = modal_block_sum((double)dsum2);
-    if (t == 0) ch.dotp2[cta] = bs;
   }
 }
 
@@ -1035,7 +1019,7 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb, int tz) {
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0, nullptr, nullptr};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0};
   if (residual) launch_modal<T, 1>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
   else launch_modal<T, 0>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
 }
@@ -1050,7 +1034,7 @@ int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, con
   const dim3 grid = modal_grid<T>(d, tz, 1);
   const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
   if (nparts > cap) return 0;
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0, nullptr, nullptr};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0};
   launch_modal<T, 0>(s, d, rhop, vmask, u, nullptr, out, tz, 1, ch);
   return (int)nparts;
 }
@@ -1086,7 +1070,7 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
 template <typename T>
 int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
-                     int tz, bool d_is_u, double* dot_fo, double* dot_ow, const T* w2, int cap) {
+                     int tz, bool d_is_u, double* dot_fo, int cap) {
   // the FP64 kernel always reads d and has no fused dots
   int nparts = 0;
   if (sizeof(T) == 4 && dot_fo && nb == 1) {
@@ -1094,7 +1078,7 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
     nparts = (int64_t)grid.x * grid.y * grid.z <= cap ? (int)(grid.x * grid.y * grid.z) : 0;
   }
   const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nparts ? dot_fo : nullptr,
-                    (d_is_u && sizeof(T) == 4) ? 1 : 0, nparts ? dot_ow : nullptr, w2};
+                    (d_is_u && sizeof(T) == 4) ? 1 : 0};
   if constexpr (sizeof(T) == 4) {
     if (nparts) {  // the step with the fused sums is its own instantiation
       launch_modal<T, 3>(s, d, rhop, vmask, u, f, uout, tz, nb, ch);
@@ -1107,10 +1091,10 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
 
 template int launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                       const double*, const double*, double*, const double*, double*, double,
-                                      double, bool, int, int, bool, double*, double*, const double*, int);
+                                      double, bool, int, int, bool, double*, int);
 template int launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
                                      const float*, const float*, float*, const float*, float*, double, double,
-                                     bool, int, int, bool, double*, double*, const float*, int);
+                                     bool, int, int, bool, double*, int);
 
 // First Chebyshev step from a zero iterate (every pre-smoothing sweep of a
 // preconditioning V-cycle starts from u = 0): K u vanishes, so r = f on the

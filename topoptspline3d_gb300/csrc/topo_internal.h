@@ -92,14 +92,13 @@ template <typename T>
 void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                           T* dinv);
 // FP32, one right-hand side: with dot_fo the kernel also leaves per-CTA partial
-// sums of f.uout in dot_fo and of uout.w2 in dot_ow (when w2 is given); returns
-// their count (sum them with launch_finalize_sum), or 0 when none were formed
-// (FP64, a batch, or more CTAs than cap).
+// sums of f.uout in dot_fo; returns their count (sum them with
+// launch_finalize_sum), or 0 when none were formed (FP64, a batch, or more
+// CTAs than cap).
 template <typename T>
 int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first,
-                     int nb = 1, int tz = 0, bool d_is_u = false, double* dot_fo = nullptr,
-                     double* dot_ow = nullptr, const T* w2 = nullptr, int cap = 0);
+                     int nb = 1, int tz = 0, bool d_is_u = false, double* dot_fo = nullptr, int cap = 0);
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);

@@ -108,6 +108,9 @@ struct topo_handle {
   double* partial = nullptr;
   double* fdot = nullptr;  // per-CTA partials of the fine operator's fused dot
   int fdot_cap = 0;
+  // ticket counter of the reductions whose last block writes the total (the
+  // handle's stream runs them one at a time; the last block resets it)
+  unsigned* ctr = nullptr;
   // inner CG: the FP32 V-cycle's last Chebyshev step also forms r.z (partials
   // in vdot) when vdot_on; the sum lands in *vdot_out
   double* vdot = nullptr;
@@ -359,12 +362,11 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bo
       const int np = launch_fine_cheb<T>(
           h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), c_old, c_new,
           k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr,
-          h->fdot_cap);
+          h->fdot_cap, h->vdot_out, h->ctr);
       prof_end(h, ev);
-      if (dots) {  // r.z of the cycle's result (F is r, the output is z)
-        if (np > 0) launch_finalize_sum(h->stream, h->vdot, np, h->vdot_out);
-        else launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out);
-        count_launch(np > 0 ? 1 : 2);
+      if (dots && np == 0) {  // r.z of the cycle's result (F is r, the output is z), unfused
+        launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out, h->ctr);
+        count_launch();
       }
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
@@ -563,14 +565,14 @@ int estimate_lmax(topo_handle* h, int l, double* out) {
   // Rayleigh estimate (s x).z = s (x.z); x <- z.
   auto power_steps = [&](int k) {
     for (int it = 0; it < k; ++it) {
-      launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP);
+      launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP, h->ctr);
       if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, x, nullptr, y, false, 1,
                                        sizeof(T) == 4 ? h->tz32 : h->tz64);
       else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), x, nullptr, y, false);
       k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), y, z, h->sc + S_TMP);
-      launch_dot<T>(h->stream, x, z, n3, h->partial, h->sc + S_TMP + 1);
+      launch_dot<T>(h->stream, x, z, n3, h->partial, h->sc + S_TMP + 1, h->ctr);
       std::swap(x, z);
-      count_launch(6);
+      count_launch(4);
     }
   };
   double lam = 0.0;
@@ -629,8 +631,8 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
   } else {
     level_apply<T>(h, 0, x, b, r, true);  // r = b - A x
   }
-  launch_dot<T>(h->stream, r, r, n3, h->partial, sc + S_RR);
-  count_launch(2);
+  launch_dot<T>(h->stream, r, r, n3, h->partial, sc + S_RR, h->ctr);
+  count_launch();
   RET(read_scalars(h, base + S_RR, 1));
   double rn = std::sqrt(h->hsc[base + S_RR]);
   const double bn = bnorm_ref;
@@ -638,11 +640,11 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
   while (rn / bn > rtol && it < maxit) {
     RET(prec(r, z));
     if (!prec_dots) {  // else the preconditioner left r.z and z.rold in the scalar slots
-      launch_dot<T>(h->stream, r, z, n3, h->partial, sc + S_RZ);
-      count_launch(2);
+      launch_dot<T>(h->stream, r, z, n3, h->partial, sc + S_RZ, h->ctr);
+      count_launch();
       if (it > 0) {
-        launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD);
-        count_launch(2);
+        launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD, h->ctr);
+        count_launch();
       }
     }
     if (it > 0) launch_scalar_ratio(h->stream, sc, S_RZ, S_ZROLD, S_RZOLD, S_BETA);
@@ -652,24 +654,23 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
     if (sizeof(T) == 4 && h->fdot && h->nb == 1) {
       EventPair* ev = prof_begin(h, P<T>::fam_apply);
       nparts = launch_fine_apply_dot<T>(h->stream, L0.d, P<T>::rhop(h), L0.vmask, d, q, h->tz32, h->fdot,
-                                        h->fdot_cap);
+                                        h->fdot_cap, sc + S_DQ, h->ctr);
       prof_end(h, ev);
     }
     if (nparts > 0) {
-      launch_finalize_sum(h->stream, h->fdot, nparts, sc + S_DQ);
-      count_launch(2);
+      count_launch();
     } else {
       level_apply<T>(h, 0, d, nullptr, q, false);
-      launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ);
-      count_launch(2);
+      launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ, h->ctr);
+      count_launch();
     }
     launch_scalar_ratio(h->stream, sc, S_RZ, -1, S_DQ, S_ALPHA);
     // x += alpha d, rold = r, r -= alpha q with r.r of the new residual; rold
     // is not kept when the preconditioner runs the plain (Fletcher-Reeves) form
     launch_pcg_update_rr<T>(h->stream, x, r, (prec_dots && h->inner_fr) ? nullptr : rold, d, q, sc, S_ALPHA, n3,
-                            h->partial, sc + S_RR);
+                            h->partial, sc + S_RR, h->ctr);
     CK(cudaMemcpyAsync(sc + S_RZOLD, sc + S_RZ, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-    count_launch(it > 0 ? 5 : 4);
+    count_launch(it > 0 ? 4 : 3);
     CKL();
     RET(read_scalars(h, base + S_RR, 1));
     rn = std::sqrt(h->hsc[base + S_RR]);
@@ -811,6 +812,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     h->fdot_cap = (int)std::min<int64_t>(1 << 24, (int64_t)((d0.vx + 30) / 31) * ((d0.vy + 6) / 7) * ((d0.vz + 3) / 4));
     A(dalloc(hp, &h->fdot, h->fdot_cap));
     A(dalloc(hp, &h->vdot, h->fdot_cap));
+    A(dalloc(hp, &h->ctr, 1));
   }
   if (rc == TOPO_OK && nl > 1) {
     const LevelDims& dl = h->lv.back().d;
@@ -1378,9 +1380,9 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       RET(rc);
       RET(net(r, L0.U32));
       if (!fused) {
-        launch_dot<float>(h->stream, r, L0.U32, n3, h->partial, s_rz);
-        launch_dot<float>(h->stream, L0.U32, h->rold32, n3, h->partial, s_zr);
-        count_launch(4);
+        launch_dot<float>(h->stream, r, L0.U32, n3, h->partial, s_rz, h->ctr);
+        launch_dot<float>(h->stream, L0.U32, h->rold32, n3, h->partial, s_zr, h->ctr);
+        count_launch(2);
       }
       return TOPO_OK;
     };
@@ -1463,8 +1465,8 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     } else {
       level_residual<double>(h, 0);
     }
-    launch_dot<double>(h->stream, L0.R, L0.R, n3, h->partial, h->sc + S_RR);
-    count_launch(2);
+    launch_dot<double>(h->stream, L0.R, L0.R, n3, h->partial, h->sc + S_RR, h->ctr);
+    count_launch();
     RET(read_scalars(h, S_RR, 1));
     st.relres = std::sqrt(h->hsc[S_RR]) / fn;
   }

@@ -190,9 +190,32 @@ struct ChebArgs {
   int first;
   double* dotp;      // per-CTA partial sums: MODE 0 u.out, FP32 MODE 3 f.out (null: none)
   int d_is_u;        // MODE 2, FP32: d equals u on entry (the step after a zero start); dvec is not read
+  double* dot;       // with ctr: the last CTA sums the partials into *dot
+  unsigned* ctr;     // zeroed ticket counter (reset by the last CTA)
 };
 
 // Sum of v over the CTA (valid in thread 0); every thread must call it.
+__device__ __forceinline__ double modal_block_sum(double v);
+
+// After thread 0 of every CTA published its partial: the CTA that takes the last
+// ticket sums the n partials in index order (independent of which CTA is last)
+// into *out and resets the counter.  Every thread must call it.
+__device__ __forceinline__ void modal_finish_sum(const double* partial, int64_t n, double* out, unsigned* ctr) {
+  __shared__ bool last;
+  __threadfence();
+  if (threadIdx.x == 0) last = atomicAdd(ctr, 1u) == (unsigned)(n - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(partial + i);
+  s = modal_block_sum(s);
+  if (threadIdx.x == 0) {
+    *out = s;
+    *ctr = 0u;
+  }
+}
+
 __device__ __forceinline__ double modal_block_sum(double v) {
   __shared__ double ws[32];
 #pragma unroll
@@ -670,6 +693,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   if ((MODE == 0 || DOTS) && ch.dotp) {
     const double bs = modal_block_sum((double)dsum);
     if (t == 0) ch.dotp[cta] = bs;
+    if (ch.ctr) modal_finish_sum(ch.dotp, (int64_t)gridDim.x * gridDim.y * gridDim.z, ch.dot, ch.ctr);
   }
 }
 
@@ -1019,7 +1043,7 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb, int tz) {
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0, nullptr, nullptr};
   if (residual) launch_modal<T, 1>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
   else launch_modal<T, 0>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
 }
@@ -1029,20 +1053,20 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
 // CTAs than the cap partial slots.
 template <typename T>
 int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                          T* out, int tz, double* partial, int cap) {
+                          T* out, int tz, double* partial, int cap, double* dot, unsigned* ctr) {
   if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid = modal_grid<T>(d, tz, 1);
   const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
   if (nparts > cap) return 0;
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0};
+  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0, dot, dot ? ctr : nullptr};
   launch_modal<T, 0>(s, d, rhop, vmask, u, nullptr, out, tz, 1, ch);
   return (int)nparts;
 }
 
 template int launch_fine_apply_dot<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
-                                          const float*, float*, int, double*, int);
+                                          const float*, float*, int, double*, int, double*, unsigned*);
 template int launch_fine_apply_dot<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
-                                           const double*, double*, int, double*, int);
+                                           const double*, double*, int, double*, int, double*, unsigned*);
 
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
                           const double* u, const double* f, double* out, bool residual, int nb, int tz,
@@ -1070,7 +1094,7 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
 template <typename T>
 int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
-                     int tz, bool d_is_u, double* dot_fo, int cap) {
+                     int tz, bool d_is_u, double* dot_fo, int cap, double* dot, unsigned* ctr) {
   // the FP64 kernel always reads d and has no fused dots
   int nparts = 0;
   if (sizeof(T) == 4 && dot_fo && nb == 1) {
@@ -1078,7 +1102,7 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
     nparts = (int64_t)grid.x * grid.y * grid.z <= cap ? (int)(grid.x * grid.y * grid.z) : 0;
   }
   const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nparts ? dot_fo : nullptr,
-                    (d_is_u && sizeof(T) == 4) ? 1 : 0};
+                    (d_is_u && sizeof(T) == 4) ? 1 : 0, dot, (nparts && dot) ? ctr : nullptr};
   if constexpr (sizeof(T) == 4) {
     if (nparts) {  // the step with the fused sums is its own instantiation
       launch_modal<T, 3>(s, d, rhop, vmask, u, f, uout, tz, nb, ch);
@@ -1091,10 +1115,10 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
 
 template int launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                       const double*, const double*, double*, const double*, double*, double,
-                                      double, bool, int, int, bool, double*, int);
+                                      double, bool, int, int, bool, double*, int, double*, unsigned*);
 template int launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
                                      const float*, const float*, float*, const float*, float*, double, double,
-                                     bool, int, int, bool, double*, int);
+                                     bool, int, int, bool, double*, int, double*, unsigned*);
 
 // First Chebyshev step from a zero iterate (every pre-smoothing sweep of a
 // preconditioning V-cycle starts from u = 0): K u vanishes, so r = f on the

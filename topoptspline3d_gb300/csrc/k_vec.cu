@@ -39,17 +39,42 @@ __device__ __forceinline__ double block_sum(double v) {
   return s;  // valid in thread 0
 }
 
+// Completion by the last block: each block's thread 0 has published its partial;
+// every block then takes a ticket, and the block with the last one sums all nb
+// partials in index order (the order of k_finalize_sum, so the result does not
+// depend on which block finishes last) and resets the counter for the next use.
+// Saves the separate finalising launch.  ctr: one counter per stream in order.
+__device__ __forceinline__ void finish_sum(const double* partial, int nb, double* out, unsigned* ctr) {
+  __shared__ bool last;
+  __threadfence();
+  if (threadIdx.x == 0) last = atomicAdd(ctr, 1u) == (unsigned)(nb - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += __ldcg(partial + i);
+  s = block_sum(s);
+  if (threadIdx.x == 0) {
+    *out = s;
+    *ctr = 0u;
+  }
+}
+
 // Per-thread partial sums are accumulated in the vector's precision (FP32
 // vectors: a few dozen terms per thread, inside the FP32 inner solver only) and
-// combined in FP64 across threads and blocks.
+// combined in FP64 across threads and blocks.  With ctr the last block also
+// writes the total to out.
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_dot_partial(const T* __restrict__ a, const T* __restrict__ b,
-                                                             int64_t n, double* __restrict__ partial) {
+                                                             int64_t n, double* __restrict__ partial,
+                                                             double* __restrict__ out = nullptr,
+                                                             unsigned* __restrict__ ctr = nullptr) {
   T s = T(0);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     s += a[i] * (b ? b[i] : T(1));
   const double bs = block_sum((double)s);
   if (threadIdx.x == 0) partial[blockIdx.x] = bs;
+  if (ctr) finish_sum(partial, gridDim.x, out, ctr);
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_finalize_sum(const double* __restrict__ partial, int nb,
@@ -86,10 +111,14 @@ __global__ void k_finalize_max(const double* __restrict__ partial, int nb, doubl
 }
 
 template <typename T>
-void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out) {
+void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out, unsigned* ctr) {
   const int nb = reduce_blocks(n);
-  k_dot_partial<T><<<nb, RED_THREADS, 0, s>>>(a, b, n, partial);
-  k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, out);
+  if (ctr) {
+    k_dot_partial<T><<<nb, RED_THREADS, 0, s>>>(a, b, n, partial, out, ctr);
+  } else {
+    k_dot_partial<T><<<nb, RED_THREADS, 0, s>>>(a, b, n, partial);
+    k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, out);
+  }
 }
 
 void launch_sum(cudaStream_t s, const double* a, int64_t n, double* partial, double* out) {
@@ -218,7 +247,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_rr(T* __restrict__ x
                                                                T* __restrict__ rold, const T* __restrict__ d,
                                                                const T* __restrict__ q, const double* __restrict__ sc,
                                                                int alpha_slot, int64_t n, double* __restrict__ partial,
-                                                               int packed) {
+                                                               int packed, double* __restrict__ rr, unsigned* __restrict__ ctr) {
   constexpr int W = 16 / sizeof(T);
   using P = Pack16<T, W>;
   const T alpha = (T)sc[alpha_slot];
@@ -249,22 +278,24 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update_rr(T* __restrict__ x
   }
   const double bs = block_sum((double)acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = bs;
+  if (ctr) finish_sum(partial, gridDim.x, rr, ctr);
 }
 
 template <typename T>
 void launch_pcg_update_rr(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
-                          int alpha_slot, int64_t n, double* partial, double* rr) {
+                          int alpha_slot, int64_t n, double* partial, double* rr, unsigned* ctr) {
   // 16-byte packs when all five vectors start on 16-byte boundaries
   const uintptr_t al = (uintptr_t)x | (uintptr_t)r | (uintptr_t)rold | (uintptr_t)d | (uintptr_t)q;
   const int nb = reduce_blocks(n);
-  k_pcg_update_rr<T><<<nb, RED_THREADS, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n, partial, (al & 15) == 0);
-  k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, rr);
+  k_pcg_update_rr<T><<<nb, RED_THREADS, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n, partial, (al & 15) == 0,
+                                                 rr, ctr);
+  if (!ctr) k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, rr);
 }
 
 template void launch_pcg_update_rr<double>(cudaStream_t, double*, double*, double*, const double*, const double*,
-                                           const double*, int, int64_t, double*, double*);
+                                           const double*, int, int64_t, double*, double*, unsigned*);
 template void launch_pcg_update_rr<float>(cudaStream_t, float*, float*, float*, const float*, const float*,
-                                          const double*, int, int64_t, double*, double*);
+                                          const double*, int, int64_t, double*, double*, unsigned*);
 
 void launch_finalize_sum(cudaStream_t s, const double* partial, int nb, double* out) {
   k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, out);
@@ -288,8 +319,8 @@ void launch_scale_by_rnorm(cudaStream_t s, const T* y, T* x, const double* sc, i
 template void launch_scale_by_rnorm<double>(cudaStream_t, const double*, double*, const double*, int, int64_t);
 template void launch_scale_by_rnorm<float>(cudaStream_t, const float*, float*, const double*, int, int64_t);
 
-template void launch_dot<double>(cudaStream_t, const double*, const double*, int64_t, double*, double*);
-template void launch_dot<float>(cudaStream_t, const float*, const float*, int64_t, double*, double*);
+template void launch_dot<double>(cudaStream_t, const double*, const double*, int64_t, double*, double*, unsigned*);
+template void launch_dot<float>(cudaStream_t, const float*, const float*, int64_t, double*, double*, unsigned*);
 template void launch_fill<double>(cudaStream_t, double*, double, int64_t);
 template void launch_fill<float>(cudaStream_t, float*, float, int64_t);
 template void launch_copy<double>(cudaStream_t, const double*, double*, int64_t);

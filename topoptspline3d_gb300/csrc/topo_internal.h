@@ -79,7 +79,7 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
 // launches nothing when the kernel would need more than cap partial slots.
 template <typename T>
 int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                          T* out, int tz, double* partial, int cap);
+                          T* out, int tz, double* partial, int cap, double* dot = nullptr, unsigned* ctr = nullptr);
 // FP64 vectors, double-float arithmetic (k_fine_modal_df)
 // energy (residual only, one right-hand side): per-element u_e . (rho^p Ke u_e)
 void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
@@ -98,7 +98,8 @@ void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, con
 template <typename T>
 int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first,
-                     int nb = 1, int tz = 0, bool d_is_u = false, double* dot_fo = nullptr, int cap = 0);
+                     int nb = 1, int tz = 0, bool d_is_u = false, double* dot_fo = nullptr, int cap = 0,
+                     double* dot = nullptr, unsigned* ctr = nullptr);
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);
@@ -152,7 +153,9 @@ void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* 
 // vectors and reductions (k_vec.cu)
 int reduce_blocks(int64_t n);
 template <typename T>
-void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out);
+// ctr (optional): a zeroed counter; the last block then writes out itself (one launch)
+void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out,
+                unsigned* ctr = nullptr);
 // b == nullptr sums a.
 void launch_sum(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);
 void launch_axpby(cudaStream_t s, double a, const double* x, double b, double* y, int64_t n);
@@ -173,7 +176,7 @@ void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T*
 // rold may be null (not kept)
 template <typename T>
 void launch_pcg_update_rr(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
-                          int alpha_slot, int64_t n, double* partial, double* rr);
+                          int alpha_slot, int64_t n, double* partial, double* rr, unsigned* ctr = nullptr);
 // out = sum of nb partials in a fixed order
 void launch_finalize_sum(cudaStream_t s, const double* partial, int nb, double* out);
 template <typename T>

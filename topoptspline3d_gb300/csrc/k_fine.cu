@@ -202,11 +202,13 @@ __device__ __forceinline__ double modal_block_sum(double v);
 // into *out and resets the counter.  Every thread must call it.
 __device__ __forceinline__ void modal_finish_sum(const double* partial, int64_t n, double* out, unsigned* ctr) {
   __shared__ bool last;
-  __threadfence();
-  if (threadIdx.x == 0) last = atomicAdd(ctr, 1u) == (unsigned)(n - 1);
+  if (threadIdx.x == 0) {  // thread 0 wrote the block's partial: fence, then take a ticket
+    __threadfence();
+    last = atomicAdd(ctr, 1u) == (unsigned)(n - 1);
+    if (last) __threadfence();
+  }
   __syncthreads();
   if (!last) return;
-  __threadfence();
   double s = 0.0;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(partial + i);
   s = modal_block_sum(s);

@@ -46,11 +46,13 @@ __device__ __forceinline__ double block_sum(double v) {
 // Saves the separate finalising launch.  ctr: one counter per stream in order.
 __device__ __forceinline__ void finish_sum(const double* partial, int nb, double* out, unsigned* ctr) {
   __shared__ bool last;
-  __threadfence();
-  if (threadIdx.x == 0) last = atomicAdd(ctr, 1u) == (unsigned)(nb - 1);
+  if (threadIdx.x == 0) {  // thread 0 wrote the block's partial: fence, then take a ticket
+    __threadfence();
+    last = atomicAdd(ctr, 1u) == (unsigned)(nb - 1);
+    if (last) __threadfence();
+  }
   __syncthreads();
   if (!last) return;
-  __threadfence();
   double s = 0.0;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) s += __ldcg(partial + i);
   s = block_sum(s);

@@ -103,6 +103,7 @@ struct topo_handle {
   double filt_radius = -1.0;
   int4* filt_offs = nullptr;
   double* filt_w = nullptr;
+  float2* filt_wdf = nullptr;  // the weights split into (hi, lo) floats
   int filt_n = 0;
   // reductions
   double* partial = nullptr;
@@ -881,6 +882,7 @@ void topo_destroy(topo_handle* h) {
   if (h->filt_offs) cudaFree(h->filt_offs);
   if (h->timer_ev[0]) { cudaEventDestroy(h->timer_ev[0]); cudaEventDestroy(h->timer_ev[1]); }
   if (h->filt_w) cudaFree(h->filt_w);
+  if (h->filt_wdf) cudaFree(h->filt_wdf);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -1006,6 +1008,19 @@ int topo_set_spline(topo_handle* h, int order, const int* partition3, const doub
     CK(cudaMemcpyAsync(lo, h->st.lo[a].data(), sizeof(int) * sd.nb[a], cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(hi, h->st.hi[a].data(), sizeof(int) * sd.nb[a], cudaMemcpyHostToDevice, h->stream));
     sd.i0[a] = i0; sd.N[a] = N; sd.lo[a] = lo; sd.hi[a] = hi;
+  }
+  {  // x-axis basis values split for the double-float density pass
+    std::vector<float2> ndf(h->st.N[0].size());
+    for (size_t k = 0; k < ndf.size(); ++k) {
+      const double v = h->st.N[0][k];
+      const float hi = (float)v;
+      ndf[k] = make_float2(hi, (float)(v - (double)hi));
+    }
+    float2* Nx = nullptr;
+    RET(dalloc(h, &Nx, (int64_t)ndf.size()));
+    CK(cudaMemcpyAsync(Nx, ndf.data(), sizeof(float2) * ndf.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    sd.Nx_df = Nx;
   }
   const int64_t nc = (int64_t)sd.nb[0] * sd.nb[1] * sd.nb[2];
   RET(dalloc(h, &h->coeff, nc));
@@ -1524,17 +1539,26 @@ int topo_filter(topo_handle* h, double radius) {
     filter_table(radius, offs, w);
     if (h->filt_offs) { cudaFree(h->filt_offs); h->filt_offs = nullptr; }
     if (h->filt_w) { cudaFree(h->filt_w); h->filt_w = nullptr; }
+    if (h->filt_wdf) { cudaFree(h->filt_wdf); h->filt_wdf = nullptr; }
+    std::vector<float2> wdf(w.size());
+    for (size_t k = 0; k < w.size(); ++k) {
+      const float hi = (float)w[k];
+      wdf[k] = make_float2(hi, (float)(w[k] - (double)hi));
+    }
     CK(cudaMalloc((void**)&h->filt_offs, sizeof(int4) * offs.size()));
     CK(cudaMalloc((void**)&h->filt_w, sizeof(double) * w.size()));
+    CK(cudaMalloc((void**)&h->filt_wdf, sizeof(float2) * w.size()));
     CK(cudaMemcpyAsync(h->filt_offs, offs.data(), sizeof(int4) * offs.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->filt_w, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->filt_wdf, wdf.data(), sizeof(float2) * w.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->filt_n = (int)offs.size();
     h->filt_radius = radius;
   }
-  CK(cudaMemcpyAsync(h->sens_tmp, h->sens, sizeof(double) * L.d.ne, cudaMemcpyDeviceToDevice, h->stream));
-  launch_filter(h->stream, L.d, L.eactive, h->sens_tmp, h->sens, h->filt_offs, h->filt_w, h->filt_n);
-  count_launch();
+  // double-float on the FP32 pipe, sens_tmp holding the split sensitivities
+  launch_filter_df(h->stream, L.d, L.eactive, h->sens, reinterpret_cast<float2*>(h->sens_tmp), h->filt_offs,
+                   h->filt_wdf, h->filt_n);
+  count_launch(2);
   CKL();
   return TOPO_OK;
 }

@@ -79,9 +79,10 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int nb, doubl
 }
 
 // Separable evaluation, pass 1: B[z][y][i] = sum_{s,t} c[i, iy+s, iz+t] Ny[y][s] Nz[z][t]
-// for every x-basis index i (0 where y or z is outside the spline range).
+// for every x-basis index i (0 where y or z is outside the spline range), in
+// FP64, stored split into (hi, lo) floats for the double-float pass 2.
 __global__ void k_spline_yz(LevelDims d, SplineDev sp, const double* __restrict__ coeff,
-                            double* __restrict__ B) {
+                            float2* __restrict__ B) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int nbx = sp.nb[0];
   if (gid >= (int64_t)nbx * d.ey * d.ez) return;
@@ -100,23 +101,47 @@ __global__ void k_spline_yz(LevelDims d, SplineDev sp, const double* __restrict_
       v += ns * a;
     }
   }
-  B[gid] = v;
+  const df vd = df_from(v);
+  B[gid] = make_float2(vd.hi, vd.lo);
 }
 
-// Pass 2: value at element (x,y,z) = sum_r Nx[x][r] B[z][y][ix + r], or -0.2 out of range.
-__device__ __forceinline__ double spline_from_B(const SplineDev& sp, const double* __restrict__ B,
-                                                int x, int y, int z, int ey) {
+// Pass 2: value at element (x,y,z) = sum_r Nx[x][r] B[z][y][ix + r], or -0.2 out of
+// range, in double-float arithmetic (about 1e-15 relative; FP64 here would be
+// bound by GB300's FP64 pipe, and each OC bisection trial evaluates it on every
+// element).
+__device__ __forceinline__ df spline_from_B(const SplineDev& sp, const float2* __restrict__ B,
+                                            int x, int y, int z, int ey) {
   const int ix = sp.i0[0][x];
-  if (ix < 0 || sp.i0[1][y] < 0 || sp.i0[2][z] < 0) return -0.2;
+  if (ix < 0 || sp.i0[1][y] < 0 || sp.i0[2][z] < 0) return df_from(-0.2);
   const int k = sp.order;
-  const double* b = B + (int64_t)sp.nb[0] * (y + (int64_t)ey * z) + ix;
-  double v = 0.0;
-  for (int r = 0; r < k; ++r) v += sp.N[0][x * k + r] * b[r];
+  const float2* b = B + (int64_t)sp.nb[0] * (y + (int64_t)ey * z) + ix;
+  df v(0);
+  for (int r = 0; r < k; ++r) {
+    const float2 n = sp.Nx_df[x * k + r], bb = b[r];
+    v += df(n.x, n.y) * df(bb.x, bb.y);
+  }
   return v;
 }
 
+// (x, y, z) of element e, in 32-bit arithmetic when the grid allows
+__device__ __forceinline__ void elem_xyz(const LevelDims& d, int64_t e, int& x, int& y, int& z) {
+  if (d.ne < (int64_t)1 << 31) {
+    const unsigned ee = (unsigned)e, ex = (unsigned)d.ex, t = ee / ex;
+    x = (int)(ee - t * ex);
+    y = (int)(t % (unsigned)d.ey);
+    z = (int)(t / (unsigned)d.ey);
+  } else {
+    x = (int)(e % d.ex);
+    const int64_t t = e / d.ex;
+    y = (int)(t % d.ey);
+    z = (int)(t / d.ey);
+  }
+}
+
+__device__ __forceinline__ bool df_lt(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+
 __global__ void k_density_from_B(LevelDims d, const uint8_t* __restrict__ eactive, SplineDev sp,
-                                 const double* __restrict__ B, double rho_min, double penal,
+                                 const float2* __restrict__ B, double rho_min, double penal,
                                  double* __restrict__ rho, double* __restrict__ rhop, float* __restrict__ rhop32) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.ne) return;
@@ -124,25 +149,28 @@ __global__ void k_density_from_B(LevelDims d, const uint8_t* __restrict__ eactiv
     rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
     return;
   }
-  const int x = (int)(e % d.ex);
-  const int64_t t = e / d.ex;
-  const int y = (int)(t % d.ey), z = (int)(t / d.ey);
-  const double v = fmin(fmax(spline_from_B(sp, B, x, y, z, d.ey), rho_min), 1.0);
+  int x, y, z;
+  elem_xyz(d, e, x, y, z);
+  const double v = fmin(fmax(df_to(spline_from_B(sp, B, x, y, z, d.ey)), rho_min), 1.0);
   const double vp = simp_pow(v, penal);
   rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
 }
 
 __global__ void __launch_bounds__(VOL_THREADS) k_volume_from_B(LevelDims d, const uint8_t* __restrict__ eactive,
-                                                               SplineDev sp, const double* __restrict__ B,
+                                                               SplineDev sp, const float2* __restrict__ B,
                                                                double rho_min, double* __restrict__ partial) {
-  double s = 0.0;
+  const df lo = df_from(rho_min), one(1.f, 0.f);
+  df sd(0);
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < d.ne; e += (int64_t)gridDim.x * blockDim.x) {
     if (!eactive[e]) continue;
-    const int x = (int)(e % d.ex);
-    const int64_t t = e / d.ex;
-    const int y = (int)(t % d.ey), z = (int)(t / d.ey);
-    s += fmin(fmax(spline_from_B(sp, B, x, y, z, d.ey), rho_min), 1.0);
+    int x, y, z;
+    elem_xyz(d, e, x, y, z);
+    df v = spline_from_B(sp, B, x, y, z, d.ey);
+    if (df_lt(v, lo)) v = lo;
+    if (df_lt(one, v)) v = one;
+    sd += v;
   }
+  double s = df_to(sd);
   __shared__ double ws[VOL_THREADS / 32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -159,18 +187,20 @@ void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* 
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,
                              double* rho, double* rhop, float* rhop32, double* Btmp) {
   const int64_t nB = (int64_t)sp.nb[0] * d.ey * d.ez;
-  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, Btmp);
-  k_density_from_B<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, Btmp, rho_min, penal, rho, rhop, rhop32);
+  float2* B = reinterpret_cast<float2*>(Btmp);  // nB (hi, lo) pairs in the nB-double scratch
+  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, B);
+  k_density_from_B<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, B, rho_min, penal, rho, rhop, rhop32);
 }
 
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                          const SplineDev& sp, const double* coeff, double rho_min, double* partial,
                          double* out, double* Btmp) {
   const int64_t nB = (int64_t)sp.nb[0] * d.ey * d.ez;
-  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, Btmp);
+  float2* B = reinterpret_cast<float2*>(Btmp);  // nB (hi, lo) pairs in the nB-double scratch
+  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, B);
   int nb = (int)std::min<int64_t>(1024, (d.ne + VOL_THREADS * 4 - 1) / (VOL_THREADS * 4));
   if (nb < 1) nb = 1;
-  k_volume_from_B<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, Btmp, rho_min, partial);
+  k_volume_from_B<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, partial);
   k_sum_partials<<<1, 256, 0, s>>>(partial, nb, out);
 }
 
@@ -315,6 +345,65 @@ __global__ void k_filter(LevelDims d, const uint8_t* __restrict__ eactive, const
 void launch_filter(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* src,
                    double* dst, const int4* offs, const double* wts, int noffs) {
   k_filter<<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, src, dst, offs, wts, noffs);
+}
+
+// The same filter in double-float arithmetic (about 1e-14 relative): the
+// sensitivities and weights arrive split into (hi, lo) floats, the weighted
+// sums run on the FP32 pipe, and the quotient is a double-float division
+// (FP32 quotient, one correction from the double-float remainder; Dekker
+// 1971).  The FP64 form is bound by GB300's FP64 pipe (66 FP64 operations
+// per element).
+__device__ __forceinline__ df df_div(df a, df b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const df r = a - b * df(q1, 0.f);
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  return df_fast2sum(q1, q2);
+}
+
+__global__ void k_to_df(int64_t n, const double* __restrict__ a, float2* __restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const df v = df_from(a[i]);
+  b[i] = make_float2(v.hi, v.lo);
+}
+
+__global__ void k_filter_df(LevelDims d, const uint8_t* __restrict__ eactive, const float2* __restrict__ src,
+                            double* __restrict__ dst, const int4* __restrict__ offs,
+                            const float2* __restrict__ wts, int noffs) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.ne) return;
+  if (!eactive[e]) { dst[e] = 0.0; return; }
+  int x, y, z;
+  if (d.ne < (int64_t)1 << 31) {  // 32-bit index arithmetic
+    const unsigned ee = (unsigned)e, ex = (unsigned)d.ex, t = ee / ex;
+    x = (int)(ee - t * ex);
+    y = (int)(t % (unsigned)d.ey);
+    z = (int)(t / (unsigned)d.ey);
+  } else {
+    x = (int)(e % d.ex);
+    const int64_t t = e / d.ex;
+    y = (int)(t % d.ey);
+    z = (int)(t / d.ey);
+  }
+  df ws(0), gs(0);
+  for (int k = 0; k < noffs; ++k) {
+    const int4 o = offs[k];
+    const int nx = x + o.x, ny = y + o.y, nz = z + o.z;
+    if (nx < 0 || ny < 0 || nz < 0 || nx >= d.ex || ny >= d.ey || nz >= d.ez) continue;
+    const int64_t n = nx + (int64_t)d.ex * (ny + (int64_t)d.ey * nz);
+    if (!eactive[n]) continue;
+    const float2 wv = wts[k], sv = src[n];
+    const df w(wv.x, wv.y);
+    gs += w * df(sv.x, sv.y);
+    ws += w;
+  }
+  dst[e] = df_to(df_div(gs, ws));
+}
+
+void launch_filter_df(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, double* sens,
+                      float2* sens_df, const int4* offs, const float2* wts, int noffs) {
+  k_to_df<<<nblk(d.ne, 256), 256, 0, s>>>(d.ne, sens, sens_df);
+  k_filter_df<<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, sens_df, sens, offs, wts, noffs);
 }
 
 // Ball offsets within r^2 <= R^2, R_int = floor(R + 0.5), weight

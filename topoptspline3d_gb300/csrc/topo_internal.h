@@ -188,6 +188,7 @@ struct SplineDev {
   int nb[3];
   const int* i0[3];      // device [n_axis]: first basis index of each element slice, -1 out of range
   const double* N[3];    // device [n_axis][order]: basis values at the element centres
+  const float2* Nx_df;   // device [n_x][order]: x-axis values split into (hi, lo) floats
   const int* lo[3];      // device [nb]: first element slice in the support of basis i
   const int* hi[3];      // device [nb]: one past the last element slice
 };
@@ -221,6 +222,10 @@ void launch_sensitivity_from_energy(cudaStream_t s, int64_t ne, const uint8_t* e
                                     double penal, double* sens);
 void launch_filter(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* src,
                    double* dst, const int4* offs, const double* wts, int noffs);
+// The same filter in double-float, in place on sens (sens_df: ne float2 scratch;
+// wts: the weights split into (hi, lo) floats)
+void launch_filter_df(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, double* sens,
+                      float2* sens_df, const int4* offs, const float2* wts, int noffs);
 void filter_table(double R, std::vector<int4>& offs, std::vector<double>& w);
 void launch_spline_adjoint(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                            const SplineDev& sp, const double* sens, double* csens, double* tmp1,

@@ -102,12 +102,64 @@ __device__ __forceinline__ void wht_bwd(T v[8]) {
       }
 }
 
+// The transforms of the three displacement components.  FP32: components 0
+// and 1 go through the packed two-lane FP32 instructions of sm_100 and later
+// (__fadd2_rn, __ffma2_rn; per lane the same rounding as the scalar forms, so
+// the results are identical), which halves their instruction count in an
+// issue-bound kernel.
+template <typename T>
+__device__ __forceinline__ void wht3_fwd(T c[3][8]) {
+  wht_fwd<T>(c[0]); wht_fwd<T>(c[1]); wht_fwd<T>(c[2]);
+}
+template <typename T>
+__device__ __forceinline__ void wht3_bwd(T g[3][8]) {
+  wht_bwd<T>(g[0]); wht_bwd<T>(g[1]); wht_bwd<T>(g[2]);
+}
+template <>
+__device__ __forceinline__ void wht3_fwd<float>(float c[3][8]) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  float2 p[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) p[a] = make_float2(c[0][a], c[1][a]);
+#pragma unroll
+  for (int hb = 1; hb < 8; hb <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (!(i & hb)) {
+        const float2 a = p[i], b = p[i | hb];
+        p[i] = __fadd2_rn(a, b);
+        p[i | hb] = __ffma2_rn(a, m1, b);  // b - a
+      }
+#pragma unroll
+  for (int a = 0; a < 8; ++a) { c[0][a] = p[a].x; c[1][a] = p[a].y; }
+  wht_fwd<float>(c[2]);
+}
+template <>
+__device__ __forceinline__ void wht3_bwd<float>(float g[3][8]) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  float2 p[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) p[a] = make_float2(g[0][a], g[1][a]);
+#pragma unroll
+  for (int hb = 1; hb < 8; hb <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (!(i & hb)) {
+        const float2 a = p[i], b = p[i | hb];
+        p[i] = __ffma2_rn(b, m1, a);  // a - b
+        p[i | hb] = __fadd2_rn(a, b);
+      }
+#pragma unroll
+  for (int a = 0; a < 8; ++a) { g[0][a] = p[a].x; g[1][a] = p[a].y; }
+  wht_bwd<float>(g[2]);
+}
+
 // In: c[3][8] nodal values per component.  Out: c[3][8] nodal forces of pe*Ke*u.
 // EN: also *energy = u . (pe Ke u) = sum over modes of (transformed u) . (modal
 // force), since the backward transform is the forward one's transpose.
 template <typename T, bool EN = false>
 __device__ __forceinline__ void modal_element(T c[3][8], T pe, T* energy = nullptr) {
-  wht_fwd<T>(c[0]); wht_fwd<T>(c[1]); wht_fwd<T>(c[2]);
+  wht3_fwd<T>(c);
   const T L = modal_c<T>(0) * pe, M = modal_c<T>(1) * pe;
   const T k0 = modal_c<T>(2), k1 = modal_c<T>(3), k2 = modal_c<T>(4);
   T g[3][8];
@@ -165,12 +217,11 @@ __device__ __forceinline__ void modal_element(T c[3][8], T pe, T* energy = nullp
       for (int a = 1; a < 8; ++a) e += c[i][a] * g[i][a];  // g[i][0] = 0: rigid translation
     *energy = e;
   }
+  wht3_bwd<T>(g);
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    wht_bwd<T>(g[i]);
+  for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int a = 0; a < 8; ++a) c[i][a] = g[i][a];
-  }
 }
 
 // y = K(rho) u (or f - K u) on level 0.  A CTA owns a (TXE-1) x (TYE-1) column of

@@ -506,11 +506,14 @@ def main():
     nv, ne = (d0[0] + 1) * (d0[1] + 1) * (d0[2] + 1), d0[0] * d0[1] * d0[2]
     fams = {capi.K_FINE_APPLY64: ("k_fine_modal_df (FP64 K.u in double-float, outer CG)",
                                   nv * (24 + 24 + 1) + ne * 8, ne * 240.0),
-            # u in, f in, d in/out, u out (FP32 x3 each), vertex mask, the stored
-            # 3x3 block-Jacobi inverse (FP32 x9), rho^p
-            capi.K_FINE_SMOOTH32: ("k_fine_modal<float, Chebyshev> (FP32 smoother step)",
-                                   nv * (12 + 12 + 24 + 12 + 1 + 36) + ne * 4, ne * 240.0 + nv * 30.0),
-            capi.K_FINE_APPLY32: ("k_fine_modal<float> (FP32 K.u)", nv * (12 + 12 + 1) + ne * 4, ne * 240.0),
+            # u in, f in, d out, u out (FP32 x3 each), vertex mask, the stored 3x3
+            # block-Jacobi inverse (FP32 x9), rho^p; d is read by one step in three
+            # (a V(1,1) degree-2 cycle's pre-smoothing second step takes d from u,
+            # the post-smoothing first step starts it)
+            capi.K_FINE_SMOOTH32: ("k_fine_modal32<8,2|3> (FP32 Chebyshev step)",
+                                   nv * (12 + 12 + 12 + 12 + 12 / 3 + 1 + 36) + ne * 4, ne * 240.0 + nv * 30.0),
+            capi.K_FINE_APPLY32: ("k_fine_modal32<8,0|1> (FP32 K.u, residual)", nv * (12 + 12 + 1) + ne * 4,
+                                  ne * 240.0),
             capi.K_FINE_SMOOTH64: ("k_fine_gs<double>", nv * (24 + 24 + 24 + 1) + ne * 8, nv * 1170.0)}
     dom = max(prof, key=lambda k: prof[k][1])
     name, bytes_per, flops_per = fams[dom]

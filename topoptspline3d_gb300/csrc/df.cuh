@@ -49,4 +49,28 @@ __device__ __forceinline__ df df_from(double x) {
 }
 __device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.lo; }
 
+// Two double-float values in the lanes of the packed two-lane FP32 instructions
+// of sm_100 and later (__fadd2_rn, __ffma2_rn, __fmul2_rn): per lane the same
+// operations and roundings as the scalar forms above, so the results are
+// identical, with half the instructions.
+struct df2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {  // a - b, one rounding
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ df2 df2_add(df2 a, df2 b) {
+  const float2 s = f2_add(a.hi, b.hi);
+  const float2 bb = f2_sub(s, a.hi);
+  const float2 e = f2_add(f2_sub(a.hi, f2_sub(s, bb)), f2_sub(b.hi, bb));
+  const float2 t = f2_add(e, f2_add(a.lo, b.lo));
+  const float2 s2 = f2_add(s, t);
+  return {s2, f2_sub(t, f2_sub(s2, s))};
+}
+__device__ __forceinline__ df2 df2_neg(df2 a) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  return {__fmul2_rn(a.hi, m1), __fmul2_rn(a.lo, m1)};
+}
+
 }  // namespace topo

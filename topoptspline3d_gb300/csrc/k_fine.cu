@@ -154,6 +154,52 @@ __device__ __forceinline__ void wht3_bwd<float>(float g[3][8]) {
   wht_bwd<float>(g[2]);
 }
 
+// Double-float: components 0 and 1 in the lanes of df2.
+template <>
+__device__ __forceinline__ void wht3_fwd<df>(df c[3][8]) {
+  df2 p[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+    p[a] = {make_float2(c[0][a].hi, c[1][a].hi), make_float2(c[0][a].lo, c[1][a].lo)};
+#pragma unroll
+  for (int hb = 1; hb < 8; hb <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (!(i & hb)) {
+        const df2 a = p[i], b = p[i | hb];
+        p[i] = df2_add(a, b);
+        p[i | hb] = df2_add(b, df2_neg(a));  // b - a
+      }
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    c[0][a] = df(p[a].hi.x, p[a].lo.x);
+    c[1][a] = df(p[a].hi.y, p[a].lo.y);
+  }
+  wht_fwd<df>(c[2]);
+}
+template <>
+__device__ __forceinline__ void wht3_bwd<df>(df g[3][8]) {
+  df2 p[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+    p[a] = {make_float2(g[0][a].hi, g[1][a].hi), make_float2(g[0][a].lo, g[1][a].lo)};
+#pragma unroll
+  for (int hb = 1; hb < 8; hb <<= 1)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (!(i & hb)) {
+        const df2 a = p[i], b = p[i | hb];
+        p[i] = df2_add(a, df2_neg(b));  // a - b
+        p[i | hb] = df2_add(a, b);
+      }
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    g[0][a] = df(p[a].hi.x, p[a].lo.x);
+    g[1][a] = df(p[a].hi.y, p[a].lo.y);
+  }
+  wht_bwd<df>(g[2]);
+}
+
 // In: c[3][8] nodal values per component.  Out: c[3][8] nodal forces of pe*Ke*u.
 // EN: also *energy = u . (pe Ke u) = sum over modes of (transformed u) . (modal
 // force), since the backward transform is the forward one's transpose.

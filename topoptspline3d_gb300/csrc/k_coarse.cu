@@ -609,8 +609,10 @@ __global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims 
                                                         const double* __restrict__ Ke,
                                                         const int* __restrict__ list,
                                                         T* __restrict__ kel) {
-  __shared__ double sK[576];
-  __shared__ double sQ[8][8];
+  // products in the operator's precision: FP32 for the FP32 preconditioner's
+  // operators (the FP64 form is bound by GB300's FP64 pipe), FP64 for FP64
+  __shared__ T sK[576];
+  __shared__ T sQ[8][8];
   __shared__ uint8_t sfree[24];
   __shared__ int sflag;
   const int64_t ce = list[blockIdx.x];
@@ -620,7 +622,7 @@ __global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims 
   const int ent = threadIdx.x;
   const int R = ent / 24, S = ent % 24;
   const int A = R / 3, i = R % 3, B = S / 3, j = S % 3;
-  double acc = 0.0;
+  T acc = T(0);
   for (int pos = 0; pos < FCT * FCT * FCT; ++pos) {
     const int px = pos % FCT, py = pos / FCT % FCT, pz = pos / (FCT * FCT);
     const int fx = cx * FCT + px, fy = cy * FCT + py, fz = cz * FCT + pz;
@@ -645,7 +647,7 @@ __global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims 
       const int r = ent / 24, s2 = ent % 24;
       double k = pe * Ke[ent];
       if (!sfree[r] || !sfree[s2]) k = (r == s2) ? 1e6 : 0.0;
-      sK[ent] = k;
+      sK[ent] = T(k);
     }
     if (ent < 64) {
       const int a = ent / 8, C = ent % 8;
@@ -653,20 +655,20 @@ __global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims 
       const int cc[3] = {C & 1, (C >> 1) & 1, C >> 2};
       double w = 1.0;
       for (int k = 0; k < 3; ++k) w *= cc[k] ? (double)q[k] / FCT : (double)(FCT - q[k]) / FCT;
-      sQ[a][C] = w;
+      sQ[a][C] = T(w);
     }
     __syncthreads();
-    double s = 0.0;
+    T s = T(0);
     for (int a = 0; a < 8; ++a) {
-      const double qa = sQ[a][A];
-      if (qa == 0.0) continue;
-      double inner = 0.0;
+      const T qa = sQ[a][A];
+      if (qa == T(0)) continue;
+      T inner = T(0);
       for (int b = 0; b < 8; ++b) inner += sK[(3 * a + i) * 24 + 3 * b + j] * sQ[b][B];
       s += qa * inner;
     }
     acc += s;
   }
-  if (acc != 0.0) kel[ce * 576 + ent] += T(acc);
+  if (acc != T(0)) kel[ce * 576 + ent] += acc;
 }
 
 // Dyadic Galerkin: K_E = sum_children Q_c^T K_child Q_c (grid/Grid.cu:839-896 in

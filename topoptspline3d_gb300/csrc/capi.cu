@@ -242,7 +242,6 @@ template <> struct P<double> {
   static double* F(DevLevel& L) { return L.F; }
   static double* R(DevLevel& L) { return L.R; }
   static double* st(DevLevel& L) { return L.stencil; }
-  static const double* sym(DevLevel&) { return nullptr; }
   static double* dinv(DevLevel& L) { return L.dinv; }
   static double* cd(DevLevel& L) { return L.cd; }
   static double* rhop(topo_handle* h) { return h->rhop; }
@@ -258,7 +257,6 @@ template <> struct P<float> {
   static float* F(DevLevel& L) { return L.F32; }
   static float* R(DevLevel& L) { return L.R32; }
   static float* st(DevLevel& L) { return L.stencil32; }
-  static const float* sym(DevLevel& L) { return L.stsym32; }
   static float* dinv(DevLevel& L) { return L.dinv32; }
   static float* cd(DevLevel& L) { return L.cd32; }
   static float* rhop(topo_handle* h) { return h->rhop32; }
@@ -284,7 +282,7 @@ void level_apply(topo_handle* h, int l, const T* u, const T* f, T* out, bool res
                            sizeof(T) == 4 ? h->tz32 : h->tz64);
     prof_end(h, ev);
   } else {
-    launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual, h->nb, P<T>::sym(L));
+    launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual, h->nb);
   }
   count_launch();
 }
@@ -373,7 +371,7 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bo
       }
     } else {
       launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
-                             c_old, c_new, k == 0, h->nb, P<T>::sym(L));
+                             c_old, c_new, k == 0, h->nb);
     }
     count_launch();
     std::swap(ua, ub);
@@ -571,7 +569,7 @@ int estimate_lmax(topo_handle* h, int l, double* out) {
       launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP, h->ctr);
       if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, x, nullptr, y, false, 1,
                                        sizeof(T) == 4 ? h->tz32 : h->tz64);
-      else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), x, nullptr, y, false, 1, P<T>::sym(L));
+      else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), x, nullptr, y, false);
       k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), y, z, h->sc + S_TMP);
       launch_dot<T>(h->stream, x, z, n3, h->partial, h->sc + S_TMP + 1, h->ctr);
       std::swap(x, z);
@@ -791,7 +789,6 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     if (l > 0) {
       A(dalloc(hp, &L.kel, 576 * ne)); A(dalloc(hp, &L.kel32, 576 * ne));
       A(dalloc(hp, &L.stencil, 243 * nv)); A(dalloc(hp, &L.stencil32, 243 * nv));
-      A(dalloc(hp, &L.stsym32, 126 * nv));
     }
     if (rc != TOPO_OK) break;
     std::vector<uint8_t> vm(h->H.vactive[l]);
@@ -1160,11 +1157,7 @@ int topo_update_operators(topo_handle* h) {
       count_launch((b64 ? 1 : 0) + (b32 ? 1 : 0));
     }
     if (b64) launch_assemble_stencil_t<double>(h->stream, C.d, C.eactive, C.vmask, C.kel, C.stencil);
-    if (b32) {
-      launch_assemble_stencil_t<float>(h->stream, C.d, C.eactive, C.vmask, C.kel32, C.stencil32);
-      launch_stencil_compact(h->stream, C.d.nv, C.stencil32, C.stsym32);
-      count_launch();
-    }
+    if (b32) launch_assemble_stencil_t<float>(h->stream, C.d, C.eactive, C.vmask, C.kel32, C.stencil32);
     count_launch((b64 ? 1 : 0) + (b32 ? 1 : 0));
     CKL();
   }

@@ -99,11 +99,7 @@ __global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st,
 // enough loads in flight on the small coarse levels.
 constexpr int SV = 64;
 
-// Row `row` of vertex v: sum over the 27 neighbours of the 3x3 block times the
-// neighbour's 3-vector.  SYM: st is the symmetric form [126][nv]; the upper
-// blocks (k > 13) are read transposed from the neighbour's lower block 26 - k,
-// which halves the stencil bytes per application.
-template <typename T, bool SYM = false>
+template <typename T>
 __device__ __forceinline__ T stencil_row_i(const LevelDims& d, const T* __restrict__ st, const T* __restrict__ u,
                                            int x, int y, int z, int64_t v, int row) {
   T o = T(0);
@@ -113,27 +109,13 @@ __device__ __forceinline__ T stencil_row_i(const LevelDims& d, const T* __restri
     const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
     if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) continue;
     const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
-    if (!SYM || k <= 13) {
-      const T* s = st + (int64_t)(k * 9 + 3 * row) * nv + v;
-      o += s[0] * u[n] + s[nv] * u[nv + n] + s[2 * nv] * u[2 * nv + n];
-    } else {
-      const T* s = st + (int64_t)((26 - k) * 9 + row) * nv + n;  // column `row` of the neighbour's block
-      o += s[0] * u[n] + s[3 * nv] * u[nv + n] + s[6 * nv] * u[2 * nv + n];
-    }
+    const T* s = st + (int64_t)(k * 9 + 3 * row) * nv + v;
+    o += s[0] * u[n] + s[nv] * u[nv + n] + s[2 * nv] * u[2 * nv + n];
   }
   return o;
 }
 
-__global__ void k_stencil_compact(int64_t n, const float* __restrict__ st, float* __restrict__ sym) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) sym[i] = st[i];  // blocks 0..13 are the first 126 rows of [243][nv]
-}
-
-void launch_stencil_compact(cudaStream_t s, int64_t nv, const float* st, float* sym) {
-  k_stencil_compact<<<nblk(126 * nv, 256), 256, 0, s>>>(126 * nv, st, sym);
-}
-
-template <typename T, bool SYM = false>
+template <typename T>
 __global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st,
                                                            const T* __restrict__ u, const T* __restrict__ f,
                                                            T* __restrict__ out, bool residual) {
@@ -147,13 +129,13 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T*
   const int x = (int)(v % d.vx);
   const int64_t t = v / d.vx;
   const int y = (int)(t % d.vy), z = (int)(t / d.vy);
-  const T o = stencil_row_i<T, SYM>(d, st, u, x, y, z, v, row);
+  const T o = stencil_row_i<T>(d, st, u, x, y, z, v, row);
   const int64_t i = row * d.nv + v;
   out[i] = residual ? f[i] - o : o;
 }
 
 // One Chebyshev step on a stencil level: uout = u + d, d = c_old d + c_new Dinv (f - A u).
-template <typename T, bool SYM = false>
+template <typename T>
 __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* __restrict__ st,
                                                          const T* __restrict__ u, const T* __restrict__ f,
                                                          T* __restrict__ uout, const T* __restrict__ dinv,
@@ -172,7 +154,7 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* _
     const int x = (int)(v % d.vx);
     const int64_t t = v / d.vx;
     const int y = (int)(t % d.vy), z = (int)(t / d.vy);
-    sr[row][lv] = f[row * nv + v] - stencil_row_i<T, SYM>(d, st, u, x, y, z, v, row);
+    sr[row][lv] = f[row * nv + v] - stencil_row_i<T>(d, st, u, x, y, z, v, row);
   }
   __syncthreads();
   if (!ok) return;
@@ -268,33 +250,28 @@ constexpr int64_t STENCIL_WARP_MAX_NV = 32768;
 
 template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
-                          T* out, bool residual, int nb, const T* sym) {
+                          T* out, bool residual, int nb) {
   if (d.nv < STENCIL_WARP_MAX_NV)
     k_stencil_apply_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, out, residual);
-  else if (sym)
-    k_stencil_apply3<T, true><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, sym, u, f, out, residual);
   else
     k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
 }
 
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
-                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb, const T* sym) {
+                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb) {
   if (d.nv < STENCIL_WARP_MAX_NV)
     k_stencil_cheb_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
                                                                          (T)c_new, first);
-  else if (sym)
-    k_stencil_cheb<T, true><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, sym, u, f, uout, dinv, dvec, (T)c_old,
-                                                                        (T)c_new, first);
   else
     k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
                                                                   (T)c_new, first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,
-                                          const double*, double*, const double*, double*, double, double, bool, int, const double*);
+                                          const double*, double*, const double*, double*, double, double, bool, int);
 template void launch_stencil_cheb<float>(cudaStream_t, const LevelDims&, const float*, const float*,
-                                         const float*, float*, const float*, float*, double, double, bool, int, const float*);
+                                         const float*, float*, const float*, float*, double, double, bool, int);
 
 // First Chebyshev step from a zero iterate with a stored block-Jacobi inverse
 // (coarse levels; FP64 level 0 with its free-DOF mask): r = f, d = c_new D^-1 r,
@@ -1137,9 +1114,9 @@ void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* 
 }
 
 template void launch_stencil_apply<double>(cudaStream_t, const LevelDims&, const double*, const double*,
-                                           const double*, double*, bool, int, const double*);
+                                           const double*, double*, bool, int);
 template void launch_stencil_apply<float>(cudaStream_t, const LevelDims&, const float*, const float*,
-                                          const float*, float*, bool, int, const float*);
+                                          const float*, float*, bool, int);
 template void launch_stencil_gs<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                         double*, const double*, int, bool);
 template void launch_stencil_gs<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,

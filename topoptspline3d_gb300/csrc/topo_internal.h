@@ -35,7 +35,6 @@ struct DevLevel {
   float* kel32 = nullptr;       // coarse: FP32 element matrices [ne][576]
   double* stencil = nullptr;    // coarse: FP64 [243][nv]
   float* stencil32 = nullptr;   // coarse: FP32 [243][nv]
-  float* stsym32 = nullptr;     // coarse: FP32 [126][nv], the centre and lower 13 blocks (symmetric form)
   double* dinv = nullptr;       // FP64 inverse diagonal blocks [9][nv] (Chebyshev)
   float* dinv32 = nullptr;      // FP32 inverse diagonal blocks [9][nv]
   double* cd = nullptr;         // FP64 Chebyshev direction [3nv]
@@ -103,11 +102,7 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
                      double* dot = nullptr, unsigned* ctr = nullptr);
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
-                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1, const T* sym = nullptr);
-// Symmetric form of an FP32 stencil: blocks k = 0..13 of [27][9][nv] (the
-// lower neighbours and the centre); block k > 13 of vertex v is the transpose
-// of block 26 - k of its neighbour.  sym in the stencil launchers selects it.
-void launch_stencil_compact(cudaStream_t s, int64_t nv, const float* st, float* sym);
+                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);
 // First Chebyshev step from a zero iterate (u = 0): d = c_new D^-1 f, uout = d.
 // FP32: dvec may be null, and the next step then takes d from u (d_is_u).
 template <typename T>
@@ -124,7 +119,7 @@ void upload_template(const double* Ke576, double lam, double mu, double h);
 // coarse levels (k_coarse.cu)
 template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
-                          T* out, bool residual, int nb = 1, const T* sym = nullptr);
+                          T* out, bool residual, int nb = 1);
 template <typename T>
 void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask, T* u,
                        const T* f, int colour, bool reverse);

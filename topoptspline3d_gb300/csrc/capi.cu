@@ -31,7 +31,7 @@ namespace {
 // Slots 0-7 belong to one CG level; a nested CG uses base 8 (slots 8-15).
 enum Slot {
   S_RZ = 0, S_ZROLD = 1, S_RZOLD = 2, S_DQ = 3, S_RR = 4, S_FF = 5, S_ALPHA = 6, S_BETA = 7,
-  S_TMP = 16, S_COUNT = 24
+  S_TMP = 16, S_PW = 24, S_MAXLEV = 16, S_COUNT = S_PW + 2 * S_MAXLEV
 };
 
 struct EventPair {
@@ -538,75 +538,89 @@ inline unsigned nb256(int64_t n) { return (unsigned)((n + 255) / 256); }
 
 int read_scalars(topo_handle* h, int first, int count);
 
+// Largest eigenvalue of D^-1 A of every level whose bound is stale, by power
+// iteration.  First estimate of a level: 12 steps from the deterministic start
+// (as the oracle).  After an operator update: 4 steps from the previous
+// design's vector (the design moves a little per iteration, so the estimate
+// keeps refining); if that estimate falls more than 5% below the previous one
+// (an abrupt change of the operator), 8 more.  The levels' steps are launched
+// back to back with their own scalar slots, so all levels cost one host read
+// (two when a warm estimate dropped).
+// One step: with s = 1/|x|, z = D^-1 A (s x) = s D^-1 (A x) and the Rayleigh
+// estimate (s x).z = s (x.z); x <- z.  Work vectors: the level's R, U2 and
+// Chebyshev direction buffers (all free outside a V-cycle).
 template <typename T>
-int estimate_lmax(topo_handle* h, int l, double* out) {
-  DevLevel& L = h->lv[l];
-  const int64_t n3 = 3 * L.d.nv;
-  // work vectors in precision T: the level's R, U2 and Chebyshev direction
-  // buffers (all free outside a V-cycle)
-  T* x = P<T>::R(L);
-  T* y = P<T>::cd(L);
-  T* z = P<T>::U2(L);
-  // First estimate: 12 steps from the deterministic start (as the oracle).
-  // After an operator update: 4 steps from the previous design's vector (the
-  // design moves a little per iteration, so the estimate keeps refining); if
-  // that estimate falls more than 5% below the previous one (an abrupt change
-  // of the operator), continue to 12 steps.
-  int steps = 12;
-  const bool warm = P<T>::eig(L) != nullptr;
-  if (warm) {
-    CK(cudaMemcpyAsync(x, P<T>::eig(L), sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
-    steps = 4;
-  } else {
-    RET(dalloc(h, &P<T>::eig(L), n3));
-    k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, x);
-    count_launch();
+int estimate_bounds(topo_handle* h) {
+  const int nl = (int)h->lv.size();
+  if (nl > S_MAXLEV) return fail(h, TOPO_E_STATE, "%d levels exceed the %d of the spectral-bound slots", nl, S_MAXLEV);
+  struct Run {
+    int l;
+    bool warm;
+    T *x, *y, *z;
+    double lam;
+  };
+  std::vector<Run> runs;
+  for (int l = 0; l < nl; ++l) {
+    DevLevel& L = h->lv[l];
+    if (P<T>::lmax(L) != 0.0) continue;
+    diag_inv_level<T>(h, l);
+    Run r{l, P<T>::eig(L) != nullptr, P<T>::R(L), P<T>::cd(L), P<T>::U2(L), 0.0};
+    const int64_t n3 = 3 * L.d.nv;
+    if (r.warm) {
+      CK(cudaMemcpyAsync(r.x, P<T>::eig(L), sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    } else {
+      RET(dalloc(h, &P<T>::eig(L), n3));
+      k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, r.x);
+      count_launch();
+    }
+    runs.push_back(r);
   }
-  // One step: with s = 1/|x|, z = D^-1 A (s x) = s D^-1 (A x) and the
-  // Rayleigh estimate (s x).z = s (x.z); x <- z.
-  auto power_steps = [&](int k) {
+  if (runs.empty()) return TOPO_OK;
+  auto power_steps = [&](Run& r, int k) {
+    DevLevel& L = h->lv[r.l];
+    const int64_t n3 = 3 * L.d.nv;
+    double* sl = h->sc + S_PW + 2 * r.l;
     for (int it = 0; it < k; ++it) {
-      launch_dot<T>(h->stream, x, x, n3, h->partial, h->sc + S_TMP, h->ctr);
-      if (l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, x, nullptr, y, false, 1,
-                                       sizeof(T) == 4 ? h->tz32 : h->tz64);
-      else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), x, nullptr, y, false);
-      k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), y, z, h->sc + S_TMP);
-      launch_dot<T>(h->stream, x, z, n3, h->partial, h->sc + S_TMP + 1, h->ctr);
-      std::swap(x, z);
+      launch_dot<T>(h->stream, r.x, r.x, n3, h->partial, sl, h->ctr);
+      if (r.l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, r.x, nullptr, r.y, false, 1,
+                                         sizeof(T) == 4 ? h->tz32 : h->tz64);
+      else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), r.x, nullptr, r.y, false);
+      k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), r.y, r.z, sl);
+      launch_dot<T>(h->stream, r.x, r.z, n3, h->partial, sl + 1, h->ctr);
+      std::swap(r.x, r.z);
       count_launch(4);
     }
   };
-  double lam = 0.0;
-  auto estimate = [&]() -> int {
-    RET(read_scalars(h, S_TMP, 2));
-    const double xx = h->hsc[S_TMP], xz = h->hsc[S_TMP + 1];
-    lam = xx > 0 ? xz / std::sqrt(xx) : 0.0;
+  auto read_all = [&]() -> int {
+    RET(read_scalars(h, S_PW, 2 * nl));
+    for (Run& r : runs) {
+      const double xx = h->hsc[S_PW + 2 * r.l], xz = h->hsc[S_PW + 2 * r.l + 1];
+      r.lam = xx > 0 ? xz / std::sqrt(xx) : 0.0;
+    }
     return TOPO_OK;
   };
-  power_steps(steps);
-  if (warm) {
-    RET(estimate());
-    if (lam < 0.95 * P<T>::lprev(L)) power_steps(8);
+  for (Run& r : runs) power_steps(r, r.warm ? 4 : 12);
+  RET(read_all());
+  bool more = false;
+  for (Run& r : runs)
+    if (r.warm && r.lam < 0.95 * P<T>::lprev(h->lv[r.l])) {
+      power_steps(r, 8);
+      more = true;
+    }
+  if (more) RET(read_all());
+  for (Run& r : runs) {
+    DevLevel& L = h->lv[r.l];
+    CK(cudaMemcpyAsync(P<T>::eig(L), r.x, sizeof(T) * 3 * L.d.nv, cudaMemcpyDeviceToDevice, h->stream));
+    P<T>::lmax(L) = r.lam;
+    P<T>::lprev(L) = r.lam;
   }
-  CK(cudaMemcpyAsync(P<T>::eig(L), x, sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
-  RET(estimate());
-  *out = lam;
-  P<T>::lprev(L) = lam;
   return TOPO_OK;
 }
 
 template <typename T>
 int prepare_smoother(topo_handle* h, int smoother) {
   if (smoother != TOPO_SMOOTH_CHEBYSHEV) return TOPO_OK;
-  for (size_t l = 0; l < h->lv.size(); ++l) {
-    DevLevel& L = h->lv[l];
-    if (P<T>::lmax(L) != 0.0) continue;
-    diag_inv_level<T>(h, (int)l);
-    double lm = 0;
-    RET(estimate_lmax<T>(h, (int)l, &lm));
-    P<T>::lmax(L) = lm;
-  }
-  return TOPO_OK;
+  return estimate_bounds<T>(h);
 }
 
 int read_scalars(topo_handle* h, int first, int count) {

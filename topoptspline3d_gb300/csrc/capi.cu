@@ -81,6 +81,7 @@ struct topo_handle {
   SplineTables st;
   SplineDev sd{};
   double *coeff = nullptr, *csens = nullptr, *coeff_old = nullptr, *coeff_tmp = nullptr;
+  float2* coeff_df = nullptr;  // OC trial coefficients split into (hi, lo) floats
   double* volcsens = nullptr;  // scale * d volume / d coefficient (topo_volume_csens)
   double *adj1 = nullptr, *adj2 = nullptr;
   // level-0 work vectors
@@ -1023,18 +1024,18 @@ int topo_set_spline(topo_handle* h, int order, const int* partition3, const doub
     CK(cudaMemcpyAsync(hi, h->st.hi[a].data(), sizeof(int) * sd.nb[a], cudaMemcpyHostToDevice, h->stream));
     sd.i0[a] = i0; sd.N[a] = N; sd.lo[a] = lo; sd.hi[a] = hi;
   }
-  {  // x-axis basis values split for the double-float density pass
-    std::vector<float2> ndf(h->st.N[0].size());
+  for (int a = 0; a < 3; ++a) {  // basis values split for the double-float spline passes
+    std::vector<float2> ndf(h->st.N[a].size());
     for (size_t k = 0; k < ndf.size(); ++k) {
-      const double v = h->st.N[0][k];
+      const double v = h->st.N[a][k];
       const float hi = (float)v;
       ndf[k] = make_float2(hi, (float)(v - (double)hi));
     }
-    float2* Nx = nullptr;
-    RET(dalloc(h, &Nx, (int64_t)ndf.size()));
-    CK(cudaMemcpyAsync(Nx, ndf.data(), sizeof(float2) * ndf.size(), cudaMemcpyHostToDevice, h->stream));
+    float2* Nd = nullptr;
+    RET(dalloc(h, &Nd, (int64_t)ndf.size()));
+    CK(cudaMemcpyAsync(Nd, ndf.data(), sizeof(float2) * ndf.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    sd.Nx_df = Nx;
+    sd.Ndf[a] = Nd;
   }
   const int64_t nc = (int64_t)sd.nb[0] * sd.nb[1] * sd.nb[2];
   RET(dalloc(h, &h->coeff, nc));
@@ -1042,6 +1043,7 @@ int topo_set_spline(topo_handle* h, int order, const int* partition3, const doub
   RET(dalloc(h, &h->volcsens, nc));
   RET(dalloc(h, &h->coeff_old, nc));
   RET(dalloc(h, &h->coeff_tmp, nc));
+  RET(dalloc(h, &h->coeff_df, nc));
   RET(dalloc(h, &h->adj1, (int64_t)sd.nb[0] * d0.ey * d0.ez));
   RET(dalloc(h, &h->adj2, (int64_t)sd.nb[0] * sd.nb[1] * d0.ez));
   CK(cudaStreamSynchronize(h->stream));
@@ -2046,8 +2048,9 @@ int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) 
   int itn = 0, trials = 0;
   do {
     thres = 0.5 * (lo + hi);
-    launch_oc_trial(h->stream, nc, h->coeff_old, h->csens, thres, o->damp, o->step, o->cmin, o->cmax, h->coeff);
-    launch_trial_volume(h->stream, L.d, L.eactive, h->sd, h->coeff, h->cfg.min_density, h->partial,
+    launch_oc_trial(h->stream, nc, h->coeff_old, h->csens, thres, o->damp, o->step, o->cmin, o->cmax, h->coeff,
+                    h->coeff_df);
+    launch_trial_volume(h->stream, L.d, L.eactive, h->sd, h->coeff_df, h->cfg.min_density, h->partial,
                         h->sc + S_TMP, h->adj1);
     count_launch(4);
     CKL();

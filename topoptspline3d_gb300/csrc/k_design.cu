@@ -105,6 +105,34 @@ __global__ void k_spline_yz(LevelDims d, SplineDev sp, const double* __restrict_
   B[gid] = make_float2(vd.hi, vd.lo);
 }
 
+// Pass 1 of an OC trial in double-float, from coefficients already split into
+// (hi, lo) floats (FP64 here would be bound by the FP64 pipe on every trial).
+__global__ void k_spline_yz_df(LevelDims d, SplineDev sp, const float2* __restrict__ coeff,
+                               float2* __restrict__ B) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nbx = sp.nb[0];
+  if (gid >= (int64_t)nbx * d.ey * d.ez) return;
+  const int i = (int)(gid % nbx);
+  const int64_t yz = gid / nbx;
+  const int y = (int)(yz % d.ey), z = (int)(yz / d.ey);
+  const int iy = sp.i0[1][y], iz = sp.i0[2][z];
+  df v(0);
+  if (iy >= 0 && iz >= 0) {
+    const int k = sp.order;
+    for (int s2 = 0; s2 < k; ++s2) {
+      const float2 ns = sp.Ndf[1][y * k + s2];
+      df a(0);
+      for (int t = 0; t < k; ++t) {
+        const float2 c = coeff[i + (int64_t)nbx * ((iy + s2) + (int64_t)sp.nb[1] * (iz + t))];
+        const float2 nz = sp.Ndf[2][z * k + t];
+        a += df(c.x, c.y) * df(nz.x, nz.y);
+      }
+      v += df(ns.x, ns.y) * a;
+    }
+  }
+  B[gid] = make_float2(v.hi, v.lo);
+}
+
 // Pass 2: value at element (x,y,z) = sum_r Nx[x][r] B[z][y][ix + r], or -0.2 out of
 // range, in double-float arithmetic (about 1e-15 relative; FP64 here would be
 // bound by GB300's FP64 pipe, and each OC bisection trial evaluates it on every
@@ -117,7 +145,7 @@ __device__ __forceinline__ df spline_from_B(const SplineDev& sp, const float2* _
   const float2* b = B + (int64_t)sp.nb[0] * (y + (int64_t)ey * z) + ix;
   df v(0);
   for (int r = 0; r < k; ++r) {
-    const float2 n = sp.Nx_df[x * k + r], bb = b[r];
+    const float2 n = sp.Ndf[0][x * k + r], bb = b[r];
     v += df(n.x, n.y) * df(bb.x, bb.y);
   }
   return v;
@@ -193,12 +221,13 @@ void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* 
 }
 
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
-                         const SplineDev& sp, const double* coeff, double rho_min, double* partial,
+                         const SplineDev& sp, const float2* coeff_df, double rho_min, double* partial,
                          double* out, double* Btmp) {
   const int64_t nB = (int64_t)sp.nb[0] * d.ey * d.ez;
   float2* B = reinterpret_cast<float2*>(Btmp);  // nB (hi, lo) pairs in the nB-double scratch
-  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, B);
-  int nb = (int)std::min<int64_t>(1024, (d.ne + VOL_THREADS * 4 - 1) / (VOL_THREADS * 4));
+  k_spline_yz_df<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff_df, B);
+  // two elements per thread at most (up to 2048 partials)
+  int nb = (int)std::min<int64_t>(2048, (d.ne + VOL_THREADS * 2 - 1) / (VOL_THREADS * 2));
   if (nb < 1) nb = 1;
   k_volume_from_B<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, partial);
   k_sum_partials<<<1, 256, 0, s>>>(partial, nb, out);
@@ -518,7 +547,7 @@ void launch_penalise(cudaStream_t s, int64_t ne, const uint8_t* eactive, const d
 // c' = clamp(clamp(c (max(-dc,0)/thres)^damp, c-step, c+step), cmin, cmax).
 __global__ void k_oc_trial(int64_t nc, const double* __restrict__ cold, const double* __restrict__ csens,
                            double thres, double damp, double step, double cmin, double cmax,
-                           double* __restrict__ cnew) {
+                           double* __restrict__ cnew, float2* __restrict__ cnew_df) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   double g = csens[i];
@@ -529,11 +558,15 @@ __global__ void k_oc_trial(int64_t nc, const double* __restrict__ cold, const do
   cn = fmin(fmax(cn, co - step), co + step);
   cn = fmin(fmax(cn, cmin), cmax);
   cnew[i] = cn;
+  if (cnew_df) {
+    const df v = df_from(cn);
+    cnew_df[i] = make_float2(v.hi, v.lo);
+  }
 }
 
 void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,
-                     double damp, double step, double cmin, double cmax, double* cnew) {
-  k_oc_trial<<<nblk(nc, 256), 256, 0, s>>>(nc, cold, csens, thres, damp, step, cmin, cmax, cnew);
+                     double damp, double step, double cmin, double cmax, double* cnew, float2* cnew_df) {
+  k_oc_trial<<<nblk(nc, 256), 256, 0, s>>>(nc, cold, csens, thres, damp, step, cmin, cmax, cnew, cnew_df);
 }
 
 }  // namespace topo

@@ -188,7 +188,7 @@ struct SplineDev {
   int nb[3];
   const int* i0[3];      // device [n_axis]: first basis index of each element slice, -1 out of range
   const double* N[3];    // device [n_axis][order]: basis values at the element centres
-  const float2* Nx_df;   // device [n_x][order]: x-axis values split into (hi, lo) floats
+  const float2* Ndf[3];  // device [n_axis][order]: the same values split into (hi, lo) floats
   const int* lo[3];      // device [nb]: first element slice in the support of basis i
   const int* hi[3];      // device [nb]: one past the last element slice
 };
@@ -211,8 +211,9 @@ void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* 
 void launch_coeff_to_density_direct(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                                     const SplineDev& sp, const double* coeff, double rho_min, double penal,
                                     double* rho, double* rhop, float* rhop32);
+// coeff_df: the trial coefficients split into (hi, lo) floats (from launch_oc_trial)
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
-                         const SplineDev& sp, const double* coeff, double rho_min, double* partial,
+                         const SplineDev& sp, const float2* coeff_df, double rho_min, double* partial,
                          double* out, double* Btmp);
 void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                         const double* rho, const double* u, double penal, double lam, double mu,
@@ -242,8 +243,9 @@ struct SplineView {
 };
 int handle_spline_view(topo_handle* h, SplineView* out);
 int handle_fail(topo_handle* h, int code, const char* msg);
+// cnew_df (optional): cnew split into (hi, lo) floats as well
 void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,
-                     double damp, double step, double cmin, double cmax, double* cnew);
+                     double damp, double step, double cmin, double cmax, double* cnew, float2* cnew_df = nullptr);
 void launch_maxabs(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);
 
 // bc_regions.cpp: region-predicate boundary conditions (host).

@@ -24,45 +24,6 @@ __device__ __forceinline__ double simp_pow(double v, double p) {
   return pow(v, p);
 }
 
-// Spline value at element (x,y,z): sum over order^3 taps of c * Nx Ny Nz, or the
-// reference's out-of-range value -0.2 (grid/Grid.cu:3396-3430).
-__device__ __forceinline__ double spline_at(const SplineDev& sp, const double* __restrict__ coeff,
-                                            int x, int y, int z) {
-  const int ix = sp.i0[0][x], iy = sp.i0[1][y], iz = sp.i0[2][z];
-  if (ix < 0 || iy < 0 || iz < 0) return -0.2;
-  const int k = sp.order;
-  double val = 0.0;
-  for (int r = 0; r < k; ++r) {
-    const double nr = sp.N[0][x * k + r];
-    for (int s = 0; s < k; ++s) {
-      const double ns = sp.N[1][y * k + s];
-      for (int t = 0; t < k; ++t) {
-        const int64_t idx = (ix + r) + (int64_t)sp.nb[0] * ((iy + s) + (int64_t)sp.nb[1] * (iz + t));
-        val += coeff[idx] * nr * ns * sp.N[2][z * k + t];
-      }
-    }
-  }
-  return val;
-}
-
-__global__ void k_coeff_to_density(LevelDims d, const uint8_t* __restrict__ eactive, SplineDev sp,
-                                   const double* __restrict__ coeff, double rho_min, double penal,
-                                   double* __restrict__ rho, double* __restrict__ rhop,
-                                   float* __restrict__ rhop32) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= d.ne) return;
-  const int x = (int)(e % d.ex);
-  const int64_t t = e / d.ex;
-  const int y = (int)(t % d.ey), z = (int)(t / d.ey);
-  if (!eactive[e]) {
-    rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
-    return;
-  }
-  const double v = fmin(fmax(spline_at(sp, coeff, x, y, z), rho_min), 1.0);
-  const double vp = simp_pow(v, penal);
-  rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
-}
-
 constexpr int VOL_THREADS = 256;
 
 __global__ void k_sum_partials(const double* __restrict__ partial, int nb, double* __restrict__ out) {
@@ -233,15 +194,6 @@ void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eact
   k_sum_partials<<<1, 256, 0, s>>>(partial, nb, out);
 }
 
-// Direct (non-separable) density evaluation, kept as the cross-check of the
-// two-pass path: 27 taps per element.
-void launch_coeff_to_density_direct(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
-                                    const SplineDev& sp, const double* coeff, double rho_min, double penal,
-                                    double* rho, double* rhop, float* rhop32) {
-  k_coeff_to_density<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, coeff, rho_min, penal, rho, rhop,
-                                                     rhop32);
-}
-
 // Element sensitivity g_e = -p rho^(p-1) u_e^T Ke u_e (optimization/optimization.cu:96-159),
 // with u_e^T Ke u_e evaluated in the sum-factorised modal form: Walsh-Hadamard
 // coefficients of the nodal values, the displacement gradient split over the
@@ -348,40 +300,11 @@ void launch_sensitivity_from_energy(cudaStream_t s, int64_t ne, const uint8_t* e
 // r^2 <= R^2, R_int = floor(R + 0.5), weight 1 - 6s^2 + 8s^3 - 3s^4 with s = r/R.
 // The ball's offsets and weights depend only on R; they come precomputed (in the
 // reference's loop order dx, dy, dz) so no square root is taken per neighbour.
-__global__ void k_filter(LevelDims d, const uint8_t* __restrict__ eactive, const double* __restrict__ src,
-                         double* __restrict__ dst, const int4* __restrict__ offs,
-                         const double* __restrict__ wts, int noffs) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= d.ne) return;
-  if (!eactive[e]) { dst[e] = 0.0; return; }
-  const int x = (int)(e % d.ex);
-  const int64_t t = e / d.ex;
-  const int y = (int)(t % d.ey), z = (int)(t / d.ey);
-  double ws = 0.0, gs = 0.0;
-  for (int k = 0; k < noffs; ++k) {
-    const int4 o = offs[k];
-    const int nx = x + o.x, ny = y + o.y, nz = z + o.z;
-    if (nx < 0 || ny < 0 || nz < 0 || nx >= d.ex || ny >= d.ey || nz >= d.ez) continue;
-    const int64_t n = nx + (int64_t)d.ex * (ny + (int64_t)d.ey * nz);
-    if (!eactive[n]) continue;
-    const double w = wts[k];
-    gs += w * src[n];
-    ws += w;
-  }
-  dst[e] = gs / ws;
-}
-
-void launch_filter(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* src,
-                   double* dst, const int4* offs, const double* wts, int noffs) {
-  k_filter<<<nblk(d.ne, 128), 128, 0, s>>>(d, eactive, src, dst, offs, wts, noffs);
-}
-
-// The same filter in double-float arithmetic (about 1e-14 relative): the
-// sensitivities and weights arrive split into (hi, lo) floats, the weighted
-// sums run on the FP32 pipe, and the quotient is a double-float division
-// (FP32 quotient, one correction from the double-float remainder; Dekker
-// 1971).  The FP64 form is bound by GB300's FP64 pipe (66 FP64 operations
-// per element).
+// It runs in double-float arithmetic (about 1e-14 relative): the sensitivities
+// and weights arrive split into (hi, lo) floats, the weighted sums run on the
+// FP32 pipe, and the quotient is a double-float division (FP32 quotient, one
+// correction from the double-float remainder; Dekker 1971).  An FP64 form is
+// bound by GB300's FP64 pipe (66 FP64 operations per element).
 __device__ __forceinline__ df df_div(df a, df b) {
   const float q1 = __fdiv_rn(a.hi, b.hi);
   const df r = a - b * df(q1, 0.f);

@@ -219,27 +219,8 @@ void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta
   k_pcg_dir<T><<<nblk(threads, 256), 256, 0, s>>>(z, d, sc, beta_slot, first, n, packed ? 1 : 0);
 }
 
-// alpha = sc[alpha_slot]; rold = r; x += alpha d; r -= alpha q.
-template <typename T>
-__global__ void k_pcg_update(T* __restrict__ x, T* __restrict__ r, T* __restrict__ rold,
-                             const T* __restrict__ d, const T* __restrict__ q,
-                             const double* __restrict__ sc, int alpha_slot, int64_t n) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const T alpha = (T)sc[alpha_slot];
-  const T ri = r[i];
-  rold[i] = ri;
-  x[i] = x[i] + alpha * d[i];
-  r[i] = ri - alpha * q[i];
-}
-
-template <typename T>
-void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
-                       int alpha_slot, int64_t n) {
-  k_pcg_update<T><<<nblk(n, 256), 256, 0, s>>>(x, r, rold, d, q, sc, alpha_slot, n);
-}
-
-// The same update fused with the new residual's squared norm: per-thread sums
+// x += alpha d, rold = r, r -= alpha q (alpha = sc[alpha_slot]), fused with the
+// new residual's squared norm: per-thread sums
 // in the vectors' precision, combined in FP64 in a fixed order (deterministic).
 // Each thread moves 16-byte packs (4 floats / 2 doubles) so enough bytes are in
 // flight to stream at HBM bandwidth; the tail past the last whole pack is scalar.
@@ -299,27 +280,7 @@ template void launch_pcg_update_rr<double>(cudaStream_t, double*, double*, doubl
 template void launch_pcg_update_rr<float>(cudaStream_t, float*, float*, float*, const float*, const float*,
                                           const double*, int, int64_t, double*, double*, unsigned*);
 
-void launch_finalize_sum(cudaStream_t s, const double* partial, int nb, double* out) {
-  k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, out);
-}
 
-// x = a * sc_scale(y) where the scale is 1/sqrt(sc[slot]) (power-iteration normalisation).
-template <typename T>
-__global__ void k_scale_by_rnorm(const T* __restrict__ y, T* __restrict__ x, const double* __restrict__ sc,
-                                 int slot, int64_t n) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const T s = (T)rsqrt(sc[slot]);
-  x[i] = y[i] * s;
-}
-
-template <typename T>
-void launch_scale_by_rnorm(cudaStream_t s, const T* y, T* x, const double* sc, int slot, int64_t n) {
-  k_scale_by_rnorm<T><<<nblk(n, 256), 256, 0, s>>>(y, x, sc, slot, n);
-}
-
-template void launch_scale_by_rnorm<double>(cudaStream_t, const double*, double*, const double*, int, int64_t);
-template void launch_scale_by_rnorm<float>(cudaStream_t, const float*, float*, const double*, int, int64_t);
 
 template void launch_dot<double>(cudaStream_t, const double*, const double*, int64_t, double*, double*, unsigned*);
 template void launch_dot<float>(cudaStream_t, const float*, const float*, int64_t, double*, double*, unsigned*);
@@ -329,9 +290,5 @@ template void launch_copy<double>(cudaStream_t, const double*, double*, int64_t)
 template void launch_copy<float>(cudaStream_t, const float*, float*, int64_t);
 template void launch_pcg_dir<double>(cudaStream_t, const double*, double*, const double*, int, bool, int64_t);
 template void launch_pcg_dir<float>(cudaStream_t, const float*, float*, const double*, int, bool, int64_t);
-template void launch_pcg_update<double>(cudaStream_t, double*, double*, double*, const double*,
-                                        const double*, const double*, int, int64_t);
-template void launch_pcg_update<float>(cudaStream_t, float*, float*, float*, const float*, const float*,
-                                       const double*, int, int64_t);
 
 }  // namespace topo

@@ -75,8 +75,9 @@ template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb = 1, int tz = 0);
 // out = K u (level 0, one right-hand side) with per-CTA partial sums of u.out
-// in partial; returns their count (sum them with launch_finalize_sum), or 0 and
-// launches nothing when the kernel would need more than cap partial slots.
+// in partial; with dot and ctr (a zeroed counter) the last CTA also writes
+// their total to *dot.  Returns the number of partials, or 0, launching
+// nothing, when the kernel would need more than cap partial slots.
 template <typename T>
 int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                           T* out, int tz, double* partial, int cap, double* dot = nullptr, unsigned* ctr = nullptr);
@@ -92,9 +93,9 @@ template <typename T>
 void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                           T* dinv);
 // FP32, one right-hand side: with dot_fo the kernel also leaves per-CTA partial
-// sums of f.uout in dot_fo; returns their count (sum them with
-// launch_finalize_sum), or 0 when none were formed (FP64, a batch, or more
-// CTAs than cap).
+// sums of f.uout in dot_fo, and with dot and ctr (a zeroed counter) the last
+// CTA writes their total to *dot.  Returns the number of partials, or 0 when
+// none were formed (FP64, a batch, or more CTAs than cap).
 template <typename T>
 int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                      const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first,
@@ -169,18 +170,12 @@ void launch_f2d_add(cudaStream_t s, const float* a, double* b, int64_t n);
 void launch_scalar_ratio(cudaStream_t s, double* sc, int num, int sub, int den, int out);
 template <typename T>
 void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta_slot, bool first, int64_t n);
-template <typename T>
-void launch_pcg_update(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q,
-                       const double* sc, int alpha_slot, int64_t n);
 // launch_pcg_update fused with rr = r.r of the updated residual (2 launches);
 // rold may be null (not kept)
 template <typename T>
 void launch_pcg_update_rr(cudaStream_t s, T* x, T* r, T* rold, const T* d, const T* q, const double* sc,
                           int alpha_slot, int64_t n, double* partial, double* rr, unsigned* ctr = nullptr);
 // out = sum of nb partials in a fixed order
-void launch_finalize_sum(cudaStream_t s, const double* partial, int nb, double* out);
-template <typename T>
-void launch_scale_by_rnorm(cudaStream_t s, const T* y, T* x, const double* sc, int slot, int64_t n);
 
 // design chain (k_design.cu)
 struct SplineDev {
@@ -208,9 +203,6 @@ void spline_tables(int order, const int* partition, const double* bmin, const do
 void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,
                              double* rho, double* rhop, float* rhop32, double* Btmp);
-void launch_coeff_to_density_direct(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
-                                    const SplineDev& sp, const double* coeff, double rho_min, double penal,
-                                    double* rho, double* rhop, float* rhop32);
 // coeff_df: the trial coefficients split into (hi, lo) floats (from launch_oc_trial)
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                          const SplineDev& sp, const float2* coeff_df, double rho_min, double* partial,
@@ -221,8 +213,6 @@ void launch_sensitivity(cudaStream_t s, const LevelDims& d, const uint8_t* eacti
 // sens = -p E / rho in place, from element energies E = u_e . (rho^p Ke u_e)
 void launch_sensitivity_from_energy(cudaStream_t s, int64_t ne, const uint8_t* eactive, const double* rho,
                                     double penal, double* sens);
-void launch_filter(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* src,
-                   double* dst, const int4* offs, const double* wts, int noffs);
 // The same filter in double-float, in place on sens (sens_df: ne float2 scratch;
 // wts: the weights split into (hi, lo) floats)
 void launch_filter_df(cudaStream_t s, const LevelDims& d, const uint8_t* eactive, double* sens,

@@ -31,8 +31,17 @@ namespace {
 // Slots 0-7 belong to one CG level; a nested CG uses base 8 (slots 8-15).
 enum Slot {
   S_RZ = 0, S_ZROLD = 1, S_RZOLD = 2, S_DQ = 3, S_RR = 4, S_FF = 5, S_ALPHA = 6, S_BETA = 7,
-  S_TMP = 16, S_PW = 24, S_MAXLEV = 16, S_COUNT = S_PW + 2 * S_MAXLEV
+  S_TMP = 16, S_PW = 24, S_MAXLEV = 16,
+  // device-controlled inner CG loop: iterations of the current inner solve,
+  // its ||b|| reference, the first iteration whose r.r was non-finite
+  // (1-based, 0 = none), inner iterations summed over the solve
+  S_LOOP = S_PW + 2 * S_MAXLEV, S_COUNT = S_LOOP + 4
 };
+
+// Chebyshev step coefficients (c_old, c_new) in device memory: per precision
+// (FP64 first), level and step, then the pair (0, 1).
+constexpr int CHEB_MAX_DEG = 32;
+constexpr int CHEB_TABLE = 2 * (2 * S_MAXLEV * CHEB_MAX_DEG + 1);
 
 struct EventPair {
   cudaEvent_t a, b;
@@ -52,6 +61,13 @@ struct topo_handle {
   cudaGraphExec_t vgraph = nullptr;
   std::vector<double> vkey;
   long long vgraph_kernels = 0;
+  // inner FP32 CG of the mixed solve as one graph with a device-side WHILE
+  // loop (igraph); kernels of its fixed part and of one loop iteration
+  bool in_capture = false;
+  bool igraph_ok = true;
+  cudaGraphExec_t igraph = nullptr;
+  std::vector<double> ikey;
+  long long igraph_fixed = 0, igraph_body = 0;
   // profiling inside the graph: event pairs captured as external event-record
   // nodes, collected after each replay has completed
   bool capturing = false;
@@ -119,6 +135,8 @@ struct topo_handle {
   bool vdot_on = false;
   double* vdot_out = nullptr;
   bool inner_fr = false;  // inner CG in Fletcher-Reeves form (z.rold taken as 0)
+  double* chebc = nullptr;          // Chebyshev coefficient table (device)
+  std::vector<double> chebc_host;   // its last uploaded contents
   double* sc = nullptr;    // device scalar slots
   double* hsc = nullptr;   // pinned host mirror
   int64_t active_elements = 0, gs_padded_elements = 0;
@@ -251,6 +269,7 @@ template <> struct P<double> {
   static double*& eig(DevLevel& L) { return L.eig; }
   static double& lprev(DevLevel& L) { return L.lprev; }
   static const int fam_apply = TOPO_K_FINE_APPLY64, fam_smooth = TOPO_K_FINE_SMOOTH64;
+  static const int table = 0;  // Chebyshev coefficient table block
 };
 template <> struct P<float> {
   static float* U(DevLevel& L) { return L.U32; }
@@ -266,7 +285,14 @@ template <> struct P<float> {
   static float*& eig(DevLevel& L) { return L.eig32; }
   static double& lprev(DevLevel& L) { return L.lprev32; }
   static const int fam_apply = TOPO_K_FINE_APPLY32, fam_smooth = TOPO_K_FINE_SMOOTH32;
+  static const int table = 1;
 };
+
+// (c_old, c_new) of Chebyshev step k on level l in precision T
+template <typename T>
+const double* cheb_coef(const topo_handle* h, int l, int k) {
+  return h->chebc + 2 * ((P<T>::table * S_MAXLEV + l) * CHEB_MAX_DEG + k);
+}
 
 // out = A_l u (residual: out = f - A_l u)
 template <typename T>
@@ -329,24 +355,16 @@ struct ChebParams {
 // Each step is one fused kernel that reads the iterate from one buffer and
 // writes the next into the other; the result ends in level U.  With
 // zero_start the iterate is known to be zero on entry (level U is not read),
-// and the first step is the operator-free d = c_new D^-1 f.
+// and the first step is the operator-free d = c_new D^-1 f.  The step
+// coefficients come from the device table (cheb_upload), so a captured cycle
+// stays valid when the spectral bounds move.
 template <typename T>
 void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bool last_dots = false) {
   DevLevel& L = h->lv[l];
-  const double lmax = P<T>::lmax(L) * cp.hi, lmin = P<T>::lmax(L) * cp.lo;
-  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
-  const double sigma = theta / delta;
-  double rho_old = 1.0 / sigma;
   T* ua = P<T>::U(L);
   T* ub = P<T>::U2(L);
   for (int k = 0; k < cp.degree; ++k) {
-    double c_old = 0.0, c_new = 1.0 / theta;
-    if (k > 0) {
-      const double rho_new = 1.0 / (2.0 * sigma - rho_old);
-      c_old = rho_new * rho_old;
-      c_new = 2.0 * rho_new / delta;
-      rho_old = rho_new;
-    }
+    const double* coef = cheb_coef<T>(h, l, k);
     // FP32 level 0 after a zero start: d = u after the first step, so it is
     // not stored and the second step reads it from u
     const bool d_in_u = l == 0 && sizeof(T) == 4 && zero_start;
@@ -354,25 +372,25 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bo
       // not in the smoother's profiling family: no operator is applied
       if (l == 0)
         launch_fine_cheb_zero<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, P<T>::F(L), ub, P<T>::dinv(L),
-                                 d_in_u ? nullptr : P<T>::cd(L), c_new, h->nb);
+                                 d_in_u ? nullptr : P<T>::cd(L), coef, h->nb);
       else
-        launch_cheb_zero_stored<T>(h->stream, L.d.nv, nullptr, P<T>::dinv(L), P<T>::F(L), P<T>::cd(L), ub, c_new,
+        launch_cheb_zero_stored<T>(h->stream, L.d.nv, nullptr, P<T>::dinv(L), P<T>::F(L), P<T>::cd(L), ub, coef,
                                    h->nb);
     } else if (l == 0) {
       const bool dots = last_dots && k == cp.degree - 1;
       EventPair* ev = prof_begin(h, P<T>::fam_smooth);
       const int np = launch_fine_cheb<T>(
-          h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), c_old, c_new,
-          k == 0, h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr,
-          h->fdot_cap, h->vdot_out, h->ctr);
+          h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), coef, k == 0,
+          h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr, h->fdot_cap,
+          h->vdot_out, h->ctr);
       prof_end(h, ev);
       if (dots && np == 0) {  // r.z of the cycle's result (F is r, the output is z), unfused
         launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out, h->ctr);
         count_launch();
       }
     } else {
-      launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L),
-                             c_old, c_new, k == 0, h->nb);
+      launch_stencil_cheb<T>(h->stream, L.d, P<T>::st(L), ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), coef,
+                             k == 0, h->nb);
     }
     count_launch();
     std::swap(ua, ub);
@@ -452,25 +470,32 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
   }
 }
 
+// What a captured FP32 V-cycle depends on besides buffer contents.
+static std::vector<double> vcycle_key(const topo_handle* h, int pre, int post, int smoother, const ChebParams& cp,
+                                      bool zero0) {
+  std::vector<double> key = {(double)pre, (double)post, (double)smoother, (double)cp.degree,
+                             (double)h->tz32, (double)h->nb, (double)h->prof, (double)zero0,
+                             (double)h->vdot_on, (double)(uintptr_t)h->vdot_out};
+  for (const DevLevel& L : h->lv) {
+    key.push_back((double)(uintptr_t)L.U32);
+    key.push_back((double)(uintptr_t)L.F32);
+  }
+  return key;
+}
+
 // The FP32 preconditioning V-cycle as one CUDA graph launch.  The cycle is a
 // fixed sequence of kernels, memsets and device copies for a given schedule,
-// spectral bounds, tiles and buffers, so it is captured once and replayed;
-// any change of that key re-captures it.  Small grids and the coarse levels
+// tiles and buffers, so it is captured once and replayed; any change of that
+// key re-captures it.  The Chebyshev coefficients are read from the device
+// table, so new spectral bounds need no new capture.  Small grids and the coarse levels
 // are launch-bound, and one graph launch replaces about forty.
 static void vcycle32(topo_handle* h, int pre, int post, int smoother, const ChebParams& cp, bool zero0) {
-  if (!h->graphs) {
+  if (!h->graphs || h->in_capture) {  // (inside a capture the cycle's kernels join the captured graph)
     vcycle_core<float>(h, pre, post, true, smoother, cp, zero0);
     return;
   }
   prof_collect(h);
-  std::vector<double> key = {(double)pre, (double)post, (double)smoother, (double)cp.degree, cp.lo, cp.hi,
-                             (double)h->tz32, (double)h->nb, (double)h->prof, (double)zero0,
-                             (double)h->vdot_on, (double)(uintptr_t)h->vdot_out};
-  for (const DevLevel& L : h->lv) {
-    key.push_back(L.lmax32);
-    key.push_back((double)(uintptr_t)L.U32);
-    key.push_back((double)(uintptr_t)L.F32);
-  }
+  const std::vector<double> key = vcycle_key(h, pre, post, smoother, cp, zero0);
   if (!h->vgraph || key != h->vkey) {
     if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
     prof_drop_graph_events(h);
@@ -536,6 +561,44 @@ __global__ void k_to_double(int64_t n, const T* a, double* b) {
 }
 
 inline unsigned nb256(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+// Loop control of the device-side inner CG (slots loop[0..3]: iterations of
+// this solve, ||b|| reference, first non-finite iteration (1-based, 0 none),
+// iterations summed over the solve).  Start: zero the count, take ||b|| from
+// the outer residual (1 if that is 0) and test ||r|| / ||b|| > rtol.
+__global__ void k_loop_start(double* loop, const double* rr_outer, const double* rr, double rtol, int maxit,
+                             cudaGraphConditionalHandle hc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double bo = sqrt(*rr_outer);
+  const double bn = bo > 0 ? bo : 1.0;
+  loop[0] = 0.0;
+  loop[1] = bn;
+  cudaGraphSetConditional(hc, (sqrt(*rr) / bn > rtol && 0 < maxit) ? 1u : 0u);
+}
+
+// End of one iteration: count it and test again; a non-finite ||r|| stops the
+// loop and is recorded.
+__global__ void k_loop_step(double* loop, const double* rr, double rtol, int maxit, cudaGraphConditionalHandle hc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double it = loop[0] + 1.0;
+  loop[0] = it;
+  loop[3] += 1.0;
+  const double rn = sqrt(*rr);
+  unsigned go = 0;
+  if (!isfinite(rn)) {
+    if (loop[2] == 0.0) loop[2] = it;
+  } else {
+    go = (rn / loop[1] > rtol && it < (double)maxit) ? 1u : 0u;
+  }
+  cudaGraphSetConditional(hc, go);
+}
+
+// beta = (r.z - z.rold) / rold.z after the first iteration (the host loop's
+// scalar ratio, taken when the iteration counter is past 0).
+__global__ void k_loop_beta(const double* loop, double* sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (loop[0] > 0.0) sc[S_BETA] = (sc[S_RZ] - sc[S_ZROLD]) / sc[S_RZOLD];
+}
 
 int read_scalars(topo_handle* h, int first, int count);
 
@@ -618,16 +681,105 @@ int estimate_bounds(topo_handle* h) {
   return TOPO_OK;
 }
 
+// Chebyshev coefficients of every level in precision T from the spectral
+// bounds [lo, hi] x lmax (three-term recurrence, Saad, Iterative Methods for
+// Sparse Linear Systems, Alg. 12.1), written to the device table when they
+// changed.  The copy is from pageable host memory, which the runtime stages
+// before the call returns, so the host vector may change right after.
 template <typename T>
-int prepare_smoother(topo_handle* h, int smoother) {
+int cheb_upload(topo_handle* h, const ChebParams& cp) {
+  if (cp.degree > CHEB_MAX_DEG)
+    return fail(h, TOPO_E_BAD_INPUT, "Chebyshev degree %d above %d", cp.degree, CHEB_MAX_DEG);
+  std::vector<double> tab(2 * S_MAXLEV * CHEB_MAX_DEG, 0.0);
+  for (int l = 0; l < (int)h->lv.size(); ++l) {
+    const double lm = P<T>::lmax(h->lv[l]);
+    const double lmax = lm * cp.hi, lmin = lm * cp.lo;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    const double sigma = theta / delta;
+    double rho_old = 1.0 / sigma;
+    for (int k = 0; k < cp.degree; ++k) {
+      double c_old = 0.0, c_new = 1.0 / theta;
+      if (k > 0) {
+        const double rho_new = 1.0 / (2.0 * sigma - rho_old);
+        c_old = rho_new * rho_old;
+        c_new = 2.0 * rho_new / delta;
+        rho_old = rho_new;
+      }
+      tab[2 * (l * CHEB_MAX_DEG + k)] = c_old;
+      tab[2 * (l * CHEB_MAX_DEG + k) + 1] = c_new;
+    }
+  }
+  const size_t off = (size_t)P<T>::table * tab.size();
+  if (!std::equal(tab.begin(), tab.end(), h->chebc_host.begin() + off)) {
+    std::copy(tab.begin(), tab.end(), h->chebc_host.begin() + off);
+    CK(cudaMemcpyAsync(h->chebc + off, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->stream));
+  }
+  return TOPO_OK;
+}
+
+template <typename T>
+int prepare_smoother(topo_handle* h, int smoother, const ChebParams& cp) {
   if (smoother != TOPO_SMOOTH_CHEBYSHEV) return TOPO_OK;
-  return estimate_bounds<T>(h);
+  RET(estimate_bounds<T>(h));
+  return cheb_upload<T>(h, cp);
 }
 
 int read_scalars(topo_handle* h, int first, int count) {
   CK(cudaMemcpyAsync(h->hsc + first, h->sc + first, sizeof(double) * count, cudaMemcpyDeviceToHost,
                      h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  return TOPO_OK;
+}
+
+// One iteration of the flexible CG below: z = M r, the new direction d,
+// q = A d with d.q, x += alpha d, r -= alpha q with the new r.r in sc[S_RR].
+// `it` is the iteration number when the host runs the loop; it is -1 when the
+// loop runs on the device (the graphed inner solve), where the iteration
+// counter in the loop slots tells the first iteration from the others.
+template <typename T, typename Prec>
+int fcg_body(topo_handle* h, T* x, T* r, T* d, T* q, T* rold, T* z, double* sc, Prec&& prec, bool prec_dots,
+             int it) {
+  DevLevel& L0 = h->lv[0];
+  const int64_t n3 = 3 * L0.d.nv;
+  RET(prec(r, z));
+  if (!prec_dots) {  // else the preconditioner left r.z and z.rold in the scalar slots
+    launch_dot<T>(h->stream, r, z, n3, h->partial, sc + S_RZ, h->ctr);
+    count_launch();
+    if (it != 0) {
+      launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD, h->ctr);
+      count_launch();
+    }
+  }
+  if (it < 0) {
+    k_loop_beta<<<1, 32, 0, h->stream>>>(h->sc + S_LOOP, sc);
+    count_launch();
+  } else if (it > 0) {
+    launch_scalar_ratio(h->stream, sc, S_RZ, S_ZROLD, S_RZOLD, S_BETA);
+  }
+  launch_pcg_dir<T>(h->stream, z, d, sc, S_BETA, it == 0, n3, it < 0 ? h->sc + S_LOOP : nullptr);
+  // q = A d with d.q: fused into the FP32 operator's epilogue
+  int nparts = 0;
+  if (sizeof(T) == 4 && h->fdot && h->nb == 1) {
+    EventPair* ev = prof_begin(h, P<T>::fam_apply);
+    nparts = launch_fine_apply_dot<T>(h->stream, L0.d, P<T>::rhop(h), L0.vmask, d, q, h->tz32, h->fdot,
+                                      h->fdot_cap, sc + S_DQ, h->ctr);
+    prof_end(h, ev);
+  }
+  if (nparts > 0) {
+    count_launch();
+  } else {
+    level_apply<T>(h, 0, d, nullptr, q, false);
+    launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ, h->ctr);
+    count_launch();
+  }
+  launch_scalar_ratio(h->stream, sc, S_RZ, -1, S_DQ, S_ALPHA);
+  // x += alpha d, rold = r, r -= alpha q with r.r of the new residual; rold
+  // is not kept when the preconditioner runs the plain (Fletcher-Reeves) form
+  launch_pcg_update_rr<T>(h->stream, x, r, (prec_dots && h->inner_fr) ? nullptr : rold, d, q, sc, S_ALPHA, n3,
+                          h->partial, sc + S_RR, h->ctr);
+  CK(cudaMemcpyAsync(sc + S_RZOLD, sc + S_RZ, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  count_launch(it > 0 ? 4 : 3);
+  CKL();
   return TOPO_OK;
 }
 
@@ -654,40 +806,7 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
   const double bn = bnorm_ref;
   int it = 0;
   while (rn / bn > rtol && it < maxit) {
-    RET(prec(r, z));
-    if (!prec_dots) {  // else the preconditioner left r.z and z.rold in the scalar slots
-      launch_dot<T>(h->stream, r, z, n3, h->partial, sc + S_RZ, h->ctr);
-      count_launch();
-      if (it > 0) {
-        launch_dot<T>(h->stream, z, rold, n3, h->partial, sc + S_ZROLD, h->ctr);
-        count_launch();
-      }
-    }
-    if (it > 0) launch_scalar_ratio(h->stream, sc, S_RZ, S_ZROLD, S_RZOLD, S_BETA);
-    launch_pcg_dir<T>(h->stream, z, d, sc, S_BETA, it == 0, n3);
-    // q = A d with d.q: fused into the FP32 operator's epilogue
-    int nparts = 0;
-    if (sizeof(T) == 4 && h->fdot && h->nb == 1) {
-      EventPair* ev = prof_begin(h, P<T>::fam_apply);
-      nparts = launch_fine_apply_dot<T>(h->stream, L0.d, P<T>::rhop(h), L0.vmask, d, q, h->tz32, h->fdot,
-                                        h->fdot_cap, sc + S_DQ, h->ctr);
-      prof_end(h, ev);
-    }
-    if (nparts > 0) {
-      count_launch();
-    } else {
-      level_apply<T>(h, 0, d, nullptr, q, false);
-      launch_dot<T>(h->stream, d, q, n3, h->partial, sc + S_DQ, h->ctr);
-      count_launch();
-    }
-    launch_scalar_ratio(h->stream, sc, S_RZ, -1, S_DQ, S_ALPHA);
-    // x += alpha d, rold = r, r -= alpha q with r.r of the new residual; rold
-    // is not kept when the preconditioner runs the plain (Fletcher-Reeves) form
-    launch_pcg_update_rr<T>(h->stream, x, r, (prec_dots && h->inner_fr) ? nullptr : rold, d, q, sc, S_ALPHA, n3,
-                            h->partial, sc + S_RR, h->ctr);
-    CK(cudaMemcpyAsync(sc + S_RZOLD, sc + S_RZ, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-    count_launch(it > 0 ? 4 : 3);
-    CKL();
+    RET(fcg_body<T>(h, x, r, d, q, rold, z, sc, prec, prec_dots, it));
     RET(read_scalars(h, base + S_RR, 1));
     rn = std::sqrt(h->hsc[base + S_RR]);
     if (!std::isfinite(rn)) return fail(h, TOPO_E_NONFINITE, "CG residual became non-finite at iteration %d", it);
@@ -695,6 +814,104 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
   }
   *iters = it;
   *rel_out = rn / bn;
+  return TOPO_OK;
+}
+
+// The FP32 inner CG of the mixed solve, z = CG(r) from x = 0, as one CUDA
+// graph: set-up (r in FP32, x = 0, r.r and the stopping test), a WHILE node
+// whose body is one CG iteration (fcg_body) closed by a kernel that counts the
+// iteration and sets the loop condition, and the copy of x to FP64 in z.  The
+// iterations are the host loop's, kernel for kernel, with the same stopping
+// rule (||r|| / ||b|| > rtol and fewer than maxit iterations; ||b|| is the
+// outer residual's norm, 1 if that is 0) decided on the device, so the host
+// does not wait for the GPU between inner iterations.  The graph is captured
+// once per key (buffers, schedule, bounds, tiles) and replayed.  Iteration
+// totals and a non-finite r.r are left in the loop slots for the caller.
+template <typename Prec>
+int inner_cg_graphed(topo_handle* h, const double* rin, double* zout, double rtol, int maxit, Prec&& prec,
+                     std::vector<double> key) {
+  DevLevel& L0 = h->lv[0];
+  const int64_t n3 = 3 * L0.d.nv;
+  double* sc = h->sc + 8;
+  key.insert(key.end(), {rtol, (double)maxit, (double)(uintptr_t)rin, (double)(uintptr_t)zout,
+                         (double)(uintptr_t)h->x32, (double)(uintptr_t)h->d32, (double)(uintptr_t)h->q32,
+                         (double)h->tz32, (double)(uintptr_t)h->fdot, (double)h->fdot_cap});
+  if (!h->igraph || key != h->ikey) {
+    if (h->igraph) { cudaGraphExecDestroy(h->igraph); h->igraph = nullptr; }
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle hc = 0;
+    cudaGraphNode_t cnode = nullptr;
+    std::vector<cudaGraphNode_t> deps;
+    const long long l0 = g_launches.load();
+    long long l1 = l0, l2 = l0;
+    int rc = TOPO_OK;
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+              cudaGraphConditionalHandleCreate(&hc, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+    // set-up, captured into g; its last nodes are the loop's dependencies
+    if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      h->in_capture = true;
+      launch_d2f(h->stream, rin, L0.F32, n3);
+      cudaMemsetAsync(h->x32, 0, sizeof(float) * n3, h->stream);
+      launch_dot<float>(h->stream, L0.F32, L0.F32, n3, h->partial, sc + S_RR, h->ctr);
+      k_loop_start<<<1, 32, 0, h->stream>>>(h->sc + S_LOOP, h->sc + S_RR, sc + S_RR, rtol, maxit, hc);
+      count_launch(3);
+      cudaStreamCaptureStatus cs;
+      const cudaGraphNode_t* dp = nullptr;
+      size_t nd = 0;
+      ok = cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, nullptr, &dp, nullptr, &nd) == cudaSuccess;
+      if (ok) deps.assign(dp, dp + nd);
+      cudaGraph_t gs = nullptr;
+      ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && ok;
+    }
+    // the loop node and its body
+    cudaGraph_t body = nullptr;
+    if (ok) {
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = hc;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      ok = cudaGraphAddNode(&cnode, g, deps.data(), nullptr, deps.size(), &cp) == cudaSuccess;
+      if (ok) body = cp.conditional.phGraph_out[0];
+    }
+    if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      l1 = g_launches.load();
+      rc = fcg_body<float>(h, h->x32, L0.F32, h->d32, h->q32, h->rold32, L0.U32, sc, prec, true, -1);
+      k_loop_step<<<1, 32, 0, h->stream>>>(h->sc + S_LOOP, sc + S_RR, rtol, maxit, hc);
+      count_launch();
+      l2 = g_launches.load();
+      cudaGraph_t gs = nullptr;
+      ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && rc == TOPO_OK;
+    }
+    // z = x in FP64 after the loop
+    if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, g, &cnode, nullptr, 1,
+                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      k_to_double<float><<<nb256(n3), 256, 0, h->stream>>>(n3, h->x32, zout);
+      count_launch();
+      cudaGraph_t gs = nullptr;
+      ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess;
+    }
+    h->in_capture = false;
+    h->igraph_body = l2 - l1;
+    h->igraph_fixed = (g_launches.load() - l0) - h->igraph_body;
+    g_launches.fetch_sub(g_launches.load() - l0);
+    if (ok) ok = cudaGraphInstantiate(&h->igraph, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (!ok) {  // conditional graphs not available: the host runs the loop from now on
+      h->igraph = nullptr;
+      h->igraph_ok = false;
+      return TOPO_E_STATE;
+    }
+    h->ikey = key;
+  }
+  CK(cudaGraphLaunch(h->igraph, h->stream));
+  count_launch((int)h->igraph_fixed);
   return TOPO_OK;
 }
 
@@ -829,6 +1046,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     A(dalloc(hp, &h->fdot, h->fdot_cap));
     A(dalloc(hp, &h->vdot, h->fdot_cap));
     A(dalloc(hp, &h->ctr, 1));
+    A(dalloc(hp, &h->chebc, CHEB_TABLE));
   }
   if (rc == TOPO_OK && nl > 1) {
     const LevelDims& dl = h->lv.back().d;
@@ -853,6 +1071,9 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
   }
   if (rc == TOPO_OK) {
     cudaMemcpyAsync(h->dKe, h->Ke, sizeof(double) * 576, cudaMemcpyHostToDevice, h->stream);
+    h->chebc_host.assign(CHEB_TABLE, 0.0);
+    h->chebc_host[CHEB_TABLE - 1] = 1.0;
+    cudaMemcpyAsync(h->chebc, h->chebc_host.data(), sizeof(double) * CHEB_TABLE, cudaMemcpyHostToDevice, h->stream);
     cudaHostAlloc((void**)&h->hsc, sizeof(double) * S_COUNT, cudaHostAllocDefault);
     // density starts at 1 on active elements
     std::vector<double> one(d0.ne);
@@ -883,6 +1104,7 @@ void topo_destroy(topo_handle* h) {
   if (h->unet) unet_free(h->unet);
   if (h->mat_registered) material_release(h->cfg.device);
   if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
+  if (h->igraph) cudaGraphExecDestroy(h->igraph);
   prof_drop_graph_events(h);
   if (h->multi) {
     for (void* p : h->multi->allocs) cudaFree(p);
@@ -1319,7 +1541,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     st.relres = 0.0;
   } else if (o->mode == TOPO_SOLVE_VCYCLE) {
     if (!h->ops64) return fail(h, TOPO_E_STATE, "FP64 operators not built");
-    RET(prepare_smoother<double>(h, o->smoother));
+    RET(prepare_smoother<double>(h, o->smoother, cp));
     double rr = 1.0;
     int it = 0;
     while (rr > o->rtol && it < o->max_iter) {
@@ -1338,7 +1560,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     st.relres = rr;
   } else if (o->mode == TOPO_SOLVE_PCG64) {
     if (!h->ops64) return fail(h, TOPO_E_STATE, "FP64 operators not built");
-    RET(prepare_smoother<double>(h, o->smoother));
+    RET(prepare_smoother<double>(h, o->smoother, cp));
     CK(cudaMemcpyAsync(h->x, L0.U, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->f, L0.F, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     int it = 0;
@@ -1362,7 +1584,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     // preconditioner is an FP32 multigrid solve: one FP32 V-cycle, or up to
     // inner_max FP32 FCG iterations to a relative reduction of inner_rtol.
     if (!h->ops32) return fail(h, TOPO_E_STATE, "FP32 operators not built");
-    RET(prepare_smoother<float>(h, o->smoother));
+    RET(prepare_smoother<float>(h, o->smoother, cp));
     CK(cudaMemcpyAsync(h->x, L0.U, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(h->f, L0.F, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-1;
@@ -1396,6 +1618,11 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
     // network (a varying preconditioner) it stays flexible, with separate
     // r.z and z.rold after the cycle.
     const bool vdots = o->smoother == TOPO_SMOOTH_CHEBYSHEV && o->post >= 1 && cp.degree >= 1 && h->nb == 1;
+    // the inner CG on the device (one graph per inner solve) where its
+    // iteration is a fixed kernel sequence: fused r.z, no network, no profiler
+    bool igraph = h->graphs && h->igraph_ok && !h->prof && vdots && !o->learned && inner_max > 1;
+    bool igraph_used = false;
+    if (igraph) CK(cudaMemsetAsync(h->sc + S_LOOP + 2, 0, 2 * sizeof(double), h->stream));
     auto prec32 = [&](const float* r, float* z) -> int {
       (void)z;
       ++nvc;
@@ -1454,13 +1681,28 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
         count_launch(2);
         return TOPO_OK;
       }
+      if (igraph) {  // the whole inner solve as one graph launch, no host wait
+        const int nvc0 = nvc;  // (a capture runs prec32 once on the host)
+        h->vdot_on = true;
+        h->vdot_out = h->sc + 8 + S_RZ;
+        const int grc = inner_cg_graphed(h, r, z, inner_rtol, inner_max, prec32,
+                                         vcycle_key(h, o->pre, o->post, o->smoother, cp, true));
+        h->vdot_on = false;
+        nvc = nvc0;
+        if (grc == TOPO_OK) {
+          igraph_used = true;
+          return TOPO_OK;
+        }
+        if (h->igraph_ok) return grc;
+        igraph = false;  // capture failed: the host loop from here on
+      }
       launch_d2f(h->stream, r, L0.F32, n3);
       CK(cudaMemsetAsync(h->x32, 0, sizeof(float) * n3, h->stream));
       count_launch();
       int iit = 0;
       double irel = 0;
-      // relative to ||r|| (FP64 norm of the outer residual)
-      RET(read_scalars(h, S_RR, 1));
+      // relative to ||r||, the FP64 norm of the outer residual, which the
+      // outer CG has just read into the host slots
       const double rnorm = std::sqrt(h->hsc[S_RR]);
       // the inner residual lives in level-0 F32, the V-cycle's right-hand side,
       // so the preconditioner needs no copy; x32 = 0 gives r = b without a matvec
@@ -1474,6 +1716,15 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
                        &it, &rel, fn);
     CK(cudaMemcpyAsync(L0.F, h->f, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(L0.U, h->x, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    if (igraph_used) {  // inner iterations the device ran, and a non-finite inner residual
+      RET(read_scalars(h, S_LOOP + 2, 2));
+      const long long inner_its = (long long)h->hsc[S_LOOP + 3];
+      nvc += (int)inner_its;
+      count_launch((int)(inner_its * h->igraph_body));
+      if (h->hsc[S_LOOP + 2] != 0.0)
+        return fail(h, TOPO_E_NONFINITE, "inner CG residual became non-finite at iteration %d",
+                    (int)h->hsc[S_LOOP + 2] - 1);
+    }
     if (rc != TOPO_OK) return rc;
     if (harvest) {
       const cudaError_t e = unet_harvest_finish(h->unet, h->stream, L0.d, L0.vmask, h->x, h->unet_crops, h->partial);
@@ -1607,6 +1858,8 @@ int topo_set_graphs(topo_handle* h, int enable) {
   if (!h) return TOPO_E_BAD_INPUT;
   h->graphs = enable != 0;
   if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
+  if (h->igraph) { cudaGraphExecDestroy(h->igraph); h->igraph = nullptr; }
+  h->igraph_ok = true;
   return TOPO_OK;
 }
 
@@ -1673,7 +1926,12 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
   cudaEvent_t t0, t1, a, b;
   CK(cudaEventCreate(&t0)); CK(cudaEventCreate(&t1)); CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
   CK(cudaEventRecord(t0, h->stream));
-  RET(prepare_smoother<float>(h, TOPO_SMOOTH_CHEBYSHEV));
+  ChebParams cp;
+  if (base->cheb_degree > 0) cp.degree = base->cheb_degree;
+  if (base->cheb_lo > 0) cp.lo = base->cheb_lo;
+  if (base->cheb_hi > 0) cp.hi = base->cheb_hi;
+  RET(prepare_smoother<float>(h, TOPO_SMOOTH_CHEBYSHEV, cp));
+  const double* unit = h->chebc + CHEB_TABLE - 2;  // (c_old, c_new) = (0, 1)
   // ---- stage 1: z-march depth of the fine kernels
   const int tzs[4] = {4, 8, 16, 32};
   int best32 = h->tz32, best64 = h->tz64;
@@ -1683,7 +1941,7 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
       CK(cudaEventRecord(a, h->stream));
       for (int i = 0; i < 5; ++i)
         launch_fine_cheb<float>(h->stream, L0.d, h->rhop32, L0.vmask, L0.U32, L0.F32, L0.U2_32, L0.dinv32, L0.cd32,
-                                0.0, 1.0, true, 1, tzs[k]);
+                                unit, true, 1, tzs[k]);
       CK(cudaEventRecord(b, h->stream));
       CK(cudaEventSynchronize(b));
       float ms = 0;
@@ -1801,7 +2059,7 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
   if (o->cheb_degree > 0) cp.degree = o->cheb_degree;
   if (o->cheb_lo > 0) cp.lo = o->cheb_lo;
   if (o->cheb_hi > 0) cp.hi = o->cheb_hi;
-  RET(prepare_smoother<float>(h, TOPO_SMOOTH_CHEBYSHEV));
+  RET(prepare_smoother<float>(h, TOPO_SMOOTH_CHEBYSHEV, cp));
   MultiRhs& m = *h->multi;
   DevLevel& L0 = h->lv[0];
   const int nb = nrhs;

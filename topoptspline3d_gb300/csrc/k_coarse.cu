@@ -139,7 +139,8 @@ template <typename T>
 __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* __restrict__ st,
                                                          const T* __restrict__ u, const T* __restrict__ f,
                                                          T* __restrict__ uout, const T* __restrict__ dinv,
-                                                         T* __restrict__ dv, T c_old, T c_new, bool first) {
+                                                         T* __restrict__ dv, const double* __restrict__ coef,
+                                                         bool first) {
   __shared__ T sr[3][SV];
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
@@ -161,6 +162,7 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* _
   const T zz = dinv[(3 * row) * nv + v] * sr[0][lv] + dinv[(3 * row + 1) * nv + v] * sr[1][lv] +
                dinv[(3 * row + 2) * nv + v] * sr[2][lv];
   const int64_t i = row * nv + v;
+  const T c_old = (T)__ldg(coef), c_new = (T)__ldg(coef + 1);
   const T dn = first ? c_new * zz : c_old * dv[i] + c_new * zz;
   dv[i] = dn;
   uout[i] = u[i] + dn;
@@ -222,7 +224,8 @@ template <typename T>
 __global__ void __launch_bounds__(32 * WV) k_stencil_cheb_warp(LevelDims d, const T* __restrict__ st,
                                                                const T* __restrict__ u, const T* __restrict__ f,
                                                                T* __restrict__ uout, const T* __restrict__ dinv,
-                                                               T* __restrict__ dv, T c_old, T c_new, bool first) {
+                                                               T* __restrict__ dv, const double* __restrict__ coef,
+                                                               bool first) {
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
   f += bo;
@@ -239,6 +242,7 @@ __global__ void __launch_bounds__(32 * WV) k_stencil_cheb_warp(LevelDims d, cons
     const T zz = dinv[(3 * lane) * nv + v] * r0 + dinv[(3 * lane + 1) * nv + v] * r1 +
                  dinv[(3 * lane + 2) * nv + v] * r2;
     const int64_t i = lane * nv + v;
+    const T c_old = (T)__ldg(coef), c_new = (T)__ldg(coef + 1);
     const T dn = first ? c_new * zz : c_old * dv[i] + c_new * zz;
     dv[i] = dn;
     uout[i] = u[i] + dn;
@@ -259,26 +263,25 @@ void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const
 
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
-                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb) {
+                         const T* dinv, T* dvec, const double* coef, bool first, int nb) {
   if (d.nv < STENCIL_WARP_MAX_NV)
-    k_stencil_cheb_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
-                                                                         (T)c_new, first);
+    k_stencil_cheb_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
   else
-    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, (T)c_old,
-                                                                  (T)c_new, first);
+    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,
-                                          const double*, double*, const double*, double*, double, double, bool, int);
+                                          const double*, double*, const double*, double*, const double*, bool, int);
 template void launch_stencil_cheb<float>(cudaStream_t, const LevelDims&, const float*, const float*,
-                                         const float*, float*, const float*, float*, double, double, bool, int);
+                                         const float*, float*, const float*, float*, const double*, bool, int);
 
 // First Chebyshev step from a zero iterate with a stored block-Jacobi inverse
 // (coarse levels; FP64 level 0 with its free-DOF mask): r = f, d = c_new D^-1 r,
 // u_out = d.  Equals the full step on u = 0, since A 0 = 0 exactly.
 template <typename T>
 __global__ void k_cheb_zero_stored(int64_t nv, const uint8_t* __restrict__ vmask, const T* __restrict__ dinv,
-                                   const T* __restrict__ f, T* __restrict__ dv, T* __restrict__ uout, T c_new) {
+                                   const T* __restrict__ f, T* __restrict__ dv, T* __restrict__ uout,
+                                   const double* __restrict__ coef) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   const int64_t bo = (int64_t)blockIdx.y * 3 * nv;
@@ -289,6 +292,7 @@ __global__ void k_cheb_zero_stored(int64_t nv, const uint8_t* __restrict__ vmask
   T r[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] : T(0);
+  const T c_new = (T)__ldg(coef + 1);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const T zz = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
@@ -300,14 +304,14 @@ __global__ void k_cheb_zero_stored(int64_t nv, const uint8_t* __restrict__ vmask
 
 template <typename T>
 void launch_cheb_zero_stored(cudaStream_t s, int64_t nv, const uint8_t* vmask, const T* dinv, const T* f, T* dvec,
-                             T* uout, double c_new, int nb) {
-  k_cheb_zero_stored<T><<<dim3(nblk(nv, 256), nb), 256, 0, s>>>(nv, vmask, dinv, f, dvec, uout, (T)c_new);
+                             T* uout, const double* coef, int nb) {
+  k_cheb_zero_stored<T><<<dim3(nblk(nv, 256), nb), 256, 0, s>>>(nv, vmask, dinv, f, dvec, uout, coef);
 }
 
 template void launch_cheb_zero_stored<double>(cudaStream_t, int64_t, const uint8_t*, const double*, const double*,
-                                              double*, double*, double, int);
+                                              double*, double*, const double*, int);
 template void launch_cheb_zero_stored<float>(cudaStream_t, int64_t, const uint8_t*, const float*, const float*,
-                                             float*, float*, double, int);
+                                             float*, float*, const double*, int);
 
 template <typename T>
 void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask, T* u,

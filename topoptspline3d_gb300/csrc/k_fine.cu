@@ -283,7 +283,7 @@ __device__ __forceinline__ void modal_element(T c[3][8], T pe, T* energy = nullp
 struct ChebArgs {
   const void* dinv;  // [9][nv]
   void* dvec;        // [3][nv]
-  double c_old, c_new;
+  const double* coef;  // (c_old, c_new) of the step, in device memory
   int first;
   double* dotp;      // per-CTA partial sums: MODE 0 u.out, FP32 MODE 3 f.out (null: none)
   int d_is_u;        // MODE 2, FP32: d equals u on entry (the step after a zero start); dvec is not read
@@ -567,7 +567,8 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
             zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const T dn = ch.first ? T(ch.c_new) * zc[c] : T(ch.c_old) * dv_c[c] + T(ch.c_new) * zc[c];
+            const T c_old = T(__ldg(ch.coef)), c_new = T(__ldg(ch.coef + 1));
+            const T dn = ch.first ? c_new * zc[c] : c_old * dv_c[c] + c_new * zc[c];
             dv[c * nv + v] = dn;
             out[c * nv + v] = uv[c] + dn;
           }
@@ -607,6 +608,7 @@ struct Modal32Smem {
   float4 plane[4][NP];  // vertex planes (u0, u1, u2, -) in a 4-slot ring
   float4 xa[2][NT];     // exchanged y = 0 forces: (z = 0: c0, c1, c2; z = 1: c0)
   float2 xb[2][NT];     //                         (z = 1: c1, c2)
+  float coef[2];        // Chebyshev (c_old, c_new), read after each plane's barrier
 };
 
 template <int TYE, int MODE>
@@ -622,6 +624,10 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   extern __shared__ __align__(16) unsigned char m32_smem[];
   S& sm = *reinterpret_cast<S*>(m32_smem);
   const int t = threadIdx.x, i = t & 31, j = t >> 5;
+  if (CHEB && t == 0) {
+    sm.coef[0] = float(ch.coef[0]);
+    sm.coef[1] = float(ch.coef[1]);
+  }
   const int zblk = (d.vz + TZ - 1) / TZ;
   const int rhs = blockIdx.z / zblk;
   const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
@@ -739,7 +745,8 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const float dold = ch.d_is_u ? uv[c] : dv_c[c];
-              const float dn = ch.first ? float(ch.c_new) * zc[c] : float(ch.c_old) * dold + float(ch.c_new) * zc[c];
+              const float c_old = sm.coef[0], c_new = sm.coef[1];
+              const float dn = ch.first ? c_new * zc[c] : c_old * dold + c_new * zc[c];
               dv[c * nv + v] = dn;
               const float o = uv[c] + dn;
               out[c * nv + v] = o;
@@ -1142,7 +1149,7 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
 template <typename T>
 void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                        const T* u, const T* f, T* out, bool residual, int nb, int tz) {
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, nullptr, 0, nullptr, nullptr};
+  const ChebArgs ch{nullptr, nullptr, nullptr, 0, nullptr, 0, nullptr, nullptr};
   if (residual) launch_modal<T, 1>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
   else launch_modal<T, 0>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
 }
@@ -1157,7 +1164,7 @@ int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, con
   const dim3 grid = modal_grid<T>(d, tz, 1);
   const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
   if (nparts > cap) return 0;
-  const ChebArgs ch{nullptr, nullptr, 0.0, 0.0, 0, partial, 0, dot, dot ? ctr : nullptr};
+  const ChebArgs ch{nullptr, nullptr, nullptr, 0, partial, 0, dot, dot ? ctr : nullptr};
   launch_modal<T, 0>(s, d, rhop, vmask, u, nullptr, out, tz, 1, ch);
   return (int)nparts;
 }
@@ -1189,10 +1196,11 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
     k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, nullptr);
 }
 
-// One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u).
+// One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u)
+// and (c_old, c_new) = coef[0..1] in device memory.
 template <typename T>
 int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                     const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb,
+                     const T* f, T* uout, const T* dinv, T* dvec, const double* coef, bool first, int nb,
                      int tz, bool d_is_u, double* dot_fo, int cap, double* dot, unsigned* ctr) {
   // the FP64 kernel always reads d and has no fused dots
   int nparts = 0;
@@ -1200,7 +1208,7 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
     const dim3 grid = modal_grid<T>(d, tz <= 0 ? MODAL_TZ : tz, 1);
     nparts = (int64_t)grid.x * grid.y * grid.z <= cap ? (int)(grid.x * grid.y * grid.z) : 0;
   }
-  const ChebArgs ch{dinv, dvec, c_old, c_new, first ? 1 : 0, nparts ? dot_fo : nullptr,
+  const ChebArgs ch{dinv, dvec, coef, first ? 1 : 0, nparts ? dot_fo : nullptr,
                     (d_is_u && sizeof(T) == 4) ? 1 : 0, dot, (nparts && dot) ? ctr : nullptr};
   if constexpr (sizeof(T) == 4) {
     if (nparts) {  // the step with the fused sums is its own instantiation
@@ -1213,10 +1221,10 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
 }
 
 template int launch_fine_cheb<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
-                                      const double*, const double*, double*, const double*, double*, double,
-                                      double, bool, int, int, bool, double*, int, double*, unsigned*);
+                                      const double*, const double*, double*, const double*, double*,
+                                      const double*, bool, int, int, bool, double*, int, double*, unsigned*);
 template int launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
-                                     const float*, const float*, float*, const float*, float*, double, double,
+                                     const float*, const float*, float*, const float*, float*, const double*,
                                      bool, int, int, bool, double*, int, double*, unsigned*);
 
 // First Chebyshev step from a zero iterate (every pre-smoothing sweep of a
@@ -1228,7 +1236,7 @@ template int launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float
 // the stored inverse.  blockIdx.y is the right-hand side of a batch.
 __global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
                                    const float* __restrict__ f, float* __restrict__ dv, float* __restrict__ out,
-                                   float c_new) {
+                                   const double* __restrict__ coef) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= d.nv) return;
   const int64_t nv = d.nv, bo = (int64_t)blockIdx.y * 3 * nv;
@@ -1270,6 +1278,7 @@ __global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, 
 #pragma unroll
   for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] : 0.f;
   block_solve_free<float>(S, (m & 8) ? (m & 7) : 0, r, zc);
+  const float c_new = (float)__ldg(coef + 1);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const float dn = c_new * zc[c];
@@ -1280,20 +1289,20 @@ __global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, 
 
 template <typename T>
 void launch_fine_cheb_zero(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* f,
-                           T* uout, const T* dinv, T* dvec, double c_new, int nb) {
+                           T* uout, const T* dinv, T* dvec, const double* coef, int nb) {
   if (sizeof(T) == 4) {  // dvec may be null: d is not stored (the next step takes d = u)
     k_fine_cheb_zero32<<<dim3(blocks_for(d.nv, 256), nb), 256, 0, s>>>(
         d, reinterpret_cast<const float*>(rhop), vmask, reinterpret_cast<const float*>(f),
-        reinterpret_cast<float*>(dvec), reinterpret_cast<float*>(uout), (float)c_new);
+        reinterpret_cast<float*>(dvec), reinterpret_cast<float*>(uout), coef);
   } else {
-    launch_cheb_zero_stored<T>(s, d.nv, vmask, dinv, f, dvec, uout, c_new, nb);
+    launch_cheb_zero_stored<T>(s, d.nv, vmask, dinv, f, dvec, uout, coef, nb);
   }
 }
 
 template void launch_fine_cheb_zero<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
-                                            const double*, double*, const double*, double*, double, int);
+                                            const double*, double*, const double*, double*, const double*, int);
 template void launch_fine_cheb_zero<float>(cudaStream_t, const LevelDims&, const float*, const uint8_t*,
-                                           const float*, float*, const float*, float*, double, int);
+                                           const float*, float*, const float*, float*, const double*, int);
 
 // Dense-row form of the same operator (thread per vertex, 8 x 3 x 24 products);
 // kept as the cross-check of the modal kernel.

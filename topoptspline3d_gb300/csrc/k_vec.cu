@@ -186,12 +186,16 @@ void launch_scalar_ratio(cudaStream_t s, double* sc, int num, int sub, int den, 
   k_scalar_ratio<<<1, 32, 0, s>>>(sc, num, sub, den, out);
 }
 
-// d = z + beta d (beta = sc[beta_slot]), or d = z.
+// d = z + beta d (beta = sc[beta_slot]), or d = z.  With first_if_zero the
+// choice is made on the device: d = z when *first_if_zero is 0 (an iteration
+// counter).
 template <typename T>
 __global__ void k_pcg_dir(const T* __restrict__ z, T* __restrict__ d, const double* __restrict__ sc,
-                          int beta_slot, bool first, int64_t n, int packed) {
+                          int beta_slot, bool first_host, int64_t n, int packed,
+                          const double* __restrict__ first_if_zero) {
   constexpr int W = 16 / sizeof(T);
   using P = Pack16<T, W>;
+  const bool first = first_if_zero ? (*first_if_zero == 0.0) : first_host;
   const T beta = first ? T(0) : (T)sc[beta_slot];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t npk = packed ? n / W : 0;
@@ -212,11 +216,11 @@ __global__ void k_pcg_dir(const T* __restrict__ z, T* __restrict__ d, const doub
 // d = z (first) or z + beta d, in 16-byte packs when both vectors are aligned
 template <typename T>
 void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta_slot, bool first,
-                    int64_t n) {
+                    int64_t n, const double* first_if_zero) {
   constexpr int W = 16 / sizeof(T);
   const bool packed = (((uintptr_t)z | (uintptr_t)d) & 15) == 0;
   const int64_t threads = packed ? std::max<int64_t>(n / W, W) : n;
-  k_pcg_dir<T><<<nblk(threads, 256), 256, 0, s>>>(z, d, sc, beta_slot, first, n, packed ? 1 : 0);
+  k_pcg_dir<T><<<nblk(threads, 256), 256, 0, s>>>(z, d, sc, beta_slot, first, n, packed ? 1 : 0, first_if_zero);
 }
 
 // x += alpha d, rold = r, r -= alpha q (alpha = sc[alpha_slot]), fused with the
@@ -288,7 +292,9 @@ template void launch_fill<double>(cudaStream_t, double*, double, int64_t);
 template void launch_fill<float>(cudaStream_t, float*, float, int64_t);
 template void launch_copy<double>(cudaStream_t, const double*, double*, int64_t);
 template void launch_copy<float>(cudaStream_t, const float*, float*, int64_t);
-template void launch_pcg_dir<double>(cudaStream_t, const double*, double*, const double*, int, bool, int64_t);
-template void launch_pcg_dir<float>(cudaStream_t, const float*, float*, const double*, int, bool, int64_t);
+template void launch_pcg_dir<double>(cudaStream_t, const double*, double*, const double*, int, bool, int64_t,
+                                      const double*);
+template void launch_pcg_dir<float>(cudaStream_t, const float*, float*, const double*, int, bool, int64_t,
+                                     const double*);
 
 }  // namespace topo

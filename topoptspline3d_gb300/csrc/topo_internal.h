@@ -98,20 +98,21 @@ void launch_fine_diag_inv(cudaStream_t s, const LevelDims& d, const T* rhop, con
 // none were formed (FP64, a batch, or more CTAs than cap).
 template <typename T>
 int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
-                     const T* f, T* uout, const T* dinv, T* dvec, double c_old, double c_new, bool first,
+                     const T* f, T* uout, const T* dinv, T* dvec, const double* coef, bool first,
                      int nb = 1, int tz = 0, bool d_is_u = false, double* dot_fo = nullptr, int cap = 0,
                      double* dot = nullptr, unsigned* ctr = nullptr);
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
-                         const T* dinv, T* dvec, double c_old, double c_new, bool first, int nb = 1);
-// First Chebyshev step from a zero iterate (u = 0): d = c_new D^-1 f, uout = d.
+                         const T* dinv, T* dvec, const double* coef, bool first, int nb = 1);
+// First Chebyshev step from a zero iterate (u = 0): d = c_new D^-1 f, uout = d,
+// with c_new = coef[1] in device memory.
 // FP32: dvec may be null, and the next step then takes d from u (d_is_u).
 template <typename T>
 void launch_fine_cheb_zero(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* f,
-                           T* uout, const T* dinv, T* dvec, double c_new, int nb = 1);
+                           T* uout, const T* dinv, T* dvec, const double* coef, int nb = 1);
 template <typename T>
 void launch_cheb_zero_stored(cudaStream_t s, int64_t nv, const uint8_t* vmask, const T* dinv, const T* f, T* dvec,
-                             T* uout, double c_new, int nb = 1);
+                             T* uout, const double* coef, int nb = 1);
 template <typename T>
 void launch_fine_apply_dense(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask,
                              const T* u, const T* f, T* out, bool residual);
@@ -169,7 +170,8 @@ void launch_f2d_add(cudaStream_t s, const float* a, double* b, int64_t n);
 // PCG helpers with device-resident scalars (sc: double scalar slots)
 void launch_scalar_ratio(cudaStream_t s, double* sc, int num, int sub, int den, int out);
 template <typename T>
-void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta_slot, bool first, int64_t n);
+void launch_pcg_dir(cudaStream_t s, const T* z, T* d, const double* sc, int beta_slot, bool first, int64_t n,
+                    const double* first_if_zero = nullptr);
 // launch_pcg_update fused with rr = r.r of the updated residual (2 launches);
 // rold may be null (not kept)
 template <typename T>

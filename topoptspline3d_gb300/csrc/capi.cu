@@ -49,6 +49,12 @@ struct EventPair {
 
 }  // namespace
 
+// CTAs per SM of the coarsest inversion when it runs on the side stream next
+// to the solve's set-up kernels
+#ifndef TOPO_GJ_SIDE_PER_SM
+#define TOPO_GJ_SIDE_PER_SM 1
+#endif
+
 struct topo_handle {
   topo_config cfg{};
   topo::UNetState* unet = nullptr;  // learned preconditioner (topo_unet_enable)
@@ -68,6 +74,16 @@ struct topo_handle {
   cudaGraphExec_t igraph = nullptr;
   std::vector<double> ikey;
   long long igraph_fixed = 0, igraph_body = 0;
+  // coarsest inversion of a design iteration on a second stream (side),
+  // overlapped with the solve's set-up; the main stream waits for ev_coarse
+  // before its first V-cycle (coarse_join) and the status is read at the end
+  // of the solve (coarse_finish)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_ops = nullptr, ev_coarse = nullptr;
+  int* hstat = nullptr;           // pinned copy of the inversion status
+  bool defer_coarse = false;      // topo_design_iteration's operator update
+  bool coarse_pending = false;    // the main stream has not waited for it yet
+  bool coarse_unchecked = false;  // its status has not been read yet
   // profiling inside the graph: event pairs captured as external event-record
   // nodes, collected after each replay has completed
   bool capturing = false;
@@ -1102,7 +1118,12 @@ void topo_destroy(topo_handle* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->unet) unet_free(h->unet);
+  if (h->side) cudaStreamSynchronize(h->side);
   if (h->mat_registered) material_release(h->cfg.device);
+  if (h->side) cudaStreamDestroy(h->side);
+  if (h->ev_ops) cudaEventDestroy(h->ev_ops);
+  if (h->ev_coarse) cudaEventDestroy(h->ev_coarse);
+  if (h->hstat) cudaFreeHost(h->hstat);
   if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
   if (h->igraph) cudaGraphExecDestroy(h->igraph);
   prof_drop_graph_events(h);
@@ -1413,6 +1434,30 @@ int topo_update_operators(topo_handle* h) {
     CKL();
     // FP32-only operators: the matrix comes from FP32 stencils; the updates
     // in double-float keep twice their precision on the FP32 pipe
+    if (h->defer_coarse) {  // on the side stream, one CTA per SM, joined later
+      if (!h->side) {
+        CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_ops, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_coarse, cudaEventDisableTiming));
+        CK(cudaHostAlloc((void**)&h->hstat, 2 * sizeof(int), cudaHostAllocDefault));
+      }
+      CK(cudaEventRecord(h->ev_ops, h->stream));
+      CK(cudaStreamWaitEvent(h->side, h->ev_ops, 0));
+      const int e = coarsest_invert(h->side, h->ndense, h->A, h->gjwork, h->status, !b64, TOPO_GJ_SIDE_PER_SM);
+      count_launch();
+      if (e != (int)cudaSuccess)
+        return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));
+      CK(cudaMemcpyAsync(h->hstat, h->status, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->side));
+      launch_to_float(h->side, h->A, h->A32, (int64_t)h->ndense * h->ndense);
+      count_launch();
+      CK(cudaEventRecord(h->ev_coarse, h->side));
+      h->coarse_pending = h->coarse_unchecked = true;
+      for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
+      h->ops64 = b64;
+      h->ops32 = b32;
+      h->ops_ready = true;
+      return TOPO_OK;
+    }
     int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status, !b64);
     count_launch();
     if (e != (int)cudaSuccess)
@@ -1515,7 +1560,34 @@ int topo_vcycle(topo_handle* h, int pre, int post, double* relres) {
   return TOPO_OK;
 }
 
+// The main stream waits for a coarsest inversion running on the side stream.
+static int coarse_join(topo_handle* h) {
+  if (!h->coarse_pending) return TOPO_OK;
+  CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, 0));
+  h->coarse_pending = false;
+  return TOPO_OK;
+}
+
+// Joins the side stream's inversion and reads its status.
+static int coarse_finish(topo_handle* h) {
+  RET(coarse_join(h));
+  if (!h->coarse_unchecked) return TOPO_OK;
+  CK(cudaEventSynchronize(h->ev_coarse));
+  h->coarse_unchecked = false;
+  if (h->hstat[1] != 0) return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", h->hstat[1] - 1);
+  h->coarse_dropped = h->hstat[0];
+  return TOPO_OK;
+}
+
+static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats);
+
 int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats) {
+  const int rc = solve_impl(h, o, stats);
+  if (h) RET(coarse_finish(h));
+  return rc;
+}
+
+static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats) {
   RET(check_ready(h, true));
   h->energy_ready = false;
   if (!o || o->rtol <= 0 || o->max_iter < 0 || o->pre < 0 || o->post < 0) return TOPO_E_BAD_INPUT;
@@ -1536,6 +1608,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
   RET(read_scalars(h, S_FF, 1));
   const double fn = std::sqrt(h->hsc[S_FF]);
   int rc = TOPO_OK;
+  if (o->mode != TOPO_SOLVE_MIXED) RET(coarse_join(h));
   if (fn == 0.0) {
     CK(cudaMemsetAsync(L0.U, 0, sizeof(double) * n3, h->stream));
     st.relres = 0.0;
@@ -1645,6 +1718,7 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
       return TOPO_OK;
     };
     auto prec = [&](const double* r, double* z) -> int {
+      RET(coarse_join(h));  // the first V-cycle needs the coarsest inverse
       const double rn = std::sqrt(h->hsc[S_RR]);
       // Fall back to the plain V-cycle for the rest of the solve when the
       // positivity guard fired (r.z <= 0 with the correction), or after 10
@@ -2464,7 +2538,10 @@ int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_sta
   CK(cudaEventCreate(&e1));
   CK(cudaEventRecord(e0, h->stream));
   topo_iter_stats st{};
-  RET(topo_update_operators(h));
+  h->defer_coarse = true;  // the coarsest inversion overlaps the solve's set-up
+  const int urc = topo_update_operators(h);
+  h->defer_coarse = false;
+  RET(urc);
   h->want_energy = true;
   int rc = topo_solve(h, &o->solve, &st.solve);
   h->want_energy = false;

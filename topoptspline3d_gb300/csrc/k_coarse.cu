@@ -1082,7 +1082,8 @@ void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double*
   k_symmetrize<<<nblk(n * n, 256), 256, 0, s>>>((int)n, A);
 }
 
-int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev, bool df_update) {
+int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev, bool df_update,
+                    int max_per_sm) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1092,7 +1093,7 @@ int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
     if (per_sm < 1) return (int)cudaErrorCooperativeLaunchTooLarge;
     const int tiles = ((n + GJB - 1) / GJB) * ((n + GJB - 1) / GJB);
-    const int blocks = std::max(1, std::min(tiles, nsm * std::min(per_sm, 2)));
+    const int blocks = std::max(1, std::min(tiles, nsm * std::min(per_sm, std::max(1, max_per_sm))));
     cudaMemsetAsync(status_dev, 0, 2 * sizeof(int), s);
     void* args[] = {&n, &A, &work, &status_dev};
     return (int)cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, s);

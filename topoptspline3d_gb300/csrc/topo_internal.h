@@ -147,7 +147,10 @@ void launch_assemble_stencil_t(cudaStream_t s, const LevelDims& d, const uint8_t
 void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double* st, double* A);
 // work: the blocked kernel's panels (GJB*GJB + 2*GJB*n doubles; null selects
 // the unblocked kernel); df_update: rank-GJB updates in double-float arithmetic.
-int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev, bool df_update = false);
+// max_per_sm caps the blocked form's CTAs per SM (it runs beside other work
+// on a second stream with 1).
+int coarsest_invert(cudaStream_t s, int n, double* A, double* work, int* status_dev, bool df_update = false,
+                    int max_per_sm = 2);
 void launch_to_float(cudaStream_t s, const double* a, float* b, int64_t n);
 template <typename T>
 void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv, int nb = 1);

@@ -453,6 +453,8 @@ def main():
     if not args.no_autotune and args.smoother == "chebyshev":
         p.update_operators()  # operators of the current design (the last OC step changed it)
         opts, tune = p.autotune(opts)
+        # one more untimed iteration on the tuned schedule: captures its graphs
+        p.design_iteration(solve=opts, oc=oc)
     # ---- timed region: K design iterations, device-resident inputs
     sampler = ClockSampler(device)
     barrier(pg)

@@ -37,12 +37,12 @@ def test_batch_equals_sequential():
 
 @pytest.mark.parametrize("inner_rtol", [1e-1, 1e-3])
 def test_graphs_do_not_change_results(inner_rtol):
-    """Graphs on: the V-cycle replays as one graph and the inner FP32 CG runs
-    as one graph whose loop is decided on the device (stopping on the inner
-    tolerance, or on the iteration cap with the tighter one).  Graphs off: the
-    same kernels launched one by one with the loop on the host.  Results,
-    iteration and V-cycle counts agree exactly, over design iterations whose
-    spectral bounds differ."""
+    """Graphs on: the V-cycle replays as one graph, and the inner FP32 CG and
+    the OC bisection each run as one graph whose loop is decided on the device
+    (the CG stopping on the inner tolerance, or on the iteration cap with the
+    tighter one).  Graphs off: the same kernels launched one by one with the
+    loops on the host.  Results, iteration, V-cycle and trial counts agree
+    exactly, over design iterations whose spectral bounds differ."""
     wl = workloads.small_cases()["mbb32"]
     solve = dict(SOLVE, inner_rtol=inner_rtol)
     runs = []
@@ -50,8 +50,10 @@ def test_graphs_do_not_change_results(inner_rtol):
         p = _make(wl)
         p.set_graphs(g)
         s = [p.design_iteration(solve=solve, oc=dict(vgoal=0.35)) for _ in range(3)]
-        runs.append(([(x["compliance"], x["iterations"], x["vcycles"], x["relres"]) for x in s], p.get("u")))
-    assert runs[0][0] == runs[1][0] and np.array_equal(runs[0][1], runs[1][1])
+        runs.append(([(x["compliance"], x["iterations"], x["vcycles"], x["relres"], x["oc_trials"], x["volume"])
+                      for x in s], p.get("u"), p.get("coeff")))
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][1], runs[1][1]) and np.array_equal(runs[0][2], runs[1][2])
     assert all(x[2] > x[1] for x in runs[1][0])  # several inner iterations per outer one
 
 

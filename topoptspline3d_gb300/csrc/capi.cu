@@ -35,7 +35,10 @@ enum Slot {
   // device-controlled inner CG loop: iterations of the current inner solve,
   // its ||b|| reference, the first iteration whose r.r was non-finite
   // (1-based, 0 = none), inner iterations summed over the solve
-  S_LOOP = S_PW + 2 * S_MAXLEV, S_COUNT = S_LOOP + 4
+  S_LOOP = S_PW + 2 * S_MAXLEV,
+  // device-side OC bisection: lo, hi, the current trial's threshold, its
+  // volume fraction, trials, repeats (the reference loop's itn)
+  S_OC = S_LOOP + 4, S_COUNT = S_OC + 6
 };
 
 // Chebyshev step coefficients (c_old, c_new) in device memory: per precision
@@ -74,6 +77,11 @@ struct topo_handle {
   cudaGraphExec_t igraph = nullptr;
   std::vector<double> ikey;
   long long igraph_fixed = 0, igraph_body = 0;
+  // OC bisection as one graph with a device-side WHILE loop (ograph)
+  bool ograph_ok = true;
+  cudaGraphExec_t ograph = nullptr;
+  std::vector<double> okey;
+  long long ograph_fixed = 0, ograph_body = 0;
   // coarsest inversion of a design iteration on a second stream (side),
   // overlapped with the solve's set-up; the main stream waits for ev_coarse
   // before its first V-cycle (coarse_join) and the status is read at the end
@@ -609,6 +617,42 @@ __global__ void k_loop_step(double* loop, const double* rr, double rtol, int max
   cudaGraphSetConditional(hc, go);
 }
 
+// OC bisection on the device (slots oc[0..5]: lo, hi, threshold of the
+// current trial, its volume fraction, trials, repeats).  Start: lo = 0, hi =
+// max |dc|, the first threshold; the loop body (a do-while) runs at least once.
+__global__ void k_ocl_start(double* oc, const double* gmax, cudaGraphConditionalHandle hc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  oc[0] = 0.0;
+  oc[1] = *gmax;
+  oc[2] = 0.5 * (oc[0] + oc[1]);
+  oc[4] = 0.0;
+  oc[5] = 0.0;
+  cudaGraphSetConditional(hc, 1u);
+}
+
+// After a trial of volume *vol: the volume fraction, the new bracket and the
+// loop test of the reference (repeat while |V - vgoal| > 1e-4 and itn++ < 30,
+// at most 32 trials); the next threshold when it repeats.
+__global__ void k_ocl_step(double* oc, const double* vol, double den, double vgoal, cudaGraphConditionalHandle hc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double thres = oc[2];
+  const double V = *vol / den;
+  oc[3] = V;
+  oc[4] += 1.0;
+  double lo = oc[0], hi = oc[1];
+  if (V > vgoal) lo = thres;
+  else if (V < vgoal) hi = thres;
+  oc[0] = lo;
+  oc[1] = hi;
+  bool go = fabs(V - vgoal) > 1e-4;
+  if (go) {
+    go = oc[5] < 30.0;
+    oc[5] += 1.0;
+  }
+  if (go) oc[2] = 0.5 * (lo + hi);
+  cudaGraphSetConditional(hc, go ? 1u : 0u);
+}
+
 // beta = (r.z - z.rold) / rold.z after the first iteration (the host loop's
 // scalar ratio, taken when the iteration counter is past 0).
 __global__ void k_loop_beta(const double* loop, double* sc) {
@@ -833,6 +877,77 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
   return TOPO_OK;
 }
 
+// Captures, on h->stream, one executable graph made of set-up kernels, a
+// WHILE node and tail kernels.  setup(hc) ends with a kernel that sets the loop
+// condition through hc; body(hc) is one pass of the loop and ends with a
+// kernel that sets it again (the loop is bounded by that kernel).  Kernels
+// counted while capturing come back split into the fixed part and one body
+// pass.  TOPO_E_STATE: conditional graphs are not available here.
+template <typename Setup, typename Body, typename Tail>
+int capture_loop_graph(topo_handle* h, Setup&& setup, Body&& body, Tail&& tail, cudaGraphExec_t* exec,
+                       long long* fixed, long long* per_body) {
+  cudaGraph_t g = nullptr;
+  cudaGraphConditionalHandle hc = 0;
+  cudaGraphNode_t cnode = nullptr;
+  std::vector<cudaGraphNode_t> deps;
+  const long long l0 = g_launches.load();
+  long long l1 = l0, l2 = l0;
+  int rc = TOPO_OK;
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+            cudaGraphConditionalHandleCreate(&hc, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+  h->in_capture = true;
+  // set-up; its last nodes are the loop node's dependencies
+  if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0, mode) == cudaSuccess;
+  if (ok) {
+    rc = setup(hc);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* dp = nullptr;
+    size_t nd = 0;
+    ok = cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, nullptr, &dp, nullptr, &nd) == cudaSuccess;
+    if (ok) deps.assign(dp, dp + nd);
+    cudaGraph_t gs = nullptr;
+    ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && ok && rc == TOPO_OK;
+  }
+  cudaGraph_t bg = nullptr;
+  if (ok) {
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = hc;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    ok = cudaGraphAddNode(&cnode, g, deps.data(), nullptr, deps.size(), &cp) == cudaSuccess;
+    if (ok) bg = cp.conditional.phGraph_out[0];
+  }
+  if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, bg, nullptr, nullptr, 0, mode) == cudaSuccess;
+  if (ok) {
+    l1 = g_launches.load();
+    rc = body(hc);
+    l2 = g_launches.load();
+    cudaGraph_t gs = nullptr;
+    ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && rc == TOPO_OK;
+  }
+  if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, g, &cnode, nullptr, 1, mode) == cudaSuccess;
+  if (ok) {
+    rc = tail();
+    cudaGraph_t gs = nullptr;
+    ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && rc == TOPO_OK;
+  }
+  h->in_capture = false;
+  *per_body = l2 - l1;
+  *fixed = (g_launches.load() - l0) - *per_body;
+  g_launches.fetch_sub(g_launches.load() - l0);
+  *exec = nullptr;
+  if (ok) ok = cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+  if (!ok) {
+    *exec = nullptr;
+    return rc != TOPO_OK ? rc : TOPO_E_STATE;
+  }
+  return TOPO_OK;
+}
+
 // The FP32 inner CG of the mixed solve, z = CG(r) from x = 0, as one CUDA
 // graph: set-up (r in FP32, x = 0, r.r and the stopping test), a WHILE node
 // whose body is one CG iteration (fcg_body) closed by a kernel that counts the
@@ -841,8 +956,8 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
 // rule (||r|| / ||b|| > rtol and fewer than maxit iterations; ||b|| is the
 // outer residual's norm, 1 if that is 0) decided on the device, so the host
 // does not wait for the GPU between inner iterations.  The graph is captured
-// once per key (buffers, schedule, bounds, tiles) and replayed.  Iteration
-// totals and a non-finite r.r are left in the loop slots for the caller.
+// once per key (buffers, schedule, tiles) and replayed.  Iteration totals and
+// a non-finite r.r are left in the loop slots for the caller.
 template <typename Prec>
 int inner_cg_graphed(topo_handle* h, const double* rin, double* zout, double rtol, int maxit, Prec&& prec,
                      std::vector<double> key) {
@@ -854,75 +969,29 @@ int inner_cg_graphed(topo_handle* h, const double* rin, double* zout, double rto
                          (double)h->tz32, (double)(uintptr_t)h->fdot, (double)h->fdot_cap});
   if (!h->igraph || key != h->ikey) {
     if (h->igraph) { cudaGraphExecDestroy(h->igraph); h->igraph = nullptr; }
-    cudaGraph_t g = nullptr;
-    cudaGraphConditionalHandle hc = 0;
-    cudaGraphNode_t cnode = nullptr;
-    std::vector<cudaGraphNode_t> deps;
-    const long long l0 = g_launches.load();
-    long long l1 = l0, l2 = l0;
-    int rc = TOPO_OK;
-    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
-              cudaGraphConditionalHandleCreate(&hc, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
-    // set-up, captured into g; its last nodes are the loop's dependencies
-    if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0,
-                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-    if (ok) {
-      h->in_capture = true;
+    auto setup = [&](cudaGraphConditionalHandle hc) -> int {
       launch_d2f(h->stream, rin, L0.F32, n3);
-      cudaMemsetAsync(h->x32, 0, sizeof(float) * n3, h->stream);
+      CK(cudaMemsetAsync(h->x32, 0, sizeof(float) * n3, h->stream));
       launch_dot<float>(h->stream, L0.F32, L0.F32, n3, h->partial, sc + S_RR, h->ctr);
       k_loop_start<<<1, 32, 0, h->stream>>>(h->sc + S_LOOP, h->sc + S_RR, sc + S_RR, rtol, maxit, hc);
       count_launch(3);
-      cudaStreamCaptureStatus cs;
-      const cudaGraphNode_t* dp = nullptr;
-      size_t nd = 0;
-      ok = cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, nullptr, &dp, nullptr, &nd) == cudaSuccess;
-      if (ok) deps.assign(dp, dp + nd);
-      cudaGraph_t gs = nullptr;
-      ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && ok;
-    }
-    // the loop node and its body
-    cudaGraph_t body = nullptr;
-    if (ok) {
-      cudaGraphNodeParams cp = {};
-      cp.type = cudaGraphNodeTypeConditional;
-      cp.conditional.handle = hc;
-      cp.conditional.type = cudaGraphCondTypeWhile;
-      cp.conditional.size = 1;
-      ok = cudaGraphAddNode(&cnode, g, deps.data(), nullptr, deps.size(), &cp) == cudaSuccess;
-      if (ok) body = cp.conditional.phGraph_out[0];
-    }
-    if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0,
-                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-    if (ok) {
-      l1 = g_launches.load();
-      rc = fcg_body<float>(h, h->x32, L0.F32, h->d32, h->q32, h->rold32, L0.U32, sc, prec, true, -1);
+      return TOPO_OK;
+    };
+    auto body = [&](cudaGraphConditionalHandle hc) -> int {
+      RET(fcg_body<float>(h, h->x32, L0.F32, h->d32, h->q32, h->rold32, L0.U32, sc, prec, true, -1));
       k_loop_step<<<1, 32, 0, h->stream>>>(h->sc + S_LOOP, sc + S_RR, rtol, maxit, hc);
       count_launch();
-      l2 = g_launches.load();
-      cudaGraph_t gs = nullptr;
-      ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && rc == TOPO_OK;
-    }
-    // z = x in FP64 after the loop
-    if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, g, &cnode, nullptr, 1,
-                                               cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-    if (ok) {
+      return TOPO_OK;
+    };
+    auto tail = [&]() -> int {  // z = x in FP64 after the loop
       k_to_double<float><<<nb256(n3), 256, 0, h->stream>>>(n3, h->x32, zout);
       count_launch();
-      cudaGraph_t gs = nullptr;
-      ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess;
-    }
-    h->in_capture = false;
-    h->igraph_body = l2 - l1;
-    h->igraph_fixed = (g_launches.load() - l0) - h->igraph_body;
-    g_launches.fetch_sub(g_launches.load() - l0);
-    if (ok) ok = cudaGraphInstantiate(&h->igraph, g, 0) == cudaSuccess;
-    if (g) cudaGraphDestroy(g);
-    cudaGetLastError();
-    if (!ok) {  // conditional graphs not available: the host runs the loop from now on
-      h->igraph = nullptr;
-      h->igraph_ok = false;
-      return TOPO_E_STATE;
+      return TOPO_OK;
+    };
+    const int rc = capture_loop_graph(h, setup, body, tail, &h->igraph, &h->igraph_fixed, &h->igraph_body);
+    if (rc != TOPO_OK) {  // conditional graphs not available: the host runs the loop from now on
+      if (rc == TOPO_E_STATE) h->igraph_ok = false;
+      return rc;
     }
     h->ikey = key;
   }
@@ -1126,6 +1195,7 @@ void topo_destroy(topo_handle* h) {
   if (h->hstat) cudaFreeHost(h->hstat);
   if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
   if (h->igraph) cudaGraphExecDestroy(h->igraph);
+  if (h->ograph) cudaGraphExecDestroy(h->ograph);
   prof_drop_graph_events(h);
   if (h->multi) {
     for (void* p : h->multi->allocs) cudaFree(p);
@@ -1933,7 +2003,8 @@ int topo_set_graphs(topo_handle* h, int enable) {
   h->graphs = enable != 0;
   if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
   if (h->igraph) { cudaGraphExecDestroy(h->igraph); h->igraph = nullptr; }
-  h->igraph_ok = true;
+  if (h->ograph) { cudaGraphExecDestroy(h->ograph); h->ograph = nullptr; }
+  h->igraph_ok = h->ograph_ok = true;
   return TOPO_OK;
 }
 
@@ -2363,6 +2434,61 @@ int handle_spline_view(topo_handle* h, SplineView* out) {
 int handle_fail(topo_handle* h, int code, const char* msg) { return fail(h, code, "%s", msg); }
 }  // namespace topo
 
+// The OC bisection of topo_oc_update as one CUDA graph: start (bracket [0,
+// max |dc|] from the device slot S_TMP), a WHILE node whose body is one trial
+// (coefficients at the threshold, their volume) closed by the bracket update
+// and loop test, and the second application when asked.  The trials, their
+// thresholds and the stopping rule are the host loop's, decided on the
+// device; the trial count and final threshold are left in the OC slots.
+static int oc_bisection_graphed(topo_handle* h, const topo_oc_opts* o, int64_t nc, double den) {
+  const DevLevel& L = h->lv[0];
+  double* oc = h->sc + S_OC;
+  const SplineDev& sp = h->sd;
+  std::vector<double> key = {(double)nc, den, o->vgoal, o->damp, o->step, o->cmin, o->cmax,
+                             (double)o->apply_twice, (double)sp.order, h->cfg.min_density};
+  for (int a = 0; a < 3; ++a)
+    key.insert(key.end(), {(double)sp.nb[a], (double)(uintptr_t)sp.i0[a], (double)(uintptr_t)sp.Ndf[a]});
+  for (const void* p : {(const void*)h->coeff, (const void*)h->coeff_old, (const void*)h->csens,
+                        (const void*)h->coeff_df, (const void*)h->coeff_tmp, (const void*)h->adj1,
+                        (const void*)L.eactive})
+    key.push_back((double)(uintptr_t)p);
+  if (!h->ograph || key != h->okey) {
+    if (h->ograph) { cudaGraphExecDestroy(h->ograph); h->ograph = nullptr; }
+    auto setup = [&](cudaGraphConditionalHandle hc) -> int {
+      k_ocl_start<<<1, 32, 0, h->stream>>>(oc, h->sc + S_TMP, hc);
+      count_launch();
+      return TOPO_OK;
+    };
+    auto body = [&](cudaGraphConditionalHandle hc) -> int {
+      launch_oc_trial(h->stream, nc, h->coeff_old, h->csens, 0.0, o->damp, o->step, o->cmin, o->cmax, h->coeff,
+                      h->coeff_df, oc + 2);
+      launch_trial_volume(h->stream, L.d, L.eactive, h->sd, h->coeff_df, h->cfg.min_density, h->partial,
+                          h->sc + S_TMP, h->adj1);
+      k_ocl_step<<<1, 32, 0, h->stream>>>(oc, h->sc + S_TMP, den, o->vgoal, hc);
+      count_launch(5);
+      return TOPO_OK;
+    };
+    auto tail = [&]() -> int {
+      if (o->apply_twice) {
+        launch_oc_trial(h->stream, nc, h->coeff, h->csens, 0.0, o->damp, o->step, o->cmin, o->cmax, h->coeff_tmp,
+                        nullptr, oc + 2);
+        CK(cudaMemcpyAsync(h->coeff, h->coeff_tmp, sizeof(double) * nc, cudaMemcpyDeviceToDevice, h->stream));
+        count_launch();
+      }
+      return TOPO_OK;
+    };
+    const int rc = capture_loop_graph(h, setup, body, tail, &h->ograph, &h->ograph_fixed, &h->ograph_body);
+    if (rc != TOPO_OK) {
+      if (rc == TOPO_E_STATE) h->ograph_ok = false;
+      return rc;
+    }
+    h->okey = key;
+  }
+  CK(cudaGraphLaunch(h->ograph, h->stream));
+  count_launch((int)h->ograph_fixed);
+  return TOPO_OK;
+}
+
 extern "C" {
 
 int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) {
@@ -2373,9 +2499,29 @@ int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) 
   const double den = (double)(o->reference_volume ? h->gs_padded_elements : h->active_elements);
   launch_maxabs(h->stream, h->csens, nc, h->partial, h->sc + S_TMP);
   count_launch(2);
-  RET(read_scalars(h, S_TMP, 1));
-  const double gmax = h->hsc[S_TMP];
+  double gmax = 0.0;
+  if (!(h->graphs && h->ograph_ok)) {  // the device-side bisection reads it in place
+    RET(read_scalars(h, S_TMP, 1));
+    gmax = h->hsc[S_TMP];
+  }
   CK(cudaMemcpyAsync(h->coeff_old, h->coeff, sizeof(double) * nc, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->graphs && h->ograph_ok) {
+    const int rc = oc_bisection_graphed(h, o, nc, den);
+    if (rc == TOPO_OK) {
+      RET(topo_coeff_to_density(h));
+      if (stats) {
+        double v = 0;
+        RET(topo_volume(h, o->reference_volume, &v));
+        RET(read_scalars(h, S_OC, 6));
+        count_launch((int)((long long)h->hsc[S_OC + 4] * h->ograph_body));
+        stats->trials = (int)h->hsc[S_OC + 4];
+        stats->lambda = h->hsc[S_OC + 2];
+        stats->volume = v;
+      }
+      return TOPO_OK;
+    }
+    if (rc != TOPO_E_STATE) return rc;  // else the host loop below, from now on
+  }
   double lo = 0.0, hi = gmax, thres = 0.5 * (lo + hi), V = 0.0;
   int itn = 0, trials = 0;
   do {

@@ -468,16 +468,20 @@ void launch_penalise(cudaStream_t s, int64_t ne, const uint8_t* eactive, const d
 
 // OC trial on the coefficients (optimization/optimization.cu:559-587):
 // c' = clamp(clamp(c (max(-dc,0)/thres)^damp, c-step, c+step), cmin, cmax).
+// The threshold is thres, or *thres_p when that is given (the device-side
+// bisection).  For damp = 1/2 the power is the correctly rounded square root.
 __global__ void k_oc_trial(int64_t nc, const double* __restrict__ cold, const double* __restrict__ csens,
-                           double thres, double damp, double step, double cmin, double cmax,
-                           double* __restrict__ cnew, float2* __restrict__ cnew_df) {
+                           double thres, const double* __restrict__ thres_p, double damp, double step,
+                           double cmin, double cmax, double* __restrict__ cnew, float2* __restrict__ cnew_df) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
+  if (thres_p) thres = *thres_p;
   double g = csens[i];
   if (g > 0) g = 0;
   g = fabs(g);
   const double co = cold[i];
-  double cn = co * pow(g / thres, damp);
+  const double q = g / thres;
+  double cn = co * (damp == 0.5 ? sqrt(q) : pow(q, damp));
   cn = fmin(fmax(cn, co - step), co + step);
   cn = fmin(fmax(cn, cmin), cmax);
   cnew[i] = cn;
@@ -488,8 +492,10 @@ __global__ void k_oc_trial(int64_t nc, const double* __restrict__ cold, const do
 }
 
 void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,
-                     double damp, double step, double cmin, double cmax, double* cnew, float2* cnew_df) {
-  k_oc_trial<<<nblk(nc, 256), 256, 0, s>>>(nc, cold, csens, thres, damp, step, cmin, cmax, cnew, cnew_df);
+                     double damp, double step, double cmin, double cmax, double* cnew, float2* cnew_df,
+                     const double* thres_p) {
+  k_oc_trial<<<nblk(nc, 256), 256, 0, s>>>(nc, cold, csens, thres, thres_p, damp, step, cmin, cmax, cnew,
+                                           cnew_df);
 }
 
 }  // namespace topo

@@ -238,9 +238,11 @@ struct SplineView {
 };
 int handle_spline_view(topo_handle* h, SplineView* out);
 int handle_fail(topo_handle* h, int code, const char* msg);
-// cnew_df (optional): cnew split into (hi, lo) floats as well
+// cnew_df (optional): cnew split into (hi, lo) floats as well; thres_p
+// (optional): the threshold read from device memory instead of thres
 void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,
-                     double damp, double step, double cmin, double cmax, double* cnew, float2* cnew_df = nullptr);
+                     double damp, double step, double cmin, double cmax, double* cnew, float2* cnew_df = nullptr,
+                     const double* thres_p = nullptr);
 void launch_maxabs(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);
 
 // bc_regions.cpp: region-predicate boundary conditions (host).

@@ -615,10 +615,11 @@ __global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims 
                                                         T* __restrict__ kel) {
   // products in the operator's precision: FP32 for the FP32 preconditioner's
   // operators (the FP64 form is bound by GB300's FP64 pipe), FP64 for FP64
+  constexpr int NP = FCT * FCT * FCT;  // fine elements in the coarse element
   __shared__ T sK[576];
   __shared__ T sQ[8][8];
-  __shared__ uint8_t sfree[24];
-  __shared__ int sflag;
+  __shared__ uint8_t sfree[NP][24];
+  __shared__ uint8_t sflag[NP];
   const int64_t ce = list[blockIdx.x];
   const int cx = (int)(ce % cd.ex);
   const int64_t t = ce / cd.ex;
@@ -626,31 +627,33 @@ __global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims 
   const int ent = threadIdx.x;
   const int R = ent / 24, S = ent % 24;
   const int A = R / 3, i = R % 3, B = S / 3, j = S % 3;
+  // free-DOF pattern of every fine element at once (one thread each); the
+  // fine elements with all 24 DOFs free are left to the GEMM pass
+  if (ent < NP) {
+    const int px = ent % FCT, py = ent / FCT % FCT, pz = ent / (FCT * FCT);
+    const int fx = cx * FCT + px, fy = cy * FCT + py, fz = cz * FCT + pz;
+    int flag = 0;
+    if (fx < fd.ex && fy < fd.ey && fz < fd.ez && eactive[fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz)]) {
+      for (int a = 0; a < 8; ++a) {
+        const int64_t vv = (fx + (a & 1)) + (int64_t)fd.vx * ((fy + ((a >> 1) & 1)) + (int64_t)fd.vy * (fz + (a >> 2)));
+        const uint8_t m = vmask[vv];
+        for (int c = 0; c < 3; ++c) sfree[ent][3 * a + c] = (m >> c) & 1;
+        if ((m & 7) != 7) flag = 1;
+      }
+    }
+    sflag[ent] = (uint8_t)flag;
+  }
+  __syncthreads();
   T acc = T(0);
-  for (int pos = 0; pos < FCT * FCT * FCT; ++pos) {
+  for (int pos = 0; pos < NP; ++pos) {
+    if (!sflag[pos]) continue;  // the same for the whole CTA
     const int px = pos % FCT, py = pos / FCT % FCT, pz = pos / (FCT * FCT);
     const int fx = cx * FCT + px, fy = cy * FCT + py, fz = cz * FCT + pz;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int flag = 0;
-      if (fx < fd.ex && fy < fd.ey && fz < fd.ez &&
-          eactive[fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz)]) {
-        for (int a = 0; a < 8; ++a) {
-          const int64_t vv = (fx + (a & 1)) + (int64_t)fd.vx * ((fy + ((a >> 1) & 1)) + (int64_t)fd.vy * (fz + (a >> 2)));
-          const uint8_t m = vmask[vv];
-          for (int c = 0; c < 3; ++c) sfree[3 * a + c] = (m >> c) & 1;
-          if ((m & 7) != 7) flag = 1;
-        }
-      }
-      sflag = flag;
-    }
-    __syncthreads();
-    if (!sflag) continue;
     const double pe = rhop[fx + (int64_t)fd.ex * (fy + (int64_t)fd.ey * fz)];
     {
       const int r = ent / 24, s2 = ent % 24;
       double k = pe * Ke[ent];
-      if (!sfree[r] || !sfree[s2]) k = (r == s2) ? 1e6 : 0.0;
+      if (!sfree[pos][r] || !sfree[pos][s2]) k = (r == s2) ? 1e6 : 0.0;
       sK[ent] = T(k);
     }
     if (ent < 64) {
@@ -671,6 +674,7 @@ __global__ void __launch_bounds__(576) k_galerkin_fixed(LevelDims fd, LevelDims 
       s += qa * inner;
     }
     acc += s;
+    __syncthreads();  // sK and sQ are rewritten for the next fine element
   }
   if (acc != T(0)) kel[ce * 576 + ent] += acc;
 }

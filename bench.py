@@ -61,6 +61,9 @@ def parse():
                          "autotuning (e.g. the values an earlier run's autotune chose)")
     ap.add_argument("--profile-solve-steps", type=int, default=0,
                     help="with --profile-iteration: stop the solve after this many outer CG steps")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch every kernel on its own (no CUDA graphs); with --profile-iteration this lists the "
+                         "kernels the device-side loops run inside graphs")
     ap.add_argument("--profile-warmup", type=int, default=0,
                     help="with --profile-iteration: run this many design iterations first and open the profiler's "
                          "capture range (cudaProfilerStart) only around the last one, for ncu --profile-from-start off")
@@ -426,6 +429,8 @@ def main():
     wl, p = make_problem(nx, ny, nz, device, op_precision=2, case=args.case)
     opts = solve_opts(capi.SOLVE_MIXED, args.smoother)
     oc = dict(vgoal=wl.vgoal, damp=0.5, step=0.03, cmin=0.0, cmax=1.0)
+    if args.no_graphs:
+        p.set_graphs(0)
     if args.schedule:
         inner, pre, deg, tz32, tz64 = (int(v) for v in args.schedule.split(","))
         opts.update(inner_max=inner, pre=pre, post=pre, cheb_degree=deg)

@@ -99,36 +99,18 @@ __global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st,
 // enough loads in flight on the small coarse levels.
 constexpr int SV = 64;
 
-// Row `row` of A u at vertex v (x, y, z).  The 27 neighbours are taken one
-// z-plane (9 neighbours) at a time, with every load of a plane issued before
-// its products: a neighbour off the grid reads a valid address (the vertex
-// itself) and counts as zero, so no load waits behind a bounds test and each
-// thread makes three rounds to memory instead of 27.  The products are summed
-// in neighbour order.
 template <typename T>
 __device__ __forceinline__ T stencil_row_i(const LevelDims& d, const T* __restrict__ st, const T* __restrict__ u,
                                            int x, int y, int z, int64_t v, int row) {
   T o = T(0);
   const int64_t nv = d.nv;
 #pragma unroll
-  for (int kz = 0; kz < 3; ++kz) {
-    T sv[9][3], uv[9][3];
-#pragma unroll
-    for (int kk = 0; kk < 9; ++kk) {
-      const int k = 9 * kz + kk;
-      const int nx = x + kk % 3 - 1, ny = y + kk / 3 - 1, nz = z + kz - 1;
-      const bool ok = nx >= 0 && ny >= 0 && nz >= 0 && nx < d.vx && ny < d.vy && nz < d.vz;
-      const int64_t n = ok ? nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz) : v;
-      const T* s = st + (int64_t)(k * 9 + 3 * row) * nv + v;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        sv[kk][c] = s[c * nv];
-        const T uc = u[c * nv + n];
-        uv[kk][c] = ok ? uc : T(0);
-      }
-    }
-#pragma unroll
-    for (int kk = 0; kk < 9; ++kk) o += sv[kk][0] * uv[kk][0] + sv[kk][1] * uv[kk][1] + sv[kk][2] * uv[kk][2];
+  for (int k = 0; k < 27; ++k) {
+    const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
+    if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) continue;
+    const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
+    const T* s = st + (int64_t)(k * 9 + 3 * row) * nv + v;
+    o += s[0] * u[n] + s[nv] * u[nv + n] + s[2 * nv] * u[2 * nv + n];
   }
   return o;
 }
@@ -409,33 +391,20 @@ __global__ void __launch_bounds__(32 * R4_WARPS) k_restrict4(LevelDims fd, Level
     const int dz = w - 3, fz = 4 * z + dz;
     if (fz >= 0 && fz < fd.vz) {
       const T wz = T(4 - (dz < 0 ? -dz : dz));
-      // one fine row (7 taps x 3 components) per round: every load of the row
-      // is issued before its products; taps off the grid read the row's
-      // centre and count as zero
       for (int dy = -3; dy <= 3; ++dy) {
         const int fy = 4 * y + dy;
-        const bool oky = fy >= 0 && fy < fd.vy;
+        if (fy < 0 || fy >= fd.vy) continue;
         const T wyz = wz * T(4 - (dy < 0 ? -dy : dy));
-        const int64_t rowv = (int64_t)fd.vx * ((oky ? fy : 4 * y) + (int64_t)fd.vy * fz);
-        T a[7][3];
+        const int64_t rowv = (int64_t)fd.vx * (fy + (int64_t)fd.vy * fz);
 #pragma unroll
-        for (int k = 0; k < 7; ++k) {
-          const int fx = 4 * x + k - 3;
-          const bool ok = oky && fx >= 0 && fx < fd.vx;
-          const int64_t fv = rowv + (ok ? fx : 4 * x);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const T r = rf[c * fd.nv + fv];
-            a[k][c] = ok ? r : T(0);
-          }
-        }
-#pragma unroll
-        for (int k = 0; k < 7; ++k) {
-          const int dx = k - 3;
+        for (int dx = -3; dx <= 3; ++dx) {
+          const int fx = 4 * x + dx;
+          if (fx < 0 || fx >= fd.vx) continue;
           const T wt = wyz * T(4 - (dx < 0 ? -dx : dx));
-          s0 += wt * a[k][0];
-          s1 += wt * a[k][1];
-          s2 += wt * a[k][2];
+          const int64_t fv = rowv + fx;
+          s0 += wt * rf[fv];
+          s1 += wt * rf[fd.nv + fv];
+          s2 += wt * rf[2 * fd.nv + fv];
         }
       }
     }

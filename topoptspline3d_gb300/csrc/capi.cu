@@ -1452,8 +1452,8 @@ int topo_coeff_to_density(topo_handle* h) {
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set (call topo_set_spline)");
   const DevLevel& L = h->lv[0];
   launch_coeff_to_density(h->stream, L.d, L.eactive, h->sd, h->coeff, h->cfg.min_density,
-                          h->cfg.power_penalty, h->rho, h->rhop, h->rhop32, h->adj1);
-  count_launch(2);
+                          h->cfg.power_penalty, h->rho, h->rhop, h->rhop32, h->adj1, h->coeff_df);
+  count_launch(3);
   CKL();
   h->rhop_stale = false;
   h->ops_ready = false;

@@ -1,5 +1,6 @@
 // Design-chain kernels: B-spline density, element sensitivity, sensitivity
 // filter, spline adjoint and the OC coefficient trial.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -172,13 +173,200 @@ __global__ void __launch_bounds__(VOL_THREADS) k_volume_from_B(LevelDims d, cons
   }
 }
 
+// (hi, lo) float split of n doubles
+__global__ void k_to_df(int64_t n, const double* __restrict__ a, float2* __restrict__ b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const df v = df_from(a[i]);
+  b[i] = make_float2(v.hi, v.lo);
+}
+
+// Pass 1 in double-float, one CTA per element layer z, separable: first
+// C[j][i] = sum_t c[i, j, iz+t] Nz[z][t] for every x- and y-basis index into
+// shared memory, then B[z][y][i] = sum_s Ny[y][s] C[iy+s][i] (0 where y or z is
+// outside the spline range).  The products and their order are those of
+// k_spline_yz_df (inner sum over t, outer over s), with each coefficient read
+// once per layer instead of once per output.
+__global__ void __launch_bounds__(256) k_spline_yz_sep(LevelDims d, SplineDev sp, const float2* __restrict__ coeff,
+                                                       float2* __restrict__ B) {
+  extern __shared__ float2 sC[];  // [nb1][nb0]
+  const int z = blockIdx.x;
+  const int nbx = sp.nb[0], nby = sp.nb[1], k = sp.order;
+  const int iz = sp.i0[2][z];
+  float2* Bz = B + (int64_t)nbx * d.ey * z;
+  if (iz < 0) {
+    for (int q = threadIdx.x; q < nbx * d.ey; q += blockDim.x) Bz[q] = make_float2(0.f, 0.f);
+    return;
+  }
+  df nz[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const float2 n = t < k ? sp.Ndf[2][z * k + t] : make_float2(0.f, 0.f);
+    nz[t] = df(n.x, n.y);
+  }
+  for (int q = threadIdx.x; q < nbx * nby; q += blockDim.x) {
+    const int i = q % nbx, j = q / nbx;
+    df a(0);
+    for (int t = 0; t < k; ++t) {
+      const float2 c = coeff[i + (int64_t)nbx * (j + (int64_t)nby * (iz + t))];
+      a += df(c.x, c.y) * nz[t];
+    }
+    sC[q] = make_float2(a.hi, a.lo);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nbx * d.ey; q += blockDim.x) {
+    const int i = q % nbx, y = q / nbx;
+    const int iy = sp.i0[1][y];
+    df v(0);
+    if (iy >= 0) {
+      for (int s2 = 0; s2 < k; ++s2) {
+        const float2 ns = sp.Ndf[1][y * k + s2];
+        const float2 a = sC[i + nbx * (iy + s2)];
+        v += df(ns.x, ns.y) * df(a.x, a.y);
+      }
+    }
+    Bz[q] = make_float2(v.hi, v.lo);
+  }
+}
+
+// Pass 2 one element row (y, z) at a time: the row's pass-1 values B[z][y][:]
+// are staged in shared memory, and the next row's values and activity flags
+// are loaded while this row's elements are evaluated (values as
+// spline_from_B).  Rows of at most ROW_PF * VOL_THREADS elements and basis
+// indices.
+constexpr int ROW_PF = 4;
+
+struct RowStage {
+  float2 b[ROW_PF];
+  uint8_t a[ROW_PF];
+};
+
+__device__ __forceinline__ void row_fetch(RowStage& r, const float2* __restrict__ B, const uint8_t* __restrict__ eactive,
+                                          int nbx, int ex, int row) {
+  const float2* b = B + (int64_t)nbx * row;
+  const uint8_t* ea = eactive + (int64_t)ex * row;
+#pragma unroll
+  for (int q = 0; q < ROW_PF; ++q) {
+    const int i = threadIdx.x + q * VOL_THREADS;
+    r.b[q] = i < nbx ? b[i] : make_float2(0.f, 0.f);
+    r.a[q] = i < ex ? ea[i] : 0;
+  }
+}
+
+__device__ __forceinline__ df row_value(const SplineDev& sp, const float2* sB, int x, bool yz_in) {
+  const int ix = sp.i0[0][x];
+  if (ix < 0 || !yz_in) return df_from(-0.2);
+  const int k = sp.order;
+  df v(0);
+  for (int r = 0; r < k; ++r) {
+    const float2 n = sp.Ndf[0][x * k + r], bb = sB[ix + r];
+    v += df(n.x, n.y) * df(bb.x, bb.y);
+  }
+  return v;
+}
+
+// MODE 0: volume partial sums (clamped values of active elements, per CTA);
+// MODE 1: densities rho, rho^p (FP64 and FP32) of every element.
+template <int MODE>
+__global__ void __launch_bounds__(VOL_THREADS) k_spline_rows(LevelDims d, const uint8_t* __restrict__ eactive,
+                                                             SplineDev sp, const float2* __restrict__ B,
+                                                             double rho_min, double penal,
+                                                             double* __restrict__ partial, double* __restrict__ rho,
+                                                             double* __restrict__ rhop, float* __restrict__ rhop32) {
+  __shared__ float2 sB[ROW_PF * VOL_THREADS];
+  const int nbx = sp.nb[0], ex = d.ex, nrows = d.ey * d.ez;
+  const df lo = df_from(rho_min), one(1.f, 0.f);
+  df sd(0);
+  RowStage st;
+  int row = blockIdx.x;
+  if (row < nrows) row_fetch(st, B, eactive, nbx, ex, row);
+  for (; row < nrows; row += gridDim.x) {
+    __syncthreads();  // the previous row's readers are done with sB
+    uint8_t act[ROW_PF];
+#pragma unroll
+    for (int q = 0; q < ROW_PF; ++q) {
+      const int i = threadIdx.x + q * VOL_THREADS;
+      if (i < nbx) sB[i] = st.b[q];
+      act[q] = st.a[q];
+    }
+    __syncthreads();
+    if (row + (int)gridDim.x < nrows) row_fetch(st, B, eactive, nbx, ex, row + gridDim.x);
+    const int y = row % d.ey, z = row / d.ey;
+    const bool yz_in = sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0;
+#pragma unroll
+    for (int q = 0; q < ROW_PF; ++q) {
+      const int x = threadIdx.x + q * VOL_THREADS;
+      if (x >= ex) continue;
+      if (MODE == 0) {
+        if (!act[q]) continue;
+        df v = row_value(sp, sB, x, yz_in);
+        if (df_lt(v, lo)) v = lo;
+        if (df_lt(one, v)) v = one;
+        sd += v;
+      } else {
+        const int64_t e = x + (int64_t)ex * row;
+        if (!act[q]) {
+          rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
+          continue;
+        }
+        const double v = fmin(fmax(df_to(row_value(sp, sB, x, yz_in)), rho_min), 1.0);
+        const double vp = simp_pow(v, penal);
+        rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
+      }
+    }
+  }
+  if (MODE != 0) return;
+  double s = df_to(sd);
+  __shared__ double ws[VOL_THREADS / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < VOL_THREADS / 32; ++w) r += ws[w];
+    partial[blockIdx.x] = r;
+  }
+}
+
+// Pass 1 through the separable kernel when its layer table fits in shared
+// memory (returns false otherwise).
+static bool spline_yz_sep(cudaStream_t s, const LevelDims& d, const SplineDev& sp, const float2* coeff_df,
+                          float2* B) {
+  const size_t smem = sizeof(float2) * (size_t)sp.nb[0] * sp.nb[1];
+  if (sp.order > 4 || smem > 200 * 1024) return false;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_spline_yz_sep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  k_spline_yz_sep<<<d.ez, 256, smem, s>>>(d, sp, coeff_df, B);
+  return true;
+}
+
+static bool rows_fit(const LevelDims& d, const SplineDev& sp) {
+  return d.ex <= ROW_PF * VOL_THREADS && sp.nb[0] <= ROW_PF * VOL_THREADS;
+}
+
+static int rows_blocks(const LevelDims& d) { return (int)std::min<int64_t>(1024, (int64_t)d.ey * d.ez); }
+
 void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,
-                             double* rho, double* rhop, float* rhop32, double* Btmp) {
+                             double* rho, double* rhop, float* rhop32, double* Btmp, float2* coeff_df) {
   const int64_t nB = (int64_t)sp.nb[0] * d.ey * d.ez;
+  const int64_t nc = (int64_t)sp.nb[0] * sp.nb[1] * sp.nb[2];
   float2* B = reinterpret_cast<float2*>(Btmp);  // nB (hi, lo) pairs in the nB-double scratch
-  k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, B);
-  k_density_from_B<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, B, rho_min, penal, rho, rhop, rhop32);
+  bool sep = false;
+  if (coeff_df) {
+    k_to_df<<<nblk(nc, 256), 256, 0, s>>>(nc, coeff, coeff_df);
+    sep = spline_yz_sep(s, d, sp, coeff_df, B);
+  }
+  if (!sep) k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, B);
+  if (rows_fit(d, sp))
+    k_spline_rows<1><<<rows_blocks(d), VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, penal, nullptr, rho, rhop,
+                                                            rhop32);
+  else
+    k_density_from_B<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, B, rho_min, penal, rho, rhop, rhop32);
 }
 
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
@@ -186,11 +374,16 @@ void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eact
                          double* out, double* Btmp) {
   const int64_t nB = (int64_t)sp.nb[0] * d.ey * d.ez;
   float2* B = reinterpret_cast<float2*>(Btmp);  // nB (hi, lo) pairs in the nB-double scratch
-  k_spline_yz_df<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff_df, B);
-  // two elements per thread at most (up to 2048 partials)
-  int nb = (int)std::min<int64_t>(2048, (d.ne + VOL_THREADS * 2 - 1) / (VOL_THREADS * 2));
-  if (nb < 1) nb = 1;
-  k_volume_from_B<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, partial);
+  if (!spline_yz_sep(s, d, sp, coeff_df, B)) k_spline_yz_df<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff_df, B);
+  int nb;
+  if (rows_fit(d, sp)) {
+    nb = rows_blocks(d);
+    k_spline_rows<0><<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, 0.0, partial, nullptr, nullptr, nullptr);
+  } else {  // two elements per thread at most (up to 2048 partials)
+    nb = (int)std::min<int64_t>(2048, (d.ne + VOL_THREADS * 2 - 1) / (VOL_THREADS * 2));
+    if (nb < 1) nb = 1;
+    k_volume_from_B<<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, partial);
+  }
   k_sum_partials<<<1, 256, 0, s>>>(partial, nb, out);
 }
 
@@ -310,13 +503,6 @@ __device__ __forceinline__ df df_div(df a, df b) {
   const df r = a - b * df(q1, 0.f);
   const float q2 = __fdiv_rn(r.hi, b.hi);
   return df_fast2sum(q1, q2);
-}
-
-__global__ void k_to_df(int64_t n, const double* __restrict__ a, float2* __restrict__ b) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const df v = df_from(a[i]);
-  b[i] = make_float2(v.hi, v.lo);
 }
 
 __global__ void k_filter_df(LevelDims d, const uint8_t* __restrict__ eactive, const float2* __restrict__ src,

@@ -205,9 +205,11 @@ struct SplineTables {
 void spline_tables(int order, const int* partition, const double* bmin, const double* bmax,
                    const int* nelem, double h, SplineTables& t);
 // Two-pass separable evaluation; Btmp holds nb[0]*ey*ez doubles.
+// coeff_df (optional scratch of nc float2): the coefficients are split into
+// (hi, lo) floats there and both passes run in double-float
 void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,
-                             double* rho, double* rhop, float* rhop32, double* Btmp);
+                             double* rho, double* rhop, float* rhop32, double* Btmp, float2* coeff_df = nullptr);
 // coeff_df: the trial coefficients split into (hi, lo) floats (from launch_oc_trial)
 void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                          const SplineDev& sp, const float2* coeff_df, double rho_min, double* partial,

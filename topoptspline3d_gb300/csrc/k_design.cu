@@ -181,31 +181,72 @@ __global__ void k_to_df(int64_t n, const double* __restrict__ a, float2* __restr
   b[i] = make_float2(v.hi, v.lo);
 }
 
-// Pass 1 in double-float, one CTA per element layer z, separable: first
-// C[j][i] = sum_t c[i, j, iz+t] Nz[z][t] for every x- and y-basis index into
-// shared memory, then B[z][y][i] = sum_s Ny[y][s] C[iy+s][i] (0 where y or z is
-// outside the spline range).  The products and their order are those of
-// k_spline_yz_df (inner sum over t, outer over s), with each coefficient read
-// once per layer instead of once per output.
+// Pass 1 in double-float, separable, one CTA per (element layer z, chunk of
+// SEP_Y element rows y): first C[j][i] = sum_t c[i, j, iz+t] Nz[z][t] for the
+// y-basis indices j the chunk's rows use, into shared memory, then
+// B[z][y][i] = sum_s Ny[y][s] C[iy+s][i] (0 where y or z is outside the spline
+// range).  The products and their order are those of k_spline_yz_df (inner
+// sum over t, outer over s); each coefficient is read once per CTA instead of
+// once per output.  The shared table holds cap_j y-basis rows; a chunk whose
+// rows use more (a spline partition finer than the elements) forms its
+// outputs straight from the coefficients.
+constexpr int SEP_Y = 16;
+
+__device__ __forceinline__ df spline_yz_at(const LevelDims& d, const SplineDev& sp, const float2* __restrict__ coeff,
+                                           int i, int y, int iz, const df* nz) {
+  const int iy = sp.i0[1][y], k = sp.order, nbx = sp.nb[0];
+  df v(0);
+  if (iy < 0) return v;
+  for (int s2 = 0; s2 < k; ++s2) {
+    const float2 ns = sp.Ndf[1][y * k + s2];
+    df a(0);
+    for (int t = 0; t < k; ++t) {
+      const float2 c = coeff[i + (int64_t)nbx * ((iy + s2) + (int64_t)sp.nb[1] * (iz + t))];
+      a += df(c.x, c.y) * nz[t];
+    }
+    v += df(ns.x, ns.y) * a;
+  }
+  return v;
+}
+
 __global__ void __launch_bounds__(256) k_spline_yz_sep(LevelDims d, SplineDev sp, const float2* __restrict__ coeff,
-                                                       float2* __restrict__ B) {
-  extern __shared__ float2 sC[];  // [nb1][nb0]
-  const int z = blockIdx.x;
+                                                       float2* __restrict__ B, int cap_j) {
+  extern __shared__ float2 sC[];  // [j - jlo][nb0]
+  __shared__ int sj[2];
+  const int z = blockIdx.x, y0 = blockIdx.y * SEP_Y, y1 = min(y0 + SEP_Y, d.ey);
   const int nbx = sp.nb[0], nby = sp.nb[1], k = sp.order;
   const int iz = sp.i0[2][z];
   float2* Bz = B + (int64_t)nbx * d.ey * z;
   if (iz < 0) {
-    for (int q = threadIdx.x; q < nbx * d.ey; q += blockDim.x) Bz[q] = make_float2(0.f, 0.f);
+    for (int q = threadIdx.x; q < nbx * (y1 - y0); q += blockDim.x) Bz[nbx * y0 + q] = make_float2(0.f, 0.f);
     return;
   }
+  if (threadIdx.x == 0) {  // y-basis indices of the chunk's rows
+    int lo = nby, hi = -1;
+    for (int y = y0; y < y1; ++y) {
+      const int iy = sp.i0[1][y];
+      if (iy >= 0) { lo = min(lo, iy); hi = max(hi, iy + k - 1); }
+    }
+    sj[0] = lo;
+    sj[1] = hi;
+  }
+  __syncthreads();
+  const int jlo = sj[0], nj = sj[1] - sj[0] + 1;
   df nz[4];
 #pragma unroll
   for (int t = 0; t < 4; ++t) {
     const float2 n = t < k ? sp.Ndf[2][z * k + t] : make_float2(0.f, 0.f);
     nz[t] = df(n.x, n.y);
   }
-  for (int q = threadIdx.x; q < nbx * nby; q += blockDim.x) {
-    const int i = q % nbx, j = q / nbx;
+  if (nj > cap_j) {  // (uniform over the CTA)
+    for (int q = threadIdx.x; q < nbx * (y1 - y0); q += blockDim.x) {
+      const df v = spline_yz_at(d, sp, coeff, q % nbx, y0 + q / nbx, iz, nz);
+      Bz[nbx * y0 + q] = make_float2(v.hi, v.lo);
+    }
+    return;
+  }
+  for (int q = threadIdx.x; q < nbx * nj; q += blockDim.x) {
+    const int i = q % nbx, j = jlo + q / nbx;
     df a(0);
     for (int t = 0; t < k; ++t) {
       const float2 c = coeff[i + (int64_t)nbx * (j + (int64_t)nby * (iz + t))];
@@ -214,24 +255,24 @@ __global__ void __launch_bounds__(256) k_spline_yz_sep(LevelDims d, SplineDev sp
     sC[q] = make_float2(a.hi, a.lo);
   }
   __syncthreads();
-  for (int q = threadIdx.x; q < nbx * d.ey; q += blockDim.x) {
-    const int i = q % nbx, y = q / nbx;
+  for (int q = threadIdx.x; q < nbx * (y1 - y0); q += blockDim.x) {
+    const int i = q % nbx, y = y0 + q / nbx;
     const int iy = sp.i0[1][y];
     df v(0);
     if (iy >= 0) {
       for (int s2 = 0; s2 < k; ++s2) {
         const float2 ns = sp.Ndf[1][y * k + s2];
-        const float2 a = sC[i + nbx * (iy + s2)];
+        const float2 a = sC[i + nbx * (iy - jlo + s2)];
         v += df(ns.x, ns.y) * df(a.x, a.y);
       }
     }
-    Bz[q] = make_float2(v.hi, v.lo);
+    Bz[nbx * y0 + q] = make_float2(v.hi, v.lo);
   }
 }
 
-// Pass 2 one element row (y, z) at a time: the row's pass-1 values B[z][y][:]
-// are staged in shared memory, and the next row's values and activity flags
-// are loaded while this row's elements are evaluated (values as
+// Pass 2 two element rows (y, z) at a time: the rows' pass-1 values B[z][y][:]
+// are staged in shared memory, and the next rows' values and activity flags
+// are loaded while these rows' elements are evaluated (values as
 // spline_from_B).  Rows of at most ROW_PF * VOL_THREADS elements and basis
 // indices.
 constexpr int ROW_PF = 4;
@@ -273,45 +314,58 @@ __global__ void __launch_bounds__(VOL_THREADS) k_spline_rows(LevelDims d, const 
                                                              double rho_min, double penal,
                                                              double* __restrict__ partial, double* __restrict__ rho,
                                                              double* __restrict__ rhop, float* __restrict__ rhop32) {
-  __shared__ float2 sB[ROW_PF * VOL_THREADS];
+  // two rows per round: CTA b takes rows 2b, 2b + 1, then 2 gridDim further
+  __shared__ float2 sB[2][ROW_PF * VOL_THREADS];
   const int nbx = sp.nb[0], ex = d.ex, nrows = d.ey * d.ez;
   const df lo = df_from(rho_min), one(1.f, 0.f);
   df sd(0);
-  RowStage st;
-  int row = blockIdx.x;
-  if (row < nrows) row_fetch(st, B, eactive, nbx, ex, row);
-  for (; row < nrows; row += gridDim.x) {
-    __syncthreads();  // the previous row's readers are done with sB
-    uint8_t act[ROW_PF];
+  RowStage st[2];
+  int row = 2 * blockIdx.x;
 #pragma unroll
-    for (int q = 0; q < ROW_PF; ++q) {
-      const int i = threadIdx.x + q * VOL_THREADS;
-      if (i < nbx) sB[i] = st.b[q];
-      act[q] = st.a[q];
-    }
+  for (int r = 0; r < 2; ++r)
+    if (row + r < nrows) row_fetch(st[r], B, eactive, nbx, ex, row + r);
+  for (; row < nrows; row += 2 * gridDim.x) {
+    __syncthreads();  // the previous rows' readers are done with sB
+    uint8_t act[2][ROW_PF];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int q = 0; q < ROW_PF; ++q) {
+        const int i = threadIdx.x + q * VOL_THREADS;
+        if (i < nbx) sB[r][i] = st[r].b[q];
+        act[r][q] = st[r].a[q];
+      }
     __syncthreads();
-    if (row + (int)gridDim.x < nrows) row_fetch(st, B, eactive, nbx, ex, row + gridDim.x);
-    const int y = row % d.ey, z = row / d.ey;
-    const bool yz_in = sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0;
+    const int nxt = row + 2 * (int)gridDim.x;
 #pragma unroll
-    for (int q = 0; q < ROW_PF; ++q) {
-      const int x = threadIdx.x + q * VOL_THREADS;
-      if (x >= ex) continue;
-      if (MODE == 0) {
-        if (!act[q]) continue;
-        df v = row_value(sp, sB, x, yz_in);
-        if (df_lt(v, lo)) v = lo;
-        if (df_lt(one, v)) v = one;
-        sd += v;
-      } else {
-        const int64_t e = x + (int64_t)ex * row;
-        if (!act[q]) {
-          rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
-          continue;
+    for (int r = 0; r < 2; ++r)
+      if (nxt + r < nrows) row_fetch(st[r], B, eactive, nbx, ex, nxt + r);
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int rr = row + r;
+      if (rr >= nrows) break;
+      const int y = rr % d.ey, z = rr / d.ey;
+      const bool yz_in = sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0;
+#pragma unroll
+      for (int q = 0; q < ROW_PF; ++q) {
+        const int x = threadIdx.x + q * VOL_THREADS;
+        if (x >= ex) continue;
+        if (MODE == 0) {
+          if (!act[r][q]) continue;
+          df v = row_value(sp, sB[r], x, yz_in);
+          if (df_lt(v, lo)) v = lo;
+          if (df_lt(one, v)) v = one;
+          sd += v;
+        } else {
+          const int64_t e = x + (int64_t)ex * rr;
+          if (!act[r][q]) {
+            rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
+            continue;
+          }
+          const double v = fmin(fmax(df_to(row_value(sp, sB[r], x, yz_in)), rho_min), 1.0);
+          const double vp = simp_pow(v, penal);
+          rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
         }
-        const double v = fmin(fmax(df_to(row_value(sp, sB, x, yz_in)), rho_min), 1.0);
-        const double vp = simp_pow(v, penal);
-        rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
       }
     }
   }
@@ -333,14 +387,17 @@ __global__ void __launch_bounds__(VOL_THREADS) k_spline_rows(LevelDims d, const 
 // memory (returns false otherwise).
 static bool spline_yz_sep(cudaStream_t s, const LevelDims& d, const SplineDev& sp, const float2* coeff_df,
                           float2* B) {
-  const size_t smem = sizeof(float2) * (size_t)sp.nb[0] * sp.nb[1];
+  // rows of SEP_Y elements span SEP_Y + order - 1 y-basis indices when the
+  // partition is no finer than the elements (the kernel checks each chunk)
+  const int cap_j = std::min(sp.nb[1], SEP_Y + sp.order - 1);
+  const size_t smem = sizeof(float2) * (size_t)sp.nb[0] * cap_j;
   if (sp.order > 4 || smem > 200 * 1024) return false;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_spline_yz_sep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  k_spline_yz_sep<<<d.ez, 256, smem, s>>>(d, sp, coeff_df, B);
+  k_spline_yz_sep<<<dim3(d.ez, (d.ey + SEP_Y - 1) / SEP_Y), 256, smem, s>>>(d, sp, coeff_df, B, cap_j);
   return true;
 }
 
@@ -348,7 +405,7 @@ static bool rows_fit(const LevelDims& d, const SplineDev& sp) {
   return d.ex <= ROW_PF * VOL_THREADS && sp.nb[0] <= ROW_PF * VOL_THREADS;
 }
 
-static int rows_blocks(const LevelDims& d) { return (int)std::min<int64_t>(1024, (int64_t)d.ey * d.ez); }
+static int rows_blocks(const LevelDims& d) { return (int)std::min<int64_t>(1024, ((int64_t)d.ey * d.ez + 1) / 2); }
 
 void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,

@@ -270,9 +270,9 @@ __global__ void __launch_bounds__(256) k_spline_yz_sep(LevelDims d, SplineDev sp
   }
 }
 
-// Pass 2 two element rows (y, z) at a time: the rows' pass-1 values B[z][y][:]
-// are staged in shared memory, and the next rows' values and activity flags
-// are loaded while these rows' elements are evaluated (values as
+// Pass 2 one element row (y, z) at a time: the row's pass-1 values B[z][y][:]
+// are staged in shared memory, and the next row's values and activity flags
+// are loaded while this row's elements are evaluated (values as
 // spline_from_B).  Rows of at most ROW_PF * VOL_THREADS elements and basis
 // indices.
 constexpr int ROW_PF = 4;
@@ -314,58 +314,45 @@ __global__ void __launch_bounds__(VOL_THREADS) k_spline_rows(LevelDims d, const 
                                                              double rho_min, double penal,
                                                              double* __restrict__ partial, double* __restrict__ rho,
                                                              double* __restrict__ rhop, float* __restrict__ rhop32) {
-  // two rows per round: CTA b takes rows 2b, 2b + 1, then 2 gridDim further
-  __shared__ float2 sB[2][ROW_PF * VOL_THREADS];
+  __shared__ float2 sB[ROW_PF * VOL_THREADS];
   const int nbx = sp.nb[0], ex = d.ex, nrows = d.ey * d.ez;
   const df lo = df_from(rho_min), one(1.f, 0.f);
   df sd(0);
-  RowStage st[2];
-  int row = 2 * blockIdx.x;
+  RowStage st;
+  int row = blockIdx.x;
+  if (row < nrows) row_fetch(st, B, eactive, nbx, ex, row);
+  for (; row < nrows; row += gridDim.x) {
+    __syncthreads();  // the previous row's readers are done with sB
+    uint8_t act[ROW_PF];
 #pragma unroll
-  for (int r = 0; r < 2; ++r)
-    if (row + r < nrows) row_fetch(st[r], B, eactive, nbx, ex, row + r);
-  for (; row < nrows; row += 2 * gridDim.x) {
-    __syncthreads();  // the previous rows' readers are done with sB
-    uint8_t act[2][ROW_PF];
-#pragma unroll
-    for (int r = 0; r < 2; ++r)
-#pragma unroll
-      for (int q = 0; q < ROW_PF; ++q) {
-        const int i = threadIdx.x + q * VOL_THREADS;
-        if (i < nbx) sB[r][i] = st[r].b[q];
-        act[r][q] = st[r].a[q];
-      }
+    for (int q = 0; q < ROW_PF; ++q) {
+      const int i = threadIdx.x + q * VOL_THREADS;
+      if (i < nbx) sB[i] = st.b[q];
+      act[q] = st.a[q];
+    }
     __syncthreads();
-    const int nxt = row + 2 * (int)gridDim.x;
+    if (row + (int)gridDim.x < nrows) row_fetch(st, B, eactive, nbx, ex, row + gridDim.x);
+    const int y = row % d.ey, z = row / d.ey;
+    const bool yz_in = sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0;
 #pragma unroll
-    for (int r = 0; r < 2; ++r)
-      if (nxt + r < nrows) row_fetch(st[r], B, eactive, nbx, ex, nxt + r);
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-      const int rr = row + r;
-      if (rr >= nrows) break;
-      const int y = rr % d.ey, z = rr / d.ey;
-      const bool yz_in = sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0;
-#pragma unroll
-      for (int q = 0; q < ROW_PF; ++q) {
-        const int x = threadIdx.x + q * VOL_THREADS;
-        if (x >= ex) continue;
-        if (MODE == 0) {
-          if (!act[r][q]) continue;
-          df v = row_value(sp, sB[r], x, yz_in);
-          if (df_lt(v, lo)) v = lo;
-          if (df_lt(one, v)) v = one;
-          sd += v;
-        } else {
-          const int64_t e = x + (int64_t)ex * rr;
-          if (!act[r][q]) {
-            rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
-            continue;
-          }
-          const double v = fmin(fmax(df_to(row_value(sp, sB[r], x, yz_in)), rho_min), 1.0);
-          const double vp = simp_pow(v, penal);
-          rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
+    for (int q = 0; q < ROW_PF; ++q) {
+      const int x = threadIdx.x + q * VOL_THREADS;
+      if (x >= ex) continue;
+      if (MODE == 0) {
+        if (!act[q]) continue;
+        df v = row_value(sp, sB, x, yz_in);
+        if (df_lt(v, lo)) v = lo;
+        if (df_lt(one, v)) v = one;
+        sd += v;
+      } else {
+        const int64_t e = x + (int64_t)ex * row;
+        if (!act[q]) {
+          rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
+          continue;
         }
+        const double v = fmin(fmax(df_to(row_value(sp, sB, x, yz_in)), rho_min), 1.0);
+        const double vp = simp_pow(v, penal);
+        rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
       }
     }
   }
@@ -405,7 +392,7 @@ static bool rows_fit(const LevelDims& d, const SplineDev& sp) {
   return d.ex <= ROW_PF * VOL_THREADS && sp.nb[0] <= ROW_PF * VOL_THREADS;
 }
 
-static int rows_blocks(const LevelDims& d) { return (int)std::min<int64_t>(1024, ((int64_t)d.ey * d.ez + 1) / 2); }
+static int rows_blocks(const LevelDims& d) { return (int)std::min<int64_t>(1024, (int64_t)d.ey * d.ez); }
 
 void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                              const SplineDev& sp, const double* coeff, double rho_min, double penal,

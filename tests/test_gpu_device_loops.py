@@ -1,0 +1,68 @@
+"""The loops that run on the device inside CUDA graphs (the mixed solve's inner
+FP32 CG, the OC bisection) against the same loops run from the host: their
+stopping rules (tolerance, iteration cap, a non-finite residual) give the same
+outcome, and a failed solve leaves the handle usable."""
+import numpy as np
+import pytest
+
+from topoptspline3d_gb300 import capi, workloads
+
+pytestmark = pytest.mark.gpu
+
+SOLVE = dict(mode=capi.SOLVE_MIXED, smoother=capi.SMOOTH_CHEBYSHEV, rtol=1e-6, max_iter=300, inner_max=4)
+
+
+def _make(graphs):
+    wl = workloads.small_cases()["mbb32"]
+    p = capi.Problem(wl.nx, wl.ny, wl.nz)
+    p.set_bc(wl.fixed, wl.loads)
+    bmin, bmax = wl.spline_box()
+    p.set_spline(wl.order, wl.partition, bmin, bmax)
+    p.put("coeff", np.full(p.num_coeffs(), wl.coeff0))
+    p.coeff_to_density()
+    p.set_operator_precision(2)
+    p.set_graphs(graphs)
+    p.update_operators()
+    return p
+
+
+@pytest.mark.parametrize("graphs", [0, 1])
+def test_inner_cap(graphs):
+    """An inner tolerance that is never met: every inner solve stops at the cap,
+    so the V-cycle count is the cap times the outer iterations."""
+    p = _make(graphs)
+    s = p.solve(**dict(SOLVE, inner_rtol=1e-30, inner_max=3))
+    assert s["relres"] <= 1e-6
+    assert s["vcycles"] == 3 * s["iterations"]
+
+
+@pytest.mark.parametrize("graphs", [0, 1])
+def test_nonfinite_inner_residual(graphs):
+    """A start vector of 1e30 is finite in FP64, but its squares overflow the
+    FP32 inner solver: both loop forms stop and report a non-finite residual,
+    and the next solve from zero converges on the same handle."""
+    p = _make(graphs)
+    n3 = p.get("u").size
+    p.put("u", np.full(n3, 1e30))
+    with pytest.raises(capi.TopoError) as e:
+        p.solve(**SOLVE)
+    assert e.value.code == capi.TOPO_E_NONFINITE
+    p.put("u", np.zeros(n3))
+    s = p.solve(**SOLVE)
+    assert s["relres"] <= 1e-6
+
+
+def test_oc_loop_matches_host():
+    """Same sensitivities and volume goal: the device bisection and the host one
+    take the same number of trials to the same threshold and coefficients."""
+    res = []
+    for graphs in (0, 1):
+        p = _make(graphs)
+        p.solve(**SOLVE)
+        p.sensitivity()
+        p.filter(2.0)
+        p.spline_adjoint()
+        trials, lam = p.oc_update(0.3)
+        res.append((trials, lam, p.get("coeff"), p.get("rho")))
+    assert res[0][0] == res[1][0] and res[0][1] == res[1][1]
+    assert np.array_equal(res[0][2], res[1][2]) and np.array_equal(res[0][3], res[1][3])

@@ -1905,6 +1905,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
   st.ms = ms;
   if (stats) *stats = st;
   CKL();
+  if (!std::isfinite(st.relres)) return fail(h, TOPO_E_NONFINITE, "final residual is not finite");
   if (st.relres > o->rtol) return fail(h, TOPO_E_NOT_CONVERGED, "relative residual %.3e above %.3e after %d iterations", st.relres, o->rtol, st.iterations);
   return TOPO_OK;
 }

@@ -38,12 +38,14 @@ def test_inner_cap(graphs):
 
 @pytest.mark.parametrize("graphs", [0, 1])
 def test_nonfinite_inner_residual(graphs):
-    """A start vector of 1e30 is finite in FP64, but its squares overflow the
-    FP32 inner solver: both loop forms stop and report a non-finite residual,
-    and the next solve from zero converges on the same handle."""
+    """A start vector of random values of size 1e30 (not a rigid translation,
+    so K u is of that size too) is finite in FP64, but the residual's squares
+    overflow the FP32 inner solver: both loop forms stop and report a
+    non-finite residual, and the next solve from zero converges on the same
+    handle."""
     p = _make(graphs)
     n3 = p.get("u").size
-    p.put("u", np.full(n3, 1e30))
+    p.put("u", 1e30 * np.random.default_rng(0).uniform(-1.0, 1.0, n3))
     with pytest.raises(capi.TopoError) as e:
         p.solve(**SOLVE)
     assert e.value.code == capi.TOPO_E_NONFINITE

@@ -368,75 +368,52 @@ __global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
   fc[v] = s0; fc[cd.nv + v] = s1; fc[2 * cd.nv + v] = s2;
 }
 
-// Restriction by a factor of 4 (7 taps per axis, weights (4 - |d|)) with the
-// fine z taps split across the 7 warps of a CTA and the fine rows read whole:
-// lanes that each gathered their own vertex's taps read fine x at a 16-byte
-// stride, 16 sectors per request, and ran L1-bound (41 us at 256x128x128).
+// Restriction by a factor of 4 with the fine z taps split across warps: a CTA
+// of 7 warps covers 32 consecutive coarse vertices; warp w gathers the fine
+// plane z = 4 cz + w - 3 (7 x 7 taps, weights (4 - |d|) per axis) for its lane's
+// vertex, and warp 0 sums the seven partial sums in a fixed order.  Seven
+// times the threads of a vertex-per-thread gather keep the loads in flight.
 constexpr int R4_WARPS = 7;
 
 template <typename T>
 __global__ void __launch_bounds__(32 * R4_WARPS) k_restrict4(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
                                                              T* __restrict__ fc) {
-  // CTA: a segment of up to 32 coarse vertices X0 .. X0 + 31 of the coarse row
-  // (Y, Z); warp w takes the fine plane 4Z + w - 3.  For each of its fine rows
-  // the warp reads the segment's fine x range (4 X0 - 3 .. 4 X0 + 127) with
-  // consecutive lanes on consecutive x into shared memory, one padding word
-  // per 32 so that lane j's reads at 4j .. 4j + 6 fall in distinct banks, and
-  // lane j forms the 7-tap x sum of coarse vertex X0 + j.  The warps' plane
-  // sums are added in shared memory in z order.
-  constexpr int ROWLEN = 4 * 31 + 7, NCH = (ROWLEN + 31) / 32, PADLEN = 32 * NCH + NCH;
-  __shared__ T rowbuf[R4_WARPS][3][PADLEN];
   __shared__ T part[R4_WARPS][3][32];
   rf += (int64_t)blockIdx.y * 3 * fd.nv;  // right-hand side of the batch
   fc += (int64_t)blockIdx.y * 3 * cd.nv;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int nseg = (cd.vx + 31) / 32;
-  const int seg = (int)(blockIdx.x % nseg), rowc = (int)(blockIdx.x / nseg);
-  const int Y = rowc % cd.vy, Z = rowc / cd.vy;
-  const int X0 = 32 * seg, xs = 4 * X0 - 3;
+  const int64_t v = (int64_t)blockIdx.x * 32 + lane;
   T s0 = T(0), s1 = T(0), s2 = T(0);
-  const int dz = w - 3, fz = 4 * Z + dz;
-  if (fz >= 0 && fz < fd.vz) {  // the same for the whole warp
-    const T wz = T(4 - (dz < 0 ? -dz : dz));
-    for (int dy = -3; dy <= 3; ++dy) {
-      const int fy = 4 * Y + dy;
-      if (fy < 0 || fy >= fd.vy) continue;  // the same for the whole warp
-      const T wyz = wz * T(4 - (dy < 0 ? -dy : dy));
-      const T* src = rf + (int64_t)fd.vx * (fy + (int64_t)fd.vy * fz);
-      T v[3][NCH];
+  if (v < cd.nv) {
+    const int x = (int)(v % cd.vx);
+    const int64_t t = v / cd.vx;
+    const int y = (int)(t % cd.vy), z = (int)(t / cd.vy);
+    const int dz = w - 3, fz = 4 * z + dz;
+    if (fz >= 0 && fz < fd.vz) {
+      const T wz = T(4 - (dz < 0 ? -dz : dz));
+      for (int dy = -3; dy <= 3; ++dy) {
+        const int fy = 4 * y + dy;
+        if (fy < 0 || fy >= fd.vy) continue;
+        const T wyz = wz * T(4 - (dy < 0 ? -dy : dy));
+        const int64_t rowv = (int64_t)fd.vx * (fy + (int64_t)fd.vy * fz);
 #pragma unroll
-      for (int k = 0; k < NCH; ++k) {
-        const int rel = lane + 32 * k, fx = xs + rel;
-        const bool ok = rel < ROWLEN && fx >= 0 && fx < fd.vx;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) v[c][k] = ok ? src[c * fd.nv + fx] : T(0);
+        for (int dx = -3; dx <= 3; ++dx) {
+          const int fx = 4 * x + dx;
+          if (fx < 0 || fx >= fd.vx) continue;
+          const T wt = wyz * T(4 - (dx < 0 ? -dx : dx));
+          const int64_t fv = rowv + fx;
+          s0 += wt * rf[fv];
+          s1 += wt * rf[fd.nv + fv];
+          s2 += wt * rf[2 * fd.nv + fv];
+        }
       }
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int k = 0; k < NCH; ++k) rowbuf[w][c][lane + 33 * k] = v[c][k];
-      __syncwarp();
-      T xr[3] = {T(0), T(0), T(0)};
-#pragma unroll
-      for (int t = 0; t < 7; ++t) {
-        const int rel = 4 * lane + t;
-        const T wx = T(4 - (t < 3 ? 3 - t : t - 3));
-#pragma unroll
-        for (int c = 0; c < 3; ++c) xr[c] += wx * rowbuf[w][c][rel + rel / 32];
-      }
-      s0 += wyz * xr[0];
-      s1 += wyz * xr[1];
-      s2 += wyz * xr[2];
-      __syncwarp();  // the buffer is refilled for the next row
     }
   }
   part[w][0][lane] = s0;
   part[w][1][lane] = s1;
   part[w][2][lane] = s2;
   __syncthreads();
-  const int X = X0 + lane;
-  if (w == 0 && X < cd.vx) {
-    const int64_t v = X + (int64_t)cd.vx * rowc;
+  if (w == 0 && v < cd.nv) {
     const T inv = T(1) / T(64);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -494,75 +471,78 @@ template <typename T>
 void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
                      T* fc, int nb) {
   if (coarse.factor == 4) {
-    const int64_t nseg = (coarse.vx + 31) / 32;
-    k_restrict4<T><<<dim3((unsigned)(nseg * coarse.vy * coarse.vz), nb), 32 * R4_WARPS, 0, s>>>(fine, coarse, rf,
-                                                                                             fc);
+    k_restrict4<T><<<dim3(nblk(coarse.nv, 32), nb), 32 * R4_WARPS, 0, s>>>(fine, coarse, rf, fc);
   } else {
     k_restrict<T, 2><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
   }
 }
 
-// Prolongation by a factor of 4, one warp per 32 consecutive fine vertices of
-// a fine row (y, z), one lane per vertex, so the fine values, masks and
-// updates move in whole cache lines.  The row's coarse corners are weighted in
-// y and z once per coarse x: lane L forms that sum for coarse x = x0/4 + L
-// (L < 10), and each lane takes its two corner sums by shuffle.  Corners with a
-// zero weight are not read (they may lie outside the coarse grid).  Lanes of a
-// 4-vertex group reading x at a 16-byte stride ran at 8.7 sectors per request
-// (40 us at 256x128x128).
+// Prolongation by a factor of 4 with one thread per 4 fine vertices along x
+// (x = 4 cx .. 4 cx + 3 share the coarse corners cx, cx + 1): the 24 coarse
+// values are read once per 4 fine vertices instead of once per vertex.
 template <typename T>
 __global__ void __launch_bounds__(256) k_prolong4x(LevelDims fd, LevelDims cd, const T* __restrict__ uc,
                                                    T* __restrict__ uf, const uint8_t* __restrict__ vmask) {
   uc += (int64_t)blockIdx.y * 3 * cd.nv;  // right-hand side of the batch
   uf += (int64_t)blockIdx.y * 3 * fd.nv;
-  const int lane = threadIdx.x & 31;
-  const int nch = (fd.vx + 31) / 32;  // 32-vertex chunks per fine row
-  const int64_t chunk = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (chunk >= (int64_t)nch * fd.vy * fd.vz) return;  // whole warp
-  const int xc = (int)(chunk % nch);
-  const int64_t t = chunk / nch;
+  const int nqx = (fd.vx + 3) / 4;  // 4-vertex groups per fine row
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nq = (int64_t)nqx * fd.vy * fd.vz;
+  if (q >= nq) return;
+  const int cx = (int)(q % nqx);
+  const int64_t t = q / nqx;
   const int y = (int)(t % fd.vy), z = (int)(t / fd.vy);
   const int cy = y / 4, cz = z / 4, ry = y % 4, rz = z % 4;
-  const int x0 = 32 * xc, X0 = x0 / 4;
-  // lane L < 10: corners of coarse x = X0 + L weighted in y and z
-  T cyz[3] = {T(0), T(0), T(0)};
-  if (lane < 10 && X0 + lane < cd.vx) {
+  // coarse corners (cx + ox, cy + oy, cz + oz) weighted in y and z; corners
+  // with a zero weight are not read (they may lie outside the coarse grid)
+  T cyz[2][3];  // [ox][component]: sum over oy, oz of wy wz u_c
+#pragma unroll
+  for (int ox = 0; ox < 2; ++ox) {
+    cyz[ox][0] = cyz[ox][1] = cyz[ox][2] = T(0);
+    if (cx + ox >= cd.vx) continue;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int oy = k & 1, oz = k >> 1;
       const int w = (oy ? ry : 4 - ry) * (oz ? rz : 4 - rz);
       if (w == 0) continue;
-      const int64_t cv = (X0 + lane) + (int64_t)cd.vx * ((cy + oy) + (int64_t)cd.vy * (cz + oz));
-      cyz[0] += T(w) * uc[cv];
-      cyz[1] += T(w) * uc[cd.nv + cv];
-      cyz[2] += T(w) * uc[2 * cd.nv + cv];
+      const int64_t cv = (cx + ox) + (int64_t)cd.vx * ((cy + oy) + (int64_t)cd.vy * (cz + oz));
+      cyz[ox][0] += T(w) * uc[cv];
+      cyz[ox][1] += T(w) * uc[cd.nv + cv];
+      cyz[ox][2] += T(w) * uc[2 * cd.nv + cv];
     }
   }
-  const int x = x0 + lane;
-  const int a = x / 4 - X0, rx = x % 4;
-  T c0[3], c1[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    c0[c] = __shfl_sync(0xffffffffu, cyz[c], a);
-    c1[c] = __shfl_sync(0xffffffffu, cyz[c], a + 1);
-  }
-  if (x >= fd.vx) return;
-  const int64_t v = x + (int64_t)fd.vx * (y + (int64_t)fd.vy * z);
-  const uint8_t m = vmask[v];
-  if (!(m & 7) || !(m & 8)) return;
   const T inv = T(1) / T(64);
-  const T w0 = T(4 - rx), w1 = T(rx);
+  const int64_t row = (int64_t)fd.vx * (y + (int64_t)fd.vy * z);
+  // masks and fine values of the four vertices are loaded together (a vertex
+  // past the row's end reads the group's first), then the corrections added
+  uint8_t mm[4];
+  T uo[4][3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
-    if ((m >> c) & 1) uf[c * fd.nv + v] += (w0 * c0[c] + w1 * c1[c]) * inv;
+  for (int rx = 0; rx < 4; ++rx) {
+    const int x = 4 * cx + rx;
+    const int64_t v = row + (x < fd.vx ? x : 4 * cx);
+    mm[rx] = x < fd.vx ? vmask[v] : 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) uo[rx][c] = uf[c * fd.nv + v];
+  }
+#pragma unroll
+  for (int rx = 0; rx < 4; ++rx) {
+    const uint8_t m = mm[rx];
+    if (!(m & 7) || !(m & 8)) continue;
+    const int64_t v = row + 4 * cx + rx;
+    const T w0 = T(4 - rx), w1 = T(rx);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      if ((m >> c) & 1) uf[c * fd.nv + v] = uo[rx][c] + (w0 * cyz[0][c] + w1 * cyz[1][c]) * inv;
+  }
 }
 
 template <typename T>
 void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* uc,
                     T* uf, const uint8_t* vmask_fine, int nb) {
   if (coarse.factor == 4) {
-    const int64_t nchunks = (int64_t)((fine.vx + 31) / 32) * fine.vy * fine.vz;
-    k_prolong4x<T><<<dim3(nblk(nchunks, 8), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
+    const int64_t nq = (int64_t)((fine.vx + 3) / 4) * fine.vy * fine.vz;
+    k_prolong4x<T><<<dim3(nblk(nq, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
   } else
     k_prolong<T, 2><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
 }

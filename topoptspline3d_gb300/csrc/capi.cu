@@ -567,13 +567,25 @@ __global__ void k_power_start(int64_t nv, const uint8_t* vmask, T* x) {
 }
 
 // z = s D^-1 r with s = 1/sqrt(*nrm2) (the power iteration's normalisation of
-// its vector, applied after the operator, which is linear).
+// its vector, applied after the operator, which is linear).  D^-1 is [9][nv],
+// or with sym the packed symmetric layout of level 0's FP32 inverse (float4
+// d00 d01 d02 d11 per vertex, then float2 d12 d22).
 template <typename T>
-__global__ void k_dinv_apply(int64_t nv, const T* dinv, const T* r, T* z, const double* nrm2) {
+__global__ void k_dinv_apply(int64_t nv, const T* dinv, const T* r, T* z, const double* nrm2, bool sym) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   const T sc = (T)rsqrt(*nrm2);
   const T r0 = r[v] * sc, r1 = r[nv + v] * sc, r2 = r[2 * nv + v] * sc;
+  if constexpr (sizeof(T) == 4) {
+    if (sym) {
+      const float4 a = reinterpret_cast<const float4*>(dinv)[v];
+      const float2 b = reinterpret_cast<const float2*>(dinv + 4 * nv)[v];
+      z[v] = a.x * r0 + a.y * r1 + a.z * r2;
+      z[nv + v] = a.y * r0 + a.w * r1 + b.x * r2;
+      z[2 * nv + v] = a.z * r0 + b.x * r1 + b.y * r2;
+      return;
+    }
+  }
   for (int i = 0; i < 3; ++i)
     z[i * nv + v] = dinv[(3 * i) * nv + v] * r0 + dinv[(3 * i + 1) * nv + v] * r1 + dinv[(3 * i + 2) * nv + v] * r2;
 }
@@ -709,7 +721,8 @@ int estimate_bounds(topo_handle* h) {
       if (r.l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, r.x, nullptr, r.y, false, 1,
                                          sizeof(T) == 4 ? h->tz32 : h->tz64);
       else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), r.x, nullptr, r.y, false);
-      k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), r.y, r.z, sl);
+      k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), r.y, r.z, sl,
+                                                           sizeof(T) == 4 && r.l == 0);
       launch_dot<T>(h->stream, r.x, r.z, n3, h->partial, sl + 1, h->ctr);
       std::swap(r.x, r.z);
       count_launch(4);

@@ -32,9 +32,6 @@ __device__ __forceinline__ double modal_c<double>(int i) { return cModal64[i]; }
 template <>
 __device__ __forceinline__ float modal_c<float>(int i) { return cModal32[i]; }
 
-// Diagonal 3x3 blocks Ke[a,a] of the eight local nodes (FP32 smoother epilogue).
-__constant__ float cKdiag32[8][9];
-
 // Modal constants split into hi + lo floats.
 __constant__ float2 cModalDF[5];
 template <>
@@ -48,11 +45,6 @@ void upload_template(const double* Ke576, double lam, double mu, double h) {
   for (int i = 0; i < 576; ++i) k32[i] = (float)Ke576[i];
   cudaMemcpyToSymbol(cKe64, Ke576, sizeof(double) * 576);
   cudaMemcpyToSymbol(cKe32, k32, sizeof(float) * 576);
-  float kd[8][9];
-  for (int a = 0; a < 8; ++a)
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) kd[a][3 * i + j] = (float)Ke576[(3 * a + i) * 24 + 3 * a + j];
-  cudaMemcpyToSymbol(cKdiag32, kd, sizeof(kd));
   const double m64[5] = {lam, mu, h / 16.0, h / 48.0, h / 144.0};
   const float m32[5] = {(float)m64[0], (float)m64[1], (float)m64[2], (float)m64[3], (float)m64[4]};
   cudaMemcpyToSymbol(cModal64, m64, sizeof(m64));
@@ -281,7 +273,7 @@ __device__ __forceinline__ void modal_element(T c[3][8], T pe, T* energy = nullp
 // MODE 0: out = K u; 1: out = f - K u; 2: one Chebyshev step, r = f - K u,
 // z = Dinv r, d = c_old d + c_new z (first: c_new z), out = u + d (out != u).
 struct ChebArgs {
-  const void* dinv;  // [9][nv]
+  const void* dinv;  // block inverse: [9][nv] (FP64), packed symmetric (FP32, dinv_sym_apply)
   void* dvec;        // [3][nv]
   const double* coef;  // (c_old, c_new) of the step, in device memory
   int first;
@@ -360,29 +352,17 @@ struct ModalSmem {
   Vec4<T> fe[8][NT];     // nodal forces of the layer's elements, per local node
 };
 
-// z = S^-1 r for the free-DOF part of a symmetric 3x3 block S (fixed rows and
-// columns act as identity and give z = 0), by the adjugate.
-template <typename T>
-__device__ __forceinline__ void block_solve_free(const T S_in[9], uint8_t fb, const T r[3], T z[3]) {
-  T S[9];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      S[3 * i + j] = (((fb >> i) & 1) && ((fb >> j) & 1)) ? S_in[3 * i + j] : (i == j ? T(1) : T(0));
-  const T a = S[0], b = S[1], c = S[2], dd = S[4], e = S[5], f = S[8];
-  const T A0 = dd * f - e * e, A1 = c * e - b * f, A2 = b * e - c * dd;
-  const T A4 = a * f - c * c, A5 = b * c - a * e, A8 = a * dd - b * b;
-  const T rd = T(1) / (a * A0 + b * A1 + c * A2);
-  T rr[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) rr[i] = ((fb >> i) & 1) ? r[i] : T(0);
-  z[0] = (A0 * rr[0] + A1 * rr[1] + A2 * rr[2]) * rd;
-  z[1] = (A1 * rr[0] + A4 * rr[1] + A5 * rr[2]) * rd;
-  z[2] = (A2 * rr[0] + A5 * rr[1] + A8 * rr[2]) * rd;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-    if (!((fb >> i) & 1)) z[i] = T(0);
+// z = D^-1 r with level 0's FP32 block inverse in its packed symmetric layout:
+// float4 (d00, d01, d02, d11) per vertex, then float2 (d12, d22) per vertex
+// (24 bytes and two loads per vertex instead of nine; the same products in the
+// same order as the [9][nv] form, since the stored block is symmetric).
+__device__ __forceinline__ void dinv_sym_apply(const float* __restrict__ dinv, int64_t nv, int64_t v, const float r[3],
+                                               float z[3]) {
+  const float4 a = reinterpret_cast<const float4*>(dinv)[v];
+  const float2 b = reinterpret_cast<const float2*>(dinv + 4 * nv)[v];
+  z[0] = a.x * r[0] + a.y * r[1] + a.z * r[2];
+  z[1] = a.y * r[0] + a.w * r[1] + b.x * r[2];
+  z[2] = a.z * r[0] + b.x * r[1] + b.y * r[2];
 }
 
 // Build-time choices for the FP32 kernel, measured on GB300 (half-MBB
@@ -734,14 +714,11 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
               if (MODE == 0) dsum += uv[c] * o;
             }
           } else {
-            const float* __restrict__ dinv = static_cast<const float*>(ch.dinv);
             float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * nv;
             float r[3], zc[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : 0.f;
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-              zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
+            dinv_sym_apply(static_cast<const float*>(ch.dinv), nv, v, r, zc);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const float dold = ch.d_is_u ? uv[c] : dv_c[c];
@@ -1056,7 +1033,8 @@ __global__ void __launch_bounds__(256) k_fine_gs(LevelDims d, const T* __restric
   block_update<T>(u, d.nv, v, r, S, fb, reverse);
 }
 
-// Inverse of the free-DOF part of each diagonal 3x3 block, [9][nv] (Chebyshev).
+// Inverse of the free-DOF part of each diagonal 3x3 block (Chebyshev): [9][nv]
+// in FP64, the packed symmetric layout of dinv_sym_apply in FP32.
 template <typename T>
 __device__ __forceinline__ void invert_block(const T S_in[9], uint8_t fb, T* dinv, int64_t nv,
                                              int64_t v) {
@@ -1071,11 +1049,19 @@ __device__ __forceinline__ void invert_block(const T S_in[9], uint8_t fb, T* din
   const T det = a * A0 + b * A1 + c * A2;
   const T inv[9] = {A0, A1, A2, A1, a * f - c * c, b * c - a * e, A2, b * c - a * e, a * dd - b * b};
   const T rd = T(1) / det;
+  T o[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const int i = k / 3, j = k % 3;
     const bool keep = ((fb >> i) & 1) && ((fb >> j) & 1);
-    dinv[k * nv + v] = keep ? inv[k] * rd : T(0);
+    o[k] = keep ? inv[k] * rd : T(0);
+  }
+  if constexpr (sizeof(T) == 4) {  // FP32: the packed symmetric layout (the block is symmetric entry for entry)
+    reinterpret_cast<float4*>(dinv)[v] = make_float4(o[0], o[1], o[2], o[4]);
+    reinterpret_cast<float2*>(dinv + 4 * nv)[v] = make_float2(o[5], o[8]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dinv[k * nv + v] = o[k];
   }
 }
 
@@ -1230,54 +1216,25 @@ template int launch_fine_cheb<float>(cudaStream_t, const LevelDims&, const float
 // First Chebyshev step from a zero iterate (every pre-smoothing sweep of a
 // preconditioning V-cycle starts from u = 0): K u vanishes, so r = f on the
 // free DOFs, d = c_new D^-1 r and u_out = d.  No vertex planes are read and no
-// element operator is applied; the result equals the fused step's on u = 0.
-// The FP32 diagonal block is rebuilt from the eight incident elements' rho^p
-// (four in layer z, four in layer z - 1) in the fused step's order; FP64 uses
-// the stored inverse.  blockIdx.y is the right-hand side of a batch.
-__global__ void k_fine_cheb_zero32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
+// element operator is applied; with the stored FP32 block inverse (packed
+// symmetric layout) the result equals the fused step's on u = 0.  Rebuilding
+// the blocks from the eight incident elements' rho^p here took about 350
+// instructions per vertex and ran issue-bound (47 us at 256x128x128).
+// blockIdx.y is the right-hand side of a batch.
+__global__ void k_fine_cheb_zero32(int64_t nv, const uint8_t* __restrict__ vmask, const float* __restrict__ dinv,
                                    const float* __restrict__ f, float* __restrict__ dv, float* __restrict__ out,
                                    const double* __restrict__ coef) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= d.nv) return;
-  const int64_t nv = d.nv, bo = (int64_t)blockIdx.y * 3 * nv;
+  if (v >= nv) return;
+  const int64_t bo = (int64_t)blockIdx.y * 3 * nv;
   f += bo;
   if (dv) dv += bo;
   out += bo;
   const uint8_t m = vmask[v];
-  int x, y, z;
-  if (nv < (int64_t)1 << 31) {  // 32-bit index arithmetic
-    const unsigned vv = (unsigned)v, vx = (unsigned)d.vx, tt = vv / vx;
-    x = (int)(vv - tt * vx);
-    y = (int)(tt % (unsigned)d.vy);
-    z = (int)(tt / (unsigned)d.vy);
-  } else {
-    x = (int)(v % d.vx);
-    const int64_t t = v / d.vx;
-    y = (int)(t % d.vy);
-    z = (int)(t / d.vy);
-  }
-  float pl[4], pp[4];
-#pragma unroll
-  for (int w = 0; w < 4; ++w) {
-    const int ex = x - 1 + (w & 1), ey = y - 1 + (w >> 1);
-    const bool xy = ex >= 0 && ey >= 0 && ex < d.ex && ey < d.ey;
-    const int64_t e = ex + (int64_t)d.ex * (ey + (int64_t)d.ey * z);
-    pl[w] = (xy && z < d.ez) ? rhop[e] : 0.f;
-    pp[w] = (xy && z >= 1 && z - 1 < d.ez) ? rhop[e - (int64_t)d.ex * d.ey] : 0.f;
-  }
-  float S[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) S[k] = 0.f;
-#pragma unroll
-  for (int w = 0; w < 4; ++w) {
-    const int a = (1 - (w & 1)) + 2 * (1 - (w >> 1));
-#pragma unroll
-    for (int k = 0; k < 9; ++k) S[k] += pl[w] * cKdiag32[a][k] + pp[w] * cKdiag32[a + 4][k];
-  }
   float r[3], zc[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] : 0.f;
-  block_solve_free<float>(S, (m & 8) ? (m & 7) : 0, r, zc);
+  dinv_sym_apply(dinv, nv, v, r, zc);
   const float c_new = (float)__ldg(coef + 1);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -1292,7 +1249,7 @@ void launch_fine_cheb_zero(cudaStream_t s, const LevelDims& d, const T* rhop, co
                            T* uout, const T* dinv, T* dvec, const double* coef, int nb) {
   if (sizeof(T) == 4) {  // dvec may be null: d is not stored (the next step takes d = u)
     k_fine_cheb_zero32<<<dim3(blocks_for(d.nv, 256), nb), 256, 0, s>>>(
-        d, reinterpret_cast<const float*>(rhop), vmask, reinterpret_cast<const float*>(f),
+        d.nv, vmask, reinterpret_cast<const float*>(dinv), reinterpret_cast<const float*>(f),
         reinterpret_cast<float*>(dvec), reinterpret_cast<float*>(uout), coef);
   } else {
     launch_cheb_zero_stored<T>(s, d.nv, vmask, dinv, f, dvec, uout, coef, nb);

@@ -36,7 +36,7 @@ struct DevLevel {
   double* stencil = nullptr;    // coarse: FP64 [243][nv]
   float* stencil32 = nullptr;   // coarse: FP32 [243][nv]
   double* dinv = nullptr;       // FP64 inverse diagonal blocks [9][nv] (Chebyshev)
-  float* dinv32 = nullptr;      // FP32 inverse diagonal blocks [9][nv]
+  float* dinv32 = nullptr;      // FP32 inverse diagonal blocks [9][nv]; level 0: packed symmetric (float4 d00 d01 d02 d11 [nv], float2 d12 d22 [nv])
   double* cd = nullptr;         // FP64 Chebyshev direction [3nv]
   float* cd32 = nullptr;        // FP32 Chebyshev direction [3nv]
   double* U2 = nullptr;         // FP64 second iterate buffer (Chebyshev ping-pong) [3nv]

@@ -93,89 +93,72 @@ __global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st,
   for (int k = 0; k < 9; ++k) dinv[k * d.nv + v] = act ? inv[k] * rd : T(0);
 }
 
-// Row- and plane-split stencil kernels: a CTA of 3 x 3 x SV threads covers SV
-// vertices, one thread per (vertex, row, neighbour z-plane); the plane sums
-// meet in shared memory and are added in plane order.  One thread per (vertex,
-// row) walked all 27 neighbours and left level 1 of 256x128x128 (70,785
-// vertices) one partial wave of latency-bound threads (22 us per Chebyshev
-// step, 64% of warp slots occupied).
-constexpr int SV = 32;
+// Row-split stencil kernels: a CTA of 3 x SV threads covers SV vertices, one
+// thread per (vertex, row); the three rows of a vertex share its neighbours'
+// values through L1.  Three times the threads of a vertex-per-thread kernel keep
+// enough loads in flight on the small coarse levels.
+constexpr int SV = 64;
 
-// Row `row` of A u at vertex v (x, y, z), neighbours in z-plane z + kz - 1.
 template <typename T>
-__device__ __forceinline__ T stencil_row_plane(const LevelDims& d, const T* __restrict__ st, const T* __restrict__ u,
-                                               int x, int y, int z, int64_t v, int row, int kz) {
+__device__ __forceinline__ T stencil_row_i(const LevelDims& d, const T* __restrict__ st, const T* __restrict__ u,
+                                           int x, int y, int z, int64_t v, int row) {
   T o = T(0);
   const int64_t nv = d.nv;
-  const int nz = z + kz - 1;
-  if (nz < 0 || nz >= d.vz) return o;
 #pragma unroll
-  for (int kk = 0; kk < 9; ++kk) {
-    const int nx = x + kk % 3 - 1, ny = y + kk / 3 - 1;
-    if (nx < 0 || ny < 0 || nx >= d.vx || ny >= d.vy) continue;
+  for (int k = 0; k < 27; ++k) {
+    const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
+    if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) continue;
     const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
-    const T* s = st + (int64_t)((9 * kz + kk) * 9 + 3 * row) * nv + v;
+    const T* s = st + (int64_t)(k * 9 + 3 * row) * nv + v;
     o += s[0] * u[n] + s[nv] * u[nv + n] + s[2 * nv] * u[2 * nv + n];
   }
   return o;
 }
 
-// Plane partial sums of the rows of A u at the CTA's vertices into
-// part[kz][row][lv], valid after the barrier every thread reaches.
 template <typename T>
-__device__ __forceinline__ void stencil_rows_cta(const LevelDims& d, const T* __restrict__ st, const T* __restrict__ u,
-                                                 T (*part)[3][SV], int64_t v, int row, int kz, int lv) {
-  T o = T(0);
-  if (v < d.nv) {
-    const int x = (int)(v % d.vx);
-    const int64_t t = v / d.vx;
-    const int y = (int)(t % d.vy), z = (int)(t / d.vy);
-    o = stencil_row_plane<T>(d, st, u, x, y, z, v, row, kz);
-  }
-  part[kz][row][lv] = o;
-  __syncthreads();
-}
-
-template <typename T>
-__global__ void __launch_bounds__(9 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st,
+__global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st,
                                                            const T* __restrict__ u, const T* __restrict__ f,
                                                            T* __restrict__ out, bool residual) {
-  __shared__ T part[3][3][SV];
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
   if (f) f += bo;
   out += bo;
-  const int kz = threadIdx.x / (3 * SV), row = threadIdx.x / SV % 3, lv = threadIdx.x % SV;
-  const int64_t v = (int64_t)blockIdx.x * SV + lv;
-  stencil_rows_cta<T>(d, st, u, part, v, row, kz, lv);
-  if (kz != 0 || v >= d.nv) return;
-  const T o = part[0][row][lv] + part[1][row][lv] + part[2][row][lv];
+  const int row = threadIdx.x / SV;
+  const int64_t v = (int64_t)blockIdx.x * SV + threadIdx.x % SV;
+  if (v >= d.nv) return;
+  const int x = (int)(v % d.vx);
+  const int64_t t = v / d.vx;
+  const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+  const T o = stencil_row_i<T>(d, st, u, x, y, z, v, row);
   const int64_t i = row * d.nv + v;
   out[i] = residual ? f[i] - o : o;
 }
 
 // One Chebyshev step on a stencil level: uout = u + d, d = c_old d + c_new Dinv (f - A u).
 template <typename T>
-__global__ void __launch_bounds__(9 * SV) k_stencil_cheb(LevelDims d, const T* __restrict__ st,
+__global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* __restrict__ st,
                                                          const T* __restrict__ u, const T* __restrict__ f,
                                                          T* __restrict__ uout, const T* __restrict__ dinv,
                                                          T* __restrict__ dv, const double* __restrict__ coef,
                                                          bool first) {
-  __shared__ T part[3][3][SV];
   __shared__ T sr[3][SV];
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
   f += bo;
   uout += bo;
   dv += bo;
-  const int kz = threadIdx.x / (3 * SV), row = threadIdx.x / SV % 3, lv = threadIdx.x % SV;
+  const int row = threadIdx.x / SV, lv = threadIdx.x % SV;
   const int64_t v = (int64_t)blockIdx.x * SV + lv;
   const int64_t nv = d.nv;
   const bool ok = v < nv;
-  stencil_rows_cta<T>(d, st, u, part, v, row, kz, lv);
-  if (kz == 0 && ok) sr[row][lv] = f[row * nv + v] - (part[0][row][lv] + part[1][row][lv] + part[2][row][lv]);
+  if (ok) {
+    const int x = (int)(v % d.vx);
+    const int64_t t = v / d.vx;
+    const int y = (int)(t % d.vy), z = (int)(t / d.vy);
+    sr[row][lv] = f[row * nv + v] - stencil_row_i<T>(d, st, u, x, y, z, v, row);
+  }
   __syncthreads();
-  if (kz != 0 || !ok) return;
+  if (!ok) return;
   const T zz = dinv[(3 * row) * nv + v] * sr[0][lv] + dinv[(3 * row + 1) * nv + v] * sr[1][lv] +
                dinv[(3 * row + 2) * nv + v] * sr[2][lv];
   const int64_t i = row * nv + v;
@@ -275,7 +258,7 @@ void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const
   if (d.nv < STENCIL_WARP_MAX_NV)
     k_stencil_apply_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, out, residual);
   else
-    k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 9 * SV, 0, s>>>(d, st, u, f, out, residual);
+    k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
 }
 
 template <typename T>
@@ -284,7 +267,7 @@ void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const 
   if (d.nv < STENCIL_WARP_MAX_NV)
     k_stencil_cheb_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
   else
-    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 9 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
+    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,

@@ -5,6 +5,7 @@
 // are zero; vectors are kept zero on fixed DOFs, which removes the fixed columns
 // exactly as the reference's WS kernels do (grid/Grid.cu:2277-2333, 1699-1842).
 #include <mutex>
+#include <type_traits>
 
 #include "df.cuh"
 #include "topo_internal.h"
@@ -356,7 +357,8 @@ struct ModalSmem {
 // float4 (d00, d01, d02, d11) per vertex, then float2 (d12, d22) per vertex
 // (24 bytes and two loads per vertex instead of nine; the same products in the
 // same order as the [9][nv] form, since the stored block is symmetric).
-__device__ __forceinline__ void dinv_sym_apply(const float* __restrict__ dinv, int64_t nv, int64_t v, const float r[3],
+template <typename I>
+__device__ __forceinline__ void dinv_sym_apply(const float* __restrict__ dinv, I nv, I v, const float r[3],
                                                float z[3]) {
   const float4 a = reinterpret_cast<const float4*>(dinv)[v];
   const float2 b = reinterpret_cast<const float2*>(dinv + 4 * nv)[v];
@@ -591,14 +593,17 @@ struct Modal32Smem {
   float coef[2];        // Chebyshev (c_old, c_new), read after each plane's barrier
 };
 
-template <int TYE, int MODE>
+template <int TYE, int MODE, bool I32>
 __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ? TOPO_FINE32_CHEB_THREADS_PER_SM
                                                                                : TOPO_FINE32_THREADS_PER_SM))
     k_fine_modal32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
                    const float* __restrict__ u, const float* __restrict__ f, float* __restrict__ out, int TZ,
                    ChebArgs ch) {
-  // MODE 3: the Chebyshev step of MODE 2 that also sums f.out
+  // MODE 3: the Chebyshev step of MODE 2 that also sums f.out.  I32: vertex and
+  // element offsets within one right-hand side in 32-bit arithmetic (3 nv and
+  // ne below 2^31), one instruction per address instead of two.
   constexpr bool CHEB = MODE >= 2, DOTS = MODE == 3;
+  using I = typename std::conditional<I32, int, int64_t>::type;
   using S = Modal32Smem<TYE>;
   constexpr int TXE = 32, NT = S::NT, PX = S::PX, NP = S::NP;
   extern __shared__ __align__(16) unsigned char m32_smem[];
@@ -611,10 +616,10 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   const int zblk = (d.vz + TZ - 1) / TZ;
   const int rhs = blockIdx.z / zblk;
   const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
-  const int64_t nv = d.nv;
-  u += (int64_t)rhs * 3 * nv;
-  if (f) f += (int64_t)rhs * 3 * nv;
-  out += (int64_t)rhs * 3 * nv;
+  const I nv = (I)d.nv;
+  u += (int64_t)rhs * 3 * d.nv;
+  if (f) f += (int64_t)rhs * 3 * d.nv;
+  out += (int64_t)rhs * 3 * d.nv;
   const int gx = x0 + i, gy = y0 + j;
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
   const int zend = min(z0 + TZ, d.vz);
@@ -626,18 +631,18 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
     const int vx = x0 - 1 + px, vy = y0 - 1 + py;
     pxy[s] = (k < NP && vx >= 0 && vy >= 0 && vx < d.vx && vy < d.vy) ? vx + d.vx * vy : -1;
   }
-  const int64_t plane_n = (int64_t)d.vx * d.vy;
+  const I plane_n = (I)d.vx * d.vy;
   auto prefetch = [&](int z) {
     if (z <= zend) {
       float4* dst = sm.plane[(z + 4) & 3];
       const bool zok = z >= 0 && z < d.vz;
-      const int64_t zoff = (int64_t)z * plane_n;
+      const I zoff = (I)z * plane_n;
 #pragma unroll
       for (int s = 0; s < KS; ++s) {
         const int k = t + s * NT;
         if (k < NP) {
           const bool ok = zok && pxy[s] >= 0;
-          const int64_t v = ok ? zoff + pxy[s] : 0;
+          const I v = ok ? zoff + pxy[s] : 0;
           cp_async_4(&dst[k].x, u + v, ok);
           cp_async_4(&dst[k].y, u + nv + v, ok);
           cp_async_4(&dst[k].z, u + 2 * nv + v, ok);
@@ -649,16 +654,16 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   const int pex = gx - 1, pey = gy - 1;
   const bool pe_xy = pex >= 0 && pey >= 0 && pex < d.ex && pey < d.ey;
   auto load_pe = [&](int ez) -> float {
-    return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (int64_t)d.ex * (pey + (int64_t)d.ey * ez)] : 0.f;
+    return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (I)d.ex * (pey + (I)d.ey * ez)] : 0.f;
   };
   const float* __restrict__ dvin =
-      (CHEB && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
+      (CHEB && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * d.nv : nullptr;
   // operands of the owned vertex at plane z, read in step z and used in step z + 1
   uint8_t vm_n = 0;
   float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f};
   auto load_vertex = [&](int z) {
     if (!own || z < z0 || z >= zend) return;
-    const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * z);
+    const I v = gx + (I)d.vx * (gy + (I)d.vy * z);
     vm_n = vmask[v];
     if (MODE >= 1) {
 #pragma unroll
@@ -702,7 +707,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
           top[c] = own1[1][c] + r1[c];
         }
         if (p >= z0) {
-          const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * p);
+          const I v = gx + (I)d.vx * (gy + (I)d.vy * p);
           const uint8_t m = vm_c;
           const float uv[3] = {uo[0], uo[1], uo[2]};
           if (!CHEB) {
@@ -714,7 +719,7 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
               if (MODE == 0) dsum += uv[c] * o;
             }
           } else {
-            float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * nv;
+            float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * d.nv;
             float r[3], zc[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : 0.f;
@@ -1118,9 +1123,13 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
     const size_t smem = sizeof(Modal32Smem<TYE>);
     static std::once_flag once;
     std::call_once(once, [smem] {
-      cudaFuncSetAttribute(k_fine_modal32<TYE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
-    k_fine_modal32<TYE, MODE><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+    if (3 * d.nv < ((int64_t)1 << 31) && d.ne < ((int64_t)1 << 31))
+      k_fine_modal32<TYE, MODE, true><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+    else
+      k_fine_modal32<TYE, MODE, false><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
   } else {
     const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
     static std::once_flag once;

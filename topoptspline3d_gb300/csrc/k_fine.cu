@@ -1126,7 +1126,9 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
       cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
-    if (3 * d.nv < ((int64_t)1 << 31) && d.ne < ((int64_t)1 << 31))
+    // (MODE 3 keeps 64-bit offsets: with 32-bit ones it spilled 32 bytes and
+    // ran 122 against 118 us at 256x128x128, where modes 0-2 gained 4-9 us)
+    if (MODE != 3 && 3 * d.nv < ((int64_t)1 << 31) && d.ne < ((int64_t)1 << 31))
       k_fine_modal32<TYE, MODE, true><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
     else
       k_fine_modal32<TYE, MODE, false><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);

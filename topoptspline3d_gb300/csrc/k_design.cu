@@ -270,38 +270,20 @@ __global__ void __launch_bounds__(256) k_spline_yz_sep(LevelDims d, SplineDev sp
   }
 }
 
-// Pass 2 one element row (y, z) at a time: the row's pass-1 values B[z][y][:]
-// are staged in shared memory, and the next row's values and activity flags
-// are loaded while this row's elements are evaluated (values as
-// spline_from_B).  Rows of at most ROW_PF * VOL_THREADS elements and basis
-// indices.
-constexpr int ROW_PF = 4;
+// Pass 2 one element row (y, z) at a time, one thread per element column x
+// (the CTA is the row's width rounded up to whole warps): the row's pass-1
+// values B[z][y][:] are staged in shared memory, the next row's values and
+// activity flags are loaded while this row's elements are evaluated, and each
+// thread keeps its column's basis index and weights in registers for all rows
+// (values as spline_from_B).  Rows of at most ROW_MAX elements.
+constexpr int ROW_MAX = 1024;
 
-struct RowStage {
-  float2 b[ROW_PF];
-  uint8_t a[ROW_PF];
-};
-
-__device__ __forceinline__ void row_fetch(RowStage& r, const float2* __restrict__ B, const uint8_t* __restrict__ eactive,
-                                          int nbx, int ex, int row) {
-  const float2* b = B + (int64_t)nbx * row;
-  const uint8_t* ea = eactive + (int64_t)ex * row;
-#pragma unroll
-  for (int q = 0; q < ROW_PF; ++q) {
-    const int i = threadIdx.x + q * VOL_THREADS;
-    r.b[q] = i < nbx ? b[i] : make_float2(0.f, 0.f);
-    r.a[q] = i < ex ? ea[i] : 0;
-  }
-}
-
-__device__ __forceinline__ df row_value(const SplineDev& sp, const float2* sB, int x, bool yz_in) {
-  const int ix = sp.i0[0][x];
-  if (ix < 0 || !yz_in) return df_from(-0.2);
-  const int k = sp.order;
+__device__ __forceinline__ df row_value(const float2* sB, int ix, const df* nx, int k, bool in) {
+  if (!in) return df_from(-0.2);
   df v(0);
   for (int r = 0; r < k; ++r) {
-    const float2 n = sp.Ndf[0][x * k + r], bb = sB[ix + r];
-    v += df(n.x, n.y) * df(bb.x, bb.y);
+    const float2 bb = sB[ix + r];
+    v += nx[r] * df(bb.x, bb.y);
   }
   return v;
 }
@@ -309,63 +291,82 @@ __device__ __forceinline__ df row_value(const SplineDev& sp, const float2* sB, i
 // MODE 0: volume partial sums (clamped values of active elements, per CTA);
 // MODE 1: densities rho, rho^p (FP64 and FP32) of every element.
 template <int MODE>
-__global__ void __launch_bounds__(VOL_THREADS) k_spline_rows(LevelDims d, const uint8_t* __restrict__ eactive,
-                                                             SplineDev sp, const float2* __restrict__ B,
-                                                             double rho_min, double penal,
-                                                             double* __restrict__ partial, double* __restrict__ rho,
-                                                             double* __restrict__ rhop, float* __restrict__ rhop32) {
-  __shared__ float2 sB[ROW_PF * VOL_THREADS];
-  const int nbx = sp.nb[0], ex = d.ex, nrows = d.ey * d.ez;
+__global__ void __launch_bounds__(ROW_MAX) k_spline_rows(LevelDims d, const uint8_t* __restrict__ eactive,
+                                                         SplineDev sp, const float2* __restrict__ B,
+                                                         double rho_min, double penal,
+                                                         double* __restrict__ partial, double* __restrict__ rho,
+                                                         double* __restrict__ rhop, float* __restrict__ rhop32) {
+  extern __shared__ float2 sB[];  // nb0
+  const int nbx = sp.nb[0], ex = d.ex, nrows = d.ey * d.ez, k = sp.order;
+  const int x = threadIdx.x;
+  const bool col = x < ex;
+  // the column's basis index and weights, for every row
+  int ix = -1;
+  df nx[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) nx[r] = df(0);
+  if (col) {
+    ix = sp.i0[0][x];
+    for (int r = 0; r < k; ++r) {
+      const float2 n = sp.Ndf[0][x * k + r];
+      nx[r] = df(n.x, n.y);
+    }
+  }
   const df lo = df_from(rho_min), one(1.f, 0.f);
   df sd(0);
-  RowStage st;
+  float2 pb[4];
+  uint8_t pa = 0;
+  auto fetch = [&](int row) {
+    const float2* b = B + (int64_t)nbx * row;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = x + q * (int)blockDim.x;
+      pb[q] = i < nbx ? b[i] : make_float2(0.f, 0.f);
+    }
+    pa = col ? eactive[x + (int64_t)ex * row] : 0;
+  };
   int row = blockIdx.x;
-  if (row < nrows) row_fetch(st, B, eactive, nbx, ex, row);
+  if (row < nrows) fetch(row);
   for (; row < nrows; row += gridDim.x) {
     __syncthreads();  // the previous row's readers are done with sB
-    uint8_t act[ROW_PF];
 #pragma unroll
-    for (int q = 0; q < ROW_PF; ++q) {
-      const int i = threadIdx.x + q * VOL_THREADS;
-      if (i < nbx) sB[i] = st.b[q];
-      act[q] = st.a[q];
+    for (int q = 0; q < 4; ++q) {
+      const int i = x + q * (int)blockDim.x;
+      if (i < nbx) sB[i] = pb[q];
     }
+    const uint8_t act = pa;
     __syncthreads();
-    if (row + (int)gridDim.x < nrows) row_fetch(st, B, eactive, nbx, ex, row + gridDim.x);
+    if (row + (int)gridDim.x < nrows) fetch(row + gridDim.x);
+    if (!col) continue;
     const int y = row % d.ey, z = row / d.ey;
-    const bool yz_in = sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0;
-#pragma unroll
-    for (int q = 0; q < ROW_PF; ++q) {
-      const int x = threadIdx.x + q * VOL_THREADS;
-      if (x >= ex) continue;
-      if (MODE == 0) {
-        if (!act[q]) continue;
-        df v = row_value(sp, sB, x, yz_in);
-        if (df_lt(v, lo)) v = lo;
-        if (df_lt(one, v)) v = one;
-        sd += v;
-      } else {
-        const int64_t e = x + (int64_t)ex * row;
-        if (!act[q]) {
-          rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
-          continue;
-        }
-        const double v = fmin(fmax(df_to(row_value(sp, sB, x, yz_in)), rho_min), 1.0);
-        const double vp = simp_pow(v, penal);
-        rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
+    const bool in = ix >= 0 && sp.i0[1][y] >= 0 && sp.i0[2][z] >= 0;
+    if (MODE == 0) {
+      if (!act) continue;
+      df v = row_value(sB, ix, nx, k, in);
+      if (df_lt(v, lo)) v = lo;
+      if (df_lt(one, v)) v = one;
+      sd += v;
+    } else {
+      const int64_t e = x + (int64_t)ex * row;
+      if (!act) {
+        rho[e] = 0.0; rhop[e] = 0.0; rhop32[e] = 0.0f;
+        continue;
       }
+      const double v = fmin(fmax(df_to(row_value(sB, ix, nx, k, in)), rho_min), 1.0);
+      const double vp = simp_pow(v, penal);
+      rho[e] = v; rhop[e] = vp; rhop32[e] = (float)vp;
     }
   }
   if (MODE != 0) return;
   double s = df_to(sd);
-  __shared__ double ws[VOL_THREADS / 32];
+  __shared__ double ws[ROW_MAX / 32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     double r = 0.0;
-    for (int w = 0; w < VOL_THREADS / 32; ++w) r += ws[w];
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += ws[w];
     partial[blockIdx.x] = r;
   }
 }
@@ -388,8 +389,12 @@ static bool spline_yz_sep(cudaStream_t s, const LevelDims& d, const SplineDev& s
   return true;
 }
 
+static int rows_threads(const LevelDims& d) { return std::min(ROW_MAX, (d.ex + 31) / 32 * 32); }
+
+// Rows fit the row kernel: at most ROW_MAX elements, a staged row of basis
+// values within 4 per thread, spline order at most 4.
 static bool rows_fit(const LevelDims& d, const SplineDev& sp) {
-  return d.ex <= ROW_PF * VOL_THREADS && sp.nb[0] <= ROW_PF * VOL_THREADS;
+  return d.ex <= ROW_MAX && sp.nb[0] <= 4 * rows_threads(d) && sp.order <= 4;
 }
 
 static int rows_blocks(const LevelDims& d) { return (int)std::min<int64_t>(1024, (int64_t)d.ey * d.ez); }
@@ -407,8 +412,8 @@ void launch_coeff_to_density(cudaStream_t s, const LevelDims& d, const uint8_t* 
   }
   if (!sep) k_spline_yz<<<nblk(nB, 256), 256, 0, s>>>(d, sp, coeff, B);
   if (rows_fit(d, sp))
-    k_spline_rows<1><<<rows_blocks(d), VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, penal, nullptr, rho, rhop,
-                                                            rhop32);
+    k_spline_rows<1><<<rows_blocks(d), rows_threads(d), sizeof(float2) * sp.nb[0], s>>>(
+        d, eactive, sp, B, rho_min, penal, nullptr, rho, rhop, rhop32);
   else
     k_density_from_B<<<nblk(d.ne, 256), 256, 0, s>>>(d, eactive, sp, B, rho_min, penal, rho, rhop, rhop32);
 }
@@ -422,7 +427,8 @@ void launch_trial_volume(cudaStream_t s, const LevelDims& d, const uint8_t* eact
   int nb;
   if (rows_fit(d, sp)) {
     nb = rows_blocks(d);
-    k_spline_rows<0><<<nb, VOL_THREADS, 0, s>>>(d, eactive, sp, B, rho_min, 0.0, partial, nullptr, nullptr, nullptr);
+    k_spline_rows<0><<<nb, rows_threads(d), sizeof(float2) * sp.nb[0], s>>>(d, eactive, sp, B, rho_min, 0.0, partial,
+                                                                           nullptr, nullptr, nullptr);
   } else {  // two elements per thread at most (up to 2048 partials)
     nb = (int)std::min<int64_t>(2048, (d.ne + VOL_THREADS * 2 - 1) / (VOL_THREADS * 2));
     if (nb < 1) nb = 1;

@@ -1118,7 +1118,9 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     A(dalloc(hp, &L.U2, 3 * nv)); A(dalloc(hp, &L.U2_32, 3 * nv));
     if (l > 0) {
       A(dalloc(hp, &L.kel, 576 * ne)); A(dalloc(hp, &L.kel32, 576 * ne));
-      A(dalloc(hp, &L.stencil, 243 * nv)); A(dalloc(hp, &L.stencil32, 243 * nv));
+      A(dalloc(hp, &L.stencil, 243 * nv));
+      // FP32: room for the tiled layout (243 x 32 values per started group of 32 vertices)
+      A(dalloc(hp, &L.stencil32, 243 * ((nv + 31) / 32 * 32)));
     }
     if (rc != TOPO_OK) break;
     std::vector<uint8_t> vm(h->H.vactive[l]);

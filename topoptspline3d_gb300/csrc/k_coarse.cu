@@ -13,31 +13,54 @@ namespace topo {
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// Coarse levels below this vertex count run the warp-per-vertex stencil kernels.
+constexpr int64_t STENCIL_WARP_MAX_NV = 32768;
+
+// Where stencil coefficient q (neighbour k times 9 plus block entry, 0..242) of
+// vertex v lives: base(v) + q * stride().  [243][nv] for FP64 and for the small
+// levels; tiled for the FP32 levels the row kernels serve (vertex count at
+// least STENCIL_WARP_MAX_NV): the 243 x 32 coefficients of each group of 32
+// vertices lie together, so a warp of consecutive vertices reads one
+// contiguous block instead of 243 arrays.  A tiled array holds 243 x 32
+// values per started group of 32 vertices.
+struct StIdx {
+  int64_t nv;
+  bool tiled;
+  __device__ __forceinline__ int64_t base(int64_t v) const { return tiled ? (v >> 5) * (243 * 32) + (v & 31) : v; }
+  __device__ __forceinline__ int64_t stride() const { return tiled ? 32 : nv; }
+};
+
+template <typename T>
+StIdx st_idx(const LevelDims& d) {
+  return StIdx{d.nv, sizeof(T) == 4 && d.nv >= STENCIL_WARP_MAX_NV};
+}
+
 // ---------------------------------------------------------------------------
 // Stencil apply: y_v = sum_d S(v,d) u_{v+d}  (grid/Grid.cu:2126-2224 residual form).
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ __forceinline__ void stencil_row(const LevelDims& d, const T* __restrict__ st,
+__device__ __forceinline__ void stencil_row(const LevelDims& d, const T* __restrict__ st, StIdx si,
                                             const T* __restrict__ u, int x, int y, int z, int64_t v,
                                             T o[3]) {
   o[0] = o[1] = o[2] = T(0);
-  const int64_t nv = d.nv;
+  const int64_t nv = d.nv, ss = si.stride();
+  const T* sb = st + si.base(v);
 #pragma unroll
   for (int k = 0; k < 27; ++k) {
     const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
     if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) continue;
     const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
     const T u0 = u[n], u1 = u[nv + n], u2 = u[2 * nv + n];
-    const T* s = st + (int64_t)(k * 9) * nv + v;
-    o[0] += s[0] * u0 + s[nv] * u1 + s[2 * nv] * u2;
-    o[1] += s[3 * nv] * u0 + s[4 * nv] * u1 + s[5 * nv] * u2;
-    o[2] += s[6 * nv] * u0 + s[7 * nv] * u1 + s[8 * nv] * u2;
+    const T* s = sb + (int64_t)(k * 9) * ss;
+    o[0] += s[0] * u0 + s[ss] * u1 + s[2 * ss] * u2;
+    o[1] += s[3 * ss] * u0 + s[4 * ss] * u1 + s[5 * ss] * u2;
+    o[2] += s[6 * ss] * u0 + s[7 * ss] * u1 + s[8 * ss] * u2;
   }
 }
 
 
 template <typename T>
-__global__ void k_stencil_gs(LevelDims d, const T* __restrict__ st, const uint8_t* __restrict__ vmask,
+__global__ void k_stencil_gs(LevelDims d, const T* __restrict__ st, StIdx si, const uint8_t* __restrict__ vmask,
                              T* u, const T* __restrict__ f, int cx, int cy, int cz, int hx, int hy,
                              int64_t cnt, bool reverse) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,9 +71,9 @@ __global__ void k_stencil_gs(LevelDims d, const T* __restrict__ st, const uint8_
   const int64_t v = x + (int64_t)d.vx * (y + (int64_t)d.vy * z);
   if (!(vmask[v] & 8)) return;
   T o[3], S[9], r[3];
-  stencil_row<T>(d, st, u, x, y, z, v, o);
+  stencil_row<T>(d, st, si, u, x, y, z, v, o);
 #pragma unroll
-  for (int k = 0; k < 9; ++k) S[k] = st[(int64_t)(13 * 9 + k) * d.nv + v];
+  for (int k = 0; k < 9; ++k) S[k] = st[si.base(v) + (int64_t)(13 * 9 + k) * si.stride()];
 #pragma unroll
   for (int c = 0; c < 3; ++c) r[c] = f[c * d.nv + v] - o[c];
   T du[3] = {T(0), T(0), T(0)};
@@ -76,13 +99,13 @@ __global__ void k_stencil_gs(LevelDims d, const T* __restrict__ st, const uint8_
 }
 
 template <typename T>
-__global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st,
+__global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st, StIdx si,
                                    const uint8_t* __restrict__ vmask, T* __restrict__ dinv) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= d.nv) return;
   T S[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) S[k] = st[(int64_t)(13 * 9 + k) * d.nv + v];
+  for (int k = 0; k < 9; ++k) S[k] = st[si.base(v) + (int64_t)(13 * 9 + k) * si.stride()];
   const T a = S[0], b = S[1], c = S[2], dd = S[4], e = S[5], f = S[8];
   const T A0 = dd * f - e * e, A1 = c * e - b * f, A2 = b * e - c * dd;
   const T det = a * A0 + b * A1 + c * A2;
@@ -100,23 +123,24 @@ __global__ void k_stencil_diag_inv(LevelDims d, const T* __restrict__ st,
 constexpr int SV = 64;
 
 template <typename T>
-__device__ __forceinline__ T stencil_row_i(const LevelDims& d, const T* __restrict__ st, const T* __restrict__ u,
-                                           int x, int y, int z, int64_t v, int row) {
+__device__ __forceinline__ T stencil_row_i(const LevelDims& d, const T* __restrict__ st, StIdx si,
+                                           const T* __restrict__ u, int x, int y, int z, int64_t v, int row) {
   T o = T(0);
-  const int64_t nv = d.nv;
+  const int64_t nv = d.nv, ss = si.stride();
+  const T* sb = st + si.base(v);
 #pragma unroll
   for (int k = 0; k < 27; ++k) {
     const int nx = x + k % 3 - 1, ny = y + k / 3 % 3 - 1, nz = z + k / 9 - 1;
     if (nx < 0 || ny < 0 || nz < 0 || nx >= d.vx || ny >= d.vy || nz >= d.vz) continue;
     const int64_t n = nx + (int64_t)d.vx * (ny + (int64_t)d.vy * nz);
-    const T* s = st + (int64_t)(k * 9 + 3 * row) * nv + v;
-    o += s[0] * u[n] + s[nv] * u[nv + n] + s[2 * nv] * u[2 * nv + n];
+    const T* s = sb + (int64_t)(k * 9 + 3 * row) * ss;
+    o += s[0] * u[n] + s[ss] * u[nv + n] + s[2 * ss] * u[2 * nv + n];
   }
   return o;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st,
+__global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st, StIdx si,
                                                            const T* __restrict__ u, const T* __restrict__ f,
                                                            T* __restrict__ out, bool residual) {
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
@@ -129,14 +153,14 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T*
   const int x = (int)(v % d.vx);
   const int64_t t = v / d.vx;
   const int y = (int)(t % d.vy), z = (int)(t / d.vy);
-  const T o = stencil_row_i<T>(d, st, u, x, y, z, v, row);
+  const T o = stencil_row_i<T>(d, st, si, u, x, y, z, v, row);
   const int64_t i = row * d.nv + v;
   out[i] = residual ? f[i] - o : o;
 }
 
 // One Chebyshev step on a stencil level: uout = u + d, d = c_old d + c_new Dinv (f - A u).
 template <typename T>
-__global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* __restrict__ st,
+__global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* __restrict__ st, StIdx si,
                                                          const T* __restrict__ u, const T* __restrict__ f,
                                                          T* __restrict__ uout, const T* __restrict__ dinv,
                                                          T* __restrict__ dv, const double* __restrict__ coef,
@@ -155,7 +179,7 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* _
     const int x = (int)(v % d.vx);
     const int64_t t = v / d.vx;
     const int y = (int)(t % d.vy), z = (int)(t / d.vy);
-    sr[row][lv] = f[row * nv + v] - stencil_row_i<T>(d, st, u, x, y, z, v, row);
+    sr[row][lv] = f[row * nv + v] - stencil_row_i<T>(d, st, si, u, x, y, z, v, row);
   }
   __syncthreads();
   if (!ok) return;
@@ -250,7 +274,6 @@ __global__ void __launch_bounds__(32 * WV) k_stencil_cheb_warp(LevelDims d, cons
 }
 
 // Levels with fewer vertices than this use the warp-per-vertex kernels.
-constexpr int64_t STENCIL_WARP_MAX_NV = 32768;
 
 template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
@@ -258,7 +281,7 @@ void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const
   if (d.nv < STENCIL_WARP_MAX_NV)
     k_stencil_apply_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, out, residual);
   else
-    k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, out, residual);
+    k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, st_idx<T>(d), u, f, out, residual);
 }
 
 template <typename T>
@@ -267,7 +290,8 @@ void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const 
   if (d.nv < STENCIL_WARP_MAX_NV)
     k_stencil_cheb_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
   else
-    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
+    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, st_idx<T>(d), u, f, uout, dinv, dvec, coef,
+                                                                  first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,
@@ -320,13 +344,13 @@ void launch_stencil_gs(cudaStream_t s, const LevelDims& d, const T* st, const ui
   const int hx = (d.vx - cx + 1) / 2, hy = (d.vy - cy + 1) / 2, hz = (d.vz - cz + 1) / 2;
   const int64_t cnt = (int64_t)hx * hy * hz;
   if (cnt <= 0) return;
-  k_stencil_gs<T><<<nblk(cnt, 128), 128, 0, s>>>(d, st, vmask, u, f, cx, cy, cz, hx, hy, cnt, reverse);
+  k_stencil_gs<T><<<nblk(cnt, 128), 128, 0, s>>>(d, st, st_idx<T>(d), vmask, u, f, cx, cy, cz, hx, hy, cnt, reverse);
 }
 
 template <typename T>
 void launch_stencil_diag_inv(cudaStream_t s, const LevelDims& d, const T* st, const uint8_t* vmask,
                              T* dinv) {
-  k_stencil_diag_inv<T><<<nblk(d.nv, 256), 256, 0, s>>>(d, st, vmask, dinv);
+  k_stencil_diag_inv<T><<<nblk(d.nv, 256), 256, 0, s>>>(d, st, st_idx<T>(d), vmask, dinv);
 }
 
 // ---------------------------------------------------------------------------
@@ -747,7 +771,7 @@ __global__ void __launch_bounds__(576) k_galerkin_dyadic(LevelDims fd, LevelDims
 template <typename T>
 __global__ void k_assemble_stencil(LevelDims d, const uint8_t* __restrict__ eactive,
                                    const uint8_t* __restrict__ vmask, const T* __restrict__ kel,
-                                   T* __restrict__ st) {
+                                   T* __restrict__ st, StIdx si) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= 27 * d.nv) return;
   const int k = (int)(gid / d.nv);
@@ -787,7 +811,7 @@ __global__ void k_assemble_stencil(LevelDims d, const uint8_t* __restrict__ eact
     blk[0] = T(1); blk[4] = T(1); blk[8] = T(1);
   }
 #pragma unroll
-  for (int q = 0; q < 9; ++q) st[(int64_t)(k * 9 + q) * d.nv + v] = blk[q];
+  for (int q = 0; q < 9; ++q) st[si.base(v) + (int64_t)(k * 9 + q) * si.stride()] = blk[q];
 }
 
 __global__ void k_dense_from_stencil(LevelDims d, const double* __restrict__ st,
@@ -1086,7 +1110,7 @@ void launch_galerkin_dyadic_t(cudaStream_t s, const LevelDims& fd, const LevelDi
 template <typename T>
 void launch_assemble_stencil_t(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                                const uint8_t* vmask, const T* kel, T* st) {
-  k_assemble_stencil<T><<<nblk(27 * d.nv, 256), 256, 0, s>>>(d, eactive, vmask, kel, st);
+  k_assemble_stencil<T><<<nblk(27 * d.nv, 256), 256, 0, s>>>(d, eactive, vmask, kel, st, st_idx<T>(d));
 }
 
 void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double* st, double* A) {

@@ -34,7 +34,7 @@ struct DevLevel {
   double* kel = nullptr;        // coarse: FP64 element matrices [ne][576]
   float* kel32 = nullptr;       // coarse: FP32 element matrices [ne][576]
   double* stencil = nullptr;    // coarse: FP64 [243][nv]
-  float* stencil32 = nullptr;   // coarse: FP32 [243][nv]
+  float* stencil32 = nullptr;   // coarse: FP32 [243][nv], tiled on levels of 32,768 vertices or more (StIdx)
   double* dinv = nullptr;       // FP64 inverse diagonal blocks [9][nv] (Chebyshev)
   float* dinv32 = nullptr;      // FP32 inverse diagonal blocks [9][nv]; level 0: packed symmetric (float4 d00 d01 d02 d11 [nv], float2 d12 d22 [nv])
   double* cd = nullptr;         // FP64 Chebyshev direction [3nv]

@@ -95,102 +95,11 @@ __device__ __forceinline__ void wht_bwd(T v[8]) {
       }
 }
 
-// One component's transform in FP32 with its first two stages in packed
-// two-lane instructions: the values sit as (v0, v4), (v1, v5), (v2, v6),
-// (v3, v7), so the butterflies of the stages across bits 0 and 1 pair up lane
-// for lane; the stage across bit 2 works within each pair.  Same stages in the
-// same order as wht_fwd / wht_bwd, same results.
-__device__ __forceinline__ void wht_fwd_packed(float v[8]) {
-  const float2 m1 = make_float2(-1.f, -1.f);
-  float2 P[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) P[i] = make_float2(v[i], v[i + 4]);
-#pragma unroll
-  for (int hb = 1; hb < 4; hb <<= 1)
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if (!(i & hb)) {
-        const float2 a = P[i], b = P[i | hb];
-        P[i] = __fadd2_rn(a, b);
-        P[i | hb] = __ffma2_rn(a, m1, b);  // b - a
-      }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    v[i] = P[i].x + P[i].y;
-    v[i + 4] = P[i].y - P[i].x;
-  }
-}
-__device__ __forceinline__ void wht_bwd_packed(float v[8]) {
-  const float2 m1 = make_float2(-1.f, -1.f);
-  float2 P[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) P[i] = make_float2(v[i], v[i + 4]);
-#pragma unroll
-  for (int hb = 1; hb < 4; hb <<= 1)
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if (!(i & hb)) {
-        const float2 a = P[i], b = P[i | hb];
-        P[i] = __ffma2_rn(b, m1, a);  // a - b
-        P[i | hb] = __fadd2_rn(a, b);
-      }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    v[i] = P[i].x - P[i].y;
-    v[i + 4] = P[i].x + P[i].y;
-  }
-}
-
-// The same in double-float with packed df2 pairs.
-__device__ __forceinline__ df2 df2_pair(df a, df b) {
-  return {make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)};
-}
-__device__ __forceinline__ void wht_fwd_packed(df v[8]) {
-  df2 P[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) P[i] = df2_pair(v[i], v[i + 4]);
-#pragma unroll
-  for (int hb = 1; hb < 4; hb <<= 1)
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if (!(i & hb)) {
-        const df2 a = P[i], b = P[i | hb];
-        P[i] = df2_add(a, b);
-        P[i | hb] = df2_add(b, df2_neg(a));  // b - a
-      }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const df a(P[i].hi.x, P[i].lo.x), b(P[i].hi.y, P[i].lo.y);
-    v[i] = a + b;
-    v[i + 4] = b - a;
-  }
-}
-__device__ __forceinline__ void wht_bwd_packed(df v[8]) {
-  df2 P[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) P[i] = df2_pair(v[i], v[i + 4]);
-#pragma unroll
-  for (int hb = 1; hb < 4; hb <<= 1)
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-      if (!(i & hb)) {
-        const df2 a = P[i], b = P[i | hb];
-        P[i] = df2_add(a, df2_neg(b));  // a - b
-        P[i | hb] = df2_add(a, b);
-      }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const df a(P[i].hi.x, P[i].lo.x), b(P[i].hi.y, P[i].lo.y);
-    v[i] = a - b;
-    v[i + 4] = a + b;
-  }
-}
-
 // The transforms of the three displacement components.  FP32: components 0
 // and 1 go through the packed two-lane FP32 instructions of sm_100 and later
 // (__fadd2_rn, __ffma2_rn; per lane the same rounding as the scalar forms, so
 // the results are identical), which halves their instruction count in an
-// issue-bound kernel; component 2 pairs its own butterflies (wht_fwd_packed).
+// issue-bound kernel.
 template <typename T>
 __device__ __forceinline__ void wht3_fwd(T c[3][8]) {
   wht_fwd<T>(c[0]); wht_fwd<T>(c[1]); wht_fwd<T>(c[2]);
@@ -216,7 +125,7 @@ __device__ __forceinline__ void wht3_fwd<float>(float c[3][8]) {
       }
 #pragma unroll
   for (int a = 0; a < 8; ++a) { c[0][a] = p[a].x; c[1][a] = p[a].y; }
-  wht_fwd_packed(c[2]);
+  wht_fwd<float>(c[2]);
 }
 template <>
 __device__ __forceinline__ void wht3_bwd<float>(float g[3][8]) {
@@ -235,7 +144,7 @@ __device__ __forceinline__ void wht3_bwd<float>(float g[3][8]) {
       }
 #pragma unroll
   for (int a = 0; a < 8; ++a) { g[0][a] = p[a].x; g[1][a] = p[a].y; }
-  wht_bwd_packed(g[2]);
+  wht_bwd<float>(g[2]);
 }
 
 // Double-float: components 0 and 1 in the lanes of df2.
@@ -259,7 +168,7 @@ __device__ __forceinline__ void wht3_fwd<df>(df c[3][8]) {
     c[0][a] = df(p[a].hi.x, p[a].lo.x);
     c[1][a] = df(p[a].hi.y, p[a].lo.y);
   }
-  wht_fwd_packed(c[2]);
+  wht_fwd<df>(c[2]);
 }
 template <>
 __device__ __forceinline__ void wht3_bwd<df>(df g[3][8]) {
@@ -281,7 +190,7 @@ __device__ __forceinline__ void wht3_bwd<df>(df g[3][8]) {
     g[0][a] = df(p[a].hi.x, p[a].lo.x);
     g[1][a] = df(p[a].hi.y, p[a].lo.y);
   }
-  wht_bwd_packed(g[2]);
+  wht_bwd<df>(g[2]);
 }
 
 // In: c[3][8] nodal values per component.  Out: c[3][8] nodal forces of pe*Ke*u.

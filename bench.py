@@ -518,11 +518,11 @@ def main():
     fams = {capi.K_FINE_APPLY64: ("k_fine_modal_df (FP64 K.u in double-float, outer CG)",
                                   nv * (24 + 24 + 1) + ne * 8, ne * 240.0),
             # u in, f in, d out, u out (FP32 x3 each), vertex mask, the stored 3x3
-            # block-Jacobi inverse (FP32 x9), rho^p; d is read by one step in three
+            # block-Jacobi inverse (FP32, 6 of the symmetric 3x3), rho^p; d is read by one step in three
             # (a V(1,1) degree-2 cycle's pre-smoothing second step takes d from u,
             # the post-smoothing first step starts it)
             capi.K_FINE_SMOOTH32: ("k_fine_modal32<8,2|3> (FP32 Chebyshev step)",
-                                   nv * (12 + 12 + 12 + 12 + 12 / 3 + 1 + 36) + ne * 4, ne * 240.0 + nv * 30.0),
+                                   nv * (12 + 12 + 12 + 12 + 12 / 3 + 1 + 24) + ne * 4, ne * 240.0 + nv * 30.0),
             capi.K_FINE_APPLY32: ("k_fine_modal32<8,0|1> (FP32 K.u, residual)", nv * (12 + 12 + 1) + ne * 4,
                                   ne * 240.0),
             capi.K_FINE_SMOOTH64: ("k_fine_gs<double>", nv * (24 + 24 + 24 + 1) + ne * 8, nv * 1170.0)}
@@ -538,7 +538,9 @@ def main():
     peak_note = "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else "fallback 6800 GB/s"
     hbm_peak = hbm_peak or 6800.0
     achieved = bytes_per / avg_s / 1e9
-    traffic = load_traffic().get(name.split(" ")[0])
+    # (the ncu traffic figure is for the 256x128x128 half-MBB launch)
+    traffic = (load_traffic().get(name.split(" ")[0])
+               if args.case == "mbb" and args.size == "256x128x128" else None)
     roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "peak_source": peak_note,
             "traffic": traffic, "launches": nl, "avg_launch_ms": avg_s * 1e3,

@@ -143,7 +143,6 @@ template <typename T>
 __global__ void __launch_bounds__(3 * SV) k_stencil_apply3(LevelDims d, const T* __restrict__ st, StIdx si,
                                                            const T* __restrict__ u, const T* __restrict__ f,
                                                            T* __restrict__ out, bool residual) {
-  pdl_wait();
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
   if (f) f += bo;
@@ -166,7 +165,6 @@ __global__ void __launch_bounds__(3 * SV) k_stencil_cheb(LevelDims d, const T* _
                                                          T* __restrict__ uout, const T* __restrict__ dinv,
                                                          T* __restrict__ dv, const double* __restrict__ coef,
                                                          bool first) {
-  pdl_wait();
   __shared__ T sr[3][SV];
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
@@ -230,7 +228,6 @@ template <typename T>
 __global__ void __launch_bounds__(32 * WV) k_stencil_apply_warp(LevelDims d, const T* __restrict__ st,
                                                                 const T* __restrict__ u, const T* __restrict__ f,
                                                                 T* __restrict__ out, bool residual) {
-  pdl_wait();
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
   if (f) f += bo;
@@ -253,7 +250,6 @@ __global__ void __launch_bounds__(32 * WV) k_stencil_cheb_warp(LevelDims d, cons
                                                                T* __restrict__ uout, const T* __restrict__ dinv,
                                                                T* __restrict__ dv, const double* __restrict__ coef,
                                                                bool first) {
-  pdl_wait();
   const int64_t bo = (int64_t)blockIdx.y * 3 * d.nv;  // right-hand side of the batch
   u += bo;
   f += bo;
@@ -283,21 +279,19 @@ template <typename T>
 void launch_stencil_apply(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f,
                           T* out, bool residual, int nb) {
   if (d.nv < STENCIL_WARP_MAX_NV)
-    launch_pdl(k_stencil_apply_warp<T>, dim3(nblk(d.nv, WV), nb), dim3(32 * WV), 0, s, d, st, u, f, out, residual);
+    k_stencil_apply_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, out, residual);
   else
-    launch_pdl(k_stencil_apply3<T>, dim3(nblk(d.nv, SV), nb), dim3(3 * SV), 0, s, d, st, st_idx<T>(d), u, f, out,
-               residual);
+    k_stencil_apply3<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, st_idx<T>(d), u, f, out, residual);
 }
 
 template <typename T>
 void launch_stencil_cheb(cudaStream_t s, const LevelDims& d, const T* st, const T* u, const T* f, T* uout,
                          const T* dinv, T* dvec, const double* coef, bool first, int nb) {
   if (d.nv < STENCIL_WARP_MAX_NV)
-    launch_pdl(k_stencil_cheb_warp<T>, dim3(nblk(d.nv, WV), nb), dim3(32 * WV), 0, s, d, st, u, f, uout, dinv, dvec,
-               coef, first);
+    k_stencil_cheb_warp<T><<<dim3(nblk(d.nv, WV), nb), 32 * WV, 0, s>>>(d, st, u, f, uout, dinv, dvec, coef, first);
   else
-    launch_pdl(k_stencil_cheb<T>, dim3(nblk(d.nv, SV), nb), dim3(3 * SV), 0, s, d, st, st_idx<T>(d), u, f, uout, dinv,
-               dvec, coef, first);
+    k_stencil_cheb<T><<<dim3(nblk(d.nv, SV), nb), 3 * SV, 0, s>>>(d, st, st_idx<T>(d), u, f, uout, dinv, dvec, coef,
+                                                                  first);
 }
 
 template void launch_stencil_cheb<double>(cudaStream_t, const LevelDims&, const double*, const double*,
@@ -312,7 +306,6 @@ template <typename T>
 __global__ void k_cheb_zero_stored(int64_t nv, const uint8_t* __restrict__ vmask, const T* __restrict__ dinv,
                                    const T* __restrict__ f, T* __restrict__ dv, T* __restrict__ uout,
                                    const double* __restrict__ coef) {
-  pdl_wait();
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   const int64_t bo = (int64_t)blockIdx.y * 3 * nv;
@@ -336,7 +329,7 @@ __global__ void k_cheb_zero_stored(int64_t nv, const uint8_t* __restrict__ vmask
 template <typename T>
 void launch_cheb_zero_stored(cudaStream_t s, int64_t nv, const uint8_t* vmask, const T* dinv, const T* f, T* dvec,
                              T* uout, const double* coef, int nb) {
-  launch_pdl(k_cheb_zero_stored<T>, dim3(nblk(nv, 256), nb), dim3(256), 0, s, nv, vmask, dinv, f, dvec, uout, coef);
+  k_cheb_zero_stored<T><<<dim3(nblk(nv, 256), nb), 256, 0, s>>>(nv, vmask, dinv, f, dvec, uout, coef);
 }
 
 template void launch_cheb_zero_stored<double>(cudaStream_t, int64_t, const uint8_t*, const double*, const double*,
@@ -367,7 +360,6 @@ void launch_stencil_diag_inv(cudaStream_t s, const LevelDims& d, const T* st, co
 // ---------------------------------------------------------------------------
 template <typename T, int FCT>
 __global__ void k_restrict(LevelDims fd, LevelDims cd, const T* __restrict__ rf, T* __restrict__ fc) {
-  pdl_wait();
   rf += (int64_t)blockIdx.y * 3 * fd.nv;  // right-hand side of the batch
   fc += (int64_t)blockIdx.y * 3 * cd.nv;
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -410,7 +402,6 @@ constexpr int R4_WARPS = 7;
 template <typename T>
 __global__ void __launch_bounds__(32 * R4_WARPS) k_restrict4(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
                                                              T* __restrict__ fc) {
-  pdl_wait();
   __shared__ T part[R4_WARPS][3][32];
   rf += (int64_t)blockIdx.y * 3 * fd.nv;  // right-hand side of the batch
   fc += (int64_t)blockIdx.y * 3 * cd.nv;
@@ -461,7 +452,6 @@ __global__ void __launch_bounds__(32 * R4_WARPS) k_restrict4(LevelDims fd, Level
 template <typename T, int FCT>
 __global__ void k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc, T* __restrict__ uf,
                           const uint8_t* __restrict__ vmask) {
-  pdl_wait();
   uc += (int64_t)blockIdx.y * 3 * cd.nv;  // right-hand side of the batch
   uf += (int64_t)blockIdx.y * 3 * fd.nv;
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -505,9 +495,9 @@ template <typename T>
 void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
                      T* fc, int nb) {
   if (coarse.factor == 4) {
-    launch_pdl(k_restrict4<T>, dim3(nblk(coarse.nv, 32), nb), dim3(32 * R4_WARPS), 0, s, fine, coarse, rf, fc);
+    k_restrict4<T><<<dim3(nblk(coarse.nv, 32), nb), 32 * R4_WARPS, 0, s>>>(fine, coarse, rf, fc);
   } else {
-    launch_pdl(k_restrict<T, 2>, dim3(nblk(coarse.nv, 128), nb), dim3(128), 0, s, fine, coarse, rf, fc);
+    k_restrict<T, 2><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
   }
 }
 
@@ -517,7 +507,6 @@ void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coa
 template <typename T>
 __global__ void __launch_bounds__(256) k_prolong4x(LevelDims fd, LevelDims cd, const T* __restrict__ uc,
                                                    T* __restrict__ uf, const uint8_t* __restrict__ vmask) {
-  pdl_wait();
   uc += (int64_t)blockIdx.y * 3 * cd.nv;  // right-hand side of the batch
   uf += (int64_t)blockIdx.y * 3 * fd.nv;
   const int nqx = (fd.vx + 3) / 4;  // 4-vertex groups per fine row
@@ -577,9 +566,9 @@ void launch_prolong(cudaStream_t s, const LevelDims& fine, const LevelDims& coar
                     T* uf, const uint8_t* vmask_fine, int nb) {
   if (coarse.factor == 4) {
     const int64_t nq = (int64_t)((fine.vx + 3) / 4) * fine.vy * fine.vz;
-    launch_pdl(k_prolong4x<T>, dim3(nblk(nq, 256), nb), dim3(256), 0, s, fine, coarse, uc, uf, vmask_fine);
+    k_prolong4x<T><<<dim3(nblk(nq, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
   } else
-    launch_pdl(k_prolong<T, 2>, dim3(nblk(fine.nv, 256), nb), dim3(256), 0, s, fine, coarse, uc, uf, vmask_fine);
+    k_prolong<T, 2><<<dim3(nblk(fine.nv, 256), nb), 256, 0, s>>>(fine, coarse, uc, uf, vmask_fine);
 }
 
 // ---------------------------------------------------------------------------
@@ -1074,7 +1063,6 @@ __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, 
 template <typename T>
 __global__ void k_dense_gemv(int n, const T* __restrict__ Ainv, const T* __restrict__ f, T* __restrict__ u,
                              int64_t nv) {
-  pdl_wait();
   f += (int64_t)blockIdx.y * 3 * nv;  // right-hand side of the batch
   u += (int64_t)blockIdx.y * 3 * nv;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -1165,7 +1153,7 @@ void launch_to_float(cudaStream_t s, const double* a, float* b, int64_t n) {
 
 template <typename T>
 void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* u_soa, int64_t nv, int nb) {
-  launch_pdl(k_dense_gemv<T>, dim3(nblk((int64_t)n * 32, 256), nb), dim3(256), 0, s, n, Ainv, f_soa, u_soa, nv);
+  k_dense_gemv<T><<<dim3(nblk((int64_t)n * 32, 256), nb), 256, 0, s>>>(n, Ainv, f_soa, u_soa, nv);
 }
 
 template void launch_stencil_apply<double>(cudaStream_t, const LevelDims&, const double*, const double*,

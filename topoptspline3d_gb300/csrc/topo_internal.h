@@ -6,7 +6,6 @@
 
 #include <atomic>
 #include <string>
-#include <utility>
 #include <vector>
 
 #include "../../include/topo_gb300.h"
@@ -16,37 +15,6 @@ namespace topo {
 // Process-wide count of kernel launches issued by this library.
 extern std::atomic<long long> g_launches;
 inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
-
-// Programmatic dependent launch: the kernel may be scheduled while the kernel
-// before it on the stream drains (inside a graph the dependency becomes a
-// programmatic edge).  Every kernel launched this way calls pdl_wait() before
-// any access to global memory, which waits for the previous kernel to finish
-// and its writes to be visible, so results are those of a plain launch; what
-// overlaps is the launch and the scheduling of the new grid.
-template <typename... ExpTypes, typename... ActTypes>
-inline void launch_pdl(void (*kernel)(ExpTypes...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                       ActTypes&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr;
-  attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr.val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = &attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, std::forward<ActTypes>(args)...);
-}
-#ifdef __CUDACC__
-// Waits for the previous grid, then lets the next one be launched: its blocks
-// may be scheduled once every block of this grid has passed this point (so
-// none of this grid's blocks can be kept from running), and they wait in turn.
-__device__ __forceinline__ void pdl_wait() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-#endif
 
 // Dense grid level.  Element/vertex numbering is lexicographic (x fastest).
 struct LevelDims {

@@ -2145,18 +2145,35 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
   double bt = 1e30;
   int rc0 = run(*base, &r.base_ms);
   if (rc0 == TOPO_OK) bt = r.base_ms;
+  // FP32 inner iterations x V(s,s) x Chebyshev degree x lower end of the
+  // Chebyshev interval (the base's, and 0.1 lambda_max: on the 256x128x128
+  // half-MBB beam the lower end 0.1 took 19 V-cycles per solve where 0.3 took 23)
   const int inners[4] = {1, 2, 4, 6};
+  const double base_lo = base->cheb_lo > 0 ? base->cheb_lo : ChebParams{}.lo;
+  const double los[2] = {base_lo, 0.1};
+  const int nlo = base_lo == 0.1 ? 1 : 2;
   for (int ii = 0; ii < 4; ++ii)
     for (int sm = 1; sm <= 2; ++sm)
-      for (int deg = 2; deg <= 3; ++deg) {
-        topo_solve_opts o = *base;
-        o.inner_max = inners[ii];
-        o.pre = o.post = sm;
-        o.cheb_degree = deg;
-        double ms = 0;
-        ++r.candidates;
-        if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
-      }
+      for (int deg = 2; deg <= 3; ++deg)
+        for (int il = 0; il < nlo; ++il) {
+          topo_solve_opts o = *base;
+          o.inner_max = inners[ii];
+          o.pre = o.post = sm;
+          o.cheb_degree = deg;
+          o.cheb_lo = los[il];
+          double ms = 0;
+          ++r.candidates;
+          if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+        }
+  // ---- stage 3: the lower end of the interval around the best schedule's
+  for (const double lo : {0.05, 0.2}) {
+    if (lo == best->cheb_lo) continue;
+    topo_solve_opts o = *best;
+    o.cheb_lo = lo;
+    double ms = 0;
+    ++r.candidates;
+    if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+  }
   r.best_ms = bt;
   cudaMemcpyAsync(L0.U, u0, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream);
   CK(cudaEventRecord(t1, h->stream));

@@ -57,8 +57,9 @@ def parse():
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run exactly one mixed design iteration and exit (for ncu captures)")
     ap.add_argument("--schedule", default=None,
-                    help="inner,pre,degree,tz32,tz64: use this mixed-solver schedule and these tiles instead of "
-                         "autotuning (e.g. the values an earlier run's autotune chose)")
+                    help="inner,pre,degree,tz32,tz64[,lo]: use this mixed-solver schedule (lo: lower end of the "
+                         "Chebyshev interval, a fraction of lambda_max) and these tiles instead of autotuning (e.g. "
+                         "the values an earlier run's autotune chose)")
     ap.add_argument("--profile-solve-steps", type=int, default=0,
                     help="with --profile-iteration: stop the solve after this many outer CG steps")
     ap.add_argument("--no-graphs", action="store_true",
@@ -432,8 +433,11 @@ def main():
     if args.no_graphs:
         p.set_graphs(0)
     if args.schedule:
-        inner, pre, deg, tz32, tz64 = (int(v) for v in args.schedule.split(","))
+        sched = args.schedule.split(",")
+        inner, pre, deg, tz32, tz64 = (int(v) for v in sched[:5])
         opts.update(inner_max=inner, pre=pre, post=pre, cheb_degree=deg)
+        if len(sched) > 5:
+            opts["cheb_lo"] = float(sched[5])
         p.set_tiles(tz32, tz64)
         args.no_autotune = True
     if args.profile_iteration:
@@ -578,7 +582,9 @@ def main():
                       "lattice": [q + wl.order for q in wl.partition],
                       "solver": f"FP64 flexible CG (fine matvec in double-float, ~1e-14 of FP64) + "
                                 f"{opts['inner_max']} FP32 CG its with {args.smoother} V({opts['pre']},"
-                                f"{opts['post']}) degree-{opts['cheb_degree']} multigrid, rel-res 1e-6",
+                                f"{opts['post']}) degree-{opts['cheb_degree']} on "
+                                f"[{opts.get('cheb_lo', 0.3):g}, {opts.get('cheb_hi', 1.1):g}] lambda_max multigrid, "
+                                f"rel-res 1e-6",
                       "autotune": tune,
                       "l2": "working set (>2 GB) larger than L2; no flush",
                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},

@@ -821,12 +821,15 @@ def mma_design_iteration(p, mma, vfrac, dvol_ptr=None, solve=None, filter_radius
 
 def design_batch(problems, iterations, threads=None, solve=None, ocs=None, filter_radius=2.0):
     """topo_design_batch: `iterations` design iterations on every problem, from
-    `threads` host threads (default: one per problem).  ocs: one OC dict per
-    problem (or None).  Returns (per-problem last-iteration stats, batch stats)."""
+    `threads` host threads (default: one per problem).  solve: one solve-options
+    dict for all, or a list with one per problem; ocs: one OC dict per problem
+    (or None).  Returns (per-problem last-iteration stats, batch stats)."""
     lib = load()
     n = len(problems)
     hs = (C.c_void_p * n)(*[p.h for p in problems])
-    opts = (IterOpts * n)(*[Problem.iter_opts(solve, (ocs[k] if ocs else None), filter_radius) for k in range(n)])
+    solves = list(solve) if isinstance(solve, (list, tuple)) else [solve] * n
+    opts = (IterOpts * n)(*[Problem.iter_opts(solves[k], (ocs[k] if ocs else None), filter_radius)
+                            for k in range(n)])
     last = (IterStats * n)()
     bs = BatchStats()
     rc = lib.topo_design_batch(hs, n, opts, n, iterations, threads or n, last, C.byref(bs))

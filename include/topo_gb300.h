@@ -392,8 +392,9 @@ int topo_design_batch(topo_handle** handles, int n, const topo_iter_opts* opts, 
  * 5 launches each) and keeps the fastest for the handle.  Stage 2 solves from the
  * current U with each candidate schedule of the mixed solver (FP32 inner
  * iterations 1, 2, 4, 6 x smoothing steps 1, 2 x Chebyshev degree 2, 3 x lower
- * end of the Chebyshev interval base->cheb_lo, 0.1), stage 3 tries the lower
- * ends 0.05 and 0.2 with the best schedule, and the fastest that converges is
+ * end of the Chebyshev interval base->cheb_lo, 0.1 x inner tolerance
+ * base->inner_rtol, 0.03), stage 3 tries the lower ends 0.05 and 0.2 with the
+ * best schedule, and the fastest that converges is
  * written into *best (other fields from *base, which must be TOPO_SOLVE_MIXED
  * with the Chebyshev smoother).  U is restored. */
 typedef struct topo_tune_report {

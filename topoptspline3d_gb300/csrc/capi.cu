@@ -2146,25 +2146,30 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
   int rc0 = run(*base, &r.base_ms);
   if (rc0 == TOPO_OK) bt = r.base_ms;
   // FP32 inner iterations x V(s,s) x Chebyshev degree x lower end of the
-  // Chebyshev interval (the base's, and 0.1 lambda_max: on the 256x128x128
-  // half-MBB beam the lower end 0.1 took 19 V-cycles per solve where 0.3 took 23)
+  // Chebyshev interval (the base's, and 0.1 lambda_max) x inner tolerance (the
+  // base's, and 0.03).  On the 256x128x128 half-MBB beam: lower end 0.3 took 23
+  // V-cycles per solve, 0.1 took 19; degree 3 with 0.06 and inner tolerance
+  // 0.03 took 3 outer iterations and 14 V-cycles.
   const int inners[4] = {1, 2, 4, 6};
   const double base_lo = base->cheb_lo > 0 ? base->cheb_lo : ChebParams{}.lo;
-  const double los[2] = {base_lo, 0.1};
-  const int nlo = base_lo == 0.1 ? 1 : 2;
+  const double base_irt = base->inner_rtol > 0 ? base->inner_rtol : 1e-1;
+  const double los[2] = {base_lo, 0.1}, irts[2] = {base_irt, 0.03};
+  const int nlo = base_lo == 0.1 ? 1 : 2, nirt = base_irt == 0.03 ? 1 : 2;
   for (int ii = 0; ii < 4; ++ii)
     for (int sm = 1; sm <= 2; ++sm)
       for (int deg = 2; deg <= 3; ++deg)
-        for (int il = 0; il < nlo; ++il) {
-          topo_solve_opts o = *base;
-          o.inner_max = inners[ii];
-          o.pre = o.post = sm;
-          o.cheb_degree = deg;
-          o.cheb_lo = los[il];
-          double ms = 0;
-          ++r.candidates;
-          if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
-        }
+        for (int il = 0; il < nlo; ++il)
+          for (int ir = 0; ir < nirt; ++ir) {
+            topo_solve_opts o = *base;
+            o.inner_max = inners[ii];
+            o.pre = o.post = sm;
+            o.cheb_degree = deg;
+            o.cheb_lo = los[il];
+            o.inner_rtol = irts[ir];
+            double ms = 0;
+            ++r.candidates;
+            if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+          }
   // ---- stage 3: the lower end of the interval around the best schedule's
   for (const double lo : {0.05, 0.2}) {
     if (lo == best->cheb_lo) continue;

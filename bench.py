@@ -57,9 +57,10 @@ def parse():
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run exactly one mixed design iteration and exit (for ncu captures)")
     ap.add_argument("--schedule", default=None,
-                    help="inner,pre,degree,tz32,tz64[,lo]: use this mixed-solver schedule (lo: lower end of the "
-                         "Chebyshev interval, a fraction of lambda_max) and these tiles instead of autotuning (e.g. "
-                         "the values an earlier run's autotune chose)")
+                    help="inner,pre,degree,tz32,tz64[,lo[,inner_rtol]]: use this mixed-solver schedule (lo: lower "
+                         "end of the Chebyshev interval, a fraction of lambda_max; inner_rtol: tolerance of the FP32 "
+                         "inner CG) and these tiles instead of autotuning (e.g. the values an earlier run's autotune "
+                         "chose)")
     ap.add_argument("--profile-solve-steps", type=int, default=0,
                     help="with --profile-iteration: stop the solve after this many outer CG steps")
     ap.add_argument("--no-graphs", action="store_true",
@@ -446,6 +447,8 @@ def main():
         opts.update(inner_max=inner, pre=pre, post=pre, cheb_degree=deg)
         if len(sched) > 5:
             opts["cheb_lo"] = float(sched[5])
+        if len(sched) > 6:
+            opts["inner_rtol"] = float(sched[6])
         p.set_tiles(tz32, tz64)
         args.no_autotune = True
     if args.profile_iteration:
@@ -589,7 +592,8 @@ def main():
                       "dofs": 3 * nv, "active_fraction": float(np.mean(wl.eactive)) if wl.eactive is not None else 1.0,
                       "lattice": [q + wl.order for q in wl.partition],
                       "solver": f"FP64 flexible CG (fine matvec in double-float, ~1e-14 of FP64) + "
-                                f"{opts['inner_max']} FP32 CG its with {args.smoother} V({opts['pre']},"
+                                f"{opts['inner_max']} FP32 CG its (to {opts.get('inner_rtol', 0.1):g}) with "
+                                f"{args.smoother} V({opts['pre']},"
                                 f"{opts['post']}) degree-{opts['cheb_degree']} on "
                                 f"[{opts.get('cheb_lo', 0.3):g}, {opts.get('cheb_hi', 1.1):g}] lambda_max multigrid, "
                                 f"rel-res 1e-6",

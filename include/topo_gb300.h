@@ -393,8 +393,9 @@ int topo_design_batch(topo_handle** handles, int n, const topo_iter_opts* opts, 
  * current U with each candidate schedule of the mixed solver (FP32 inner
  * iterations 1, 2, 4, 6 x smoothing steps 1, 2 x Chebyshev degree 2, 3 x lower
  * end of the Chebyshev interval base->cheb_lo, 0.1 x inner tolerance
- * base->inner_rtol, 0.03), stage 3 tries the lower ends 0.05 and 0.2 with the
- * best schedule, and the fastest that converges is
+ * base->inner_rtol, 0.03), stage 3 runs two passes of coordinate search from
+ * the best schedule over the lower end (0.05, 0.1, 0.2, base), the inner
+ * tolerance (0.03, base) and the degree, and the fastest that converges is
  * written into *best (other fields from *base, which must be TOPO_SOLVE_MIXED
  * with the Chebyshev smoother).  U is restored. */
 typedef struct topo_tune_report {

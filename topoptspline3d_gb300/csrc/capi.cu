@@ -54,6 +54,12 @@ struct EventPair {
 
 // CTAs per SM of the coarsest inversion when it runs on the side stream next
 // to the solve's set-up kernels
+// The sums fused into the FP32 fine kernels finish in their last CTA (1) or
+// in a one-CTA kernel after them (0)
+#ifndef TOPO_FUSED_DOT_TICKET
+#define TOPO_FUSED_DOT_TICKET 1
+#endif
+
 #ifndef TOPO_GJ_SIDE_PER_SM
 #define TOPO_GJ_SIDE_PER_SM 1
 #endif
@@ -406,7 +412,11 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bo
       const int np = launch_fine_cheb<T>(
           h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), coef, k == 0,
           h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr, h->fdot_cap,
-          h->vdot_out, h->ctr);
+          h->vdot_out, TOPO_FUSED_DOT_TICKET ? h->ctr : nullptr);
+      if (np > 0 && !TOPO_FUSED_DOT_TICKET) {
+        launch_sum_partials(h->stream, h->vdot, np, h->vdot_out);
+        count_launch();
+      }
       prof_end(h, ev);
       if (dots && np == 0) {  // r.z of the cycle's result (F is r, the output is z), unfused
         launch_dot<T>(h->stream, P<T>::F(L), ub, 3 * L.d.nv, h->partial, h->vdot_out, h->ctr);
@@ -835,7 +845,11 @@ int fcg_body(topo_handle* h, T* x, T* r, T* d, T* q, T* rold, T* z, double* sc, 
   if (sizeof(T) == 4 && h->fdot && h->nb == 1) {
     EventPair* ev = prof_begin(h, P<T>::fam_apply);
     nparts = launch_fine_apply_dot<T>(h->stream, L0.d, P<T>::rhop(h), L0.vmask, d, q, h->tz32, h->fdot,
-                                      h->fdot_cap, sc + S_DQ, h->ctr);
+                                      h->fdot_cap, sc + S_DQ, TOPO_FUSED_DOT_TICKET ? h->ctr : nullptr);
+    if (nparts > 0 && !TOPO_FUSED_DOT_TICKET) {
+      launch_sum_partials(h->stream, h->fdot, nparts, sc + S_DQ);
+      count_launch();
+    }
     prof_end(h, ev);
   }
   if (nparts > 0) {

@@ -123,6 +123,10 @@ void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* parti
   }
 }
 
+void launch_sum_partials(cudaStream_t s, const double* partial, int nb, double* out) {
+  k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, out);
+}
+
 void launch_sum(cudaStream_t s, const double* a, int64_t n, double* partial, double* out) {
   const int nb = reduce_blocks(n);
   k_dot_partial<double><<<nb, RED_THREADS, 0, s>>>(a, nullptr, n, partial);

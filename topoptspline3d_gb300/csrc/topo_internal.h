@@ -157,8 +157,10 @@ void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* 
 
 // vectors and reductions (k_vec.cu)
 int reduce_blocks(int64_t n);
-template <typename T>
+// *out = sum of partial[0 .. nb) in index order (one CTA)
+void launch_sum_partials(cudaStream_t s, const double* partial, int nb, double* out);
 // ctr (optional): a zeroed counter; the last block then writes out itself (one launch)
+template <typename T>
 void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out,
                 unsigned* ctr = nullptr);
 // b == nullptr sums a.

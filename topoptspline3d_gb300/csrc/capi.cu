@@ -21,6 +21,7 @@
 
 namespace topo {
 std::atomic<long long> g_launches{0};
+thread_local long long t_launches = 0;
 }
 
 using namespace topo;
@@ -537,7 +538,7 @@ static void vcycle32(topo_handle* h, int pre, int post, int smoother, const Cheb
   if (!h->vgraph || key != h->vkey) {
     if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
     prof_drop_graph_events(h);
-    const long long l0 = g_launches.load();
+    const long long l0 = t_launches;
     cudaGraph_t g = nullptr;
     bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
@@ -546,8 +547,9 @@ static void vcycle32(topo_handle* h, int pre, int post, int smoother, const Cheb
       h->capturing = false;
       ok = cudaStreamEndCapture(h->stream, &g) == cudaSuccess && g;
     }
-    h->vgraph_kernels = g_launches.load() - l0;
+    h->vgraph_kernels = t_launches - l0;
     g_launches.fetch_sub(h->vgraph_kernels);
+    t_launches = l0;
     if (ok) ok = cudaGraphInstantiate(&h->vgraph, g, 0) == cudaSuccess;
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
@@ -921,7 +923,7 @@ int capture_loop_graph(topo_handle* h, Setup&& setup, Body&& body, Tail&& tail, 
   cudaGraphConditionalHandle hc = 0;
   cudaGraphNode_t cnode = nullptr;
   std::vector<cudaGraphNode_t> deps;
-  const long long l0 = g_launches.load();
+  const long long l0 = t_launches;
   long long l1 = l0, l2 = l0;
   int rc = TOPO_OK;
   const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
@@ -952,9 +954,9 @@ int capture_loop_graph(topo_handle* h, Setup&& setup, Body&& body, Tail&& tail, 
   }
   if (ok) ok = cudaStreamBeginCaptureToGraph(h->stream, bg, nullptr, nullptr, 0, mode) == cudaSuccess;
   if (ok) {
-    l1 = g_launches.load();
+    l1 = t_launches;
     rc = body(hc);
-    l2 = g_launches.load();
+    l2 = t_launches;
     cudaGraph_t gs = nullptr;
     ok = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess && rc == TOPO_OK;
   }
@@ -966,8 +968,9 @@ int capture_loop_graph(topo_handle* h, Setup&& setup, Body&& body, Tail&& tail, 
   }
   h->in_capture = false;
   *per_body = l2 - l1;
-  *fixed = (g_launches.load() - l0) - *per_body;
-  g_launches.fetch_sub(g_launches.load() - l0);
+  *fixed = (t_launches - l0) - *per_body;
+  g_launches.fetch_sub(t_launches - l0);
+  t_launches = l0;
   *exec = nullptr;
   if (ok) ok = cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
   if (g) cudaGraphDestroy(g);

@@ -12,9 +12,15 @@
 
 namespace topo {
 
-// Process-wide count of kernel launches issued by this library.
+// Process-wide count of kernel launches issued by this library, and the
+// calling thread's own count (graph captures measure their kernels with the
+// latter, so launches from other threads are not mixed in).
 extern std::atomic<long long> g_launches;
-inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+extern thread_local long long t_launches;
+inline void count_launch(int n = 1) {
+  g_launches.fetch_add(n, std::memory_order_relaxed);
+  t_launches += n;
+}
 
 // Dense grid level.  Element/vertex numbering is lexicographic (x fastest).
 struct LevelDims {

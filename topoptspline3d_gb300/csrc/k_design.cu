@@ -11,7 +11,7 @@ namespace topo {
 
 static inline unsigned nblk(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-constexpr int MAX_ORDER = 4;
+constexpr int MAX_ORDER = 4;  // highest spline order (cubic B-splines)
 
 // v^p for the SIMP exponent: repeated products for small integer p (the
 // reference default p = 3), the general pow otherwise.
@@ -232,9 +232,9 @@ __global__ void __launch_bounds__(256) k_spline_yz_sep(LevelDims d, SplineDev sp
   }
   __syncthreads();
   const int jlo = sj[0], nj = sj[1] - sj[0] + 1;
-  df nz[4];
+  df nz[MAX_ORDER];
 #pragma unroll
-  for (int t = 0; t < 4; ++t) {
+  for (int t = 0; t < MAX_ORDER; ++t) {
     const float2 n = t < k ? sp.Ndf[2][z * k + t] : make_float2(0.f, 0.f);
     nz[t] = df(n.x, n.y);
   }
@@ -302,9 +302,9 @@ __global__ void __launch_bounds__(ROW_MAX) k_spline_rows(LevelDims d, const uint
   const bool col = x < ex;
   // the column's basis index and weights, for every row
   int ix = -1;
-  df nx[4];
+  df nx[MAX_ORDER];
 #pragma unroll
-  for (int r = 0; r < 4; ++r) nx[r] = df(0);
+  for (int r = 0; r < MAX_ORDER; ++r) nx[r] = df(0);
   if (col) {
     ix = sp.i0[0][x];
     for (int r = 0; r < k; ++r) {
@@ -379,7 +379,7 @@ static bool spline_yz_sep(cudaStream_t s, const LevelDims& d, const SplineDev& s
   // partition is no finer than the elements (the kernel checks each chunk)
   const int cap_j = std::min(sp.nb[1], SEP_Y + sp.order - 1);
   const size_t smem = sizeof(float2) * (size_t)sp.nb[0] * cap_j;
-  if (sp.order > 4 || smem > 200 * 1024) return false;
+  if (sp.order > MAX_ORDER || smem > 200 * 1024) return false;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_spline_yz_sep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
@@ -392,9 +392,9 @@ static bool spline_yz_sep(cudaStream_t s, const LevelDims& d, const SplineDev& s
 static int rows_threads(const LevelDims& d) { return std::min(ROW_MAX, (d.ex + 31) / 32 * 32); }
 
 // Rows fit the row kernel: at most ROW_MAX elements, a staged row of basis
-// values within 4 per thread, spline order at most 4.
+// values within 4 per thread, spline order at most MAX_ORDER.
 static bool rows_fit(const LevelDims& d, const SplineDev& sp) {
-  return d.ex <= ROW_MAX && sp.nb[0] <= 4 * rows_threads(d) && sp.order <= 4;
+  return d.ex <= ROW_MAX && sp.nb[0] <= 4 * rows_threads(d) && sp.order <= MAX_ORDER;
 }
 
 static int rows_blocks(const LevelDims& d) { return (int)std::min<int64_t>(1024, (int64_t)d.ey * d.ez); }

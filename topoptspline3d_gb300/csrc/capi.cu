@@ -217,6 +217,20 @@ int fail(topo_handle* h, int code, const char* fmt, ...) {
                   __FILE__, __LINE__);                                                     \
   } while (0)
 
+// Runs the rest of an entry point on the handle's device (null handle: nothing).
+#define DEVICE_SCOPE(h) topo::DeviceScope device_scope_((h) ? (h)->cfg.device : -1)
+
+// CUDA event destroyed when it leaves scope, on every return path.
+struct ScopedEvent {
+  cudaEvent_t e = nullptr;
+  cudaError_t create() { return cudaEventCreate(&e); }
+  operator cudaEvent_t() const { return e; }
+  ScopedEvent() = default;
+  ScopedEvent(const ScopedEvent&) = delete;
+  ScopedEvent& operator=(const ScopedEvent&) = delete;
+  ~ScopedEvent() { if (e) cudaEventDestroy(e); }
+};
+
 #define RET(x)                   \
   do {                           \
     int rc_ = (x);               \
@@ -1108,6 +1122,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     int dev; bool keep = false;
     ~Release() { if (!keep) material_release(dev); }
   } release{cfg->device};
+  topo::DeviceScope device_scope(cfg->device);
   auto h = std::make_unique<topo_handle>();
   h->cfg = *cfg;
   if (h->cfg.max_coarse_elements <= 0) h->cfg.max_coarse_elements = 400;
@@ -1220,6 +1235,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
 }
 
 void topo_destroy(topo_handle* h) {
+  DEVICE_SCOPE(h);
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->unet) unet_free(h->unet);
@@ -1254,12 +1270,14 @@ void topo_destroy(topo_handle* h) {
 const char* topo_last_error(const topo_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
 int topo_num_levels(const topo_handle* h, int* n) {
+  DEVICE_SCOPE(h);
   if (!h || !n) return TOPO_E_BAD_INPUT;
   *n = (int)h->lv.size();
   return TOPO_OK;
 }
 
 int topo_level_dims(const topo_handle* h, int level, int* dims3, int* factor) {
+  DEVICE_SCOPE(h);
   if (!h || !dims3 || level < 0 || level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
   const LevelDims& d = h->lv[level].d;
   dims3[0] = d.ex; dims3[1] = d.ey; dims3[2] = d.ez;
@@ -1268,12 +1286,14 @@ int topo_level_dims(const topo_handle* h, int level, int* dims3, int* factor) {
 }
 
 int topo_sync(topo_handle* h) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   CK(cudaStreamSynchronize(h->stream));
   return TOPO_OK;
 }
 
 int topo_set_bc_regions(topo_handle* h, const topo_bc_regions* spec, int* nfixed, int* nloaded) {
+  DEVICE_SCOPE(h);
   if (!h || !spec) return TOPO_E_BAD_INPUT;
   if ((spec->nfixed > 0 && !spec->fixed) || (spec->nload > 0 && !spec->load) || (spec->nforce > 0 && !spec->force) ||
       spec->nfixed < 0 || spec->nload < 0 || spec->nforce < 0 || !(spec->spacing > 0))
@@ -1294,6 +1314,7 @@ int topo_plan_bc_regions(int nx, int ny, int nz, const uint8_t* eactive, const t
 }
 
 int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads) {
+  DEVICE_SCOPE(h);
   if (!h || !fixed || !loads) return TOPO_E_BAD_INPUT;
   DevLevel& L = h->lv[0];
   const int64_t nv = L.d.nv;
@@ -1351,6 +1372,7 @@ int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads) {
 
 int topo_set_spline(topo_handle* h, int order, const int* partition3, const double* bmin3,
                     const double* bmax3) {
+  DEVICE_SCOPE(h);
   if (!h || !partition3 || !bmin3 || !bmax3 || order < 2 || order > 4) return TOPO_E_BAD_INPUT;
   for (int a = 0; a < 3; ++a)
     if (partition3[a] < 0 || !(bmax3[a] > bmin3[a])) return TOPO_E_BAD_INPUT;
@@ -1401,6 +1423,7 @@ int topo_set_spline(topo_handle* h, int order, const int* partition3, const doub
 }
 
 int topo_num_coeffs(const topo_handle* h, int* n) {
+  DEVICE_SCOPE(h);
   if (!h || !n) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return TOPO_E_STATE;
   *n = h->sd.nb[0] * h->sd.nb[1] * h->sd.nb[2];
@@ -1408,6 +1431,7 @@ int topo_num_coeffs(const topo_handle* h, int* n) {
 }
 
 int topo_get_knots(const topo_handle* h, int axis, double* out, size_t count) {
+  DEVICE_SCOPE(h);
   if (!h || !out || axis < 0 || axis > 2) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return TOPO_E_STATE;
   if (count != h->st.knots[axis].size()) return TOPO_E_BAD_INPUT;
@@ -1445,12 +1469,14 @@ static int array_info(topo_handle* h, int which, int level, void** dptr, size_t*
 }
 
 int topo_array_size(const topo_handle* h, int which, int level, size_t* count) {
+  DEVICE_SCOPE(h);
   if (!h || !count) return TOPO_E_BAD_INPUT;
   void* p; size_t es;
   return array_info(const_cast<topo_handle*>(h), which, level, &p, count, &es);
 }
 
 int topo_put_array(topo_handle* h, int which, int level, const void* src, size_t count) {
+  DEVICE_SCOPE(h);
   if (!h || !src) return TOPO_E_BAD_INPUT;
   void* p; size_t n, es;
   int rc = array_info(h, which, level, &p, &n, &es);
@@ -1466,6 +1492,7 @@ int topo_put_array(topo_handle* h, int which, int level, const void* src, size_t
 }
 
 int topo_get_array(topo_handle* h, int which, int level, void* dst, size_t count) {
+  DEVICE_SCOPE(h);
   if (!h || !dst) return TOPO_E_BAD_INPUT;
   void* p; size_t n, es;
   int rc = array_info(h, which, level, &p, &n, &es);
@@ -1478,12 +1505,14 @@ int topo_get_array(topo_handle* h, int which, int level, void* dst, size_t count
 }
 
 int topo_device_ptr(topo_handle* h, int which, int level, void** dptr) {
+  DEVICE_SCOPE(h);
   if (!h || !dptr) return TOPO_E_BAD_INPUT;
   size_t n, es;
   return array_info(h, which, level, dptr, &n, &es);
 }
 
 int topo_coeff_to_density(topo_handle* h) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set (call topo_set_spline)");
   const DevLevel& L = h->lv[0];
@@ -1497,6 +1526,7 @@ int topo_coeff_to_density(topo_handle* h) {
 }
 
 int topo_set_operator_precision(topo_handle* h, int mask) {
+  DEVICE_SCOPE(h);
   if (!h || mask < 1 || mask > 3) return TOPO_E_BAD_INPUT;
   h->op_precision = mask;
   h->ops_ready = false;
@@ -1504,6 +1534,7 @@ int topo_set_operator_precision(topo_handle* h, int mask) {
 }
 
 int topo_update_operators(topo_handle* h) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, false));
   RET(update_penalised_if_stale(h));
   const int nl = (int)h->lv.size();
@@ -1585,6 +1616,7 @@ int topo_update_operators(topo_handle* h) {
 }
 
 int topo_apply_fine(topo_handle* h, int precision) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, false));
   RET(update_penalised_if_stale(h));
   DevLevel& L = h->lv[0];
@@ -1610,6 +1642,7 @@ int topo_apply_fine(topo_handle* h, int precision) {
 }
 
 int topo_residual(topo_handle* h, int level) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, level > 0));
   if (level < 0 || level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
   RET(update_penalised_if_stale(h));
@@ -1619,6 +1652,7 @@ int topo_residual(topo_handle* h, int level) {
 }
 
 int topo_smooth(topo_handle* h, int level, int sweeps, int reverse) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, level > 0));
   if (level < 0 || level >= (int)h->lv.size() || sweeps < 0) return TOPO_E_BAD_INPUT;
   RET(update_penalised_if_stale(h));
@@ -1628,6 +1662,7 @@ int topo_smooth(topo_handle* h, int level, int sweeps, int reverse) {
 }
 
 int topo_restrict(topo_handle* h, int coarse_level) {
+  DEVICE_SCOPE(h);
   if (!h || coarse_level < 1 || coarse_level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
   restrict_T<double>(h, coarse_level);
   CKL();
@@ -1635,6 +1670,7 @@ int topo_restrict(topo_handle* h, int coarse_level) {
 }
 
 int topo_prolong(topo_handle* h, int fine_level) {
+  DEVICE_SCOPE(h);
   if (!h || fine_level < 0 || fine_level >= (int)h->lv.size() - 1) return TOPO_E_BAD_INPUT;
   prolong_T<double>(h, fine_level);
   CKL();
@@ -1642,6 +1678,7 @@ int topo_prolong(topo_handle* h, int fine_level) {
 }
 
 int topo_coarsest_solve(topo_handle* h) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, true));
   if (h->lv.size() < 2) return TOPO_E_STATE;
   coarsest_solve_T<double>(h);
@@ -1650,6 +1687,7 @@ int topo_coarsest_solve(topo_handle* h) {
 }
 
 int topo_vcycle(topo_handle* h, int pre, int post, double* relres) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, true));
   if (!h->ops64) return fail(h, TOPO_E_STATE, "FP64 operators not built");
   ChebParams cp;
@@ -1688,6 +1726,7 @@ static int coarse_finish(topo_handle* h) {
 static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats);
 
 int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats) {
+  DEVICE_SCOPE(h);
   const int rc = solve_impl(h, o, stats);
   if (h) RET(coarse_finish(h));
   return rc;
@@ -1703,9 +1742,9 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
   if (o->cheb_degree > 0) cp.degree = o->cheb_degree;
   if (o->cheb_lo > 0) cp.lo = o->cheb_lo;
   if (o->cheb_hi > 0) cp.hi = o->cheb_hi;
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  ScopedEvent e0, e1;
+  CK(e0.create());
+  CK(e1.create());
   CK(cudaEventRecord(e0, h->stream));
   topo_solve_stats st{};
   // ||F||
@@ -1936,8 +1975,6 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
   CK(cudaEventSynchronize(e1));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   st.ms = ms;
   if (stats) *stats = st;
   CKL();
@@ -1947,6 +1984,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
 }
 
 int topo_compliance(topo_handle* h, double* c) {
+  DEVICE_SCOPE(h);
   if (!h || !c) return TOPO_E_BAD_INPUT;
   DevLevel& L = h->lv[0];
   launch_dot<double>(h->stream, L.F, L.U, 3 * L.d.nv, h->partial, h->sc + S_TMP);
@@ -1958,6 +1996,7 @@ int topo_compliance(topo_handle* h, double* c) {
 }
 
 int topo_volume(topo_handle* h, int refden, double* v) {
+  DEVICE_SCOPE(h);
   if (!h || !v) return TOPO_E_BAD_INPUT;
   launch_sum(h->stream, h->rho, h->lv[0].d.ne, h->partial, h->sc + S_TMP);
   count_launch(2);
@@ -1968,6 +2007,7 @@ int topo_volume(topo_handle* h, int refden, double* v) {
 }
 
 int topo_sensitivity(topo_handle* h) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   const DevLevel& L = h->lv[0];
   launch_sensitivity(h->stream, L.d, L.eactive, h->rho, L.U, h->cfg.power_penalty, h->lam, h->mu,
@@ -1978,6 +2018,7 @@ int topo_sensitivity(topo_handle* h) {
 }
 
 int topo_filter(topo_handle* h, double radius) {
+  DEVICE_SCOPE(h);
   if (!h || !(radius > 0)) return TOPO_E_BAD_INPUT;
   if (radius > 16.0) return fail(h, TOPO_E_BAD_INPUT, "filter radius %.3g above 16 elements", radius);
   const DevLevel& L = h->lv[0];
@@ -2012,6 +2053,7 @@ int topo_filter(topo_handle* h, double radius) {
 }
 
 int topo_spline_adjoint(topo_handle* h) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");
   const DevLevel& L = h->lv[0];
@@ -2029,6 +2071,7 @@ static void fine64(topo_handle* h, const LevelDims& d, const double* u, const do
 }
 
 int topo_set_tiles(topo_handle* h, int tz32, int tz64) {
+  DEVICE_SCOPE(h);
   if (!h || tz32 < 1 || tz32 > 256 || tz64 < 1 || tz64 > 256) return TOPO_E_BAD_INPUT;
   h->tz32 = tz32;
   h->tz64 = tz64;
@@ -2036,6 +2079,7 @@ int topo_set_tiles(topo_handle* h, int tz32, int tz64) {
 }
 
 int topo_set_graphs(topo_handle* h, int enable) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   h->graphs = enable != 0;
   if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
@@ -2046,6 +2090,7 @@ int topo_set_graphs(topo_handle* h, int enable) {
 }
 
 int topo_set_fine_arithmetic(topo_handle* h, int arith) {
+  DEVICE_SCOPE(h);
   if (!h || arith < 0 || arith > 1) return TOPO_E_BAD_INPUT;
   h->fine_df = arith;
   return TOPO_OK;
@@ -2098,6 +2143,7 @@ int topo_design_batch(topo_handle** hs, int n, const topo_iter_opts* opts, int n
 }
 
 int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* best, topo_tune_report* rep) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, true));
   if (!base || !best || base->mode != TOPO_SOLVE_MIXED || base->smoother != TOPO_SMOOTH_CHEBYSHEV || base->learned)
     return fail(h, TOPO_E_BAD_INPUT, "autotune: base schedule must be MIXED with the Chebyshev smoother");
@@ -2105,8 +2151,8 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
   topo_tune_report r{};
   DevLevel& L0 = h->lv[0];
   const int64_t n3 = 3 * L0.d.nv;
-  cudaEvent_t t0, t1, a, b;
-  CK(cudaEventCreate(&t0)); CK(cudaEventCreate(&t1)); CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
+  ScopedEvent t0, t1, a, b;
+  CK(t0.create()); CK(t1.create()); CK(a.create()); CK(b.create());
   CK(cudaEventRecord(t0, h->stream));
   ChebParams cp;
   if (base->cheb_degree > 0) cp.degree = base->cheb_degree;
@@ -2229,7 +2275,6 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
   float tms = 0;
   cudaEventElapsedTime(&tms, t0, t1);
   r.tune_ms = tms;
-  cudaEventDestroy(t0); cudaEventDestroy(t1); cudaEventDestroy(a); cudaEventDestroy(b);
   h->err.clear();
   if (rep) *rep = r;
   if (bt >= 1e30) return fail(h, TOPO_E_NOT_CONVERGED, "autotune: no schedule converged");
@@ -2237,6 +2282,7 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
 }
 
 int topo_multi_reserve(topo_handle* h, int capacity) {
+  DEVICE_SCOPE(h);
   if (!h || capacity <= 0 || capacity > 1024) return TOPO_E_BAD_INPUT;
   if (h->multi) {
     for (void* p : h->multi->allocs) cudaFree(p);
@@ -2273,6 +2319,7 @@ int topo_multi_reserve(topo_handle* h, int capacity) {
 }
 
 int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_multi_stats* stats, double* relres) {
+  DEVICE_SCOPE(h);
   RET(check_ready(h, true));
   if (!o || o->rtol <= 0 || o->max_iter < 0 || o->pre < 0 || o->post < 0) return TOPO_E_BAD_INPUT;
   if (!h->multi) return fail(h, TOPO_E_STATE, "call topo_multi_reserve first");
@@ -2312,9 +2359,9 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
   enum { B_RR, B_FF, B_RZ, B_ZROLD, B_RZOLD, B_DQ, B_ALPHA, B_BETA };
   double* sb = m.sc;
   auto slot = [&](int k) { return sb + (size_t)k * m.cap; };
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  ScopedEvent e0, e1;
+  CK(e0.create());
+  CK(e1.create());
   CK(cudaEventRecord(e0, h->stream));
   // r = f - A x, ||r||^2, ||f||^2 per right-hand side
   fine64(h, L0.d, m.x, m.f, m.r, true, nb);
@@ -2367,8 +2414,6 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
   CK(cudaEventSynchronize(e1));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   double worst = 0;
   for (int k = 0; k < nb; ++k) {
     const double rel = ff[k] > 0 ? std::sqrt(rr[k] / ff[k]) : 0.0;
@@ -2386,6 +2431,7 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
 }
 
 int topo_unet_enable(topo_handle* h, unsigned long long seed) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   if (h->unet) { unet_free(h->unet); h->unet = nullptr; }
   const cudaError_t e = unet_create(&h->unet, h->stream, seed);
@@ -2406,6 +2452,7 @@ static int unet_ready(topo_handle* h) {
 }
 
 int topo_unet_get_params(topo_handle* h, float* dst, size_t n) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   if (!dst || n != unet_param_count()) return fail(h, TOPO_E_BAD_INPUT, "expected %zu parameters", unet_param_count());
   CK(unet_get_params(h->unet, h->stream, dst));
@@ -2413,6 +2460,7 @@ int topo_unet_get_params(topo_handle* h, float* dst, size_t n) {
 }
 
 int topo_unet_set_params(topo_handle* h, const float* src, size_t n) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   if (!src || n != unet_param_count()) return fail(h, TOPO_E_BAD_INPUT, "expected %zu parameters", unet_param_count());
   for (size_t i = 0; i < n; ++i)
@@ -2428,6 +2476,7 @@ static int unet_dims_ok(topo_handle* h, int X, int Y, int Z, int nb) {
 }
 
 int topo_unet_forward(topo_handle* h, int X, int Y, int Z, int nb, const float* x, float* y) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   RET(unet_dims_ok(h, X, Y, Z, nb));
   if (!x || !y) return TOPO_E_BAD_INPUT;
@@ -2437,6 +2486,7 @@ int topo_unet_forward(topo_handle* h, int X, int Y, int Z, int nb, const float* 
 
 int topo_unet_loss_grad(topo_handle* h, int X, int Y, int Z, int nb, const float* x, const float* t,
                         const uint8_t* mask, double* loss, float* grad) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   RET(unet_dims_ok(h, X, Y, Z, nb));
   if (!x || !t || !mask || !loss || !grad) return TOPO_E_BAD_INPUT;
@@ -2445,6 +2495,7 @@ int topo_unet_loss_grad(topo_handle* h, int X, int Y, int Z, int nb, const float
 }
 
 int topo_unet_dataset_reserve(topo_handle* h, int capacity, int crop, int crops_per_iterate) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   if (capacity <= 0 || crop <= 0 || crop % 8 || crop > 64 || crops_per_iterate <= 0 || crops_per_iterate > 4096)
     return fail(h, TOPO_E_BAD_INPUT, "dataset: capacity > 0, crop a multiple of 8 up to 64, 1..4096 crops per iterate");
@@ -2456,6 +2507,7 @@ int topo_unet_dataset_reserve(topo_handle* h, int capacity, int crop, int crops_
 }
 
 int topo_unet_dataset_size(topo_handle* h, int* n) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   if (!n) return TOPO_E_BAD_INPUT;
   *n = unet_dataset_count(h->unet);
@@ -2463,6 +2515,7 @@ int topo_unet_dataset_size(topo_handle* h, int* n) {
 }
 
 int topo_unet_dataset_get(topo_handle* h, int slot, float* x, float* t, uint8_t* mask, int* crop) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   if (!x || !t || !mask || !crop) return TOPO_E_BAD_INPUT;
   *crop = unet_crop_side(h->unet);
@@ -2474,6 +2527,7 @@ int topo_unet_dataset_get(topo_handle* h, int slot, float* x, float* t, uint8_t*
 
 int topo_unet_train(topo_handle* h, int steps, int batch, double lr, unsigned long long seed, int lo, int hi,
                     int update, double* loss) {
+  DEVICE_SCOPE(h);
   RET(unet_ready(h));
   if (!loss || steps <= 0 || steps > 65536 || batch <= 0 || batch > 64 || !(lr > 0))
     return fail(h, TOPO_E_BAD_INPUT, "train: 1..65536 steps, batch 1..64, lr > 0");
@@ -2484,6 +2538,7 @@ int topo_unet_train(topo_handle* h, int steps, int batch, double lr, unsigned lo
 }
 
 int topo_volume_csens(topo_handle* h, int refden, double scale, double* out_dev) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");
   if (!out_dev) out_dev = h->volcsens;
@@ -2572,6 +2627,7 @@ static int oc_bisection_graphed(topo_handle* h, const topo_oc_opts* o, int64_t n
 extern "C" {
 
 int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) {
+  DEVICE_SCOPE(h);
   if (!h || !o) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set");
   const DevLevel& L = h->lv[0];
@@ -2680,6 +2736,7 @@ static int gs_maps_impl(topo_handle* h, const LevelDims& d, const std::vector<ui
 
 int topo_gs_maps(topo_handle* h, int level, int* vidmap, size_t nvid, int* eidmap, size_t neid,
                  int* gs_num8, int* n_gsvertices, int* n_gselements) {
+  DEVICE_SCOPE(h);
   if (!h || level < 0 || level >= (int)h->lv.size()) return TOPO_E_BAD_INPUT;
   return gs_maps_impl(h, h->lv[level].d, h->H.vactive[level], h->H.eactive[level], vidmap, nvid,
                       eidmap, neid, gs_num8, n_gsvertices, n_gselements);
@@ -2738,6 +2795,7 @@ int topo_host_free(void* ptr) {
 }
 
 int topo_timer_start(topo_handle* h) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   if (!h->timer_ev[0]) {
     CK(cudaEventCreate(&h->timer_ev[0]));
@@ -2748,6 +2806,7 @@ int topo_timer_start(topo_handle* h) {
 }
 
 int topo_timer_stop(topo_handle* h, double* ms) {
+  DEVICE_SCOPE(h);
   if (!h || !ms || !h->timer_ev[0]) return TOPO_E_BAD_INPUT;
   CK(cudaEventRecord(h->timer_ev[1], h->stream));
   CK(cudaEventSynchronize(h->timer_ev[1]));
@@ -2758,10 +2817,11 @@ int topo_timer_stop(topo_handle* h, double* ms) {
 }
 
 int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* stats) {
+  DEVICE_SCOPE(h);
   if (!h || !o) return TOPO_E_BAD_INPUT;
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  ScopedEvent e0, e1;
+  CK(e0.create());
+  CK(e1.create());
   CK(cudaEventRecord(e0, h->stream));
   topo_iter_stats st{};
   h->defer_coarse = true;  // the coarsest inversion overlaps the solve's set-up
@@ -2792,14 +2852,13 @@ int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_sta
   CK(cudaEventSynchronize(e1));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   st.ms = ms;
   if (stats) *stats = st;
   return rc;
 }
 
 int topo_profile_enable(topo_handle* h, int enable) {
+  DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
   h->prof = enable != 0;
   for (int f = 0; f < TOPO_K_COUNT; ++f) { h->gprof_ms[f] = 0; h->gprof_n[f] = 0; }
@@ -2807,6 +2866,7 @@ int topo_profile_enable(topo_handle* h, int enable) {
 }
 
 int topo_profile_read(topo_handle* h, int family, int* launches, double* ms) {
+  DEVICE_SCOPE(h);
   if (!h || family < 0 || family >= TOPO_K_COUNT) return TOPO_E_BAD_INPUT;
   CK(cudaStreamSynchronize(h->stream));
   prof_collect(h);
@@ -2827,6 +2887,7 @@ int topo_profile_read(topo_handle* h, int family, int* launches, double* ms) {
 }
 
 int topo_launch_count(const topo_handle* h, long long* n) {
+  DEVICE_SCOPE(h);
   (void)h;
   if (!n) return TOPO_E_BAD_INPUT;
   *n = g_launches.load();

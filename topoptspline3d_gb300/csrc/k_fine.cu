@@ -1112,7 +1112,7 @@ dim3 modal_grid(const LevelDims& d, int tz, int nb) {
 
 // One launch of the modal operator in mode MODE: the single-barrier kernel for
 // FP32, the generic kernel for FP64.  Kernels are opted into their dynamic
-// shared memory once.
+// shared memory once per device.
 template <typename T, int MODE>
 void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u, const T* f,
                   T* out, int tz, int nb, const ChebArgs& ch) {
@@ -1121,10 +1121,12 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
   constexpr int TYE = modal_tye<T>();
   if constexpr (sizeof(T) == 4) {
     const size_t smem = sizeof(Modal32Smem<TYE>);
-    static std::once_flag once;
-    std::call_once(once, [smem] {
-      cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static PerDeviceOnce once;
+    once_per_device(once, [smem] {
+      cudaError_t e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      return e;
     });
     // (MODE 3 keeps 64-bit offsets: with 32-bit ones it spilled 32 bytes and
     // ran 122 against 118 us at 256x128x128, where modes 0-2 gained 4-9 us)
@@ -1134,10 +1136,10 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
       k_fine_modal32<TYE, MODE, false><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
   } else {
     const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
-    static std::once_flag once;
-    std::call_once(once, [smem] {
-      cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
+    static PerDeviceOnce once;
+    once_per_device(once, [smem] {
+      return cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem);
     });
     k_fine_modal<T, MODAL_TXE, TYE, MODE><<<grid, MODAL_TXE * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
   }
@@ -1179,11 +1181,14 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
                   ((d.vz + tz - 1) / tz) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(DfSmem<MODAL_TXE, MODAL_TYE>);
-  static std::once_flag once;
-  std::call_once(once, [smem] {
-    cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static PerDeviceOnce once;
+  once_per_device(once, [smem] {
+    cudaError_t e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e;
   });
   if (residual && energy)
     k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, energy);

@@ -53,6 +53,7 @@ extern "C" int topo_spline_adjoint_noalloc(topo_handle* h, const double* sens_de
   SplineView sv;
   const int rc = handle_spline_view(h, &sv);
   if (rc != TOPO_OK) return rc;
+  DeviceScope device_scope(sv.device);
   const int64_t n1 = (int64_t)sv.sp.nb[0] * sv.d.ey * sv.d.ez;
   const int64_t n2 = (int64_t)sv.sp.nb[0] * sv.sp.nb[1] * sv.d.ez;
   if (n1 + n2 > kNoallocScratchDoubles)

@@ -431,11 +431,10 @@ static size_t conv_smem() {
 template <int CIN, int COUT>
 static cudaError_t conv_launch(cudaStream_t s, const ConvIn& in, const __nv_bfloat16* W, const float* bias, int X,
                                int Y, int Z, int nb, int relu, int out_mode, void* out) {
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
+  static PerDeviceOnce once;
   const size_t smem = conv_smem<CIN, COUT>();
-  std::call_once(once, [smem] {
-    attr_err = cudaFuncSetAttribute(k_conv3<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const cudaError_t attr_err = once_per_device(once, [smem] {
+    return cudaFuncSetAttribute(k_conv3<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
   if (attr_err != cudaSuccess) return attr_err;
   dim3 grid((X + kTX - 1) / kTX, (Y + kTY - 1) / kTY, nb * Z / kTZ);

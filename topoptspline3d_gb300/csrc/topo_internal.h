@@ -22,6 +22,46 @@ inline void count_launch(int n = 1) {
   t_launches += n;
 }
 
+// Makes device `dev` current for the scope of one API call and gives the
+// calling thread its previous device back on exit.  Every entry point that
+// takes a handle runs on the handle's device, whatever device the calling
+// thread had selected (a handle on GPU 1 driven from a thread left on GPU 0,
+// the worker threads of topo_design_batch).  dev < 0 does nothing.
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(int dev) {
+    if (dev < 0) return;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) { cudaGetLastError(); return; }
+    if (cur == dev) return;
+    if (cudaSetDevice(dev) != cudaSuccess) { cudaGetLastError(); return; }
+    prev = cur;
+  }
+  ~DeviceScope() { if (prev >= 0) cudaSetDevice(prev); }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
+// Runs `fn` (returning cudaError_t) once per CUDA device, on the calling
+// thread's current device: settings such as a kernel's dynamic shared-memory
+// opt-in belong to one device, so a process with handles on several GPUs needs
+// them on each.  A failed attempt is retried by the next call.
+struct PerDeviceOnce {
+  std::atomic<unsigned long long> done{0};
+};
+template <typename Fn>
+inline cudaError_t once_per_device(PerDeviceOnce& o, Fn&& fn) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return fn();
+  const unsigned long long bit = 1ull << dev;
+  if (o.done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  e = fn();
+  if (e == cudaSuccess) o.done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
+
 // Dense grid level.  Element/vertex numbering is lexicographic (x fastest).
 struct LevelDims {
   int ex, ey, ez;

@@ -62,6 +62,7 @@ def _load():
         "orc_put": (None, [vp, C.c_int, C.c_int, vp]),
         "orc_get": (None, [vp, C.c_int, C.c_int, vp]),
         "orc_size": (i64, [vp, C.c_int, C.c_int]),
+        "orc_spline_basis": (C.c_int, [vp, C.c_int, C.c_double, dp]),
         "orc_coeff_to_density": (None, [vp]),
         "orc_update_penalised": (None, [vp]),
         "orc_update_operators": (None, [vp]),
@@ -157,6 +158,12 @@ class Oracle:
         out = np.zeros(2 * order + partition)
         self.lib.orc_get_knots(self.h, axis, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
+
+    def basis(self, axis: int, x: float, order: int):
+        """(first basis index or -1, the order basis values) at coordinate x."""
+        out = np.zeros(8)
+        i0 = self.lib.orc_spline_basis(self.h, axis, float(x), out.ctypes.data_as(C.POINTER(C.c_double)))
+        return i0, out[:order]
 
     # --- arrays
     def get(self, name: str, level: int = 0) -> np.ndarray:

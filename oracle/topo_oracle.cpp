@@ -951,6 +951,12 @@ static int spline_basis(const orc_problem* p, int axis, double x, double* N) {
   return i - k;
 }
 
+// Basis values at an arbitrary coordinate, for the golden vectors of the
+// reference's SplineBasisX/Y/Z: N[order], returns the first basis index or -1.
+extern "C" int orc_spline_basis(const orc_problem* p, int axis, double x, double* N) {
+  return spline_basis(p, axis, x, N);
+}
+
 extern "C" void orc_coeff_to_density(orc_problem* p) {
   const Level& L = p->lv[0];
   int k = p->order;

@@ -437,6 +437,53 @@ int topo_multi_reserve(topo_handle* h, int capacity);
 int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* opts, topo_multi_stats* stats,
                      double* relres);
 
+/* --- worst-case (robust) compliance ---------------------------------------- */
+/* The reference's default optimisation (optimization/optimization.cpp:673-767)
+ * designs against the worst unit load on a load region: the largest
+ * compliance f.K^-1 f over loads f of unit norm on the region's vertices
+ * (modifiedPM, optimization/optimization.cpp:213-351).  With supports, a load
+ * either acts along each load vertex's normal (the reference's
+ * with_support_constrain_force_direction: forceProject removes the tangential
+ * parts, optimization/projection.cpp:289-360) or in any direction
+ * (with_support_free_force).  The worst load is the leading eigenvector of
+ * M = S^T K^-1 S, S the scatter from load coordinates to nodal forces. */
+
+/* Replaces setLoadNodes (optimization/projection.cpp:129-269) and
+ * uploadLoadNodes (optimization/projection.cu:71-118): n load vertices
+ * (level-0 vertex ids) with unit outward normals normals[3*n] (xyz per
+ * vertex; ignored with free_direction).  Fixed DOFs carry no load. */
+int topo_set_load_region(topo_handle* h, int n, const int* vertices, const double* normals);
+
+typedef struct topo_worst_opts {
+  topo_solve_opts solve;      /* multi-RHS solve per block iteration: MIXED, CHEBYSHEV, inner_max <= 1;
+                                 solve.rtol is the FP64 tolerance of the final solve */
+  int free_direction;         /* 0: force along each vertex normal; 1: any direction */
+  int block;                  /* load vectors iterated together (1 = the reference's single vector) */
+  int max_iter;               /* block iterations (reference 500) */
+  double tol;                 /* stop when the worst load changes by less than this (reference fch 1e-4) */
+  unsigned long long seed;    /* start vectors (the reference seeds cuRAND by time, Q10) */
+} topo_worst_opts;
+
+typedef struct topo_worst_stats {
+  double compliance;          /* worst-case compliance f.U of the unit worst load */
+  double second;              /* next Ritz value (the leading one's gap) */
+  double change;              /* last change of the worst load, |f_new - f_old| */
+  double relres;              /* FP64 relative residual of the final solve */
+  int iterations;             /* block iterations */
+  int solve_iterations;       /* outer FP64 CG iterations summed over the block solves */
+  double ms;                  /* device time */
+} topo_worst_stats;
+
+/* Replaces modifiedPM (optimization/optimization.cpp:213-351) with a block
+ * (subspace) iteration of Rayleigh-Ritz steps over `block` load vectors, each
+ * step one multi-right-hand-side solve warm-started from the previous step's
+ * displacements rotated into the new basis.  Leaves the unit worst load in
+ * TOPO_F and its displacement in TOPO_U (level 0), so topo_sensitivity and the
+ * rest of the design chain act on the worst case as the reference's
+ * optimization() does.  Needs topo_update_operators with FP32 operators and
+ * reserves multi-RHS buffers for `block` right-hand sides. */
+int topo_worst_compliance(topo_handle* h, const topo_worst_opts* opts, topo_worst_stats* stats);
+
 /* --- learned preconditioner (U-Net) --------------------------------------- */
 /* A 3-level 3D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, 245,203
  * effective parameters, bf16 weights, fp32 accumulation) corrects the FP32

@@ -46,6 +46,7 @@ EXPORTED = [
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
     "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
+    "topo_set_load_region", "topo_worst_compliance",
 ]
 
 
@@ -97,6 +98,16 @@ class TuneReport(C.Structure):
 
 class MultiStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("vcycles", C.c_int), ("max_relres", C.c_double), ("ms", C.c_double)]
+
+
+class WorstOpts(C.Structure):
+    _fields_ = [("solve", SolveOpts), ("free_direction", C.c_int), ("block", C.c_int), ("max_iter", C.c_int),
+                ("tol", C.c_double), ("seed", C.c_ulonglong)]
+
+
+class WorstStats(C.Structure):
+    _fields_ = [("compliance", C.c_double), ("second", C.c_double), ("change", C.c_double), ("relres", C.c_double),
+                ("iterations", C.c_int), ("solve_iterations", C.c_int), ("ms", C.c_double)]
 
 
 class MmaStats(C.Structure):
@@ -195,6 +206,8 @@ def load(build: bool = True):
         "topo_unet_train": (i, [vp, i, i, d, C.c_ulonglong, i, i, i, dp]),
         "topo_set_bc_regions": (i, [vp, vp, ip, ip]),
         "topo_plan_bc_regions": (i, [i, i, i, vp, vp, vp, vp, ip, ip]),
+        "topo_set_load_region": (i, [vp, i, ip, dp]),
+        "topo_worst_compliance": (i, [vp, C.POINTER(WorstOpts), C.POINTER(WorstStats)]),
         "topo_mma_create": (i, [i, i, i, C.POINTER(vp)]),
         "topo_mma_create_for": (i, [vp, i, C.POINTER(vp)]),
         "topo_mma_destroy": (None, [vp]),
@@ -596,6 +609,29 @@ class Problem:
         loss = C.c_double()
         self._ck(self.lib.topo_unet_train(self.h, steps, batch, lr, seed, lo, hi, int(update), C.byref(loss)))
         return loss.value
+
+    def set_load_region(self, vertices, normals=None):
+        """Load region of the worst-case compliance: level-0 vertex ids and (for
+        loads along the normal) their outward normals [n][3]."""
+        v = np.ascontiguousarray(vertices, dtype=np.int32).ravel()
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64).ravel()
+        self._ck(self.lib.topo_set_load_region(self.h, int(v.size), v.ctypes.data_as(C.POINTER(C.c_int)),
+                                               None if nrm is None else nrm.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def worst_compliance(self, block=8, free_direction=False, max_iter=100, tol=1e-4, seed=1, check=True, **solve):
+        """Worst-case compliance over unit loads on the load region; leaves the
+        worst load in F and its displacement in U."""
+        so = dict(mode=SOLVE_MIXED, smoother=SMOOTH_CHEBYSHEV, pre=1, post=1, rtol=1e-6, max_iter=300,
+                  inner_rtol=0.1, cheb_degree=2, cheb_lo=0.3, cheb_hi=1.1, inner_max=1, learned=0, learned_stall=0.0)
+        so.update(solve)
+        o = WorstOpts(SolveOpts(*[so[f[0]] for f in SolveOpts._fields_]), int(bool(free_direction)), int(block),
+                      int(max_iter), float(tol), int(seed))
+        st = WorstStats()
+        rc = self.lib.topo_worst_compliance(self.h, C.byref(o), C.byref(st))
+        if check or rc not in (TOPO_OK, TOPO_E_NOT_CONVERGED):
+            self._ck(rc)
+        return {"compliance": st.compliance, "second": st.second, "change": st.change, "relres": st.relres,
+                "iterations": st.iterations, "solve_iterations": st.solve_iterations, "ms": st.ms, "rc": rc}
 
     def compliance(self) -> float:
         c = C.c_double()

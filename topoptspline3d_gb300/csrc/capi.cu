@@ -111,6 +111,7 @@ struct topo_handle {
   double gprof_ms[TOPO_K_COUNT] = {0};
   int gprof_n[TOPO_K_COUNT] = {0};
   topo::MultiRhs* multi = nullptr;  // batched buffers (topo_multi_reserve)
+  topo::WorstState* worst = nullptr;  // load region and block buffers (topo_set_load_region)
   int unet_crops = 64;              // crops per harvested iterate
   cudaStream_t stream = nullptr;
   std::string err;
@@ -1253,6 +1254,7 @@ void topo_destroy(topo_handle* h) {
     for (void* p : h->multi->allocs) cudaFree(p);
     delete h->multi;
   }
+  if (h->worst) worst_free(h->worst);
   for (void* p : h->allocs) cudaFree(p);
   for (int f = 0; f < TOPO_K_COUNT; ++f)
     for (auto& e : h->evs[f]) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
@@ -2567,6 +2569,15 @@ int handle_spline_view(topo_handle* h, SplineView* out) {
   return TOPO_OK;
 }
 int handle_fail(topo_handle* h, int code, const char* msg) { return fail(h, code, "%s", msg); }
+int handle_level_view(topo_handle* h, LevelView* out) {
+  if (!h || !out) return TOPO_E_BAD_INPUT;
+  out->d = h->lv[0].d;
+  out->vmask = h->lv[0].vmask;
+  out->stream = h->stream;
+  out->device = h->cfg.device;
+  return TOPO_OK;
+}
+WorstState*& handle_worst_slot(topo_handle* h) { return h->worst; }
 }  // namespace topo
 
 // The OC bisection of topo_oc_update as one CUDA graph: start (bracket [0,

@@ -288,6 +288,22 @@ struct SplineView {
 };
 int handle_spline_view(topo_handle* h, SplineView* out);
 int handle_fail(topo_handle* h, int code, const char* msg);
+// Level-0 view of the handle for the worst-case compliance driver (worst.cu).
+struct LevelView {
+  LevelDims d;
+  const uint8_t* vmask;
+  cudaStream_t stream;
+  int device;
+};
+int handle_level_view(topo_handle* h, LevelView* out);
+struct WorstState;
+void worst_free(WorstState* w);
+WorstState*& handle_worst_slot(topo_handle* h);
+#define RET_IF(x)                   \
+  do {                              \
+    const int rc_ = (x);            \
+    if (rc_ != TOPO_OK) return rc_; \
+  } while (0)
 // cnew_df (optional): cnew split into (hi, lo) floats as well; thres_p
 // (optional): the threshold read from device memory instead of thres
 void launch_oc_trial(cudaStream_t s, int64_t nc, const double* cold, const double* csens, double thres,

@@ -518,6 +518,48 @@ int topo_unet_dataset_get(topo_handle* h, int slot, float* x, float* t, uint8_t*
 int topo_unet_train(topo_handle* h, int steps, int batch, double lr, unsigned long long seed, int lo, int hi,
                     int update, double* loss);
 
+/* --- domains, files and checkpoints -------------------------------------- */
+/* The reference's domain input: an LSB-first uint32 bit mask over a
+ * reso[0] x reso[1] x reso[2] frame, bit b of word w = element 32w + b with x
+ * fastest (HierarchyGrid::genFromMesh(const std::vector<unsigned>&, int[3]),
+ * grid/Grid.cpp:977; the frame is the next power of two above the part,
+ * voxelizer/voxelize_main.cpp:312-340).  The handle's grid is the nx x ny x nz
+ * box at the frame's origin; a set bit outside it is TOPO_E_BAD_INPUT. */
+int topo_bitmask_to_eactive(const int* reso3, const uint32_t* words, int nx, int ny, int nz, uint8_t* eactive);
+/* The inverse: words[ceil(reso0*reso1*reso2 / 32)] from eactive (NULL = all active). */
+int topo_eactive_to_bitmask(int nx, int ny, int nz, const uint8_t* eactive, const int* reso3, uint32_t* words);
+/* Replaces HierarchyGrid::genFromMesh(const std::vector<unsigned>&, int[3])
+ * (grid/Grid.cpp:977-1040): topo_create on the bit mask's domain. */
+int topo_create_bitmask(const topo_config* cfg, const int* reso3, const uint32_t* words, topo_handle** out);
+
+/* Raw binary records, the reference's bio::write_vector / read_vector
+ * (utils/binaryIO.h:70-108): the array as count values, FP64 or (fp32 = 1)
+ * FP32, no header.  topo_write_array(h, TOPO_COEFF, 0, path, 1) is
+ * HierarchyGrid::writeCoeff (grid/Grid.cpp:2139-2156); reading checks that
+ * the file holds exactly the array. */
+int topo_write_array(topo_handle* h, int which, int level, const char* path, int fp32);
+int topo_read_array(topo_handle* h, int which, int level, const char* path, int fp32);
+/* The active elements' (x, y, z, value) as FP32 records, 4 per element in
+ * lexicographic order: what HierarchyGrid::writeDensity / writeSensitivity
+ * (grid/Grid.cpp:1266-1310, 2062-2098) pass to OpenVDB.  which = TOPO_RHO or
+ * TOPO_SENS; count (may be NULL) receives the number of records. */
+int topo_write_active_records(topo_handle* h, int which, const char* path, int64_t* count);
+
+/* Checkpoint of a design run (no reference counterpart: the reference
+ * restarts from a coefficient file).  Holds the coefficients, the density,
+ * the warm-start displacement, the spectral-bound warm starts of every level,
+ * the z-march depths and `user_bytes` of caller data (iteration counters,
+ * solver options).  A run resumed from it on a handle with the same grid,
+ * boundary conditions, spline and settings repeats the uninterrupted run bit
+ * for bit.  Loading fails with TOPO_E_BAD_INPUT on another grid or spline;
+ * user (may be NULL) receives at most user_cap bytes, *user_bytes the size. */
+int topo_checkpoint_save(topo_handle* h, const char* path, const void* user, size_t user_bytes);
+int topo_checkpoint_load(topo_handle* h, const char* path, void* user, size_t user_cap, size_t* user_bytes);
+/* The MMA state (iterate and history, bounds, asymptotes, amplifiers, stop
+ * counter) of the same size. */
+int topo_mma_checkpoint_save(topo_mma* mma, const char* path);
+int topo_mma_checkpoint_load(topo_mma* mma, const char* path);
+
 /* --- host-only set-up helpers (no GPU needed) ----------------------------- */
 /* Element template (element/templateMatrix.cpp:31-99), row-major 24x24. */
 int topo_element_template(double E, double nu, double h, double* Ke576);

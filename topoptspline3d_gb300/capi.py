@@ -46,7 +46,9 @@ EXPORTED = [
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
     "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
-    "topo_set_load_region", "topo_worst_compliance",
+    "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
+    "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
+    "topo_checkpoint_save", "topo_checkpoint_load", "topo_mma_checkpoint_save", "topo_mma_checkpoint_load",
 ]
 
 
@@ -208,6 +210,16 @@ def load(build: bool = True):
         "topo_plan_bc_regions": (i, [i, i, i, vp, vp, vp, vp, ip, ip]),
         "topo_set_load_region": (i, [vp, i, ip, dp]),
         "topo_worst_compliance": (i, [vp, C.POINTER(WorstOpts), C.POINTER(WorstStats)]),
+        "topo_bitmask_to_eactive": (i, [ip, vp, i, i, i, vp]),
+        "topo_eactive_to_bitmask": (i, [i, i, i, vp, ip, vp]),
+        "topo_create_bitmask": (i, [C.POINTER(TopoConfig), ip, vp, C.POINTER(vp)]),
+        "topo_write_array": (i, [vp, i, i, C.c_char_p, i]),
+        "topo_read_array": (i, [vp, i, i, C.c_char_p, i]),
+        "topo_write_active_records": (i, [vp, i, C.c_char_p, C.POINTER(C.c_int64)]),
+        "topo_checkpoint_save": (i, [vp, C.c_char_p, vp, sz]),
+        "topo_checkpoint_load": (i, [vp, C.c_char_p, vp, sz, C.POINTER(sz)]),
+        "topo_mma_checkpoint_save": (i, [vp, C.c_char_p]),
+        "topo_mma_checkpoint_load": (i, [vp, C.c_char_p]),
         "topo_mma_create": (i, [i, i, i, C.POINTER(vp)]),
         "topo_mma_create_for": (i, [vp, i, C.POINTER(vp)]),
         "topo_mma_destroy": (None, [vp]),
@@ -339,23 +351,53 @@ class PinnedBuffer:
             pass
 
 
+def bitmask_to_eactive(reso, words, nx, ny, nz) -> np.ndarray:
+    """Host-only: the reference's LSB-first uint32 domain bit mask over a reso
+    frame -> element mask of the nx x ny x nz box at its origin."""
+    lib = load()
+    r = (C.c_int * 3)(*reso)
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    out = np.zeros(nx * ny * nz, dtype=np.uint8)
+    _ck_free(lib.topo_bitmask_to_eactive(r, w.ctypes.data, nx, ny, nz, out.ctypes.data), "bitmask_to_eactive")
+    return out
+
+
+def eactive_to_bitmask(nx, ny, nz, eactive, reso) -> np.ndarray:
+    """Host-only: element mask -> LSB-first uint32 words over the reso frame."""
+    lib = load()
+    r = (C.c_int * 3)(*reso)
+    ea = None if eactive is None else np.ascontiguousarray(eactive, dtype=np.uint8).ravel()
+    out = np.zeros((int(np.prod(reso)) + 31) // 32, dtype=np.uint32)
+    _ck_free(lib.topo_eactive_to_bitmask(nx, ny, nz, None if ea is None else ea.ctypes.data, r, out.ctypes.data),
+             "eactive_to_bitmask")
+    return out
+
+
 class Problem:
     """One topology-optimisation problem on one GPU (wraps ``topo_handle``)."""
 
     def __init__(self, nx, ny, nz, h=1.0, E=1e6, nu=0.4, penal=3.0, rho_min=1e-3, eactive=None,
-                 max_coarse_elements=400, device=0):
+                 max_coarse_elements=400, device=0, bitmask=None):
+        """bitmask = (reso[3], uint32 words): the reference's domain input
+        (topo_create_bitmask) instead of eactive."""
         self.lib = load()
         self.dims = (nx, ny, nz)
         self.nv = (nx + 1) * (ny + 1) * (nz + 1)
         self.ne = nx * ny * nz
         cfg = TopoConfig(nx, ny, nz, h, E, nu, penal, rho_min, max_coarse_elements, device)
-        mask = None
-        if eactive is not None:
-            self._mask = np.ascontiguousarray(eactive, dtype=np.uint8).ravel()
-            assert self._mask.size == self.ne
-            mask = self._mask.ctypes.data
         hp = C.c_void_p()
-        rc = self.lib.topo_create(C.byref(cfg), mask, C.byref(hp))
+        if bitmask is not None:
+            reso, words = bitmask
+            self._words = np.ascontiguousarray(words, dtype=np.uint32)
+            rc = self.lib.topo_create_bitmask(C.byref(cfg), (C.c_int * 3)(*reso), self._words.ctypes.data,
+                                              C.byref(hp))
+        else:
+            mask = None
+            if eactive is not None:
+                self._mask = np.ascontiguousarray(eactive, dtype=np.uint8).ravel()
+                assert self._mask.size == self.ne
+                mask = self._mask.ctypes.data
+            rc = self.lib.topo_create(C.byref(cfg), mask, C.byref(hp))
         if rc != TOPO_OK:
             raise TopoError(rc, "topo_create failed")
         self.h = hp
@@ -633,6 +675,30 @@ class Problem:
         return {"compliance": st.compliance, "second": st.second, "change": st.change, "relres": st.relres,
                 "iterations": st.iterations, "solve_iterations": st.solve_iterations, "ms": st.ms, "rc": rc}
 
+    # --- files and checkpoints
+    def write_array(self, name, path, fp32=False, level=0):
+        """Raw record of an array (bio::write_vector); fp32 as the reference's writeCoeff."""
+        self._ck(self.lib.topo_write_array(self.h, ARRAYS[name], level, os.fsencode(path), int(bool(fp32))))
+
+    def read_array(self, name, path, fp32=False, level=0):
+        self._ck(self.lib.topo_read_array(self.h, ARRAYS[name], level, os.fsencode(path), int(bool(fp32))))
+
+    def write_active_records(self, name, path) -> int:
+        """(x, y, z, value) FP32 records of the active elements (density or sensitivity)."""
+        n = C.c_int64()
+        self._ck(self.lib.topo_write_active_records(self.h, ARRAYS[name], os.fsencode(path), C.byref(n)))
+        return n.value
+
+    def checkpoint_save(self, path, user=b""):
+        buf = C.create_string_buffer(bytes(user), max(len(user), 1))
+        self._ck(self.lib.topo_checkpoint_save(self.h, os.fsencode(path), buf, len(user)))
+
+    def checkpoint_load(self, path, user_cap=4096) -> bytes:
+        buf = C.create_string_buffer(max(user_cap, 1))
+        n = C.c_size_t()
+        self._ck(self.lib.topo_checkpoint_load(self.h, os.fsencode(path), buf, user_cap, C.byref(n)))
+        return buf.raw[:min(n.value, user_cap)]
+
     def compliance(self) -> float:
         c = C.c_double()
         self._ck(self.lib.topo_compliance(self.h, C.byref(c)))
@@ -800,6 +866,12 @@ class MMA:
         self._ck(self.lib.topo_mma_update(self.h, C.c_void_p(int(df_ptr)), dg, _dp(gv), C.byref(st)))
         return {"subiterations": st.subiterations, "kkt_err": st.kkt_err, "step": st.step,
                 "dx_norm": st.dx_norm, "overflow": bool(st.overflow), "converged": bool(st.converged)}
+
+    def checkpoint_save(self, path):
+        self._ck(self.lib.topo_mma_checkpoint_save(self.h, os.fsencode(path)))
+
+    def checkpoint_load(self, path):
+        self._ck(self.lib.topo_mma_checkpoint_load(self.h, os.fsencode(path)))
 
     def get_x(self, dst_ptr):
         self._ck(self.lib.topo_mma_get_x(self.h, C.c_void_p(int(dst_ptr))))

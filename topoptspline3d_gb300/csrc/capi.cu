@@ -26,35 +26,6 @@ thread_local long long t_launches = 0;
 
 using namespace topo;
 
-namespace {
-
-// Scalar slots in device memory used by the PCG drivers.
-// Slots 0-7 belong to one CG level; a nested CG uses base 8 (slots 8-15).
-enum Slot {
-  S_RZ = 0, S_ZROLD = 1, S_RZOLD = 2, S_DQ = 3, S_RR = 4, S_FF = 5, S_ALPHA = 6, S_BETA = 7,
-  S_TMP = 16, S_PW = 24, S_MAXLEV = 16,
-  // device-controlled inner CG loop: iterations of the current inner solve,
-  // its ||b|| reference, the first iteration whose r.r was non-finite
-  // (1-based, 0 = none), inner iterations summed over the solve
-  S_LOOP = S_PW + 2 * S_MAXLEV,
-  // device-side OC bisection: lo, hi, the current trial's threshold, its
-  // volume fraction, trials, repeats (the reference loop's itn)
-  S_OC = S_LOOP + 4, S_COUNT = S_OC + 6
-};
-
-// Chebyshev step coefficients (c_old, c_new) in device memory: per precision
-// (FP64 first), level and step, then the pair (0, 1).
-constexpr int CHEB_MAX_DEG = 32;
-constexpr int CHEB_TABLE = 2 * (2 * S_MAXLEV * CHEB_MAX_DEG + 1);
-
-struct EventPair {
-  cudaEvent_t a, b;
-};
-
-}  // namespace
-
-// CTAs per SM of the coarsest inversion when it runs on the side stream next
-// to the solve's set-up kernels
 // The sums fused into the FP32 fine kernels finish in their last CTA (1) or
 // in a one-CTA kernel after them (0).  Measured at 256x128x128: without the
 // last-CTA ticket (a fence and an atomic per CTA while the CTA waits) the
@@ -65,128 +36,13 @@ struct EventPair {
 #define TOPO_FUSED_DOT_TICKET 1
 #endif
 
+// CTAs per SM of the coarsest inversion when it runs on the side stream next
+// to the solve's set-up kernels
 #ifndef TOPO_GJ_SIDE_PER_SM
 #define TOPO_GJ_SIDE_PER_SM 1
 #endif
 
-struct topo_handle {
-  topo_config cfg{};
-  topo::UNetState* unet = nullptr;  // learned preconditioner (topo_unet_enable)
-  bool mat_registered = false;      // holds a reference on the device's element constants
-  int nb = 1;                       // right-hand sides the level vectors hold (multi-RHS solve)
-  int fine_df = 1;                  // FP64 fine operator in double-float arithmetic (topo_set_fine_arithmetic)
-  int tz32 = 16, tz64 = 16;         // z-march depth of the fine kernels, FP32 / FP64 (topo_autotune)
-  // FP32 V-cycle replayed as one CUDA graph (topo_set_graphs); re-captured when its key changes
-  bool graphs = true;
-  cudaGraphExec_t vgraph = nullptr;
-  std::vector<double> vkey;
-  long long vgraph_kernels = 0;
-  // inner FP32 CG of the mixed solve as one graph with a device-side WHILE
-  // loop (igraph); kernels of its fixed part and of one loop iteration
-  bool in_capture = false;
-  bool igraph_ok = true;
-  cudaGraphExec_t igraph = nullptr;
-  std::vector<double> ikey;
-  long long igraph_fixed = 0, igraph_body = 0;
-  // OC bisection as one graph with a device-side WHILE loop (ograph)
-  bool ograph_ok = true;
-  cudaGraphExec_t ograph = nullptr;
-  std::vector<double> okey;
-  long long ograph_fixed = 0, ograph_body = 0;
-  // coarsest inversion of a design iteration on a second stream (side),
-  // overlapped with the solve's set-up; the main stream waits for ev_coarse
-  // before its first V-cycle (coarse_join) and the status is read at the end
-  // of the solve (coarse_finish)
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_ops = nullptr, ev_coarse = nullptr;
-  int* hstat = nullptr;           // pinned copy of the inversion status
-  bool defer_coarse = false;      // topo_design_iteration's operator update
-  bool coarse_pending = false;    // the main stream has not waited for it yet
-  bool coarse_unchecked = false;  // its status has not been read yet
-  // profiling inside the graph: event pairs captured as external event-record
-  // nodes, collected after each replay has completed
-  bool capturing = false;
-  std::vector<std::pair<int, EventPair>> gprof;
-  bool gprof_pending = false;
-  double gprof_ms[TOPO_K_COUNT] = {0};
-  int gprof_n[TOPO_K_COUNT] = {0};
-  topo::MultiRhs* multi = nullptr;  // batched buffers (topo_multi_reserve)
-  topo::WorstState* worst = nullptr;  // load region and block buffers (topo_set_load_region)
-  int unet_crops = 64;              // crops per harvested iterate
-  cudaStream_t stream = nullptr;
-  std::string err;
-  Hierarchy H;
-  std::vector<DevLevel> lv;
-  double Ke[576];
-  double lam = 0, mu = 0;
-  std::vector<void*> allocs;
-  // element template and Galerkin tables
-  double* dKe = nullptr;
-  double* dT64 = nullptr;
-  float* dT32 = nullptr;
-  // level-0 design arrays
-  double *rho = nullptr, *rhop = nullptr, *sens = nullptr, *sens_tmp = nullptr;
-  float* rhop32 = nullptr;
-  bool rhop_stale = false;
-  // spline
-  bool spline_set = false;
-  SplineTables st;
-  SplineDev sd{};
-  double *coeff = nullptr, *csens = nullptr, *coeff_old = nullptr, *coeff_tmp = nullptr;
-  float2* coeff_df = nullptr;  // OC trial coefficients split into (hi, lo) floats
-  double* volcsens = nullptr;  // scale * d volume / d coefficient (topo_volume_csens)
-  double *adj1 = nullptr, *adj2 = nullptr;
-  // level-0 work vectors
-  double *work = nullptr, *x = nullptr, *r = nullptr, *d = nullptr, *q = nullptr, *rold = nullptr,
-         *f = nullptr;
-  float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *q32 = nullptr, *rold32 = nullptr;
-  // coarsest level
-  int ndense = 0;
-  double* A = nullptr;
-  float* A32 = nullptr;
-  double* gjwork = nullptr;  // panels of the blocked Gauss-Jordan inversion
-  double* coarse64tmp = nullptr;  // FP64 copy of an FP32 coarsest stencil
-  int* status = nullptr;
-  // first coarse level: elements whose fine elements touch fixed DOFs
-  int* gal_fixed = nullptr;
-  int n_gal_fixed = 0;
-  int coarse_dropped = 0;  // null directions dropped by the coarsest inverse
-  cudaEvent_t timer_ev[2] = {nullptr, nullptr};
-  // sensitivity filter ball (offsets and weights) for the last radius used
-  double filt_radius = -1.0;
-  int4* filt_offs = nullptr;
-  double* filt_w = nullptr;
-  float2* filt_wdf = nullptr;  // the weights split into (hi, lo) floats
-  int filt_n = 0;
-  // reductions
-  double* partial = nullptr;
-  double* fdot = nullptr;  // per-CTA partials of the fine operator's fused dot
-  int fdot_cap = 0;
-  // ticket counter of the reductions whose last block writes the total (the
-  // handle's stream runs them one at a time; the last block resets it)
-  unsigned* ctr = nullptr;
-  // inner CG: the FP32 V-cycle's last Chebyshev step also forms r.z (partials
-  // in vdot) when vdot_on; the sum lands in *vdot_out
-  double* vdot = nullptr;
-  bool vdot_on = false;
-  double* vdot_out = nullptr;
-  bool inner_fr = false;  // inner CG in Fletcher-Reeves form (z.rold taken as 0)
-  double* chebc = nullptr;          // Chebyshev coefficient table (device)
-  std::vector<double> chebc_host;   // its last uploaded contents
-  double* sc = nullptr;    // device scalar slots
-  double* hsc = nullptr;   // pinned host mirror
-  int64_t active_elements = 0, gs_padded_elements = 0;
-  bool bc_set = false, ops_ready = false;
-  // design iteration: the solve's final residual also writes element energies
-  // into sens (want_energy), and says so (energy_ready)
-  bool want_energy = false, energy_ready = false;
-  int op_precision = 3;    // bit0 FP64 operators, bit1 FP32 operators
-  bool ops64 = false, ops32 = false;
-  // profiling
-  bool prof = false;
-  std::vector<EventPair> evs[TOPO_K_COUNT];
-  std::vector<EventPair> evpool;
-};
+#include "handle.h"
 
 namespace {
 

@@ -29,7 +29,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstring>
 #include <string>
+#include <vector>
 
 #include "topo_internal.h"
 
@@ -591,7 +594,7 @@ int topo_mma_set_constraint_amplifier(topo_mma* o, double c, double d) {
 }
 
 static int mma_init_impl(topo_mma* o, const double* lb, const double* ub, double lbu, double ubu) {
-  MCK(cudaSetDevice(o->device));
+  DeviceScope device_scope(o->device);
   const double* dlb = nullptr;
   const double* dub = nullptr;
   if (lb && ub) {
@@ -628,7 +631,7 @@ int topo_mma_update(topo_mma* o, const double* df_dev, const double* const* dg_d
   if (!o) return TOPO_E_BAD_INPUT;
   if (!df_dev || !dg_dev || !g) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: null gradient or constraint");
   if (!o->initialised) return mma_fail(o, TOPO_E_STATE, "MMA: call topo_mma_init first");
-  MCK(cudaSetDevice(o->device));
+  DeviceScope device_scope(o->device);
   MmaArgs A{};
   A.n = o->n;
   A.m = o->m;
@@ -678,22 +681,72 @@ int topo_mma_update(topo_mma* o, const double* df_dev, const double* const* dg_d
 
 int topo_mma_get_x(topo_mma* o, double* dst_dev) {
   if (!o || !dst_dev) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: null destination");
-  MCK(cudaSetDevice(o->device));
+  DeviceScope device_scope(o->device);
   MCK(cudaMemcpyAsync(dst_dev, o->x, sizeof(double) * o->n, cudaMemcpyDeviceToDevice, o->stream));
   return TOPO_OK;
 }
 
 int topo_mma_read_x(topo_mma* o, double* dst_host) {
   if (!o || !dst_host) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: null destination");
-  MCK(cudaSetDevice(o->device));
+  DeviceScope device_scope(o->device);
   MCK(cudaMemcpyAsync(dst_host, o->x, sizeof(double) * o->n, cudaMemcpyDeviceToHost, o->stream));
   MCK(cudaStreamSynchronize(o->stream));
   return TOPO_OK;
 }
 
+// Persistent MMA state: the iterate and its history (x, xold), the bounds,
+// the asymptotes and their last step (the first nine per-variable arrays),
+// the bound arrays, the constraint amplifiers and the stop counter.  The
+// per-update scratch (subproblem variables, partial sums) is not kept.
+static const char kMmaMagic[8] = {'T', 'O', 'P', 'O', 'M', 'M', 'A', '1'};
+
+int topo_mma_checkpoint_save(topo_mma* o, const char* path) {
+  if (!o || !path) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: null path");
+  DeviceScope device_scope(o->device);
+  const size_t n = o->n;
+  std::vector<double> st(11 * n);
+  MCK(cudaMemcpyAsync(st.data(), o->x, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost, o->stream));
+  MCK(cudaMemcpyAsync(st.data() + 9 * n, o->lbub, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, o->stream));
+  MCK(cudaStreamSynchronize(o->stream));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: cannot open checkpoint file");
+  const int32_t hdr[4] = {o->n, o->m, o->stop_counter, o->initialised ? 1 : 0};
+  bool ok = std::fwrite(kMmaMagic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(hdr), 1, f) == 1 &&
+            std::fwrite(o->c, sizeof(o->c), 1, f) == 1 && std::fwrite(o->d, sizeof(o->d), 1, f) == 1 &&
+            std::fwrite(st.data(), sizeof(double), st.size(), f) == st.size();
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? TOPO_OK : mma_fail(o, TOPO_E_BAD_INPUT, "MMA: checkpoint write failed");
+}
+
+int topo_mma_checkpoint_load(topo_mma* o, const char* path) {
+  if (!o || !path) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: null path");
+  DeviceScope device_scope(o->device);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: cannot open checkpoint file");
+  char magic[8];
+  int32_t hdr[4];
+  double c[kMmaMaxM], d[kMmaMaxM];
+  std::vector<double> st(11 * (size_t)o->n);
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kMmaMagic, 8) == 0 &&
+            std::fread(hdr, sizeof(hdr), 1, f) == 1 && hdr[0] == o->n && hdr[1] == o->m &&
+            std::fread(c, sizeof(c), 1, f) == 1 && std::fread(d, sizeof(d), 1, f) == 1 &&
+            std::fread(st.data(), sizeof(double), st.size(), f) == st.size();
+  std::fclose(f);
+  if (!ok) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: not a checkpoint of this size");
+  MCK(cudaMemcpyAsync(o->x, st.data(), sizeof(double) * 9 * o->n, cudaMemcpyHostToDevice, o->stream));
+  MCK(cudaMemcpyAsync(o->lbub, st.data() + 9 * (size_t)o->n, sizeof(double) * 2 * o->n, cudaMemcpyHostToDevice,
+                      o->stream));
+  MCK(cudaStreamSynchronize(o->stream));
+  std::memcpy(o->c, c, sizeof(c));
+  std::memcpy(o->d, d, sizeof(d));
+  o->stop_counter = hdr[2];
+  o->initialised = hdr[3] != 0;
+  return TOPO_OK;
+}
+
 int topo_mma_write_x(topo_mma* o, const double* src_host) {
   if (!o || !src_host) return mma_fail(o, TOPO_E_BAD_INPUT, "MMA: null source");
-  MCK(cudaSetDevice(o->device));
+  DeviceScope device_scope(o->device);
   MCK(cudaMemcpyAsync(o->x, src_host, sizeof(double) * o->n, cudaMemcpyHostToDevice, o->stream));
   MCK(cudaStreamSynchronize(o->stream));
   return TOPO_OK;

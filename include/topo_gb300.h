@@ -532,6 +532,18 @@ int topo_eactive_to_bitmask(int nx, int ny, int nz, const uint8_t* eactive, cons
  * (grid/Grid.cpp:977-1040): topo_create on the bit mask's domain. */
 int topo_create_bitmask(const topo_config* cfg, const int* reso3, const uint32_t* words, topo_handle** out);
 
+/* Mesh -> domain bit mask (voxelizer/voxelize_main.cpp:344-406 with the solid
+ * rule of voxelizer/voxelize_solid.cu:78-166): a closed triangle mesh
+ * (verts[3*nverts] xyz, tris[3*ntris] vertex ids) in a cube frame around its
+ * bounding box, padded to the next power of two above preferred_resolution
+ * (reso_out; box6_out = min xyz, max xyz).  A voxel is solid when an odd
+ * number of triangles lie beyond its centre along x.  words (may be NULL for
+ * a size query) receives reso^3 / 32 LSB-first words, the input of
+ * topo_create_bitmask.  topo_voxel_frame computes only the frame (host). */
+int topo_voxel_frame(const float* verts, int nverts, int preferred_resolution, int* reso_out, float* box6_out);
+int topo_voxelize_mesh(int device, const float* verts, int nverts, const int* tris, int ntris, int preferred_resolution,
+                       int* reso_out, float* box6_out, uint32_t* words, size_t nwords_cap);
+
 /* Raw binary records, the reference's bio::write_vector / read_vector
  * (utils/binaryIO.h:70-108): the array as count values, FP64 or (fp32 = 1)
  * FP32, no header.  topo_write_array(h, TOPO_COEFF, 0, path, 1) is

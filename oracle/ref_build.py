@@ -11,6 +11,10 @@ missing), but these routines are self-contained arithmetic:
   grid/Grid.cu    ddensity2dcoeff_kernel + the node_diff lambda of Grid::ddensity2dcoeff_update
   grid/Grid.cu    filterSensitivity_kernel + the fr weight lambda of Grid::filterSensitivity
   grid/Grid.h     BitCount;  culib/lib.cuh  gBitSAT, read_gbit(word), clamp
+  voxelizer/voxelize_solid.cu   voxelize_triangle_solid and its helpers (solid
+                                voxelisation by x-ray parity, Schwarz-Seidel)
+  voxelizer/voxelize_main.cpp   get_point_bb, padd2SatifyResolution (the cube frame)
+  voxelizer/util.h              AABox, voxinfo
 
 The recipe cuts those blocks out of the reference sources where they lie (by
 their opening lines, brace-matched) into oracle/_ref/, never into the
@@ -18,7 +22,10 @@ repository, and compiles them with oracle/ref_harness.cpp, which supplies the
 CUDA keywords, thread indices and __constant__ symbols as host globals and runs
 each kernel as a serial loop over its threads.  Two libraries are built: the
 reference's tap count m_iM = 3 (grid/Grid.h:35) and m_iM = 4 (the same code at
-cubic order, which the reference's hard-wired constant does not allow).
+cubic order, which the reference's hard-wired constant does not allow).  The
+voxeliser pieces go into a third (oracle/ref_vox_harness.cpp), which supplies
+the few glm vector operations they use, written from glm's documented
+definitions (normalize = v * inversesqrt(dot(v, v)), the usual cross product).
 
   python -m oracle.ref_build [--reference DIR]
 """
@@ -91,13 +98,25 @@ def extract(ref: str) -> dict:
     parts["ref_fr.inc"] = _block(gcu, _find(gcu, "auto fr = [=] __device__(float r)", flt))
     parts["ref_knots.inc"] = _block(gcpp, _find(gcpp, "void grid::Grid::set_spline_knot_series(void)"),
                                     stop_marker="// upload to device")
+    vs, vm, vu = read("voxelizer/voxelize_solid.cu"), read("voxelizer/voxelize_main.cpp"), read("voxelizer/util.h")
+    parts["ref_vox.inc"] = (
+        [vs[_find(vs, "#define float_error")]]
+        + sum((_block(vs, _find(vs, sig)) for sig in (
+            "__device__ __inline__ void setBitXor(", "__device__ inline int check_point_triangle(",
+            "__device__ inline float get_x_coordinate(", "__device__ inline bool checkCCW(",
+            "__device__ inline bool TopLeftEdge(", "__global__ void voxelize_triangle_solid(")), []))
+    parts["ref_vox_frame.inc"] = (
+        _block(vu, _find(vu, "struct AABox {"), template_prev=True)
+        + _block(vu, _find(vu, "struct voxinfo {"))
+        + _block(vm, _find(vm, "std::pair<glm::vec3, glm::vec3> get_point_bb("))
+        + _block(vm, _find(vm, "int padd2SatifyResolution(")))
     return {k: "\n".join(v) + "\n" for k, v in parts.items()}
 
 
 def build(ref: str = DEFAULT_REF, force: bool = False) -> list:
-    """Returns the paths of the two libraries (m_iM = 3, 4); builds them when the
-    reference sources are present."""
-    libs = [os.path.join(OUT, f"libref_pieces_m{m}.so") for m in (3, 4)]
+    """Returns the paths of the libraries (spline pieces at m_iM = 3 and 4, the
+    voxeliser); builds them when the reference sources are present."""
+    libs = [os.path.join(OUT, f"libref_pieces_m{m}.so") for m in (3, 4)] + [os.path.join(OUT, "libref_vox.so")]
     if not force and all(os.path.exists(p) for p in libs):
         return libs
     if not os.path.isdir(os.path.join(ref, "grid")):
@@ -112,6 +131,10 @@ def build(ref: str = DEFAULT_REF, force: bool = False) -> list:
         subprocess.check_call(["g++", "-O1", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off",
                                "-w", f"-DREF_M_IM={m}", "-I" + OUT, harness, "-o", tmp])
         os.replace(tmp, lib)
+    tmp = libs[2] + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", "-O1", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-w",
+                           "-I" + OUT, os.path.join(HERE, "ref_vox_harness.cpp"), "-o", tmp])
+    os.replace(tmp, libs[2])
     return libs
 
 

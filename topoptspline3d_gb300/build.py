@@ -21,8 +21,11 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "libtopo_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["capi.cu", "k_fine.cu", "k_coarse.cu", "k_vec.cu", "k_design.cu", "k_noalloc.cu", "k_mma.cu", "k_unet.cu", "unet.cu", "k_multi.cu", "worst.cu", "io.cu"]
+CU_SOURCES = ["capi.cu", "k_fine.cu", "k_coarse.cu", "k_vec.cu", "k_design.cu", "k_noalloc.cu", "k_mma.cu", "k_unet.cu", "unet.cu", "k_multi.cu", "worst.cu", "io.cu", "voxel.cu"]
 CPP_SOURCES = ["host_setup.cpp", "bc_regions.cpp"]
+# per-file nvcc flags: the voxeliser reproduces the reference's FP32 tests
+# operation for operation, so no multiply-add contraction there
+FILE_FLAGS = {"voxel.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -57,6 +60,7 @@ def _compile(src: str) -> str:
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include")]
     if src.endswith(".cu"):
         cmd = [nvcc, ARCH, "-lineinfo", "--expt-relaxed-constexpr", "-c", src, "-o", obj] + common
+        cmd += FILE_FLAGS.get(os.path.basename(src), [])
         cmd += os.environ.get("TOPO_NVCC_FLAGS", "").split()
     else:
         cmd = [nvcc, "-x", "c++", "-c", src, "-o", obj] + common

@@ -49,6 +49,7 @@ EXPORTED = [
     "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
     "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
     "topo_checkpoint_save", "topo_checkpoint_load", "topo_mma_checkpoint_save", "topo_mma_checkpoint_load",
+    "topo_voxel_frame", "topo_voxelize_mesh",
 ]
 
 
@@ -210,6 +211,8 @@ def load(build: bool = True):
         "topo_plan_bc_regions": (i, [i, i, i, vp, vp, vp, vp, ip, ip]),
         "topo_set_load_region": (i, [vp, i, ip, dp]),
         "topo_worst_compliance": (i, [vp, C.POINTER(WorstOpts), C.POINTER(WorstStats)]),
+        "topo_voxel_frame": (i, [vp, i, i, ip, vp]),
+        "topo_voxelize_mesh": (i, [i, vp, i, vp, i, i, ip, vp, vp, sz]),
         "topo_bitmask_to_eactive": (i, [ip, vp, i, i, i, vp]),
         "topo_eactive_to_bitmask": (i, [i, i, i, vp, ip, vp]),
         "topo_create_bitmask": (i, [C.POINTER(TopoConfig), ip, vp, C.POINTER(vp)]),
@@ -371,6 +374,31 @@ def eactive_to_bitmask(nx, ny, nz, eactive, reso) -> np.ndarray:
     _ck_free(lib.topo_eactive_to_bitmask(nx, ny, nz, None if ea is None else ea.ctypes.data, r, out.ctypes.data),
              "eactive_to_bitmask")
     return out
+
+
+def voxel_frame(verts, preferred_resolution):
+    """Host-only: (resolution, box[6]) of the voxelisation frame of a mesh."""
+    lib = load()
+    v = np.ascontiguousarray(verts, dtype=np.float32).ravel()
+    r = C.c_int()
+    box = np.zeros(6, dtype=np.float32)
+    _ck_free(lib.topo_voxel_frame(v.ctypes.data, v.size // 3, int(preferred_resolution), C.byref(r), box.ctypes.data),
+             "voxel_frame")
+    return r.value, box
+
+
+def voxelize_mesh(verts, tris, preferred_resolution, device=0):
+    """Solid voxelisation on the GPU: (resolution, box[6], LSB-first uint32 words)."""
+    lib = load()
+    v = np.ascontiguousarray(verts, dtype=np.float32).ravel()
+    t = np.ascontiguousarray(tris, dtype=np.int32).ravel()
+    reso, box = voxel_frame(v, preferred_resolution)
+    words = np.zeros((reso ** 3 + 31) // 32, dtype=np.uint32)
+    r = C.c_int()
+    _ck_free(lib.topo_voxelize_mesh(device, v.ctypes.data, v.size // 3, t.ctypes.data, t.size // 3,
+                                    int(preferred_resolution), C.byref(r), box.ctypes.data, words.ctypes.data,
+                                    words.size), "voxelize_mesh")
+    return r.value, box, words
 
 
 class Problem:

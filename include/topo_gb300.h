@@ -56,7 +56,12 @@ enum topo_array {
   TOPO_WORK = 13,    /* double[3*nv] scratch vector (level 0): input of topo_apply_fine */
   TOPO_VOLCSENS = 14, /* double[nc]  scaled d volume / d coefficient (topo_volume_csens) */
   TOPO_MULTI_F = 15,  /* double[cap*3*nv] right-hand sides of topo_solve_multi (after topo_multi_reserve) */
-  TOPO_MULTI_U = 16   /* double[cap*3*nv] solutions / initial guesses of topo_solve_multi */
+  TOPO_MULTI_U = 16,  /* double[cap*3*nv] solutions / initial guesses of topo_solve_multi */
+  TOPO_SSCSENS = 17,  /* double[nc]  d self-support constraint / d coefficient (topo_support_constraints) */
+  TOPO_DRIPCSENS = 18, /* double[nc] d drip constraint / d coefficient */
+  TOPO_RHO_INIT = 19, /* double[ne]  density before the Heaviside projection (topo_heaviside_project) */
+  TOPO_SURF_POINTS = 20,  /* double[3*npts] surface points of the last topo_support_constraints, SoA xyz */
+  TOPO_SURF_NORMALS = 21  /* double[3*npts] their spline gradients (the constraint's normals) */
 };
 
 typedef struct topo_config {
@@ -483,6 +488,62 @@ typedef struct topo_worst_stats {
  * optimization() does.  Needs topo_update_operators with FP32 operators and
  * reserves multi-RHS buffers for `block` right-hand sides. */
 int topo_worst_compliance(topo_handle* h, const topo_worst_opts* opts, topo_worst_stats* stats);
+
+/* --- Heaviside projection and manufacturing constraints ------------------- */
+/* Replaces projectDensities (optimization/optimization.cu:313-353):
+ * TOPO_RHO_INIT <- rho, rho <- clamp(H_beta(rho_init), rho_min, 1) with
+ * H_beta(s) = (tanh(beta/2) + tanh(beta (s - 1/2))) / (2 tanh(beta/2)). */
+int topo_heaviside_project(topo_handle* h, double beta);
+/* Chain rule of the projection on TOPO_SENS (before topo_filter):
+ * sens *= dH/drho(rho_init) (computeProjectionSensitivity_kernel,
+ * optimization/optimization.cu:161-183). */
+int topo_heaviside_sensitivity(topo_handle* h, double beta);
+/* The projected volume's coefficient gradient of computeSensitivity2
+ * (optimization/optimization.cu:243-311): scale / den * dH/drho on active
+ * elements, filtered with filter_radius (> 0) and taken through the spline
+ * adjoint into out_dev[nc] (NULL = TOPO_VOLCSENS); den as topo_volume_csens. */
+int topo_heaviside_volume_csens(topo_handle* h, double beta, int refden, double filter_radius, double scale,
+                                double* out_dev);
+
+/* Self-support and drip constraints of the spline design
+ * (deal_surface_points, optimization/optimization.cpp:1103-1127;
+ * grid/Grid.cu:5529-7156).  Surface points: the crossings of the spline's 1/2
+ * level set with the edges of a (lattice + 2)^3 lattice of cell centres over
+ * the domain box padded by one cell (spline - 1/2 inside the box, -1/2
+ * outside; compute_background_mcPoints_value, grid/Grid.cu:3986-4095), kept in
+ * lattice order when they lie in an active element, thinned to max_points by
+ * the reference's equidistant pick.  Normal = spline gradient; when most
+ * points see solid a small step along it (Heaviside with `beta` at 1/2), all
+ * normals are flipped.  Per point inner = n_z / |n| / cos(print_angle pi);
+ * the self-support value by ss_mode (0 p-norm, 1 p-norm all, 2 h, 3 h all,
+ * 4 overhang sigmoid, 5 overhang all; "down only" modes count points with
+ * n_z < 0), the drip value by drip_mode (6 exp, 7 exp all; 0-5 contribute
+ * zero, as in the reference's compute_spline_drip_constraint_test), each
+ * averaged over its count (p-norm modes: mean^(1/p) - 1).  Their coefficient
+ * gradients (points held fixed, each point's terms summed in point order per
+ * coefficient, divided by the count) go to TOPO_SSCSENS / TOPO_DRIPCSENS. */
+typedef struct topo_support_opts {
+  int lattice;            /* lattice cells per axis (reference 64) */
+  int max_points;         /* surface points kept (reference 200000) */
+  double print_angle;     /* in units of pi (reference opt_print_angle; its flag default 3/4 parses as 0) */
+  int ss_mode;            /* 0..5 as above (reference default "oh" = 4) */
+  int drip_mode;          /* 0..7 (reference default "oh" = 4, which contributes zero) */
+  double beta;            /* Heaviside sharpness of the normal-direction test */
+  double p_norm, hfunction_c, sigmoid_c;   /* 0 = the reference's 8, 10, 0.09 */
+  double drip_beta, drip_mu, drip_angle, drip_alpha, drip_beta_scale; /* 0 = 128, 32, 160 deg (radians), 4, 10 */
+  int drip_version;       /* 1: Gaussian of the gradient slope; else the sigmoid of the angle */
+  int reference_quirks;   /* drip gradient as the reference computes it (Hessian derivatives summed over the
+                             taps already visited, the y slope derivative written over the x one) */
+} topo_support_opts;
+typedef struct topo_support_stats {
+  int candidates;         /* level-set crossings in active elements */
+  int points;             /* points used */
+  int overhang_points;    /* points with n_z < 0 */
+  int flipped;            /* normals flipped by the direction test */
+  double ss_value;        /* global self-support value (the MMA constraint is scale * (ss - 1)) */
+  double drip_value;      /* global drip value (the constraint is scale * drip) */
+} topo_support_stats;
+int topo_support_constraints(topo_handle* h, const topo_support_opts* opts, topo_support_stats* stats);
 
 /* --- learned preconditioner (U-Net) --------------------------------------- */
 /* A 3-level 3D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, 245,203

@@ -20,7 +20,7 @@ STATUS_NAMES = {0: "TOPO_OK", 1: "TOPO_E_CUDA", 2: "TOPO_E_BAD_INPUT", 3: "TOPO_
 
 ARRAYS = {"rho": 0, "rhop": 1, "coeff": 2, "sens": 3, "csens": 4, "u": 5, "f": 6, "r": 7,
           "stencil": 8, "kelem": 9, "vmask": 10, "eactive": 11, "ke": 12, "work": 13, "volcsens": 14, "multi_f": 15,
-          "multi_u": 16}
+          "multi_u": 16, "sscsens": 17, "dripcsens": 18, "rho_init": 19, "surf_points": 20, "surf_normals": 21}
 BYTE_ARRAYS = {"vmask", "eactive"}
 
 SOLVE_VCYCLE, SOLVE_PCG64, SOLVE_MIXED = 0, 1, 2
@@ -49,7 +49,8 @@ EXPORTED = [
     "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
     "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
     "topo_checkpoint_save", "topo_checkpoint_load", "topo_mma_checkpoint_save", "topo_mma_checkpoint_load",
-    "topo_voxel_frame", "topo_voxelize_mesh",
+    "topo_voxel_frame", "topo_voxelize_mesh", "topo_heaviside_project", "topo_heaviside_sensitivity",
+    "topo_heaviside_volume_csens", "topo_support_constraints",
 ]
 
 
@@ -111,6 +112,24 @@ class WorstOpts(C.Structure):
 class WorstStats(C.Structure):
     _fields_ = [("compliance", C.c_double), ("second", C.c_double), ("change", C.c_double), ("relres", C.c_double),
                 ("iterations", C.c_int), ("solve_iterations", C.c_int), ("ms", C.c_double)]
+
+
+class SupportOpts(C.Structure):
+    _fields_ = [("lattice", C.c_int), ("max_points", C.c_int), ("print_angle", C.c_double), ("ss_mode", C.c_int),
+                ("drip_mode", C.c_int), ("beta", C.c_double), ("p_norm", C.c_double), ("hfunction_c", C.c_double),
+                ("sigmoid_c", C.c_double), ("drip_beta", C.c_double), ("drip_mu", C.c_double),
+                ("drip_angle", C.c_double), ("drip_alpha", C.c_double), ("drip_beta_scale", C.c_double),
+                ("drip_version", C.c_int), ("reference_quirks", C.c_int)]
+
+
+class SupportStats(C.Structure):
+    _fields_ = [("candidates", C.c_int), ("points", C.c_int), ("overhang_points", C.c_int), ("flipped", C.c_int),
+                ("ss_value", C.c_double), ("drip_value", C.c_double)]
+
+
+SUPPORT_DEFAULTS = dict(lattice=64, max_points=200000, print_angle=0.75, ss_mode=4, drip_mode=4, beta=4.0,
+                        p_norm=0.0, hfunction_c=0.0, sigmoid_c=0.0, drip_beta=0.0, drip_mu=0.0, drip_angle=0.0,
+                        drip_alpha=0.0, drip_beta_scale=0.0, drip_version=0, reference_quirks=0)
 
 
 class MmaStats(C.Structure):
@@ -211,6 +230,10 @@ def load(build: bool = True):
         "topo_plan_bc_regions": (i, [i, i, i, vp, vp, vp, vp, ip, ip]),
         "topo_set_load_region": (i, [vp, i, ip, dp]),
         "topo_worst_compliance": (i, [vp, C.POINTER(WorstOpts), C.POINTER(WorstStats)]),
+        "topo_heaviside_project": (i, [vp, d]),
+        "topo_heaviside_sensitivity": (i, [vp, d]),
+        "topo_heaviside_volume_csens": (i, [vp, d, i, d, d, vp]),
+        "topo_support_constraints": (i, [vp, C.POINTER(SupportOpts), C.POINTER(SupportStats)]),
         "topo_voxel_frame": (i, [vp, i, i, ip, vp]),
         "topo_voxelize_mesh": (i, [i, vp, i, vp, i, i, ip, vp, vp, sz]),
         "topo_bitmask_to_eactive": (i, [ip, vp, i, i, i, vp]),
@@ -702,6 +725,27 @@ class Problem:
             self._ck(rc)
         return {"compliance": st.compliance, "second": st.second, "change": st.change, "relres": st.relres,
                 "iterations": st.iterations, "solve_iterations": st.solve_iterations, "ms": st.ms, "rc": rc}
+
+    # --- Heaviside projection and manufacturing constraints
+    def heaviside_project(self, beta):
+        self._ck(self.lib.topo_heaviside_project(self.h, float(beta)))
+
+    def heaviside_sensitivity(self, beta):
+        self._ck(self.lib.topo_heaviside_sensitivity(self.h, float(beta)))
+
+    def heaviside_volume_csens(self, beta, filter_radius=2.0, scale=1.0, reference_denominator=True, dst_ptr=None):
+        self._ck(self.lib.topo_heaviside_volume_csens(self.h, float(beta), int(bool(reference_denominator)),
+                                                      float(filter_radius), float(scale), dst_ptr))
+
+    def support_constraints(self, **opts):
+        """Self-support and drip constraint values; gradients in "sscsens" / "dripcsens",
+        points and normals in "surf_points" / "surf_normals"."""
+        o = dict(SUPPORT_DEFAULTS)
+        o.update(opts)
+        so = SupportOpts(*[o[f[0]] for f in SupportOpts._fields_])
+        st = SupportStats()
+        self._ck(self.lib.topo_support_constraints(self.h, C.byref(so), C.byref(st)))
+        return {f[0]: getattr(st, f[0]) for f in SupportStats._fields_}
 
     # --- files and checkpoints
     def write_array(self, name, path, fp32=False, level=0):

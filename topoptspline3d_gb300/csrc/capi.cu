@@ -1111,6 +1111,9 @@ void topo_destroy(topo_handle* h) {
     delete h->multi;
   }
   if (h->worst) worst_free(h->worst);
+  if (h->support) support_free(h->support);
+  if (h->rho_init) cudaFree(h->rho_init);
+  if (h->vsens) cudaFree(h->vsens);
   for (void* p : h->allocs) cudaFree(p);
   for (int f = 0; f < TOPO_K_COUNT; ++f)
     for (auto& e : h->evs[f]) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
@@ -1321,6 +1324,10 @@ static int array_info(topo_handle* h, int which, int level, void** dptr, size_t*
     case TOPO_EACTIVE: *dptr = L.eactive; *count = L.d.ne; *esize = 1; break;
     case TOPO_KE: *dptr = h->dKe; *count = 576; break;
     case TOPO_WORK: if (level != 0) return TOPO_E_BAD_INPUT; *dptr = h->work; *count = 3 * d0.nv; break;
+    case TOPO_RHO_INIT: if (!h->rho_init || level != 0) return TOPO_E_STATE; *dptr = h->rho_init; *count = d0.ne; break;
+    case TOPO_SSCSENS: case TOPO_DRIPCSENS: case TOPO_SURF_POINTS: case TOPO_SURF_NORMALS:
+      if (level != 0) return TOPO_E_BAD_INPUT;
+      return support_array(h->support, which, dptr, count);
     default: return TOPO_E_BAD_INPUT;
   }
   return TOPO_OK;
@@ -1875,11 +1882,14 @@ int topo_sensitivity(topo_handle* h) {
   return TOPO_OK;
 }
 
-int topo_filter(topo_handle* h, double radius) {
-  DEVICE_SCOPE(h);
-  if (!h || !(radius > 0)) return TOPO_E_BAD_INPUT;
+}  // extern "C"
+
+namespace topo {
+// Neighbour offsets and weights of the sensitivity filter for `radius`
+// (rebuilt when the radius changes).
+int handle_filter_prepare(topo_handle* h, double radius) {
+  if (!(radius > 0)) return TOPO_E_BAD_INPUT;
   if (radius > 16.0) return fail(h, TOPO_E_BAD_INPUT, "filter radius %.3g above 16 elements", radius);
-  const DevLevel& L = h->lv[0];
   if (radius != h->filt_radius) {
     std::vector<int4> offs;
     std::vector<double> w;
@@ -1902,6 +1912,17 @@ int topo_filter(topo_handle* h, double radius) {
     h->filt_n = (int)offs.size();
     h->filt_radius = radius;
   }
+  return TOPO_OK;
+}
+}  // namespace topo
+
+extern "C" {
+
+int topo_filter(topo_handle* h, double radius) {
+  DEVICE_SCOPE(h);
+  if (!h || !(radius > 0)) return TOPO_E_BAD_INPUT;
+  RET(handle_filter_prepare(h, radius));
+  const DevLevel& L = h->lv[0];
   // double-float on the FP32 pipe, sens_tmp holding the split sensitivities
   launch_filter_df(h->stream, L.d, L.eactive, h->sens, reinterpret_cast<float2*>(h->sens_tmp), h->filt_offs,
                    h->filt_wdf, h->filt_n);

@@ -79,6 +79,11 @@ struct topo_handle {
   int gprof_n[TOPO_K_COUNT] = {0};
   topo::MultiRhs* multi = nullptr;  // batched buffers (topo_multi_reserve)
   topo::WorstState* worst = nullptr;  // load region and block buffers (topo_set_load_region)
+  topo::SupportState* support = nullptr;  // surface points and constraint gradients (topo_support_constraints)
+  // Heaviside projection: rho = H(rho_init) after topo_heaviside_project
+  double* rho_init = nullptr;
+  double* vsens = nullptr;          // projected volume sensitivity before its adjoint
+  bool rho_projected = false;
   int unet_crops = 64;              // crops per harvested iterate
   cudaStream_t stream = nullptr;
   std::string err;

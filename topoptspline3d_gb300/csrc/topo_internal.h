@@ -296,8 +296,12 @@ struct LevelView {
   int device;
 };
 int handle_level_view(topo_handle* h, LevelView* out);
+int handle_filter_prepare(topo_handle* h, double radius);
 struct WorstState;
 void worst_free(WorstState* w);
+struct SupportState;
+void support_free(SupportState* s);
+int support_array(SupportState* s, int which, void** ptr, size_t* count);
 WorstState*& handle_worst_slot(topo_handle* h);
 #define RET_IF(x)                   \
   do {                              \

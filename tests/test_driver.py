@@ -84,3 +84,26 @@ def test_driver_mma_matches_oracle_history(oracle_mod):
         o.sensitivity(); o.filter(2.0); o.spline_adjoint()
         om.update(o.get("csens"), dv, [1e3 * (vol - 0.4)])
     assert np.allclose(summary["compliance"], co, rtol=1e-6, atol=0), (summary["compliance"], co)
+
+
+def test_driver_projection_needs_mma():
+    r = subprocess.run([_driver(), "--selfsupport"], capture_output=True, text=True)
+    assert r.returncode == 2 and "--optimizer mma" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_mma_with_projection_and_constraints():
+    """--optimizer mma --heaviside 4 --selfsupport: the reference's README
+    example path (projection, volume + self-support + drip constraints) runs,
+    stays finite and is repeatable."""
+    cmd = [_driver(), "--case", "cantilever", "--nx", "24", "--ny", "12", "--nz", "12", "--lattice", "9", "6", "6",
+           "--iters", "6", "--mode", "pcg64", "--optimizer", "mma", "--heaviside", "4", "--selfsupport",
+           "--surface-lattice", "24"]
+    runs = [subprocess.run(cmd, capture_output=True, text=True, timeout=300) for _ in range(2)]
+    for r in runs:
+        assert r.returncode == 0, r.stderr
+    s = [json.loads(r.stdout.strip().splitlines()[-1]) for r in runs]
+    assert s[0]["compliance"] == s[1]["compliance"]
+    assert all(np.isfinite(s[0]["compliance"]))
+    lines = [ln for ln in runs[0].stdout.splitlines() if ln.startswith("-- iter")]
+    assert len(lines) == 6 and all("ss = " in ln for ln in lines)

@@ -192,6 +192,34 @@ inline void computeSensitivity(grid::HierarchyGrid& grids, double filter_radius)
   grids[0]->ddensity2dcoeff_update();
 }
 
+// reference projectDensities(beta) (optimization/optimization.cu:313-353).
+inline void projectDensities(grid::HierarchyGrid& grids, double beta) {
+  grid::check(grids.handle(), topo_heaviside_project(grids.handle(), beta), "projectDensities");
+}
+
+// reference computeSensitivity2(beta) (optimization/optimization.cu:243-311):
+// sensitivity and the projected volume's gradient through the projection's
+// derivative, the filter and the spline adjoint (volume gradient scaled by
+// vol_scale into the VOLCSENS array).
+inline void computeSensitivity2(grid::HierarchyGrid& grids, double beta, double filter_radius, double vol_scale) {
+  grid::check(grids.handle(), topo_sensitivity(grids.handle()), "computeSensitivity2");
+  grid::check(grids.handle(), topo_heaviside_sensitivity(grids.handle(), beta), "computeSensitivity2");
+  grids[0]->filterSensitivity(filter_radius);
+  grids[0]->ddensity2dcoeff_update();
+  grid::check(grids.handle(), topo_heaviside_volume_csens(grids.handle(), beta, 1, filter_radius, vol_scale, nullptr),
+              "computeSensitivity2");
+}
+
+// reference deal_surface_points(beta) + global_selfsupp_constraint() +
+// global_drip_constraint() (optimization/optimization.cpp:1103-1127,
+// grid/Grid.cu:6101-6145, 6485-6534): the constraint values; their gradients
+// are left in the SSCSENS and DRIPCSENS arrays.
+inline topo_support_stats deal_surface_points(grid::HierarchyGrid& grids, const topo_support_opts& o) {
+  topo_support_stats st{};
+  grid::check(grids.handle(), topo_support_constraints(grids.handle(), &o, &st), "deal_surface_points");
+  return st;
+}
+
 // reference updateCoeff(Vgoal) (optimization/optimization.cu:589-695); returns the multiplier.
 inline double updateCoeff(grid::HierarchyGrid& grids, double vgoal, double damp = 0.5, double step = 0.03,
                           double cmin = 0.0, double cmax = 1.0, bool reference_double_step = false) {

@@ -5,10 +5,16 @@
 //   topopt_driver [--case cantilever|mbb] [--nx N --ny N --nz N] [--iters K]
 //                 [--mode vcycle|pcg64|mixed] [--vf 0.4] [--filter 2] [--order 3]
 //                 [--lattice LX LY LZ] [--optimizer oc|mma]
+//                 [--heaviside BETA] [--selfsupport] [--print-angle R]
+//                 [--ss-mode M] [--drip-mode M] [--surface-lattice N]
 //
 // --optimizer mma runs the loop of TestSuit::testOrdinarySplineTopoptMMA
 // (utils/test_utils.cpp:972-1217): MMA on the coefficients with the volume
 // constraint 1e3 * (vol - vf) <= 0 and coefficient bounds [1e-3, 1].
+// --heaviside projects the density (ENABLE_HEAVISIDE: beta doubled every 10
+// iterations up to 32) and --selfsupport adds the self-support and drip
+// constraints (ENABLE_SELFSUPPORT: scales 1e-1 / 1e2, raised to 1e0 / 1e3
+// after 30 iterations and 1e1 / 1e4 after 80).
 //
 // Prints one line per design iteration and a JSON summary line.
 #include <chrono>
@@ -30,6 +36,10 @@ struct Args {
   std::string mode = "mixed";
   std::string optimizer = "oc";
   double vf = 0.4, filter = 2.0;
+  double heaviside = 0.0;        // initial beta (0 = no projection)
+  bool selfsupport = false;
+  double print_angle = 0.75;     // in units of pi
+  int ss_mode = 4, drip_mode = 6, surface_lattice = 64;
 };
 
 Args parse(int argc, char** argv) {
@@ -51,9 +61,19 @@ Args parse(int argc, char** argv) {
     else if (s == "--order") a.order = std::atoi(next());
     else if (s == "--lattice") { for (int k = 0; k < 3; ++k) a.lattice[k] = std::atoi(next()); }
     else if (s == "--optimizer") a.optimizer = next();
+    else if (s == "--heaviside") a.heaviside = std::atof(next());
+    else if (s == "--selfsupport") a.selfsupport = true;
+    else if (s == "--print-angle") a.print_angle = std::atof(next());
+    else if (s == "--ss-mode") a.ss_mode = std::atoi(next());
+    else if (s == "--drip-mode") a.drip_mode = std::atoi(next());
+    else if (s == "--surface-lattice") a.surface_lattice = std::atoi(next());
     else { std::fprintf(stderr, "unknown argument %s\n", s.c_str()); std::exit(2); }
   }
   if (a.optimizer != "oc" && a.optimizer != "mma") { std::fprintf(stderr, "--optimizer oc|mma\n"); std::exit(2); }
+  if ((a.selfsupport || a.heaviside > 0) && a.optimizer != "mma") {
+    std::fprintf(stderr, "--heaviside and --selfsupport need --optimizer mma\n");
+    std::exit(2);
+  }
   return a;
 }
 
@@ -116,12 +136,21 @@ int main(int argc, char** argv) {
     std::unique_ptr<MMA::mma_t> mma;
     double* dcoeff = nullptr;
     double* dvol = nullptr;
+    const int ncon = a.selfsupport ? 3 : 1;
+    double beta = a.heaviside;
+    double ss_scale = 1e-1, drip_scale = 1e2;  // SSScale, dripScale (utils/test_utils.cpp:1058-1061)
+    topo_support_opts sup{};
+    sup.lattice = a.surface_lattice;
+    sup.max_points = 200000;
+    sup.print_angle = a.print_angle;
+    sup.ss_mode = a.ss_mode;
+    sup.drip_mode = a.drip_mode;
     if (use_mma) {
-      mma.reset(new MMA::mma_t(grids, 1));
+      mma.reset(new MMA::mma_t(grids, ncon));
       mma->init(1e-3, 1.0);
       dcoeff = static_cast<double*>(grids[0]->devicePtr(TOPO_COEFF));
       dvol = static_cast<double*>(grids[0]->devicePtr(TOPO_VOLCSENS));
-      grid::check(grids.handle(), topo_volume_csens(grids.handle(), 1, vol_scale, nullptr), "dvol2dcoeff");
+      if (beta <= 0) grid::check(grids.handle(), topo_volume_csens(grids.handle(), 1, vol_scale, nullptr), "dvol2dcoeff");
     }
     for (int itn = 1; itn <= a.iters; ++itn) {
       const auto t0 = std::chrono::steady_clock::now();
@@ -129,16 +158,42 @@ int main(int argc, char** argv) {
       if (use_mma) {
         mma->get_x(dcoeff);  // setCoeff(mma.get_x())
         grids[0]->coeff2density();
+        if (beta > 0) projectDensities(grids, beta);
         vol = grids[0]->volumeRatio();
       }
       grids.update_stencil();
       topo_solve_stats st = grids.solve(so);
       const double c = grids[0]->compliance();
-      computeSensitivity(grids, a.filter);
+      topo_support_stats sst{};
+      if (a.selfsupport) {
+        if (itn > 80) { ss_scale = 1e1; drip_scale = 1e4; }
+        else if (itn > 30) { ss_scale = 1e0; drip_scale = 1e3; }
+        sup.beta = beta > 0 ? beta : 4.0;
+        sst = deal_surface_points(grids, sup);
+      }
+      if (beta > 0) computeSensitivity2(grids, beta, a.filter, vol_scale);
+      else computeSensitivity(grids, a.filter);
       if (use_mma) {
-        const double g = vol_scale * (vol - a.vf);
-        const double* dg[1] = {dvol};
-        mma->update(static_cast<const double*>(grids[0]->devicePtr(TOPO_CSENS)), dg, &g);
+        std::vector<double> g = {vol_scale * (vol - a.vf)};
+        std::vector<const double*> dg = {dvol};
+        if (a.selfsupport) {
+          // the constraint gradients scaled in place (scaleVector in the reference)
+          double* dss = static_cast<double*>(grids[0]->devicePtr(TOPO_SSCSENS));
+          double* ddr = static_cast<double*>(grids[0]->devicePtr(TOPO_DRIPCSENS));
+          std::vector<double> hv(grids[0]->n_cijk());
+          grid::check(grids.handle(), topo_get_array(grids.handle(), TOPO_SSCSENS, 0, hv.data(), hv.size()), "ss");
+          for (double& v : hv) v *= ss_scale;
+          grid::check(grids.handle(), topo_put_array(grids.handle(), TOPO_SSCSENS, 0, hv.data(), hv.size()), "ss");
+          grid::check(grids.handle(), topo_get_array(grids.handle(), TOPO_DRIPCSENS, 0, hv.data(), hv.size()), "drip");
+          for (double& v : hv) v *= drip_scale;
+          grid::check(grids.handle(), topo_put_array(grids.handle(), TOPO_DRIPCSENS, 0, hv.data(), hv.size()), "drip");
+          g.push_back(ss_scale * (sst.ss_value - 1.0));
+          g.push_back(drip_scale * sst.drip_value);
+          dg.push_back(dss);
+          dg.push_back(ddr);
+        }
+        mma->update(static_cast<const double*>(grids[0]->devicePtr(TOPO_CSENS)), dg.data(), g.data());
+        if (beta > 0 && itn % 10 == 0 && itn > 2 && beta < 32) beta *= 2;  // utils/test_utils.cpp:1174-1177
       } else {
         updateCoeff(grids, a.vf);
         vol = grids[0]->volumeRatio();
@@ -146,8 +201,10 @@ int main(int argc, char** argv) {
       const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       total_ms += ms;
       crec.push_back(c);
-      std::printf("-- iter %3d  c = %.10e  v = %.6f  its = %d  r = %.2e  %.2f ms\n", itn, c, vol, st.iterations,
+      std::printf("-- iter %3d  c = %.10e  v = %.6f  its = %d  r = %.2e  %.2f ms", itn, c, vol, st.iterations,
                   st.relres, ms);
+      if (a.selfsupport) std::printf("  ss = %.6f  drip = %.3e  points = %d", sst.ss_value, sst.drip_value, sst.points);
+      std::printf("\n");
     }
     std::printf("{\"driver\": \"topopt_driver\", \"case\": \"%s\", \"grid\": [%d, %d, %d], \"iters\": %d, "
                 "\"mode\": \"%s\", \"optimizer\": \"%s\", \"ms_per_iter\": %.4f, \"compliance\": [",

@@ -546,22 +546,27 @@ typedef struct topo_support_stats {
 int topo_support_constraints(topo_handle* h, const topo_support_opts* opts, topo_support_stats* stats);
 
 /* --- learned preconditioner (U-Net) --------------------------------------- */
-/* A 3-level 3D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, 245,203
+/* A 3-level 3D convolutional U-Net (16/32/64 channels, 3x3x3 kernels, 246,931
  * effective parameters, bf16 weights, fp32 accumulation) corrects the FP32
- * multigrid preconditioner of TOPO_SOLVE_MIXED: z = V(r) + rms(V(r)) N(r/rms(r),
- * log rho).  It is trained with the library's own forward, backward and Adam
- * kernels on crops harvested from the solver's iterates (target (e_k - z_k)/rms(z_k),
- * e_k = u* - u_k).  The last layer starts at zero (N = 0: the plain V-cycle).
- * No reference counterpart. */
+ * multigrid preconditioner of TOPO_SOLVE_MIXED: with z = V(r),
+ * z' = z + beta lz N(s(r/lr), s(z/lz), log rho), lr and lz the local rms of r
+ * and z (blocks of 8^3 vertices, floored at 1e-2 of the global rms),
+ * s(x) = x/(1+|x|/8), and beta the energy-optimal amount of the correction
+ * c = lz N, beta = c.(r - A z) / c.(A c) (beta = 0 keeps z).  It is trained with
+ * the library's own forward, backward and Adam kernels (clipped gradients,
+ * warm-up and cosine step size) on crops harvested from the solver's iterates
+ * (target (e_k - z_k)/lz_k, e_k = u* - u_k).  The last layer starts at zero
+ * (N = 0: the plain V-cycle).  No reference counterpart. */
 /* Creates the network of h with He-normal weights from `seed`. */
 int topo_unet_enable(topo_handle* h, unsigned long long seed);
 /* Parameter count of the flat fp32 layout: per layer W[cout][27][cin] then b[cout],
  * layers L0a L0b L1a L1b L2a L2b D1a D1b D0a D0b (cin of L0a padded to 16 with
- * channels 0-3 used, cout of D0b 16 with channels 0-2 used). */
+ * channels 0-7 used, cout of D0b 16 with channels 0-2 used). */
 int topo_unet_num_params(size_t* n);
 int topo_unet_get_params(topo_handle* h, float* dst, size_t n);
 int topo_unet_set_params(topo_handle* h, const float* src, size_t n);
-/* Host-tensor passes: x [nb][Z][Y][X][4] (residual xyz, log-density), X, Y, Z
+/* Host-tensor passes: x [nb][Z][Y][X][8] (residual xyz, V-cycle output xyz,
+ * log-density, 0; residual and output in local units), X, Y, Z
  * multiples of 8; y [..][3] network output; loss = sum m (y - t)^2 / sum m t^2
  * over DOFs with mask bit c set; grad [n] its parameter gradient. */
 int topo_unet_forward(topo_handle* h, int X, int Y, int Z, int nb, const float* x, float* y);
@@ -571,7 +576,7 @@ int topo_unet_loss_grad(topo_handle* h, int X, int Y, int Z, int nb, const float
  * each harvesting solve adds crops_per_iterate crops per recorded iterate. */
 int topo_unet_dataset_reserve(topo_handle* h, int capacity, int crop, int crops_per_iterate);
 int topo_unet_dataset_size(topo_handle* h, int* n);
-/* Host copy of crop `slot`: x [crop^3][4], t [crop^3][3], mask [crop^3] (crop
+/* Host copy of crop `slot`: x [crop^3][8], t [crop^3][3], mask [crop^3] (crop
  * side returned in *crop; size the arrays for the reserved side). */
 int topo_unet_dataset_get(topo_handle* h, int slot, float* x, float* t, uint8_t* mask, int* crop);
 /* `steps` Adam steps (update = 1) or evaluations (update = 0) on random batches

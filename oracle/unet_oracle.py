@@ -12,7 +12,7 @@ from __future__ import annotations
 import numpy as np
 
 # (cin, cout, relu, cin_real, cout_real), same order as unet.cu
-LAYERS = [(16, 16, 1, 4, 16), (16, 16, 1, 16, 16), (16, 32, 1, 16, 32), (32, 32, 1, 32, 32),
+LAYERS = [(16, 16, 1, 8, 16), (16, 16, 1, 16, 16), (16, 32, 1, 16, 32), (32, 32, 1, 32, 32),
           (32, 64, 1, 32, 64), (64, 32, 1, 64, 32), (64, 32, 1, 64, 32), (32, 16, 1, 32, 16),
           (32, 16, 1, 32, 16), (16, 16, 0, 16, 3)]
 L0A, L0B, L1A, L1B, L2A, L2B, D1A, D1B, D0A, D0B = range(10)
@@ -125,11 +125,11 @@ class UNetOracle:
             y = np.maximum(y, 0.0)
         return self.r(y)
 
-    def forward(self, x4):
-        """x4 [nb, Z, Y, X, 4] -> output [nb, Z, Y, X, 3]; keeps activations."""
+    def forward(self, x8):
+        """x8 [nb, Z, Y, X, 8] -> output [nb, Z, Y, X, 3]; keeps activations."""
         r = self.r
-        x0 = np.zeros(x4.shape[:4] + (16,))
-        x0[..., :4] = x4
+        x0 = np.zeros(x8.shape[:4] + (16,))
+        x0[..., :8] = x8
         x0 = r(x0)
         a = {}
         a["x0"] = x0
@@ -150,9 +150,9 @@ class UNetOracle:
         self.a = a
         return a[D0B][..., :3]
 
-    def loss_grad(self, x4, t, m):
+    def loss_grad(self, x8, t, m):
         """Relative loss sum m (y - t)^2 / sum m t^2 and the flat parameter gradient."""
-        y = self.forward(x4)
+        y = self.forward(x8)
         mb = np.stack([(m >> c) & 1 for c in range(3)], axis=-1).astype(np.float64)
         den = float((mb * t * t).sum())
         loss = float((mb * (y - t) ** 2).sum()) / den

@@ -15,15 +15,16 @@ from oracle import unet_oracle as uo
 def _inputs(shape, seed):
     rng = np.random.default_rng(seed)
     nb, Z, Y, X = shape
-    x = rng.standard_normal((nb, Z, Y, X, 4))
-    x[..., 3] = rng.uniform(-0.5, 0.5, (nb, Z, Y, X))
+    x = rng.standard_normal((nb, Z, Y, X, 8))
+    x[..., 6] = rng.uniform(-0.5, 0.5, (nb, Z, Y, X))
+    x[..., 7] = 0.0
     t = rng.standard_normal((nb, Z, Y, X, 3)) * 0.3
     m = rng.integers(0, 16, (nb, Z, Y, X)).astype(np.uint8) | 7
     return x, t, m
 
 
 def test_parameter_count():
-    assert uo.effective_params() == 245_203
+    assert uo.effective_params() == 246_931
     from topoptspline3d_gb300 import capi
     assert capi.Problem.unet_num_params() == uo.num_params()
 

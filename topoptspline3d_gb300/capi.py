@@ -24,6 +24,7 @@ ARRAYS = {"rho": 0, "rhop": 1, "coeff": 2, "sens": 3, "csens": 4, "u": 5, "f": 6
 BYTE_ARRAYS = {"vmask", "eactive"}
 
 SOLVE_VCYCLE, SOLVE_PCG64, SOLVE_MIXED = 0, 1, 2
+UNET_IN = 8  # network input channels: r xyz, z xyz (local units), log-density, 0
 SMOOTH_GS, SMOOTH_CHEBYSHEV = 0, 1
 K_FINE_APPLY64, K_FINE_APPLY32, K_FINE_SMOOTH64, K_FINE_SMOOTH32 = 0, 1, 2, 3
 
@@ -660,7 +661,7 @@ class Problem:
         self._ck(self.lib.topo_unet_set_params(self.h, p.ctypes.data, p.size))
 
     def unet_forward(self, x):
-        """x [nb, Z, Y, X, 4] float32 -> [nb, Z, Y, X, 3]."""
+        """x [nb, Z, Y, X, 8] float32 (r xyz, z xyz, log-density, 0) -> [nb, Z, Y, X, 3]."""
         x = np.ascontiguousarray(x, dtype=np.float32)
         nb, Z, Y, X, _ = x.shape
         y = np.zeros((nb, Z, Y, X, 3), dtype=np.float32)
@@ -688,7 +689,7 @@ class Problem:
 
     def unet_dataset_get(self, slot, crop=32):
         per = crop ** 3
-        x = np.zeros((per, 4), dtype=np.float32)
+        x = np.zeros((per, UNET_IN), dtype=np.float32)
         t = np.zeros((per, 3), dtype=np.float32)
         m = np.zeros(per, dtype=np.uint8)
         side = C.c_int()
@@ -696,7 +697,7 @@ class Problem:
                                                 C.byref(side)))
         assert side.value == crop
         s3 = (crop, crop, crop)
-        return x.reshape(s3 + (4,)), t.reshape(s3 + (3,)), m.reshape(s3)
+        return x.reshape(s3 + (UNET_IN,)), t.reshape(s3 + (3,)), m.reshape(s3)
 
     def unet_train(self, steps, batch=8, lr=1e-3, seed=1, lo=0, hi=0, update=True) -> float:
         loss = C.c_double()

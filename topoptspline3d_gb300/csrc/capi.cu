@@ -1689,7 +1689,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
     }
     auto net = [&](const float* r32, float* z32) -> int {
       if (!net_on) return TOPO_OK;
-      const cudaError_t e = unet_apply(h->unet, h->stream, L0.d, L0.vmask, r32, z32, h->partial);
+      const cudaError_t e = unet_apply(h->unet, h->stream, L0.d, L0.vmask, h->rhop32, h->tz32, r32, z32, h->partial);
       if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "U-Net apply: %s", cudaGetErrorString(e));
       ++st.learned_applied;
       return TOPO_OK;

@@ -401,12 +401,19 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ W, int cin, int
 
 // Adam on fp32 master weights, bf16 copy for the kernels (bias-corrected,
 // Kingma & Ba 2015, Algorithm 1).
+// Adam step; with gn2 (the gradient's squared norm) the gradient is scaled to
+// a norm of at most clip.
 __global__ void k_adam(int64_t n, const float* __restrict__ grad, float lr, float b1, float b2, float eps, float c1,
                        float c2, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
-                       __nv_bfloat16* __restrict__ wb) {
+                       __nv_bfloat16* __restrict__ wb, const double* __restrict__ gn2, float clip) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float g = grad[i];
+  float sc = 1.f;
+  if (gn2) {
+    const double nrm = sqrt(*gn2);
+    if (nrm > clip) sc = (float)(clip / nrm);
+  }
+  const float g = grad[i] * sc;
   const float mi = b1 * m[i] + (1.f - b1) * g;
   const float vi = b2 * v[i] + (1.f - b2) * g * g;
   m[i] = mi;
@@ -512,9 +519,9 @@ void unet_flip(cudaStream_t s, const __nv_bfloat16* W, int cin, int cout, __nv_b
 }
 
 void unet_adam(cudaStream_t s, int64_t n, const float* grad, float lr, float b1, float b2, float eps, int step,
-               float* w, float* m, float* v, __nv_bfloat16* wb) {
+               float* w, float* m, float* v, __nv_bfloat16* wb, const double* gn2, float clip) {
   const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-  k_adam<<<nblk64(n, 256), 256, 0, s>>>(n, grad, lr, b1, b2, eps, c1, c2, w, m, v, wb);
+  k_adam<<<nblk64(n, 256), 256, 0, s>>>(n, grad, lr, b1, b2, eps, c1, c2, w, m, v, wb, gn2, clip);
 }
 
 void unet_to_bf16(cudaStream_t s, const float* a, int64_t n, __nv_bfloat16* b) {

@@ -328,7 +328,8 @@ cudaError_t unet_set_params(UNetState* u, cudaStream_t s, const float* host);
 cudaError_t unet_get_params(UNetState* u, cudaStream_t s, float* host);
 cudaError_t unet_prepare(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* eactive, const double* rho,
                          double rho_min);
-cudaError_t unet_apply(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* vmask, const float* r, float* z,
+cudaError_t unet_apply(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* vmask, const float* rhop32,
+                       int tz, const float* r, float* z,
                        double* partial);
 cudaError_t unet_rejected(UNetState* u, cudaStream_t s, int* out);
 cudaError_t unet_harvest_record(UNetState* u, cudaStream_t s, int64_t n3, const double* r, const float* z,

@@ -1,21 +1,28 @@
 // Learned preconditioner: network definition, training and application.
 //
 // U-Net on the vertex grid (3 levels, 16/32/64 channels, 3x3x3 kernels):
-//   L0a conv 16->16 relu (input: r/rms(r) xyz, log-density, 12 zero channels)
+//   L0a conv 16->16 relu (input: r/lr xyz, z/lz xyz, log-density, 9 zero channels)
 //   L0b conv 16->16 relu                      -> s0
 //   pool -> L1a conv 16->32 relu, L1b conv 32->32 relu -> s1
 //   pool -> L2a conv 32->64 relu, L2b conv 64->32 relu -> b2
 //   D1a conv [up(b2), s1] 64->32 relu, D1b conv 32->16 relu -> d1
 //   D0a conv [up(d1), s0] 32->16 relu, D0b conv 16->16 (channels 0-2 used)
-// 245,203 effective parameters (3x3x3 kernels on the real input and output
+// 246,931 effective parameters (3x3x3 kernels on the real input and output
 // channels plus biases).  Weights are stored in fp32 (Adam master copy) and
 // bf16 (what the tensor cores read); activations are bf16, accumulation fp32.
 //
 // The network corrects the FP32 multigrid preconditioner of the mixed solver:
-//   z = V(r) + rms(V(r)) * N(s(r / rms(r)), log rho),  s(x) = x / (1 + |x|/8)
-// and is trained on pairs harvested from the solver's own iterates: for a
-// residual r_k with V-cycle output z_k and error e_k = u* - u_k, the target is
-// (e_k - z_k) / rms(z_k).  Its last layer starts at zero, so an untrained
+//   z' = z + beta lz * N(s(r / lr), s(z / lz), log rho),  z = V(r),  s(x) = x / (1 + |x|/8)
+// with lr, lz the local rms of r and z (over blocks of 8^3 vertices, floored at
+// 1e-2 of the global rms), and the correction c = lz * N taken in the amount
+// that minimises the energy norm of the error: beta = c.(r - A z) / c.(A c)
+// (two FP32 operator applications; beta = 0 keeps z, so the correction never
+// makes the error larger in that norm).  Every input and the target are in
+// local units, so crops from stiff and soft regions, loads and far field have
+// targets of the same size, and the network sees the V-cycle output it
+// corrects.  It is trained on pairs harvested from the solver's own iterates:
+// for a residual r_k with V-cycle output z_k and error e_k = u* - u_k, the
+// target is (e_k - z_k) / lz_k.  Its last layer starts at zero, so an untrained
 // network leaves the V-cycle unchanged.
 #include <cuda_bf16.h>
 
@@ -44,15 +51,17 @@ void unet_up_bwd(cudaStream_t s, const float* dfull, int X, int Y, int Z, int nb
 void unet_slice(cudaStream_t s, const float* src, int64_t nvox, int cfull, int c0, int c, int accumulate, float* dst);
 void unet_flip(cudaStream_t s, const __nv_bfloat16* W, int cin, int cout, __nv_bfloat16* Wt);
 void unet_adam(cudaStream_t s, int64_t n, const float* grad, float lr, float b1, float b2, float eps, int step,
-               float* w, float* m, float* v, __nv_bfloat16* wb);
+               float* w, float* m, float* v, __nv_bfloat16* wb, const double* gn2 = nullptr, float clip = 1.f);
 void unet_to_bf16(cudaStream_t s, const float* a, int64_t n, __nv_bfloat16* b);
 
 namespace {
 
-constexpr int kIn = 16;  // padded input channels (3 residual + 1 log-density used)
+constexpr int kIn = 16;     // padded input channels
+constexpr int kInUsed = 8;  // stored input channels: r xyz, z xyz, log-density, 0
+constexpr int kBlk = 8;     // vertex block side of the local rms
 enum { L0A, L0B, L1A, L1B, L2A, L2B, D1A, D1B, D0A, D0B, NLAYER };
 struct LayerDef { int cin, cout, relu, cin_real, cout_real; };
-constexpr LayerDef kDef[NLAYER] = {{kIn, 16, 1, 4, 16},  {16, 16, 1, 16, 16}, {16, 32, 1, 16, 32},
+constexpr LayerDef kDef[NLAYER] = {{kIn, 16, 1, kInUsed, 16},  {16, 16, 1, 16, 16}, {16, 32, 1, 16, 32},
                                    {32, 32, 1, 32, 32},  {32, 64, 1, 32, 64}, {64, 32, 1, 64, 32},
                                    {64, 32, 1, 64, 32},  {32, 16, 1, 32, 16}, {32, 16, 1, 32, 16},
                                    {16, 16, 0, 16, 3}};
@@ -96,17 +105,66 @@ __global__ void k_vertex_logrho(LevelDims d, const uint8_t* __restrict__ eactive
   lr[v] = (float)(l / 3.0 + 0.5);
 }
 
-// z[c][v] += s * out[v'][c] on free DOFs.
+// z[c][v] += lz[v] * out[v'][c] on free DOFs.
 __global__ void k_unpack_add(LevelDims d, int X, int Y, const __nv_bfloat16* __restrict__ out, const uint8_t* vmask,
-                             const float* __restrict__ s_dev, float* __restrict__ z) {
+                             const float* __restrict__ lz, float* __restrict__ z) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= d.nv) return;
   const int x = (int)(v % d.vx), y = (int)((v / d.vx) % d.vy), zz = (int)(v / ((int64_t)d.vx * d.vy));
   const int64_t u = ((int64_t)zz * Y + y) * X + x;
   const uint8_t m = vmask[v];
-  const float s = *s_dev;
+  const float s = lz[v];
   for (int k = 0; k < 3; ++k)
     if ((m >> k) & 1) z[k * d.nv + v] += s * __bfloat162float(out[u * 16 + k]);
+}
+
+// Mean square of a [3][nv] field over each block of kBlk^3 vertices.
+__global__ void k_block_ms(LevelDims d, const float* __restrict__ f, float* __restrict__ blk) {
+  const int nbx = (d.vx + kBlk - 1) / kBlk, nby = (d.vy + kBlk - 1) / kBlk, nbz = (d.vz + kBlk - 1) / kBlk;
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (int64_t)nbx * nby * nbz) return;
+  const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((int64_t)nbx * nby));
+  double s = 0;
+  int n = 0;
+  for (int z = bz * kBlk; z < min(d.vz, (bz + 1) * kBlk); ++z)
+    for (int y = by * kBlk; y < min(d.vy, (by + 1) * kBlk); ++y)
+      for (int x = bx * kBlk; x < min(d.vx, (bx + 1) * kBlk); ++x) {
+        const int64_t v = x + (int64_t)d.vx * (y + (int64_t)d.vy * z);
+        for (int k = 0; k < 3; ++k) s += (double)f[k * d.nv + v] * f[k * d.nv + v];
+        n += 3;
+      }
+  blk[b] = (float)(s / max(n, 1));
+}
+
+// Local rms per vertex: its block's rms, floored at 1e-2 of the global rms
+// (gsum = sum of squares over the 3 nv entries).
+__global__ void k_local_rms(LevelDims d, const float* __restrict__ blk, const double* __restrict__ gsum,
+                            float* __restrict__ out) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.nv) return;
+  const int nbx = (d.vx + kBlk - 1) / kBlk, nby = (d.vy + kBlk - 1) / kBlk;
+  const int x = (int)(v % d.vx), y = (int)((v / d.vx) % d.vy), z = (int)(v / ((int64_t)d.vx * d.vy));
+  const int64_t b = x / kBlk + (int64_t)nbx * (y / kBlk + (int64_t)nby * (z / kBlk));
+  const double floor2 = 1e-4 * (*gsum / (3.0 * d.nv));
+  const double ms = fmax((double)blk[b], floor2);
+  out[v] = ms > 0 ? (float)sqrt(ms) : 1.f;
+}
+
+// a <- b - a
+__global__ void k_sub_into(int64_t n, const float* __restrict__ b, float* __restrict__ a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = b[i] - a[i];
+}
+
+// z += beta c, beta = num / den clamped to [-2, 2] (0 if den <= 0); beta kept in *beta_out.
+__global__ void k_axpy_ratio(int64_t n, const double* __restrict__ num, const double* __restrict__ den,
+                             const float* __restrict__ c, float* __restrict__ z, double* __restrict__ beta_out) {
+  const double dd = *den;
+  double beta = dd > 0 ? *num / dd : 0.0;
+  beta = fmin(fmax(beta, -2.0), 2.0);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) z[i] += (float)beta * c[i];
+  if (i == 0) *beta_out = beta;
 }
 
 // Positivity guard: if r.z <= 0 after the correction, restore the plain
@@ -120,28 +178,25 @@ __global__ void k_guard(int64_t n, const double* __restrict__ rz, const float* _
   }
 }
 
-// sqrt(sum/n) of a device scalar into an fp32 device scalar (and its inverse).
-__global__ void k_rms(const double* __restrict__ sum, double n, float* __restrict__ out, float* __restrict__ inv) {
-  const double r = sqrt(*sum / n);
-  *out = (float)r;
-  *inv = r > 0 ? (float)(1.0 / r) : 0.f;
-}
-
-// Full-grid network input: channels 0-2 = r / rms(r), 3 = log-density, 4-15 = 0.
-template <typename T>
-__global__ void k_pack_input_dev(LevelDims d, int X, int Y, int Z, const T* __restrict__ r,
-                                 const float* __restrict__ inv_s, const float* __restrict__ lr,
+// Full-grid network input: channels 0-2 = s(r / lr), 3-5 = s(z / lz),
+// 6 = log-density, 7-15 = 0.
+__global__ void k_pack_input_dev(LevelDims d, int X, int Y, int Z, const float* __restrict__ r,
+                                 const float* __restrict__ zin, const float* __restrict__ lrr,
+                                 const float* __restrict__ lzz, const float* __restrict__ lr,
                                  __nv_bfloat16* __restrict__ x0) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)X * Y * Z) return;
-  const float is = *inv_s;
   const int x = (int)(i % X), y = (int)((i / X) % Y), z = (int)(i / ((int64_t)X * Y));
   __align__(16) __nv_bfloat16 c[16];
   for (int k = 0; k < 16; ++k) c[k] = __float2bfloat16_rn(0.f);
   if (x < d.vx && y < d.vy && z < d.vz) {
     const int64_t v = x + (int64_t)d.vx * (y + (int64_t)d.vy * z);
-    for (int k = 0; k < 3; ++k) c[k] = __float2bfloat16_rn(squash((float)r[k * d.nv + v] * is));
-    c[3] = __float2bfloat16_rn(lr[v]);
+    const float ir = 1.f / lrr[v], iz = 1.f / lzz[v];
+    for (int k = 0; k < 3; ++k) {
+      c[k] = __float2bfloat16_rn(squash(r[k * d.nv + v] * ir));
+      c[3 + k] = __float2bfloat16_rn(squash(zin[k * d.nv + v] * iz));
+    }
+    c[6] = __float2bfloat16_rn(lr[v]);
   }
   uint4* dst = reinterpret_cast<uint4*>(x0 + i * 16);
   dst[0] = reinterpret_cast<const uint4*>(c)[0];
@@ -149,11 +204,11 @@ __global__ void k_pack_input_dev(LevelDims d, int X, int Y, int Z, const T* __re
 }
 
 // Crop extraction: crop j (origin org[j]) of side S into dataset slot slot0 + j:
-// X[slot][v][4] = (r * inv_r, lr), T[slot][v][3] = t * inv_t, M[slot][v] = vmask.
+// X[slot][v][8] = (s(r/lr), s(z/lz), log-density, 0), T[slot][v][3] = t / lz, M[slot][v] = vmask.
 __global__ void k_crop(LevelDims d, int S, const int* __restrict__ org, int ncrop, int slot0,
-                       const float* __restrict__ r, const float* __restrict__ t, const float* __restrict__ lr,
-                       const uint8_t* __restrict__ vmask, const float* __restrict__ inv_r,
-                       const float* __restrict__ inv_t, __nv_bfloat16* __restrict__ DX, float* __restrict__ DT,
+                       const float* __restrict__ r, const float* __restrict__ zk, const float* __restrict__ t,
+                       const float* __restrict__ lrr, const float* __restrict__ lzz, const float* __restrict__ lr,
+                       const uint8_t* __restrict__ vmask, __nv_bfloat16* __restrict__ DX, float* __restrict__ DT,
                        uint8_t* __restrict__ DM) {
   const int64_t per = (int64_t)S * S * S;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -163,22 +218,21 @@ __global__ void k_crop(LevelDims d, int S, const int* __restrict__ org, int ncro
   const int cx = (int)(q % S), cy = (int)((q / S) % S), cz = (int)(q / ((int64_t)S * S));
   const int x = org[3 * j] + cx, y = org[3 * j + 1] + cy, z = org[3 * j + 2] + cz;
   const int64_t o = (int64_t)(slot0 + j) * per + q;
-  float rv[3] = {0, 0, 0}, tv[3] = {0, 0, 0}, l = 0;
+  float in[kInUsed] = {0, 0, 0, 0, 0, 0, 0, 0}, tv[3] = {0, 0, 0};
   uint8_t m = 0;
   if (x < d.vx && y < d.vy && z < d.vz) {
     const int64_t v = x + (int64_t)d.vx * (y + (int64_t)d.vy * z);
     m = vmask[v];
-    l = lr[v];
+    const float ir = 1.f / lrr[v], iz = 1.f / lzz[v];
     for (int k = 0; k < 3; ++k) {
-      rv[k] = squash(r[k * d.nv + v] * *inv_r);
-      tv[k] = t[k * d.nv + v] * *inv_t;
+      in[k] = squash(r[k * d.nv + v] * ir);
+      in[3 + k] = squash(zk[k * d.nv + v] * iz);
+      tv[k] = t[k * d.nv + v] * iz;
     }
+    in[6] = lr[v];
   }
-  for (int k = 0; k < 3; ++k) {
-    DX[o * 4 + k] = __float2bfloat16_rn(rv[k]);
-    DT[o * 3 + k] = tv[k];
-  }
-  DX[o * 4 + 3] = __float2bfloat16_rn(l);
+  for (int k = 0; k < kInUsed; ++k) DX[o * kInUsed + k] = __float2bfloat16_rn(in[k]);
+  for (int k = 0; k < 3; ++k) DT[o * 3 + k] = tv[k];
   DM[o] = m;
 }
 
@@ -192,7 +246,7 @@ __global__ void k_gather(int64_t per, const int* __restrict__ idx, int nb, const
   const int64_t q = i - b * per, s = (int64_t)idx[b] * per + q;
   __align__(16) __nv_bfloat16 c[16];
   for (int k = 0; k < 16; ++k) c[k] = __float2bfloat16_rn(0.f);
-  for (int k = 0; k < 4; ++k) c[k] = DX[s * 4 + k];
+  for (int k = 0; k < kInUsed; ++k) c[k] = DX[s * kInUsed + k];
   uint4* dst = reinterpret_cast<uint4*>(x0 + i * 16);
   dst[0] = reinterpret_cast<const uint4*>(c)[0];
   dst[1] = reinterpret_cast<const uint4*>(c)[1];
@@ -200,11 +254,11 @@ __global__ void k_gather(int64_t per, const int* __restrict__ idx, int nb, const
   M[i] = DM[s];
 }
 
-// Host-tensor input: x[v][4] fp32 -> x0[v][16] bf16.
+// Host-tensor input: x[v][8] fp32 -> x0[v][16] bf16.
 __global__ void k_expand_input(int64_t n, const float* __restrict__ x, __nv_bfloat16* __restrict__ x0) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  for (int k = 0; k < 16; ++k) x0[i * 16 + k] = __float2bfloat16_rn(k < 4 ? x[i * 4 + k] : 0.f);
+  for (int k = 0; k < 16; ++k) x0[i * 16 + k] = __float2bfloat16_rn(k < kInUsed ? x[i * kInUsed + k] : 0.f);
 }
 
 __global__ void k_extract_output(int64_t n, const __nv_bfloat16* __restrict__ out, float* __restrict__ y) {
@@ -316,8 +370,7 @@ struct UNetState {
   float* part = nullptr;    // weight-gradient partials
   float* bpart = nullptr;   // bias-gradient partials
   double *lpart = nullptr, *lres = nullptr, *loss_log = nullptr;
-  float* scal = nullptr;    // [0] rms(r), [1] 1/rms(r), [2] rms(z), [3] 1/rms(z)
-  double* dsum = nullptr;   // reduction outputs (2 doubles)
+  double* dsum = nullptr;   // reduction outputs (4 doubles)
   double* dpart = nullptr;  // reduction partials
   int step = 0;
   int groups = 16;
@@ -331,6 +384,9 @@ struct UNetState {
   int* didx = nullptr;
   // harvest buffers
   float* lr = nullptr;     // vertex log-density [nv]
+  float *lfr = nullptr, *lfz = nullptr;  // local rms of r and z per vertex [nv]
+  float* blk = nullptr;                  // block mean squares
+  float *cbuf = nullptr, *az = nullptr, *ac = nullptr;  // correction, A z, A c [3nv]
   float* zsave = nullptr;  // plain V-cycle output kept for the positivity guard [3nv]
   int* reject = nullptr;   // sticky flag: the guard restored the plain output
   std::vector<float*> hr, hz, hx;
@@ -387,7 +443,6 @@ static cudaError_t unet_new(UNetState** out) {
   UCK(u->alloc(&u->lres, 8));
   UCK(cudaMemset(u->lres, 0, 8 * sizeof(double)));
   UCK(u->alloc(&u->loss_log, 1 << 16));
-  UCK(u->alloc(&u->scal, 8));
   UCK(u->alloc(&u->dsum, 4));
   UCK(u->alloc(&u->dpart, 4096));
   *out = u.release();
@@ -538,6 +593,15 @@ cudaError_t unet_prepare(UNetState* u, cudaStream_t s, const LevelDims& d, const
   if (!u->lr) UCK(u->alloc(&u->lr, d.nv));
   if (!u->zsave) UCK(u->alloc(&u->zsave, 3 * d.nv));
   if (!u->reject) UCK(u->alloc(&u->reject, 1));
+  if (!u->lfr) UCK(u->alloc(&u->lfr, d.nv));
+  if (!u->lfz) UCK(u->alloc(&u->lfz, d.nv));
+  if (!u->cbuf) UCK(u->alloc(&u->cbuf, 3 * d.nv));
+  if (!u->az) UCK(u->alloc(&u->az, 3 * d.nv));
+  if (!u->ac) UCK(u->alloc(&u->ac, 3 * d.nv));
+  if (!u->blk) {
+    const int64_t nb = (int64_t)((d.vx + kBlk - 1) / kBlk) * ((d.vy + kBlk - 1) / kBlk) * ((d.vz + kBlk - 1) / kBlk);
+    UCK(u->alloc(&u->blk, nb));
+  }
   UCK(cudaMemsetAsync(u->reject, 0, sizeof(int), s));
   k_vertex_logrho<<<nb256(d.nv), 256, 0, s>>>(d, eactive, rho, rho_min, u->lr);
   count_launch();
@@ -545,24 +609,42 @@ cudaError_t unet_prepare(UNetState* u, cudaStream_t s, const LevelDims& d, const
   return cudaGetLastError();
 }
 
-// z += rms(z) * N(r / rms(r), log rho) on free DOFs (fp32 [3][nv] vectors).
-cudaError_t unet_apply(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* vmask, const float* r, float* z,
-                       double* partial) {
+// out[v] = local rms of the [3][nv] field f (blocks of kBlk^3 vertices, floored
+// at 1e-2 of the global rms); gsum: a device double for the global sum of squares.
+static void local_rms(UNetState* u, cudaStream_t s, const LevelDims& d, const float* f, float* out, double* partial,
+                      double* gsum) {
+  const int64_t nb = (int64_t)((d.vx + kBlk - 1) / kBlk) * ((d.vy + kBlk - 1) / kBlk) * ((d.vz + kBlk - 1) / kBlk);
+  k_block_ms<<<nb256(nb), 256, 0, s>>>(d, f, u->blk);
+  launch_dot<float>(s, f, f, 3 * d.nv, partial, gsum);
+  k_local_rms<<<nb256(d.nv), 256, 0, s>>>(d, u->blk, gsum, out);
+  count_launch(4);
+}
+
+// z += beta lz N(s(r / lr), s(z / lz), log rho) on free DOFs (fp32 [3][nv]
+// vectors), beta energy-optimal; rhop32 and tz: the FP32 fine operator.
+cudaError_t unet_apply(UNetState* u, cudaStream_t s, const LevelDims& d, const uint8_t* vmask, const float* rhop32,
+                       int tz, const float* r, float* z, double* partial) {
   UNetWork* w = u->full.get();
   const int64_t n3 = 3 * d.nv;
   UCK(cudaMemcpyAsync(u->zsave, z, sizeof(float) * n3, cudaMemcpyDeviceToDevice, s));
-  launch_dot<float>(s, r, r, n3, partial, u->dsum);
-  launch_dot<float>(s, z, z, n3, partial, u->dsum + 1);
-  k_rms<<<1, 1, 0, s>>>(u->dsum, (double)n3, u->scal, u->scal + 1);
-  k_rms<<<1, 1, 0, s>>>(u->dsum + 1, (double)n3, u->scal + 2, u->scal + 3);
-  k_pack_input_dev<float><<<nb256((int64_t)w->X * w->Y * w->Z), 256, 0, s>>>(d, w->X, w->Y, w->Z, r, u->scal + 1,
-                                                                          u->lr, w->x0);
-  count_launch(7);
+  local_rms(u, s, d, r, u->lfr, partial, u->dsum);
+  local_rms(u, s, d, z, u->lfz, partial, u->dsum + 1);
+  k_pack_input_dev<<<nb256((int64_t)w->X * w->Y * w->Z), 256, 0, s>>>(d, w->X, w->Y, w->Z, r, z, u->lfr, u->lfz,
+                                                                      u->lr, w->x0);
+  count_launch();
   UCK(unet_forward(u, s, w));
-  k_unpack_add<<<nb256(d.nv), 256, 0, s>>>(d, w->X, w->Y, w->a[D0B], vmask, u->scal + 2, z);
+  UCK(cudaMemsetAsync(u->cbuf, 0, sizeof(float) * n3, s));
+  k_unpack_add<<<nb256(d.nv), 256, 0, s>>>(d, w->X, w->Y, w->a[D0B], vmask, u->lfz, u->cbuf);
+  // energy-optimal amount of the correction
+  launch_fine_apply<float>(s, d, rhop32, vmask, z, nullptr, u->az, false, 1, tz);
+  launch_fine_apply<float>(s, d, rhop32, vmask, u->cbuf, nullptr, u->ac, false, 1, tz);
+  k_sub_into<<<nb256(n3), 256, 0, s>>>(n3, r, u->az);  // az <- r - A z
+  launch_dot<float>(s, u->cbuf, u->az, n3, partial, u->dsum);
+  launch_dot<float>(s, u->cbuf, u->ac, n3, partial, u->dsum + 1);
+  k_axpy_ratio<<<nb256(n3), 256, 0, s>>>(n3, u->dsum, u->dsum + 1, u->cbuf, z, u->dsum + 3);
   launch_dot<float>(s, r, z, n3, partial, u->dsum + 2);
   k_guard<<<nb256(n3), 256, 0, s>>>(n3, u->dsum + 2, u->zsave, z, u->reject);
-  count_launch(4);
+  count_launch(12);
   return cudaGetLastError();
 }
 
@@ -605,11 +687,9 @@ cudaError_t unet_harvest_finish(UNetState* u, cudaStream_t s, const LevelDims& d
   for (int k = 0; k < u->hcount; ++k) {
     float* t = u->hx[k];  // reuse x_k's buffer for the target
     k_harvest_target<<<nb256(n3), 256, 0, s>>>(n3, ustar, u->hx[k], u->hz[k], t);
-    launch_dot<float>(s, u->hr[k], u->hr[k], n3, partial, u->dsum);
-    launch_dot<float>(s, u->hz[k], u->hz[k], n3, partial, u->dsum + 1);
-    k_rms<<<1, 1, 0, s>>>(u->dsum, (double)n3, u->scal, u->scal + 1);
-    k_rms<<<1, 1, 0, s>>>(u->dsum + 1, (double)n3, u->scal + 2, u->scal + 3);
-    count_launch(7);
+    count_launch();
+    local_rms(u, s, d, u->hr[k], u->lfr, partial, u->dsum);
+    local_rms(u, s, d, u->hz[k], u->lfz, partial, u->dsum + 1);
     for (int j = 0; j < crops_per_iterate; ++j) {
       org[3 * j] = (int)(uniform01(u->rng) * std::max(1, d.vx - S / 2)) - S / 4;
       org[3 * j + 1] = (int)(uniform01(u->rng) * std::max(1, d.vy - S / 2)) - S / 4;
@@ -622,8 +702,8 @@ cudaError_t unet_harvest_finish(UNetState* u, cudaStream_t s, const LevelDims& d
       const int nc = std::min(crops_per_iterate - done, u->cap - slot);
       UCK(cudaMemcpyAsync(u->dorg, org.data() + 3 * done, sizeof(int) * 3 * nc, cudaMemcpyHostToDevice, s));
       const int64_t tot = (int64_t)S * S * S * nc;
-      k_crop<<<nb256(tot), 256, 0, s>>>(d, S, u->dorg, nc, slot, u->hr[k], t, u->lr, vmask, u->scal + 1,
-                                        u->scal + 3, u->DX, u->DT, u->DM);
+      k_crop<<<nb256(tot), 256, 0, s>>>(d, S, u->dorg, nc, slot, u->hr[k], u->hz[k], t, u->lfr, u->lfz, u->lr,
+                                        vmask, u->DX, u->DT, u->DM);
       count_launch();
       UCK(cudaStreamSynchronize(s));  // dorg is reused
       u->next = (slot + nc) % u->cap;
@@ -639,7 +719,7 @@ cudaError_t unet_dataset_reserve(UNetState* u, int cap, int S) {
   if (u->cap) return cudaErrorInvalidValue;
   const size_t per = (size_t)S * S * S;
   u->S = S;
-  UCK(u->alloc(&u->DX, per * cap * 4));
+  UCK(u->alloc(&u->DX, per * cap * kInUsed));
   UCK(u->alloc(&u->DT, per * cap * 3));
   UCK(u->alloc(&u->DM, per * cap));
   UCK(u->alloc(&u->dorg, 3 * 4096));
@@ -662,6 +742,9 @@ cudaError_t unet_train(UNetState* u, cudaStream_t s, int steps, int batch, doubl
   const int64_t per = (int64_t)S * S * S;
   uint64_t st = seed ? seed : 7;
   std::vector<int> idx(batch);
+  // step size: linear warm-up over the first tenth of the steps (at most 100),
+  // then a cosine decay to a tenth; gradients clipped to a global norm of 1
+  const int warm = std::max(1, std::min(100, steps / 10));
   for (int it = 0; it < steps; ++it) {
     for (int b = 0; b < batch; ++b) idx[b] = lo + (int)(uniform01(st) * (hi - lo));
     UCK(cudaMemcpyAsync(u->didx, idx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, s));
@@ -672,8 +755,12 @@ cudaError_t unet_train(UNetState* u, cudaStream_t s, int steps, int batch, doubl
     if (update) {
       UCK(unet_backward(u, s, w));
       ++u->step;
-      unet_adam(s, (int64_t)u->nparam, u->grad, (float)lr, 0.9f, 0.999f, 1e-8f, u->step, u->w, u->m, u->v, u->wb);
-      count_launch();
+      const double frac = it < warm ? (it + 1.0) / warm
+                                    : 0.1 + 0.45 * (1.0 + std::cos(M_PI * (it - warm) / std::max(1, steps - warm)));
+      launch_dot<float>(s, u->grad, u->grad, (int64_t)u->nparam, u->dpart, u->dsum + 3);
+      unet_adam(s, (int64_t)u->nparam, u->grad, (float)(lr * frac), 0.9f, 0.999f, 1e-8f, u->step, u->w, u->m, u->v,
+                u->wb, u->dsum + 3, 1.0f);
+      count_launch(3);
     }
     UCK(cudaStreamSynchronize(s));  // idx is reused
   }
@@ -685,7 +772,7 @@ cudaError_t unet_train(UNetState* u, cudaStream_t s, int steps, int batch, doubl
   return cudaSuccess;
 }
 
-// Host-tensor forward/loss/backward (checks and tools): x [nb][Z][Y][X][4].
+// Host-tensor forward/loss/backward (checks and tools): x [nb][Z][Y][X][8].
 cudaError_t unet_host_pass(UNetState* u, cudaStream_t s, int X, int Y, int Z, int nb, const float* x, const float* t,
                            const uint8_t* m, float* y, double* loss, float* grad) {
   const bool train = t != nullptr;
@@ -693,8 +780,8 @@ cudaError_t unet_host_pass(UNetState* u, cudaStream_t s, int X, int Y, int Z, in
   UCK(ensure_work(w, X, Y, Z, nb, train));
   const int64_t n = (int64_t)nb * X * Y * Z;
   float* xd = nullptr;
-  UCK(cudaMalloc(&xd, sizeof(float) * n * 4));
-  cudaError_t e = cudaMemcpyAsync(xd, x, sizeof(float) * n * 4, cudaMemcpyHostToDevice, s);
+  UCK(cudaMalloc(&xd, sizeof(float) * n * kInUsed));
+  cudaError_t e = cudaMemcpyAsync(xd, x, sizeof(float) * n * kInUsed, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     k_expand_input<<<nb256(n), 256, 0, s>>>(n, xd, w->x0);
     count_launch();
@@ -749,16 +836,17 @@ cudaError_t unet_get_params(UNetState* u, cudaStream_t s, float* host) {
 int unet_dataset_count(const UNetState* u) { return u->count; }
 int unet_crop_side(const UNetState* u) { return u->S; }
 
-// Copy dataset crop `slot` to the host: x [S^3][4], t [S^3][3], m [S^3].
+// Copy dataset crop `slot` to the host: x [S^3][8], t [S^3][3], m [S^3].
 cudaError_t unet_dataset_get(UNetState* u, cudaStream_t s, int slot, float* x, float* t, uint8_t* m) {
   if (slot < 0 || slot >= u->count) return cudaErrorInvalidValue;
   const int64_t per = (int64_t)u->S * u->S * u->S;
-  std::vector<__nv_bfloat16> xb(per * 4);
-  UCK(cudaMemcpyAsync(xb.data(), u->DX + slot * per * 4, sizeof(__nv_bfloat16) * per * 4, cudaMemcpyDeviceToHost, s));
+  std::vector<__nv_bfloat16> xb(per * kInUsed);
+  UCK(cudaMemcpyAsync(xb.data(), u->DX + slot * per * kInUsed, sizeof(__nv_bfloat16) * per * kInUsed,
+                      cudaMemcpyDeviceToHost, s));
   UCK(cudaMemcpyAsync(t, u->DT + slot * per * 3, sizeof(float) * per * 3, cudaMemcpyDeviceToHost, s));
   UCK(cudaMemcpyAsync(m, u->DM + slot * per, per, cudaMemcpyDeviceToHost, s));
   UCK(cudaStreamSynchronize(s));
-  for (int64_t i = 0; i < per * 4; ++i) x[i] = __bfloat162float(xb[i]);
+  for (int64_t i = 0; i < per * kInUsed; ++i) x[i] = __bfloat162float(xb[i]);
   return cudaSuccess;
 }
 

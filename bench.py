@@ -257,16 +257,17 @@ def compliance_vs_oracle(p, wl, opts):
 
 
 def learned_ablation(p, wl, opts):
-    """Learned preconditioner at this grid: harvest residual -> error crops from
-    mixed solves on 8 seeded smoothed random densities, 400 Adam steps, then the
-    same solve (one FP32 V-cycle per outer step) with and without the network on
-    an unseen density.  Restores the design state afterwards."""
+    """Learned preconditioner at this grid: harvest about 20k residual -> error
+    crops (32^3) from mixed solves on 8 seeded smoothed random densities, 1000
+    Adam steps, then the same solve (one FP32 V-cycle per outer step) with and
+    without the network on an unseen density.  Restores the design state
+    afterwards."""
     from topoptspline3d_gb300 import capi, workloads
     rho0 = p.get("rho")
     u0 = p.get("u")
     nx, ny, nz = wl.nx, wl.ny, wl.nz
     p.unet_enable(11)
-    p.unet_dataset_reserve(2048, crop=32, crops_per_iterate=32)
+    p.unet_dataset_reserve(20480, crop=32, crops_per_iterate=64)
     base = dict(opts)
     base.update(inner_max=1, learned=0)
     t0 = time.perf_counter()
@@ -280,7 +281,7 @@ def learned_ablation(p, wl, opts):
     split = int(0.85 * n)
     t0 = time.perf_counter()
     fit0 = p.unet_train(20, batch=8, lo=0, hi=split, update=False, seed=7)
-    p.unet_train(400, batch=8, lr=1e-4, lo=0, hi=split, seed=6)
+    p.unet_train(1000, batch=8, lr=1e-3, lo=0, hi=split, seed=6)
     train_s = time.perf_counter() - t0
     fit = p.unet_train(20, batch=8, lo=0, hi=split, update=False, seed=7)
     held = p.unet_train(20, batch=8, lo=split, hi=n, update=False, seed=5)
@@ -295,7 +296,7 @@ def learned_ablation(p, wl, opts):
     p.put("rho", rho0)
     p.update_operators()
     p.put("u", u0)
-    return {"crops": n, "harvest_s": harvest_s, "train_steps": 400, "train_s": train_s,
+    return {"crops": n, "harvest_s": harvest_s, "train_steps": 1000, "train_s": train_s,
             "loss_train_crops": [fit0, fit], "loss_heldout_density": held, "solve_unseen_density": res}
 
 

@@ -1,7 +1,14 @@
 """Learned preconditioner end to end on the GPU: harvest residual -> error pairs
 from the mixed solver on seeded random densities, train the U-Net with the
 library's own kernels, and compare the solve with and without the network
-(the ablation).  The FP64 residual judges every solve."""
+(the ablation).  The FP64 residual judges every solve.
+
+What is asserted is what holds: the training loss falls on the training crops
+and the fit carries over to crops of a density never trained on; the solve
+with the network converges to the same tolerance with every V-cycle
+corrected.  The network does not cut iterations at these sizes (measured:
+33 against 32 here, 38 against 34 at 256x128x128), so the iteration bound is
+a cap on the damage the energy-optimal blend can do, not a claimed gain."""
 import numpy as np
 import pytest
 
@@ -65,11 +72,12 @@ def test_harvest_train_ablation():
     before = p.unet_train(20, batch=8, lo=split, hi=n, update=False, seed=5)
     fit0 = p.unet_train(20, batch=8, lo=0, hi=split, update=False, seed=7)
     assert abs(before - 1.0) < 1e-12 and abs(fit0 - 1.0) < 1e-12  # zero last layer: prediction 0
-    p.unet_train(400, batch=8, lr=3e-4, lo=0, hi=split, seed=6)
+    p.unet_train(400, batch=8, lr=1e-3, lo=0, hi=split, seed=6)
     fit = p.unet_train(20, batch=8, lo=0, hi=split, update=False, seed=7)
     after = p.unet_train(20, batch=8, lo=split, hi=n, update=False, seed=5)
     print(f"relative loss: training crops {fit0:.4f} -> {fit:.4f}; held-out density {before:.4f} -> {after:.4f}")
-    assert fit < 0.97 * fit0 and np.isfinite(after)
+    assert fit < 0.9 * fit0
+    assert after < 0.9 * before  # generalises to an unseen density
     # ablation on an unseen density: same solver with and without the network;
     # the positivity guard and stagnation fallback keep the learned solve sound
     rho = workloads.random_density(NX, NY, NZ, 3999)
@@ -80,4 +88,5 @@ def test_harvest_train_ablation():
           f"(applied {learned['learned_applied']}, fallback {learned['learned_fallback']})")
     for s in (plain, learned):
         assert s["relres"] <= 1e-6
-    assert learned["iterations"] <= plain["iterations"] + 10
+    assert learned["learned_applied"] == learned["vcycles"] and not learned["learned_fallback"]
+    assert learned["iterations"] <= 1.25 * plain["iterations"] + 1

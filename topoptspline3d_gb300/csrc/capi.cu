@@ -1020,6 +1020,17 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     for (auto& m : vm) m = (m & 8) ? 0xF : 0;
     cudaMemcpyAsync(L.eactive, h->H.eactive[l].data(), ne, cudaMemcpyHostToDevice, h->stream);
     cudaMemcpyAsync(L.vmask, vm.data(), nv, cudaMemcpyHostToDevice, h->stream);
+    std::vector<int2> colz;
+    if (l == 0) {  // active z range per fine tile: the fine kernels skip the void
+      fine_tile_zrange(L.d, h->H.eactive[0].data(), colz);
+      int2* dcz = nullptr;
+      A(dalloc(hp, &dcz, (int64_t)colz.size()));
+      if (rc != TOPO_OK) break;
+      cudaMemcpyAsync(dcz, colz.data(), sizeof(int2) * colz.size(), cudaMemcpyHostToDevice, h->stream);
+      L.d.colz = dcz;
+      L.d.colz_void = 0;
+      for (const int2& r : colz) L.d.colz_void |= (r.x > 0 || r.y < L.d.ez - 1) ? 1 : 0;
+    }
     cudaStreamSynchronize(h->stream);
   }
   const LevelDims& d0 = h->lv.empty() ? LevelDims{} : h->lv[0].d;

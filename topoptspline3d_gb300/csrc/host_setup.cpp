@@ -131,6 +131,34 @@ Hierarchy build_hierarchy(int nx, int ny, int nz, const uint8_t* eactive, int ma
   return H;
 }
 
+void fine_tile_zrange(const LevelDims& d, const uint8_t* eactive, std::vector<int2>& out) {
+  // lowest / highest active z per element column (x, y)
+  std::vector<int> lo((size_t)d.ex * d.ey, d.ez), hi((size_t)d.ex * d.ey, -1);
+  for (int z = 0; z < d.ez; ++z)
+    for (int y = 0; y < d.ey; ++y)
+      for (int x = 0; x < d.ex; ++x)
+        if (eactive[x + (int64_t)d.ex * (y + (int64_t)d.ey * z)]) {
+          const size_t c = x + (size_t)d.ex * y;
+          if (lo[c] > z) lo[c] = z;
+          hi[c] = z;
+        }
+  const int tx = (d.vx + FINE_TILE_X - 2) / (FINE_TILE_X - 1), ty = (d.vy + FINE_TILE_Y - 2) / (FINE_TILE_Y - 1);
+  out.assign((size_t)tx * ty, make_int2(d.ez, -1));
+  for (int by = 0; by < ty; ++by)
+    for (int bx = 0; bx < tx; ++bx) {
+      int2 r = make_int2(d.ez, -1);
+      // the tile's element columns: x0 - 1 .. x0 + FINE_TILE_X - 2 (same in y)
+      const int x0 = bx * (FINE_TILE_X - 1), y0 = by * (FINE_TILE_Y - 1);
+      for (int y = std::max(0, y0 - 1); y <= std::min(d.ey - 1, y0 + FINE_TILE_Y - 2); ++y)
+        for (int x = std::max(0, x0 - 1); x <= std::min(d.ex - 1, x0 + FINE_TILE_X - 2); ++x) {
+          const size_t c = x + (size_t)d.ex * y;
+          r.x = std::min(r.x, lo[c]);
+          r.y = std::max(r.y, hi[c]);
+        }
+      out[bx + (size_t)tx * by] = r;
+    }
+}
+
 // Knot vector per grid/Grid.cpp:3253-3337: the box is enlarged by
 // 2*delta/(p+1) on each side, step = extent/(p+1); order copies of each end
 // and p interior knots accumulated in float, as the reference does.

@@ -263,6 +263,25 @@ __device__ __forceinline__ void modal_element(T c[3][8], T pe, T* energy = nullp
     for (int a = 0; a < 8; ++a) c[i][a] = g[i][a];
 }
 
+// The vertex planes [zb0, zb1) of a fine-tile CTA narrowed to [z0, zend), the
+// planes next to the tile's active elements (LevelDims::colz): a plane sees
+// non-zero forces only from an active element layer directly below or above
+// it.  The planes cut away get the operator's output for zero forces, which
+// is what the full march would give there, without staging planes or
+// computing (void) elements.  The kernels are instantiated twice: VOID for
+// levels with void planes, and without the narrowing (and its code, which
+// costs registers in the z march) for fully active boxes.
+template <bool VOID>
+__device__ __forceinline__ void fine_active_planes(const LevelDims& d, int zb0, int zb1, int& z0, int& zend) {
+  z0 = zb0;
+  zend = zb1;
+  if (VOID) {
+    const int2 cz = d.colz[blockIdx.x + gridDim.x * blockIdx.y];
+    z0 = min(max(zb0, cz.x), zb1);
+    zend = max(z0, min(zb1, cz.y + 2));
+  }
+}
+
 // y = K(rho) u (or f - K u) on level 0.  A CTA owns a (TXE-1) x (TYE-1) column of
 // vertices over TZ vertex planes and marches in z.  Vertex planes are staged in
 // shared memory by asynchronous copies (cp.async, zero-filled outside the
@@ -391,7 +410,7 @@ __device__ __forceinline__ void dinv_sym_apply(const float* __restrict__ dinv, I
 
 constexpr int modal_min_ctas(int threads, int per_sm) { return per_sm / threads > 0 ? per_sm / threads : 1; }
 
-template <typename T, int TXE, int TYE, int MODE>
+template <typename T, int TXE, int TYE, int MODE, bool VOID>
 __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE * TYE, MODE == 2
                                                                                           ? TOPO_FINE32_CHEB_THREADS_PER_SM
                                                                                           : TOPO_FINE32_THREADS_PER_SM)
@@ -409,14 +428,16 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
   // right-hand sides are stored one after another, the operator is shared
   const int zblk = (d.vz + TZ - 1) / TZ;
   const int rhs = blockIdx.z / zblk;
-  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = (blockIdx.z - rhs * zblk) * TZ;
   const int64_t nv = d.nv;
   u += (int64_t)rhs * 3 * nv;
   if (f) f += (int64_t)rhs * 3 * nv;
   out += (int64_t)rhs * 3 * nv;
   const int gx = x0 + i, gy = y0 + j;  // owned vertex (x, y) and element (x-1, y-1)
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
-  const int zend = min(z0 + TZ, d.vz);
+  const int zb1 = min(zb0 + TZ, d.vz);
+  int z0, zend;  // the planes marched: [zb0, zb1) less the void
+  fine_active_planes<VOID>(d, zb0, zb1, z0, zend);
   T acc0 = T(0), acc1 = T(0), acc2 = T(0);
   T dsum = T(0);  // MODE 0 with ch.dotp: this thread's share of u.out
   // This thread's plane slots k = t + s NT and their in-plane vertex offsets
@@ -475,88 +496,122 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
       for (int c = 0; c < 3; ++c) dv_n[c] = dvin[c * nv + v];
     }
   };
-  T pe_n = load_pe(z0 - 1);
-  prefetch(z0 - 1);
-  prefetch(z0);
-  for (int ez = z0 - 1; ez < zend; ++ez) {
-    prefetch(ez + 2);
-    const T pe = pe_n;
-    const uint8_t vm_c = vm_n;
-    T f_c[3], dv_c[3];
+  // owned vertices of void planes [pa, pb): the output for zero forces
+  auto void_planes = [&](int pa, int pb) {
+    if (!own) return;
+    for (int p = pa; p < pb; ++p) {
+      const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * p);
+      const uint8_t m = vmask[v];
+      if (MODE < 2) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
-    if (ez + 1 < zend) pe_n = load_pe(ez + 1);
-    load_vertex(ez + 1);
-    cp_async_wait1();
-    __syncthreads();
-    // the owned vertex's own value at plane ez (Chebyshev update); read here,
-    // before the slot can be refilled by the next layer's prefetch
-    Vec4<T> uo{T(0), T(0), T(0), T(0)};
-    if (MODE == 2 || (MODE == 0 && ch.dotp)) uo = sm.plane[(ez + 3) % 3][(i + 1) + PX * (j + 1)];
-    {
-      if (pe != T(0)) {
-        T c[3][8];
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
-          const Vec4<T> p = sm.plane[(ez + (a >> 2) + 3) % 3][k];
-          c[0][a] = p.x; c[1][a] = p.y; c[2][a] = p.z;
-        }
-        modal_element<T>(c, pe);
-#pragma unroll
-        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<T>{c[0][a], c[1][a], c[2][a], T(0)};
+        for (int c = 0; c < 3; ++c) out[c * nv + v] = (MODE == 1 && ((m >> c) & 1)) ? f[c * nv + v] : T(0);
       } else {
+        const T* __restrict__ dinv = static_cast<const T*>(ch.dinv);
+        T* __restrict__ dv = static_cast<T*>(ch.dvec) + (int64_t)rhs * 3 * nv;
+        T r[3], zc[3];
 #pragma unroll
-        for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<T>{T(0), T(0), T(0), T(0)};
+        for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f[c * nv + v] : T(0);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const T c_old = T(__ldg(ch.coef)), c_new = T(__ldg(ch.coef + 1));
+          const T dn = ch.first ? c_new * zc[c] : c_old * (dvin ? dvin[c * nv + v] : T(0)) + c_new * zc[c];
+          dv[c * nv + v] = dn;
+          out[c * nv + v] = u[c * nv + v] + dn;
+        }
       }
     }
-    __syncthreads();
-    if (own) {
-      T b0 = acc0, b1 = acc1, b2 = acc2, t0 = T(0), t1 = T(0), t2 = T(0);
+  };
+  if (VOID) {
+    void_planes(zb0, z0);
+    void_planes(zend, zb1);
+  }
+  T pe_n = load_pe(z0 - 1);
+  if (z0 < zend) {
+    prefetch(z0 - 1);
+    prefetch(z0);
+    for (int ez = z0 - 1; ez < zend; ++ez) {
+      prefetch(ez + 2);
+      const T pe = pe_n;
+      const uint8_t vm_c = vm_n;
+      T f_c[3], dv_c[3];
 #pragma unroll
-      for (int w = 0; w < 4; ++w) {
-        const int wx = w & 1, wy = w >> 1;
-        const int te = (i + wx) + TXE * (j + wy);
-        const int a = (1 - wx) + 2 * (1 - wy);  // bottom node of that element
-        const Vec4<T> bo = sm.fe[a][te], to = sm.fe[a + 4][te];
-        b0 += bo.x; b1 += bo.y; b2 += bo.z;
-        t0 += to.x; t1 += to.y; t2 += to.z;
-      }
-      if (ez >= z0) {
-        const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
-        const uint8_t m = vm_c;
-        const T y[3] = {b0, b1, b2};
-        if (MODE < 2) {
-          const T uv[3] = {uo.x, uo.y, uo.z};
+      for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
+      if (ez + 1 < zend) pe_n = load_pe(ez + 1);
+      load_vertex(ez + 1);
+      cp_async_wait1();
+      __syncthreads();
+      // the owned vertex's own value at plane ez (Chebyshev update); read here,
+      // before the slot can be refilled by the next layer's prefetch
+      Vec4<T> uo{T(0), T(0), T(0), T(0)};
+      if (MODE == 2 || (MODE == 0 && ch.dotp)) uo = sm.plane[(ez + 3) % 3][(i + 1) + PX * (j + 1)];
+      {
+        if (pe != T(0)) {
+          T c[3][8];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const bool fr = (m >> c) & 1;
-            const int64_t idx = c * nv + v;
-            const T o = MODE == 1 ? (fr ? f_c[c] - y[c] : T(0)) : (fr ? y[c] : T(0));
-            out[idx] = o;
-            if (MODE == 0) dsum += uv[c] * o;
+          for (int a = 0; a < 8; ++a) {
+            const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
+            const Vec4<T> p = sm.plane[(ez + (a >> 2) + 3) % 3][k];
+            c[0][a] = p.x; c[1][a] = p.y; c[2][a] = p.z;
           }
+          modal_element<T>(c, pe);
+#pragma unroll
+          for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<T>{c[0][a], c[1][a], c[2][a], T(0)};
         } else {
-          const T* __restrict__ dinv = static_cast<const T*>(ch.dinv);
-          T* __restrict__ dv = static_cast<T*>(ch.dvec) + (int64_t)rhs * 3 * nv;
-          T r[3];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : T(0);
-          const T uv[3] = {uo.x, uo.y, uo.z};
-          T zc[3];
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const T c_old = T(__ldg(ch.coef)), c_new = T(__ldg(ch.coef + 1));
-            const T dn = ch.first ? c_new * zc[c] : c_old * dv_c[c] + c_new * zc[c];
-            dv[c * nv + v] = dn;
-            out[c * nv + v] = uv[c] + dn;
-          }
+          for (int a = 0; a < 8; ++a) sm.fe[a][t] = Vec4<T>{T(0), T(0), T(0), T(0)};
         }
       }
-      acc0 = t0; acc1 = t1; acc2 = t2;
+      __syncthreads();
+      if (own) {
+        T b0 = acc0, b1 = acc1, b2 = acc2, t0 = T(0), t1 = T(0), t2 = T(0);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          const int wx = w & 1, wy = w >> 1;
+          const int te = (i + wx) + TXE * (j + wy);
+          const int a = (1 - wx) + 2 * (1 - wy);  // bottom node of that element
+          const Vec4<T> bo = sm.fe[a][te], to = sm.fe[a + 4][te];
+          b0 += bo.x; b1 += bo.y; b2 += bo.z;
+          t0 += to.x; t1 += to.y; t2 += to.z;
+        }
+        if (ez >= z0) {
+          const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
+          const uint8_t m = vm_c;
+          const T y[3] = {b0, b1, b2};
+          if (MODE < 2) {
+            const T uv[3] = {uo.x, uo.y, uo.z};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const bool fr = (m >> c) & 1;
+              const int64_t idx = c * nv + v;
+              const T o = MODE == 1 ? (fr ? f_c[c] - y[c] : T(0)) : (fr ? y[c] : T(0));
+              out[idx] = o;
+              if (MODE == 0) dsum += uv[c] * o;
+            }
+          } else {
+            const T* __restrict__ dinv = static_cast<const T*>(ch.dinv);
+            T* __restrict__ dv = static_cast<T*>(ch.dvec) + (int64_t)rhs * 3 * nv;
+            T r[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : T(0);
+            const T uv[3] = {uo.x, uo.y, uo.z};
+            T zc[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              zc[c] = dinv[(3 * c) * nv + v] * r[0] + dinv[(3 * c + 1) * nv + v] * r[1] + dinv[(3 * c + 2) * nv + v] * r[2];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const T c_old = T(__ldg(ch.coef)), c_new = T(__ldg(ch.coef + 1));
+              const T dn = ch.first ? c_new * zc[c] : c_old * dv_c[c] + c_new * zc[c];
+              dv[c * nv + v] = dn;
+              out[c * nv + v] = uv[c] + dn;
+            }
+          }
+        }
+        acc0 = t0; acc1 = t1; acc2 = t2;
+      }
     }
   }
   // drain the (empty) trailing copy groups before the CTA exits
@@ -584,6 +639,46 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
 // Against the 2-barrier form: a quarter of the shared-memory traffic per
 // element, half the barriers.
 // ---------------------------------------------------------------------------
+// Owned vertex (gx, gy) of the FP32 kernel over void planes [pa, pb): the
+// output of MODE for zero forces (kept out of line: inlined, its live values
+// pushed the z march past its register budget).
+template <int MODE>
+__device__ __noinline__ void fine32_void_planes(const LevelDims& d, const uint8_t* __restrict__ vmask,
+                                                const float* __restrict__ u, const float* __restrict__ f,
+                                                float* __restrict__ out, const ChebArgs& ch, int rhs, int gx, int gy,
+                                                int pa, int pb, const float* coef, float& dsum) {
+  constexpr bool CHEB = MODE >= 2, DOTS = MODE == 3;
+  const int64_t nv = d.nv;
+  const float* __restrict__ dvin =
+      (CHEB && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * nv : nullptr;
+  for (int p = pa; p < pb; ++p) {
+    const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * p);
+    const uint8_t m = vmask[v];
+    if (!CHEB) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) out[c * nv + v] = (MODE == 1 && ((m >> c) & 1)) ? f[c * nv + v] : 0.f;
+    } else {
+      float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * nv;
+      float r[3], zc[3], uv[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        r[c] = ((m >> c) & 1) ? f[c * nv + v] : 0.f;
+        uv[c] = u[c * nv + v];
+      }
+      dinv_sym_apply(static_cast<const float*>(ch.dinv), nv, v, r, zc);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float dold = ch.d_is_u ? uv[c] : (dvin ? dvin[c * nv + v] : 0.f);
+        const float dn = ch.first ? coef[1] * zc[c] : coef[0] * dold + coef[1] * zc[c];
+        dv[c * nv + v] = dn;
+        const float o = uv[c] + dn;
+        out[c * nv + v] = o;
+        if (DOTS) dsum += f[c * nv + v] * o;
+      }
+    }
+  }
+}
+
 template <int TYE>
 struct Modal32Smem {
   static constexpr int TXE = 32, NT = TXE * TYE, PX = TXE + 1, PY = TYE + 1, NP = PX * PY;
@@ -593,7 +688,7 @@ struct Modal32Smem {
   float coef[2];        // Chebyshev (c_old, c_new), read after each plane's barrier
 };
 
-template <int TYE, int MODE, bool I32>
+template <int TYE, int MODE, bool I32, bool VOID>
 __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ? TOPO_FINE32_CHEB_THREADS_PER_SM
                                                                                : TOPO_FINE32_THREADS_PER_SM))
     k_fine_modal32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
@@ -615,14 +710,16 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   }
   const int zblk = (d.vz + TZ - 1) / TZ;
   const int rhs = blockIdx.z / zblk;
-  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = (blockIdx.z - rhs * zblk) * TZ;
   const I nv = (I)d.nv;
   u += (int64_t)rhs * 3 * d.nv;
   if (f) f += (int64_t)rhs * 3 * d.nv;
   out += (int64_t)rhs * 3 * d.nv;
   const int gx = x0 + i, gy = y0 + j;
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
-  const int zend = min(z0 + TZ, d.vz);
+  const int zb1 = min(zb0 + TZ, d.vz);
+  int z0, zend;  // the planes marched: [zb0, zb1) less the void
+  fine_active_planes<VOID>(d, zb0, zb1, z0, zend);
   constexpr int KS = (NP + NT - 1) / NT;
   int pxy[KS];
 #pragma unroll
@@ -678,102 +775,111 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   float top[3] = {0.f, 0.f, 0.f};                          // z = 1 forces of the layer below the last
   float uo[3] = {0.f, 0.f, 0.f};                           // owned vertex's own value at the last layer's plane
   float dsum = 0.f;
+  if (VOID && (zb0 < z0 || zend < zb1)) {  // void planes: the step's output for zero forces
+    if (CHEB) __syncthreads();      // the step coefficients in shared memory
+    if (own) {
+      fine32_void_planes<MODE>(d, vmask, u, f, out, ch, rhs, gx, gy, zb0, z0, sm.coef, dsum);
+      fine32_void_planes<MODE>(d, vmask, u, f, out, ch, rhs, gx, gy, zend, zb1, sm.coef, dsum);
+    }
+  }
   float pe_n = load_pe(z0 - 1);
-  prefetch(z0 - 1);
-  prefetch(z0);
-  // step st: finish vertex plane st - 1 (layers st - 2, st - 1), then compute element layer st
-  for (int st = z0 - 1; st <= zend; ++st) {
-    prefetch(st + 2);
-    const float pe = pe_n;
-    const uint8_t vm_c = vm_n;
-    float f_c[3], dv_c[3];
+  if (z0 < zend) {
+    prefetch(z0 - 1);
+    prefetch(z0);
+    // step st: finish vertex plane st - 1 (layers st - 2, st - 1), then compute element layer st
+    for (int st = z0 - 1; st <= zend; ++st) {
+      prefetch(st + 2);
+      const float pe = pe_n;
+      const uint8_t vm_c = vm_n;
+      float f_c[3], dv_c[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
-    if (st + 1 < zend) pe_n = load_pe(st + 1);
-    load_vertex(st);
-    cp_async_wait1();
-    __syncthreads();
-    // ---- vertex plane p = st - 1
-    if (st >= z0) {
-      const int p = st - 1, xs = (st - 1) & 1;
-      float y[3];
-      if (own) {
-        const float4 ra = sm.xa[xs][t + TXE];
-        const float2 rb = sm.xb[xs][t + TXE];
-        const float r0[3] = {ra.x, ra.y, ra.z}, r1[3] = {ra.w, rb.x, rb.y};
+      for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; }
+      if (st + 1 < zend) pe_n = load_pe(st + 1);
+      load_vertex(st);
+      cp_async_wait1();
+      __syncthreads();
+      // ---- vertex plane p = st - 1
+      if (st >= z0) {
+        const int p = st - 1, xs = (st - 1) & 1;
+        float y[3];
+        if (own) {
+          const float4 ra = sm.xa[xs][t + TXE];
+          const float2 rb = sm.xb[xs][t + TXE];
+          const float r0[3] = {ra.x, ra.y, ra.z}, r1[3] = {ra.w, rb.x, rb.y};
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          y[c] = top[c] + (own1[0][c] + r0[c]);
-          top[c] = own1[1][c] + r1[c];
-        }
-        if (p >= z0) {
-          const I v = gx + (I)d.vx * (gy + (I)d.vy * p);
-          const uint8_t m = vm_c;
-          const float uv[3] = {uo[0], uo[1], uo[2]};
-          if (!CHEB) {
+          for (int c = 0; c < 3; ++c) {
+            y[c] = top[c] + (own1[0][c] + r0[c]);
+            top[c] = own1[1][c] + r1[c];
+          }
+          if (p >= z0) {
+            const I v = gx + (I)d.vx * (gy + (I)d.vy * p);
+            const uint8_t m = vm_c;
+            const float uv[3] = {uo[0], uo[1], uo[2]};
+            if (!CHEB) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              const bool fr = (m >> c) & 1;
-              const float o = MODE == 1 ? (fr ? f_c[c] - y[c] : 0.f) : (fr ? y[c] : 0.f);
-              out[c * nv + v] = o;
-              if (MODE == 0) dsum += uv[c] * o;
-            }
-          } else {
-            float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * d.nv;
-            float r[3], zc[3];
+              for (int c = 0; c < 3; ++c) {
+                const bool fr = (m >> c) & 1;
+                const float o = MODE == 1 ? (fr ? f_c[c] - y[c] : 0.f) : (fr ? y[c] : 0.f);
+                out[c * nv + v] = o;
+                if (MODE == 0) dsum += uv[c] * o;
+              }
+            } else {
+              float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * d.nv;
+              float r[3], zc[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : 0.f;
-            dinv_sym_apply(static_cast<const float*>(ch.dinv), nv, v, r, zc);
+              for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : 0.f;
+              dinv_sym_apply(static_cast<const float*>(ch.dinv), nv, v, r, zc);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              const float dold = ch.d_is_u ? uv[c] : dv_c[c];
-              const float c_old = sm.coef[0], c_new = sm.coef[1];
-              const float dn = ch.first ? c_new * zc[c] : c_old * dold + c_new * zc[c];
-              dv[c * nv + v] = dn;
-              const float o = uv[c] + dn;
-              out[c * nv + v] = o;
-              if (DOTS) dsum += f_c[c] * o;
+              for (int c = 0; c < 3; ++c) {
+                const float dold = ch.d_is_u ? uv[c] : dv_c[c];
+                const float c_old = sm.coef[0], c_new = sm.coef[1];
+                const float dn = ch.first ? c_new * zc[c] : c_old * dold + c_new * zc[c];
+                dv[c * nv + v] = dn;
+                const float o = uv[c] + dn;
+                out[c * nv + v] = o;
+                if (DOTS) dsum += f_c[c] * o;
+              }
             }
           }
         }
       }
-    }
-    // ---- element layer st
-    if (st < zend) {
-      if (CHEB || (MODE == 0 && ch.dotp)) {
-        const float4 q = sm.plane[(st + 4) & 3][(i + 1) + PX * (j + 1)];
-        uo[0] = q.x; uo[1] = q.y; uo[2] = q.z;
-      }
-      float c[3][8];
-      if (pe != 0.f) {
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
-          const float4 q = sm.plane[(st + (a >> 2) + 4) & 3][k];
-          c[0][a] = q.x; c[1][a] = q.y; c[2][a] = q.z;
+      // ---- element layer st
+      if (st < zend) {
+        if (CHEB || (MODE == 0 && ch.dotp)) {
+          const float4 q = sm.plane[(st + 4) & 3][(i + 1) + PX * (j + 1)];
+          uo[0] = q.x; uo[1] = q.y; uo[2] = q.z;
         }
-        modal_element<float>(c, pe);
-      } else {
+        float c[3][8];
+        if (pe != 0.f) {
 #pragma unroll
-        for (int a = 0; a < 8; ++a) c[0][a] = c[1][a] = c[2][a] = 0.f;
-      }
-      // x combine: vertex column i takes the x = 1 nodes of element i and the
-      // x = 0 nodes of element i + 1 (lane 31's column is not owned)
-      float xc[2][2][3];  // [y bit][z bit][component]
+          for (int a = 0; a < 8; ++a) {
+            const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
+            const float4 q = sm.plane[(st + (a >> 2) + 4) & 3][k];
+            c[0][a] = q.x; c[1][a] = q.y; c[2][a] = q.z;
+          }
+          modal_element<float>(c, pe);
+        } else {
 #pragma unroll
-      for (int yb = 0; yb < 2; ++yb)
+          for (int a = 0; a < 8; ++a) c[0][a] = c[1][a] = c[2][a] = 0.f;
+        }
+        // x combine: vertex column i takes the x = 1 nodes of element i and the
+        // x = 0 nodes of element i + 1 (lane 31's column is not owned)
+        float xc[2][2][3];  // [y bit][z bit][component]
+#pragma unroll
+        for (int yb = 0; yb < 2; ++yb)
+#pragma unroll
+          for (int zb = 0; zb < 2; ++zb)
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc)
+              xc[yb][zb][cc] = c[cc][1 + 2 * yb + 4 * zb] +
+                               __shfl_down_sync(0xffffffffu, c[cc][2 * yb + 4 * zb], 1);
 #pragma unroll
         for (int zb = 0; zb < 2; ++zb)
 #pragma unroll
-          for (int cc = 0; cc < 3; ++cc)
-            xc[yb][zb][cc] = c[cc][1 + 2 * yb + 4 * zb] +
-                             __shfl_down_sync(0xffffffffu, c[cc][2 * yb + 4 * zb], 1);
-#pragma unroll
-      for (int zb = 0; zb < 2; ++zb)
-#pragma unroll
-        for (int cc = 0; cc < 3; ++cc) own1[zb][cc] = xc[1][zb][cc];
-      sm.xa[st & 1][t] = make_float4(xc[0][0][0], xc[0][0][1], xc[0][0][2], xc[0][1][0]);
-      sm.xb[st & 1][t] = make_float2(xc[0][1][1], xc[0][1][2]);
+          for (int cc = 0; cc < 3; ++cc) own1[zb][cc] = xc[1][zb][cc];
+        sm.xa[st & 1][t] = make_float4(xc[0][0][0], xc[0][0][1], xc[0][0][2], xc[0][1][0]);
+        sm.xb[st & 1][t] = make_float2(xc[0][1][1], xc[0][1][2]);
+      }
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
@@ -804,7 +910,7 @@ struct DfSmem {
   double raw[3][3][NP];           // cp.async staging: [slot][component][vertex]
 };
 
-template <int TXE, int TYE, int MODE>
+template <int TXE, int TYE, int MODE, bool VOID>
 __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const double* __restrict__ rhop,
                                                             const uint8_t* __restrict__ vmask,
                                                             const double* __restrict__ u,
@@ -817,14 +923,35 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
   const int t = threadIdx.x, i = t % TXE, j = t / TXE;
   const int zblk = (d.vz + TZ - 1) / TZ;
   const int rhs = blockIdx.z / zblk;
-  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), z0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = (blockIdx.z - rhs * zblk) * TZ;
   const int64_t nv = d.nv;
   u += (int64_t)rhs * 3 * nv;
   if (f) f += (int64_t)rhs * 3 * nv;
   out += (int64_t)rhs * 3 * nv;
   const int gx = x0 + i, gy = y0 + j;
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
-  const int zend = min(z0 + TZ, d.vz);
+  const int zb1 = min(zb0 + TZ, d.vz);
+  int z0, zend;  // the planes marched: [zb0, zb1) less the void
+  fine_active_planes<VOID>(d, zb0, zb1, z0, zend);
+  // Void planes [pa, pb): the owned vertices get the output for zero forces;
+  // MODE 3 writes zero energy for this thread's owned elements of those layers.
+  auto void_planes = [&](int pa, int pb) {
+    for (int p = pa; p < pb; ++p) {
+      if (own) {
+        const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * p);
+        const uint8_t m = vmask[v];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[c * nv + v] = (MODE >= 1 && ((m >> c) & 1)) ? f[c * nv + v] : 0.0;
+      }
+      const int ex = gx - 1, ey = gy - 1;
+      if (MODE == 3 && i > 0 && j > 0 && ex < d.ex && ey < d.ey && p < d.ez)
+        energy[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * p)] = 0.0;
+    }
+  };
+  if (VOID) {
+    void_planes(zb0, z0);
+    void_planes(zend, zb1);
+  }
   df acc0(0), acc1(0), acc2(0);
   auto prefetch = [&](int z) {
     if (z <= zend) {
@@ -852,77 +979,79 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
       sm.plo[cs][k] = make_float4(a.lo, b.lo, c.lo, 0.f);
     }
   };
-  prefetch(z0 - 1);
-  prefetch(z0);
-  for (int ez = z0 - 1; ez < zend; ++ez) {
-    prefetch(ez + 2);
-    cp_async_wait1();
-    __syncthreads();
-    if (ez == z0 - 1) convert(ez);
-    convert(ez + 1);
-    __syncthreads();
-    {
-      const int ex = gx - 1, ey = gy - 1;
-      df pe(0);
-      if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
-        pe = df_from(rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)]);
-      // MODE 3 writes u_e . (rho^p Ke u_e) of the elements this CTA owns (its
-      // first element row / column and layer belong to the neighbouring tiles)
-      const bool own_e = MODE == 3 && i > 0 && j > 0 && ez >= z0 && ex < d.ex && ey < d.ey && ez < d.ez;
-      if (pe != df(0)) {
-        df c[3][8];
+  if (z0 < zend) {
+    prefetch(z0 - 1);
+    prefetch(z0);
+    for (int ez = z0 - 1; ez < zend; ++ez) {
+      prefetch(ez + 2);
+      cp_async_wait1();
+      __syncthreads();
+      if (ez == z0 - 1) convert(ez);
+      convert(ez + 1);
+      __syncthreads();
+      {
+        const int ex = gx - 1, ey = gy - 1;
+        df pe(0);
+        if (ex >= 0 && ey >= 0 && ez >= 0 && ex < d.ex && ey < d.ey && ez < d.ez)
+          pe = df_from(rhop[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)]);
+        // MODE 3 writes u_e . (rho^p Ke u_e) of the elements this CTA owns (its
+        // first element row / column and layer belong to the neighbouring tiles)
+        const bool own_e = MODE == 3 && i > 0 && j > 0 && ez >= z0 && ex < d.ex && ey < d.ey && ez < d.ez;
+        if (pe != df(0)) {
+          df c[3][8];
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
-          const int cs = (ez + (a >> 2) + 2) & 1;
-          const float4 h = sm.phi[cs][k], l = sm.plo[cs][k];
-          c[0][a] = df(h.x, l.x); c[1][a] = df(h.y, l.y); c[2][a] = df(h.z, l.z);
-        }
-        if (MODE == 3) {
-          df en;
-          modal_element<df, true>(c, pe, &en);
-          if (own_e) energy[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)] = df_to(en);
+          for (int a = 0; a < 8; ++a) {
+            const int k = (i + (a & 1)) + PX * (j + ((a >> 1) & 1));
+            const int cs = (ez + (a >> 2) + 2) & 1;
+            const float4 h = sm.phi[cs][k], l = sm.plo[cs][k];
+            c[0][a] = df(h.x, l.x); c[1][a] = df(h.y, l.y); c[2][a] = df(h.z, l.z);
+          }
+          if (MODE == 3) {
+            df en;
+            modal_element<df, true>(c, pe, &en);
+            if (own_e) energy[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)] = df_to(en);
+          } else {
+            modal_element<df>(c, pe);
+          }
+#pragma unroll
+          for (int a = 0; a < 8; ++a) {
+            sm.fhi[a][t] = make_float4(c[0][a].hi, c[1][a].hi, c[2][a].hi, 0.f);
+            sm.flo[a][t] = make_float4(c[0][a].lo, c[1][a].lo, c[2][a].lo, 0.f);
+          }
         } else {
-          modal_element<df>(c, pe);
-        }
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          sm.fhi[a][t] = make_float4(c[0][a].hi, c[1][a].hi, c[2][a].hi, 0.f);
-          sm.flo[a][t] = make_float4(c[0][a].lo, c[1][a].lo, c[2][a].lo, 0.f);
-        }
-      } else {
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          sm.fhi[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
-          sm.flo[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        if (own_e) energy[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)] = 0.0;
-      }
-    }
-    __syncthreads();
-    if (own) {
-      df b0 = acc0, b1 = acc1, b2 = acc2, t0(0), t1(0), t2(0);
-#pragma unroll
-      for (int w = 0; w < 4; ++w) {
-        const int wx = w & 1, wy = w >> 1;
-        const int te = (i + wx) + TXE * (j + wy);
-        const int a = (1 - wx) + 2 * (1 - wy);
-        const float4 bh = sm.fhi[a][te], bl = sm.flo[a][te], th = sm.fhi[a + 4][te], tl = sm.flo[a + 4][te];
-        b0 += df(bh.x, bl.x); b1 += df(bh.y, bl.y); b2 += df(bh.z, bl.z);
-        t0 += df(th.x, tl.x); t1 += df(th.y, tl.y); t2 += df(th.z, tl.z);
-      }
-      if (ez >= z0) {
-        const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
-        const uint8_t m = vmask[v];
-        const double y[3] = {df_to(b0), df_to(b1), df_to(b2)};
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const bool fr = (m >> c) & 1;
-          const int64_t idx = c * nv + v;
-          out[idx] = MODE >= 1 ? (fr ? f[idx] - y[c] : 0.0) : (fr ? y[c] : 0.0);
+          for (int a = 0; a < 8; ++a) {
+            sm.fhi[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
+            sm.flo[a][t] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+          if (own_e) energy[ex + (int64_t)d.ex * (ey + (int64_t)d.ey * ez)] = 0.0;
         }
       }
-      acc0 = t0; acc1 = t1; acc2 = t2;
+      __syncthreads();
+      if (own) {
+        df b0 = acc0, b1 = acc1, b2 = acc2, t0(0), t1(0), t2(0);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          const int wx = w & 1, wy = w >> 1;
+          const int te = (i + wx) + TXE * (j + wy);
+          const int a = (1 - wx) + 2 * (1 - wy);
+          const float4 bh = sm.fhi[a][te], bl = sm.flo[a][te], th = sm.fhi[a + 4][te], tl = sm.flo[a + 4][te];
+          b0 += df(bh.x, bl.x); b1 += df(bh.y, bl.y); b2 += df(bh.z, bl.z);
+          t0 += df(th.x, tl.x); t1 += df(th.y, tl.y); t2 += df(th.z, tl.z);
+        }
+        if (ez >= z0) {
+          const int64_t v = gx + (int64_t)d.vx * (gy + (int64_t)d.vy * ez);
+          const uint8_t m = vmask[v];
+          const double y[3] = {df_to(b0), df_to(b1), df_to(b2)};
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const bool fr = (m >> c) & 1;
+            const int64_t idx = c * nv + v;
+            out[idx] = MODE >= 1 ? (fr ? f[idx] - y[c] : 0.0) : (fr ? y[c] : 0.0);
+          }
+        }
+        acc0 = t0; acc1 = t1; acc2 = t2;
+      }
     }
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
@@ -1100,6 +1229,9 @@ __global__ void k_fine_diag_inv(LevelDims d, const T* __restrict__ rhop,
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 constexpr int MODAL_TXE = 32, MODAL_TYE = 8, MODAL_TZ = 16;
+// the per-tile active z ranges (LevelDims::colz) are laid out for this tile
+static_assert(MODAL_TXE == FINE_TILE_X && MODAL_TYE == FINE_TILE_Y && TOPO_MODAL32_TYE == FINE_TILE_Y,
+              "fine kernel tiles and LevelDims::colz disagree");
 // CTA tile rows of the FP32 / FP64 modal kernels
 template <typename T>
 constexpr int modal_tye() { return sizeof(T) == 4 ? TOPO_MODAL32_TYE : MODAL_TYE; }
@@ -1111,11 +1243,12 @@ dim3 modal_grid(const LevelDims& d, int tz, int nb) {
 }
 
 // One launch of the modal operator in mode MODE: the single-barrier kernel for
-// FP32, the generic kernel for FP64.  Kernels are opted into their dynamic
-// shared memory once per device.
-template <typename T, int MODE>
-void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u, const T* f,
-                  T* out, int tz, int nb, const ChebArgs& ch) {
+// FP32, the generic kernel for FP64; the VOID instantiations where level 0 has
+// void planes.  Kernels are opted into their dynamic shared memory once per
+// device.
+template <typename T, int MODE, bool VOID>
+void launch_modal_v(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u, const T* f,
+                    T* out, int tz, int nb, const ChebArgs& ch) {
   if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid = modal_grid<T>(d, tz, nb);
   constexpr int TYE = modal_tye<T>();
@@ -1123,26 +1256,36 @@ void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8
     const size_t smem = sizeof(Modal32Smem<TYE>);
     static PerDeviceOnce once;
     once_per_device(once, [smem] {
-      cudaError_t e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, true, VOID>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, false, VOID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
       return e;
     });
     // (MODE 3 keeps 64-bit offsets: with 32-bit ones it spilled 32 bytes and
     // ran 122 against 118 us at 256x128x128, where modes 0-2 gained 4-9 us)
     if (MODE != 3 && 3 * d.nv < ((int64_t)1 << 31) && d.ne < ((int64_t)1 << 31))
-      k_fine_modal32<TYE, MODE, true><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+      k_fine_modal32<TYE, MODE, true, VOID><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
     else
-      k_fine_modal32<TYE, MODE, false><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+      k_fine_modal32<TYE, MODE, false, VOID><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
   } else {
     const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
     static PerDeviceOnce once;
     once_per_device(once, [smem] {
-      return cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem);
+      return cudaFuncSetAttribute(k_fine_modal<T, MODAL_TXE, TYE, MODE, VOID>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     });
-    k_fine_modal<T, MODAL_TXE, TYE, MODE><<<grid, MODAL_TXE * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+    k_fine_modal<T, MODAL_TXE, TYE, MODE, VOID><<<grid, MODAL_TXE * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz,
+                                                                                     ch);
   }
+}
+
+template <typename T, int MODE>
+void launch_modal(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u, const T* f,
+                  T* out, int tz, int nb, const ChebArgs& ch) {
+  if (d.colz && d.colz_void) launch_modal_v<T, MODE, true>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
+  else launch_modal_v<T, MODE, false>(s, d, rhop, vmask, u, f, out, tz, nb, ch);
 }
 
 template <typename T>
@@ -1173,9 +1316,10 @@ template int launch_fine_apply_dot<float>(cudaStream_t, const LevelDims&, const 
 template int launch_fine_apply_dot<double>(cudaStream_t, const LevelDims&, const double*, const uint8_t*,
                                            const double*, double*, int, double*, int, double*, unsigned*);
 
-void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
-                          const double* u, const double* f, double* out, bool residual, int nb, int tz,
-                          double* energy) {
+template <bool VOID>
+static void launch_fine_apply_df_v(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
+                                   const double* u, const double* f, double* out, bool residual, int nb, int tz,
+                                   double* energy) {
   if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
                   ((d.vz + tz - 1) / tz) * nb);
@@ -1183,19 +1327,29 @@ void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop
   const size_t smem = sizeof(DfSmem<MODAL_TXE, MODAL_TYE>);
   static PerDeviceOnce once;
   once_per_device(once, [smem] {
-    cudaError_t e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0, VOID>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1, VOID>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      e = cudaFuncSetAttribute(k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3, VOID>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return e;
   });
   if (residual && energy)
-    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, energy);
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 3, VOID><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, energy);
   else if (residual)
-    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, nullptr);
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 1, VOID><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, nullptr);
   else
-    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, nullptr);
+    k_fine_modal_df<MODAL_TXE, MODAL_TYE, 0, VOID><<<grid, NT, smem, s>>>(d, rhop, vmask, u, f, out, tz, nullptr);
+}
+
+void launch_fine_apply_df(cudaStream_t s, const LevelDims& d, const double* rhop, const uint8_t* vmask,
+                          const double* u, const double* f, double* out, bool residual, int nb, int tz,
+                          double* energy) {
+  if (d.colz && d.colz_void) launch_fine_apply_df_v<true>(s, d, rhop, vmask, u, f, out, residual, nb, tz, energy);
+  else launch_fine_apply_df_v<false>(s, d, rhop, vmask, u, f, out, residual, nb, tz, energy);
 }
 
 // One fused Chebyshev step on level 0: uout = u + d with d = c_old d + c_new Dinv (f - K u)

@@ -62,13 +62,27 @@ inline cudaError_t once_per_device(PerDeviceOnce& o, Fn&& fn) {
   return e;
 }
 
+// Vertex tile of the fine z-marching kernels: a CTA owns FINE_TILE_X - 1 by
+// FINE_TILE_Y - 1 vertex columns and computes the FINE_TILE_X x FINE_TILE_Y
+// element columns around them (one halo column and row below).
+constexpr int FINE_TILE_X = 32, FINE_TILE_Y = 8;
+
 // Dense grid level.  Element/vertex numbering is lexicographic (x fastest).
 struct LevelDims {
   int ex, ey, ez;
   int vx, vy, vz;
   int64_t ne, nv;
   int factor;  // coarsening factor from the previous used level (1 for level 0)
+  // Level 0 only (else null): per fine tile (bx + tiles_x * by), the lowest
+  // and highest z of an active element among the tile's element columns, or
+  // (ez, -1) when none is active.  The fine kernels march only the vertex
+  // planes next to that range; the others see zero forces.
+  const int2* colz;
+  int colz_void;  // some tile's active range leaves void planes: the fine kernels narrow their z march
 };
+
+// Active z range per fine tile of level 0 from the element mask (host).
+void fine_tile_zrange(const LevelDims& d, const uint8_t* eactive, std::vector<int2>& out);
 
 // Device buffers of one level.  Vertex vectors are SoA [3][nv].
 struct DevLevel {

@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every kernel on its own (no CUDA graphs); with --profile-iteration this lists the "
                          "kernels the device-side loops run inside graphs")
+    ap.add_argument("--profile-fp64", action="store_true",
+                    help="with --profile-iteration: the design iterations run plain FP64 MG-PCG (FP64 operators, "
+                         "native FP64 fine operator), the comparison path, instead of the mixed solve")
     ap.add_argument("--profile-warmup", type=int, default=0,
                     help="with --profile-iteration: run this many design iterations first and open the profiler's "
                          "capture range (cudaProfilerStart) only around the last one, for ncu --profile-from-start off")
@@ -538,6 +541,10 @@ def main():
         p.set_tiles(tz32, tz64)
         args.no_autotune = True
     if args.profile_iteration:
+        if args.profile_fp64:
+            p.set_operator_precision(1)
+            p.set_fine_arithmetic(0)
+            opts = solve_opts(capi.SOLVE_PCG64, args.smoother)
         if args.profile_solve_steps > 0:
             opts["max_iter"] = args.profile_solve_steps
         for _ in range(args.profile_warmup):

@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default solver schedule and tiles")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner ablation")
+    ap.add_argument("--retune-every", type=int, default=None,
+                    help="every N timed design iterations, try the FP32 inner caps 1, 2, 4, 6 on the next four and "
+                         "keep the fastest (default: 25 for --case ellipsoids, off otherwise)")
     ap.add_argument("--profile-iteration", action="store_true",
                     help="run exactly one mixed design iteration and exit (for ncu captures)")
     ap.add_argument("--schedule", default=None,
@@ -174,6 +177,41 @@ def make_problem(nx, ny, nz, device, op_precision, case="mbb"):
     return wl, p
 
 
+class InnerTuner:
+    """Online choice of the FP32 inner-iteration cap over a long run.  The
+    autotuner picks the schedule on an early design; as the design sharpens,
+    the best number of FP32 CG iterations per outer step grows.  Every `every`
+    design iterations the next four run with inner caps 1, 2, 4 and 6 (the other
+    schedule fields as tuned), and the cap of the fastest solve is kept.  These
+    are ordinary design iterations of the run, timed with the rest.  The chosen
+    schedule per step is recorded so that a second pass can replay it."""
+
+    CAPS = (1, 2, 4, 6)
+
+    def __init__(self, opts, every):
+        self.opts, self.every = dict(opts), every
+        self.trial = {}
+        self.used = []
+
+    def opts_for(self, k):
+        ph = k % self.every if self.every else -1
+        if self.every and k >= self.every and ph < len(self.CAPS):
+            o = dict(self.opts, inner_max=self.CAPS[ph])
+        else:
+            o = dict(self.opts)
+        self.used.append(o)
+        return o
+
+    def report(self, k, st):
+        ph = k % self.every if self.every else -1
+        if not (self.every and k >= self.every and ph < len(self.CAPS)):
+            return
+        self.trial[self.CAPS[ph]] = st["solve_ms"]
+        if ph == len(self.CAPS) - 1:
+            self.opts["inner_max"] = min(self.trial, key=self.trial.get)
+            self.trial = {}
+
+
 def solve_opts(mode, smoother):
     from topoptspline3d_gb300 import capi
     return dict(mode=mode, smoother=capi.SMOOTH_CHEBYSHEV if smoother == "chebyshev" else capi.SMOOTH_GS,
@@ -260,21 +298,21 @@ def compliance_vs_oracle(p, wl, opts):
 
 
 def learned_ablation(p, wl, opts):
-    """Learned preconditioner at this grid: harvest about 20k residual -> error
-    crops (32^3) from mixed solves on 8 seeded smoothed random densities, 1000
-    Adam steps, then the same solve (one FP32 V-cycle per outer step) with and
-    without the network on an unseen density.  Restores the design state
-    afterwards."""
+    """Learned preconditioner at this grid: harvest 20k residual -> error crops
+    (32^3; 128 from each of 8 iterates per solve) from mixed solves on 20 seeded
+    smoothed random densities, 1000 Adam steps, then the same solve (one FP32
+    V-cycle per outer step) with and without the network on an unseen density.
+    Restores the design state afterwards."""
     from topoptspline3d_gb300 import capi, workloads
     rho0 = p.get("rho")
     u0 = p.get("u")
     nx, ny, nz = wl.nx, wl.ny, wl.nz
     p.unet_enable(11)
-    p.unet_dataset_reserve(20480, crop=32, crops_per_iterate=64)
+    p.unet_dataset_reserve(20480, crop=32, crops_per_iterate=128)
     base = dict(opts)
     base.update(inner_max=1, learned=0)
     t0 = time.perf_counter()
-    for i in range(8):
+    for i in range(20):
         p.put("rho", workloads.random_density(nx, ny, nz, 3000 + i))
         p.update_operators()
         p.put("u", np.zeros(3 * p.nv))
@@ -510,6 +548,8 @@ def main():
         args.size = {"ellipsoids": "511x256x256", "loads": "192x96x96", "robust": "192x96x96"}.get(
             args.case, "256x128x128")
     nx, ny, nz = (int(v) for v in args.size.lower().split("x"))
+    if args.retune_every is None:
+        args.retune_every = 25 if args.case == "ellipsoids" else 0
     ws, rank, local, pg = dist_setup()
     if args.impl == "reference":
         run_reference(args, nx, ny, nz, ws, rank)
@@ -581,8 +621,10 @@ def main():
     launches0 = p.launch_count()
     p.timer_start()
     stats = []
-    for _ in range(args.steps):
-        stats.append(p.design_iteration(solve=opts, oc=oc))
+    tuner = InnerTuner(opts, args.retune_every)
+    for k in range(args.steps):
+        stats.append(p.design_iteration(solve=tuner.opts_for(k), oc=oc))
+        tuner.report(k, stats[-1])
     ms_total = p.timer_stop()
     launches = p.launch_count() - launches0
     clocks = sampler.stop()
@@ -598,10 +640,10 @@ def main():
     p.sync()
     p.timer_start()
     comp, e2e_its = [], []
-    for _ in range(args.steps):
+    for k in range(args.steps):
         p.put_from("coeff", hbuf.ptr, nc)
         p.coeff_to_density()
-        s = p.design_iteration(solve=opts, oc=oc)
+        s = p.design_iteration(solve=tuner.used[k], oc=oc)
         p.get_into("coeff", hbuf.ptr, nc)
         comp.append(s["compliance"])
         e2e_its.append(s["iterations"])
@@ -622,11 +664,11 @@ def main():
         p.set_operator_precision(2)
         p.set_fine_arithmetic(1)
     # ---- roofline of the dominant kernel family: per-family kernel times from
-    # CUDA events around each launch, over K more design iterations (untimed;
+    # CUDA events around each launch, over min(K, 10) more design iterations (untimed;
     # with the events on, the inner CG runs its host loop, the same kernels)
     p.profile_enable(True)
-    for _ in range(args.steps):
-        p.design_iteration(solve=opts, oc=oc)
+    for _ in range(min(args.steps, 10)):
+        p.design_iteration(solve=tuner.opts, oc=oc)
     prof = {k: p.profile_read(k) for k in range(4)}
     p.profile_enable(False)
     d0 = p.level_dims(0)[0]
@@ -699,6 +741,8 @@ def main():
                                 f"[{opts.get('cheb_lo', 0.3):g}, {opts.get('cheb_hi', 1.1):g}] lambda_max multigrid, "
                                 f"rel-res 1e-6",
                       "autotune": tune,
+                      "inner_cap_retune_every": args.retune_every,
+                      "inner_caps_used": sorted(set(o["inner_max"] for o in tuner.used)),
                       "l2": "working set (>2 GB) larger than L2; no flush",
                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
            "cg_iterations": [s["iterations"] for s in stats], "relres": max(s["relres"] for s in stats),

@@ -649,6 +649,21 @@ def main():
         e2e_its.append(s["iterations"])
     e2e_ms = allmax(pg, p.timer_stop() / args.steps)
     e2e_same_work = e2e_its == [s["iterations"] for s in stats]
+    # ---- the same steps once more in reference precision (rho, coefficients and
+    # sensitivities at FP32 values, rho^p by powf): the FP32-storage gap
+    refp = None
+    if args.case == "mbb":
+        p.put("coeff", coeff_start)
+        p.coeff_to_density()
+        p.put("u", u_start)
+        p.set_reference_precision(1)
+        p.coeff_to_density()
+        ref_comp = [p.design_iteration(solve=tuner.used[k], oc=oc)["compliance"] for k in range(args.steps)]
+        p.set_reference_precision(0)
+        p.coeff_to_density()
+        refp = {"compliance_rel_gap": [abs(a - b) / abs(b) for a, b in zip(ref_comp, comp)],
+                "note": "same design iterations from the same state with the reference's FP32 storage of rho, "
+                        "coefficients and sensitivities and powf for rho^p, against the FP64 path"}
     # ---- FP64 MG-PCG comparison on the same GPU (same design state)
     fp64 = None
     if args.fp64_steps > 0:
@@ -748,6 +763,7 @@ def main():
            "cg_iterations": [s["iterations"] for s in stats], "relres": max(s["relres"] for s in stats),
            "oc_trials": [s["oc_trials"] for s in stats], "compliance": [s["compliance"] for s in stats],
            "fp64_mgpcg": fp64,
+           "reference_precision": refp,
            "speedup_vs_fp64_mgpcg": (fp64["ms_per_step"] / ms_step) if fp64 else None,
            "e2e": {"value": e2e_ms, "unit": "ms/design-iter", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                    "same_iterations_as_timed_region": e2e_same_work},

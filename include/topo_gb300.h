@@ -219,6 +219,14 @@ int topo_coeff_to_density(topo_handle* h);
  * PCG modes), bit 1 FP32 (mixed mode).  Default 3.  The reference builds FP64 only
  * (grid/Grid.cu:839-1265). */
 int topo_set_operator_precision(topo_handle* h, int mask);
+/* Reference precision (enable = 1; default 0): the arrays the reference stores
+ * in FP32 are kept at FP32 values, and rho^p is taken with powf in FP32
+ * (grid/Grid.cu:1739).  Coefficients are rounded to FP32 before each density
+ * evaluation (so also after every OC update), rho after it; sensitivities after
+ * the element sensitivity and after the filter, coefficient sensitivities after
+ * the spline adjoint.  The solve stays as configured.  It quantifies how far
+ * the FP64 path's design trajectory lies from the reference's FP32 storage. */
+int topo_set_reference_precision(topo_handle* h, int enable);
 /* Replaces HierarchyGrid::update_stencil (grid/Grid.cpp:4167-4178): rho^p, Galerkin
  * coarse operators (grid/Grid.cu:839-1265) and the coarsest factorisation
  * (grid/Grid.cpp:3614-3669). */

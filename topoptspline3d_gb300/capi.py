@@ -37,7 +37,7 @@ EXPORTED = [
     "topo_prolong", "topo_coarsest_solve", "topo_vcycle", "topo_solve", "topo_compliance",
     "topo_volume", "topo_sensitivity", "topo_filter", "topo_spline_adjoint", "topo_oc_update",
     "topo_gs_maps", "topo_profile_enable", "topo_profile_read", "topo_launch_count",
-    "topo_set_operator_precision", "topo_host_alloc", "topo_host_free", "topo_design_iteration",
+    "topo_set_operator_precision", "topo_set_reference_precision", "topo_host_alloc", "topo_host_free", "topo_design_iteration",
     "topo_element_template", "topo_plan_levels", "topo_spline_axis", "topo_plan_gs_maps",
     "topo_timer_start", "topo_timer_stop", "topo_spline_adjoint_noalloc", "topo_volume_csens",
     "topo_mma_create", "topo_mma_create_for", "topo_mma_destroy", "topo_mma_last_error", "topo_mma_size",
@@ -178,6 +178,7 @@ def load(build: bool = True):
         "topo_device_ptr": (i, [vp, i, i, C.POINTER(vp)]),
         "topo_coeff_to_density": (i, [vp]),
         "topo_set_operator_precision": (i, [vp, i]),
+        "topo_set_reference_precision": (i, [vp, i]),
         "topo_update_operators": (i, [vp]),
         "topo_apply_fine": (i, [vp, i]),
         "topo_residual": (i, [vp, i]),
@@ -549,6 +550,10 @@ class Problem:
 
     def set_operator_precision(self, mask):
         self._ck(self.lib.topo_set_operator_precision(self.h, mask))
+
+    def set_reference_precision(self, enable):
+        """1: rho, coefficients and sensitivities kept at FP32 values, rho^p by powf (the reference's storage)."""
+        self._ck(self.lib.topo_set_reference_precision(self.h, int(enable)))
 
     def update_operators(self):
         self._ck(self.lib.topo_update_operators(self.h))

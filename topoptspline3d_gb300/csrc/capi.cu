@@ -927,8 +927,12 @@ int check_ready(topo_handle* h, bool need_ops) {
 
 int update_penalised_if_stale(topo_handle* h) {
   if (!h->rhop_stale) return TOPO_OK;
-  launch_penalise(h->stream, h->lv[0].d.ne, h->lv[0].eactive, h->rho, h->cfg.power_penalty, h->rhop,
-                  h->rhop32);
+  if (h->ref_fp32)
+    launch_penalise_ref32(h->stream, h->lv[0].d.ne, h->lv[0].eactive, h->rho, h->cfg.power_penalty, h->rhop,
+                          h->rhop32);
+  else
+    launch_penalise(h->stream, h->lv[0].d.ne, h->lv[0].eactive, h->rho, h->cfg.power_penalty, h->rhop,
+                    h->rhop32);
   count_launch();
   CKL();
   h->rhop_stale = false;
@@ -1392,11 +1396,25 @@ int topo_coeff_to_density(topo_handle* h) {
   if (!h) return TOPO_E_BAD_INPUT;
   if (!h->spline_set) return fail(h, TOPO_E_STATE, "spline not set (call topo_set_spline)");
   const DevLevel& L = h->lv[0];
+  if (h->ref_fp32) launch_round_f32(h->stream, (int64_t)h->sd.nb[0] * h->sd.nb[1] * h->sd.nb[2], h->coeff);
   launch_coeff_to_density(h->stream, L.d, L.eactive, h->sd, h->coeff, h->cfg.min_density,
                           h->cfg.power_penalty, h->rho, h->rhop, h->rhop32, h->adj1, h->coeff_df);
   count_launch(3);
+  if (h->ref_fp32) {  // rho stored in FP32, rho^p by powf
+    launch_penalise_ref32(h->stream, L.d.ne, L.eactive, h->rho, h->cfg.power_penalty, h->rhop, h->rhop32);
+    count_launch(2);
+  }
   CKL();
   h->rhop_stale = false;
+  h->ops_ready = false;
+  return TOPO_OK;
+}
+
+int topo_set_reference_precision(topo_handle* h, int enable) {
+  DEVICE_SCOPE(h);
+  if (!h) return TOPO_E_BAD_INPUT;
+  h->ref_fp32 = enable != 0;
+  h->rhop_stale = true;
   h->ops_ready = false;
   return TOPO_OK;
 }
@@ -1889,6 +1907,7 @@ int topo_sensitivity(topo_handle* h) {
   launch_sensitivity(h->stream, L.d, L.eactive, h->rho, L.U, h->cfg.power_penalty, h->lam, h->mu,
                      h->cfg.h, h->sens);
   count_launch();
+  if (h->ref_fp32) { launch_round_f32(h->stream, L.d.ne, h->sens); count_launch(); }
   CKL();
   return TOPO_OK;
 }
@@ -1938,6 +1957,7 @@ int topo_filter(topo_handle* h, double radius) {
   launch_filter_df(h->stream, L.d, L.eactive, h->sens, reinterpret_cast<float2*>(h->sens_tmp), h->filt_offs,
                    h->filt_wdf, h->filt_n);
   count_launch(2);
+  if (h->ref_fp32) { launch_round_f32(h->stream, L.d.ne, h->sens); count_launch(); }
   CKL();
   return TOPO_OK;
 }
@@ -1949,6 +1969,10 @@ int topo_spline_adjoint(topo_handle* h) {
   const DevLevel& L = h->lv[0];
   launch_spline_adjoint(h->stream, L.d, L.eactive, h->sd, h->sens, h->csens, h->adj1, h->adj2);
   count_launch(3);
+  if (h->ref_fp32) {
+    launch_round_f32(h->stream, (int64_t)h->sd.nb[0] * h->sd.nb[1] * h->sd.nb[2], h->csens);
+    count_launch();
+  }
   CKL();
   return TOPO_OK;
 }
@@ -2737,6 +2761,7 @@ int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_sta
     const DevLevel& L = h->lv[0];
     launch_sensitivity_from_energy(h->stream, L.d.ne, L.eactive, h->rho, h->cfg.power_penalty, h->sens);
     count_launch();
+    if (h->ref_fp32) { launch_round_f32(h->stream, L.d.ne, h->sens); count_launch(); }
     h->energy_ready = false;
   } else {
     RET(topo_sensitivity(h));

@@ -153,6 +153,7 @@ struct topo_handle {
   // into sens (want_energy), and says so (energy_ready)
   bool want_energy = false, energy_ready = false;
   int op_precision = 3;    // bit0 FP64 operators, bit1 FP32 operators
+  bool ref_fp32 = false;   // reference precision: rho, coefficients, sensitivities kept in FP32, rho^p by powf
   bool ops64 = false, ops32 = false;
   // profiling
   bool prof = false;

@@ -702,6 +702,34 @@ void launch_penalise(cudaStream_t s, int64_t ne, const uint8_t* eactive, const d
   k_penalise<<<nblk(ne, 256), 256, 0, s>>>(ne, eactive, rho, penal, rhop, rhop32);
 }
 
+// Reference precision (the reference keeps rho in FP32 and takes rho^p with
+// powf, grid/Grid.cu:1739): rho rounded to FP32, rho^p = powf(rho, p) in FP32.
+__global__ void k_penalise_ref32(int64_t ne, const uint8_t* __restrict__ eactive, double* __restrict__ rho,
+                                 float penal, double* __restrict__ rhop, float* __restrict__ rhop32) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const float r = (float)rho[e];
+  rho[e] = (double)r;
+  const float v = eactive[e] ? powf(r, penal) : 0.f;
+  rhop[e] = (double)v;
+  rhop32[e] = v;
+}
+
+void launch_penalise_ref32(cudaStream_t s, int64_t ne, const uint8_t* eactive, double* rho, double penal,
+                           double* rhop, float* rhop32) {
+  k_penalise_ref32<<<nblk(ne, 256), 256, 0, s>>>(ne, eactive, rho, (float)penal, rhop, rhop32);
+}
+
+// x[i] rounded to FP32 in place: the arrays the reference stores as float.
+__global__ void k_round_f32(int64_t n, double* __restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = (double)(float)x[i];
+}
+
+void launch_round_f32(cudaStream_t s, int64_t n, double* x) {
+  if (n > 0) k_round_f32<<<nblk(n, 256), 256, 0, s>>>(n, x);
+}
+
 // OC trial on the coefficients (optimization/optimization.cu:559-587):
 // c' = clamp(clamp(c (max(-dc,0)/thres)^damp, c-step, c+step), cmin, cmax).
 // The threshold is thres, or *thres_p when that is given (the device-side

@@ -292,6 +292,9 @@ void launch_spline_adjoint(cudaStream_t s, const LevelDims& d, const uint8_t* ea
                            double* tmp2);
 void launch_penalise(cudaStream_t s, int64_t ne, const uint8_t* eactive, const double* rho,
                      double penal, double* rhop, float* rhop32);
+void launch_penalise_ref32(cudaStream_t s, int64_t ne, const uint8_t* eactive, double* rho, double penal,
+                           double* rhop, float* rhop32);
+void launch_round_f32(cudaStream_t s, int64_t n, double* x);
 // Handle state used by the allocation-free entry point (k_noalloc.cu).
 struct SplineView {
   LevelDims d;

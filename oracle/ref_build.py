@@ -15,6 +15,10 @@ missing), but these routines are self-contained arithmetic:
                                 voxelisation by x-ray parity, Schwarz-Seidel)
   voxelizer/voxelize_main.cpp   get_point_bb, padd2SatifyResolution (the cube frame)
   voxelizer/util.h              AABox, voxinfo
+  grid/Grid.cu    applyK_OTFA_kernel, update_residual_OTFA_WS_kernel,
+                  gs_relax_OTFA_WS_kernel and the helpers they call (isValidNode,
+                  loadTemplateMatrix, loadNeighborNodesAndFlags)
+  grid/Grid.h     the Bitmask enum of grid::Grid;  culib/lib.cuh  devArray_t
 
 The recipe cuts those blocks out of the reference sources where they lie (by
 their opening lines, brace-matched) into oracle/_ref/, never into the
@@ -26,6 +30,9 @@ cubic order, which the reference's hard-wired constant does not allow).  The
 voxeliser pieces go into a third (oracle/ref_vox_harness.cpp), which supplies
 the few glm vector operations they use, written from glm's documented
 definitions (normalize = v * inversesqrt(dot(v, v)), the usual cross product).
+The fine-level elasticity kernels go into a fourth (oracle/ref_ops_harness.cpp),
+which runs every thread of a block as a host thread so their __syncthreads and
+shared-memory block sums behave as on the GPU.
 
   python -m oracle.ref_build [--reference DIR]
 """
@@ -110,13 +117,24 @@ def extract(ref: str) -> dict:
         + _block(vu, _find(vu, "struct voxinfo {"))
         + _block(vm, _find(vm, "std::pair<glm::vec3, glm::vec3> get_point_bb("))
         + _block(vm, _find(vm, "int padd2SatifyResolution(")))
+    parts["ref_bitmask.inc"] = _block(gh, _find(gh, "enum Bitmask {"))
+    parts["ref_devarray.inc"] = _block(lib, _find(lib, "struct devArray_t {"), template_prev=True)
+    parts["ref_ops.inc"] = (
+        _block(gcu, _find(gcu, "__device__ bool isValidNode(int vid)"))
+        + _block(gcu, _find(gcu, "__device__ void loadTemplateMatrix("))
+        + _block(gcu, _find(gcu, "__device__ void loadNeighborNodesAndFlags("))
+        + _block(gcu, _find(gcu, "__global__ void gs_relax_OTFA_WS_kernel("), template_prev=True)
+        + _block(gcu, _find(gcu, "__global__ void update_residual_OTFA_WS_kernel(int nv, float* rholist)"))
+        + _block(gcu, _find(gcu, "__global__ void applyK_OTFA_kernel(")))
     return {k: "\n".join(v) + "\n" for k, v in parts.items()}
 
 
 def build(ref: str = DEFAULT_REF, force: bool = False) -> list:
     """Returns the paths of the libraries (spline pieces at m_iM = 3 and 4, the
-    voxeliser); builds them when the reference sources are present."""
-    libs = [os.path.join(OUT, f"libref_pieces_m{m}.so") for m in (3, 4)] + [os.path.join(OUT, "libref_vox.so")]
+    voxeliser, the fine-level elasticity kernels); builds them when the
+    reference sources are present."""
+    libs = ([os.path.join(OUT, f"libref_pieces_m{m}.so") for m in (3, 4)] + [os.path.join(OUT, "libref_vox.so")]
+            + [os.path.join(OUT, "libref_ops.so")])
     if not force and all(os.path.exists(p) for p in libs):
         return libs
     if not os.path.isdir(os.path.join(ref, "grid")):
@@ -135,6 +153,10 @@ def build(ref: str = DEFAULT_REF, force: bool = False) -> list:
     subprocess.check_call(["g++", "-O1", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-w",
                            "-I" + OUT, os.path.join(HERE, "ref_vox_harness.cpp"), "-o", tmp])
     os.replace(tmp, libs[2])
+    tmp = libs[3] + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", "-O1", "-fPIC", "-shared", "-std=c++20", "-pthread", "-ffp-contract=off", "-w",
+                           "-I" + OUT, os.path.join(HERE, "ref_ops_harness.cpp"), "-o", tmp])
+    os.replace(tmp, libs[3])
     return libs
 
 

@@ -2181,6 +2181,28 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
       }
     }
   }
+  // ---- stage 4: joint moves the coordinate search cannot make one at a time:
+  // degrees 2, 3, 4 x lower ends 0.02, 0.04, 0.06 x inner tolerances 0.03, 0.05,
+  // from the best schedule's inner iterations and smoothing steps.  On the
+  // 256x128x128 beam degree 3 wants a lower interval end and a tighter inner
+  // tolerance together (fewer outer iterations, each V-cycle stronger), while
+  // either change alone is slower: 3 outer iterations and 14 V-cycles against
+  // 5 and 19 (solve 21.1 against 22.9 ms); degree 4 takes 12 V-cycles (20.8 ms).
+  {
+    const topo_solve_opts cur = *best;
+    const double lo4[3] = {0.02, 0.04, 0.06}, irt4[2] = {0.03, 0.05};
+    for (int deg = 2; deg <= 4; ++deg)
+      for (const double lo : lo4)
+        for (const double irt : irt4) {
+          topo_solve_opts o = cur;
+          o.cheb_degree = deg;
+          o.cheb_lo = lo;
+          o.inner_rtol = irt;
+          double ms = 0;
+          ++r.candidates;
+          if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+        }
+  }
   r.best_ms = bt;
   cudaMemcpyAsync(L0.U, u0, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream);
   CK(cudaEventRecord(t1, h->stream));

@@ -240,6 +240,14 @@ int topo_apply_fine(topo_handle* h, int precision);
  * error-free transformations, ~48-bit significands, on the FP32 pipe; default).
  * Vectors, dot products and step lengths stay FP64 either way. */
 int topo_set_fine_arithmetic(topo_handle* h, int arith);
+/* Element products of the FP32 fine kernels (the multigrid smoother, residual
+ * and operator on level 0, the preconditioner's side of the mixed solve): 0 =
+ * the modal form on the FP32 pipe, 1 = on the tensor cores (tcgen05.mma in
+ * three-term TF32, u_hi K_hi + u_hi K_lo + u_lo K_hi with fp32 accumulators in
+ * tensor memory: FP32-level accuracy).  Levels with void planes keep the modal
+ * form.  Grid::gs_relax / update_residual on the finest level
+ * (grid/Grid.cu:1698-1842, 2277-2333) have no tensor-core counterpart. */
+int topo_set_fine_tensor_cores(topo_handle* h, int on);
 /* FP32 V-cycles of the mixed solver replayed as one CUDA graph per handle
  * (captured on first use, re-captured when the schedule, spectral bounds,
  * tiles or buffers change): 1 = on (default), 0 = direct launches.  Graphs are
@@ -401,8 +409,10 @@ int topo_design_batch(topo_handle** handles, int n, const topo_iter_opts* opts, 
 /* --- autotuner ------------------------------------------------------------ */
 /* Tile and schedule choice for the current problem state (no reference
  * counterpart).  Stage 1 times the fine-level kernels at z-march depths
- * 4, 8, 16 and 32 (the FP32 Chebyshev step and the FP64 operator, CUDA events,
- * 5 launches each) and keeps the fastest for the handle.  Stage 2 solves from the
+ * 4, 8, 16 and 32 (the FP32 Chebyshev step with the modal and with the
+ * tensor-core element products, and the FP64 operator; CUDA events, 5 launches
+ * each) and keeps the fastest for the handle (depths and
+ * topo_set_fine_tensor_cores).  Stage 2 solves from the
  * current U with each candidate schedule of the mixed solver (FP32 inner
  * iterations 1, 2, 4, 6 x smoothing steps 1, 2 x Chebyshev degree 2, 3 x lower
  * end of the Chebyshev interval base->cheb_lo, 0.1 x inner tolerance
@@ -419,6 +429,8 @@ typedef struct topo_tune_report {
   int candidates;           /* schedules tried */
   double base_ms, best_ms;  /* solve time of *base and of *best */
   double tune_ms;           /* device time spent tuning */
+  int tc;                   /* FP32 fine element products chosen: 1 tensor cores, 0 modal */
+  double cheb_tc_ms[4];     /* FP32 Chebyshev step on the tensor cores at depths 4, 8, 16, 32 */
 } topo_tune_report;
 int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* best, topo_tune_report* report);
 /* Sets the fine kernels' z-march depths (FP32 kernels, FP64 operator) directly,
@@ -568,6 +580,14 @@ int topo_support_constraints(topo_handle* h, const topo_support_opts* opts, topo
  * (N = 0: the plain V-cycle).  No reference counterpart. */
 /* Creates the network of h with He-normal weights from `seed`. */
 int topo_unet_enable(topo_handle* h, unsigned long long seed);
+/* Kernel of the network's 3x3x3 convolutions (forward and data gradient):
+ * TOPO_CONV_TCGEN05 (default) runs them on the 5th-generation tensor cores
+ * (tcgen05.mma, fp32 accumulators in tensor memory, input halo by TMA tensor
+ * loads), TOPO_CONV_MMA_SYNC on the warp-level mma.sync path.  Both compute
+ * bf16 x bf16 -> fp32 in the same layouts; they differ only in the fp32
+ * summation order. */
+enum { TOPO_CONV_MMA_SYNC = 0, TOPO_CONV_TCGEN05 = 1 };
+int topo_unet_set_conv_kernel(topo_handle* h, int kind);
 /* Parameter count of the flat fp32 layout: per layer W[cout][27][cin] then b[cout],
  * layers L0a L0b L1a L1b L2a L2b D1a D1b D0a D0b (cin of L0a padded to 16 with
  * channels 0-7 used, cout of D0b 16 with channels 0-2 used). */

@@ -21,7 +21,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "libtopo_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["capi.cu", "k_fine.cu", "k_coarse.cu", "k_vec.cu", "k_design.cu", "k_noalloc.cu", "k_mma.cu", "k_unet.cu", "unet.cu", "k_multi.cu", "worst.cu", "io.cu", "voxel.cu", "support.cu"]
+CU_SOURCES = ["capi.cu", "k_fine.cu", "k_coarse.cu", "k_vec.cu", "k_design.cu", "k_noalloc.cu", "k_mma.cu", "k_unet.cu", "k_conv_tc.cu", "unet.cu", "k_multi.cu", "worst.cu", "io.cu", "voxel.cu", "support.cu"]
 CPP_SOURCES = ["host_setup.cpp", "bc_regions.cpp"]
 # per-file nvcc flags: the voxeliser reproduces the reference's FP32 tests
 # operation for operation, so no multiply-add contraction there

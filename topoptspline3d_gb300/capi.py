@@ -24,6 +24,7 @@ ARRAYS = {"rho": 0, "rhop": 1, "coeff": 2, "sens": 3, "csens": 4, "u": 5, "f": 6
 BYTE_ARRAYS = {"vmask", "eactive"}
 
 SOLVE_VCYCLE, SOLVE_PCG64, SOLVE_MIXED = 0, 1, 2
+CONV_MMA_SYNC, CONV_TCGEN05 = 0, 1
 UNET_IN = 8  # network input channels: r xyz, z xyz (local units), log-density, 0
 SMOOTH_GS, SMOOTH_CHEBYSHEV = 0, 1
 K_FINE_APPLY64, K_FINE_APPLY32, K_FINE_SMOOTH64, K_FINE_SMOOTH32 = 0, 1, 2, 3
@@ -43,9 +44,9 @@ EXPORTED = [
     "topo_mma_create", "topo_mma_create_for", "topo_mma_destroy", "topo_mma_last_error", "topo_mma_size",
     "topo_mma_set_constraint_amplifier", "topo_mma_init", "topo_mma_init_uniform", "topo_mma_update",
     "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x", "topo_set_bc_regions", "topo_plan_bc_regions",
-    "topo_unet_enable", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
+    "topo_unet_enable", "topo_unet_set_conv_kernel", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
-    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic",
+    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic", "topo_set_fine_tensor_cores",
     "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
     "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
     "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
@@ -98,7 +99,8 @@ class BatchStats(C.Structure):
 
 class TuneReport(C.Structure):
     _fields_ = [("tz32", C.c_int), ("tz64", C.c_int), ("cheb_ms", C.c_double * 4), ("apply_ms", C.c_double * 4),
-                ("candidates", C.c_int), ("base_ms", C.c_double), ("best_ms", C.c_double), ("tune_ms", C.c_double)]
+                ("candidates", C.c_int), ("base_ms", C.c_double), ("best_ms", C.c_double), ("tune_ms", C.c_double),
+                ("tc", C.c_int), ("cheb_tc_ms", C.c_double * 4)]
 
 
 class MultiStats(C.Structure):
@@ -210,8 +212,10 @@ def load(build: bool = True):
         "topo_spline_adjoint_noalloc": (i, [vp, vp, vp]),
         "topo_volume_csens": (i, [vp, i, d, vp]),
         "topo_unet_enable": (i, [vp, C.c_ulonglong]),
+        "topo_unet_set_conv_kernel": (i, [vp, i]),
         "topo_multi_reserve": (i, [vp, i]),
         "topo_set_fine_arithmetic": (i, [vp, i]),
+        "topo_set_fine_tensor_cores": (i, [vp, i]),
         "topo_set_graphs": (i, [vp, i]),
         "topo_set_tiles": (i, [vp, i, i]),
         "topo_profiler_range": (i, [i]),
@@ -548,6 +552,10 @@ class Problem:
         """0: native FP64 fine operator, 1: double-float (default)."""
         self._ck(self.lib.topo_set_fine_arithmetic(self.h, arith))
 
+    def set_fine_tensor_cores(self, on):
+        """FP32 fine element products on the tcgen05 tensor cores (three-term TF32)."""
+        self._ck(self.lib.topo_set_fine_tensor_cores(self.h, int(bool(on))))
+
     def set_operator_precision(self, mask):
         self._ck(self.lib.topo_set_operator_precision(self.h, mask))
 
@@ -611,7 +619,8 @@ class Problem:
         self._ck(self.lib.topo_autotune(self.h, C.byref(o), C.byref(best), C.byref(r)))
         bd = {k: getattr(best, k) for k in keys}
         rep = {"tz32": r.tz32, "tz64": r.tz64, "cheb_ms": list(r.cheb_ms), "apply_ms": list(r.apply_ms),
-               "candidates": r.candidates, "base_ms": r.base_ms, "best_ms": r.best_ms, "tune_ms": r.tune_ms}
+               "candidates": r.candidates, "base_ms": r.base_ms, "best_ms": r.best_ms, "tune_ms": r.tune_ms,
+               "tc": r.tc, "cheb_tc_ms": list(r.cheb_tc_ms)}
         return bd, rep
 
     # --- many load cases
@@ -648,6 +657,10 @@ class Problem:
 
     def unet_enable(self, seed=1):
         self._ck(self.lib.topo_unet_enable(self.h, seed))
+
+    def unet_set_conv_kernel(self, kind):
+        """CONV_TCGEN05 (default) or CONV_MMA_SYNC for the network's convolutions."""
+        self._ck(self.lib.topo_unet_set_conv_kernel(self.h, kind))
 
     @staticmethod
     def unet_num_params() -> int:

@@ -26,6 +26,7 @@ thread_local long long t_launches = 0;
 
 using namespace topo;
 
+
 // The sums fused into the FP32 fine kernels finish in their last CTA (1) or
 // in a one-CTA kernel after them (0).  Measured at 256x128x128: without the
 // last-CTA ticket (a fence and an atomic per CTA while the CTA waits) the
@@ -43,6 +44,9 @@ using namespace topo;
 #endif
 
 #include "handle.h"
+
+// z-march depth argument of the handle's FP32 fine-kernel launches
+static inline int tz32_arg(const topo_handle* h) { return h->tz32 | (h->fine_tc ? TOPO_FINE_TC_FLAG : 0); }
 
 namespace {
 
@@ -212,7 +216,7 @@ void level_apply(topo_handle* h, int l, const T* u, const T* f, T* out, bool res
                            reinterpret_cast<double*>(out), residual, h->nb, h->tz64);
     else
       launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, u, f, out, residual, h->nb,
-                           sizeof(T) == 4 ? h->tz32 : h->tz64);
+                           sizeof(T) == 4 ? tz32_arg(h) : h->tz64);
     prof_end(h, ev);
   } else {
     launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), u, f, out, residual, h->nb);
@@ -287,7 +291,7 @@ void cheb_level(topo_handle* h, int l, const ChebParams& cp, bool zero_start, bo
       EventPair* ev = prof_begin(h, P<T>::fam_smooth);
       const int np = launch_fine_cheb<T>(
           h->stream, L.d, P<T>::rhop(h), L.vmask, ua, P<T>::F(L), ub, P<T>::dinv(L), P<T>::cd(L), coef, k == 0,
-          h->nb, sizeof(T) == 4 ? h->tz32 : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr, h->fdot_cap,
+          h->nb, sizeof(T) == 4 ? tz32_arg(h) : h->tz64, d_in_u && k == 1, dots ? h->vdot : nullptr, h->fdot_cap,
           h->vdot_out, TOPO_FUSED_DOT_TICKET ? h->ctr : nullptr);
       if (np > 0 && !TOPO_FUSED_DOT_TICKET) {
         launch_sum_partials(h->stream, h->vdot, np, h->vdot_out);
@@ -384,7 +388,7 @@ void vcycle_core(topo_handle* h, int pre, int post, bool sym, int smoother, cons
 static std::vector<double> vcycle_key(const topo_handle* h, int pre, int post, int smoother, const ChebParams& cp,
                                       bool zero0) {
   std::vector<double> key = {(double)pre, (double)post, (double)smoother, (double)cp.degree,
-                             (double)h->tz32, (double)h->nb, (double)h->prof, (double)zero0,
+                             (double)tz32_arg(h), (double)h->nb, (double)h->prof, (double)zero0,
                              (double)h->vdot_on, (double)(uintptr_t)h->vdot_out};
   for (const DevLevel& L : h->lv) {
     key.push_back((double)(uintptr_t)L.U32);
@@ -606,7 +610,7 @@ int estimate_bounds(topo_handle* h) {
     for (int it = 0; it < k; ++it) {
       launch_dot<T>(h->stream, r.x, r.x, n3, h->partial, sl, h->ctr);
       if (r.l == 0) launch_fine_apply<T>(h->stream, L.d, P<T>::rhop(h), L.vmask, r.x, nullptr, r.y, false, 1,
-                                         sizeof(T) == 4 ? h->tz32 : h->tz64);
+                                         sizeof(T) == 4 ? tz32_arg(h) : h->tz64);
       else launch_stencil_apply<T>(h->stream, L.d, P<T>::st(L), r.x, nullptr, r.y, false);
       k_dinv_apply<T><<<nb256(L.d.nv), 256, 0, h->stream>>>(L.d.nv, P<T>::dinv(L), r.y, r.z, sl,
                                                            sizeof(T) == 4 && r.l == 0);
@@ -721,7 +725,7 @@ int fcg_body(topo_handle* h, T* x, T* r, T* d, T* q, T* rold, T* z, double* sc, 
   int nparts = 0;
   if (sizeof(T) == 4 && h->fdot && h->nb == 1) {
     EventPair* ev = prof_begin(h, P<T>::fam_apply);
-    nparts = launch_fine_apply_dot<T>(h->stream, L0.d, P<T>::rhop(h), L0.vmask, d, q, h->tz32, h->fdot,
+    nparts = launch_fine_apply_dot<T>(h->stream, L0.d, P<T>::rhop(h), L0.vmask, d, q, tz32_arg(h), h->fdot,
                                       h->fdot_cap, sc + S_DQ, TOPO_FUSED_DOT_TICKET ? h->ctr : nullptr);
     if (nparts > 0 && !TOPO_FUSED_DOT_TICKET) {
       launch_sum_partials(h->stream, h->fdot, nparts, sc + S_DQ);
@@ -871,7 +875,7 @@ int inner_cg_graphed(topo_handle* h, const double* rin, double* zout, double rto
   double* sc = h->sc + 8;
   key.insert(key.end(), {rtol, (double)maxit, (double)(uintptr_t)rin, (double)(uintptr_t)zout,
                          (double)(uintptr_t)h->x32, (double)(uintptr_t)h->d32, (double)(uintptr_t)h->q32,
-                         (double)h->tz32, (double)(uintptr_t)h->fdot, (double)h->fdot_cap});
+                         (double)tz32_arg(h), (double)(uintptr_t)h->fdot, (double)h->fdot_cap});
   if (!h->igraph || key != h->ikey) {
     if (h->igraph) { cudaGraphExecDestroy(h->igraph); h->igraph = nullptr; }
     auto setup = [&](cudaGraphConditionalHandle hc) -> int {
@@ -1718,7 +1722,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
     }
     auto net = [&](const float* r32, float* z32) -> int {
       if (!net_on) return TOPO_OK;
-      const cudaError_t e = unet_apply(h->unet, h->stream, L0.d, L0.vmask, h->rhop32, h->tz32, r32, z32, h->partial);
+      const cudaError_t e = unet_apply(h->unet, h->stream, L0.d, L0.vmask, h->rhop32, tz32_arg(h), r32, z32, h->partial);
       if (e != cudaSuccess) return fail(h, TOPO_E_CUDA, "U-Net apply: %s", cudaGetErrorString(e));
       ++st.learned_applied;
       return TOPO_OK;
@@ -2003,6 +2007,13 @@ int topo_set_graphs(topo_handle* h, int enable) {
   return TOPO_OK;
 }
 
+int topo_set_fine_tensor_cores(topo_handle* h, int on) {
+  DEVICE_SCOPE(h);
+  if (!h || on < 0 || on > 1) return TOPO_E_BAD_INPUT;
+  h->fine_tc = on != 0;
+  return TOPO_OK;
+}
+
 int topo_set_fine_arithmetic(topo_handle* h, int arith) {
   DEVICE_SCOPE(h);
   if (!h || arith < 0 || arith > 1) return TOPO_E_BAD_INPUT;
@@ -2078,17 +2089,21 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
   const int tzs[4] = {4, 8, 16, 32};
   int best32 = h->tz32, best64 = h->tz64;
   double b32 = 1e30, b64 = 1e30;
+  int best_tc = h->fine_tc ? 1 : 0;
   for (int k = 0; k < 4; ++k) {
-    for (int rep = 0; rep < 2; ++rep) {  // warm-up, then timed
-      CK(cudaEventRecord(a, h->stream));
-      for (int i = 0; i < 5; ++i)
-        launch_fine_cheb<float>(h->stream, L0.d, h->rhop32, L0.vmask, L0.U32, L0.F32, L0.U2_32, L0.dinv32, L0.cd32,
-                                unit, true, 1, tzs[k]);
-      CK(cudaEventRecord(b, h->stream));
-      CK(cudaEventSynchronize(b));
-      float ms = 0;
-      cudaEventElapsedTime(&ms, a, b);
-      r.cheb_ms[k] = ms / 5;
+    // the FP32 Chebyshev step with the modal element products and on the tensor cores
+    for (int tc = 0; tc < 2; ++tc) {
+      for (int rep = 0; rep < 2; ++rep) {  // warm-up, then timed
+        CK(cudaEventRecord(a, h->stream));
+        for (int i = 0; i < 5; ++i)
+          launch_fine_cheb<float>(h->stream, L0.d, h->rhop32, L0.vmask, L0.U32, L0.F32, L0.U2_32, L0.dinv32,
+                                  L0.cd32, unit, true, 1, tzs[k] | (tc ? TOPO_FINE_TC_FLAG : 0));
+        CK(cudaEventRecord(b, h->stream));
+        CK(cudaEventSynchronize(b));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        (tc ? r.cheb_tc_ms : r.cheb_ms)[k] = ms / 5;
+      }
     }
     for (int rep = 0; rep < 2; ++rep) {
       CK(cudaEventRecord(a, h->stream));
@@ -2102,15 +2117,18 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
       cudaEventElapsedTime(&ms, a, b);
       r.apply_ms[k] = ms / 5;
     }
-    count_launch(20);
-    if (r.cheb_ms[k] < b32) { b32 = r.cheb_ms[k]; best32 = tzs[k]; }
+    count_launch(30);
+    if (r.cheb_ms[k] < b32) { b32 = r.cheb_ms[k]; best32 = tzs[k]; best_tc = 0; }
+    if (r.cheb_tc_ms[k] < b32) { b32 = r.cheb_tc_ms[k]; best32 = tzs[k]; best_tc = 1; }
     if (r.apply_ms[k] < b64) { b64 = r.apply_ms[k]; best64 = tzs[k]; }
   }
   CKL();
   h->tz32 = best32;
   h->tz64 = best64;
+  h->fine_tc = best_tc != 0;
   r.tz32 = best32;
   r.tz64 = best64;
+  r.tc = best_tc;
   // ---- stage 2: solver schedule, each candidate from the same initial U
   double* u0 = nullptr;
   CK(cudaMalloc((void**)&u0, sizeof(double) * n3));
@@ -2372,6 +2390,14 @@ int topo_unet_enable(topo_handle* h, unsigned long long seed) {
   if (h->unet) { unet_free(h->unet); h->unet = nullptr; }
   const cudaError_t e = unet_create(&h->unet, h->stream, seed);
   if (e != cudaSuccess) { h->unet = nullptr; return fail(h, e == cudaErrorMemoryAllocation ? TOPO_E_NOMEM : TOPO_E_CUDA, "U-Net: %s", cudaGetErrorString(e)); }
+  return TOPO_OK;
+}
+
+int topo_unet_set_conv_kernel(topo_handle* h, int kind) {
+  if (!h) return TOPO_E_BAD_INPUT;
+  if (!h->unet) return fail(h, TOPO_E_STATE, "learned preconditioner not enabled (topo_unet_enable)");
+  if (kind != TOPO_CONV_TCGEN05 && kind != TOPO_CONV_MMA_SYNC) return fail(h, TOPO_E_BAD_INPUT, "unknown convolution kernel %d", kind);
+  unet_set_conv_kernel(h->unet, kind);
   return TOPO_OK;
 }
 

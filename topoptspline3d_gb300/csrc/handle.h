@@ -43,6 +43,7 @@ struct topo_handle {
   int nb = 1;                       // right-hand sides the level vectors hold (multi-RHS solve)
   int fine_df = 1;                  // FP64 fine operator in double-float arithmetic (topo_set_fine_arithmetic)
   int tz32 = 16, tz64 = 16;         // z-march depth of the fine kernels, FP32 / FP64 (topo_autotune)
+  bool fine_tc = false;             // FP32 fine element products on the tensor cores (topo_set_fine_tensor_cores)
   // FP32 V-cycle replayed as one CUDA graph (topo_set_graphs); re-captured when its key changes
   bool graphs = true;
   cudaGraphExec_t vgraph = nullptr;

@@ -426,16 +426,17 @@ __global__ void __launch_bounds__(TXE* TYE, sizeof(T) == 4 ? modal_min_ctas(TXE 
   const int t = threadIdx.x, i = t % TXE, j = t / TXE;
   // blockIdx.z enumerates (right-hand side, z block): vectors of a batch of
   // right-hand sides are stored one after another, the operator is shared
-  const int zblk = (d.vz + TZ - 1) / TZ;
+  const int zblk = fine_zblocks(d.vz, TZ);
   const int rhs = blockIdx.z / zblk;
-  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int kz = blockIdx.z - rhs * zblk;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = kz * TZ;
   const int64_t nv = d.nv;
   u += (int64_t)rhs * 3 * nv;
   if (f) f += (int64_t)rhs * 3 * nv;
   out += (int64_t)rhs * 3 * nv;
   const int gx = x0 + i, gy = y0 + j;  // owned vertex (x, y) and element (x-1, y-1)
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
-  const int zb1 = min(zb0 + TZ, d.vz);
+  const int zb1 = fine_zblock_end(d.vz, TZ, kz);
   int z0, zend;  // the planes marched: [zb0, zb1) less the void
   fine_active_planes<VOID>(d, zb0, zb1, z0, zend);
   T acc0 = T(0), acc1 = T(0), acc2 = T(0);
@@ -708,16 +709,17 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
     sm.coef[0] = float(ch.coef[0]);
     sm.coef[1] = float(ch.coef[1]);
   }
-  const int zblk = (d.vz + TZ - 1) / TZ;
+  const int zblk = fine_zblocks(d.vz, TZ);
   const int rhs = blockIdx.z / zblk;
-  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int kz = blockIdx.z - rhs * zblk;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = kz * TZ;
+  const int zb1 = zb0 + TZ + (kz + 1 == zblk ? d.vz - zblk * TZ : 0);  // fine_zblock_end
   const I nv = (I)d.nv;
   u += (int64_t)rhs * 3 * d.nv;
   if (f) f += (int64_t)rhs * 3 * d.nv;
   out += (int64_t)rhs * 3 * d.nv;
   const int gx = x0 + i, gy = y0 + j;
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
-  const int zb1 = min(zb0 + TZ, d.vz);
   int z0, zend;  // the planes marched: [zb0, zb1) less the void
   fine_active_planes<VOID>(d, zb0, zb1, z0, zend);
   constexpr int KS = (NP + NT - 1) / NT;
@@ -891,6 +893,370 @@ __global__ void __launch_bounds__(32 * TYE, modal_min_ctas(32 * TYE, MODE >= 2 ?
   }
 }
 
+// ---------------------------------------------------------------------------
+// The FP32 z march with the element products on the tensor cores (tcgen05,
+// kind::tf32, fp32 accumulators in tensor memory), in three-term TF32
+// arithmetic: u = u_hi + u_lo and Ke = K_hi + K_lo with u_hi, K_hi exact in
+// TF32, and u.Ke ~ u_hi K_hi + u_hi K_lo + u_lo K_hi (the dropped u_lo K_lo is
+// 2^-22 of the product), which keeps the FP32 kernel's accuracy.
+//
+// Per element layer the products are one GEMM per half tile: M = 128 elements
+// (32 along x by 4 rows of y), N = 32 (8 nodes x (3 force components + 1
+// zero)), K = 32 (8 nodes x (3 displacement components + 1 zero)), issued as
+// 4 K steps of 8, one per (dy, dz) node pair: the A operand of K step (dy,
+// dz) is the staged vertex plane z + dz, rows y + dy, read straight from
+// shared memory (float4 per vertex, 32 vertices per row: core matrices of 8
+// consecutive x, 128 bytes apart; the second 4 K values are the x + 1 vertex,
+// 16 bytes on -- the leading-dimension offset).  Lane i of warp j reads the
+// 32 columns of its element (i, j) from tensor-memory lane i + 32 (j % 4), so
+// after the read-back the thread holds exactly what the SIMT kernel's
+// modal_element leaves (times rho^p), and the rest of the step (x combine,
+// y exchange, vertex update) is the SIMT kernel's.
+//
+// A 32-vertex plane row has no halo column: lane 31's element reads the next
+// row's first vertex (or a zero padding row) for its x + 1 nodes and is not
+// used, so a CTA owns 30 vertex columns (the SIMT kernel: 31).
+//
+// Software pipeline, one barrier per step st:
+//   before the barrier: cp.async of plane st + 2 (2-slot raw ring), TF32 split
+//     of this thread's staged vertices of plane st + 1 (3-slot ring);
+//   after it: one thread issues the 24 MMAs of layer st into accumulator
+//     st % 2 and commits them to mbarrier st % 2; all threads update the
+//     vertices of plane st - 2 and read back layer st - 1 (issued one step
+//     earlier, so its products are normally complete by then).
+// The owned vertex's own value is read from global memory one step ahead.
+// ---------------------------------------------------------------------------
+template <int TYE>
+struct Modal32TcSmem {
+  static constexpr int TXE = 32, NT = TXE * TYE, PX = 32, PY = TYE + 1, NP = PX * PY, NPA = NP + PX;
+  float4 raw[2][NP];     // cp.async ring of vertex planes (u0, u1, u2, -)
+  float4 ahi[3][NPA];    // TF32 high parts (u0, u1, u2, 0); one zero row of padding
+  float4 alo[3][NPA];    // low parts u - hi
+  float4 bhi[4][2][32];  // Ke per K step (dy, dz): [dx][n = 4 node + component][4 displacement components]
+  float4 blo[4][2][32];
+  float4 xa[2][NT];      // exchanged y = 0 forces (as Modal32Smem)
+  float2 xb[2][NT];
+  float coef[2];
+  unsigned long long bar[2];
+  uint32_t tmem;
+};
+
+__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  // tcgen05 shared-memory descriptor, no swizzle: start, leading- and
+  // stride-dimension byte offsets (>> 4), version 0b001 at bit 46
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool tc_bar_wait(unsigned long long* bar, uint32_t parity) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+  for (int it = 0; it < (1 << 24); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ int g_fine_tc_err;
+
+template <int TYE, int MODE, bool I32>
+__global__ void __launch_bounds__(32 * TYE, 3)
+    k_fine_tc32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,
+                const float* __restrict__ u, const float* __restrict__ f, float* __restrict__ out, int TZ,
+                ChebArgs ch) {
+  static_assert(TYE == 8, "two M = 128 tiles of 32 x 4 elements per layer");
+  constexpr bool CHEB = MODE >= 2, DOTS = MODE == 3;
+  using I = typename std::conditional<I32, int, int64_t>::type;
+  using S = Modal32TcSmem<TYE>;
+  constexpr int TXE = 32, NT = S::NT, PX = S::PX, NP = S::NP, NPA = S::NPA;
+  // D fp32, A and B tf32 (format 2), K-major, N = 32, M = 128
+  constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+  constexpr uint32_t SLOT = NPA * 16;  // bytes of one plane slot
+  extern __shared__ __align__(16) unsigned char tc_smem[];
+  S& sm = *reinterpret_cast<S*>(tc_smem);
+  const int t = threadIdx.x, i = t & 31, j = t >> 5;
+  if (t == 0) {
+    if (CHEB) {
+      sm.coef[0] = float(ch.coef[0]);
+      sm.coef[1] = float(ch.coef[1]);
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&sm.bar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&sm.bar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (j == 0) {  // two accumulators of 2 x 32 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
+        (uint32_t)__cvta_generic_to_shared(&sm.tmem)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  // Ke operand: entry (s, dx, n, c) = Ke[(3 b + comp) 24 + 3 a + c], node a =
+  // dx + 2 dy + 4 dz of K step s = dy + 2 dz, n = 4 b + comp; zero rows and
+  // columns for the fourth components
+  for (int e = t; e < 4 * 2 * 32 * 4; e += NT) {
+    const int c = e & 3, n = (e >> 2) & 31, dx = (e >> 7) & 1, s = e >> 8;
+    const int a = dx + 2 * (s & 1) + 4 * (s >> 1), b = n >> 2, comp = n & 3;
+    const double k = (comp < 3 && c < 3) ? cKe64[(3 * b + comp) * 24 + 3 * a + c] : 0.0;
+    const float hi = tf32_hi((float)k);
+    reinterpret_cast<float*>(&sm.bhi[s][dx][n])[c] = hi;
+    reinterpret_cast<float*>(&sm.blo[s][dx][n])[c] = (float)(k - (double)hi);
+  }
+  for (int e = NP + t; e < NPA; e += NT) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) sm.ahi[q][e] = sm.alo[q][e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = sm.tmem;
+
+  const int zblk = fine_zblocks(d.vz, TZ);
+  const int rhs = blockIdx.z / zblk;
+  const int kz = blockIdx.z - rhs * zblk;
+  const int x0 = blockIdx.x * (TXE - 2), y0 = blockIdx.y * (TYE - 1), zb0 = kz * TZ;
+  const int zb1 = zb0 + TZ + (kz + 1 == zblk ? d.vz - zblk * TZ : 0);  // fine_zblock_end
+  const I nv = (I)d.nv;
+  u += (int64_t)rhs * 3 * d.nv;
+  if (f) f += (int64_t)rhs * 3 * d.nv;
+  out += (int64_t)rhs * 3 * d.nv;
+  const int gx = x0 + i, gy = y0 + j;
+  const bool own = (i < TXE - 2) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
+  const int z0 = zb0, zend = zb1;
+  constexpr int KS = (NP + NT - 1) / NT;
+  int pxy[KS];
+#pragma unroll
+  for (int s = 0; s < KS; ++s) {
+    const int k = t + s * NT, px = k % PX, py = k / PX;
+    const int vx = x0 - 1 + px, vy = y0 - 1 + py;
+    pxy[s] = (k < NP && vx >= 0 && vy >= 0 && vx < d.vx && vy < d.vy) ? vx + d.vx * vy : -1;
+  }
+  const I plane_n = (I)d.vx * d.vy;
+  auto prefetch = [&](int z) {
+    if (z <= zend) {
+      float4* dst = sm.raw[z & 1];
+      const bool zok = z >= 0 && z < d.vz;
+      const I zoff = (I)z * plane_n;
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        const int k = t + s * NT;
+        if (k < NP) {
+          const bool ok = zok && pxy[s] >= 0;
+          const I v = ok ? zoff + pxy[s] : 0;
+          cp_async_4(&dst[k].x, u + v, ok);
+          cp_async_4(&dst[k].y, u + nv + v, ok);
+          cp_async_4(&dst[k].z, u + 2 * nv + v, ok);
+        }
+      }
+    }
+    cp_async_commit();
+  };
+  // TF32 split of this thread's staged vertices of plane z (own cp.async
+  // copies, complete after cp_async_wait1) into slot (z + 3) % 3
+  auto split = [&](int z) {
+    const int q = (z + 3) % 3;
+#pragma unroll
+    for (int s = 0; s < KS; ++s) {
+      const int k = t + s * NT;
+      if (k < NP) {
+        const float4 v = sm.raw[z & 1][k];
+        const float h0 = tf32_hi(v.x), h1 = tf32_hi(v.y), h2 = tf32_hi(v.z);
+        sm.ahi[q][k] = make_float4(h0, h1, h2, 0.f);
+        sm.alo[q][k] = make_float4(v.x - h0, v.y - h1, v.z - h2, 0.f);
+      }
+    }
+  };
+  const int pex = gx - 1, pey = gy - 1;
+  const bool pe_xy = pex >= 0 && pey >= 0 && pex < d.ex && pey < d.ey;
+  auto load_pe = [&](int ez) -> float {
+    return (pe_xy && ez >= 0 && ez < d.ez) ? rhop[pex + (I)d.ex * (pey + (I)d.ey * ez)] : 0.f;
+  };
+  const float* __restrict__ dvin =
+      (CHEB && !ch.first && !ch.d_is_u) ? static_cast<const float*>(ch.dvec) + (int64_t)rhs * 3 * d.nv : nullptr;
+  constexpr bool NEED_U = CHEB || MODE == 0;
+  // operands of the owned vertex at plane z, read in step z + 1 and used in step z + 2
+  uint8_t vm_n = 0;
+  float f_n[3] = {0.f, 0.f, 0.f}, dv_n[3] = {0.f, 0.f, 0.f}, u_n[3] = {0.f, 0.f, 0.f};
+  auto load_vertex = [&](int z) {
+    if (!own || z < z0 || z >= zend) return;
+    const I v = gx + (I)d.vx * (gy + (I)d.vy * z);
+    vm_n = vmask[v];
+    if (MODE >= 1) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f_n[c] = f[c * nv + v];
+    }
+    if (CHEB && dvin) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) dv_n[c] = dvin[c * nv + v];
+    }
+    if (NEED_U && (CHEB || ch.dotp)) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) u_n[c] = u[c * nv + v];
+    }
+  };
+  // descriptors of slot 0 / K step 0; the others by adding the byte offset >> 4
+  // to the start-address field (shared addresses stay below 2^18 bytes)
+  const uint64_t dah0 = tc_desc((uint32_t)__cvta_generic_to_shared(&sm.ahi[0][0]), 16, 128);
+  const uint64_t dal0 = tc_desc((uint32_t)__cvta_generic_to_shared(&sm.alo[0][0]), 16, 128);
+  const uint64_t dbh0 = tc_desc((uint32_t)__cvta_generic_to_shared(&sm.bhi[0][0][0]), 512, 128);
+  const uint64_t dbl0 = tc_desc((uint32_t)__cvta_generic_to_shared(&sm.blo[0][0][0]), 512, 128);
+  float own1[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+  float top[3] = {0.f, 0.f, 0.f};
+  float dsum = 0.f;
+  bool tc_ok = true;
+  float pe_n = 0.f;  // rho^p of layer st - 1, read in step st - 1
+  if (z0 < zend) {
+    prefetch(z0 - 1);
+    prefetch(z0);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    split(z0 - 1);
+    for (int st = z0 - 1; st <= zend + 1; ++st) {
+      prefetch(st + 2);
+      const float pe = pe_n;  // layer st - 1
+      const uint8_t vm_c = vm_n;
+      float f_c[3], dv_c[3], u_c[3];  // plane st - 2
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { f_c[c] = f_n[c]; dv_c[c] = dv_n[c]; u_c[c] = u_n[c]; }
+      pe_n = load_pe(st);
+      load_vertex(st - 1);
+      cp_async_wait1();
+      split(st + 1);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int q = st - (z0 - 1);  // layer index in this CTA
+      // ---- the products of layer st into accumulator q % 2, issued by lane 0 of
+      // the last warp (its row owns no vertices, so it has the least to do)
+      if (st < zend && t == NT - 32 && tc_ok) {
+        const uint32_t s0 = (uint32_t)((st + 3) % 3), s1 = (uint32_t)((st + 4) % 3);
+#pragma unroll
+        for (int T = 0; T < 2; ++T) {
+#pragma unroll
+          for (int s = 0; s < 4; ++s) {
+            const int dy = s & 1, dz = s >> 1;
+            const uint32_t off = ((dz ? s1 : s0) * SLOT + (uint32_t)((4 * T + dy) * PX) * 16) >> 4;
+            const uint32_t boff = (uint32_t)(s * 1024) >> 4;
+            const uint32_t dt = tmem + 64 * (q & 1) + 32 * T;
+            // hi.hi (overwrites D at the first K step), hi.lo, lo.hi
+            asm volatile(
+                "{\n.reg .pred p, r;\nsetp.ne.b32 p, %6, 0;\nsetp.eq.b32 r, %6, %6;\n"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %5, p;\n"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %3, %5, r;\n"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %4, %2, %5, r;\n}\n" ::"r"(dt),
+                "l"(dah0 + off), "l"(dbh0 + boff), "l"(dbl0 + boff), "l"(dal0 + off), "r"(IDESC), "r"(s));
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(&sm.bar[q & 1]))
+                     : "memory");
+      }
+      // ---- vertex plane p = st - 2 (layers st - 3 and st - 2 read back)
+      if (st >= z0 + 1) {
+        const int p = st - 2, xs = p & 1;
+        float y[3];
+        if (own) {
+          const float4 ra = sm.xa[xs][t + TXE];
+          const float2 rb = sm.xb[xs][t + TXE];
+          const float r0[3] = {ra.x, ra.y, ra.z}, r1[3] = {ra.w, rb.x, rb.y};
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            y[c] = top[c] + (own1[0][c] + r0[c]);
+            top[c] = own1[1][c] + r1[c];
+          }
+          if (p >= z0) {
+            const I v = gx + (I)d.vx * (gy + (I)d.vy * p);
+            const uint8_t m = vm_c;
+            const float uv[3] = {u_c[0], u_c[1], u_c[2]};  // the owned vertex's value at plane p
+            if (!CHEB) {
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                const bool fr = (m >> c) & 1;
+                const float o = MODE == 1 ? (fr ? f_c[c] - y[c] : 0.f) : (fr ? y[c] : 0.f);
+                out[c * nv + v] = o;
+                if (MODE == 0) dsum += uv[c] * o;
+              }
+            } else {
+              float* __restrict__ dv = static_cast<float*>(ch.dvec) + (int64_t)rhs * 3 * d.nv;
+              float r[3], zc[3];
+#pragma unroll
+              for (int c = 0; c < 3; ++c) r[c] = ((m >> c) & 1) ? f_c[c] - y[c] : 0.f;
+              dinv_sym_apply(static_cast<const float*>(ch.dinv), nv, v, r, zc);
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                const float dold = ch.d_is_u ? uv[c] : dv_c[c];
+                const float c_old = sm.coef[0], c_new = sm.coef[1];
+                const float dn = ch.first ? c_new * zc[c] : c_old * dold + c_new * zc[c];
+                dv[c * nv + v] = dn;
+                const float o = uv[c] + dn;
+                out[c * nv + v] = o;
+                if (DOTS) dsum += f_c[c] * o;
+              }
+            }
+          }
+        }
+      }
+      // ---- read back layer st - 1 from accumulator (q - 1) % 2
+      if (st >= z0 && st <= zend) {
+        const int qp = q - 1;
+        if (tc_ok) {
+          tc_ok = tc_bar_wait(&sm.bar[qp & 1], (uint32_t)((qp >> 1) & 1));
+          if (!tc_ok) atomicExch(&g_fine_tc_err, 1);
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        uint32_t r[32];
+        const uint32_t ta = tmem + ((uint32_t)(32 * (j & 3)) << 16) + 64 * (qp & 1) + 32 * (j >> 2);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+            "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(ta));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        float c[3][8];
+        const float pw = tc_ok ? pe : 0.f;
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) c[cc][a] = pw * __uint_as_float(r[4 * a + cc]);
+        float xc[2][2][3];  // [y bit][z bit][component]
+#pragma unroll
+        for (int yb = 0; yb < 2; ++yb)
+#pragma unroll
+          for (int zb = 0; zb < 2; ++zb)
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc)
+              xc[yb][zb][cc] = c[cc][1 + 2 * yb + 4 * zb] +
+                               __shfl_down_sync(0xffffffffu, c[cc][2 * yb + 4 * zb], 1);
+#pragma unroll
+        for (int zb = 0; zb < 2; ++zb)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) own1[zb][cc] = xc[1][zb][cc];
+        sm.xa[(st - 1) & 1][t] = make_float4(xc[0][0][0], xc[0][0][1], xc[0][0][2], xc[0][1][0]);
+        sm.xb[(st - 1) & 1][t] = make_float2(xc[0][1][1], xc[0][1][2]);
+      }
+    }
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (j == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  const int64_t cta = blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z);
+  if ((MODE == 0 || DOTS) && ch.dotp) {
+    const double bs = modal_block_sum((double)dsum);
+    if (t == 0) ch.dotp[cta] = bs;
+    if (ch.ctr) modal_finish_sum(ch.dotp, (int64_t)gridDim.x * gridDim.y * gridDim.z, ch.dot, ch.ctr);
+  }
+}
+
 // The same operator (MODE 0: out = K u, MODE 1: out = f - K u) on FP64 vectors
 // computed in double-float arithmetic.  Vertex planes arrive as doubles by
 // cp.async and are split into (hi, lo) float pairs once per plane, so the only
@@ -921,16 +1287,17 @@ __global__ void __launch_bounds__(TXE* TYE) k_fine_modal_df(LevelDims d, const d
   extern __shared__ __align__(32) unsigned char modal_smem[];
   S& sm = *reinterpret_cast<S*>(modal_smem);
   const int t = threadIdx.x, i = t % TXE, j = t / TXE;
-  const int zblk = (d.vz + TZ - 1) / TZ;
+  const int zblk = fine_zblocks(d.vz, TZ);
   const int rhs = blockIdx.z / zblk;
-  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = (blockIdx.z - rhs * zblk) * TZ;
+  const int kz = blockIdx.z - rhs * zblk;
+  const int x0 = blockIdx.x * (TXE - 1), y0 = blockIdx.y * (TYE - 1), zb0 = kz * TZ;
   const int64_t nv = d.nv;
   u += (int64_t)rhs * 3 * nv;
   if (f) f += (int64_t)rhs * 3 * nv;
   out += (int64_t)rhs * 3 * nv;
   const int gx = x0 + i, gy = y0 + j;
   const bool own = (i < TXE - 1) && (j < TYE - 1) && gx < d.vx && gy < d.vy;
-  const int zb1 = min(zb0 + TZ, d.vz);
+  const int zb1 = fine_zblock_end(d.vz, TZ, kz);
   int z0, zend;  // the planes marched: [zb0, zb1) less the void
   fine_active_planes<VOID>(d, zb0, zb1, z0, zend);
   // Void planes [pa, pb): the owned vertices get the output for zero forces;
@@ -1236,10 +1603,23 @@ static_assert(MODAL_TXE == FINE_TILE_X && MODAL_TYE == FINE_TILE_Y && TOPO_MODAL
 template <typename T>
 constexpr int modal_tye() { return sizeof(T) == 4 ? TOPO_MODAL32_TYE : MODAL_TYE; }
 
+// Whether an FP32 launch with depth argument tz runs the tensor-core kernel
+// (TOPO_FINE_TC_FLAG, and no void planes: the per-tile z ranges are laid out
+// for the modal kernel's tiles).
+template <typename T>
+bool modal_tc(const LevelDims& d, int tz) {
+  return sizeof(T) == 4 && (tz & TOPO_FINE_TC_FLAG) && !(d.colz && d.colz_void);
+}
+inline int modal_depth(int tz) {
+  tz &= ~TOPO_FINE_TC_FLAG;
+  return tz <= 0 ? MODAL_TZ : tz;
+}
+
 template <typename T>
 dim3 modal_grid(const LevelDims& d, int tz, int nb) {
   constexpr int TYE = modal_tye<T>();
-  return dim3((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + TYE - 2) / (TYE - 1), ((d.vz + tz - 1) / tz) * nb);
+  const int xs = modal_tc<T>(d, tz) ? MODAL_TXE - 2 : MODAL_TXE - 1;  // owned vertex columns per CTA
+  return dim3((d.vx + xs - 1) / xs, (d.vy + TYE - 2) / (TYE - 1), fine_zblocks(d.vz, modal_depth(tz)) * nb);
 }
 
 // One launch of the modal operator in mode MODE: the single-barrier kernel for
@@ -1249,9 +1629,29 @@ dim3 modal_grid(const LevelDims& d, int tz, int nb) {
 template <typename T, int MODE, bool VOID>
 void launch_modal_v(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u, const T* f,
                     T* out, int tz, int nb, const ChebArgs& ch) {
-  if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid = modal_grid<T>(d, tz, nb);
+  const bool tc = modal_tc<T>(d, tz) && !VOID;
+  tz = modal_depth(tz);
   constexpr int TYE = modal_tye<T>();
+  if constexpr (sizeof(T) == 4 && TYE == 8 && !VOID) {
+    if (tc) {
+      const size_t smem = sizeof(Modal32TcSmem<TYE>);
+      static PerDeviceOnce once;
+      once_per_device(once, [smem] {
+        cudaError_t e = cudaFuncSetAttribute(k_fine_tc32<TYE, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e == cudaSuccess)
+          e = cudaFuncSetAttribute(k_fine_tc32<TYE, MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem);
+        return e;
+      });
+      if (MODE != 3 && 3 * d.nv < ((int64_t)1 << 31) && d.ne < ((int64_t)1 << 31))
+        k_fine_tc32<TYE, MODE, true><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+      else
+        k_fine_tc32<TYE, MODE, false><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+      return;
+    }
+  }
   if constexpr (sizeof(T) == 4) {
     const size_t smem = sizeof(Modal32Smem<TYE>);
     static PerDeviceOnce once;
@@ -1302,7 +1702,6 @@ void launch_fine_apply(cudaStream_t s, const LevelDims& d, const T* rhop, const 
 template <typename T>
 int launch_fine_apply_dot(cudaStream_t s, const LevelDims& d, const T* rhop, const uint8_t* vmask, const T* u,
                           T* out, int tz, double* partial, int cap, double* dot, unsigned* ctr) {
-  if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid = modal_grid<T>(d, tz, 1);
   const int64_t nparts = (int64_t)grid.x * grid.y * grid.z;
   if (nparts > cap) return 0;
@@ -1322,7 +1721,7 @@ static void launch_fine_apply_df_v(cudaStream_t s, const LevelDims& d, const dou
                                    double* energy) {
   if (tz <= 0) tz = MODAL_TZ;
   const dim3 grid((d.vx + MODAL_TXE - 2) / (MODAL_TXE - 1), (d.vy + MODAL_TYE - 2) / (MODAL_TYE - 1),
-                  ((d.vz + tz - 1) / tz) * nb);
+                  fine_zblocks(d.vz, tz) * nb);
   constexpr int NT = MODAL_TXE * MODAL_TYE;
   const size_t smem = sizeof(DfSmem<MODAL_TXE, MODAL_TYE>);
   static PerDeviceOnce once;
@@ -1361,7 +1760,7 @@ int launch_fine_cheb(cudaStream_t s, const LevelDims& d, const T* rhop, const ui
   // the FP64 kernel always reads d and has no fused dots
   int nparts = 0;
   if (sizeof(T) == 4 && dot_fo && nb == 1) {
-    const dim3 grid = modal_grid<T>(d, tz <= 0 ? MODAL_TZ : tz, 1);
+    const dim3 grid = modal_grid<T>(d, tz, 1);
     nparts = (int64_t)grid.x * grid.y * grid.z <= cap ? (int)(grid.x * grid.y * grid.z) : 0;
   }
   const ChebArgs ch{dinv, dvec, coef, first ? 1 : 0, nparts ? dot_fo : nullptr,

@@ -62,6 +62,19 @@ inline cudaError_t once_per_device(PerDeviceOnce& o, Fn&& fn) {
   return e;
 }
 
+// Added to the z-march depth of an FP32 fine-kernel launch: element products
+// on the tensor cores (k_fine_tc32) on levels without void planes.
+constexpr int TOPO_FINE_TC_FLAG = 1 << 16;
+
+// z blocks of the fine z-marching kernels: blocks of tz vertex planes, the
+// last one also taking the remainder (up to 2 tz - 1 planes) rather than a
+// short block of its own, which would recompute a whole element layer below
+// it for a few planes.  Block k covers planes [k tz, fine_zblock_end(k)).
+__host__ __device__ inline int fine_zblocks(int vz, int tz) { return vz / tz > 1 ? vz / tz : 1; }
+__host__ __device__ inline int fine_zblock_end(int vz, int tz, int k) {
+  return k + 1 >= fine_zblocks(vz, tz) ? vz : (k + 1) * tz;
+}
+
 // Vertex tile of the fine z-marching kernels: a CTA owns FINE_TILE_X - 1 by
 // FINE_TILE_Y - 1 vertex columns and computes the FINE_TILE_X x FINE_TILE_Y
 // element columns around them (one halo column and row below).
@@ -340,6 +353,8 @@ int bc_from_regions(int nx, int ny, int nz, const uint8_t* eactive, const topo_b
 struct UNetState;
 size_t unet_param_count();
 cudaError_t unet_create(UNetState** out, cudaStream_t s, uint64_t seed);
+int unet_conv_kernel(const UNetState* u);
+void unet_set_conv_kernel(UNetState* u, int kind);
 void unet_free(UNetState* u);
 cudaError_t unet_set_params(UNetState* u, cudaStream_t s, const float* host);
 cudaError_t unet_get_params(UNetState* u, cudaStream_t s, float* host);

@@ -43,6 +43,11 @@ cudaError_t unet_conv(cudaStream_t s, int cin, int cout, const __nv_bfloat16* s1
 cudaError_t unet_wgrad(cudaStream_t s, int cin, int cout, const __nv_bfloat16* s1, const __nv_bfloat16* s2, int c1,
                        int up1, const __nv_bfloat16* G, int X, int Y, int Z, int nb, int groups, float* part,
                        float* dW);
+// k_conv_tc.cu: the same convolution on the tcgen05 tensor cores
+cudaError_t unet_conv_tc(cudaStream_t s, int cin, int cout, const __nv_bfloat16* s1, const __nv_bfloat16* s2, int c1,
+                         int up1, const __nv_bfloat16* W, const float* bias, int X, int Y, int Z, int nb, int relu,
+                         int out_mode, void* out);
+cudaError_t conv_tc_error(int* flag);
 void unet_bias_grad(cudaStream_t s, const __nv_bfloat16* G, int64_t nvox, int C, float* part, int nblk, float* db);
 void unet_relu_grad(cudaStream_t s, const float* dY, const __nv_bfloat16* Y, int64_t n, int relu, __nv_bfloat16* G);
 void unet_pool(cudaStream_t s, const __nv_bfloat16* in, int X, int Y, int Z, int nb, int C, __nv_bfloat16* out);
@@ -374,6 +379,7 @@ struct UNetState {
   double* dpart = nullptr;  // reduction partials
   int step = 0;
   int groups = 16;
+  int conv_kind = 1;        // 3x3x3 convolutions: 1 tcgen05 + TMA, 0 mma.sync
   std::unique_ptr<UNetWork> full, batch;
   // dataset of crops
   int S = 32, cap = 0, count = 0, next = 0;
@@ -495,11 +501,19 @@ static cudaError_t work_alloc(UNetWork* w, int X, int Y, int Z, int nb, bool tra
   return cudaSuccess;
 }
 
+// One 3x3x3 convolution through the kernel the state selects.
+static cudaError_t conv_any(const UNetState* u, cudaStream_t s, int cin, int cout, const __nv_bfloat16* s1,
+                            const __nv_bfloat16* s2, int c1, int up1, const __nv_bfloat16* W, const float* bias, int X,
+                            int Y, int Z, int nb, int relu, int out_mode, void* out) {
+  if (u->conv_kind == 1) return unet_conv_tc(s, cin, cout, s1, s2, c1, up1, W, bias, X, Y, Z, nb, relu, out_mode, out);
+  return unet_conv(s, cin, cout, s1, s2, c1, up1, W, bias, X, Y, Z, nb, relu, out_mode, out);
+}
+
 static cudaError_t conv_layer(UNetState* u, cudaStream_t s, int l, const __nv_bfloat16* s1, const __nv_bfloat16* s2,
                               int c1, int up1, int X, int Y, int Z, int nb, __nv_bfloat16* out) {
   const LayerDef& L = kDef[l];
-  return unet_conv(s, L.cin, L.cout, s1, s2, c1, up1, u->wb + u->woff[l], u->w + u->boff[l], X, Y, Z, nb, L.relu,
-                   0, out);
+  return conv_any(u, s, L.cin, L.cout, s1, s2, c1, up1, u->wb + u->woff[l], u->w + u->boff[l], X, Y, Z, nb, L.relu,
+                  0, out);
 }
 
 // Forward pass on w->x0 (dims X, Y, Z per volume, nb volumes); output w->a[D0B].
@@ -536,7 +550,7 @@ static cudaError_t layer_bwd(UNetState* u, cudaStream_t s, UNetWork* w, int l, c
   count_launch(5);
   if (dX) {
     unet_flip(s, u->wb + u->woff[l], L.cin, L.cout, u->wt + u->woff[l]);
-    UCK(unet_conv(s, L.cout, L.cin, nullptr, w->G, 0, 0, u->wt + u->woff[l], nullptr, X, Y, Z, w->nb, 0, 1, dX));
+    UCK(conv_any(u, s, L.cout, L.cin, nullptr, w->G, 0, 0, u->wt + u->woff[l], nullptr, X, Y, Z, w->nb, 0, 1, dX));
     count_launch(2);
   }
   return cudaGetLastError();
@@ -731,6 +745,15 @@ cudaError_t unet_dataset_reserve(UNetState* u, int cap, int S) {
 
 // Training steps on random batches of the first `limit` dataset crops (all if
 // limit <= 0); lr = Adam step size.  loss_out: mean relative loss of the steps.
+// After a synchronisation: whether a bounded wait of the tensor-core
+// convolution gave up (cudaErrorLaunchTimeout) since the last check.
+static cudaError_t conv_wait_status(const UNetState* u) {
+  if (u->conv_kind != 1) return cudaSuccess;
+  int flag = 0;
+  UCK(conv_tc_error(&flag));
+  return flag ? cudaErrorLaunchTimeout : cudaSuccess;
+}
+
 cudaError_t unet_train(UNetState* u, cudaStream_t s, int steps, int batch, double lr, uint64_t seed, int lo, int hi,
                        bool update, double* loss_out) {
   if (u->count == 0 || steps <= 0 || batch <= 0 || steps > (1 << 16) || batch > 4096) return cudaErrorInvalidValue;
@@ -764,6 +787,7 @@ cudaError_t unet_train(UNetState* u, cudaStream_t s, int steps, int batch, doubl
     }
     UCK(cudaStreamSynchronize(s));  // idx is reused
   }
+  UCK(conv_wait_status(u));
   std::vector<double> l(steps);
   UCK(cudaMemcpy(l.data(), u->loss_log, sizeof(double) * steps, cudaMemcpyDeviceToHost));
   double m = 0;
@@ -804,9 +828,13 @@ cudaError_t unet_host_pass(UNetState* u, cudaStream_t s, int X, int Y, int Z, in
     if (e == cudaSuccess && loss) *loss = res[2];
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = conv_wait_status(u);
   cudaFree(xd);
   return e;
 }
+
+int unet_conv_kernel(const UNetState* u) { return u->conv_kind; }
+void unet_set_conv_kernel(UNetState* u, int kind) { u->conv_kind = kind; }
 
 cudaError_t unet_create(UNetState** out, cudaStream_t s, uint64_t seed) {
   UNetState* u = nullptr;

@@ -57,9 +57,11 @@ def test_learned_requires_enable_and_valid_options():
     assert np.array_equal(ua, p.get("u"))
 
 
-def test_harvest_train_ablation():
+@pytest.mark.parametrize("kernel", [capi.CONV_TCGEN05, capi.CONV_MMA_SYNC], ids=["tcgen05", "mma_sync"])
+def test_harvest_train_ablation(kernel):
     p = _problem()
     p.unet_enable(11)
+    p.unet_set_conv_kernel(kernel)
     p.unet_dataset_reserve(1024, crop=32, crops_per_iterate=16)
     for i in range(8):
         s = _solve(p, workloads.random_density(NX, NY, NZ, 3000 + i), learned=2, rtol=1e-8, max_iter=400,

@@ -659,7 +659,7 @@ class Problem:
         self._ck(self.lib.topo_unet_enable(self.h, seed))
 
     def unet_set_conv_kernel(self, kind):
-        """CONV_TCGEN05 (default) or CONV_MMA_SYNC for the network's convolutions."""
+        """CONV_MMA_SYNC (default) or CONV_TCGEN05 for the network's convolutions."""
         self._ck(self.lib.topo_unet_set_conv_kernel(self.h, kind))
 
     @staticmethod

@@ -172,8 +172,9 @@ __device__ __forceinline__ TcTile conv_tc_tile(int t, int tiles_x, int tiles_y, 
   return {tx * kTcTX, ty * kTcTY, zt - b * Z, b};
 }
 
-// Persistent kernel: each CTA stages the weights once and walks the tiles
-// blockIdx.x, blockIdx.x + gridDim.x, ...  Per tile i: thread 0 issues the
+// Each CTA stages the weights once and walks the tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... (conv_tc_launch launches one tile per CTA,
+// which measured faster).  Per tile i: thread 0 issues the
 // MMAs of tile i into accumulator i % 2 as soon as its halo has landed, while
 // all threads read back and store tile i - 1 from the other accumulator; the
 // halo of tile i + 1 is loaded (TMA and cp.async) into halo buffer (i + 1) %
@@ -391,51 +392,28 @@ cudaError_t encode_group_map(CUtensorMap* m, const __nv_bfloat16* base, int C, i
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-template <int CIN, int COUT>
-constexpr int conv_tc_nbuf() {
-  // two halo buffers where they and the weights fit in 200 KB
-  return (size_t)27 * CIN * COUT * 2 + 2 * (size_t)(CIN / 8) * kTcPlane <= 200 * 1024 ? 2 : 1;
-}
-
+// One tile per CTA.  The kernel also walks several tiles per CTA (weights
+// staged once, halo and accumulators double-buffered) when the grid is
+// smaller; measured on GB300 for the network's layers (8 x 32^3 training
+// crops), that persistent launch (one to three CTAs per SM, as shared memory
+// allows with two halo buffers) ran 1.33x slower in total than one tile per
+// CTA with one halo buffer (three to six CTAs per SM): each tile's 27 x Cin/16
+// MMAs with N = Cout <= 64 form a latency-bound chain, and more resident CTAs
+// overlap more chains.
 template <int CIN, int COUT>
 constexpr size_t conv_tc_smem() {
-  return (size_t)27 * CIN * COUT * 2 + (size_t)conv_tc_nbuf<CIN, COUT>() * (CIN / 8) * kTcPlane;
+  return (size_t)27 * CIN * COUT * 2 + (size_t)(CIN / 8) * kTcPlane;
 }
 
 template <int CIN, int COUT>
 cudaError_t conv_tc_launch(cudaStream_t s, const __nv_bfloat16* s1, const __nv_bfloat16* s2, int c1, int up1,
                            const __nv_bfloat16* W, const float* bias, int X, int Y, int Z, int nb, int relu,
                            int out_mode, void* out) {
-  constexpr int NBUF = conv_tc_nbuf<CIN, COUT>();
   constexpr size_t smem = conv_tc_smem<CIN, COUT>();
-  constexpr int NCOL = tmem_cols<2 * kTcTZ * COUT>();
-  auto kern = k_conv3_tc<CIN, COUT, NBUF>;
+  auto kern = k_conv3_tc<CIN, COUT, 1>;
   static PerDeviceOnce once;
-  static int ctas_per_sm[64];
-  static int sms[64];
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  e = once_per_device(once, [kern, dev] {
-    cudaError_t r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (r == cudaSuccess)
-      r = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-    if (r != cudaSuccess) return r;
-    int occ = 0, smem_sm = 0, smem_static = 0;
-    r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTcThreads, smem);
-    if (r == cudaSuccess) r = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (r == cudaSuccess) r = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
-    if (r != cudaSuccess) return r;
-    cudaFuncAttributes fa{};
-    if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess) smem_static = (int)fa.sharedSizeBytes;
-    // CTAs that fit by shared memory (1 KB per CTA reserved by the system),
-    // the larger of that and the occupancy query, and at most what the SM's
-    // 512 tensor-memory columns hold
-    const int by_smem = smem_sm / ((int)smem + smem_static + 1024);
-    occ = std::max(1, std::min(std::max(occ, by_smem), 512 / NCOL));
-    ctas_per_sm[dev] = occ;
-    return cudaSuccess;
+  cudaError_t e = once_per_device(once, [kern] {
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
   if (e != cudaSuccess) return e;
   TcMaps maps{};
@@ -454,9 +432,8 @@ cudaError_t conv_tc_launch(cudaStream_t s, const __nv_bfloat16* s1, const __nv_b
   const int tiles_x = (X + kTcTX - 1) / kTcTX, tiles_y = (Y + kTcTY - 1) / kTcTY;
   const int64_t ntiles = (int64_t)tiles_x * tiles_y * (nb * Z / kTcTZ);
   if (ntiles >= (int64_t)1 << 31) return cudaErrorInvalidValue;
-  const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms[dev] * ctas_per_sm[dev]);
-  kern<<<grid, kTcThreads, smem, s>>>(maps, tma, s1, c1, W, bias, X, Y, Z, relu, out_mode, out, (int)ntiles, tiles_x,
-                                      tiles_y);
+  kern<<<(unsigned)ntiles, kTcThreads, smem, s>>>(maps, tma, s1, c1, W, bias, X, Y, Z, relu, out_mode, out,
+                                                  (int)ntiles, tiles_x, tiles_y);
   return cudaGetLastError();
 }
 

@@ -379,7 +379,7 @@ struct UNetState {
   double* dpart = nullptr;  // reduction partials
   int step = 0;
   int groups = 16;
-  int conv_kind = 1;        // 3x3x3 convolutions: 1 tcgen05 + TMA, 0 mma.sync
+  int conv_kind = 0;        // 3x3x3 convolutions: 0 mma.sync (measured faster here), 1 tcgen05 + TMA
   std::unique_ptr<UNetWork> full, batch;
   // dataset of crops
   int S = 32, cap = 0, count = 0, next = 0;

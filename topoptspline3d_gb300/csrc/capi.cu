@@ -1630,6 +1630,16 @@ int topo_solve(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats
   return rc;
 }
 
+// After a synchronisation: whether a bounded wait of a tcgen05 kernel this
+// handle may have run gave up (the kernel then skipped its work).
+static int tc_wait_status(topo_handle* h) {
+  int f = 0, g = 0;
+  if (h->fine_tc) CK(fine_tc_error(&f));
+  if (h->unet && unet_conv_kernel(h->unet) == 1) CK(conv_tc_error(&g));
+  if (f || g) return fail(h, TOPO_E_CUDA, "a tensor-core kernel's bounded wait gave up (flags %d, %d)", f, g);
+  return TOPO_OK;
+}
+
 static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats* stats) {
   RET(check_ready(h, true));
   h->energy_ready = false;
@@ -1869,6 +1879,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
     RET(read_scalars(h, S_RR, 1));
     st.relres = std::sqrt(h->hsc[S_RR]) / fn;
   }
+  RET(tc_wait_status(h));
   CK(cudaEventRecord(e1, h->stream));
   CK(cudaEventSynchronize(e1));
   float ms = 0;

@@ -966,6 +966,15 @@ __device__ __forceinline__ bool tc_bar_wait(unsigned long long* bar, uint32_t pa
 
 __device__ int g_fine_tc_err;
 
+// Reads (and clears) the flag of k_fine_tc32's bounded waits: 0 when no wait
+// gave up since the last call.
+cudaError_t fine_tc_error(int* flag) {
+  int zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(flag, g_fine_tc_err, sizeof(int));
+  if (e != cudaSuccess) return e;
+  return *flag ? cudaMemcpyToSymbol(g_fine_tc_err, &zero, sizeof(int)) : cudaSuccess;
+}
+
 template <int TYE, int MODE, bool I32>
 __global__ void __launch_bounds__(32 * TYE, 3)
     k_fine_tc32(LevelDims d, const float* __restrict__ rhop, const uint8_t* __restrict__ vmask,

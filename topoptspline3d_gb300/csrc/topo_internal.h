@@ -354,6 +354,9 @@ struct UNetState;
 size_t unet_param_count();
 cudaError_t unet_create(UNetState** out, cudaStream_t s, uint64_t seed);
 int unet_conv_kernel(const UNetState* u);
+// Flags of the tcgen05 kernels' bounded waits (read and cleared; 0: none gave up).
+cudaError_t fine_tc_error(int* flag);
+cudaError_t conv_tc_error(int* flag);
 void unet_set_conv_kernel(UNetState* u, int kind);
 void unet_free(UNetState* u);
 cudaError_t unet_set_params(UNetState* u, cudaStream_t s, const float* host);

@@ -108,3 +108,22 @@ def test_multi_rhs_on_tensor_cores(oracle_mod):
     assert st_t["max_relres"] <= 1e-6 and np.all(rel_t <= 1e-6)
     for k in range(4):
         assert rel(U_t[k], U_m[k]) < 1e-5
+
+
+def test_checkpoint_keeps_tensor_core_choice(tmp_path, oracle_mod):
+    """A checkpoint carries the FP32 element-product choice with the z-march
+    depths: a handle resumed from it runs the same kernel bit for bit."""
+    wl = workloads.half_mbb(64, 32, 32, lattice=(17, 9, 9))
+    u = random_masked_u(wl.nv, setup_oracle(wl).get("vmask"), 9)
+    g = setup_gpu(wl)
+    g.set_tiles(8, 16)
+    g.set_fine_tensor_cores(1)
+    y_tc = g.apply_fine(u, 1)
+    path = str(tmp_path / "tc.ckpt")
+    g.checkpoint_save(path)
+    g2 = setup_gpu(wl)
+    y_modal = g2.apply_fine(u, 1)
+    g2.checkpoint_load(path)
+    y_resumed = g2.apply_fine(u, 1)
+    assert np.array_equal(y_resumed, y_tc)
+    assert not np.array_equal(y_modal, y_tc)

@@ -491,104 +491,11 @@ __global__ void k_prolong(LevelDims fd, LevelDims cd, const T* __restrict__ uc, 
   if (m & 4) uf[2 * fd.nv + v] += s2;
 }
 
-// Restriction by a factor of 4, separable through shared memory: a CTA owns
-// R4S_CX x R4S_CY coarse vertices of one coarse plane cz.  It streams the
-// seven fine planes 4 cz - 3 .. 4 cz + 3 (the fine x-y region under its tile
-// and the 3-vertex fringe, double-buffered by cp.async, zero outside the
-// grid), reduces each along x with the weights 4 - |dx| as it arrives and
-// accumulates the x-reduced rows with the plane's weight 4 - |dz| in
-// registers (each thread owns a fixed set of (component, fine row, coarse x)
-// sums), then reduces along y and scales by 1/64.  Every fine value is read
-// from memory once per tile it lies under (coalesced rows), instead of once
-// per tap; the sums run in a fixed order.
-constexpr int R4S_CX = 16, R4S_CY = 8, R4S_THREADS = 256;
-constexpr int R4S_FW = 4 * R4S_CX + 3, R4S_FH = 4 * R4S_CY + 3, R4S_NPL = R4S_FW * R4S_FH;
-
-template <typename T>
-__device__ __forceinline__ void r4s_cp(T* dst, const T* src, bool valid) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
-  if (sizeof(T) == 4)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(src), "r"(valid ? 4 : 0));
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(src), "r"(valid ? 8 : 0));
-}
-
-template <typename T>
-__global__ void __launch_bounds__(R4S_THREADS) k_restrict4s(LevelDims fd, LevelDims cd, const T* __restrict__ rf,
-                                                           T* __restrict__ fc) {
-  constexpr int NXO = 3 * R4S_FH * R4S_CX;  // x-reduced sums: (component, fine row, coarse x)
-  constexpr int PER = (NXO + R4S_THREADS - 1) / R4S_THREADS;
-  extern __shared__ __align__(16) unsigned char r4s_smem[];
-  T* buf = reinterpret_cast<T*>(r4s_smem);  // [2][3][R4S_NPL]
-  const int t = threadIdx.x;
-  const int cz = blockIdx.z % cd.vz, rhs = blockIdx.z / cd.vz;
-  rf += (int64_t)rhs * 3 * fd.nv;
-  fc += (int64_t)rhs * 3 * cd.nv;
-  const int cx0 = blockIdx.x * R4S_CX, cy0 = blockIdx.y * R4S_CY;
-  const int fx0 = 4 * cx0 - 3, fy0 = 4 * cy0 - 3;
-  const int zlo = max(4 * cz - 3, 0), zhi = min(4 * cz + 3, fd.vz - 1);
-  auto stage = [&](int fz, T* dst) {
-    const int64_t zoff = (int64_t)fz * fd.vx * fd.vy;
-    for (int k = t; k < 3 * R4S_NPL; k += R4S_THREADS) {
-      const int c = k / R4S_NPL, r = k - c * R4S_NPL, ly = r / R4S_FW, lx = r - ly * R4S_FW;
-      const int fx = fx0 + lx, fy = fy0 + ly;
-      const bool ok = fx >= 0 && fy >= 0 && fx < fd.vx && fy < fd.vy;
-      r4s_cp(dst + k, ok ? rf + c * fd.nv + zoff + (int64_t)fy * fd.vx + fx : rf, ok);
-    }
-    asm volatile("cp.async.commit_group;\n" ::);
-  };
-  T acc[PER];
-#pragma unroll
-  for (int q = 0; q < PER; ++q) acc[q] = T(0);
-  stage(zlo, buf);
-  for (int fz = zlo, pl = 0; fz <= zhi; ++fz, ++pl) {
-    T* cur = buf + (pl & 1) * 3 * R4S_NPL;
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-    __syncthreads();  // plane fz staged by all threads; plane fz - 1's buffer free
-    if (fz + 1 <= zhi) stage(fz + 1, buf + ((pl + 1) & 1) * 3 * R4S_NPL);
-    const T wz = T(4 - abs(fz - 4 * cz));
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int o = t + q * R4S_THREADS;
-      if (o < NXO) {
-        const int c = o / (R4S_FH * R4S_CX), r = o - c * (R4S_FH * R4S_CX), ly = r / R4S_CX, cxl = r - ly * R4S_CX;
-        const T* row = cur + c * R4S_NPL + ly * R4S_FW + 4 * cxl;
-        const T sx = (row[0] + row[6]) + T(2) * (row[1] + row[5]) + T(3) * (row[2] + row[4]) + T(4) * row[3];
-        acc[q] += wz * sx;
-      }
-    }
-  }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-  __syncthreads();
-  T* xs = buf;  // [3][R4S_FH][R4S_CX], the x- and z-reduced rows
-#pragma unroll
-  for (int q = 0; q < PER; ++q) {
-    const int o = t + q * R4S_THREADS;
-    if (o < NXO) xs[o] = acc[q];
-  }
-  __syncthreads();
-  for (int o = t; o < 3 * R4S_CY * R4S_CX; o += R4S_THREADS) {
-    const int c = o / (R4S_CY * R4S_CX), r = o - c * (R4S_CY * R4S_CX), cyl = r / R4S_CX, cxl = r - cyl * R4S_CX;
-    const int cx = cx0 + cxl, cy = cy0 + cyl;
-    if (cx >= cd.vx || cy >= cd.vy) continue;
-    const T* col = xs + (c * R4S_FH + 4 * cyl) * R4S_CX + cxl;
-    const T sy = (col[0] + col[6 * R4S_CX]) + T(2) * (col[R4S_CX] + col[5 * R4S_CX]) +
-                 T(3) * (col[2 * R4S_CX] + col[4 * R4S_CX]) + T(4) * col[3 * R4S_CX];
-    fc[c * cd.nv + cx + (int64_t)cd.vx * (cy + (int64_t)cd.vy * cz)] = sy * (T(1) / T(64));
-  }
-}
-
 template <typename T>
 void launch_restrict(cudaStream_t s, const LevelDims& fine, const LevelDims& coarse, const T* rf,
                      T* fc, int nb) {
   if (coarse.factor == 4) {
-    const size_t smem = 2 * 3 * R4S_NPL * sizeof(T);
-    static PerDeviceOnce once;
-    once_per_device(once, [smem] {
-      return cudaFuncSetAttribute(k_restrict4s<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    });
-    const dim3 grid((coarse.vx + R4S_CX - 1) / R4S_CX, (coarse.vy + R4S_CY - 1) / R4S_CY, coarse.vz * nb);
-    k_restrict4s<T><<<grid, R4S_THREADS, smem, s>>>(fine, coarse, rf, fc);
+    k_restrict4<T><<<dim3(nblk(coarse.nv, 32), nb), 32 * R4_WARPS, 0, s>>>(fine, coarse, rf, fc);
   } else {
     k_restrict<T, 2><<<dim3(nblk(coarse.nv, 128), nb), 128, 0, s>>>(fine, coarse, rf, fc);
   }

@@ -235,6 +235,12 @@ int topo_update_operators(topo_handle* h);
  * fixed rows zero.  precision: 0 = FP64 modal kernel, 1 = FP32 kernel, 2 = FP64 dense-row
  * kernel, 3 = FP64 vectors with the double-float modal kernel. */
 int topo_apply_fine(topo_handle* h, int precision);
+/* Coarse-level operator, the assembled 27-point block stencil of the residual
+ * update on coarse levels (grid/Grid.cu:2126-2224): TOPO_R(level) <-
+ * A_level TOPO_U(level) for level >= 1 with the FP64 (precision 0) or FP32
+ * (precision 1; U rounded to FP32, the result widened) operators, which
+ * topo_set_operator_precision must have built. */
+int topo_apply_level(topo_handle* h, int level, int precision);
 /* Arithmetic of the FP64 fine operator used by the solvers (residuals and the
  * outer CG matvec): 0 = native FP64, 1 = double-float (pairs of floats with
  * error-free transformations, ~48-bit significands, on the FP32 pipe; default).

@@ -46,7 +46,7 @@ EXPORTED = [
     "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x", "topo_set_bc_regions", "topo_plan_bc_regions",
     "topo_unet_enable", "topo_unet_set_conv_kernel", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
-    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic", "topo_set_fine_tensor_cores",
+    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic", "topo_set_fine_tensor_cores", "topo_apply_level",
     "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
     "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
     "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
@@ -216,6 +216,7 @@ def load(build: bool = True):
         "topo_multi_reserve": (i, [vp, i]),
         "topo_set_fine_arithmetic": (i, [vp, i]),
         "topo_set_fine_tensor_cores": (i, [vp, i]),
+        "topo_apply_level": (i, [vp, i, i]),
         "topo_set_graphs": (i, [vp, i]),
         "topo_set_tiles": (i, [vp, i, i]),
         "topo_profiler_range": (i, [i]),
@@ -570,6 +571,12 @@ class Problem:
         self.put("work", u)
         self._ck(self.lib.topo_apply_fine(self.h, precision))
         return self.get("r")
+
+    def apply_level(self, level, u, precision=0) -> np.ndarray:
+        """A_level u on a coarse level (>= 1): precision 0 FP64 operator, 1 FP32."""
+        self.put("u", u, level)
+        self._ck(self.lib.topo_apply_level(self.h, level, precision))
+        return self.get("r", level)
 
     def residual(self, level=0):
         self._ck(self.lib.topo_residual(self.h, level))

@@ -1549,6 +1549,30 @@ int topo_residual(topo_handle* h, int level) {
   return TOPO_OK;
 }
 
+int topo_apply_level(topo_handle* h, int level, int precision) {
+  DEVICE_SCOPE(h);
+  RET(check_ready(h, true));
+  if (level < 1 || level >= (int)h->lv.size() || precision < 0 || precision > 1)
+    return fail(h, TOPO_E_BAD_INPUT, "topo_apply_level: level %d (1..%d), precision %d (0 or 1)", level,
+                (int)h->lv.size() - 1, precision);
+  DevLevel& L = h->lv[level];
+  const int64_t n3 = 3 * L.d.nv;
+  if (precision == 0) {
+    if (!h->ops64) return fail(h, TOPO_E_STATE, "FP64 operators not built (topo_set_operator_precision)");
+    launch_stencil_apply<double>(h->stream, L.d, L.stencil, L.U, nullptr, L.R, false, 1);
+    count_launch();
+  } else {
+    if (!h->ops32) return fail(h, TOPO_E_STATE, "FP32 operators not built (topo_set_operator_precision)");
+    launch_d2f(h->stream, L.U, L.U32, n3);
+    launch_stencil_apply<float>(h->stream, L.d, L.stencil32, L.U32, nullptr, L.R32, false, 1);
+    CK(cudaMemsetAsync(L.R, 0, sizeof(double) * n3, h->stream));
+    launch_f2d_add(h->stream, L.R32, L.R, n3);
+    count_launch(3);
+  }
+  CKL();
+  return TOPO_OK;
+}
+
 int topo_smooth(topo_handle* h, int level, int sweeps, int reverse) {
   DEVICE_SCOPE(h);
   RET(check_ready(h, level > 0));

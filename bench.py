@@ -369,8 +369,9 @@ def mixed_learned_steps(p, ckpt, schedules, oc, ms_mixed, ms_fp64):
     """The timed region's design iterations once more from its start state (the
     checkpoint), with the trained network correcting every FP32 V-cycle of the
     mixed solve (learned = 1: energy-optimal amount, stagnation fallback, FP64
-    residual judging every solve): the configuration BASELINE's headline metric
-    names, measured and reported beside the mixed solve without the network."""
+    residual judging every solve): the mixed + learned configuration of the
+    headline comparison, measured and reported beside the mixed solve without
+    the network."""
     p.checkpoint_load(ckpt)
     p.timer_start()
     st = [p.design_iteration(solve=dict(o, learned=1), oc=oc) for o in schedules]

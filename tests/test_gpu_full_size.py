@@ -4,7 +4,7 @@ design iterations.  Each iteration starts both sides from the oracle's
 coefficients and U, so each iteration's error is its own.  The plain FP64
 MG-PCG solve matches the oracle's compliance to 1e-8 and its coefficients to
 1e-6; the mixed solve (FP32 multigrid under FP64 flexible CG) matches the
-compliance to 1e-6, the benchmark spec tolerance."""
+compliance to 1e-6, the tolerance the mixed solve is held to."""
 import numpy as np
 import pytest
 

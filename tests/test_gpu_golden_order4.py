@@ -7,8 +7,8 @@ GPU, and the full 50-iteration plain-method run (config 0).
 - Order 4 (cubic, 4 taps per axis, 64 coefficients per element) density,
   adjoint and OC update against the oracle at 1e-12 on the three small cases.
 - 48x24x24 cantilever, lattice 13x7x7, 50 design iterations of plain FP64
-  MG-PCG with the OC update (utils/test_utils.cpp:928-958 with BASELINE's
-  rel-res 1e-6 solve): compliance per iteration within 1e-8 of the oracle's.
+  MG-PCG with the OC update (utils/test_utils.cpp:928-958 with a rel-res 1e-6
+  solve): compliance per iteration within 1e-8 of the oracle's.
 """
 import numpy as np
 import pytest

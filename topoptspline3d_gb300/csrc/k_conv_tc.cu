@@ -38,7 +38,6 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
-#include <algorithm>
 #include <cstdint>
 #include <mutex>
 
@@ -162,58 +161,43 @@ __device__ __forceinline__ void conv_tc_stage_halo(const TcMaps& maps, unsigned 
   }
 }
 
-// Tile -> (x0, y0, stacked z-block start): tiles_x x tiles_y tiles per z block.
-struct TcTile {
-  int x0, y0, z0, b;
-};
-__device__ __forceinline__ TcTile conv_tc_tile(int t, int tiles_x, int tiles_y, int Z) {
-  const int tx = t % tiles_x, r = t / tiles_x, ty = r % tiles_y, zb = r / tiles_y;
-  const int zt = zb * kTcTZ, b = zt / Z;
-  return {tx * kTcTX, ty * kTcTY, zt - b * Z, b};
-}
-
-// Each CTA stages the weights once and walks the tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ... (conv_tc_launch launches one tile per CTA,
-// which measured faster).  Per tile i: thread 0 issues the
-// MMAs of tile i into accumulator i % 2 as soon as its halo has landed, while
-// all threads read back and store tile i - 1 from the other accumulator; the
-// halo of tile i + 1 is loaded (TMA and cp.async) into halo buffer (i + 1) %
-// NBUF meanwhile (NBUF = 2 where two buffers and the weights fit in shared
-// memory; with one buffer the next halo waits for tile i's MMAs).
+// One CTA per tile of 8 x 16 x 2 output voxels (blockIdx: x tile, y tile,
+// stacked z block).  Thread 0 issues the tile's 2 x 27 x Cin/16 MMAs into two
+// accumulators of Cout columns as soon as the halo has landed and commits them
+// to an mbarrier; the 4 warps then read them back and store.  (A persistent
+// form that stages the weights once per CTA and double-buffers the halo and
+// the accumulators over several tiles measured slower on the network's
+// layers: shared memory then allows fewer CTAs per SM, and each tile's MMA
+// chain is latency-bound, so throughput comes from the CTAs that overlap.)
 // tma_groups: bit cg set when channel group cg comes by TMA (maps.m[cg]); the
 // other groups are read through nearest upsampling from s1 (c1 channels at
 // half resolution).
-template <int CIN, int COUT, int NBUF>
+template <int CIN, int COUT>
 __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __grid_constant__ TcMaps maps, unsigned tma_groups,
                                                          const __nv_bfloat16* __restrict__ s1, int c1,
                                                          const __nv_bfloat16* __restrict__ W,
                                                          const float* __restrict__ bias, int X, int Y, int Z, int relu,
-                                                         int out_mode, void* out, int ntiles, int tiles_x,
-                                                         int tiles_y) {
+                                                         int out_mode, void* out) {
   static_assert(CIN % 16 == 0 && CIN <= 8 * kTcMaxGroups, "input channels");
-  static_assert(COUT % 16 == 0 && COUT <= 128, "output channels (M = 128 needs N % 16 == 0)");
-  static_assert(NBUF == 1 || NBUF == 2, "halo buffers");
+  static_assert(COUT % 16 == 0 && COUT <= 256, "output channels (M = 128 needs N % 16 == 0)");
   constexpr int CG = CIN / 8;
   constexpr int KSTEPS = CIN / 16;
-  constexpr int HALO_BYTES = CG * kTcPlane;
   constexpr int W_BYTES = 27 * CG * COUT * 16;
-  constexpr int ACC = kTcTZ * COUT;                 // TMEM columns of one accumulator
-  constexpr int NCOL = tmem_cols<2 * ACC>();
+  constexpr int NCOL = tmem_cols<kTcTZ * COUT>();
   constexpr uint32_t IDESC = idesc_bf16<128, COUT>();
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bar_tma[NBUF], bar_mma[2];
+  __shared__ __align__(8) uint64_t bar_tma, bar_mma;
   __shared__ uint32_t tmem_slot;
-  __shared__ int s_abort;
+  __shared__ int s_ok;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t wsm = su32(smem), halo0 = wsm + W_BYTES;
-  if (blockIdx.x >= ntiles) return;
+  const uint32_t wsm = su32(smem), halo = wsm + W_BYTES;
+  const int x0 = blockIdx.x * kTcTX, y0 = blockIdx.y * kTcTY;
+  const int zt = blockIdx.z * kTcTZ, b = zt / Z, z0 = zt - b * Z;
 
   if (tid == 0) {
-    for (int k = 0; k < NBUF; ++k) mbar_init(&bar_tma[k], 1);
-    mbar_init(&bar_mma[0], 1);
-    mbar_init(&bar_mma[1], 1);
-    s_abort = 0;
+    mbar_init(&bar_tma, 1);
+    mbar_init(&bar_mma, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -226,134 +210,101 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3_tc(const __grid_constant__
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_slot;
 
-  // weights once per CTA, [tap][cg][COUT][8]
+  // weights, [tap][cg][COUT][8]; the halo (TMA by thread 0, upsampled groups by all)
   for (int i = tid; i < COUT * 27 * CG; i += kTcThreads) {
     const int n = i / (27 * CG), r = i - n * (27 * CG);
     const int tap = r / CG, cg = r - tap * CG;
     cp_async16_z(wsm + ((tap * CG + cg) * COUT + n) * 16, W + (int64_t)n * 27 * CIN + tap * CIN + cg * 8, true);
   }
-  {
-    const TcTile t0 = conv_tc_tile(blockIdx.x, tiles_x, tiles_y, Z);
-    conv_tc_stage_halo<CIN>(maps, tma_groups, s1, c1, W, halo0, &bar_tma[0], t0.x0, t0.y0, t0.z0, t0.b, X, Y, Z);
-  }
+  conv_tc_stage_halo<CIN>(maps, tma_groups, s1, c1, W, halo, &bar_tma, x0, y0, z0, b, X, Y, Z);
   asm volatile("cp.async.commit_group;\ncp.async.wait_all;" ::: "memory");
+  // generic-proxy writes (cp.async) -> visible to the tensor cores' async proxy
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
 
-  int i = 0;
-  for (int tile = blockIdx.x;; tile += gridDim.x, ++i) {
-    const bool have = tile < ntiles;
-    // ---- MMAs of tile i (thread 0) into accumulator i & 1
-    if (have && tid == 0) {
-      const int hb = i % NBUF;
-      const bool landed = tma_groups == 0 || mbar_wait(&bar_tma[hb], (uint32_t)((i / NBUF) & 1));
-      if (landed) {
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t halo = halo0 + hb * HALO_BYTES;
-#pragma unroll 1
-        for (int tz = 0; tz < kTcTZ; ++tz) {
-          const uint32_t d = tmem + (i & 1) * ACC + tz * COUT;
-#pragma unroll 1
-          for (int tap = 0; tap < 27; ++tap) {
-            const int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;
-            const uint32_t a0 = halo + (((tz + dz) * kTcHY + dy) * kTcHX + dx) * 16;
-#pragma unroll
-            for (int ks = 0; ks < KSTEPS; ++ks) {
-              const uint64_t ad = smem_desc(a0 + 2 * ks * kTcPlane, kTcPlane, kTcHX * 16);
-              const uint64_t bd = smem_desc(wsm + (tap * CG + 2 * ks) * COUT * 16, COUT * 16, 128);
-              const uint32_t acc = (tap | ks) ? 1u : 0u;
-              asm volatile(
-                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-                  "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
-            }
-          }
-        }
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&bar_mma[i & 1]))
-            : "memory");
-      } else {
-        atomicExch(&g_conv_tc_err, 1);
-        s_abort = 1;
-      }
-    }
-    // ---- tile i - 1: its MMAs done -> free halo buffer, read back, store
-    const int next = tile + gridDim.x;
-    bool prev_ok = true;
-    if (i > 0) {
-      prev_ok = mbar_wait(&bar_mma[(i - 1) & 1], (uint32_t)(((i - 1) >> 1) & 1));
-      if (!prev_ok) { atomicExch(&g_conv_tc_err, 2); s_abort = 1; }
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    // halo of tile i + 1: its buffer was read by tile i + 1 - NBUF's MMAs
-    if (have && next < ntiles && prev_ok) {
-      bool free_buf = true;
-      if (NBUF == 1) {
-        free_buf = mbar_wait(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1));
-        if (!free_buf) { atomicExch(&g_conv_tc_err, 3); s_abort = 1; }
-      }
-      if (free_buf) {
-        const TcTile tn = conv_tc_tile(next, tiles_x, tiles_y, Z);
-        const int nb_ = (i + 1) % NBUF;
-        conv_tc_stage_halo<CIN>(maps, tma_groups, s1, c1, W, halo0 + nb_ * HALO_BYTES, &bar_tma[nb_], tn.x0, tn.y0,
-                                tn.z0, tn.b, X, Y, Z);
-      }
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    if (i > 0 && prev_ok) {
-      const TcTile tp = conv_tc_tile(tile - gridDim.x, tiles_x, tiles_y, Z);
-      const int m = warp * 32 + lane;
-      const int x = tp.x0 + (m & 7), y = tp.y0 + (m >> 3);
-      const bool in_xy = x < X && y < Y;
+  if (tid == 0) {
+    const bool landed = tma_groups == 0 || mbar_wait(&bar_tma, 0);
+    if (landed) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll 1
       for (int tz = 0; tz < kTcTZ; ++tz) {
-        const int z = tp.z0 + tz;
-        const int64_t v = (((int64_t)tp.b * Z + z) * Y + y) * X + x;
+        const uint32_t d = tmem + tz * COUT;
+#pragma unroll 1
+        for (int tap = 0; tap < 27; ++tap) {
+          const int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;
+          const uint32_t a0 = halo + (((tz + dz) * kTcHY + dy) * kTcHX + dx) * 16;
 #pragma unroll
-        for (int c0 = 0; c0 < COUT; c0 += 16) {
-          float o[16];
-          tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + ((i - 1) & 1) * ACC + tz * COUT + c0, o);
-          if (!in_xy) continue;
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            if (bias) o[j] += bias[c0 + j];
-            if (relu) o[j] = fmaxf(o[j], 0.f);
+          for (int ks = 0; ks < KSTEPS; ++ks) {
+            const uint64_t ad = smem_desc(a0 + 2 * ks * kTcPlane, kTcPlane, kTcHX * 16);
+            const uint64_t bd = smem_desc(wsm + (tap * CG + 2 * ks) * COUT * 16, COUT * 16, 128);
+            const uint32_t acc = (tap | ks) ? 1u : 0u;
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
           }
-          if (out_mode == 0) {
-            uint4 pk[2];
-            uint32_t* w32 = reinterpret_cast<uint32_t*>(pk);
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       su32(&bar_mma))
+                   : "memory");
+    } else {
+      atomicExch(&g_conv_tc_err, 1);
+    }
+    s_ok = landed;
+  }
+  __syncthreads();
+  bool ok = s_ok != 0;
+  if (ok) {
+    ok = mbar_wait(&bar_mma, 0);
+    if (!ok) atomicExch(&g_conv_tc_err, 2);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+
+  if (ok) {
+    const int m = warp * 32 + lane;
+    const int x = x0 + (m & 7), y = y0 + (m >> 3);
+    const bool in_xy = x < X && y < Y;
+#pragma unroll 1
+    for (int tz = 0; tz < kTcTZ; ++tz) {
+      const int64_t v = (((int64_t)b * Z + z0 + tz) * Y + y) * X + x;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const __nv_bfloat162 h2 = __floats2bfloat162_rn(o[2 * j], o[2 * j + 1]);
-              w32[j] = *reinterpret_cast<const uint32_t*>(&h2);
-            }
-            uint4* dst = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(out) + v * COUT + c0);
-            dst[0] = pk[0];
-            dst[1] = pk[1];
-          } else {
-            float4* dst = reinterpret_cast<float4*>(static_cast<float*>(out) + v * COUT + c0);
+      for (int c0 = 0; c0 < COUT; c0 += 16) {
+        float o[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + tz * COUT + c0, o);
+        if (!in_xy) continue;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              float4 q = make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
-              if (out_mode == 2) {
-                const float4 p = dst[j];
-                q.x += p.x; q.y += p.y; q.z += p.z; q.w += p.w;
-              }
-              dst[j] = q;
+        for (int j = 0; j < 16; ++j) {
+          if (bias) o[j] += bias[c0 + j];
+          if (relu) o[j] = fmaxf(o[j], 0.f);
+        }
+        if (out_mode == 0) {
+          uint4 pk[2];
+          uint32_t* w32 = reinterpret_cast<uint32_t*>(pk);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(o[2 * j], o[2 * j + 1]);
+            w32[j] = *reinterpret_cast<const uint32_t*>(&h2);
+          }
+          uint4* dst = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(out) + v * COUT + c0);
+          dst[0] = pk[0];
+          dst[1] = pk[1];
+        } else {
+          float4* dst = reinterpret_cast<float4*>(static_cast<float*>(out) + v * COUT + c0);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            float4 q = make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
+            if (out_mode == 2) {
+              const float4 p = dst[j];
+              q.x += p.x; q.y += p.y; q.z += p.z; q.w += p.w;
             }
+            dst[j] = q;
           }
         }
       }
     }
-    // thread-staged halo of tile i + 1 visible to the tensor cores; this
-    // tile's reads of accumulator (i - 1) & 1 done before tile i + 1's MMAs
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (!have || s_abort) break;
   }
+  asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL));
 }
@@ -392,14 +343,6 @@ cudaError_t encode_group_map(CUtensorMap* m, const __nv_bfloat16* base, int C, i
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// One tile per CTA.  The kernel also walks several tiles per CTA (weights
-// staged once, halo and accumulators double-buffered) when the grid is
-// smaller; measured on GB300 for the network's layers (8 x 32^3 training
-// crops), that persistent launch (one to three CTAs per SM, as shared memory
-// allows with two halo buffers) ran 1.33x slower in total than one tile per
-// CTA with one halo buffer (three to six CTAs per SM): each tile's 27 x Cin/16
-// MMAs with N = Cout <= 64 form a latency-bound chain, and more resident CTAs
-// overlap more chains.
 template <int CIN, int COUT>
 constexpr size_t conv_tc_smem() {
   return (size_t)27 * CIN * COUT * 2 + (size_t)(CIN / 8) * kTcPlane;
@@ -410,10 +353,9 @@ cudaError_t conv_tc_launch(cudaStream_t s, const __nv_bfloat16* s1, const __nv_b
                            const __nv_bfloat16* W, const float* bias, int X, int Y, int Z, int nb, int relu,
                            int out_mode, void* out) {
   constexpr size_t smem = conv_tc_smem<CIN, COUT>();
-  auto kern = k_conv3_tc<CIN, COUT, 1>;
   static PerDeviceOnce once;
-  cudaError_t e = once_per_device(once, [kern] {
-    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = once_per_device(once, [] {
+    return cudaFuncSetAttribute(k_conv3_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
   if (e != cudaSuccess) return e;
   TcMaps maps{};
@@ -429,11 +371,8 @@ cudaError_t conv_tc_launch(cudaStream_t s, const __nv_bfloat16* s1, const __nv_b
     if (e != cudaSuccess) return e;
     tma |= 1u << cg;
   }
-  const int tiles_x = (X + kTcTX - 1) / kTcTX, tiles_y = (Y + kTcTY - 1) / kTcTY;
-  const int64_t ntiles = (int64_t)tiles_x * tiles_y * (nb * Z / kTcTZ);
-  if (ntiles >= (int64_t)1 << 31) return cudaErrorInvalidValue;
-  kern<<<(unsigned)ntiles, kTcThreads, smem, s>>>(maps, tma, s1, c1, W, bias, X, Y, Z, relu, out_mode, out,
-                                                  (int)ntiles, tiles_x, tiles_y);
+  const dim3 grid((X + kTcTX - 1) / kTcTX, (Y + kTcTY - 1) / kTcTY, nb * Z / kTcTZ);
+  k_conv3_tc<CIN, COUT><<<grid, kTcThreads, smem, s>>>(maps, tma, s1, c1, W, bias, X, Y, Z, relu, out_mode, out);
   return cudaGetLastError();
 }
 

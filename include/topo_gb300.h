@@ -425,8 +425,9 @@ int topo_design_batch(topo_handle** handles, int n, const topo_iter_opts* opts, 
  * base->inner_rtol, 0.03), stage 3 runs two passes of coordinate search from
  * the best schedule over the lower end (0.05, 0.1, 0.2, base), the inner
  * tolerance (0.03, base) and the degree, stage 4 tries degrees 2, 3 and 4 jointly
- * with lower ends 0.02, 0.04, 0.06 and inner tolerances 0.03, 0.05, and the
- * fastest that converges is written into *best (other fields from *base, which must be TOPO_SOLVE_MIXED
+ * with lower ends 0.02, 0.04, 0.06 and inner tolerances 0.03, 0.05, stage 5 two
+ * and four more inner iterations with inner tolerances 0.01, 0.02 and the next
+ * degree, and the fastest that converges is written into *best (other fields from *base, which must be TOPO_SOLVE_MIXED
  * with the Chebyshev smoother).  U is restored. */
 typedef struct topo_tune_report {
   int tz32, tz64;           /* chosen z-march depths */

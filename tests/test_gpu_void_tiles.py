@@ -84,3 +84,20 @@ def test_design_iterations_element_energies(oracle_mod):
         assert abs(s["compliance"] - o.compliance()) < 1e-7 * abs(o.compliance()), it
         o.sensitivity(); o.filter(wl.filter_radius); o.spline_adjoint(); o.oc_update(wl.vgoal)
     assert rel(g.get("coeff"), o.get("coeff")) < 1e-6
+
+
+def test_tensor_core_choice_keeps_void_skipping(pair):
+    """On a level with void planes the FP32 kernels keep the modal element
+    products (the tensor-core kernel's tiles do not carry the per-tile z ranges):
+    with the tensor-core choice set, the FP32 operator is the modal one bit for
+    bit, and still the oracle's to 1e-5."""
+    wl, g, o = pair
+    u = random_masked_u(wl.nv, o.get("vmask"), 4)
+    o.update_penalised()
+    y_o = o.apply_fine(u)
+    y_modal = g.apply_fine(u, 1)
+    g.set_fine_tensor_cores(1)
+    y_tc = g.apply_fine(u, 1)
+    g.set_fine_tensor_cores(0)
+    assert np.array_equal(y_tc, y_modal)
+    assert rel(y_tc, y_o) < 1e-5

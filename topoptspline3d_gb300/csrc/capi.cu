@@ -2256,6 +2256,30 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
           if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
         }
   }
+  // ---- stage 5: stronger inner solves around the best (more FP32 iterations
+  // to a tighter tolerance, so fewer FP64 outer iterations, each with its
+  // double-float matvec) and a degree above it
+  {
+    const topo_solve_opts cur = *best;
+    const int im5[2] = {cur.inner_max + 2, cur.inner_max + 4};
+    const double irt5[2] = {0.01, 0.02};
+    for (const int im : im5)
+      for (const double irt : irt5) {
+        topo_solve_opts o = cur;
+        o.inner_max = im;
+        o.inner_rtol = irt;
+        double ms = 0;
+        ++r.candidates;
+        if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+      }
+    if (cur.cheb_degree + 1 <= CHEB_MAX_DEG) {
+      topo_solve_opts o = *best;
+      o.cheb_degree = best->cheb_degree + 1;
+      double ms = 0;
+      ++r.candidates;
+      if (run(o, &ms) == TOPO_OK && ms < bt) { bt = ms; *best = o; }
+    }
+  }
   r.best_ms = bt;
   cudaMemcpyAsync(L0.U, u0, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream);
   CK(cudaEventRecord(t1, h->stream));

@@ -35,7 +35,8 @@ enum topo_status {
   TOPO_E_NOT_CONVERGED = 4, /* solver hit its iteration cap above tolerance */
   TOPO_E_SINGULAR = 5,      /* coarsest-level factorisation met a non-positive pivot */
   TOPO_E_NOMEM = 6,         /* device allocation failed */
-  TOPO_E_NONFINITE = 7      /* NaN/Inf detected in a result */
+  TOPO_E_NONFINITE = 7,     /* NaN/Inf detected in a result */
+  TOPO_E_TIMEOUT = 8        /* a kernel's bounded device-side wait gave up (its work was skipped) */
 };
 
 /* Array ids for topo_put_array / topo_get_array / topo_device_ptr. */

@@ -14,9 +14,10 @@ import numpy as np
 from . import build as _build
 
 TOPO_OK, TOPO_E_CUDA, TOPO_E_BAD_INPUT, TOPO_E_STATE, TOPO_E_NOT_CONVERGED, TOPO_E_SINGULAR, \
-    TOPO_E_NOMEM, TOPO_E_NONFINITE = range(8)
+    TOPO_E_NOMEM, TOPO_E_NONFINITE, TOPO_E_TIMEOUT = range(9)
 STATUS_NAMES = {0: "TOPO_OK", 1: "TOPO_E_CUDA", 2: "TOPO_E_BAD_INPUT", 3: "TOPO_E_STATE",
-                4: "TOPO_E_NOT_CONVERGED", 5: "TOPO_E_SINGULAR", 6: "TOPO_E_NOMEM", 7: "TOPO_E_NONFINITE"}
+                4: "TOPO_E_NOT_CONVERGED", 5: "TOPO_E_SINGULAR", 6: "TOPO_E_NOMEM", 7: "TOPO_E_NONFINITE",
+                8: "TOPO_E_TIMEOUT"}
 
 ARRAYS = {"rho": 0, "rhop": 1, "coeff": 2, "sens": 3, "csens": 4, "u": 5, "f": 6, "r": 7,
           "stencil": 8, "kelem": 9, "vmask": 10, "eactive": 11, "ke": 12, "work": 13, "volcsens": 14, "multi_f": 15,

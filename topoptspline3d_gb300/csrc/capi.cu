@@ -1660,7 +1660,7 @@ static int tc_wait_status(topo_handle* h) {
   int f = 0, g = 0;
   if (h->fine_tc) CK(fine_tc_error(&f));
   if (h->unet && unet_conv_kernel(h->unet) == 1) CK(conv_tc_error(&g));
-  if (f || g) return fail(h, TOPO_E_CUDA, "a tensor-core kernel's bounded wait gave up (flags %d, %d)", f, g);
+  if (f || g) return fail(h, TOPO_E_TIMEOUT, "a tensor-core kernel's bounded wait gave up (flags %d, %d)", f, g);
   return TOPO_OK;
 }
 

@@ -443,13 +443,15 @@ def run_loads(args, rank):
     p.update_operators()
     F = workloads.patch_loads(nx, ny, nz, nrhs, seed0=1000, patch=8)
     p.multi_reserve(nrhs)
-    kw = dict(pre=1, post=1, rtol=1e-6, max_iter=300)
-    # lower end of the Chebyshev interval: the faster of 0.3 and 0.1 lambda_max
-    # on one solve of the batch each (untimed set-up), for both forms below
+    kw = dict(pre=1, post=1, rtol=1e-6, max_iter=300, inner_rtol=0.05)
+    # schedule: one V-cycle or 4 / 6 batched FP32 CG iterations per outer step,
+    # lower end of the Chebyshev interval 0.3 or 0.1 lambda_max: the fastest on
+    # one solve of the batch each (untimed set-up), for both forms below
     trial = {}
-    for lo in (0.3, 0.1):
-        trial[lo] = p.solve_multi(F, cheb_lo=lo, **kw)[1]["ms"]
-    kw["cheb_lo"] = min(trial, key=trial.get)
+    for inner in (1, 4, 6):
+        for lo in (0.3, 0.1):
+            trial[(inner, lo)] = p.solve_multi(F, cheb_lo=lo, inner_max=inner, **kw)[1]["ms"]
+    kw["inner_max"], kw["cheb_lo"] = min(trial, key=trial.get)
     for _ in range(args.warmup):
         p.solve_multi(F, **kw)
     ms_multi, its = [], []
@@ -458,7 +460,7 @@ def run_loads(args, rank):
         ms_multi.append(st["ms"])
         its.append(st["iterations"])
     single = dict(mode=capi.SOLVE_MIXED, smoother=capi.SMOOTH_CHEBYSHEV, pre=1, post=1, rtol=1e-6, max_iter=300,
-                  inner_max=1, cheb_lo=kw["cheb_lo"])
+                  inner_max=kw["inner_max"], inner_rtol=kw["inner_rtol"], cheb_lo=kw["cheb_lo"])
     ms_single = []
     for k in range(nrhs):
         p.put("f", F[k])
@@ -471,8 +473,10 @@ def run_loads(args, rank):
            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32 multigrid / f64 CG",
            "data": "synthetic",
            "config": {"workload": f"cantilever {nx}x{ny}x{nz}, {nrhs} seeded 8x8 patch loads",
-                      "solver": f"per-load FP64 flexible CG + batched FP32 Chebyshev V(1,1) degree 2 on "
-                                f"[{kw['cheb_lo']:g}, 1.1] lambda_max"},
+                      "solver": f"per-load FP64 flexible CG + {kw['inner_max']} batched FP32 CG its (to "
+                                f"{kw['inner_rtol']:g}) with a Chebyshev V(1,1) degree 2 on [{kw['cheb_lo']:g}, 1.1] "
+                                f"lambda_max",
+                      "schedule_trials_ms": {f"inner {k[0]}, lo {k[1]:g}": v for k, v in trial.items()}},
            "sequential_single_solves_ms": sum(ms_single), "speedup_vs_sequential": sum(ms_single) / ms,
            "iterations": its, "max_relres": float(max(rr)), "worst_case_compliance": max(comp),
            "worst_case_load": int(np.argmax(comp))}

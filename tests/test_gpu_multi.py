@@ -42,6 +42,31 @@ def test_multi_rhs_matches_oracle(oracle_mod, nrhs):
         assert abs(F[k] @ U[k] - F[k] @ uo) <= 1e-8 * abs(F[k] @ uo)
 
 
+@pytest.mark.parametrize("inner_max", [4, 6])
+def test_multi_rhs_inner_cg_matches_oracle(oracle_mod, inner_max):
+    """With a batched FP32 inner CG per outer step each load still matches the
+    oracle, in fewer outer (FP64) iterations than one V-cycle per step."""
+    wl = workloads.cantilever(48, 24, 24)
+    nc = int(np.prod([q + wl.order for q in wl.partition]))
+    coeff = random_coeff(nc, seed=23)
+    F = workloads.patch_loads(wl.nx, wl.ny, wl.nz, 5, seed0=2000, patch=8)
+    p = _problem(wl, coeff)
+    p.multi_reserve(8)
+    U1, st1, _ = p.solve_multi(F, rtol=1e-9, max_iter=300)
+    U, st, rr = p.solve_multi(F, rtol=1e-9, max_iter=300, inner_max=inner_max, inner_rtol=0.05)
+    assert st["max_relres"] <= 1e-9 and (rr <= 1e-9).all()
+    assert st["iterations"] < st1["iterations"]
+    o = setup_oracle(wl, coeff)
+    o.update_operators()
+    for k in range(5):
+        o.put("f", F[k])
+        o.put("u", np.zeros_like(F[k]))
+        o.pcg(2, 2, 1e-11, 400, 1)
+        uo = o.get("u")
+        assert rel(U[k], uo) < 1e-6, k
+        assert abs(F[k] @ U[k] - F[k] @ uo) <= 1e-8 * abs(F[k] @ uo)
+
+
 def test_multi_rhs_equals_single_solves():
     """Each right-hand side of the batch converges like its own single solve."""
     wl = workloads.cantilever(32, 16, 16, lattice=(11, 7, 7))

@@ -638,8 +638,10 @@ class Problem:
         self._multi_cap = capacity
 
     def solve_multi(self, F, U0=None, pre=2, post=2, rtol=1e-6, max_iter=200, cheb_degree=2, cheb_lo=0.3,
-                    cheb_hi=1.1, check=True):
-        """F [nrhs][3*nv] host right-hand sides -> (U [nrhs][3*nv], stats, relres[nrhs])."""
+                    cheb_hi=1.1, inner_max=1, inner_rtol=0.1, check=True):
+        """F [nrhs][3*nv] host right-hand sides -> (U [nrhs][3*nv], stats, relres[nrhs]).
+        inner_max > 1: each outer step runs that many batched FP32 CG iterations
+        (to inner_rtol per right-hand side) preconditioned by the V-cycle."""
         F = np.ascontiguousarray(F, dtype=np.float64)
         nrhs = F.shape[0]
         cap = self._multi_cap
@@ -650,8 +652,8 @@ class Problem:
         if U0 is not None:
             u[:nrhs] = U0
         self.put("multi_u", u.ravel())
-        o = SolveOpts(SOLVE_MIXED, SMOOTH_CHEBYSHEV, pre, post, rtol, max_iter, 0.1, cheb_degree, cheb_lo, cheb_hi,
-                      1, 0, 0.0)
+        o = SolveOpts(SOLVE_MIXED, SMOOTH_CHEBYSHEV, pre, post, rtol, max_iter, inner_rtol, cheb_degree, cheb_lo,
+                      cheb_hi, inner_max, 0, 0.0)
         st = MultiStats()
         rel = np.zeros(nrhs)
         rc = self.lib.topo_solve_multi(self.h, nrhs, C.byref(o), C.byref(st), rel.ctypes.data_as(C.POINTER(C.c_double)))

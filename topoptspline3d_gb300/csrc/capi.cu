@@ -2320,6 +2320,8 @@ int topo_multi_reserve(topo_handle* h, int capacity) {
   const size_t n64 = (size_t)capacity * 3 * h->lv[0].d.nv * sizeof(double);
   for (double** v : {&m->x, &m->f, &m->r, &m->d, &m->q, &m->rold, &m->z})
     if (rc == TOPO_OK) rc = alloc((void**)v, n64);
+  for (float** v : {&m->x32, &m->d32, &m->q32})
+    if (rc == TOPO_OK) rc = alloc((void**)v, n64 / 2);
   if (rc == TOPO_OK) rc = alloc((void**)&m->part, (size_t)capacity * 256 * sizeof(double));
   if (rc == TOPO_OK) rc = alloc((void**)&m->sc, (size_t)capacity * 16 * sizeof(double));
   if (rc != TOPO_OK) {
@@ -2337,8 +2339,8 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
   if (!o || o->rtol <= 0 || o->max_iter < 0 || o->pre < 0 || o->post < 0) return TOPO_E_BAD_INPUT;
   if (!h->multi) return fail(h, TOPO_E_STATE, "call topo_multi_reserve first");
   if (nrhs <= 0 || nrhs > h->multi->cap) return fail(h, TOPO_E_BAD_INPUT, "nrhs %d outside 1..%d", nrhs, h->multi->cap);
-  if (o->mode != TOPO_SOLVE_MIXED || o->smoother != TOPO_SMOOTH_CHEBYSHEV || o->inner_max > 1 || o->learned)
-    return fail(h, TOPO_E_BAD_INPUT, "multi-RHS solve: mode MIXED, Chebyshev smoother, inner_max <= 1, no learned part");
+  if (o->mode != TOPO_SOLVE_MIXED || o->smoother != TOPO_SMOOTH_CHEBYSHEV || o->learned)
+    return fail(h, TOPO_E_BAD_INPUT, "multi-RHS solve: mode MIXED, Chebyshev smoother, no learned part");
   if (!h->ops32) return fail(h, TOPO_E_STATE, "FP32 operators not built");
   ChebParams cp;
   if (o->cheb_degree > 0) cp.degree = o->cheb_degree;
@@ -2369,7 +2371,10 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
       h->nb = 1;
     }
   } swap(h, m, nb);
-  enum { B_RR, B_FF, B_RZ, B_ZROLD, B_RZOLD, B_DQ, B_ALPHA, B_BETA };
+  enum { B_RR, B_FF, B_RZ, B_ZROLD, B_RZOLD, B_DQ, B_ALPHA, B_BETA,
+         I_RR, I_FF, I_RZ, I_RZOLD, I_DQ, I_ALPHA, I_BETA, I_ZERO };  // outer, inner (16 slots)
+  const int inner_max = o->inner_max > 1 ? o->inner_max : 1;
+  const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-1;
   double* sb = m.sc;
   auto slot = [&](int k) { return sb + (size_t)k * m.cap; };
   ScopedEvent e0, e1;
@@ -2392,23 +2397,57 @@ int topo_solve_multi(topo_handle* h, int nrhs, const topo_solve_opts* o, topo_mu
     return true;
   };
   int it = 0, nvc = 0;
+  if (inner_max > 1) CK(cudaMemsetAsync(slot(I_ZERO), 0, sizeof(double) * nb, h->stream));
   while (!converged() && it < o->max_iter) {
-    // z = V(r): one FP32 V-cycle for the whole batch
     launch_d2f(h->stream, m.r, L0.F32, n3 * nb);
-    if (!cheb_zero_start(TOPO_SMOOTH_CHEBYSHEV, o->pre, cp))
-      CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3 * nb, h->stream));
-    vcycle32(h, o->pre, o->post, TOPO_SMOOTH_CHEBYSHEV, cp, true);
-    ++nvc;
-    k_to_double<float><<<nb256(n3 * nb), 256, 0, h->stream>>>(n3 * nb, L0.U32, m.z);
+    if (inner_max <= 1) {
+      // z = V(r): one FP32 V-cycle for the whole batch
+      if (!cheb_zero_start(TOPO_SMOOTH_CHEBYSHEV, o->pre, cp))
+        CK(cudaMemsetAsync(L0.U32, 0, sizeof(float) * n3 * nb, h->stream));
+      vcycle32(h, o->pre, o->post, TOPO_SMOOTH_CHEBYSHEV, cp, true);
+      ++nvc;
+      k_to_double<float><<<nb256(n3 * nb), 256, 0, h->stream>>>(n3 * nb, L0.U32, m.z);
+    } else {
+      // z = inner_max iterations of an FP32 CG per right-hand side on A z = r,
+      // preconditioned by the batched V-cycle (a fixed symmetric operator, so
+      // the Fletcher-Reeves form: zrold = 0, rold not kept).  Its residual is
+      // level-0 F32, the V-cycle's right-hand side, x32 starts at 0; a
+      // right-hand side whose inner residual fell by inner_rtol gets alpha = 0
+      // and stops there, so the loop needs no host decision.
+      float* r32 = L0.F32;
+      float* z32 = L0.U32;
+      CK(cudaMemsetAsync(m.x32, 0, sizeof(float) * n3 * nb, h->stream));
+      launch_bdot<float>(h->stream, r32, r32, n3, nb, m.part, slot(I_FF));
+      CK(cudaMemcpyAsync(slot(I_RR), slot(I_FF), sizeof(double) * nb, cudaMemcpyDeviceToDevice, h->stream));
+      count_launch(2);
+      for (int j = 0; j < inner_max; ++j) {
+        if (!cheb_zero_start(TOPO_SMOOTH_CHEBYSHEV, o->pre, cp))
+          CK(cudaMemsetAsync(z32, 0, sizeof(float) * n3 * nb, h->stream));
+        vcycle32(h, o->pre, o->post, TOPO_SMOOTH_CHEBYSHEV, cp, true);
+        ++nvc;
+        launch_bdot<float>(h->stream, r32, z32, n3, nb, m.part, slot(I_RZ));
+        launch_bbeta(h->stream, nb, slot(I_RZ), slot(I_ZERO), slot(I_RZOLD), j == 0, slot(I_BETA));
+        launch_bdir<float>(h->stream, n3, nb, z32, m.d32, slot(I_BETA));
+        launch_fine_apply<float>(h->stream, L0.d, h->rhop32, L0.vmask, m.d32, nullptr, m.q32, false, nb,
+                                 tz32_arg(h));
+        launch_bdot<float>(h->stream, m.d32, m.q32, n3, nb, m.part, slot(I_DQ));
+        launch_balpha(h->stream, nb, slot(I_RZ), slot(I_DQ), slot(I_RR), slot(I_FF), inner_rtol * inner_rtol,
+                      slot(I_ALPHA), slot(I_RZOLD));
+        launch_bupdate<float>(h->stream, n3, nb, m.x32, r32, nullptr, m.d32, m.q32, slot(I_ALPHA));
+        launch_bdot<float>(h->stream, r32, r32, n3, nb, m.part, slot(I_RR));
+        count_launch(14);
+      }
+      k_to_double<float><<<nb256(n3 * nb), 256, 0, h->stream>>>(n3 * nb, m.x32, m.z);
+    }
     launch_bdot<double>(h->stream, m.r, m.z, n3, nb, m.part, slot(B_RZ));
     if (it > 0) launch_bdot<double>(h->stream, m.z, m.rold, n3, nb, m.part, slot(B_ZROLD));
     launch_bbeta(h->stream, nb, slot(B_RZ), slot(B_ZROLD), slot(B_RZOLD), it == 0, slot(B_BETA));
-    launch_bdir(h->stream, n3, nb, m.z, m.d, slot(B_BETA));
+    launch_bdir<double>(h->stream, n3, nb, m.z, m.d, slot(B_BETA));
     fine64(h, L0.d, m.d, nullptr, m.q, false, nb);
     launch_bdot<double>(h->stream, m.d, m.q, n3, nb, m.part, slot(B_DQ));
     launch_balpha(h->stream, nb, slot(B_RZ), slot(B_DQ), slot(B_RR), slot(B_FF), rtol2, slot(B_ALPHA),
                   slot(B_RZOLD));
-    launch_bupdate(h->stream, n3, nb, m.x, m.r, m.rold, m.d, m.q, slot(B_ALPHA));
+    launch_bupdate<double>(h->stream, n3, nb, m.x, m.r, m.rold, m.d, m.q, slot(B_ALPHA));
     launch_bdot<double>(h->stream, m.r, m.r, n3, nb, m.part, slot(B_RR));
     count_launch(it > 0 ? 16 : 14);
     CKL();

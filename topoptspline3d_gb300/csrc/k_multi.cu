@@ -66,22 +66,23 @@ __global__ void k_balpha(int nb, const double* rz, const double* dq, const doubl
 }
 
 // d = z + beta d
-__global__ void k_bdir(int64_t n, int nb, const double* __restrict__ z, double* __restrict__ d,
-                       const double* __restrict__ beta) {
+template <typename T>
+__global__ void k_bdir(int64_t n, int nb, const T* __restrict__ z, T* __restrict__ d, const double* __restrict__ beta) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n * nb) return;
-  const double b = beta[i / n];
+  const T b = (T)beta[i / n];
   d[i] = z[i] + b * d[i];
 }
 
-// x += alpha d, rold = r, r -= alpha q
-__global__ void k_bupdate(int64_t n, int nb, double* __restrict__ x, double* __restrict__ r, double* __restrict__ rold,
-                          const double* __restrict__ d, const double* __restrict__ q, const double* __restrict__ alpha) {
+// x += alpha d, rold = r (when kept), r -= alpha q
+template <typename T>
+__global__ void k_bupdate(int64_t n, int nb, T* __restrict__ x, T* __restrict__ r, T* __restrict__ rold,
+                          const T* __restrict__ d, const T* __restrict__ q, const double* __restrict__ alpha) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n * nb) return;
-  const double a = alpha[i / n];
+  const T a = (T)alpha[i / n];
   x[i] += a * d[i];
-  rold[i] = r[i];
+  if (rold) rold[i] = r[i];
   r[i] -= a * q[i];
 }
 
@@ -93,12 +94,20 @@ void launch_balpha(cudaStream_t s, int nb, const double* rz, const double* dq, c
                    double rtol2, double* alpha, double* rzold) {
   k_balpha<<<nblk(nb, 64), 64, 0, s>>>(nb, rz, dq, rr, ff, rtol2, alpha, rzold);
 }
-void launch_bdir(cudaStream_t s, int64_t n, int nb, const double* z, double* d, const double* beta) {
-  k_bdir<<<nblk(n * nb, kThreads), kThreads, 0, s>>>(n, nb, z, d, beta);
+template <typename T>
+void launch_bdir(cudaStream_t s, int64_t n, int nb, const T* z, T* d, const double* beta) {
+  k_bdir<T><<<nblk(n * nb, kThreads), kThreads, 0, s>>>(n, nb, z, d, beta);
 }
-void launch_bupdate(cudaStream_t s, int64_t n, int nb, double* x, double* r, double* rold, const double* d,
-                    const double* q, const double* alpha) {
-  k_bupdate<<<nblk(n * nb, kThreads), kThreads, 0, s>>>(n, nb, x, r, rold, d, q, alpha);
+template <typename T>
+void launch_bupdate(cudaStream_t s, int64_t n, int nb, T* x, T* r, T* rold, const T* d, const T* q,
+                    const double* alpha) {
+  k_bupdate<T><<<nblk(n * nb, kThreads), kThreads, 0, s>>>(n, nb, x, r, rold, d, q, alpha);
 }
+template void launch_bdir<double>(cudaStream_t, int64_t, int, const double*, double*, const double*);
+template void launch_bdir<float>(cudaStream_t, int64_t, int, const float*, float*, const double*);
+template void launch_bupdate<double>(cudaStream_t, int64_t, int, double*, double*, double*, const double*,
+                                     const double*, const double*);
+template void launch_bupdate<float>(cudaStream_t, int64_t, int, float*, float*, float*, const float*, const float*,
+                                    const double*);
 
 }  // namespace topo

@@ -387,15 +387,18 @@ void launch_bbeta(cudaStream_t s, int nb, const double* rz, const double* zrold,
                   double* beta);
 void launch_balpha(cudaStream_t s, int nb, const double* rz, const double* dq, const double* rr, const double* ff,
                    double rtol2, double* alpha, double* rzold);
-void launch_bdir(cudaStream_t s, int64_t n, int nb, const double* z, double* d, const double* beta);
-void launch_bupdate(cudaStream_t s, int64_t n, int nb, double* x, double* r, double* rold, const double* d,
-                    const double* q, const double* alpha);
+template <typename T>
+void launch_bdir(cudaStream_t s, int64_t n, int nb, const T* z, T* d, const double* beta);
+template <typename T>
+void launch_bupdate(cudaStream_t s, int64_t n, int nb, T* x, T* r, T* rold, const T* d, const T* q,
+                    const double* alpha);
 
 // Batched buffers of the multi-right-hand-side solver (topo_multi_reserve).
 struct MultiRhs {
   int cap = 0;
   std::vector<float*> U, F, R, U2, cd;  // per level, cap * 3 nv
   double *x = nullptr, *f = nullptr, *r = nullptr, *d = nullptr, *q = nullptr, *rold = nullptr, *z = nullptr;
+  float *x32 = nullptr, *d32 = nullptr, *q32 = nullptr;  // inner FP32 CG, level 0, cap * 3 nv
   double* part = nullptr;  // reduction partials [cap][256]
   double* sc = nullptr;    // scalars [kSlots][cap]
   std::vector<void*> allocs;

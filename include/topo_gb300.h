@@ -255,6 +255,11 @@ int topo_set_fine_arithmetic(topo_handle* h, int arith);
  * form.  Grid::gs_relax / update_residual on the finest level
  * (grid/Grid.cu:1698-1842, 2277-2333) have no tensor-core counterpart. */
 int topo_set_fine_tensor_cores(topo_handle* h, int on);
+/* Element rows (4, 8 or 16) of the CTA tile (32 element columns by that many
+ * rows, marched in z) of the FP32 modal fine kernels on levels without void
+ * planes; each vertex's sum is formed the same way in every tile height, so
+ * the outputs are identical.  The autotuner times the three heights. */
+int topo_set_fine_tile_rows(topo_handle* h, int rows);
 /* FP32 V-cycles of the mixed solver replayed as one CUDA graph per handle
  * (captured on first use, re-captured when the schedule, spectral bounds,
  * tiles or buffers change): 1 = on (default), 0 = direct launches.  Graphs are
@@ -418,8 +423,9 @@ int topo_design_batch(topo_handle** handles, int n, const topo_iter_opts* opts, 
  * counterpart).  Stage 1 times the fine-level kernels at z-march depths
  * 4, 8, 16 and 32 (the FP32 Chebyshev step with the modal and with the
  * tensor-core element products, and the FP64 operator; CUDA events, 5 launches
- * each) and keeps the fastest for the handle (depths and
- * topo_set_fine_tensor_cores).  Stage 2 solves from the
+ * each; the modal form also with CTA tiles of 4 and 16 element rows) and keeps
+ * the fastest for the handle (depths, topo_set_fine_tensor_cores and
+ * topo_set_fine_tile_rows).  Stage 2 solves from the
  * current U with each candidate schedule of the mixed solver (FP32 inner
  * iterations 1, 2, 4, 6 x smoothing steps 1, 2 x Chebyshev degree 2, 3 x lower
  * end of the Chebyshev interval base->cheb_lo, 0.1 x inner tolerance
@@ -439,6 +445,8 @@ typedef struct topo_tune_report {
   double tune_ms;           /* device time spent tuning */
   int tc;                   /* FP32 fine element products chosen: 1 tensor cores, 0 modal */
   double cheb_tc_ms[4];     /* FP32 Chebyshev step on the tensor cores at depths 4, 8, 16, 32 */
+  int rows32;               /* element rows of the FP32 modal kernel's CTA tile chosen: 4, 8 or 16 */
+  double cheb_rows_ms[2][4];/* modal FP32 Chebyshev step with tiles of 4 and of 16 rows, depths 4..32 */
 } topo_tune_report;
 int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* best, topo_tune_report* report);
 /* Sets the fine kernels' z-march depths (FP32 kernels, FP64 operator) directly,

@@ -28,10 +28,14 @@ def test_autotune_picks_converging_schedule_and_restores_state():
     # then 3 degrees x 3 lower ends x 2 tolerances jointly, then 2 inner counts x 2
     # inner tolerances and the next degree
     assert rep["candidates"] == 97 and rep["best_ms"] <= rep["base_ms"]
-    # the fastest FP32 Chebyshev step over the depths and both element-product forms
-    fastest = min(rep["cheb_ms"] + rep["cheb_tc_ms"])
+    # the fastest FP32 Chebyshev step over the depths, both element-product forms
+    # and the three tile heights of the modal form
+    rows_ms = rep["cheb_rows_ms"]
+    fastest = min(rep["cheb_ms"] + rep["cheb_tc_ms"] + rows_ms[4] + rows_ms[16])
     k = (4, 8, 16, 32).index(rep["tz32"])
-    assert fastest == (rep["cheb_tc_ms"] if rep["tc"] else rep["cheb_ms"])[k]
+    assert rep["rows32"] in (4, 8, 16) and not (rep["tc"] and rep["rows32"] != 8)
+    chosen = rep["cheb_tc_ms"] if rep["tc"] else rows_ms.get(rep["rows32"], rep["cheb_ms"])
+    assert fastest == chosen[k]
     assert best["mode"] == capi.SOLVE_MIXED and best["rtol"] == 1e-6
     assert best["inner_max"] in (1, 2, 3, 4, 5, 6, 8, 10) and best["pre"] in (1, 2)
     assert 2 <= best["cheb_degree"] <= 5

@@ -88,7 +88,8 @@ def test_design_iterations_element_energies(oracle_mod):
 
 def test_tensor_core_choice_keeps_void_skipping(pair):
     """On a level with void planes the FP32 kernels keep the modal element
-    products (the tensor-core kernel's tiles do not carry the per-tile z ranges):
+    products in 8-row tiles (the tensor-core kernel's tiles and the other tile
+    heights do not carry the per-tile z ranges):
     with the tensor-core choice set, the FP32 operator is the modal one bit for
     bit, and still the oracle's to 1e-5."""
     wl, g, o = pair
@@ -101,3 +102,8 @@ def test_tensor_core_choice_keeps_void_skipping(pair):
     g.set_fine_tensor_cores(0)
     assert np.array_equal(y_tc, y_modal)
     assert rel(y_tc, y_o) < 1e-5
+    # likewise the tile heights: the void-skipping kernel keeps its 8-row tiles
+    for rows in (4, 16):
+        g.set_fine_tile_rows(rows)
+        assert np.array_equal(g.apply_fine(u, 1), y_modal)
+    g.set_fine_tile_rows(8)

@@ -47,7 +47,7 @@ EXPORTED = [
     "topo_mma_get_x", "topo_mma_read_x", "topo_mma_write_x", "topo_set_bc_regions", "topo_plan_bc_regions",
     "topo_unet_enable", "topo_unet_set_conv_kernel", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
-    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic", "topo_set_fine_tensor_cores", "topo_apply_level",
+    "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic", "topo_set_fine_tensor_cores", "topo_apply_level", "topo_set_fine_tile_rows",
     "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
     "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
     "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
@@ -101,7 +101,8 @@ class BatchStats(C.Structure):
 class TuneReport(C.Structure):
     _fields_ = [("tz32", C.c_int), ("tz64", C.c_int), ("cheb_ms", C.c_double * 4), ("apply_ms", C.c_double * 4),
                 ("candidates", C.c_int), ("base_ms", C.c_double), ("best_ms", C.c_double), ("tune_ms", C.c_double),
-                ("tc", C.c_int), ("cheb_tc_ms", C.c_double * 4)]
+                ("tc", C.c_int), ("cheb_tc_ms", C.c_double * 4), ("rows32", C.c_int),
+                ("cheb_rows_ms", (C.c_double * 4) * 2)]
 
 
 class MultiStats(C.Structure):
@@ -218,6 +219,7 @@ def load(build: bool = True):
         "topo_set_fine_arithmetic": (i, [vp, i]),
         "topo_set_fine_tensor_cores": (i, [vp, i]),
         "topo_apply_level": (i, [vp, i, i]),
+        "topo_set_fine_tile_rows": (i, [vp, i]),
         "topo_set_graphs": (i, [vp, i]),
         "topo_set_tiles": (i, [vp, i, i]),
         "topo_profiler_range": (i, [i]),
@@ -554,6 +556,10 @@ class Problem:
         """0: native FP64 fine operator, 1: double-float (default)."""
         self._ck(self.lib.topo_set_fine_arithmetic(self.h, arith))
 
+    def set_fine_tile_rows(self, rows):
+        """Element rows (4, 8, 16) of the FP32 modal fine kernels' CTA tile."""
+        self._ck(self.lib.topo_set_fine_tile_rows(self.h, rows))
+
     def set_fine_tensor_cores(self, on):
         """FP32 fine element products on the tcgen05 tensor cores (three-term TF32)."""
         self._ck(self.lib.topo_set_fine_tensor_cores(self.h, int(bool(on))))
@@ -628,7 +634,8 @@ class Problem:
         bd = {k: getattr(best, k) for k in keys}
         rep = {"tz32": r.tz32, "tz64": r.tz64, "cheb_ms": list(r.cheb_ms), "apply_ms": list(r.apply_ms),
                "candidates": r.candidates, "base_ms": r.base_ms, "best_ms": r.best_ms, "tune_ms": r.tune_ms,
-               "tc": r.tc, "cheb_tc_ms": list(r.cheb_tc_ms)}
+               "tc": r.tc, "cheb_tc_ms": list(r.cheb_tc_ms), "rows32": r.rows32,
+               "cheb_rows_ms": {4: list(r.cheb_rows_ms[0]), 16: list(r.cheb_rows_ms[1])}}
         return bd, rep
 
     # --- many load cases

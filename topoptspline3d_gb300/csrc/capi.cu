@@ -46,7 +46,9 @@ using namespace topo;
 #include "handle.h"
 
 // z-march depth argument of the handle's FP32 fine-kernel launches
-static inline int tz32_arg(const topo_handle* h) { return h->tz32 | (h->fine_tc ? TOPO_FINE_TC_FLAG : 0); }
+static inline int tz32_arg(const topo_handle* h) {
+  return h->tz32 | (h->fine_tc ? TOPO_FINE_TC_FLAG : 0) | fine_rows_flag(h->rows32);
+}
 
 namespace {
 
@@ -2042,6 +2044,13 @@ int topo_set_graphs(topo_handle* h, int enable) {
   return TOPO_OK;
 }
 
+int topo_set_fine_tile_rows(topo_handle* h, int rows) {
+  DEVICE_SCOPE(h);
+  if (!h || (rows != 4 && rows != 8 && rows != 16)) return TOPO_E_BAD_INPUT;
+  h->rows32 = rows;
+  return TOPO_OK;
+}
+
 int topo_set_fine_tensor_cores(topo_handle* h, int on) {
   DEVICE_SCOPE(h);
   if (!h || on < 0 || on > 1) return TOPO_E_BAD_INPUT;
@@ -2124,20 +2133,24 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
   const int tzs[4] = {4, 8, 16, 32};
   int best32 = h->tz32, best64 = h->tz64;
   double b32 = 1e30, b64 = 1e30;
-  int best_tc = h->fine_tc ? 1 : 0;
+  int best_tc = h->fine_tc ? 1 : 0, best_rows = h->rows32;
   for (int k = 0; k < 4; ++k) {
-    // the FP32 Chebyshev step with the modal element products and on the tensor cores
-    for (int tc = 0; tc < 2; ++tc) {
+    // the FP32 Chebyshev step: modal element products with CTA tiles of 8, 4
+    // and 16 element rows, and on the tensor cores
+    for (int form = 0; form < 4; ++form) {
+      const int flags = form == 1 ? TOPO_FINE_TC_FLAG : form == 2 ? TOPO_FINE_ROWS4_FLAG
+                        : form == 3 ? TOPO_FINE_ROWS16_FLAG : 0;
+      double* slot = form == 0 ? &r.cheb_ms[k] : form == 1 ? &r.cheb_tc_ms[k] : &r.cheb_rows_ms[form - 2][k];
       for (int rep = 0; rep < 2; ++rep) {  // warm-up, then timed
         CK(cudaEventRecord(a, h->stream));
         for (int i = 0; i < 5; ++i)
           launch_fine_cheb<float>(h->stream, L0.d, h->rhop32, L0.vmask, L0.U32, L0.F32, L0.U2_32, L0.dinv32,
-                                  L0.cd32, unit, true, 1, tzs[k] | (tc ? TOPO_FINE_TC_FLAG : 0));
+                                  L0.cd32, unit, true, 1, tzs[k] | flags);
         CK(cudaEventRecord(b, h->stream));
         CK(cudaEventSynchronize(b));
         float ms = 0;
         cudaEventElapsedTime(&ms, a, b);
-        (tc ? r.cheb_tc_ms : r.cheb_ms)[k] = ms / 5;
+        *slot = ms / 5;
       }
     }
     for (int rep = 0; rep < 2; ++rep) {
@@ -2152,18 +2165,22 @@ int topo_autotune(topo_handle* h, const topo_solve_opts* base, topo_solve_opts* 
       cudaEventElapsedTime(&ms, a, b);
       r.apply_ms[k] = ms / 5;
     }
-    count_launch(30);
-    if (r.cheb_ms[k] < b32) { b32 = r.cheb_ms[k]; best32 = tzs[k]; best_tc = 0; }
-    if (r.cheb_tc_ms[k] < b32) { b32 = r.cheb_tc_ms[k]; best32 = tzs[k]; best_tc = 1; }
+    count_launch(50);
+    if (r.cheb_ms[k] < b32) { b32 = r.cheb_ms[k]; best32 = tzs[k]; best_tc = 0; best_rows = 8; }
+    if (r.cheb_tc_ms[k] < b32) { b32 = r.cheb_tc_ms[k]; best32 = tzs[k]; best_tc = 1; best_rows = 8; }
+    for (int q = 0; q < 2; ++q)
+      if (r.cheb_rows_ms[q][k] < b32) { b32 = r.cheb_rows_ms[q][k]; best32 = tzs[k]; best_tc = 0; best_rows = q ? 16 : 4; }
     if (r.apply_ms[k] < b64) { b64 = r.apply_ms[k]; best64 = tzs[k]; }
   }
   CKL();
   h->tz32 = best32;
   h->tz64 = best64;
   h->fine_tc = best_tc != 0;
+  h->rows32 = best_rows;
   r.tz32 = best32;
   r.tz64 = best64;
   r.tc = best_tc;
+  r.rows32 = best_rows;
   // ---- stage 2: solver schedule, each candidate from the same initial U
   double* u0 = nullptr;
   CK(cudaMalloc((void**)&u0, sizeof(double) * n3));

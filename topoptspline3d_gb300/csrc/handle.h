@@ -44,6 +44,7 @@ struct topo_handle {
   int fine_df = 1;                  // FP64 fine operator in double-float arithmetic (topo_set_fine_arithmetic)
   int tz32 = 16, tz64 = 16;         // z-march depth of the fine kernels, FP32 / FP64 (topo_autotune)
   bool fine_tc = false;             // FP32 fine element products on the tensor cores (topo_set_fine_tensor_cores)
+  int rows32 = 8;                   // element rows of the FP32 modal kernel's CTA tile: 4, 8, 16 (topo_set_fine_tile_rows)
   // FP32 V-cycle replayed as one CUDA graph (topo_set_graphs); re-captured when its key changes
   bool graphs = true;
   cudaGraphExec_t vgraph = nullptr;

@@ -191,8 +191,8 @@ int topo_checkpoint_save(topo_handle* h, const char* path, const void* user, siz
   File f(path, "wb");
   if (!f.f) return io_fail(h, TOPO_E_BAD_INPUT, std::string("cannot open ") + path);
   const int32_t hdr[8] = {1, d0.ex, d0.ey, d0.ez, nl, (int32_t)nc, h->sd.order, h->fine_df};
-  // the FP32 depth carries the tensor-core choice as TOPO_FINE_TC_FLAG
-  const int32_t tiles[2] = {h->tz32 | (h->fine_tc ? TOPO_FINE_TC_FLAG : 0), h->tz64};
+  // the FP32 depth carries the tensor-core and tile-height choices as flags
+  const int32_t tiles[2] = {h->tz32 | (h->fine_tc ? TOPO_FINE_TC_FLAG : 0) | fine_rows_flag(h->rows32), h->tz64};
   std::vector<double> coeff, rho, u;
   if (!download(s, h->coeff, nc, coeff) || !download(s, h->rho, d0.ne, rho) ||
       !download(s, h->lv[0].U, 3 * d0.nv, u))
@@ -284,8 +284,9 @@ int topo_checkpoint_load(topo_handle* h, const char* path, void* user, size_t us
     }
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return io_fail(h, TOPO_E_CUDA, "checkpoint: upload");
-  h->tz32 = tiles[0] & ~TOPO_FINE_TC_FLAG;
+  h->tz32 = tiles[0] & ~TOPO_FINE_FLAGS;
   h->fine_tc = (tiles[0] & TOPO_FINE_TC_FLAG) != 0;
+  h->rows32 = (tiles[0] & TOPO_FINE_ROWS4_FLAG) ? 4 : (tiles[0] & TOPO_FINE_ROWS16_FLAG) ? 16 : 8;
   h->tz64 = tiles[1];
   h->rhop_stale = true;
   h->ops_ready = false;

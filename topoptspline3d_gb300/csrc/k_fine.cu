@@ -1620,15 +1620,44 @@ bool modal_tc(const LevelDims& d, int tz) {
   return sizeof(T) == 4 && (tz & TOPO_FINE_TC_FLAG) && !(d.colz && d.colz_void);
 }
 inline int modal_depth(int tz) {
-  tz &= ~TOPO_FINE_TC_FLAG;
+  tz &= ~TOPO_FINE_FLAGS;
   return tz <= 0 ? MODAL_TZ : tz;
+}
+// Element rows (warps) of the launch's CTA tile: the ROWS flags choose 4 or 16
+// for the FP32 modal kernel on levels without void planes.
+template <typename T>
+int modal_rows(const LevelDims& d, int tz) {
+  if (sizeof(T) != 4 || modal_tc<T>(d, tz) || (d.colz && d.colz_void)) return modal_tye<T>();
+  return (tz & TOPO_FINE_ROWS4_FLAG) ? 4 : (tz & TOPO_FINE_ROWS16_FLAG) ? 16 : modal_tye<T>();
 }
 
 template <typename T>
 dim3 modal_grid(const LevelDims& d, int tz, int nb) {
-  constexpr int TYE = modal_tye<T>();
+  const int rows = modal_rows<T>(d, tz);
   const int xs = modal_tc<T>(d, tz) ? MODAL_TXE - 2 : MODAL_TXE - 1;  // owned vertex columns per CTA
-  return dim3((d.vx + xs - 1) / xs, (d.vy + TYE - 2) / (TYE - 1), fine_zblocks(d.vz, modal_depth(tz)) * nb);
+  return dim3((d.vx + xs - 1) / xs, (d.vy + rows - 2) / (rows - 1), fine_zblocks(d.vz, modal_depth(tz)) * nb);
+}
+
+// One launch of the FP32 modal kernel with a CTA tile of ROWS element rows.
+template <int ROWS, int MODE, bool VOID>
+void launch_modal32_rows(cudaStream_t s, const LevelDims& d, const float* rhop, const uint8_t* vmask, const float* u,
+                         const float* f, float* out, int tz, const dim3& grid, const ChebArgs& ch) {
+  const size_t smem = sizeof(Modal32Smem<ROWS>);
+  static PerDeviceOnce once;
+  once_per_device(once, [smem] {
+    cudaError_t e = cudaFuncSetAttribute(k_fine_modal32<ROWS, MODE, true, VOID>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_fine_modal32<ROWS, MODE, false, VOID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+    return e;
+  });
+  // (MODE 3 keeps 64-bit offsets: with 32-bit ones it spilled 32 bytes and
+  // ran 122 against 118 us at 256x128x128, where modes 0-2 gained 4-9 us)
+  if (MODE != 3 && 3 * d.nv < ((int64_t)1 << 31) && d.ne < ((int64_t)1 << 31))
+    k_fine_modal32<ROWS, MODE, true, VOID><<<grid, 32 * ROWS, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+  else
+    k_fine_modal32<ROWS, MODE, false, VOID><<<grid, 32 * ROWS, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
 }
 
 // One launch of the modal operator in mode MODE: the single-barrier kernel for
@@ -1640,8 +1669,19 @@ void launch_modal_v(cudaStream_t s, const LevelDims& d, const T* rhop, const uin
                     T* out, int tz, int nb, const ChebArgs& ch) {
   const dim3 grid = modal_grid<T>(d, tz, nb);
   const bool tc = modal_tc<T>(d, tz) && !VOID;
+  const int rows = modal_rows<T>(d, tz);
   tz = modal_depth(tz);
   constexpr int TYE = modal_tye<T>();
+  if constexpr (sizeof(T) == 4 && !VOID) {
+    if (!tc && rows == 4) {
+      launch_modal32_rows<4, MODE, false>(s, d, rhop, vmask, u, f, out, tz, grid, ch);
+      return;
+    }
+    if (!tc && rows == 16) {
+      launch_modal32_rows<16, MODE, false>(s, d, rhop, vmask, u, f, out, tz, grid, ch);
+      return;
+    }
+  }
   if constexpr (sizeof(T) == 4 && TYE == 8 && !VOID) {
     if (tc) {
       const size_t smem = sizeof(Modal32TcSmem<TYE>);
@@ -1662,22 +1702,7 @@ void launch_modal_v(cudaStream_t s, const LevelDims& d, const T* rhop, const uin
     }
   }
   if constexpr (sizeof(T) == 4) {
-    const size_t smem = sizeof(Modal32Smem<TYE>);
-    static PerDeviceOnce once;
-    once_per_device(once, [smem] {
-      cudaError_t e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, true, VOID>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_fine_modal32<TYE, MODE, false, VOID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-      return e;
-    });
-    // (MODE 3 keeps 64-bit offsets: with 32-bit ones it spilled 32 bytes and
-    // ran 122 against 118 us at 256x128x128, where modes 0-2 gained 4-9 us)
-    if (MODE != 3 && 3 * d.nv < ((int64_t)1 << 31) && d.ne < ((int64_t)1 << 31))
-      k_fine_modal32<TYE, MODE, true, VOID><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
-    else
-      k_fine_modal32<TYE, MODE, false, VOID><<<grid, 32 * TYE, smem, s>>>(d, rhop, vmask, u, f, out, tz, ch);
+    launch_modal32_rows<TYE, MODE, VOID>(s, d, rhop, vmask, u, f, out, tz, grid, ch);
   } else {
     const size_t smem = sizeof(ModalSmem<T, MODAL_TXE, TYE>);
     static PerDeviceOnce once;

@@ -65,6 +65,15 @@ inline cudaError_t once_per_device(PerDeviceOnce& o, Fn&& fn) {
 // Added to the z-march depth of an FP32 fine-kernel launch: element products
 // on the tensor cores (k_fine_tc32) on levels without void planes.
 constexpr int TOPO_FINE_TC_FLAG = 1 << 16;
+// Added to the z-march depth of an FP32 fine-kernel launch: CTA tiles of 4 or
+// 16 element rows (warps) instead of 8, for the modal kernel on levels
+// without void planes (the per-tile z ranges are laid out for 8 rows).
+constexpr int TOPO_FINE_ROWS4_FLAG = 1 << 17, TOPO_FINE_ROWS16_FLAG = 1 << 18;
+constexpr int TOPO_FINE_FLAGS = TOPO_FINE_TC_FLAG | TOPO_FINE_ROWS4_FLAG | TOPO_FINE_ROWS16_FLAG;
+// the flag of a tile height (0 for the default 8 rows)
+inline int fine_rows_flag(int rows) {
+  return rows == 4 ? TOPO_FINE_ROWS4_FLAG : rows == 16 ? TOPO_FINE_ROWS16_FLAG : 0;
+}
 
 // z blocks of the fine z-marching kernels: blocks of tz vertex planes, the
 // last one also taking the remainder (up to 2 tz - 1 planes) rather than a

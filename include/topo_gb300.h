@@ -260,11 +260,21 @@ int topo_set_fine_tensor_cores(topo_handle* h, int on);
  * planes; each vertex's sum is formed the same way in every tile height, so
  * the outputs are identical.  The autotuner times the three heights. */
 int topo_set_fine_tile_rows(topo_handle* h, int rows);
-/* FP32 V-cycles of the mixed solver replayed as one CUDA graph per handle
- * (captured on first use, re-captured when the schedule, spectral bounds,
- * tiles or buffers change): 1 = on (default), 0 = direct launches.  Graphs are
- * not used while topo_profile_enable is on. */
+/* CUDA graphs per handle, captured on first use and re-captured when the
+ * schedule, tiles or buffers change: the FP32 V-cycle of the mixed solver; the
+ * mixed solve's outer FP64 CG as one graph with a device-side loop (one
+ * V-cycle per outer iteration, or the inner FP32 CG nested in it as a second
+ * device-side loop), so the host waits once per solve; the inner CG alone
+ * where the outer loop runs on the host; the OC bisection.  1 = on (default),
+ * 2 = on but the outer solve loop on the host, 0 = direct launches and host
+ * loops (the same kernels in the same order: the same results bit for bit).
+ * Graphs are not used while topo_profile_enable is on. */
 int topo_set_graphs(topo_handle* h, int enable);
+/* Which graphs the handle holds now (bits): 1 FP32 V-cycle, 2 inner CG on its
+ * own, 4 outer solve loop, 8 inner CG nested in the outer loop's graph, 16 OC
+ * bisection.  A form whose capture failed (a driver without conditional graph
+ * nodes, say) is left to the host from then on and not set. */
+int topo_graph_state(const topo_handle* h, int* state);
 /* Replaces Grid::update_residual (grid/Grid.cu:2420-2454). */
 int topo_residual(topo_handle* h, int level);
 /* Replaces Grid::gs_relax (grid/Grid.cu:1844-1887); reverse = adjoint sweep order. */

@@ -1,7 +1,8 @@
-"""The loops that run on the device inside CUDA graphs (the mixed solve's inner
-FP32 CG, the OC bisection) against the same loops run from the host: their
-stopping rules (tolerance, iteration cap, a non-finite residual) give the same
-outcome, and a failed solve leaves the handle usable."""
+"""The loops that run on the device inside CUDA graphs (the mixed solve's outer
+FP64 CG with the inner FP32 CG nested in it, the OC bisection) against the same
+loops run from the host: their stopping rules (tolerance, iteration cap, a
+non-finite residual) give the same outcome, and a failed solve leaves the
+handle usable."""
 import numpy as np
 import pytest
 
@@ -52,6 +53,43 @@ def test_nonfinite_inner_residual(graphs):
     p.put("u", np.zeros(n3))
     s = p.solve(**SOLVE)
     assert s["relres"] <= 1e-6
+
+
+@pytest.mark.parametrize("inner_max", [1, 4])
+def test_outer_loop_on_device_matches_host(inner_max):
+    """The outer CG as one graph launch (one V-cycle per outer iteration, or the
+    graphed inner CG as a nested WHILE loop) runs the host loop's kernels in
+    the host loop's order: the same iteration and V-cycle counts and the same
+    solution bit for bit, on the first solve (capture) and on a replay."""
+    res = []
+    for graphs in (1, 0):
+        p = _make(graphs)
+        u0 = p.get("u")
+        runs = []
+        for _ in range(2):
+            p.put("u", u0)
+            s = p.solve(**dict(SOLVE, inner_max=inner_max))
+            runs.append((s["iterations"], s["vcycles"], s["relres"], p.get("u")))
+        state = p.graph_state()
+        if graphs:  # the outer loop ran as a graph, with the inner CG nested in it
+            assert state["solve"] and state["nested_inner"] == (inner_max > 1) and not state["inner"]
+        else:
+            assert not any(state.values())
+        res.append(runs)
+    for (it_g, vc_g, rr_g, u_g), (it_h, vc_h, rr_h, u_h) in zip(res[0], res[1]):
+        assert (it_g, vc_g, rr_g) == (it_h, vc_h, rr_h)
+        assert np.array_equal(u_g, u_h)
+    assert res[0][0][2] <= 1e-6
+
+
+@pytest.mark.parametrize("graphs", [0, 1])
+def test_outer_cap(graphs):
+    """A tolerance that is never met: the outer loop stops at max_iter in both
+    forms and the solve reports that it did not converge."""
+    p = _make(graphs)
+    s = p.solve(**dict(SOLVE, rtol=1e-30, max_iter=5, inner_max=2), check=False)
+    assert s["rc"] == capi.TOPO_E_NOT_CONVERGED
+    assert s["iterations"] == 5 and s["vcycles"] <= 10
 
 
 def test_oc_loop_matches_host():

@@ -48,7 +48,7 @@ EXPORTED = [
     "topo_unet_enable", "topo_unet_set_conv_kernel", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic", "topo_set_fine_tensor_cores", "topo_apply_level", "topo_set_fine_tile_rows",
-    "topo_autotune", "topo_set_graphs", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
+    "topo_autotune", "topo_set_graphs", "topo_graph_state", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
     "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
     "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
     "topo_checkpoint_save", "topo_checkpoint_load", "topo_mma_checkpoint_save", "topo_mma_checkpoint_load",
@@ -221,6 +221,7 @@ def load(build: bool = True):
         "topo_apply_level": (i, [vp, i, i]),
         "topo_set_fine_tile_rows": (i, [vp, i]),
         "topo_set_graphs": (i, [vp, i]),
+        "topo_graph_state": (i, [vp, ip]),
         "topo_set_tiles": (i, [vp, i, i]),
         "topo_profiler_range": (i, [i]),
         "topo_design_batch": (i, [C.POINTER(vp), i, C.POINTER(IterOpts), i, i, i, C.POINTER(IterStats),
@@ -551,6 +552,13 @@ class Problem:
 
     def set_graphs(self, enable):
         self._ck(self.lib.topo_set_graphs(self.h, int(enable)))
+
+    def graph_state(self):
+        """The graphs the handle holds: {"vcycle", "inner", "solve", "nested_inner", "oc"} -> bool."""
+        st = C.c_int()
+        self._ck(self.lib.topo_graph_state(self.h, C.byref(st)))
+        names = ("vcycle", "inner", "solve", "nested_inner", "oc")
+        return {n: bool(st.value >> k & 1) for k, n in enumerate(names)}
 
     def set_fine_arithmetic(self, arith):
         """0: native FP64 fine operator, 1: double-float (default)."""

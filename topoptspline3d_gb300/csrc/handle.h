@@ -22,7 +22,10 @@ enum Slot {
   S_LOOP = S_PW + 2 * S_MAXLEV,
   // device-side OC bisection: lo, hi, the current trial's threshold, its
   // volume fraction, trials, repeats (the reference loop's itn)
-  S_OC = S_LOOP + 4, S_COUNT = S_OC + 6
+  S_OC = S_LOOP + 4,
+  // device-controlled outer CG loop of the mixed solve (the same four slots
+  // as S_LOOP)
+  S_OLOOP = S_OC + 6, S_COUNT = S_OLOOP + 4
 };
 
 // Chebyshev step coefficients (c_old, c_new) in device memory: per precision
@@ -57,6 +60,14 @@ struct topo_handle {
   cudaGraphExec_t igraph = nullptr;
   std::vector<double> ikey;
   long long igraph_fixed = 0, igraph_body = 0;
+  // the mixed solve's outer CG as one graph with a device-side WHILE loop
+  // (sgraph), the inner CG nested in it as a second WHILE loop; kernels of its
+  // fixed part, of one outer iteration (without the inner loop's body) and of
+  // one inner iteration
+  bool sgraph_ok = true;
+  cudaGraphExec_t sgraph = nullptr;
+  std::vector<double> skey;
+  long long sgraph_fixed = 0, sgraph_body = 0, sgraph_inner = 0;
   // OC bisection as one graph with a device-side WHILE loop (ograph)
   bool ograph_ok = true;
   cudaGraphExec_t ograph = nullptr;

@@ -65,12 +65,15 @@ __device__ __forceinline__ void finish_sum(const double* partial, int nb, double
 // Per-thread partial sums are accumulated in the vector's precision (FP32
 // vectors: a few dozen terms per thread, inside the FP32 inner solver only) and
 // combined in FP64 across threads and blocks.  With ctr the last block also
-// writes the total to out.
+// writes the total to out.  With skip_if_zero the whole grid does nothing while
+// *skip_if_zero is 0 (a device-side loop's first iteration).
 template <typename T>
 __global__ void __launch_bounds__(RED_THREADS) k_dot_partial(const T* __restrict__ a, const T* __restrict__ b,
                                                              int64_t n, double* __restrict__ partial,
                                                              double* __restrict__ out = nullptr,
-                                                             unsigned* __restrict__ ctr = nullptr) {
+                                                             unsigned* __restrict__ ctr = nullptr,
+                                                             const double* __restrict__ skip_if_zero = nullptr) {
+  if (skip_if_zero && *skip_if_zero == 0.0) return;
   T s = T(0);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     s += a[i] * (b ? b[i] : T(1));
@@ -113,10 +116,11 @@ __global__ void k_finalize_max(const double* __restrict__ partial, int nb, doubl
 }
 
 template <typename T>
-void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out, unsigned* ctr) {
+void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out, unsigned* ctr,
+                const double* skip_if_zero) {
   const int nb = reduce_blocks(n);
   if (ctr) {
-    k_dot_partial<T><<<nb, RED_THREADS, 0, s>>>(a, b, n, partial, out, ctr);
+    k_dot_partial<T><<<nb, RED_THREADS, 0, s>>>(a, b, n, partial, out, ctr, skip_if_zero);
   } else {
     k_dot_partial<T><<<nb, RED_THREADS, 0, s>>>(a, b, n, partial);
     k_finalize_sum<<<1, RED_THREADS, 0, s>>>(partial, nb, out);
@@ -290,8 +294,10 @@ template void launch_pcg_update_rr<float>(cudaStream_t, float*, float*, float*, 
 
 
 
-template void launch_dot<double>(cudaStream_t, const double*, const double*, int64_t, double*, double*, unsigned*);
-template void launch_dot<float>(cudaStream_t, const float*, const float*, int64_t, double*, double*, unsigned*);
+template void launch_dot<double>(cudaStream_t, const double*, const double*, int64_t, double*, double*, unsigned*,
+                                  const double*);
+template void launch_dot<float>(cudaStream_t, const float*, const float*, int64_t, double*, double*, unsigned*,
+                                 const double*);
 template void launch_fill<double>(cudaStream_t, double*, double, int64_t);
 template void launch_fill<float>(cudaStream_t, float*, float, int64_t);
 template void launch_copy<double>(cudaStream_t, const double*, double*, int64_t);

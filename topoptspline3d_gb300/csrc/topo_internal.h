@@ -241,10 +241,11 @@ void launch_dense_gemv(cudaStream_t s, int n, const T* Ainv, const T* f_soa, T* 
 int reduce_blocks(int64_t n);
 // *out = sum of partial[0 .. nb) in index order (one CTA)
 void launch_sum_partials(cudaStream_t s, const double* partial, int nb, double* out);
-// ctr (optional): a zeroed counter; the last block then writes out itself (one launch)
+// ctr (optional): a zeroed counter; the last block then writes out itself (one
+// launch).  skip_if_zero (with ctr): no work while *skip_if_zero is 0.
 template <typename T>
 void launch_dot(cudaStream_t s, const T* a, const T* b, int64_t n, double* partial, double* out,
-                unsigned* ctr = nullptr);
+                unsigned* ctr = nullptr, const double* skip_if_zero = nullptr);
 // b == nullptr sums a.
 void launch_sum(cudaStream_t s, const double* a, int64_t n, double* partial, double* out);
 void launch_axpby(cudaStream_t s, double a, const double* x, double b, double* y, int64_t n);

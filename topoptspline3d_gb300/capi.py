@@ -480,6 +480,10 @@ class Problem:
             raise TopoError(rc, self.lib.topo_last_error(self.h).decode())
         return rc
 
+    def last_error(self) -> str:
+        """The handle's last recorded message (errors, and fallbacks such as a graph not captured)."""
+        return self.lib.topo_last_error(self.h).decode()
+
     # --- hierarchy
     def num_levels(self) -> int:
         n = C.c_int()
@@ -554,10 +558,11 @@ class Problem:
         self._ck(self.lib.topo_set_graphs(self.h, int(enable)))
 
     def graph_state(self):
-        """The graphs the handle holds: {"vcycle", "inner", "solve", "nested_inner", "oc"} -> bool."""
+        """The graphs the handle holds: {"vcycle", "inner", "solve", "nested_inner", "oc",
+        "iteration"} -> bool."""
         st = C.c_int()
         self._ck(self.lib.topo_graph_state(self.h, C.byref(st)))
-        names = ("vcycle", "inner", "solve", "nested_inner", "oc")
+        names = ("vcycle", "inner", "solve", "nested_inner", "oc", "iteration")
         return {n: bool(st.value >> k & 1) for k, n in enumerate(names)}
 
     def set_fine_arithmetic(self, arith):

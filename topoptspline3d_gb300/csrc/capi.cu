@@ -567,6 +567,116 @@ __global__ void k_loop_beta(const double* loop, double* sc) {
 
 int read_scalars(topo_handle* h, int first, int count);
 
+// Inside a capture on h->stream: a conditional node of `type` (IF or WHILE)
+// with condition hc after the work captured so far, and the capture goes on
+// after it.  body() is captured as the node's body graph on a helper stream,
+// which stands in for h->stream meanwhile, so the enclosing capture stays open
+// (streams forked from it, the side stream say, need not have joined).
+// Kernels of one body pass come back in *per_body.  TOPO_E_STATE: the node
+// could not be made (no helper stream left, or a conditional node nested in
+// another one's body not available); the enclosing capture then fails.
+template <typename Body>
+int capture_cond_node(topo_handle* h, cudaGraphConditionalHandle hc, cudaGraphConditionalNodeType type,
+                      Body&& body, long long* per_body) {
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  cudaStream_t s = h->stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* dp = nullptr;
+  size_t nd = 0;
+  if (h->cdepth >= TOPO_COND_DEPTH || !h->cstream[h->cdepth]) return TOPO_E_STATE;
+  if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &dp, nullptr, &nd) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive || !g)
+    return TOPO_E_STATE;
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hc;
+  cp.conditional.type = type;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode = nullptr;
+  if (cudaGraphAddNode(&cnode, g, dp, nullptr, nd, &cp) != cudaSuccess) return TOPO_E_STATE;
+  if (cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+    return TOPO_E_STATE;
+  cudaStream_t bs = h->cstream[h->cdepth];
+  if (cudaStreamBeginCaptureToGraph(bs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0, mode) != cudaSuccess)
+    return TOPO_E_STATE;
+  h->stream = bs;
+  ++h->cdepth;
+  const long long l1 = t_launches;
+  const int rc = body();
+  *per_body = t_launches - l1;
+  --h->cdepth;
+  h->stream = s;
+  cudaGraph_t gs = nullptr;
+  const bool ended = cudaStreamEndCapture(bs, &gs) == cudaSuccess;
+  RET(rc);
+  return ended ? TOPO_OK : TOPO_E_STATE;
+}
+
+// Helper streams for the bodies of nested conditional nodes, made before a
+// capture begins.
+int ensure_cond_streams(topo_handle* h) {
+  for (int k = 0; k < TOPO_COND_DEPTH; ++k)
+    if (!h->cstream[k]) CK(cudaStreamCreateWithFlags(&h->cstream[k], cudaStreamNonBlocking));
+  return TOPO_OK;
+}
+
+// Conditions of the levels' restart nodes in a captured power iteration.
+struct LevelConds {
+  cudaGraphConditionalHandle c[S_MAXLEV];
+};
+
+// Spectral bounds on the device, slots of precision table tb: for each level
+// in `mask`, lam = (x.z) / |x| (0 when x = 0) from its power-iteration sums
+// in sc[S_PW + 2 l ..].  final = 0 (a captured estimate after its first pass):
+// sets each warm level's condition to whether lam fell more than 5% below
+// sc[S_LPREV] (8 more steps then run) and counts those levels in sc[S_DI + 2].
+// final = 1: sc[S_LAM] = sc[S_LPREV] = lam, the values the host computes from
+// the same sums when it runs the loop (IEEE division and square root).
+__global__ void k_power_lam(double* sc, int tb, unsigned mask, unsigned warm, int final, LevelConds conds) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int restarts = 0;
+  for (int l = 0; l < S_MAXLEV; ++l) {
+    if (!((mask >> l) & 1u)) continue;
+    const double xx = sc[S_PW + 2 * l], xz = sc[S_PW + 2 * l + 1];
+    const double lam = xx > 0 ? xz / sqrt(xx) : 0.0;
+    double* lp = sc + S_LPREV + tb * S_MAXLEV + l;
+    if (final) {
+      sc[S_LAM + tb * S_MAXLEV + l] = lam;
+      *lp = lam;
+    } else {
+      const bool again = ((warm >> l) & 1u) && lam < 0.95 * *lp;
+      restarts += again ? 1 : 0;
+      cudaGraphSetConditional(conds.c[l], again ? 1u : 0u);
+    }
+  }
+  if (!final) sc[S_DI + 2] = (double)restarts;
+}
+
+// Chebyshev coefficients of levels 0 .. nl-1 from their bounds lam[l] and the
+// interval [lo, hi] x lam (three-term recurrence, Saad, Iterative Methods for
+// Sparse Linear Systems, Alg. 12.1): tab[2 (l CHEB_MAX_DEG + k) + {0, 1}] =
+// (c_old, c_new) of step k.  One thread per level.
+__global__ void k_cheb_table(const double* lam, int nl, double lo, double hi, int degree, double* tab) {
+  const int l = threadIdx.x;
+  if (l >= nl) return;
+  const double lmax = lam[l] * hi, lmin = lam[l] * lo;
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+  const double sigma = theta / delta;
+  double rho_old = 1.0 / sigma;
+  for (int k = 0; k < degree; ++k) {
+    double c_old = 0.0, c_new = 1.0 / theta;
+    if (k > 0) {
+      const double rho_new = 1.0 / (2.0 * sigma - rho_old);
+      c_old = rho_new * rho_old;
+      c_new = 2.0 * rho_new / delta;
+      rho_old = rho_new;
+    }
+    tab[2 * (l * CHEB_MAX_DEG + k)] = c_old;
+    tab[2 * (l * CHEB_MAX_DEG + k) + 1] = c_new;
+  }
+}
+
 // Largest eigenvalue of D^-1 A of every level whose bound is stale, by power
 // iteration.  First estimate of a level: 12 steps from the deterministic start
 // (as the oracle).  After an operator update: 4 steps from the previous
@@ -629,57 +739,69 @@ int estimate_bounds(topo_handle* h) {
     }
     return TOPO_OK;
   };
+  unsigned mask = 0, warm = 0;
+  for (Run& r : runs) {
+    mask |= 1u << r.l;
+    warm |= r.warm ? 1u << r.l : 0u;
+  }
   for (Run& r : runs) power_steps(r, r.warm ? 4 : 12);
-  RET(read_all());
-  bool more = false;
-  for (Run& r : runs)
-    if (r.warm && r.lam < 0.95 * P<T>::lprev(h->lv[r.l])) {
-      power_steps(r, 8);
-      more = true;
+  if (h->iter_capture) {
+    // inside a captured design iteration: the restart test on the device and
+    // one conditional node per level for its 8 more steps (an even count, so
+    // the iterate ends in the same buffer either way)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess || !g)
+      return TOPO_E_STATE;
+    LevelConds conds{};
+    for (Run& r : runs)
+      if (cudaGraphConditionalHandleCreate(&conds.c[r.l], g, 0, cudaGraphCondAssignDefault) != cudaSuccess)
+        return TOPO_E_STATE;
+    k_power_lam<<<1, 32, 0, h->stream>>>(h->sc, P<T>::table, mask, warm, 0, conds);
+    count_launch();
+    for (Run& r : runs) {
+      long long per = 0;
+      RET(capture_cond_node(h, conds.c[r.l], cudaGraphCondTypeIf, [&]() -> int {
+        power_steps(r, 8);
+        return TOPO_OK;
+      }, &per));
+      h->d_if_body = per;
     }
-  if (more) RET(read_all());
+  } else {
+    RET(read_all());
+    bool more = false;
+    for (Run& r : runs)
+      if (r.warm && r.lam < 0.95 * P<T>::lprev(h->lv[r.l])) {
+        power_steps(r, 8);
+        more = true;
+      }
+    if (more) RET(read_all());
+  }
+  k_power_lam<<<1, 32, 0, h->stream>>>(h->sc, P<T>::table, mask, warm, 1, LevelConds{});
+  count_launch();
   for (Run& r : runs) {
     DevLevel& L = h->lv[r.l];
     CK(cudaMemcpyAsync(P<T>::eig(L), r.x, sizeof(T) * 3 * L.d.nv, cudaMemcpyDeviceToDevice, h->stream));
-    P<T>::lmax(L) = r.lam;
-    P<T>::lprev(L) = r.lam;
+    // (a captured estimate: the values are read after the graph ran; any
+    // nonzero mark keeps the bound from being estimated twice in the capture)
+    P<T>::lmax(L) = h->iter_capture ? -1.0 : r.lam;
+    P<T>::lprev(L) = h->iter_capture ? -1.0 : r.lam;
   }
   return TOPO_OK;
 }
 
 // Chebyshev coefficients of every level in precision T from the spectral
-// bounds [lo, hi] x lmax (three-term recurrence, Saad, Iterative Methods for
-// Sparse Linear Systems, Alg. 12.1), written to the device table when they
-// changed.  The copy is from pageable host memory, which the runtime stages
-// before the call returns, so the host vector may change right after.
+// bounds in sc[S_LAM] (on the device, so a captured design iteration computes
+// them from bounds it estimated itself, and a host-run one gets the same).
 template <typename T>
 int cheb_upload(topo_handle* h, const ChebParams& cp) {
   if (cp.degree > CHEB_MAX_DEG)
     return fail(h, TOPO_E_BAD_INPUT, "Chebyshev degree %d above %d", cp.degree, CHEB_MAX_DEG);
-  std::vector<double> tab(2 * S_MAXLEV * CHEB_MAX_DEG, 0.0);
-  for (int l = 0; l < (int)h->lv.size(); ++l) {
-    const double lm = P<T>::lmax(h->lv[l]);
-    const double lmax = lm * cp.hi, lmin = lm * cp.lo;
-    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
-    const double sigma = theta / delta;
-    double rho_old = 1.0 / sigma;
-    for (int k = 0; k < cp.degree; ++k) {
-      double c_old = 0.0, c_new = 1.0 / theta;
-      if (k > 0) {
-        const double rho_new = 1.0 / (2.0 * sigma - rho_old);
-        c_old = rho_new * rho_old;
-        c_new = 2.0 * rho_new / delta;
-        rho_old = rho_new;
-      }
-      tab[2 * (l * CHEB_MAX_DEG + k)] = c_old;
-      tab[2 * (l * CHEB_MAX_DEG + k) + 1] = c_new;
-    }
-  }
-  const size_t off = (size_t)P<T>::table * tab.size();
-  if (!std::equal(tab.begin(), tab.end(), h->chebc_host.begin() + off)) {
-    std::copy(tab.begin(), tab.end(), h->chebc_host.begin() + off);
-    CK(cudaMemcpyAsync(h->chebc + off, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->stream));
-  }
+  const size_t off = (size_t)P<T>::table * 2 * S_MAXLEV * CHEB_MAX_DEG;
+  k_cheb_table<<<1, 32, 0, h->stream>>>(h->sc + S_LAM + P<T>::table * S_MAXLEV, (int)h->lv.size(), cp.lo, cp.hi,
+                                         cp.degree, h->chebc + off);
+  count_launch();
+  CKL();
   return TOPO_OK;
 }
 
@@ -691,6 +813,9 @@ int prepare_smoother(topo_handle* h, int smoother, const ChebParams& cp) {
 }
 
 int read_scalars(topo_handle* h, int first, int count) {
+  if (h->iter_capture)  // (a captured design iteration reads its results after the launch)
+    return fail(h, TOPO_E_STATE, "host read of slots %d..%d inside a captured design iteration", first,
+                first + count - 1);
   CK(cudaMemcpyAsync(h->hsc + first, h->sc + first, sizeof(double) * count, cudaMemcpyDeviceToHost,
                      h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -798,6 +923,7 @@ int fcg_T(topo_handle* h, T* x, const T* b, T* r, T* d, T* q, T* rold, T* z, dou
 template <typename Setup, typename Body, typename Tail>
 int capture_loop_graph(topo_handle* h, Setup&& setup, Body&& body, Tail&& tail, cudaGraphExec_t* exec,
                        long long* fixed, long long* per_body) {
+  RET(ensure_cond_streams(h));
   cudaGraph_t g = nullptr;
   cudaGraphConditionalHandle hc = 0;
   cudaGraphNode_t cnode = nullptr;
@@ -861,50 +987,21 @@ int capture_loop_graph(topo_handle* h, Setup&& setup, Body&& body, Tail&& tail, 
   return TOPO_OK;
 }
 
-// Inside a capture on h->stream: a WHILE node after the work captured so far,
-// then the capture resumes after it.  setup(hc) is captured before the node
-// and ends with a kernel that sets the loop condition through hc; body(hc),
-// one pass of the loop, is captured as the node's body graph and ends with a
-// kernel that sets it again.  Kernels of one body pass come back in
-// *per_body.  TOPO_E_STATE: the node could not be made (a conditional node
-// nested in another one's body is not available, say); the capture is then
-// ended or invalid, and the caller's capture fails.
+// Inside a capture on h->stream: a WHILE node after the work captured so far.
+// setup(hc) is captured before the node and ends with a kernel that sets the
+// loop condition through hc; body(hc), one pass of the loop, is the node's
+// body graph and ends with a kernel that sets it again (capture_cond_node).
 template <typename Setup, typename Body>
 int capture_nested_loop(topo_handle* h, Setup&& setup, Body&& body, long long* per_body) {
-  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaGraph_t g = nullptr;
-  const cudaGraphNode_t* dp = nullptr;
-  size_t nd = 0;
   if (cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
       cs != cudaStreamCaptureStatusActive || !g)
     return TOPO_E_STATE;
   cudaGraphConditionalHandle hc = 0;
   if (cudaGraphConditionalHandleCreate(&hc, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return TOPO_E_STATE;
   RET(setup(hc));
-  if (cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, nullptr, &dp, nullptr, &nd) != cudaSuccess)
-    return TOPO_E_STATE;
-  const std::vector<cudaGraphNode_t> deps(dp, dp + nd);
-  cudaGraph_t gs = nullptr;
-  if (cudaStreamEndCapture(h->stream, &gs) != cudaSuccess) return TOPO_E_STATE;
-  cudaGraphNodeParams cp = {};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = hc;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t cnode = nullptr;
-  if (cudaGraphAddNode(&cnode, g, deps.data(), nullptr, deps.size(), &cp) != cudaSuccess) return TOPO_E_STATE;
-  if (cudaStreamBeginCaptureToGraph(h->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0, mode) !=
-      cudaSuccess)
-    return TOPO_E_STATE;
-  const long long l1 = t_launches;
-  const int rc = body(hc);
-  *per_body = t_launches - l1;
-  const bool ended = cudaStreamEndCapture(h->stream, &gs) == cudaSuccess;
-  RET(rc);
-  if (!ended || cudaStreamBeginCaptureToGraph(h->stream, g, &cnode, nullptr, 1, mode) != cudaSuccess)
-    return TOPO_E_STATE;
-  return TOPO_OK;
+  return capture_cond_node(h, hc, cudaGraphCondTypeWhile, [&]() { return body(hc); }, per_body);
 }
 
 // The FP32 inner CG of the mixed solve, z = CG(r) from x = 0, as one CUDA
@@ -946,7 +1043,7 @@ int inner_cg_graphed(topo_handle* h, const double* rin, double* zout, double rto
     return TOPO_OK;
   };
   if (h->in_capture) {  // inside the outer solve's capture: a nested WHILE node
-    RET(capture_nested_loop(h, setup, body, &h->sgraph_inner));
+    RET(capture_nested_loop(h, setup, body, h->iter_capture ? &h->d_inner_body : &h->sgraph_inner));
     return tail();
   }
   if (!h->igraph || key != h->ikey) {
@@ -982,20 +1079,26 @@ int outer_cg_graphed(topo_handle* h, double rtol, int maxit, Prec&& prec, std::v
                          (double)(uintptr_t)h->rold, (double)(uintptr_t)L0.U, (double)(uintptr_t)h->x32,
                          (double)(uintptr_t)h->d32, (double)(uintptr_t)h->q32, (double)(uintptr_t)h->rold32,
                          (double)tz32_arg(h), (double)(uintptr_t)h->fdot, (double)h->fdot_cap});
+  auto setup = [&](cudaGraphConditionalHandle hc) -> int {
+    CK(cudaMemsetAsync(loop + 2, 0, 2 * sizeof(double), h->stream));
+    k_loop_start<<<1, 32, 0, h->stream>>>(loop, h->sc + S_FF, h->sc + S_RR, rtol, maxit, hc);
+    count_launch();
+    return TOPO_OK;
+  };
+  auto body = [&](cudaGraphConditionalHandle hc) -> int {
+    RET(fcg_body<double>(h, h->x, h->r, h->d, h->q, h->rold, L0.U, h->sc, prec, false, -1, loop));
+    k_loop_step<<<1, 32, 0, h->stream>>>(loop, h->sc + S_RR, rtol, maxit, hc);
+    count_launch();
+    return TOPO_OK;
+  };
+  if (h->iter_capture) {  // inside a captured design iteration: a nested WHILE node
+    h->d_inner_body = 0;
+    RET(capture_nested_loop(h, setup, body, &h->d_outer_body));
+    h->d_outer_body -= h->d_inner_body;
+    return TOPO_OK;
+  }
   if (!h->sgraph || key != h->skey) {
     if (h->sgraph) { cudaGraphExecDestroy(h->sgraph); h->sgraph = nullptr; }
-    auto setup = [&](cudaGraphConditionalHandle hc) -> int {
-      CK(cudaMemsetAsync(loop + 2, 0, 2 * sizeof(double), h->stream));
-      k_loop_start<<<1, 32, 0, h->stream>>>(loop, h->sc + S_FF, h->sc + S_RR, rtol, maxit, hc);
-      count_launch();
-      return TOPO_OK;
-    };
-    auto body = [&](cudaGraphConditionalHandle hc) -> int {
-      RET(fcg_body<double>(h, h->x, h->r, h->d, h->q, h->rold, L0.U, h->sc, prec, false, -1, loop));
-      k_loop_step<<<1, 32, 0, h->stream>>>(loop, h->sc + S_RR, rtol, maxit, hc);
-      count_launch();
-      return TOPO_OK;
-    };
     auto tail = [&]() -> int { return TOPO_OK; };
     h->sgraph_inner = 0;
     const int rc = capture_loop_graph(h, setup, body, tail, &h->sgraph, &h->sgraph_fixed, &h->sgraph_body);
@@ -1185,9 +1288,10 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
   }
   if (rc == TOPO_OK) {
     cudaMemcpyAsync(h->dKe, h->Ke, sizeof(double) * 576, cudaMemcpyHostToDevice, h->stream);
-    h->chebc_host.assign(CHEB_TABLE, 0.0);
-    h->chebc_host[CHEB_TABLE - 1] = 1.0;
-    cudaMemcpyAsync(h->chebc, h->chebc_host.data(), sizeof(double) * CHEB_TABLE, cudaMemcpyHostToDevice, h->stream);
+    std::vector<double> tab(CHEB_TABLE, 0.0);
+    tab[CHEB_TABLE - 1] = 1.0;
+    cudaMemcpyAsync(h->chebc, tab.data(), sizeof(double) * CHEB_TABLE, cudaMemcpyHostToDevice, h->stream);
+    cudaMemsetAsync(h->sc, 0, sizeof(double) * S_COUNT, h->stream);
     cudaHostAlloc((void**)&h->hsc, sizeof(double) * S_COUNT, cudaHostAllocDefault);
     // density starts at 1 on active elements
     std::vector<double> one(d0.ne);
@@ -1227,6 +1331,11 @@ void topo_destroy(topo_handle* h) {
   if (h->igraph) cudaGraphExecDestroy(h->igraph);
   if (h->ograph) cudaGraphExecDestroy(h->ograph);
   if (h->sgraph) cudaGraphExecDestroy(h->sgraph);
+  if (h->dgraph) cudaGraphExecDestroy(h->dgraph);
+  for (int k = 0; k < TOPO_COND_DEPTH; ++k)
+    if (h->cstream[k]) cudaStreamDestroy(h->cstream[k]);
+  for (int k = 0; k < 2; ++k)
+    if (h->ev_solve[k]) cudaEventDestroy(h->ev_solve[k]);
   prof_drop_graph_events(h);
   if (h->multi) {
     for (void* p : h->multi->allocs) cudaFree(p);
@@ -1315,6 +1424,7 @@ int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads) {
   }
   CK(cudaMemcpyAsync(L.vmask, vm.data(), nv, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(L.F, F.data(), sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, h->stream));
+  ++h->fgen;
   if (h->lv.size() > 1) {
     // coarse elements of level 1 containing a fine element with a fixed DOF
     const LevelDims& c = h->lv[1].d;
@@ -1475,6 +1585,7 @@ int topo_put_array(topo_handle* h, int which, int level, const void* src, size_t
   CK(cudaMemcpyAsync(p, src, n * es, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (which == TOPO_RHO) { h->rhop_stale = true; h->ops_ready = false; }
+  if (which == TOPO_F && level == 0) ++h->fgen;
   return TOPO_OK;
 }
 
@@ -1740,7 +1851,7 @@ static int coarse_join(topo_handle* h) {
 // Joins the side stream's inversion and reads its status.
 static int coarse_finish(topo_handle* h) {
   RET(coarse_join(h));
-  if (!h->coarse_unchecked) return TOPO_OK;
+  if (!h->coarse_unchecked || h->iter_capture) return TOPO_OK;  // (a captured iteration reads it afterwards)
   CK(cudaEventSynchronize(h->ev_coarse));
   h->coarse_unchecked = false;
   if (h->hstat[1] != 0) return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", h->hstat[1] - 1);
@@ -1778,15 +1889,23 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
   if (o->cheb_lo > 0) cp.lo = o->cheb_lo;
   if (o->cheb_hi > 0) cp.hi = o->cheb_hi;
   ScopedEvent e0, e1;
-  CK(e0.create());
-  CK(e1.create());
-  CK(cudaEventRecord(e0, h->stream));
   topo_solve_stats st{};
+  // (inside a captured design iteration the solve is timed by external
+  // event-record nodes, ||F|| is the one read when it was captured, and the
+  // results are read after the graph ran)
+  const bool cap = h->iter_capture;
+  if (cap) {
+    CK(cudaEventRecordWithFlags(h->ev_solve[0], h->stream, cudaEventRecordExternal));
+  } else {
+    CK(e0.create());
+    CK(e1.create());
+    CK(cudaEventRecord(e0, h->stream));
+  }
   // ||F||
   launch_dot<double>(h->stream, L0.F, L0.F, n3, h->partial, h->sc + S_FF);
   count_launch(2);
-  RET(read_scalars(h, S_FF, 1));
-  const double fn = std::sqrt(h->hsc[S_FF]);
+  if (!cap) RET(read_scalars(h, S_FF, 1));
+  const double fn = cap ? h->iter_fn : std::sqrt(h->hsc[S_FF]);
   int rc = TOPO_OK;
   if (o->mode != TOPO_SOLVE_MIXED) RET(coarse_join(h));
   if (fn == 0.0) {
@@ -1970,6 +2089,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
     // preconditioner is one V-cycle or the graphed inner CG
     const bool sgraph = h->graphs && h->sgraph_ok && !h->prof && !o->learned && h->nb == 1 &&
                         (inner_max <= 1 || igraph);
+    if (cap && !sgraph) return TOPO_E_STATE;  // (a captured design iteration needs the device loop)
     bool sgraph_used = false;
     if (sgraph) {
       level_apply<double>(h, 0, h->x, h->f, h->r, true);  // r = f - A x
@@ -1982,6 +2102,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
       if (grc == TOPO_OK) {
         sgraph_used = true;
       } else {  // the capture failed: the host loop, now and for the handle's later solves
+        if (cap) return grc;
         igraph_used = false;
         CKL();
       }
@@ -1991,7 +2112,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
                          &it, &rel, fn);
     CK(cudaMemcpyAsync(L0.F, h->f, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
     CK(cudaMemcpyAsync(L0.U, h->x, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream));
-    if (sgraph_used) {  // outer (and inner) iterations the device ran, and non-finite residuals
+    if (sgraph_used && !cap) {  // outer (and inner) iterations the device ran, and non-finite residuals
       RET(read_scalars(h, S_LOOP, S_OLOOP + 4 - S_LOOP));
       const long long outer_its = (long long)h->hsc[S_OLOOP];
       const long long inner_its = igraph ? (long long)h->hsc[S_LOOP + 3] : 0;
@@ -2004,7 +2125,7 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
       if (h->hsc[S_OLOOP + 2] != 0.0)
         return fail(h, TOPO_E_NONFINITE, "CG residual became non-finite at iteration %d",
                     (int)h->hsc[S_OLOOP + 2] - 1);
-    } else if (igraph_used) {  // inner iterations the device ran, and a non-finite inner residual
+    } else if (igraph_used && !sgraph_used) {  // inner iterations the device ran, and a non-finite inner residual
       RET(read_scalars(h, S_LOOP + 2, 2));
       const long long inner_its = (long long)h->hsc[S_LOOP + 3];
       nvc += (int)inner_its;
@@ -2037,6 +2158,10 @@ static int solve_impl(topo_handle* h, const topo_solve_opts* o, topo_solve_stats
     }
     launch_dot<double>(h->stream, L0.R, L0.R, n3, h->partial, h->sc + S_RR, h->ctr);
     count_launch();
+    if (cap) {
+      CK(cudaEventRecordWithFlags(h->ev_solve[1], h->stream, cudaEventRecordExternal));
+      return TOPO_OK;
+    }
     RET(read_scalars(h, S_RR, 1));
     st.relres = std::sqrt(h->hsc[S_RR]) / fn;
   }
@@ -2057,6 +2182,12 @@ int topo_compliance(topo_handle* h, double* c) {
   DEVICE_SCOPE(h);
   if (!h || !c) return TOPO_E_BAD_INPUT;
   DevLevel& L = h->lv[0];
+  if (h->iter_capture) {  // read after the graph ran
+    launch_dot<double>(h->stream, L.F, L.U, 3 * L.d.nv, h->partial, h->sc + S_DI);
+    count_launch(2);
+    *c = 0.0;
+    return TOPO_OK;
+  }
   launch_dot<double>(h->stream, L.F, L.U, 3 * L.d.nv, h->partial, h->sc + S_TMP);
   count_launch(2);
   CKL();
@@ -2177,7 +2308,8 @@ int topo_set_graphs(topo_handle* h, int enable) {
   if (h->igraph) { cudaGraphExecDestroy(h->igraph); h->igraph = nullptr; }
   if (h->ograph) { cudaGraphExecDestroy(h->ograph); h->ograph = nullptr; }
   if (h->sgraph) { cudaGraphExecDestroy(h->sgraph); h->sgraph = nullptr; }
-  h->igraph_ok = h->ograph_ok = true;
+  if (h->dgraph) { cudaGraphExecDestroy(h->dgraph); h->dgraph = nullptr; }
+  h->igraph_ok = h->ograph_ok = h->dgraph_ok = true;
   h->sgraph_ok = enable != 2;
   return TOPO_OK;
 }
@@ -2185,7 +2317,7 @@ int topo_set_graphs(topo_handle* h, int enable) {
 int topo_graph_state(const topo_handle* h, int* state) {
   if (!h || !state) return TOPO_E_BAD_INPUT;
   *state = (h->vgraph ? 1 : 0) | (h->igraph ? 2 : 0) | (h->sgraph ? 4 : 0) |
-           (h->sgraph && h->sgraph_inner > 0 ? 8 : 0) | (h->ograph ? 16 : 0);
+           (h->sgraph && h->sgraph_inner > 0 ? 8 : 0) | (h->ograph ? 16 : 0) | (h->dgraph ? 32 : 0);
   return TOPO_OK;
 }
 
@@ -2824,31 +2956,35 @@ static int oc_bisection_graphed(topo_handle* h, const topo_oc_opts* o, int64_t n
                         (const void*)h->coeff_df, (const void*)h->coeff_tmp, (const void*)h->adj1,
                         (const void*)L.eactive})
     key.push_back((double)(uintptr_t)p);
+  auto setup = [&](cudaGraphConditionalHandle hc) -> int {
+    k_ocl_start<<<1, 32, 0, h->stream>>>(oc, h->sc + S_TMP, hc);
+    count_launch();
+    return TOPO_OK;
+  };
+  auto body = [&](cudaGraphConditionalHandle hc) -> int {
+    launch_oc_trial(h->stream, nc, h->coeff_old, h->csens, 0.0, o->damp, o->step, o->cmin, o->cmax, h->coeff,
+                    h->coeff_df, oc + 2);
+    launch_trial_volume(h->stream, L.d, L.eactive, h->sd, h->coeff_df, h->cfg.min_density, h->partial,
+                        h->sc + S_TMP, h->adj1);
+    k_ocl_step<<<1, 32, 0, h->stream>>>(oc, h->sc + S_TMP, den, o->vgoal, hc);
+    count_launch(5);
+    return TOPO_OK;
+  };
+  auto tail = [&]() -> int {
+    if (o->apply_twice) {
+      launch_oc_trial(h->stream, nc, h->coeff, h->csens, 0.0, o->damp, o->step, o->cmin, o->cmax, h->coeff_tmp,
+                      nullptr, oc + 2);
+      CK(cudaMemcpyAsync(h->coeff, h->coeff_tmp, sizeof(double) * nc, cudaMemcpyDeviceToDevice, h->stream));
+      count_launch();
+    }
+    return TOPO_OK;
+  };
+  if (h->iter_capture) {  // inside a captured design iteration: a nested WHILE node
+    RET(capture_nested_loop(h, setup, body, &h->d_oc_body));
+    return tail();
+  }
   if (!h->ograph || key != h->okey) {
     if (h->ograph) { cudaGraphExecDestroy(h->ograph); h->ograph = nullptr; }
-    auto setup = [&](cudaGraphConditionalHandle hc) -> int {
-      k_ocl_start<<<1, 32, 0, h->stream>>>(oc, h->sc + S_TMP, hc);
-      count_launch();
-      return TOPO_OK;
-    };
-    auto body = [&](cudaGraphConditionalHandle hc) -> int {
-      launch_oc_trial(h->stream, nc, h->coeff_old, h->csens, 0.0, o->damp, o->step, o->cmin, o->cmax, h->coeff,
-                      h->coeff_df, oc + 2);
-      launch_trial_volume(h->stream, L.d, L.eactive, h->sd, h->coeff_df, h->cfg.min_density, h->partial,
-                          h->sc + S_TMP, h->adj1);
-      k_ocl_step<<<1, 32, 0, h->stream>>>(oc, h->sc + S_TMP, den, o->vgoal, hc);
-      count_launch(5);
-      return TOPO_OK;
-    };
-    auto tail = [&]() -> int {
-      if (o->apply_twice) {
-        launch_oc_trial(h->stream, nc, h->coeff, h->csens, 0.0, o->damp, o->step, o->cmin, o->cmax, h->coeff_tmp,
-                        nullptr, oc + 2);
-        CK(cudaMemcpyAsync(h->coeff, h->coeff_tmp, sizeof(double) * nc, cudaMemcpyDeviceToDevice, h->stream));
-        count_launch();
-      }
-      return TOPO_OK;
-    };
     const int rc = capture_loop_graph(h, setup, body, tail, &h->ograph, &h->ograph_fixed, &h->ograph_body);
     if (rc != TOPO_OK) {
       if (rc == TOPO_E_STATE) h->ograph_ok = false;
@@ -2882,6 +3018,11 @@ int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) 
     const int rc = oc_bisection_graphed(h, o, nc, den);
     if (rc == TOPO_OK) {
       RET(topo_coeff_to_density(h));
+      if (h->iter_capture) {  // the density sum, read after the graph ran
+        launch_sum(h->stream, h->rho, L.d.ne, h->partial, h->sc + S_DI + 1);
+        count_launch(2);
+        return TOPO_OK;
+      }
       if (stats) {
         double v = 0;
         RET(topo_volume(h, o->reference_volume, &v));
@@ -2893,7 +3034,7 @@ int topo_oc_update(topo_handle* h, const topo_oc_opts* o, topo_oc_stats* stats) 
       }
       return TOPO_OK;
     }
-    if (rc != TOPO_E_STATE) return rc;  // else the host loop below, from now on
+    if (rc != TOPO_E_STATE || h->iter_capture) return rc;  // else the host loop below, from now on
   }
   double lo = 0.0, hi = gmax, thres = 0.5 * (lo + hi), V = 0.0;
   int itn = 0, trials = 0;
@@ -3053,9 +3194,213 @@ int topo_timer_stop(topo_handle* h, double* ms) {
   return TOPO_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Whether a design iteration with these options can run as one graph: the
+// mixed solve with the Chebyshev multigrid and its device loops, on a handle
+// that has run one design iteration already (side stream for the coarsest
+// inversion, warm spectral-bound vectors, filter table of this radius).
+bool iteration_graphable(const topo_handle* h, const topo_iter_opts* o) {
+  const topo_solve_opts& so = o->solve;
+  const bool vdots = so.post >= 1 && (so.cheb_degree > 0 ? so.cheb_degree : ChebParams{}.degree) >= 1;
+  if (!(h->graphs && h->dgraph_ok && h->sgraph_ok && h->ograph_ok && !h->prof && h->nb == 1))
+    return false;
+  if (so.mode != TOPO_SOLVE_MIXED || so.smoother != TOPO_SMOOTH_CHEBYSHEV || so.learned != 0) return false;
+  if (so.inner_max > 1 && !(h->igraph_ok && vdots)) return false;
+  if (!h->side || !h->spline_set || !h->bc_set || h->lv.size() < 2) return false;
+  if (h->filt_radius != (o->filter_radius > 0 ? o->filter_radius : 2.0)) return false;
+  for (const DevLevel& L : h->lv)
+    if (!L.eig32) return false;
+  return true;
+}
+
+// Writes a design iteration's results from the slots read after its graph ran.
+int iteration_graph_results(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* st) {
+  const topo_solve_opts& so = o->solve;
+  // the coarsest inversion's status (copied to pinned memory inside the graph)
+  h->coarse_pending = false;
+  h->coarse_unchecked = false;
+  if (h->hstat[1] != 0) return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", h->hstat[1] - 1);
+  h->coarse_dropped = h->hstat[0];
+  for (size_t l = 0; l < h->lv.size(); ++l) {
+    h->lv[l].lmax32 = h->hsc[S_LAM + S_MAXLEV + l];
+    h->lv[l].lprev32 = h->hsc[S_LPREV + S_MAXLEV + l];
+  }
+  const bool inner = so.inner_max > 1;
+  const long long outer_its = (long long)h->hsc[S_OLOOP];
+  const long long inner_its = inner ? (long long)h->hsc[S_LOOP + 3] : 0;
+  const long long trials = (long long)h->hsc[S_OC + 4];
+  const long long restarts = (long long)h->hsc[S_DI + 2];
+  count_launch((int)(outer_its * h->d_outer_body + inner_its * h->d_inner_body + trials * h->d_oc_body +
+                     restarts * h->d_if_body));
+  RET(tc_wait_status(h));
+  if (inner && h->hsc[S_LOOP + 2] != 0.0)
+    return fail(h, TOPO_E_NONFINITE, "inner CG residual became non-finite at iteration %d", (int)h->hsc[S_LOOP + 2] - 1);
+  if (h->hsc[S_OLOOP + 2] != 0.0)
+    return fail(h, TOPO_E_NONFINITE, "CG residual became non-finite at iteration %d", (int)h->hsc[S_OLOOP + 2] - 1);
+  st->solve.iterations = (int)outer_its;
+  st->solve.vcycles = inner ? (int)inner_its : (int)outer_its;
+  st->solve.relres = std::sqrt(h->hsc[S_RR]) / h->iter_fn;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, h->ev_solve[0], h->ev_solve[1]);
+  st->solve.ms = ms;
+  if (!std::isfinite(st->solve.relres)) return fail(h, TOPO_E_NONFINITE, "final residual is not finite");
+  st->compliance = h->hsc[S_DI];
+  if (!std::isfinite(st->compliance)) return fail(h, TOPO_E_NONFINITE, "compliance is not finite");
+  st->oc_trials = (int)trials;
+  st->volume = h->hsc[S_DI + 1] / (double)(o->oc.reference_volume ? h->gs_padded_elements : h->active_elements);
+  if (st->solve.relres > so.rtol) {
+    fail(h, TOPO_E_NOT_CONVERGED, "relative residual %.3e above %.3e after %d iterations", st->solve.relres,
+         so.rtol, st->solve.iterations);
+    return TOPO_E_NOT_CONVERGED;
+  }
+  return TOPO_OK;
+}
+
+// A whole design iteration as one CUDA graph: operator update (coarsest
+// inversion forked to the side stream and joined before the first V-cycle),
+// spectral bounds (a conditional node per level for the restart), the mixed
+// solve (its outer CG a WHILE node with the inner CG nested in it), the final
+// residual with the element energies, compliance, sensitivity, filter, spline
+// adjoint, OC bisection (a WHILE node), density and its sum.  It is the host
+// sequence of topo_design_iteration kernel for kernel, captured once per key
+// (options, tiles, load vector) and replayed; the host reads the results once,
+// after the launch.  A failure detected afterwards restores the coefficients
+// and density the iteration started from, as the host sequence, which stops
+// before the OC update, leaves them.
+int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* st) {
+  const topo_solve_opts& so = o->solve;
+  const topo_oc_opts& oc = o->oc;
+  std::vector<double> key = {(double)so.mode, (double)so.smoother, (double)so.pre, (double)so.post, so.rtol,
+                             (double)so.max_iter, so.inner_rtol, (double)so.cheb_degree, so.cheb_lo, so.cheb_hi,
+                             (double)so.inner_max, oc.vgoal, oc.damp, oc.step, oc.cmin, oc.cmax,
+                             (double)oc.apply_twice, (double)oc.reference_volume, o->filter_radius,
+                             (double)tz32_arg(h), (double)h->tz64, (double)h->fine_df, (double)h->op_precision,
+                             (double)h->ref_fp32, (double)h->fgen, (double)h->sd.order};
+  // buffers the captured kernels address (set_bc, set_spline or a multi-RHS
+  // reservation may move some)
+  for (int a = 0; a < 3; ++a)
+    key.insert(key.end(), {(double)h->sd.nb[a], (double)(uintptr_t)h->sd.i0[a], (double)(uintptr_t)h->sd.Ndf[a]});
+  for (const void* p : {(const void*)h->coeff, (const void*)h->coeff_old, (const void*)h->csens,
+                        (const void*)h->coeff_df, (const void*)h->coeff_tmp, (const void*)h->adj1,
+                        (const void*)h->rho, (const void*)h->rhop, (const void*)h->rhop32, (const void*)h->sens,
+                        (const void*)h->sens_tmp, (const void*)h->gal_fixed, (const void*)h->A,
+                        (const void*)h->A32, (const void*)h->x, (const void*)h->f, (const void*)h->x32})
+    key.push_back((double)(uintptr_t)p);
+  for (const DevLevel& L : h->lv)
+    for (const void* p : {(const void*)L.U, (const void*)L.F, (const void*)L.R, (const void*)L.U32,
+                          (const void*)L.F32, (const void*)L.R32, (const void*)L.eig32, (const void*)L.stencil32})
+      key.push_back((double)(uintptr_t)p);
+  DevLevel& L0 = h->lv[0];
+  const int64_t n3 = 3 * L0.d.nv;
+  RET(update_penalised_if_stale(h));  // (the captured sequence starts from current rho^p, as after an OC update)
+  if (!h->dgraph || key != h->dkey) {
+    if (h->dgraph) { cudaGraphExecDestroy(h->dgraph); h->dgraph = nullptr; }
+    // ||F|| for the capture (the key holds the load vector's write count)
+    launch_dot<double>(h->stream, L0.F, L0.F, n3, h->partial, h->sc + S_FF);
+    count_launch(2);
+    RET(read_scalars(h, S_FF, 1));
+    h->iter_fn = std::sqrt(h->hsc[S_FF]);
+    if (!(h->iter_fn > 0) || !std::isfinite(h->iter_fn)) return TOPO_E_STATE;
+    for (int k = 0; k < 2; ++k)
+      if (!h->ev_solve[k]) CK(cudaEventCreate(&h->ev_solve[k]));
+    RET(ensure_cond_streams(h));
+    const long long l0 = t_launches;
+    cudaGraph_t g = nullptr;
+    int rc = TOPO_OK;
+    h->err.clear();
+    bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      h->in_capture = h->iter_capture = true;
+      h->d_outer_body = h->d_inner_body = h->d_oc_body = h->d_if_body = 0;
+      h->defer_coarse = true;
+      rc = topo_update_operators(h);
+      h->defer_coarse = false;
+      topo_solve_stats ss{};
+      h->want_energy = true;
+      if (rc == TOPO_OK) rc = topo_solve(h, &so, &ss);
+      h->want_energy = false;
+      double c = 0;
+      if (rc == TOPO_OK) rc = topo_compliance(h, &c);
+      if (rc == TOPO_OK && h->energy_ready) {
+        launch_sensitivity_from_energy(h->stream, L0.d.ne, L0.eactive, h->rho, h->cfg.power_penalty, h->sens);
+        count_launch();
+        if (h->ref_fp32) { launch_round_f32(h->stream, L0.d.ne, h->sens); count_launch(); }
+        h->energy_ready = false;
+      } else if (rc == TOPO_OK) {
+        rc = TOPO_E_STATE;
+      }
+      if (rc == TOPO_OK) rc = topo_filter(h, o->filter_radius > 0 ? o->filter_radius : 2.0);
+      if (rc == TOPO_OK) rc = topo_spline_adjoint(h);
+      topo_oc_stats ocs{};
+      if (rc == TOPO_OK) rc = topo_oc_update(h, &oc, &ocs);
+      h->in_capture = h->iter_capture = false;
+      ok = cudaStreamEndCapture(h->stream, &g) == cudaSuccess && g && rc == TOPO_OK;
+    }
+    const long long total = t_launches - l0;
+    g_launches.fetch_sub(total);
+    t_launches = l0;
+    if (ok) ok = cudaGraphInstantiate(&h->dgraph, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {  // the host sequence from now on
+      const cudaError_t ce = cudaGetLastError();
+      const std::string why = h->err;
+      fail(h, TOPO_E_STATE, "design iteration not captured as a graph (status %d, %s; %s): host sequence", rc,
+           cudaGetErrorString(ce), why.c_str());
+      h->dgraph = nullptr;
+      h->dgraph_ok = false;
+      // (the capture set host state as if it had run: operators and bounds stale again)
+      h->ops_ready = false;
+      h->rhop_stale = true;
+      h->coarse_pending = h->coarse_unchecked = false;
+      for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
+      return TOPO_E_STATE;
+    }
+    h->dgraph_fixed = total - (h->d_outer_body + h->d_inner_body + h->d_oc_body) -
+                      (long long)h->lv.size() * h->d_if_body;
+    h->dkey = key;
+  }
+  ScopedEvent e0, e1;
+  CK(e0.create());
+  CK(e1.create());
+  CK(cudaEventRecord(e0, h->stream));
+  CK(cudaGraphLaunch(h->dgraph, h->stream));
+  count_launch((int)h->dgraph_fixed);
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaMemcpyAsync(h->hsc, h->sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaEventSynchronize(e1));
+  CK(cudaStreamSynchronize(h->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  st->ms = ms;
+  const int rc = iteration_graph_results(h, o, st);
+  if (rc != TOPO_OK && rc != TOPO_E_NOT_CONVERGED) {
+    // the graph ran the OC update on a failed solve: back to the start design
+    const int64_t nc = (int64_t)h->sd.nb[0] * h->sd.nb[1] * h->sd.nb[2];
+    CK(cudaMemcpyAsync(h->coeff, h->coeff_old, sizeof(double) * nc, cudaMemcpyDeviceToDevice, h->stream));
+    RET(topo_coeff_to_density(h));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
 int topo_design_iteration(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* stats) {
   DEVICE_SCOPE(h);
   if (!h || !o) return TOPO_E_BAD_INPUT;
+  if (iteration_graphable(h, o)) {
+    topo_iter_stats st{};
+    const int rc = design_iteration_graphed(h, o, &st);
+    if (rc != TOPO_E_STATE) {
+      if (stats) *stats = st;
+      return rc;
+    }
+  }
   ScopedEvent e0, e1;
   CK(e0.create());
   CK(e1.create());

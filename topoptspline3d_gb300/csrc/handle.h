@@ -11,6 +11,10 @@
 
 namespace topo {
 
+// Nesting depth of conditional graph nodes in a captured design iteration
+// (outer CG > inner CG > V-cycle; power-iteration restarts; OC bisection).
+constexpr int TOPO_COND_DEPTH = 3;
+
 // Scalar slots in device memory used by the PCG drivers.
 // Slots 0-7 belong to one CG level; a nested CG uses base 8 (slots 8-15).
 enum Slot {
@@ -25,7 +29,13 @@ enum Slot {
   S_OC = S_LOOP + 4,
   // device-controlled outer CG loop of the mixed solve (the same four slots
   // as S_LOOP)
-  S_OLOOP = S_OC + 6, S_COUNT = S_OLOOP + 4
+  S_OLOOP = S_OC + 6,
+  // spectral bounds per precision table (FP64 first) and level: the current
+  // estimate of lambda_max(D^-1 A) and the previous one (warm-start guard)
+  S_LAM = S_OLOOP + 4, S_LPREV = S_LAM + 2 * S_MAXLEV,
+  // results of a graphed design iteration: compliance F.U, the density sum
+  // after the OC update, levels whose power iteration restarted
+  S_DI = S_LPREV + 2 * S_MAXLEV, S_COUNT = S_DI + 3
 };
 
 // Chebyshev step coefficients (c_old, c_new) in device memory: per precision
@@ -68,6 +78,21 @@ struct topo_handle {
   cudaGraphExec_t sgraph = nullptr;
   std::vector<double> skey;
   long long sgraph_fixed = 0, sgraph_body = 0, sgraph_inner = 0;
+  // a whole design iteration as one graph (dgraph, topo_design_iteration),
+  // captured with iter_capture set: the functions it calls then leave their
+  // results in device slots and emit their loops as conditional nodes.
+  // Kernels of its fixed part and of one pass of each conditional body.
+  bool iter_capture = false;
+  // helper streams that capture the bodies of nested conditional nodes
+  cudaStream_t cstream[topo::TOPO_COND_DEPTH] = {};
+  int cdepth = 0;
+  bool dgraph_ok = true;
+  cudaGraphExec_t dgraph = nullptr;
+  std::vector<double> dkey;
+  long long dgraph_fixed = 0, d_outer_body = 0, d_inner_body = 0, d_oc_body = 0, d_if_body = 0;
+  double iter_fn = 0;                 // ||F|| when the design-iteration graph was captured
+  unsigned long long fgen = 0;        // writes of the level-0 load vector (topo_set_bc, topo_put_array)
+  cudaEvent_t ev_solve[2] = {nullptr, nullptr};  // recorded inside it around the solve
   // OC bisection as one graph with a device-side WHILE loop (ograph)
   bool ograph_ok = true;
   cudaGraphExec_t ograph = nullptr;
@@ -157,7 +182,6 @@ struct topo_handle {
   double* vdot_out = nullptr;
   bool inner_fr = false;  // inner CG in Fletcher-Reeves form (z.rold taken as 0)
   double* chebc = nullptr;          // Chebyshev coefficient table (device)
-  std::vector<double> chebc_host;   // its last uploaded contents
   double* sc = nullptr;    // device scalar slots
   double* hsc = nullptr;   // pinned host mirror
   int64_t active_elements = 0, gs_padded_elements = 0;

@@ -283,6 +283,15 @@ int topo_checkpoint_load(topo_handle* h, const char* path, void* user, size_t us
         return io_fail(h, TOPO_E_CUDA, "checkpoint: upload");
     }
   }
+  // the previous estimates also in the device slots the restart test reads
+  std::vector<double> lp(2 * S_MAXLEV, 0.0);
+  for (int l = 0; l < nl && l < S_MAXLEV; ++l) {
+    lp[l] = h->lv[l].lprev;
+    lp[S_MAXLEV + l] = h->lv[l].lprev32;
+  }
+  if (cudaMemcpyAsync(h->sc + S_LPREV, lp.data(), sizeof(double) * lp.size(), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return io_fail(h, TOPO_E_CUDA, "checkpoint: upload");
   if (cudaStreamSynchronize(s) != cudaSuccess) return io_fail(h, TOPO_E_CUDA, "checkpoint: upload");
   h->tz32 = tiles[0] & ~TOPO_FINE_FLAGS;
   h->fine_tc = (tiles[0] & TOPO_FINE_TC_FLAG) != 0;

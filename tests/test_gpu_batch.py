@@ -1,5 +1,6 @@
 """Many independent designs of uneven sizes at once (topo_design_batch): the
-concurrent run reproduces, bit for bit, each design run on its own."""
+concurrent run (a host thread per design, each design iteration one graph
+launch after the first) reproduces, bit for bit, each design run on its own."""
 import numpy as np
 import pytest
 
@@ -27,6 +28,8 @@ def test_batch_equals_sequential():
     batch = [_make(w) for w in wls]
     last, bs = capi.design_batch(batch, 3, threads=6, solve=SOLVE, ocs=ocs)
     assert bs["failures"] == 0 and bs["wall_ms"] > 0
+    # after each design's first iteration (host sequence) its iterations ran as one graph each
+    assert all(q.graph_state()["iteration"] for q in batch)
     for k, w in enumerate(wls):
         p = _make(w)
         for _ in range(3):

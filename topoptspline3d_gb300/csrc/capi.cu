@@ -1334,8 +1334,10 @@ void topo_destroy(topo_handle* h) {
   if (h->dgraph) cudaGraphExecDestroy(h->dgraph);
   for (int k = 0; k < TOPO_COND_DEPTH; ++k)
     if (h->cstream[k]) cudaStreamDestroy(h->cstream[k]);
-  for (int k = 0; k < 2; ++k)
+  for (int k = 0; k < 2; ++k) {
     if (h->ev_solve[k]) cudaEventDestroy(h->ev_solve[k]);
+    if (h->ev_iter[k]) cudaEventDestroy(h->ev_iter[k]);
+  }
   prof_drop_graph_events(h);
   if (h->multi) {
     for (void* p : h->multi->allocs) cudaFree(p);
@@ -1843,7 +1845,9 @@ int topo_vcycle(topo_handle* h, int pre, int post, double* relres) {
 // The main stream waits for a coarsest inversion running on the side stream.
 static int coarse_join(topo_handle* h) {
   if (!h->coarse_pending) return TOPO_OK;
-  CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, 0));
+  // (in a captured design iteration the inversion is launched before the
+  // graph, so the graph holds a wait on the event's record at launch time)
+  CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, h->iter_capture ? cudaEventWaitExternal : 0));
   h->coarse_pending = false;
   return TOPO_OK;
 }
@@ -2302,15 +2306,16 @@ int topo_set_tiles(topo_handle* h, int tz32, int tz64) {
 int topo_set_graphs(topo_handle* h, int enable) {
   DEVICE_SCOPE(h);
   if (!h) return TOPO_E_BAD_INPUT;
-  if (enable < 0 || enable > 2) return TOPO_E_BAD_INPUT;
+  if (enable < 0 || enable > 3) return TOPO_E_BAD_INPUT;
   h->graphs = enable != 0;
   if (h->vgraph) { cudaGraphExecDestroy(h->vgraph); h->vgraph = nullptr; }
   if (h->igraph) { cudaGraphExecDestroy(h->igraph); h->igraph = nullptr; }
   if (h->ograph) { cudaGraphExecDestroy(h->ograph); h->ograph = nullptr; }
   if (h->sgraph) { cudaGraphExecDestroy(h->sgraph); h->sgraph = nullptr; }
   if (h->dgraph) { cudaGraphExecDestroy(h->dgraph); h->dgraph = nullptr; }
-  h->igraph_ok = h->ograph_ok = h->dgraph_ok = true;
+  h->igraph_ok = h->ograph_ok = true;
   h->sgraph_ok = enable != 2;
+  h->dgraph_ok = enable == 1;
   return TOPO_OK;
 }
 
@@ -3259,18 +3264,19 @@ int iteration_graph_results(topo_handle* h, const topo_iter_opts* o, topo_iter_s
   return TOPO_OK;
 }
 
-// A whole design iteration as one CUDA graph: operator update (coarsest
-// inversion forked to the side stream and joined before the first V-cycle),
-// spectral bounds (a conditional node per level for the restart), the mixed
+// A design iteration as one CUDA graph after the operator update (whose
+// coarsest inversion on the side stream the graph waits for before the first
+// V-cycle): spectral bounds (a conditional node per level for the restart), the mixed
 // solve (its outer CG a WHILE node with the inner CG nested in it), the final
 // residual with the element energies, compliance, sensitivity, filter, spline
 // adjoint, OC bisection (a WHILE node), density and its sum.  It is the host
 // sequence of topo_design_iteration kernel for kernel, captured once per key
 // (options, tiles, load vector) and replayed; the host reads the results once,
-// after the launch.  A failure detected afterwards restores the coefficients
-// and density the iteration started from, as the host sequence, which stops
-// before the OC update, leaves them.
-int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* st) {
+// after the launch (iteration_graph_finish).  A failure detected afterwards
+// restores the coefficients and density the iteration started from, as the
+// host sequence, which stops before the OC update, leaves them.  This part
+// captures the graph when its key changed and launches it without waiting.
+int iteration_graph_launch(topo_handle* h, const topo_iter_opts* o) {
   const topo_solve_opts& so = o->solve;
   const topo_oc_opts& oc = o->oc;
   std::vector<double> key = {(double)so.mode, (double)so.smoother, (double)so.pre, (double)so.post, so.rtol,
@@ -3295,7 +3301,18 @@ int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_
       key.push_back((double)(uintptr_t)p);
   DevLevel& L0 = h->lv[0];
   const int64_t n3 = 3 * L0.d.nv;
-  RET(update_penalised_if_stale(h));  // (the captured sequence starts from current rho^p, as after an OC update)
+  // The operator update runs before the graph: its coarsest inversion is a
+  // cooperative kernel on the side stream, which ran at half speed as a node
+  // of the graph (20 against 9.5 ms at n = 1617); the graph waits for its
+  // event before the first V-cycle, so it still overlaps the spectral bounds
+  // and the first residual.
+  for (int k = 0; k < 2; ++k)
+    if (!h->ev_iter[k]) CK(cudaEventCreate(&h->ev_iter[k]));
+  CK(cudaEventRecord(h->ev_iter[0], h->stream));
+  h->defer_coarse = true;
+  const int urc = topo_update_operators(h);
+  h->defer_coarse = false;
+  RET(urc);
   if (!h->dgraph || key != h->dkey) {
     if (h->dgraph) { cudaGraphExecDestroy(h->dgraph); h->dgraph = nullptr; }
     // ||F|| for the capture (the key holds the load vector's write count)
@@ -3315,12 +3332,9 @@ int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_
     if (ok) {
       h->in_capture = h->iter_capture = true;
       h->d_outer_body = h->d_inner_body = h->d_oc_body = h->d_if_body = 0;
-      h->defer_coarse = true;
-      rc = topo_update_operators(h);
-      h->defer_coarse = false;
       topo_solve_stats ss{};
       h->want_energy = true;
-      if (rc == TOPO_OK) rc = topo_solve(h, &so, &ss);
+      rc = topo_solve(h, &so, &ss);
       h->want_energy = false;
       double c = 0;
       if (rc == TOPO_OK) rc = topo_compliance(h, &c);
@@ -3351,10 +3365,10 @@ int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_
            cudaGetErrorString(ce), why.c_str());
       h->dgraph = nullptr;
       h->dgraph_ok = false;
-      // (the capture set host state as if it had run: operators and bounds stale again)
-      h->ops_ready = false;
-      h->rhop_stale = true;
-      h->coarse_pending = h->coarse_unchecked = false;
+      // (the capture set host state as if it had run: the operator update
+      // launched above stands, its inversion not yet joined; bounds stale)
+      h->ops_ready = true;
+      h->coarse_pending = h->coarse_unchecked = true;
       for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
       return TOPO_E_STATE;
     }
@@ -3362,18 +3376,19 @@ int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_
                       (long long)h->lv.size() * h->d_if_body;
     h->dkey = key;
   }
-  ScopedEvent e0, e1;
-  CK(e0.create());
-  CK(e1.create());
-  CK(cudaEventRecord(e0, h->stream));
   CK(cudaGraphLaunch(h->dgraph, h->stream));
   count_launch((int)h->dgraph_fixed);
-  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventRecord(h->ev_iter[1], h->stream));
   CK(cudaMemcpyAsync(h->hsc, h->sc, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaEventSynchronize(e1));
+  return TOPO_OK;
+}
+
+// Waits for a design iteration launched by iteration_graph_launch and writes
+// its results.
+int iteration_graph_finish(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* st) {
   CK(cudaStreamSynchronize(h->stream));
   float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventElapsedTime(&ms, h->ev_iter[0], h->ev_iter[1]);
   st->ms = ms;
   const int rc = iteration_graph_results(h, o, st);
   if (rc != TOPO_OK && rc != TOPO_E_NOT_CONVERGED) {
@@ -3384,6 +3399,11 @@ int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_
     CK(cudaStreamSynchronize(h->stream));
   }
   return rc;
+}
+
+int design_iteration_graphed(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* st) {
+  RET(iteration_graph_launch(h, o));
+  return iteration_graph_finish(h, o, st);
 }
 
 }  // namespace

@@ -93,6 +93,7 @@ struct topo_handle {
   double iter_fn = 0;                 // ||F|| when the design-iteration graph was captured
   unsigned long long fgen = 0;        // writes of the level-0 load vector (topo_set_bc, topo_put_array)
   cudaEvent_t ev_solve[2] = {nullptr, nullptr};  // recorded inside it around the solve
+  cudaEvent_t ev_iter[2] = {nullptr, nullptr};   // around its launch
   // OC bisection as one graph with a device-side WHILE loop (ograph)
   bool ograph_ok = true;
   cudaGraphExec_t ograph = nullptr;

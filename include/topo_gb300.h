@@ -267,14 +267,15 @@ int topo_set_fine_tile_rows(topo_handle* h, int rows);
  * device-side loop), so the host waits once per solve; the inner CG alone
  * where the outer loop runs on the host; the OC bisection; a whole design
  * iteration of topo_design_iteration with the mixed solve and the Chebyshev
- * multigrid, from its second iteration on a handle (operator update, spectral
- * bounds, solve, compliance, sensitivity, filter, adjoint, OC update as one
- * launch; its loops decided on the device; the results read once after it;
- * the load vector must then change through topo_set_bc or topo_put_array, not
- * through a device pointer).  1 = on (default),
- * 2 = on but the outer solve loop on the host, 0 = direct launches and host
- * loops (the same kernels in the same order: the same results bit for bit).
- * Graphs are not used while topo_profile_enable is on. */
+ * multigrid, from its second iteration on a handle (after the operator update,
+ * whose coarsest inversion it waits for: spectral bounds, solve, compliance,
+ * sensitivity, filter, adjoint, OC update as one launch; its loops decided on
+ * the device; the results read once after it; the load vector must then
+ * change through topo_set_bc or topo_put_array, not through a device pointer).
+ * 1 = on (default), 2 = on but the outer solve loop on the host, 3 = on but no
+ * whole-iteration graph, 0 = direct launches and host loops (the same kernels
+ * in the same order: the same results bit for bit).  Graphs are not used while
+ * topo_profile_enable is on. */
 int topo_set_graphs(topo_handle* h, int enable);
 /* Which graphs the handle holds now (bits): 1 FP32 V-cycle, 2 inner CG on its
  * own, 4 outer solve loop, 8 inner CG nested in the outer loop's graph, 16 OC

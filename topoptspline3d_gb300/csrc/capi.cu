@@ -38,9 +38,15 @@ using namespace topo;
 #endif
 
 // CTAs per SM of the coarsest inversion when it runs on the side stream next
-// to the solve's set-up kernels
+// to the solve's set-up kernels: one up to TOPO_GJ_SIDE_LARGE_N unknowns
+// (256x128x128: n = 675, where the set-up kernels need the SMs as much as the
+// inversion), two above, where the inversion outlasts the set-up by far
+// (n = 1617: about 6 against 1 ms)
 #ifndef TOPO_GJ_SIDE_PER_SM
 #define TOPO_GJ_SIDE_PER_SM 1
+#endif
+#ifndef TOPO_GJ_SIDE_LARGE_N
+#define TOPO_GJ_SIDE_LARGE_N 1000
 #endif
 
 #include "handle.h"
@@ -1272,7 +1278,7 @@ int topo_create(const topo_config* cfg, const uint8_t* eactive, topo_handle** ou
     else {
       A(dalloc(hp, &h->A, (int64_t)h->ndense * h->ndense));
       A(dalloc(hp, &h->A32, (int64_t)h->ndense * h->ndense));
-      A(dalloc(hp, &h->gjwork, 64 * (int64_t)h->ndense + 32 * 32));
+      A(dalloc(hp, &h->gjwork, 128 * (int64_t)h->ndense + 32 * 32));  // block, panels in FP64 and split
       A(dalloc(hp, &h->coarse64tmp, 243 * dl.nv));
     }
     std::vector<double> T;
@@ -1694,7 +1700,8 @@ int topo_update_operators(topo_handle* h) {
       }
       CK(cudaEventRecord(h->ev_ops, h->stream));
       CK(cudaStreamWaitEvent(h->side, h->ev_ops, 0));
-      const int e = coarsest_invert(h->side, h->ndense, h->A, h->gjwork, h->status, !b64, TOPO_GJ_SIDE_PER_SM);
+      const int e = coarsest_invert(h->side, h->ndense, h->A, h->gjwork, h->status, !b64,
+                                    h->ndense > TOPO_GJ_SIDE_LARGE_N ? 2 : TOPO_GJ_SIDE_PER_SM);
       count_launch();
       if (e != (int)cudaSuccess)
         return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));

@@ -906,9 +906,15 @@ constexpr int GJB = 32;
 //
 // DFC: the rank-GJB updates of phase C (n^3 of the n^3 + O(n^2 GJB) work) run
 // in double-float arithmetic on the FP32 pipe (58x the FP64 rate on GB300),
-// with the panels split into (hi, lo) floats as a tile is staged; the panel
+// with the panels split into (hi, lo) floats once per panel; the panel
 // factorisation stays FP64, where its serial latency matters more than its
-// rate.  Used when the coarsest matrix comes from FP32 stencils.
+// rate.  Used when the coarsest matrix comes from FP32 stencils.  (Measured
+// at n = 1617, 304 CTAs: splitting the panels as each tile is staged kept the
+// FP64 pipe 55% busy with conversions, 6.6 ms against 5.2 ms; also holding the
+// matrix split in place for the whole inversion took the FP64 pipe to 18% but
+// ran 5.4 ms, and the update on packed two-lane FP32 instructions cut the
+// instructions by a quarter but ran 5.6 ms: the panel barriers and the serial
+// panel work then set the pace.)
 template <bool DFC>
 __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ A, double* __restrict__ work,
                                                     int* __restrict__ status) {
@@ -920,6 +926,8 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
   __shared__ double sp[GJB][GJB + 1];
   double* P = work + GJB * GJB;      // [GJB][n]
   double* Cp = P + (int64_t)GJB * n; // [n][GJB]
+  df* Pdf = reinterpret_cast<df*>(Cp + (int64_t)GJB * n);  // P split, [GJB][n]
+  df* Cdf = Pdf + (int64_t)GJB * n;                          // Cp split, [n][GJB]
   const int tid = threadIdx.x;
   double dmax = 0.0;
   for (int k = 0; k < n; ++k) dmax = fmax(dmax, fabs(A[(int64_t)k * n + k]));
@@ -992,10 +1000,13 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
         for (int m = 0; m < kb; ++m) v += sd[r][m] * A[(int64_t)(k0 + m) * n + c];
       }
       P[(int64_t)r * n + c] = v;
+      if constexpr (DFC) Pdf[(int64_t)r * n + c] = df_from(v);
     }
     for (int64_t e = gt; e < (int64_t)n * kb; e += gs) {
       const int i = (int)(e / kb), m = (int)(e % kb);
-      Cp[(int64_t)i * GJB + m] = (i < k0 || i >= k0 + kb) ? A[(int64_t)i * n + k0 + m] : 0.0;
+      const double v = (i < k0 || i >= k0 + kb) ? A[(int64_t)i * n + k0 + m] : 0.0;
+      Cp[(int64_t)i * GJB + m] = v;
+      if constexpr (DFC) Cdf[(int64_t)i * GJB + m] = df_from(v);
     }
     grid.sync();
     // ---- C: rank-kb update, GJB x GJB tiles of A.  With a next panel, CTA 0
@@ -1010,17 +1021,64 @@ __global__ void __launch_bounds__(256) k_gj_blocked(int n, double* __restrict__ 
       const int t = (ahead && blockIdx.x != 0 && t0 >= tn) ? t0 + 1 : t0;
       if (t >= nblk_tiles * nblk_tiles) break;
       const int ti = (t / nblk_tiles) * GJB, tc = (t % nblk_tiles) * GJB;
+      // a tile outside the panel's rows and columns: every element gets the update
+      const bool band = (ti < k0 + kb && ti + GJB > k0) || (tc < k0 + kb && tc + GJB > k0);
       __syncthreads();
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
-        sc[r][c] = (ti + r < n && c < kb) ? Cp[(int64_t)(ti + r) * GJB + c] : 0.0;
-        sp[r][c] = (r < kb && tc + c < n) ? P[(int64_t)r * n + tc + c] : 0.0;
+        const bool inc = ti + r < n && c < kb, inp = r < kb && tc + c < n;
+        if (!DFC || band) {
+          sc[r][c] = inc ? Cp[(int64_t)(ti + r) * GJB + c] : 0.0;
+          sp[r][c] = inp ? P[(int64_t)r * n + tc + c] : 0.0;
+        }
         if constexpr (DFC) {
-          scd[r][c] = df_from(sc[r][c]);
-          spd[r][c] = df_from(sp[r][c]);
+          scd[r][c] = inc ? Cdf[(int64_t)(ti + r) * GJB + c] : df(0.f, 0.f);
+          spd[r][c] = inp ? Pdf[(int64_t)r * n + tc + c] : df(0.f, 0.f);
         }
       }
       __syncthreads();
+      if (!band && blockDim.x == 8 * GJB) {
+        // four rows of one column per thread: four independent chains share
+        // each panel value (per element the operations and order of the loop
+        // below)
+        const int c = tid % GJB, r0 = tid / GJB, col = tc + c;
+        double* a[4];
+        bool in[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = ti + r0 + 8 * q;
+          in[q] = i < n && col < n;
+          a[q] = A + (int64_t)(in[q] ? i : 0) * n + (in[q] ? col : 0);
+        }
+        if constexpr (DFC) {
+          df v[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = df_from(in[q] ? *a[q] : 0.0);
+#pragma unroll 4
+          for (int m = 0; m < kb; ++m) {
+            const df pm = spd[m][c];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = v[q] - scd[r0 + 8 * q][m] * pm;
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (in[q]) *a[q] = df_to(v[q]);
+        } else {
+          double v[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = in[q] ? *a[q] : 0.0;
+#pragma unroll 4
+          for (int m = 0; m < kb; ++m) {
+            const double pm = sp[m][c];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] -= sc[r0 + 8 * q][m] * pm;
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (in[q]) *a[q] = v[q];
+        }
+        continue;
+      }
       for (int e = tid; e < GJB * GJB; e += blockDim.x) {
         const int r = e / GJB, c = e % GJB;
         const int i = ti + r, col = tc + c;

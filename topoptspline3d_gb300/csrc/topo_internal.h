@@ -227,7 +227,7 @@ template <typename T>
 void launch_assemble_stencil_t(cudaStream_t s, const LevelDims& d, const uint8_t* eactive,
                                const uint8_t* vmask, const T* kel, T* st);
 void launch_dense_from_stencil(cudaStream_t s, const LevelDims& d, const double* st, double* A);
-// work: the blocked kernel's panels (GJB*GJB + 2*GJB*n doubles; null selects
+// work: the blocked kernel's panels (GJB*GJB + 4*GJB*n doubles; null selects
 // the unblocked kernel); df_update: rank-GJB updates in double-float arithmetic.
 // max_per_sm caps the blocked form's CTAs per SM (it runs beside other work
 // on a second stream with 1).

@@ -68,6 +68,9 @@ def parse():
                          "chose)")
     ap.add_argument("--profile-solve-steps", type=int, default=0,
                     help="with --profile-iteration: stop the solve after this many outer CG steps")
+    ap.add_argument("--coarse-every", type=int, default=1,
+                    help="recompute the coarsest dense inverse at every K-th operator update only "
+                         "(topo_set_coarse_refresh; 1, the default, is each update as in the reference)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every kernel on its own (no CUDA graphs); with --profile-iteration this lists the "
                          "kernels the device-side loops run inside graphs")
@@ -564,6 +567,7 @@ def run_designs(args, rank):
             q.put("coeff", np.full(q.num_coeffs(), w.coeff0))
             q.coeff_to_density()
             q.set_operator_precision(2)
+            q.set_coarse_refresh(args.coarse_every)
             ps.append(q)
         return ps
 
@@ -584,7 +588,8 @@ def run_designs(args, rank):
            "warmup": args.warmup, "ms_per_step": conc["wall_ms"] / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 multigrid / f64 CG", "data": "synthetic",
            "config": {"workload": "32 cantilevers, sizes and volume fractions from default_rng(2000 + d)",
-                      "designs": [w.name for w in wls], "threads": len(ps), "autotuned_tz32": tz},
+                      "designs": [w.name for w in wls], "threads": len(ps), "autotuned_tz32": tz,
+                      "coarse_refresh_every": args.coarse_every},
            "sequential_design_iter_per_s": units / (seq["wall_ms"] / 1e3),
            "speedup_vs_sequential": seq["wall_ms"] / conc["wall_ms"]}
     if rank == 0:
@@ -619,6 +624,7 @@ def main():
     oc = dict(vgoal=wl.vgoal, damp=0.5, step=0.03, cmin=0.0, cmax=1.0)
     if args.no_graphs:
         p.set_graphs(0)
+    p.set_coarse_refresh(args.coarse_every)
     if args.schedule:
         sched = args.schedule.split(",")
         inner, pre, deg, tz32, tz64 = (int(v) for v in sched[:5])
@@ -817,6 +823,7 @@ def main():
                       "inner_cap_retune_every": args.retune_every,
                       "inner_caps_used": sorted(set(o["inner_max"] for o in tuner.used)),
                       "l2": "working set (>2 GB) larger than L2; no flush",
+                      "coarse_refresh_every": args.coarse_every,
                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
            "cg_iterations": [s["iterations"] for s in stats], "relres": max(s["relres"] for s in stats),
            "oc_trials": [s["oc_trials"] for s in stats], "compliance": [s["compliance"] for s in stats],

@@ -277,6 +277,15 @@ int topo_set_fine_tile_rows(topo_handle* h, int rows);
  * in the same order: the same results bit for bit).  Graphs are not used while
  * topo_profile_enable is on. */
 int topo_set_graphs(topo_handle* h, int enable);
+/* Recompute the coarsest level's dense inverse at every `every`-th operator
+ * update only (1, the default, is every update, as the reference does); in
+ * between, the coarse levels are current and the coarsest solve applies the
+ * inverse of the last refresh.  The mixed solve's flexible CG takes the
+ * slightly older coarse solve; it still converges to the requested residual.
+ * Boundary conditions, operator precision and a checkpoint load force a
+ * refresh at the next update (a resumed run therefore equals an uninterrupted
+ * one bit for bit only from a refresh on). */
+int topo_set_coarse_refresh(topo_handle* h, int every);
 /* Which graphs the handle holds now (bits): 1 FP32 V-cycle, 2 inner CG on its
  * own, 4 outer solve loop, 8 inner CG nested in the outer loop's graph, 16 OC
  * bisection, 32 a whole design iteration (topo_design_iteration).  A form whose

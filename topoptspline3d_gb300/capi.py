@@ -48,7 +48,7 @@ EXPORTED = [
     "topo_unet_enable", "topo_unet_set_conv_kernel", "topo_unet_num_params", "topo_unet_get_params", "topo_unet_set_params", "topo_unet_forward",
     "topo_unet_loss_grad", "topo_unet_dataset_reserve", "topo_unet_dataset_size", "topo_unet_train",
     "topo_unet_dataset_get", "topo_multi_reserve", "topo_solve_multi", "topo_set_fine_arithmetic", "topo_set_fine_tensor_cores", "topo_apply_level", "topo_set_fine_tile_rows",
-    "topo_autotune", "topo_set_graphs", "topo_graph_state", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
+    "topo_autotune", "topo_set_graphs", "topo_graph_state", "topo_set_coarse_refresh", "topo_design_batch", "topo_set_tiles", "topo_profiler_range",
     "topo_set_load_region", "topo_worst_compliance", "topo_bitmask_to_eactive", "topo_eactive_to_bitmask",
     "topo_create_bitmask", "topo_write_array", "topo_read_array", "topo_write_active_records",
     "topo_checkpoint_save", "topo_checkpoint_load", "topo_mma_checkpoint_save", "topo_mma_checkpoint_load",
@@ -222,6 +222,7 @@ def load(build: bool = True):
         "topo_set_fine_tile_rows": (i, [vp, i]),
         "topo_set_graphs": (i, [vp, i]),
         "topo_graph_state": (i, [vp, ip]),
+        "topo_set_coarse_refresh": (i, [vp, i]),
         "topo_set_tiles": (i, [vp, i, i]),
         "topo_profiler_range": (i, [i]),
         "topo_design_batch": (i, [C.POINTER(vp), i, C.POINTER(IterOpts), i, i, i, C.POINTER(IterStats),
@@ -556,6 +557,10 @@ class Problem:
 
     def set_graphs(self, enable):
         self._ck(self.lib.topo_set_graphs(self.h, int(enable)))
+
+    def set_coarse_refresh(self, every):
+        """Recompute the coarsest inverse at every `every`-th operator update (1: each)."""
+        self._ck(self.lib.topo_set_coarse_refresh(self.h, int(every)))
 
     def graph_state(self):
         """The graphs the handle holds: {"vcycle", "inner", "solve", "nested_inner", "oc",

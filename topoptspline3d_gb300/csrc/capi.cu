@@ -1467,6 +1467,7 @@ int topo_set_bc(topo_handle* h, const uint8_t* fixed, const double* loads) {
   CK(cudaStreamSynchronize(h->stream));
   h->bc_set = true;
   h->ops_ready = false;
+  h->coarse_valid = false;
   for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
   return TOPO_OK;
 }
@@ -1642,6 +1643,7 @@ int topo_set_reference_precision(topo_handle* h, int enable) {
   h->ref_fp32 = enable != 0;
   h->rhop_stale = true;
   h->ops_ready = false;
+  h->coarse_valid = false;
   return TOPO_OK;
 }
 
@@ -1650,6 +1652,7 @@ int topo_set_operator_precision(topo_handle* h, int mask) {
   if (!h || mask < 1 || mask > 3) return TOPO_E_BAD_INPUT;
   h->op_precision = mask;
   h->ops_ready = false;
+  h->coarse_valid = false;
   return TOPO_OK;
 }
 
@@ -1677,7 +1680,12 @@ int topo_update_operators(topo_handle* h) {
     count_launch((b64 ? 1 : 0) + (b32 ? 1 : 0));
     CKL();
   }
-  if (nl > 1) {
+  // a lagged coarsest inverse (topo_set_coarse_refresh): the coarse levels
+  // are current, the coarsest solve keeps the inverse of an earlier update
+  const bool keep_inverse = nl > 1 && h->coarse_valid && h->coarse_every > 1 && ++h->coarse_age < h->coarse_every;
+  if (nl > 1 && !keep_inverse) {
+    h->coarse_age = 0;
+    h->coarse_valid = true;
     DevLevel& Lc = h->lv.back();
     const double* st = Lc.stencil;
     if (!b64) {  // FP64 copy of the FP32 coarsest stencil
@@ -1723,7 +1731,10 @@ int topo_update_operators(topo_handle* h) {
     int hstat[2] = {0, 0};
     CK(cudaMemcpyAsync(hstat, h->status, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    if (hstat[1] != 0) return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", hstat[1] - 1);
+    if (hstat[1] != 0) {
+      h->coarse_valid = false;
+      return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", hstat[1] - 1);
+    }
     h->coarse_dropped = hstat[0];
     launch_to_float(h->stream, h->A, h->A32, (int64_t)h->ndense * h->ndense);
     count_launch();
@@ -1851,10 +1862,19 @@ int topo_vcycle(topo_handle* h, int pre, int post, double* relres) {
 
 // The main stream waits for a coarsest inversion running on the side stream.
 static int coarse_join(topo_handle* h) {
-  if (!h->coarse_pending) return TOPO_OK;
   // (in a captured design iteration the inversion is launched before the
-  // graph, so the graph holds a wait on the event's record at launch time)
-  CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, h->iter_capture ? cudaEventWaitExternal : 0));
+  // graph, so the graph holds one wait on the event's record at launch time,
+  // also when the capture's own update kept a lagged inverse: replays may
+  // refresh it)
+  if (h->iter_capture) {
+    if (h->iter_waited) return TOPO_OK;
+    h->iter_waited = true;
+    h->coarse_pending = false;
+    CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, cudaEventWaitExternal));
+    return TOPO_OK;
+  }
+  if (!h->coarse_pending) return TOPO_OK;
+  CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, 0));
   h->coarse_pending = false;
   return TOPO_OK;
 }
@@ -1865,7 +1885,10 @@ static int coarse_finish(topo_handle* h) {
   if (!h->coarse_unchecked || h->iter_capture) return TOPO_OK;  // (a captured iteration reads it afterwards)
   CK(cudaEventSynchronize(h->ev_coarse));
   h->coarse_unchecked = false;
-  if (h->hstat[1] != 0) return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", h->hstat[1] - 1);
+  if (h->hstat[1] != 0) {
+    h->coarse_valid = false;
+    return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", h->hstat[1] - 1);
+  }
   h->coarse_dropped = h->hstat[0];
   return TOPO_OK;
 }
@@ -2323,6 +2346,14 @@ int topo_set_graphs(topo_handle* h, int enable) {
   h->igraph_ok = h->ograph_ok = true;
   h->sgraph_ok = enable != 2;
   h->dgraph_ok = enable == 1;
+  return TOPO_OK;
+}
+
+int topo_set_coarse_refresh(topo_handle* h, int every) {
+  DEVICE_SCOPE(h);
+  if (!h || every < 1) return TOPO_E_BAD_INPUT;
+  h->coarse_every = every;
+  h->coarse_age = 0;
   return TOPO_OK;
 }
 
@@ -3232,9 +3263,13 @@ bool iteration_graphable(const topo_handle* h, const topo_iter_opts* o) {
 int iteration_graph_results(topo_handle* h, const topo_iter_opts* o, topo_iter_stats* st) {
   const topo_solve_opts& so = o->solve;
   // the coarsest inversion's status (copied to pinned memory inside the graph)
+  const bool checked = h->coarse_unchecked;
   h->coarse_pending = false;
   h->coarse_unchecked = false;
-  if (h->hstat[1] != 0) return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", h->hstat[1] - 1);
+  if (checked && h->hstat[1] != 0) {
+    h->coarse_valid = false;
+    return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", h->hstat[1] - 1);
+  }
   h->coarse_dropped = h->hstat[0];
   for (size_t l = 0; l < h->lv.size(); ++l) {
     h->lv[l].lmax32 = h->hsc[S_LAM + S_MAXLEV + l];
@@ -3338,6 +3373,7 @@ int iteration_graph_launch(topo_handle* h, const topo_iter_opts* o) {
     bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
       h->in_capture = h->iter_capture = true;
+      h->iter_waited = false;
       h->d_outer_body = h->d_inner_body = h->d_oc_body = h->d_if_body = 0;
       topo_solve_stats ss{};
       h->want_energy = true;

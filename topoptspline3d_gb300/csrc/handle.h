@@ -57,6 +57,12 @@ struct topo_handle {
   int fine_df = 1;                  // FP64 fine operator in double-float arithmetic (topo_set_fine_arithmetic)
   int tz32 = 16, tz64 = 16;         // z-march depth of the fine kernels, FP32 / FP64 (topo_autotune)
   bool fine_tc = false;             // FP32 fine element products on the tensor cores (topo_set_fine_tensor_cores)
+  // the coarsest inverse is recomputed at every coarse_every-th operator
+  // update (topo_set_coarse_refresh); coarse_age counts the updates since,
+  // coarse_valid says whether the held inverse belongs to this hierarchy
+  int coarse_every = 1;
+  int coarse_age = 0;
+  bool coarse_valid = false;
   int rows32 = 8;                   // element rows of the FP32 modal kernel's CTA tile: 4, 8, 16 (topo_set_fine_tile_rows)
   // FP32 V-cycle replayed as one CUDA graph (topo_set_graphs); re-captured when its key changes
   bool graphs = true;
@@ -83,6 +89,7 @@ struct topo_handle {
   // results in device slots and emit their loops as conditional nodes.
   // Kernels of its fixed part and of one pass of each conditional body.
   bool iter_capture = false;
+  bool iter_waited = false;           // the capture holds its wait for the coarsest inversion
   // helper streams that capture the bodies of nested conditional nodes
   cudaStream_t cstream[topo::TOPO_COND_DEPTH] = {};
   int cdepth = 0;

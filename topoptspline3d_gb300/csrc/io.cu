@@ -299,6 +299,7 @@ int topo_checkpoint_load(topo_handle* h, const char* path, void* user, size_t us
   h->tz64 = tiles[1];
   h->rhop_stale = true;
   h->ops_ready = false;
+  h->coarse_valid = false;
   return TOPO_OK;
 }
 

@@ -66,6 +66,22 @@ def test_iteration_graph_matches_host(case, inner_max):
     assert all(x[3] <= 1e-6 for x in s1)
 
 
+def test_graph_modes_agree():
+    """topo_set_graphs 1 (whole-iteration graph), 3 (outer solve graph, no
+    iteration graph), 2 (outer loop on the host) and 0 (no graphs): the same
+    design iterations bit for bit, each mode holding the graphs it names."""
+    res = {}
+    want = {1: {"iteration"}, 3: {"solve", "nested_inner", "oc"}, 2: {"inner", "oc"}, 0: set()}
+    for mode in (1, 3, 2, 0):
+        wl, p = _make(mode)
+        res[mode] = _run(p, _opts(wl, 4), 4)
+        held = {k for k, v in p.graph_state().items() if v}
+        assert want[mode] <= held, (mode, held, p.last_error())
+    for mode in (3, 2, 0):
+        assert res[mode][0] == res[1][0], mode
+        assert np.array_equal(res[mode][1], res[1][1]), mode
+
+
 def test_iteration_graph_resume(tmp_path):
     """Checkpoint after two graphed iterations, three more, then a fresh
     handle resumed from the checkpoint runs the same three bit for bit (its

@@ -462,7 +462,8 @@ int topo_design_batch(topo_handle** handles, int n, const topo_iter_opts* opts, 
  * with lower ends 0.02, 0.04, 0.06 and inner tolerances 0.03, 0.05, stage 5 two
  * and four more inner iterations with inner tolerances 0.01, 0.02 and the next
  * degree, and the fastest that converges is written into *best (other fields from *base, which must be TOPO_SOLVE_MIXED
- * with the Chebyshev smoother).  U is restored. */
+ * with the Chebyshev smoother).  With graphs on, each candidate is solved twice and timed on the second
+ * solve (the first captures its graphs, which design iterations replay).  U is restored. */
 typedef struct topo_tune_report {
   int tz32, tz64;           /* chosen z-march depths */
   double cheb_ms[4];        /* FP32 Chebyshev step at depths 4, 8, 16, 32 */

@@ -40,7 +40,8 @@ using namespace topo;
 // CTAs per SM of the coarsest inversion when it runs on the side stream next
 // to the solve's set-up kernels: one up to TOPO_GJ_SIDE_LARGE_N unknowns
 // (256x128x128: n = 675, where the set-up kernels need the SMs as much as the
-// inversion), two above, where the inversion outlasts the set-up by far
+// inversion: two CTAs per SM there ran the design iteration at 26.0-26.3
+// against 25.7 ms), two above, where the inversion outlasts the set-up by far
 // (n = 1617: about 6 against 1 ms)
 #ifndef TOPO_GJ_SIDE_PER_SM
 #define TOPO_GJ_SIDE_PER_SM 1

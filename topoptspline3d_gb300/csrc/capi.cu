@@ -1702,7 +1702,11 @@ int topo_update_operators(topo_handle* h) {
   const bool defer = h->defer_coarse && nl > 1;
   if (defer) {
     if (!h->side) {
-      CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+      // the highest priority: the coarsest inversion is on the iteration's
+      // critical path, the main stream's set-up kernels fill the gaps
+      int least = 0, greatest = 0;
+      CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      CK(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, greatest));
       CK(cudaEventCreateWithFlags(&h->ev_ops, cudaEventDisableTiming));
       CK(cudaEventCreateWithFlags(&h->ev_galerkin, cudaEventDisableTiming));
       CK(cudaEventCreateWithFlags(&h->ev_coarse, cudaEventDisableTiming));

@@ -82,6 +82,13 @@ def test_graph_modes_agree():
         assert np.array_equal(res[mode][1], res[1][1]), mode
 
 
+def test_graph_mode_argument_checked():
+    _, p = _make(1)
+    for bad in (-1, 4):
+        with pytest.raises(capi.TopoError):
+            p.set_graphs(bad)
+
+
 def test_iteration_graph_resume(tmp_path):
     """Checkpoint after two graphed iterations, three more, then a fresh
     handle resumed from the checkpoint runs the same three bit for bit (its

@@ -628,23 +628,6 @@ int ensure_cond_streams(topo_handle* h) {
   return TOPO_OK;
 }
 
-// The main stream waits for the coarse operators a deferred update builds on
-// the side stream (in a captured design iteration: one wait on the event's
-// record at launch time).
-static int galerkin_join(topo_handle* h) {
-  if (h->iter_capture) {
-    if (h->iter_gwaited || h->iter_waited) return TOPO_OK;
-    h->iter_gwaited = true;
-    h->galerkin_pending = false;
-    CK(cudaStreamWaitEvent(h->stream, h->ev_galerkin, cudaEventWaitExternal));
-    return TOPO_OK;
-  }
-  if (!h->galerkin_pending) return TOPO_OK;
-  h->galerkin_pending = false;
-  CK(cudaStreamWaitEvent(h->stream, h->ev_galerkin, 0));
-  return TOPO_OK;
-}
-
 // Conditions of the levels' restart nodes in a captured power iteration.
 struct LevelConds {
   cudaGraphConditionalHandle c[S_MAXLEV];
@@ -723,6 +706,22 @@ int estimate_bounds(topo_handle* h) {
     double lam;
   };
   std::vector<Run> runs;
+  for (int l = 0; l < nl; ++l) {
+    DevLevel& L = h->lv[l];
+    if (P<T>::lmax(L) != 0.0) continue;
+    diag_inv_level<T>(h, l);
+    Run r{l, P<T>::eig(L) != nullptr, P<T>::R(L), P<T>::cd(L), P<T>::U2(L), 0.0};
+    const int64_t n3 = 3 * L.d.nv;
+    if (r.warm) {
+      CK(cudaMemcpyAsync(r.x, P<T>::eig(L), sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
+    } else {
+      RET(dalloc(h, &P<T>::eig(L), n3));
+      k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, r.x);
+      count_launch();
+    }
+    runs.push_back(r);
+  }
+  if (runs.empty()) return TOPO_OK;
   auto power_steps = [&](Run& r, int k) {
     DevLevel& L = h->lv[r.l];
     const int64_t n3 = 3 * L.d.nv;
@@ -739,32 +738,6 @@ int estimate_bounds(topo_handle* h) {
       count_launch(4);
     }
   };
-  bool fine_stepped = false;  // the fine level's first steps launched before the coarse levels' set-up
-  for (int l = 0; l < nl; ++l) {
-    DevLevel& L = h->lv[l];
-    if (P<T>::lmax(L) != 0.0) continue;
-    if (l >= 1) {
-      // the coarse levels' stencils may still be built on the side stream (a
-      // deferred operator update): the fine level's steps go first, beside them
-      if (!runs.empty() && runs[0].l == 0 && !fine_stepped) {
-        power_steps(runs[0], runs[0].warm ? 4 : 12);
-        fine_stepped = true;
-      }
-      RET(galerkin_join(h));
-    }
-    diag_inv_level<T>(h, l);
-    Run r{l, P<T>::eig(L) != nullptr, P<T>::R(L), P<T>::cd(L), P<T>::U2(L), 0.0};
-    const int64_t n3 = 3 * L.d.nv;
-    if (r.warm) {
-      CK(cudaMemcpyAsync(r.x, P<T>::eig(L), sizeof(T) * n3, cudaMemcpyDeviceToDevice, h->stream));
-    } else {
-      RET(dalloc(h, &P<T>::eig(L), n3));
-      k_power_start<T><<<nb256(n3), 256, 0, h->stream>>>(L.d.nv, L.vmask, r.x);
-      count_launch();
-    }
-    runs.push_back(r);
-  }
-  if (runs.empty()) return TOPO_OK;
   auto read_all = [&]() -> int {
     RET(read_scalars(h, S_PW, 2 * nl));
     for (Run& r : runs) {
@@ -778,8 +751,7 @@ int estimate_bounds(topo_handle* h) {
     mask |= 1u << r.l;
     warm |= r.warm ? 1u << r.l : 0u;
   }
-  for (Run& r : runs)
-    if (!(fine_stepped && r.l == 0)) power_steps(r, r.warm ? 4 : 12);
+  for (Run& r : runs) power_steps(r, r.warm ? 4 : 12);
   if (h->iter_capture) {
     // inside a captured design iteration: the restart test on the device and
     // one conditional node per level for its 8 more steps (an even count, so
@@ -1361,7 +1333,6 @@ void topo_destroy(topo_handle* h) {
   if (h->side) cudaStreamDestroy(h->side);
   if (h->ev_ops) cudaEventDestroy(h->ev_ops);
   if (h->ev_coarse) cudaEventDestroy(h->ev_coarse);
-  if (h->ev_galerkin) cudaEventDestroy(h->ev_galerkin);
   if (h->hstat) cudaFreeHost(h->hstat);
   if (h->vgraph) cudaGraphExecDestroy(h->vgraph);
   if (h->igraph) cudaGraphExecDestroy(h->igraph);
@@ -1692,51 +1663,23 @@ int topo_update_operators(topo_handle* h) {
   RET(update_penalised_if_stale(h));
   const int nl = (int)h->lv.size();
   const bool b64 = (h->op_precision & 1) != 0, b32 = (h->op_precision & 2) != 0;
-  // In a design iteration (defer_coarse) the coarse operators and the
-  // coarsest inversion run on the side stream: the Galerkin products and
-  // stencils (then ev_galerkin), the dense coarsest matrix and its inversion
-  // (then ev_coarse), while the main stream goes on with the fine level's
-  // spectral power steps and the first residual; it waits for ev_galerkin
-  // before the coarse levels' power steps (galerkin_join) and for ev_coarse
-  // before the first V-cycle (coarse_join).
-  const bool defer = h->defer_coarse && nl > 1;
-  if (defer) {
-    if (!h->side) {
-      // the highest priority: the coarsest inversion is on the iteration's
-      // critical path, the main stream's set-up kernels fill the gaps
-      int least = 0, greatest = 0;
-      CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-      CK(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, greatest));
-      CK(cudaEventCreateWithFlags(&h->ev_ops, cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&h->ev_galerkin, cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&h->ev_coarse, cudaEventDisableTiming));
-      CK(cudaHostAlloc((void**)&h->hstat, 2 * sizeof(int), cudaHostAllocDefault));
-    }
-    CK(cudaEventRecord(h->ev_ops, h->stream));
-    CK(cudaStreamWaitEvent(h->side, h->ev_ops, 0));
-  }
-  cudaStream_t cs = defer ? h->side : h->stream;
   for (int l = 1; l < nl; ++l) {
     DevLevel& C = h->lv[l];
     DevLevel& Fl = h->lv[l - 1];
     if (l == 1) {
-      launch_galerkin_first_impl(cs, Fl.d, C.d, h->rhop, Fl.eactive, Fl.vmask, h->dT64, h->dT32,
+      launch_galerkin_first_impl(h->stream, Fl.d, C.d, h->rhop, Fl.eactive, Fl.vmask, h->dT64, h->dT32,
                                  h->dKe, h->gal_fixed, h->n_gal_fixed, b64 ? C.kel : nullptr,
                                  b32 ? C.kel32 : nullptr);
       count_launch((b64 ? 2 : 0) + (b32 ? 2 : 0));
     } else {
-      if (b64) launch_galerkin_dyadic_t<double>(cs, Fl.d, C.d, Fl.eactive, Fl.kel, C.kel);
-      if (b32) launch_galerkin_dyadic_t<float>(cs, Fl.d, C.d, Fl.eactive, Fl.kel32, C.kel32);
+      if (b64) launch_galerkin_dyadic_t<double>(h->stream, Fl.d, C.d, Fl.eactive, Fl.kel, C.kel);
+      if (b32) launch_galerkin_dyadic_t<float>(h->stream, Fl.d, C.d, Fl.eactive, Fl.kel32, C.kel32);
       count_launch((b64 ? 1 : 0) + (b32 ? 1 : 0));
     }
-    if (b64) launch_assemble_stencil_t<double>(cs, C.d, C.eactive, C.vmask, C.kel, C.stencil);
-    if (b32) launch_assemble_stencil_t<float>(cs, C.d, C.eactive, C.vmask, C.kel32, C.stencil32);
+    if (b64) launch_assemble_stencil_t<double>(h->stream, C.d, C.eactive, C.vmask, C.kel, C.stencil);
+    if (b32) launch_assemble_stencil_t<float>(h->stream, C.d, C.eactive, C.vmask, C.kel32, C.stencil32);
     count_launch((b64 ? 1 : 0) + (b32 ? 1 : 0));
     CKL();
-  }
-  if (defer) {
-    CK(cudaEventRecord(h->ev_galerkin, h->side));
-    h->galerkin_pending = true;
   }
   // a lagged coarsest inverse (topo_set_coarse_refresh): the coarse levels
   // are current, the coarsest solve keeps the inverse of an earlier update
@@ -1747,17 +1690,25 @@ int topo_update_operators(topo_handle* h) {
     DevLevel& Lc = h->lv.back();
     const double* st = Lc.stencil;
     if (!b64) {  // FP64 copy of the FP32 coarsest stencil
-      CK(cudaMemsetAsync(h->coarse64tmp, 0, sizeof(double) * 243 * Lc.d.nv, cs));
-      launch_f2d_add(cs, Lc.stencil32, h->coarse64tmp, 243 * Lc.d.nv);
+      CK(cudaMemsetAsync(h->coarse64tmp, 0, sizeof(double) * 243 * Lc.d.nv, h->stream));
+      launch_f2d_add(h->stream, Lc.stencil32, h->coarse64tmp, 243 * Lc.d.nv);
       count_launch();
       st = h->coarse64tmp;
     }
-    launch_dense_from_stencil(cs, Lc.d, st, h->A);
+    launch_dense_from_stencil(h->stream, Lc.d, st, h->A);
     count_launch(2);
     CKL();
     // FP32-only operators: the matrix comes from FP32 stencils; the updates
     // in double-float keep twice their precision on the FP32 pipe
-    if (defer) {  // on the side stream, one CTA per SM (two for large n), joined later
+    if (h->defer_coarse) {  // on the side stream, one CTA per SM, joined later
+      if (!h->side) {
+        CK(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_ops, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_coarse, cudaEventDisableTiming));
+        CK(cudaHostAlloc((void**)&h->hstat, 2 * sizeof(int), cudaHostAllocDefault));
+      }
+      CK(cudaEventRecord(h->ev_ops, h->stream));
+      CK(cudaStreamWaitEvent(h->side, h->ev_ops, 0));
       const int e = coarsest_invert(h->side, h->ndense, h->A, h->gjwork, h->status, !b64,
                                     h->ndense > TOPO_GJ_SIDE_LARGE_N ? 2 : TOPO_GJ_SIDE_PER_SM);
       count_launch();
@@ -1766,28 +1717,29 @@ int topo_update_operators(topo_handle* h) {
       CK(cudaMemcpyAsync(h->hstat, h->status, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->side));
       launch_to_float(h->side, h->A, h->A32, (int64_t)h->ndense * h->ndense);
       count_launch();
-      h->coarse_unchecked = true;
-    } else {
-      int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status, !b64);
-      count_launch();
-      if (e != (int)cudaSuccess)
-        return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));
-      int hstat[2] = {0, 0};
-      CK(cudaMemcpyAsync(hstat, h->status, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-      CK(cudaStreamSynchronize(h->stream));
-      if (hstat[1] != 0) {
-        h->coarse_valid = false;
-        return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", hstat[1] - 1);
-      }
-      h->coarse_dropped = hstat[0];
-      launch_to_float(h->stream, h->A, h->A32, (int64_t)h->ndense * h->ndense);
-      count_launch();
-      CKL();
+      CK(cudaEventRecord(h->ev_coarse, h->side));
+      h->coarse_pending = h->coarse_unchecked = true;
+      for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
+      h->ops64 = b64;
+      h->ops32 = b32;
+      h->ops_ready = true;
+      return TOPO_OK;
     }
-  }
-  if (defer) {  // (also when the inverse is kept: the coarse operators are on the side stream)
-    CK(cudaEventRecord(h->ev_coarse, h->side));
-    h->coarse_pending = true;
+    int e = coarsest_invert(h->stream, h->ndense, h->A, h->gjwork, h->status, !b64);
+    count_launch();
+    if (e != (int)cudaSuccess)
+      return fail(h, TOPO_E_CUDA, "coarsest inversion launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    int hstat[2] = {0, 0};
+    CK(cudaMemcpyAsync(hstat, h->status, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (hstat[1] != 0) {
+      h->coarse_valid = false;
+      return fail(h, TOPO_E_SINGULAR, "coarsest matrix indefinite at pivot %d", hstat[1] - 1);
+    }
+    h->coarse_dropped = hstat[0];
+    launch_to_float(h->stream, h->A, h->A32, (int64_t)h->ndense * h->ndense);
+    count_launch();
+    CKL();
   }
   for (auto& l : h->lv) { l.lmax = 0; l.lmax32 = 0; }
   h->ops64 = b64;
@@ -1918,12 +1870,11 @@ static int coarse_join(topo_handle* h) {
   if (h->iter_capture) {
     if (h->iter_waited) return TOPO_OK;
     h->iter_waited = true;
-    h->coarse_pending = h->galerkin_pending = false;
+    h->coarse_pending = false;
     CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, cudaEventWaitExternal));
     return TOPO_OK;
   }
   if (!h->coarse_pending) return TOPO_OK;
-  h->galerkin_pending = false;  // (ev_coarse follows ev_galerkin on the side stream)
   CK(cudaStreamWaitEvent(h->stream, h->ev_coarse, 0));
   h->coarse_pending = false;
   return TOPO_OK;
@@ -3423,7 +3374,7 @@ int iteration_graph_launch(topo_handle* h, const topo_iter_opts* o) {
     bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
       h->in_capture = h->iter_capture = true;
-      h->iter_waited = h->iter_gwaited = false;
+      h->iter_waited = false;
       h->d_outer_body = h->d_inner_body = h->d_oc_body = h->d_if_body = 0;
       topo_solve_stats ss{};
       h->want_energy = true;

@@ -90,7 +90,6 @@ struct topo_handle {
   // Kernels of its fixed part and of one pass of each conditional body.
   bool iter_capture = false;
   bool iter_waited = false;           // the capture holds its wait for the coarsest inversion
-  bool iter_gwaited = false;          // ... and for the coarse operators
   // helper streams that capture the bodies of nested conditional nodes
   cudaStream_t cstream[topo::TOPO_COND_DEPTH] = {};
   int cdepth = 0;
@@ -112,8 +111,7 @@ struct topo_handle {
   // before its first V-cycle (coarse_join) and the status is read at the end
   // of the solve (coarse_finish)
   cudaStream_t side = nullptr;
-  cudaEvent_t ev_ops = nullptr, ev_coarse = nullptr, ev_galerkin = nullptr;
-  bool galerkin_pending = false;  // the main stream has not waited for the side stream's coarse operators
+  cudaEvent_t ev_ops = nullptr, ev_coarse = nullptr;
   int* hstat = nullptr;           // pinned copy of the inversion status
   bool defer_coarse = false;      // topo_design_iteration's operator update
   bool coarse_pending = false;    // the main stream has not waited for it yet
